@@ -1,0 +1,257 @@
+"""ctypes mirror of include/climaland_cuda.h.
+
+Constants and structures here follow the C header one-to-one; the header is
+the source of truth for the ABI.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+# status codes
+CLM_OK = 0
+CLM_ERR_ARG = 1
+CLM_ERR_CUDA = 2
+CLM_ERR_TIMEOUT = 3
+CLM_ERR_NAN = 4
+CLM_ERR_STATE = 5
+CLM_ERR_UNSUPPORTED = 6
+
+STATUS_NAMES = {
+    0: "CLM_OK",
+    1: "CLM_ERR_ARG",
+    2: "CLM_ERR_CUDA",
+    3: "CLM_ERR_TIMEOUT",
+    4: "CLM_ERR_NAN",
+    5: "CLM_ERR_STATE",
+    6: "CLM_ERR_UNSUPPORTED",
+}
+
+# per-column flags
+CLM_COL_NONFINITE = 0x1
+CLM_COL_DIVERGED = 0x2
+CLM_COL_NOT_CONVERGED = 0x4
+CLM_COL_GUESS_FALLBACK = 0x8
+CLM_COL_PSI_POSITIVE = 0x10
+
+# enums
+CLM_MODEL_RICHARDS = 0
+CLM_MODEL_ENERGY_HYDROLOGY = 1
+CLM_PREC_FP64 = 0
+CLM_PREC_MIXED = 1
+CLM_NEWTON_FIXED = 0
+CLM_NEWTON_TOL = 1
+CLM_BC_FLUX = 0
+CLM_BC_FREE_DRAINAGE = 1
+CLM_BC_STATE = 2
+CLM_BC_FLUX_ADVECTIVE = 3
+
+CLM_P_NU = 0
+CLM_P_K_SAT = 1
+CLM_P_S_S = 2
+CLM_P_THETA_R = 3
+CLM_P_VG_ALPHA = 4
+CLM_P_VG_N = 5
+CLM_NPARAM_RICHARDS = 6
+CLM_P_KAPPA_DRY = 6
+CLM_P_KAPPA_SAT_FROZEN = 7
+CLM_P_KAPPA_SAT_UNFROZEN = 8
+CLM_P_RHOC_DS = 9
+CLM_P_NU_SS_OM = 10
+CLM_P_NU_SS_QUARTZ = 11
+CLM_P_NU_SS_GRAVEL = 12
+CLM_NPARAM_EH = 13
+
+CLM_F_BASE = 0
+CLM_F_AMP = 1
+CLM_F_OMEGA = 2
+CLM_F_PHASE = 3
+CLM_F_PULSE_AMP = 4
+CLM_F_PULSE_PERIOD = 5
+CLM_F_PULSE_DUTY = 6
+CLM_F_T_ADV = 7
+CLM_F_NFIELDS = 8
+
+CLM_BC_TOP_WATER = 0
+CLM_BC_TOP_HEAT = 1
+CLM_BC_BOTTOM_WATER = 2
+CLM_BC_BOTTOM_HEAT = 3
+
+
+class ClmEarthParams(ctypes.Structure):
+    _fields_ = [
+        ("rho_l", ctypes.c_double),
+        ("rho_i", ctypes.c_double),
+        ("cp_l", ctypes.c_double),
+        ("cp_i", ctypes.c_double),
+        ("T_0", ctypes.c_double),
+        ("T_freeze", ctypes.c_double),
+        ("LH_f0", ctypes.c_double),
+        ("grav", ctypes.c_double),
+    ]
+
+
+class ClmConfig(ctypes.Structure):
+    _fields_ = [
+        ("model", ctypes.c_int32),
+        ("ncol", ctypes.c_int32),
+        ("nlayers", ctypes.c_int32),
+        ("precision", ctypes.c_int32),
+        ("newton_mode", ctypes.c_int32),
+        ("max_iters", ctypes.c_int32),
+        ("newton_tol", ctypes.c_double),
+        ("energy_norm_scale", ctypes.c_double),
+        ("learned_guess", ctypes.c_int32),
+        ("bc_top_water", ctypes.c_int32),
+        ("bc_top_heat", ctypes.c_int32),
+        ("bc_bottom_water", ctypes.c_int32),
+        ("bc_bottom_heat", ctypes.c_int32),
+        ("kersten_alpha", ctypes.c_double),
+        ("kersten_beta", ctypes.c_double),
+        ("ice_impedance_omega", ctypes.c_double),
+        ("visc_gamma", ctypes.c_double),
+        ("visc_gamma_T_ref", ctypes.c_double),
+        ("earth", ClmEarthParams),
+        ("phase_change", ctypes.c_int32),
+        ("pad0", ctypes.c_int32),
+        ("forcing_seed", ctypes.c_uint64),
+        ("cols_per_cta", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 7),
+    ]
+
+
+# ClimaParams defaults for the LandParameters fields used on this path
+# (density_liquid_water, density_ice_water, isobaric_specific_heat_liquid,
+# isobaric_specific_heat_ice, thermodynamics_temperature_reference,
+# temperature_water_freeze, latent_heat_sublimation_at_reference -
+# latent_heat_vaporization_at_reference, gravitational_acceleration).
+DEFAULT_EARTH = dict(
+    rho_l=1000.0,
+    rho_i=916.7,
+    cp_l=4181.0,
+    cp_i=2100.0,
+    T_0=273.16,
+    T_freeze=273.15,
+    LH_f0=2834400.0 - 2500800.0,
+    grav=9.81,
+)
+
+
+def default_config() -> ClmConfig:
+    """Python twin of clm_config_default (usable without the CUDA library)."""
+    c = ClmConfig()
+    c.model = CLM_MODEL_ENERGY_HYDROLOGY
+    c.ncol = 0
+    c.nlayers = 0
+    c.precision = CLM_PREC_FP64
+    c.newton_mode = CLM_NEWTON_FIXED
+    c.max_iters = 3
+    c.newton_tol = 1e-8
+    c.energy_norm_scale = 1.0
+    c.learned_guess = 0
+    c.bc_top_water = CLM_BC_FLUX
+    c.bc_top_heat = CLM_BC_FLUX
+    c.bc_bottom_water = CLM_BC_FREE_DRAINAGE
+    c.bc_bottom_heat = CLM_BC_FREE_DRAINAGE
+    c.kersten_alpha = 0.24
+    c.kersten_beta = 18.3
+    c.ice_impedance_omega = 7.0
+    c.visc_gamma = 2.64e-2
+    c.visc_gamma_T_ref = 288.0
+    for k, v in DEFAULT_EARTH.items():
+        setattr(c.earth, k, v)
+    c.phase_change = 1
+    c.forcing_seed = 0
+    c.cols_per_cta = 0
+    return c
+
+
+def config_to_dict(c: ClmConfig) -> dict:
+    out = {}
+    for name, _ in ClmConfig._fields_:
+        v = getattr(c, name)
+        if name == "earth":
+            v = {k: getattr(v, k) for k, _ in ClmEarthParams._fields_}
+        elif name == "reserved":
+            continue
+        out[name] = v
+    return out
+
+
+PACKAGE_DIR = Path(__file__).resolve().parent
+LIB_NAME = "libclimaland_cuda.so"
+
+
+def library_path() -> Path:
+    env = os.environ.get("CLIMALAND_CUDA_LIB")
+    if env:
+        return Path(env)
+    return PACKAGE_DIR / "_build" / LIB_NAME
+
+
+_DP = ctypes.POINTER(ctypes.c_double)
+_IP = ctypes.POINTER(ctypes.c_int32)
+_UP = ctypes.POINTER(ctypes.c_uint32)
+_H = ctypes.c_void_p
+
+# (name, restype, argtypes) for every symbol declared in the header.
+SIGNATURES = [
+    ("clm_config_default", None, [ctypes.POINTER(ClmConfig)]),
+    ("clm_create", ctypes.c_int, [ctypes.POINTER(ClmConfig), ctypes.POINTER(_H)]),
+    ("clm_destroy", None, [_H]),
+    ("clm_last_error", ctypes.c_char_p, [_H]),
+    ("clm_set_geometry", ctypes.c_int, [_H, _DP, _DP, _IP]),
+    ("clm_set_params", ctypes.c_int, [_H, _DP, ctypes.c_int32]),
+    ("clm_set_bc", ctypes.c_int, [_H, ctypes.c_int32, _DP, ctypes.c_int32]),
+    ("clm_set_state", ctypes.c_int, [_H, _DP, _DP, _DP, _DP, _DP]),
+    ("clm_get_state", ctypes.c_int, [_H, _DP, _DP, _DP, _DP, _DP]),
+    ("clm_set_state_device", ctypes.c_int, [_H, ctypes.c_void_p, ctypes.c_void_p,
+                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    ("clm_get_state_device", ctypes.c_int, [_H, ctypes.c_void_p, ctypes.c_void_p,
+                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    ("clm_step", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_double, ctypes.c_int32]),
+    ("clm_step_async", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_double, ctypes.c_int32]),
+    ("clm_sync", ctypes.c_int, [_H]),
+    ("clm_get_budgets", ctypes.c_int, [_H, _DP, _DP]),
+    ("clm_get_status", ctypes.c_int, [_H, _UP, _IP]),
+    ("clm_update_aux", ctypes.c_int, [_H, ctypes.c_double, _DP, _DP, _DP, _DP, _DP, _DP, _DP]),
+    ("clm_exp_tendency", ctypes.c_int, [_H, ctypes.c_double, _DP, _DP, _DP, _DP, _DP]),
+    ("clm_imp_tendency", ctypes.c_int, [_H, ctypes.c_double, _DP, _DP, _DP, _DP, _DP]),
+    ("clm_jacobian", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_double, _DP, _DP, _DP]),
+    ("clm_solve", ctypes.c_int, [_H, _DP, _DP, _DP, _DP, _DP, _DP, _DP]),
+    ("clm_load_mlp", ctypes.c_int, [_H, ctypes.c_void_p, ctypes.c_int64]),
+    ("clm_forcing_hash01", ctypes.c_double, [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int64]),
+    ("clm_version", ctypes.c_char_p, []),
+]
+
+
+def declared_symbols() -> list[str]:
+    return [s[0] for s in SIGNATURES]
+
+
+def bind(lib: ctypes.CDLL) -> ctypes.CDLL:
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+def dptr(a):
+    """Pointer to a contiguous float64 numpy array, or NULL for None."""
+    if a is None:
+        return None
+    return a.ctypes.data_as(_DP)
+
+
+def iptr(a):
+    if a is None:
+        return None
+    return a.ctypes.data_as(_IP)
+
+
+def uptr(a):
+    if a is None:
+        return None
+    return a.ctypes.data_as(_UP)

@@ -1,0 +1,364 @@
+"""Seeded synthetic soil-column workloads.
+
+The reference publishes no column-step dataset; these generators produce
+inputs with the shapes, sizes and value ranges of the five benchmark
+configurations (plain Richards 1024x20; plain EnergyHydrology 65,536x15;
+uneven CSR columns 262,144 x U{4..30}; learned-guess evaluation
+262,144x20; full scale 1,048,576x20) from numpy PCG64 generators with fixed
+seeds. All arrays use the C ABI layout: cells column-contiguous with level 0
+at the bottom, per-column parameter and forcing rows as SoA blocks.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi as A
+
+# Reference-test constants for the derived frozen conductivity rule:
+# kappa_sat_frozen / kappa_sat_unfrozen = (kappa_ice / kappa_liq) ** nu, which
+# is what kappa_sat_frozen / kappa_sat_unfrozen
+# (soil_heat_parameterizations.jl:359-373) give for a common solid
+# conductivity; kappa_ice = 2.21, kappa_liq = 0.57
+# (test/standalone/Soil/soil_parameterizations.jl:55-56).
+KAPPA_ICE = 2.21
+KAPPA_LIQ = 0.57
+
+DAY = 86400.0
+
+
+@dataclass
+class Workload:
+    """Everything a soil-column run needs, in C ABI layout."""
+
+    name: str
+    cfg: A.ClmConfig
+    ncol: int
+    offsets: np.ndarray  # int32, ncol + 1
+    z_lo: np.ndarray
+    z_hi: np.ndarray
+    params: np.ndarray  # (nparams, ncol) float64
+    forcing: dict  # slot -> (CLM_F_NFIELDS, ncol) float64
+    vartheta_l: np.ndarray
+    theta_i: np.ndarray | None
+    rho_e_int: np.ndarray | None
+    intF_w: np.ndarray
+    intF_e: np.ndarray | None
+    t0: float
+    dt: float
+    nsteps: int
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def ncells(self) -> int:
+        return int(self.offsets[-1])
+
+    @property
+    def nlayers(self) -> np.ndarray:
+        return np.diff(self.offsets)
+
+    def copy_state(self):
+        def c(a):
+            return None if a is None else a.copy()
+
+        return (c(self.vartheta_l), c(self.theta_i), c(self.rho_e_int),
+                c(self.intF_w), c(self.intF_e))
+
+    def subset(self, ncol: int) -> "Workload":
+        """First `ncol` columns (a bounded sample of the same workload)."""
+        ncol = min(ncol, self.ncol)
+        nc = int(self.offsets[ncol])
+
+        def cells(a):
+            return None if a is None else a[:nc].copy()
+
+        def cols(a):
+            return None if a is None else a[:ncol].copy()
+
+        cfg = A.ClmConfig.from_buffer_copy(self.cfg)
+        cfg.ncol = ncol
+        return Workload(
+            name=f"{self.name}[:{ncol}]", cfg=cfg, ncol=ncol,
+            offsets=self.offsets[: ncol + 1].copy(), z_lo=cols(self.z_lo),
+            z_hi=cols(self.z_hi), params=np.ascontiguousarray(self.params[:, :ncol]),
+            forcing={k: np.ascontiguousarray(v[:, :ncol]) for k, v in self.forcing.items()},
+            vartheta_l=cells(self.vartheta_l), theta_i=cells(self.theta_i),
+            rho_e_int=cells(self.rho_e_int), intF_w=cols(self.intF_w),
+            intF_e=cols(self.intF_e), t0=self.t0, dt=self.dt,
+            nsteps=self.nsteps, meta=dict(self.meta))
+
+
+def _forcing(ncol: int) -> np.ndarray:
+    return np.zeros((A.CLM_F_NFIELDS, ncol), dtype=np.float64)
+
+
+def _hydraulics(rng: np.random.Generator, ncol: int) -> dict:
+    """Per-column van Genuchten hydraulics shared by every configuration."""
+    return dict(
+        alpha=rng.uniform(0.5, 5.0, ncol),
+        n=rng.uniform(1.2, 2.5, ncol),
+        nu=rng.uniform(0.35, 0.55, ncol),
+        theta_r=rng.uniform(0.02, 0.1, ncol),
+        K_sat=10.0 ** rng.uniform(-7.0, -4.0, ncol),
+        S_s=np.full(ncol, 1e-3),  # Soil.jl:351 default
+    )
+
+
+def _water_profile(rng, hyd, offsets, z_lo, z_hi):
+    """vartheta_l per cell: a top value uniform in [theta_r + 0.05,
+    nu - 0.05] with a linear depth gradient, clipped to the same range."""
+    ncol = len(z_lo)
+    lo = hyd["theta_r"] + 0.05
+    hi = hyd["nu"] - 0.05
+    top = rng.uniform(lo, hi)
+    grad = rng.uniform(-0.05, 0.05, ncol)  # per metre of depth
+    n = np.diff(offsets)
+    col = np.repeat(np.arange(ncol), n)
+    k = np.arange(offsets[-1]) - np.repeat(offsets[:-1], n)
+    dz = (z_hi - z_lo) / n
+    zc = z_lo[col] + (k + 0.5) * dz[col]
+    depth = z_hi[col] - zc
+    v = top[col] + grad[col] * depth
+    return np.clip(v, lo[col], hi[col]), col, zc
+
+
+def _frozen_equilibrium(theta_tot, T, hyd_c, earth):
+    """theta_l = min(theta_star(T), theta_tot), theta_i from the remainder:
+    the phase-change equilibrium of phase_change_source
+    (soil_heat_parameterizations.jl:89-122) for a given liquid-equivalent
+    water content theta_tot."""
+    alpha, n, nu, theta_r = hyd_c["alpha"], hyd_c["n"], hyd_c["nu"], hyd_c["theta_r"]
+    m = 1.0 - 1.0 / n
+    rho_l, rho_i = earth["rho_l"], earth["rho_i"]
+    LH_f0, grav, T_freeze = earth["LH_f0"], earth["grav"], earth["T_freeze"]
+    sq = np.sqrt(np.finfo(np.float64).eps)
+    tt = np.minimum(theta_tot, nu)
+    S = (np.maximum(tt, theta_r + sq) - theta_r) / (np.maximum(nu, theta_r + sq) - theta_r)
+    psi_w0 = -(((S ** (-1.0 / m) - 1.0) * alpha ** (-n)) ** (1.0 / n))
+    Tf = np.maximum(T_freeze * np.exp(grav * psi_w0 / LH_f0), 1.0)
+    H = (Tf - T > np.finfo(np.float64).eps).astype(np.float64)
+    psi_T = LH_f0 / grav * np.log(T / Tf) * H
+    S_star = (1.0 + (alpha * np.abs(psi_w0 + psi_T)) ** n) ** (-m)
+    theta_star = S_star * (nu - theta_r) + theta_r
+    theta_l = np.minimum(theta_star, theta_tot)
+    theta_i = np.maximum(theta_tot - theta_l, 0.0) * rho_l / rho_i
+    return theta_l, theta_i
+
+
+def _rho_e(theta_l, theta_i, T, rhoc_ds, earth):
+    rhoc = rhoc_ds + theta_l * earth["cp_l"] * earth["rho_l"] + theta_i * earth["cp_i"] * earth["rho_i"]
+    return rhoc * (T - earth["T_0"]) - theta_i * earth["rho_i"] * earth["LH_f0"]
+
+
+def _eh_params(rng, ncol, hyd):
+    p = np.zeros((A.CLM_NPARAM_EH, ncol))
+    p[A.CLM_P_NU] = hyd["nu"]
+    p[A.CLM_P_K_SAT] = hyd["K_sat"]
+    p[A.CLM_P_S_S] = hyd["S_s"]
+    p[A.CLM_P_THETA_R] = hyd["theta_r"]
+    p[A.CLM_P_VG_ALPHA] = hyd["alpha"]
+    p[A.CLM_P_VG_N] = hyd["n"]
+    p[A.CLM_P_RHOC_DS] = rng.uniform(1.5e6, 2.5e6, ncol)
+    p[A.CLM_P_KAPPA_DRY] = rng.uniform(0.2, 0.4, ncol)
+    ku = rng.uniform(1.5, 2.5, ncol)
+    p[A.CLM_P_KAPPA_SAT_UNFROZEN] = ku
+    p[A.CLM_P_KAPPA_SAT_FROZEN] = ku * (KAPPA_ICE / KAPPA_LIQ) ** hyd["nu"]
+    p[A.CLM_P_NU_SS_OM] = 0.0
+    p[A.CLM_P_NU_SS_QUARTZ] = rng.uniform(0.1, 0.9, ncol)
+    p[A.CLM_P_NU_SS_GRAVEL] = 0.0
+    return p
+
+
+def _earth_dict(cfg):
+    return {k: getattr(cfg.earth, k) for k, _ in A.ClmEarthParams._fields_}
+
+
+def richards_c0(ncol: int = 1024, nlayers: int = 20, seed: int = 0) -> Workload:
+    """Plain RichardsModel FP64: 1024 columns x 20 uniform layers over 2 m,
+    flux top / free-drainage bottom, dt = 900 s, 3 Newton iterations, 96 steps."""
+    rng = np.random.Generator(np.random.PCG64(1000 + seed))
+    cfg = A.default_config()
+    cfg.model = A.CLM_MODEL_RICHARDS
+    cfg.ncol = ncol
+    cfg.nlayers = nlayers
+    cfg.bc_top_water = A.CLM_BC_FLUX
+    cfg.bc_bottom_water = A.CLM_BC_FREE_DRAINAGE
+    cfg.phase_change = 0
+    hyd = _hydraulics(rng, ncol)
+    offsets = (np.arange(ncol + 1) * nlayers).astype(np.int32)
+    z_lo = np.full(ncol, -2.0)
+    z_hi = np.zeros(ncol)
+    v, _, _ = _water_profile(rng, hyd, offsets, z_lo, z_hi)
+    params = np.zeros((A.CLM_NPARAM_RICHARDS, ncol))
+    params[A.CLM_P_NU] = hyd["nu"]
+    params[A.CLM_P_K_SAT] = hyd["K_sat"]
+    params[A.CLM_P_S_S] = hyd["S_s"]
+    params[A.CLM_P_THETA_R] = hyd["theta_r"]
+    params[A.CLM_P_VG_ALPHA] = hyd["alpha"]
+    params[A.CLM_P_VG_N] = hyd["n"]
+    ftw = _forcing(ncol)
+    ftw[A.CLM_F_BASE] = rng.uniform(-5e-7, 0.0, ncol)
+    return Workload(
+        name=f"richards_{ncol}x{nlayers}", cfg=cfg, ncol=ncol, offsets=offsets,
+        z_lo=z_lo, z_hi=z_hi, params=params,
+        forcing={A.CLM_BC_TOP_WATER: ftw}, vartheta_l=v, theta_i=None,
+        rho_e_int=None, intF_w=np.zeros(ncol), intF_e=None, t0=0.0, dt=900.0,
+        nsteps=96)
+
+
+def _eh_common(rng, ncol, offsets, z_lo, z_hi, cfg, T_range=(265.0, 290.0)):
+    earth = _earth_dict(cfg)
+    hyd = _hydraulics(rng, ncol)
+    params = _eh_params(rng, ncol, hyd)
+    theta_tot, col, zc = _water_profile(rng, hyd, offsets, z_lo, z_hi)
+    T_col = rng.uniform(*T_range, ncol)
+    depth_frac = (z_hi[col] - zc) / (z_hi[col] - z_lo[col])
+    T = T_col[col] + 2.0 * depth_frac  # slightly warmer at depth
+    hyd_c = {k: hyd[k][col] for k in ("alpha", "n", "nu", "theta_r")}
+    theta_l, theta_i = _frozen_equilibrium(theta_tot, T, hyd_c, earth)
+    rho_e = _rho_e(theta_l, theta_i, T, params[A.CLM_P_RHOC_DS][col], earth)
+    return hyd, params, theta_l, theta_i, rho_e
+
+
+def energy_hydrology_c1(ncol: int = 65536, nlayers: int = 15, seed: int = 0) -> Workload:
+    """Plain EnergyHydrology FP64: 65,536 columns x 15 layers over 3 m; top heat
+    flux 150 sin(2 pi t / 86400) W/m^2 (positive upward) plus a constant water
+    flux per column; EnergyWaterFreeDrainage bottom; dt = 450 s, 192 steps."""
+    rng = np.random.Generator(np.random.PCG64(2000 + seed))
+    cfg = A.default_config()
+    cfg.model = A.CLM_MODEL_ENERGY_HYDROLOGY
+    cfg.ncol = ncol
+    cfg.nlayers = nlayers
+    offsets = (np.arange(ncol + 1) * nlayers).astype(np.int32)
+    z_lo = np.full(ncol, -3.0)
+    z_hi = np.zeros(ncol)
+    hyd, params, v, ti, e = _eh_common(rng, ncol, offsets, z_lo, z_hi, cfg)
+    ftw = _forcing(ncol)
+    ftw[A.CLM_F_BASE] = rng.uniform(-5e-7, 0.0, ncol)
+    fth = _forcing(ncol)
+    fth[A.CLM_F_AMP] = 150.0
+    fth[A.CLM_F_OMEGA] = 2.0 * np.pi / DAY
+    return Workload(
+        name=f"energy_hydrology_{ncol}x{nlayers}", cfg=cfg, ncol=ncol,
+        offsets=offsets, z_lo=z_lo, z_hi=z_hi, params=params,
+        forcing={A.CLM_BC_TOP_WATER: ftw, A.CLM_BC_TOP_HEAT: fth},
+        vartheta_l=v, theta_i=ti, rho_e_int=e, intF_w=np.zeros(ncol),
+        intF_e=np.zeros(ncol), t0=0.0, dt=450.0, nsteps=192)
+
+
+def uneven_c2(ncol: int = 262144, nmin: int = 4, nmax: int = 30, seed: int = 0) -> Workload:
+    """Uneven EnergyHydrology columns: layer count uniform in {4..30}, bedrock
+    depth uniform in [0.5, 5] m, CSR-packed; parameters and forcing as the
+    65,536x15 configuration."""
+    rng = np.random.Generator(np.random.PCG64(3000 + seed))
+    cfg = A.default_config()
+    cfg.model = A.CLM_MODEL_ENERGY_HYDROLOGY
+    cfg.ncol = ncol
+    cfg.nlayers = 0
+    n = rng.integers(nmin, nmax + 1, ncol)
+    offsets = np.zeros(ncol + 1, dtype=np.int32)
+    offsets[1:] = np.cumsum(n)
+    z_lo = -rng.uniform(0.5, 5.0, ncol)
+    z_hi = np.zeros(ncol)
+    hyd, params, v, ti, e = _eh_common(rng, ncol, offsets, z_lo, z_hi, cfg)
+    ftw = _forcing(ncol)
+    ftw[A.CLM_F_BASE] = rng.uniform(-5e-7, 0.0, ncol)
+    fth = _forcing(ncol)
+    fth[A.CLM_F_AMP] = 150.0
+    fth[A.CLM_F_OMEGA] = 2.0 * np.pi / DAY
+    return Workload(
+        name=f"uneven_{ncol}x{nmin}-{nmax}", cfg=cfg, ncol=ncol, offsets=offsets,
+        z_lo=z_lo, z_hi=z_hi, params=params,
+        forcing={A.CLM_BC_TOP_WATER: ftw, A.CLM_BC_TOP_HEAT: fth},
+        vartheta_l=v, theta_i=ti, rho_e_int=e, intF_w=np.zeros(ncol),
+        intF_e=np.zeros(ncol), t0=0.0, dt=450.0, nsteps=192)
+
+
+def full_scale_c4(ncol: int = 1048576, nlayers: int = 20, seed: int = 0) -> Workload:
+    """Full scale: 1,048,576 EnergyHydrology columns x 20 layers, depth uniform
+    in [1, 5] m, diurnal surface heat flux with amplitude U[100, 400] W/m^2,
+    air temperature U[270, 300] K carried by infiltrating water, rain pulses
+    of -1e-6 m/s on 10 % of hours (counter hash per column and hour),
+    dt = 450 s, 8 days = 1536 steps."""
+    rng = np.random.Generator(np.random.PCG64(4000 + seed))
+    cfg = A.default_config()
+    cfg.model = A.CLM_MODEL_ENERGY_HYDROLOGY
+    cfg.ncol = ncol
+    cfg.nlayers = nlayers
+    cfg.bc_top_heat = A.CLM_BC_FLUX_ADVECTIVE
+    cfg.forcing_seed = 4000 + seed
+    offsets = (np.arange(ncol + 1) * nlayers).astype(np.int32)
+    z_lo = -rng.uniform(1.0, 5.0, ncol)
+    z_hi = np.zeros(ncol)
+    hyd, params, v, ti, e = _eh_common(rng, ncol, offsets, z_lo, z_hi, cfg)
+    ftw = _forcing(ncol)
+    ftw[A.CLM_F_PULSE_AMP] = -1e-6
+    ftw[A.CLM_F_PULSE_PERIOD] = 3600.0
+    ftw[A.CLM_F_PULSE_DUTY] = 0.1
+    fth = _forcing(ncol)
+    fth[A.CLM_F_AMP] = rng.uniform(100.0, 400.0, ncol)
+    fth[A.CLM_F_OMEGA] = 2.0 * np.pi / DAY
+    fth[A.CLM_F_T_ADV] = rng.uniform(270.0, 300.0, ncol)
+    return Workload(
+        name=f"full_scale_{ncol}x{nlayers}", cfg=cfg, ncol=ncol,
+        offsets=offsets, z_lo=z_lo, z_hi=z_hi, params=params,
+        forcing={A.CLM_BC_TOP_WATER: ftw, A.CLM_BC_TOP_HEAT: fth},
+        vartheta_l=v, theta_i=ti, rho_e_int=e, intF_w=np.zeros(ncol),
+        intF_e=np.zeros(ncol), t0=0.0, dt=450.0, nsteps=1536)
+
+
+def learned_eval_c3(ncol: int = 262144, nlayers: int = 20, seed: int = 0) -> Workload:
+    """Learned-guess evaluation set: 262,144 EnergyHydrology columns x 20
+    layers with the 65,536x15 configuration's distributions."""
+    w = energy_hydrology_c1(ncol=ncol, nlayers=nlayers, seed=100 + seed)
+    w.name = f"learned_eval_{ncol}x{nlayers}"
+    return w
+
+
+CONFIGS = {
+    "c0": richards_c0,
+    "c1": energy_hydrology_c1,
+    "c2": uneven_c2,
+    "c3": learned_eval_c3,
+    "c4": full_scale_c4,
+}
+
+
+def make_workload(name, cfg, *, z_lo, z_hi, nlayers, params, forcing=None,
+                  vartheta_l, theta_i=None, rho_e_int=None, intF_w=None,
+                  intF_e=None, t0=0.0, dt=1.0, nsteps=1) -> Workload:
+    """Assemble a Workload from explicit arrays (uniform or per-column layer
+    counts). Scalars for z_lo / z_hi broadcast over columns."""
+    params = np.ascontiguousarray(params, dtype=np.float64)
+    ncol = params.shape[1]
+    nl = np.broadcast_to(np.asarray(nlayers, dtype=np.int64), (ncol,))
+    offsets = np.zeros(ncol + 1, dtype=np.int32)
+    offsets[1:] = np.cumsum(nl)
+    cfg = A.ClmConfig.from_buffer_copy(cfg)
+    cfg.ncol = ncol
+    cfg.nlayers = int(nl[0]) if np.all(nl == nl[0]) else 0
+    eh = cfg.model == A.CLM_MODEL_ENERGY_HYDROLOGY
+    nc = int(offsets[-1])
+
+    def cells(a):
+        if a is None:
+            return None
+        return np.ascontiguousarray(np.broadcast_to(np.asarray(a, dtype=np.float64), (nc,)))
+
+    return Workload(
+        name=name, cfg=cfg, ncol=ncol, offsets=offsets,
+        z_lo=np.ascontiguousarray(np.broadcast_to(np.asarray(z_lo, float), (ncol,))),
+        z_hi=np.ascontiguousarray(np.broadcast_to(np.asarray(z_hi, float), (ncol,))),
+        params=params, forcing=dict(forcing or {}), vartheta_l=cells(vartheta_l),
+        theta_i=cells(theta_i if theta_i is not None else (0.0 if eh else None)),
+        rho_e_int=cells(rho_e_int) if eh else None,
+        intF_w=np.zeros(ncol) if intF_w is None else np.asarray(intF_w, float).copy(),
+        intF_e=(np.zeros(ncol) if intF_e is None else np.asarray(intF_e, float).copy()) if eh else None,
+        t0=t0, dt=dt, nsteps=nsteps)
+
+
+def constant_forcing(ncol: int, value) -> np.ndarray:
+    f = _forcing(ncol)
+    f[A.CLM_F_BASE] = value
+    return f

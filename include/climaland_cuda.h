@@ -1,0 +1,291 @@
+/*
+ * libclimaland_cuda — C ABI of the GB300 (sm_103a) soil column step.
+ *
+ * The library replaces, for one device, the model closures that ClimaLand
+ * hands to ClimaTimeSteppers for a soil column model (RichardsModel or
+ * EnergyHydrology) and the IMEX ARS111 + Newton step that drives them.
+ * Every entry point below names the reference interface it stands in for
+ * (paths relative to the ClimaLand.jl source tree).
+ *
+ * Conventions
+ *  - All functions return an int status (CLM_OK = 0) and never abort, trap
+ *    or throw across the ABI. clm_last_error() gives a readable message.
+ *  - Host buffers are owned by the caller and copied in/out. Device buffers
+ *    are owned by the handle.
+ *  - Cell arrays use the reference's column layout: cell index =
+ *    offsets[c] + k, level k = 0 is the bottom layer (ClimaCore level 1),
+ *    levels contiguous within a column (ClimaCore VIJFH/VF "level fastest").
+ *    For uniform columns offsets[c] = c * nlayers.
+ *  - Per-column parameter blocks are structure-of-arrays: params[p*ncol + c].
+ *  - One handle per host thread; each handle owns one CUDA stream.
+ *    Calls are synchronous unless the _async form is used.
+ */
+#ifndef CLIMALAND_CUDA_H
+#define CLIMALAND_CUDA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define CLM_OK 0
+#define CLM_ERR_ARG 1         /* invalid argument (size, pointer, enum)    */
+#define CLM_ERR_CUDA 2        /* a CUDA runtime call failed                */
+#define CLM_ERR_TIMEOUT 3     /* a bounded device-side wait gave up        */
+#define CLM_ERR_NAN 4         /* non-finite state detected (per-col flags) */
+#define CLM_ERR_STATE 5       /* call order (e.g. step before set_state)   */
+#define CLM_ERR_UNSUPPORTED 6 /* option not built in this library          */
+
+/* ---- per-column status flags (clm_get_status) ------------------------ */
+#define CLM_COL_NONFINITE 0x1u     /* NaN/Inf in the column state          */
+#define CLM_COL_DIVERGED 0x2u      /* Newton increment norm grew           */
+#define CLM_COL_NOT_CONVERGED 0x4u /* tolerance mode hit max_iters         */
+#define CLM_COL_GUESS_FALLBACK 0x8u /* learned guess rejected, zero guess  */
+#define CLM_COL_PSI_POSITIVE 0x10u /* inverse_matric_potential got psi > 0 */
+
+/* ---- enums ------------------------------------------------------------ */
+enum clm_model {
+  CLM_MODEL_RICHARDS = 0,         /* src/standalone/Soil/rre.jl:67        */
+  CLM_MODEL_ENERGY_HYDROLOGY = 1  /* src/standalone/Soil/energy_hydrology.jl:226 */
+};
+
+enum clm_precision {
+  CLM_PREC_FP64 = 0,  /* plain path: everything in FP64 (drop-in)         */
+  CLM_PREC_MIXED = 1  /* FP32 Jacobian + Thomas; FP64 residual, increment
+                         accumulation, phase partition and budgets        */
+};
+
+enum clm_newton_mode {
+  CLM_NEWTON_FIXED = 0, /* max_iters iterations, no convergence check
+                           (Simulations.jl:127-135 default: 3)            */
+  CLM_NEWTON_TOL = 1    /* stop when the column increment 2-norm is below
+                           newton_tol (CTS MaximumError on the norm)       */
+};
+
+/* Boundary-condition kinds (src/standalone/Soil/boundary_conditions.jl). */
+enum clm_bc_kind {
+  CLM_BC_FLUX = 0,            /* WaterFluxBC / HeatFluxBC: F = f(t)        */
+  CLM_BC_FREE_DRAINAGE = 1,   /* FreeDrainage (water, bottom): F = -K_1;
+                                 as heat BC: EnergyWaterFreeDrainage
+                                 F_e = -K_1 rho e_liq(T_1)                 */
+  CLM_BC_STATE = 2,           /* MoistureStateBC / TemperatureStateBC      */
+  CLM_BC_FLUX_ADVECTIVE = 3   /* heat only: F_e = f(t) + F_w,top(t) *
+                                 rho e_liq(T_adv), T_adv per column        */
+};
+
+/* Per-column parameter rows for clm_set_params (SoA, row p of ncol). The
+ * first CLM_NPARAM_RICHARDS rows are RichardsParameters (rre.jl:7-21); all
+ * CLM_NPARAM_EH rows are the per-point EnergyHydrologyParameters
+ * (energy_hydrology.jl:21-78). */
+enum clm_param {
+  CLM_P_NU = 0,            /* porosity nu                                 */
+  CLM_P_K_SAT = 1,         /* saturated hydraulic conductivity (m/s)      */
+  CLM_P_S_S = 2,           /* specific storativity (1/m)                  */
+  CLM_P_THETA_R = 3,       /* residual water fraction                     */
+  CLM_P_VG_ALPHA = 4,      /* van Genuchten alpha (1/m)                   */
+  CLM_P_VG_N = 5,          /* van Genuchten n                             */
+  CLM_NPARAM_RICHARDS = 6,
+  CLM_P_KAPPA_DRY = 6,          /* W/m/K                                   */
+  CLM_P_KAPPA_SAT_FROZEN = 7,   /* W/m/K                                   */
+  CLM_P_KAPPA_SAT_UNFROZEN = 8, /* W/m/K                                   */
+  CLM_P_RHOC_DS = 9,            /* J/m^3/K                                 */
+  CLM_P_NU_SS_OM = 10,
+  CLM_P_NU_SS_QUARTZ = 11,
+  CLM_P_NU_SS_GRAVEL = 12,
+  CLM_NPARAM_EH = 13
+};
+
+/* Forcing descriptor rows for clm_set_bc (SoA, row f of ncol). A boundary
+ * value at time t for column c (original index) is
+ *   base + amp * sin(omega * t + phase)
+ *        + pulse_amp * [u(seed, c, floor(t / pulse_period)) < pulse_duty]
+ * with u() the counter hash clm_forcing_hash01 below (pulse term off when
+ * pulse_period <= 0). For CLM_BC_FLUX_ADVECTIVE row CLM_F_T_ADV is the
+ * temperature carried by the top water flux. This replaces the reference's
+ * Julia closure bc(p, t) (boundary_conditions.jl:168-180, 465-477), which
+ * cannot cross a C ABI. */
+enum clm_forcing_field {
+  CLM_F_BASE = 0,
+  CLM_F_AMP = 1,
+  CLM_F_OMEGA = 2,
+  CLM_F_PHASE = 3,
+  CLM_F_PULSE_AMP = 4,
+  CLM_F_PULSE_PERIOD = 5,
+  CLM_F_PULSE_DUTY = 6,
+  CLM_F_T_ADV = 7,
+  CLM_F_NFIELDS = 8
+};
+
+/* Which boundary value clm_set_bc addresses. */
+enum clm_bc_slot {
+  CLM_BC_TOP_WATER = 0,
+  CLM_BC_TOP_HEAT = 1,
+  CLM_BC_BOTTOM_WATER = 2,
+  CLM_BC_BOTTOM_HEAT = 3
+};
+
+/* Physical constants (ClimaLand.Parameters.LandParameters,
+ * src/shared_utilities/Parameters.jl:11-115). The Julia caller passes the
+ * values of its own earth_param_set; clm_config_default fills ClimaParams
+ * defaults. */
+typedef struct clm_earth_params {
+  double rho_l;    /* density_liquid_water (kg/m^3)                     */
+  double rho_i;    /* density_ice_water (kg/m^3)                        */
+  double cp_l;     /* isobaric_specific_heat_liquid (J/kg/K)            */
+  double cp_i;     /* isobaric_specific_heat_ice (J/kg/K)               */
+  double T_0;      /* thermodynamics_temperature_reference (K)          */
+  double T_freeze; /* temperature_water_freeze (K)                      */
+  double LH_f0;    /* LH_s0 - LH_v0 (J/kg), Parameters.jl:58            */
+  double grav;     /* gravitational_acceleration (m/s^2)                */
+} clm_earth_params;
+
+typedef struct clm_config {
+  int32_t model;          /* enum clm_model                                */
+  int32_t ncol;           /* number of columns                             */
+  int32_t nlayers;        /* >0: every column has nlayers layers;
+                             0: per-column counts from clm_set_geometry    */
+  int32_t precision;      /* enum clm_precision                            */
+  int32_t newton_mode;    /* enum clm_newton_mode                          */
+  int32_t max_iters;      /* Newton iterations (fixed) or cap (tolerance)  */
+  double newton_tol;      /* tolerance-mode threshold                      */
+  double energy_norm_scale; /* weight of rho e_int in the tolerance norm   */
+  int32_t learned_guess;  /* 1: use the loaded MLP as the Newton guess     */
+  int32_t bc_top_water, bc_top_heat, bc_bottom_water, bc_bottom_heat;
+  /* scalar EnergyHydrologyParameters (energy_hydrology.jl:44-61) */
+  double kersten_alpha, kersten_beta, ice_impedance_omega;
+  double visc_gamma, visc_gamma_T_ref;
+  clm_earth_params earth;
+  int32_t phase_change;   /* 1: PhaseChange source (energy_hydrology.jl:822)
+                             in the explicit tendency (EnergyHydrology)    */
+  int32_t pad0;
+  uint64_t forcing_seed;  /* seed of the rain-pulse hash                   */
+  int32_t cols_per_cta;   /* 0: autotuned / default                        */
+  int32_t reserved[7];
+} clm_config;
+
+typedef struct clm_handle clm_handle;
+
+/* Fill `cfg` with defaults: EnergyHydrology, FP64, fixed 3 Newton
+ * iterations (Simulations.jl:127-135), flux top / free-drainage bottom,
+ * Kersten alpha 0.24, beta 18.3, Omega 7, gamma 2.64e-2, gamma_T_ref 288
+ * (test/standalone/Soil/soil_parameterizations.jl:71-75). */
+void clm_config_default(clm_config* cfg);
+
+/* Replaces LandSimulation's model set-up (Simulations.jl:115-245) and
+ * initialize(model) (models.jl:493-499): allocates the device state. */
+int clm_create(const clm_config* cfg, clm_handle** out);
+void clm_destroy(clm_handle* h);
+const char* clm_last_error(const clm_handle* h);
+
+/* Column geometry (Domains.jl:183-247 Column, get_Δz :935-949): column c
+ * spans [z_lo[c], z_hi[c]] with uniform layers; offsets (ncol+1 entries,
+ * may be NULL when cfg->nlayers > 0) give the per-column layer counts. */
+int clm_set_geometry(clm_handle* h, const double* z_lo, const double* z_hi,
+                     const int32_t* offsets);
+
+/* Per-column parameters, nparams rows of ncol (enum clm_param). Replaces
+ * RichardsParameters / EnergyHydrologyParameters fields. */
+int clm_set_params(clm_handle* h, const double* soa_params, int32_t nparams);
+
+/* Boundary forcing for one slot, CLM_F_NFIELDS rows of ncol. Replaces the
+ * bc closures evaluated by boundary_flux! (boundary_conditions.jl:168-608). */
+int clm_set_bc(clm_handle* h, int32_t slot, const double* soa_forcing,
+               int32_t nfields);
+
+/* Prognostic state Y.soil (energy_hydrology.jl:624-625, rre.jl:282).
+ * theta_i, rho_e, intF_e may be NULL for RichardsModel. */
+int clm_set_state(clm_handle* h, const double* vartheta_l,
+                  const double* theta_i, const double* rho_e_int,
+                  const double* intF_w, const double* intF_e);
+int clm_get_state(clm_handle* h, double* vartheta_l, double* theta_i,
+                  double* rho_e_int, double* intF_w, double* intF_e);
+
+/* Same, with device pointers (caller-owned CuArray memory, reference
+ * layout). Copies device-to-device on the handle's stream. */
+int clm_set_state_device(clm_handle* h, const double* vartheta_l,
+                         const double* theta_i, const double* rho_e_int,
+                         const double* intF_w, const double* intF_e);
+int clm_get_state_device(clm_handle* h, double* vartheta_l, double* theta_i,
+                         double* rho_e_int, double* intF_w, double* intF_e);
+
+/* Advance nsteps ARS111 steps of size dt from time t. Replaces
+ * step!(landsim) (Simulations.jl:312-314) -> ClimaTimeSteppers IMEX ARS111
+ * with NewtonsMethod (Simulations.jl:127-135) calling the closures
+ * make_exp_tendency (models.jl:279-287), make_compute_imp_tendency,
+ * make_compute_jacobian (rre.jl:161-458, energy_hydrology.jl:315-576),
+ * make_update_implicit_cache (models.jl:238-246) and the block solve
+ * selected in initialize_jacobian (implicit_timestepping.jl:63-172). */
+int clm_step(clm_handle* h, double t, double dt, int32_t nsteps);
+int clm_step_async(clm_handle* h, double t, double dt, int32_t nsteps);
+int clm_sync(clm_handle* h);
+
+/* Column budgets total_water / total_energy (rre.jl:502-511,
+ * energy_hydrology.jl:1282-1320) of the current state, per column. */
+int clm_get_budgets(clm_handle* h, double* total_water, double* total_energy);
+
+/* Per-column status flags (CLM_COL_*) and Newton iteration counts of the
+ * last step call (either pointer may be NULL). Stands in for
+ * NaNCheckCallback (utils.jl:684-694). */
+int clm_get_status(clm_handle* h, uint32_t* flags, int32_t* newton_iters);
+
+/* ---- closure-level entry points (for parity of each closure) ---------
+ * All operate on the handle's current state at time t; outputs are host
+ * buffers in the reference layout. */
+
+/* make_update_aux (rre.jl:368-380; energy_hydrology.jl:722-814) followed
+ * by make_update_boundary_fluxes (rre.jl:111-149;
+ * energy_hydrology.jl:273-298). Outputs per cell: K, psi and, for
+ * EnergyHydrology, theta_l, T, kappa, Tf_depressed (NULL to skip); per
+ * column: top/bottom water and heat fluxes (bc[4*ncol], slot-major). */
+int clm_update_aux(clm_handle* h, double t, double* K, double* psi,
+                   double* theta_l, double* T, double* kappa,
+                   double* Tf_depressed, double* bc_fluxes);
+
+/* make_exp_tendency (models.jl:279-287): update_aux + boundary fluxes +
+ * compute_exp_tendency! (rre.jl:214-243; energy_hydrology.jl:315-350 with
+ * the PhaseChange source :838-906). Outputs dY in the state layout. */
+int clm_exp_tendency(clm_handle* h, double t, double* d_vartheta_l,
+                     double* d_theta_i, double* d_rho_e_int, double* d_intF_w,
+                     double* d_intF_e);
+
+/* make_compute_imp_tendency (rre.jl:161-203; energy_hydrology.jl:363-425)
+ * evaluated after make_update_cache at (state, t). */
+int clm_imp_tendency(clm_handle* h, double t, double* d_vartheta_l,
+                     double* d_theta_i, double* d_rho_e_int, double* d_intF_w,
+                     double* d_intF_e);
+
+/* make_compute_jacobian (rre.jl:391-458; energy_hydrology.jl:466-576)
+ * after make_update_cache at (state, t): tridiagonal blocks
+ * W = dtgamma * dT/dY - I, each 3 values per cell (lower, diag, upper):
+ * W_vv (d vartheta / d vartheta), W_ev (d rho_e / d vartheta), W_ee. */
+int clm_jacobian(clm_handle* h, double t, double dtgamma, double* W_vv,
+                 double* W_ev, double* W_ee);
+
+/* The block solve of initialize_jacobian's FieldMatrixSolver
+ * (BlockDiagonalSolve / BlockLowerTriangularSolve(soil.ϑ_l),
+ * implicit_timestepping.jl:160-171): given blocks and residual f, returns
+ * delta with W delta = f per column (cell layout). f_e/W_e* may be NULL for
+ * RichardsModel. */
+int clm_solve(clm_handle* h, const double* W_vv, const double* W_ev,
+              const double* W_ee, const double* f_v, const double* f_e,
+              double* delta_v, double* delta_e);
+
+/* ---- learned Newton guess (no reference counterpart) ------------------ */
+/* Load the MLP weights (layout in clm_mlp_layout) used when
+ * cfg->learned_guess = 1. */
+int clm_load_mlp(clm_handle* h, const void* weights, int64_t nbytes);
+
+/* Counter hash used by the rain-pulse forcing: uniform in [0, 1). Plain
+ * integer arithmetic, identical on host and device. */
+double clm_forcing_hash01(uint64_t seed, uint64_t column, int64_t period);
+
+/* Library version string. */
+const char* clm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CLIMALAND_CUDA_H */

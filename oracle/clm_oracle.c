@@ -1,0 +1,1018 @@
+/*
+ * ORACLE — test infrastructure only (see clm_oracle.h).
+ *
+ * FP64 CPU restatement of the ClimaLand.jl v1.11.2 soil column step. Each
+ * function cites the reference lines it follows (paths relative to the
+ * ClimaLand.jl tree). Third-party numerics that are not vendored in the
+ * reference are restated from their published semantics:
+ *   ClimaCore 0.15.2  InterpolateC2F (face = mean of the two centres),
+ *                     GradientC2F (centre difference / centre spacing,
+ *                     SetGradient(0) rows vanish at boundary faces),
+ *                     DivergenceF2C (face difference / layer width,
+ *                     SetValue supplies the boundary-face flux),
+ *                     column_integral_definite! (sum of dz * f),
+ *                     FieldMatrixSolver (Thomas per column; block lower
+ *                     triangular for EnergyHydrology).
+ *   ClimaTimeSteppers 0.10.6  IMEX ARS111 (explicit [0 0; 1 0], b = [1 0];
+ *                     implicit [0 0; 0 1], b = [0 1]) with NewtonsMethod,
+ *                     UpdateEvery(NewNewtonIteration). Assumed ordering:
+ *                     cache_imp!(U) runs on the stage value before the
+ *                     first residual; each iteration evaluates the
+ *                     residual and the Jacobian at x, solves, sets
+ *                     x -= delta and runs cache_imp!(x). The final state is
+ *                     u + dt*T_exp[1] + dt*T_imp[2] with
+ *                     T_imp[2] = (x - U) / dt.
+ */
+#include "clm_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define MAXL 256
+
+static const double SQRT_EPS = 1.4901161193847656e-08; /* sqrt(eps(Float64)) */
+static const double EPS64 = 2.220446049250313e-16;     /* eps(Float64)        */
+
+/* ======================================================================
+ * Pointwise hydrology: soil_hydrology_parameterizations.jl
+ * ====================================================================== */
+
+/* :22-31 */
+double clmo_volumetric_liquid_fraction(double vartheta_l, double nu_eff,
+                                       double theta_r) {
+  double v_safe = fmax(vartheta_l, theta_r + SQRT_EPS);
+  double nu_safe = fmax(nu_eff, theta_r + SQRT_EPS);
+  return (v_safe < nu_safe) ? v_safe : nu_safe;
+}
+
+/* :45-50 */
+double clmo_effective_saturation(double nu_eff, double vartheta_l,
+                                 double theta_r) {
+  double v_safe = fmax(vartheta_l, theta_r + SQRT_EPS);
+  double nu_safe = fmax(nu_eff, theta_r + SQRT_EPS);
+  return (v_safe - theta_r) / (nu_safe - theta_r);
+}
+
+/* :59-63 */
+double clmo_matric_potential(double alpha, double n, double m, double S) {
+  return -pow((pow(S, -1.0 / m) - 1.0) * pow(alpha, -n), 1.0 / n);
+}
+
+/* :72-77 (the reference raises an error for psi > 0; here a flag) */
+double clmo_inverse_matric_potential(double alpha, double n, double m,
+                                     double psi, int* psi_positive) {
+  if (psi > 0 && psi_positive) *psi_positive = 1;
+  return pow(1.0 + pow(alpha * fabs(psi), n), -m);
+}
+
+/* :109-127 */
+double clmo_pressure_head(double alpha, double n, double m, double theta_r,
+                          double vartheta_l, double nu_eff, double S_s) {
+  double S = clmo_effective_saturation(nu_eff, vartheta_l, theta_r);
+  double v_safe = fmax(vartheta_l, theta_r + SQRT_EPS);
+  double nu_safe = fmax(nu_eff, theta_r + SQRT_EPS);
+  if (S <= 1.0) return clmo_matric_potential(alpha, n, m, S);
+  return (v_safe - nu_safe) / S_s;
+}
+
+/* :135-152 */
+double clmo_dpsidvartheta(double alpha, double n, double m, double vartheta,
+                          double nu_eff, double theta_r, double S_s) {
+  double nu_safe = fmax(nu_eff, theta_r + SQRT_EPS);
+  double S = clmo_effective_saturation(nu_safe, vartheta, theta_r);
+  if (S < 1.0)
+    return 1.0 / (alpha * m * n) / (nu_safe - theta_r) *
+           pow(pow(S, -1.0 / m) - 1.0, 1.0 / n - 1.0) * pow(S, -1.0 / m - 1.0);
+  return 1.0 / S_s;
+}
+
+/* :161-173 */
+double clmo_hydraulic_conductivity(double m, double K_sat, double S) {
+  double K;
+  if (S < 1.0) {
+    double f = 1.0 - pow(1.0 - pow(S, 1.0 / m), m);
+    K = sqrt(S) * f * f;
+  } else {
+    K = 1.0;
+  }
+  return K * K_sat;
+}
+
+/* :302-305 */
+double clmo_impedance_factor(double f_i, double Omega) {
+  return pow(10.0, -Omega * f_i);
+}
+
+/* :320-323 */
+double clmo_viscosity_factor(double T, double gamma, double gamma_T_ref) {
+  return exp(gamma * (T - gamma_T_ref));
+}
+
+/* src/shared_utilities/utils.jl:95-101: 1 if x - a > eps(FT) else 0 */
+double clmo_heaviside(double x, double a) {
+  return (x - a > EPS64) ? 1.0 : 0.0;
+}
+
+/* ======================================================================
+ * Pointwise heat: soil_heat_parameterizations.jl
+ * ====================================================================== */
+
+/* :35-52 (argument order as the reference signature: rho_ice, rho_liq) */
+double clmo_soil_Tf_depressed(double theta_l, double theta_i, double nu,
+                              double theta_r, double alpha, double n,
+                              double m, double rho_ice, double rho_liq,
+                              double T_freeze, double grav, double LH_f0) {
+  double theta_tot = fmin(rho_ice / rho_liq * theta_i + theta_l, nu);
+  double psi_w0 = clmo_matric_potential(
+      alpha, n, m, clmo_effective_saturation(nu, theta_tot, theta_r));
+  return fmax(T_freeze * exp(grav * psi_w0 / LH_f0), 1.0);
+}
+
+/* :60-62 */
+double clmo_thermal_time(double rhoc, double dz, double kappa) {
+  return 3.0 * rhoc * dz * dz / kappa;
+}
+
+/* :89-122 */
+double clmo_phase_change_source(double theta_l, double theta_i, double T,
+                                double tau, double nu, double theta_r,
+                                double alpha, double n, double m,
+                                double rho_i, double rho_l, double LH_f0,
+                                double T_freeze, double grav,
+                                int* psi_positive) {
+  double Tf = clmo_soil_Tf_depressed(theta_l, theta_i, nu, theta_r, alpha, n,
+                                     m, rho_i, rho_l, T_freeze, grav, LH_f0);
+  double psi_T = LH_f0 / grav * log(T / Tf) * clmo_heaviside(Tf - T, 0.0);
+  double theta_tot = fmin(rho_i / rho_l * theta_i + theta_l, nu);
+  double psi_w0 = clmo_matric_potential(
+      alpha, n, m, clmo_effective_saturation(nu, theta_tot, theta_r));
+  double theta_star =
+      clmo_inverse_matric_potential(alpha, n, m, psi_w0 + psi_T,
+                                    psi_positive) *
+          (nu - theta_r) +
+      theta_r;
+  return (theta_l - theta_star) / tau;
+}
+
+/* :157-171 */
+double clmo_volumetric_heat_capacity(double theta_l, double theta_i,
+                                     double rhoc_ds,
+                                     const clm_earth_params* e) {
+  double rhocp_i = e->cp_i * e->rho_i;
+  double rhocp_l = e->cp_l * e->rho_l;
+  return rhoc_ds + theta_l * rhocp_l + theta_i * rhocp_i;
+}
+
+/* :180-192 */
+double clmo_temperature_from_rho_e_int(double rho_e_int, double theta_i,
+                                       double rhoc_s,
+                                       const clm_earth_params* e) {
+  return e->T_0 + (rho_e_int + theta_i * e->rho_i * e->LH_f0) / rhoc_s;
+}
+
+/* :201-212 */
+double clmo_volumetric_internal_energy(double theta_i, double rhoc_s,
+                                       double T, const clm_earth_params* e) {
+  return rhoc_s * (T - e->T_0) - theta_i * e->rho_i * e->LH_f0;
+}
+
+/* :221-231 */
+double clmo_volumetric_internal_energy_liq(double T,
+                                           const clm_earth_params* e) {
+  double rhocp_l = e->cp_l * e->rho_l;
+  return rhocp_l * (T - e->T_0);
+}
+
+/* :243-256 */
+double clmo_kappa_sat(double theta_l, double theta_i, double k_unfrozen,
+                      double k_frozen) {
+  double theta_w = theta_l + theta_i;
+  if (theta_w < EPS64) return (k_unfrozen + k_frozen) / 2.0;
+  return pow(k_unfrozen, theta_l / theta_w) * pow(k_frozen, theta_i / theta_w);
+}
+
+/* :267-270 */
+double clmo_thermal_conductivity(double kappa_dry, double K_e,
+                                 double kappa_sat) {
+  return K_e * kappa_sat + (1.0 - K_e) * kappa_dry;
+}
+
+/* :283-285 */
+double clmo_relative_saturation(double theta_l, double theta_i, double nu) {
+  return (theta_l + theta_i) / nu;
+}
+
+/* :301-320 */
+double clmo_kersten_number(double theta_i, double S_r, double a, double b,
+                           double nu_om, double nu_quartz, double nu_gravel) {
+  if (theta_i < EPS64) {
+    double t1 = pow(1.0 + exp(-b * S_r), -3.0);
+    double t2 = pow((1.0 - S_r) / 2.0, 3.0);
+    return pow(S_r, (1.0 + nu_om - a * nu_quartz - nu_gravel) / 2.0) *
+           pow(t1 - t2, 1.0 - nu_om);
+  }
+  return pow(S_r, 1.0 + nu_om);
+}
+
+/* :338-348 */
+double clmo_kappa_solid(double nu_om, double nu_quartz, double k_om,
+                        double k_quartz, double k_minerals) {
+  return pow(k_om, nu_om) * pow(k_quartz, nu_quartz) *
+         pow(k_minerals, 1.0 - nu_om - nu_quartz);
+}
+
+/* :359-361 */
+double clmo_kappa_sat_frozen(double kappa_solid, double nu, double kappa_ice) {
+  return pow(kappa_solid, 1.0 - nu) * pow(kappa_ice, nu);
+}
+
+/* :371-373 */
+double clmo_kappa_sat_unfrozen(double kappa_solid, double nu, double kappa_l) {
+  return pow(kappa_solid, 1.0 - nu) * pow(kappa_l, nu);
+}
+
+/* :386-392 */
+double clmo_kappa_dry(double rho_p, double nu, double kappa_solid,
+                      double kappa_air) {
+  const double a = 0.053;
+  double rho_b_dry = (1.0 - nu) * rho_p;
+  double num = (a * kappa_solid - kappa_air) * rho_b_dry + kappa_air * rho_p;
+  double den = rho_p - (1.0 - a) * rho_b_dry;
+  return num / den;
+}
+
+/* ======================================================================
+ * Forcing descriptor (stands in for the bc(p, t) closures).
+ * ====================================================================== */
+
+static uint64_t mix64(uint64_t z) { /* splitmix64 finaliser (Vigna) */
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+double clm_forcing_hash01(uint64_t seed, uint64_t column, int64_t period) {
+  uint64_t h = mix64(seed + 0x9E3779B97F4A7C15ULL * (column + 1ULL));
+  h = mix64(h ^ ((uint64_t)period * 0xD1B54A32D192ED03ULL));
+  return (double)(h >> 11) * (1.0 / 9007199254740992.0);
+}
+
+double clmo_forcing_value(const double* F, int32_t ncol, int32_t c, double t,
+                          uint64_t seed) {
+  if (!F) return 0.0;
+  double v = F[CLM_F_BASE * ncol + c];
+  double amp = F[CLM_F_AMP * ncol + c];
+  if (amp != 0.0)
+    v += amp * sin(F[CLM_F_OMEGA * ncol + c] * t + F[CLM_F_PHASE * ncol + c]);
+  double pp = F[CLM_F_PULSE_PERIOD * ncol + c];
+  if (pp > 0.0) {
+    int64_t k = (int64_t)floor(t / pp);
+    if (clm_forcing_hash01(seed, (uint64_t)c, k) < F[CLM_F_PULSE_DUTY * ncol + c])
+      v += F[CLM_F_PULSE_AMP * ncol + c];
+  }
+  return v;
+}
+
+/* ======================================================================
+ * Column model
+ * ====================================================================== */
+
+typedef struct {
+  int n;
+  int eh; /* EnergyHydrology? */
+  /* geometry (Domains.jl:183-247, get_Δz :935-949) */
+  double z[MAXL];     /* centre coordinates                     */
+  double dzc[MAXL];   /* layer widths (ClimaCore Δz_field(z))   */
+  double dzf[MAXL];   /* dzf[k]: centre spacing between k-1, k  */
+  double dz_top, dz_bottom; /* centre-to-boundary distances      */
+  /* parameters */
+  double nu, K_sat, S_s, theta_r, alpha, vgn, vgm;
+  double kappa_dry, kappa_sat_frozen, kappa_sat_unfrozen, rhoc_ds;
+  double nu_om, nu_quartz, nu_gravel;
+  const clm_config* cfg;
+  const clmo_problem* P;
+  int c;
+} col_t;
+
+typedef struct { /* p.soil */
+  double K[MAXL], psi[MAXL], theta_l[MAXL], T[MAXL], kappa[MAXL], Tf[MAXL];
+  double top_w, top_h, bot_w, bot_h;
+  int has_dflux;
+  double dfluxBCdY;
+  double total_water, total_energy;
+  int psi_positive;
+} cache_t;
+
+typedef struct {
+  double v[MAXL], ti[MAXL], e[MAXL];
+  double Fw, Fe;
+} state_t;
+
+typedef struct {
+  double vv[3][MAXL], ev[3][MAXL], ee[3][MAXL];
+} jac_t;
+
+static void col_init(col_t* C, const clmo_problem* P, int c) {
+  const clm_config* cfg = &P->cfg;
+  int ncol = P->ncol;
+  C->P = P;
+  C->cfg = cfg;
+  C->c = c;
+  C->n = P->offsets[c + 1] - P->offsets[c];
+  C->eh = (cfg->model == CLM_MODEL_ENERGY_HYDROLOGY);
+  int n = C->n;
+  double zlo = P->z_lo[c], zhi = P->z_hi[c];
+  double zf[MAXL + 1];
+  for (int k = 0; k <= n; ++k) zf[k] = zlo + (zhi - zlo) * ((double)k / n);
+  zf[n] = zhi;
+  for (int k = 0; k < n; ++k) {
+    C->z[k] = 0.5 * (zf[k] + zf[k + 1]);
+    C->dzc[k] = zf[k + 1] - zf[k];
+  }
+  C->dzf[0] = 0.0;
+  for (int k = 1; k < n; ++k) C->dzf[k] = C->z[k] - C->z[k - 1];
+  C->dz_top = zf[n] - C->z[n - 1];
+  C->dz_bottom = C->z[0] - zf[0];
+  const double* p = P->params;
+  C->nu = p[CLM_P_NU * ncol + c];
+  C->K_sat = p[CLM_P_K_SAT * ncol + c];
+  C->S_s = p[CLM_P_S_S * ncol + c];
+  C->theta_r = p[CLM_P_THETA_R * ncol + c];
+  C->alpha = p[CLM_P_VG_ALPHA * ncol + c];
+  C->vgn = p[CLM_P_VG_N * ncol + c];
+  C->vgm = 1.0 - 1.0 / C->vgn; /* retention_models.jl:364-368 */
+  if (C->eh) {
+    C->kappa_dry = p[CLM_P_KAPPA_DRY * ncol + c];
+    C->kappa_sat_frozen = p[CLM_P_KAPPA_SAT_FROZEN * ncol + c];
+    C->kappa_sat_unfrozen = p[CLM_P_KAPPA_SAT_UNFROZEN * ncol + c];
+    C->rhoc_ds = p[CLM_P_RHOC_DS * ncol + c];
+    C->nu_om = p[CLM_P_NU_SS_OM * ncol + c];
+    C->nu_quartz = p[CLM_P_NU_SS_QUARTZ * ncol + c];
+    C->nu_gravel = p[CLM_P_NU_SS_GRAVEL * ncol + c];
+  }
+}
+
+static void state_load(const col_t* C, state_t* Y, const double* v,
+                       const double* ti, const double* e, const double* Fw,
+                       const double* Fe) {
+  int o = C->P->offsets[C->c];
+  for (int k = 0; k < C->n; ++k) {
+    Y->v[k] = v[o + k];
+    Y->ti[k] = (C->eh && ti) ? ti[o + k] : 0.0;
+    Y->e[k] = (C->eh && e) ? e[o + k] : 0.0;
+  }
+  Y->Fw = Fw ? Fw[C->c] : 0.0;
+  Y->Fe = (C->eh && Fe) ? Fe[C->c] : 0.0;
+}
+
+static void state_store(const col_t* C, const state_t* Y, double* v,
+                        double* ti, double* e, double* Fw, double* Fe) {
+  int o = C->P->offsets[C->c];
+  for (int k = 0; k < C->n; ++k) {
+    if (v) v[o + k] = Y->v[k];
+    if (C->eh && ti) ti[o + k] = Y->ti[k];
+    if (C->eh && e) e[o + k] = Y->e[k];
+  }
+  if (Fw) Fw[C->c] = Y->Fw;
+  if (C->eh && Fe) Fe[C->c] = Y->Fe;
+}
+
+/* Richards update_aux!: rre.jl:368-380 */
+static void richards_update_aux(const col_t* C, const state_t* Y,
+                                 cache_t* p) {
+  double W = 0.0;
+  for (int k = 0; k < C->n; ++k) {
+    p->K[k] = clmo_hydraulic_conductivity(
+        C->vgm, C->K_sat,
+        clmo_effective_saturation(C->nu, Y->v[k], C->theta_r));
+    p->psi[k] = clmo_pressure_head(C->alpha, C->vgn, C->vgm, C->theta_r,
+                                   Y->v[k], C->nu, C->S_s);
+    W += C->dzc[k] * Y->v[k]; /* rre.jl:502-511 */
+  }
+  p->total_water = W;
+}
+
+/* EnergyHydrology update_aux!: energy_hydrology.jl:722-814 */
+static void eh_update_aux(const col_t* C, const state_t* Y, cache_t* p) {
+  const clm_config* cfg = C->cfg;
+  const clm_earth_params* e = &cfg->earth;
+  double W = 0.0, E = 0.0;
+  for (int k = 0; k < C->n; ++k) {
+    double v = Y->v[k], ti = Y->ti[k];
+    double tl = clmo_volumetric_liquid_fraction(v, C->nu - ti, C->theta_r);
+    p->theta_l[k] = tl;
+    p->kappa[k] = clmo_thermal_conductivity(
+        C->kappa_dry,
+        clmo_kersten_number(ti, clmo_relative_saturation(tl, ti, C->nu),
+                            cfg->kersten_alpha, cfg->kersten_beta, C->nu_om,
+                            C->nu_quartz, C->nu_gravel),
+        clmo_kappa_sat(tl, ti, C->kappa_sat_unfrozen, C->kappa_sat_frozen));
+    p->T[k] = clmo_temperature_from_rho_e_int(
+        Y->e[k], ti, clmo_volumetric_heat_capacity(tl, ti, C->rhoc_ds, e), e);
+    p->K[k] = clmo_impedance_factor(ti / (tl + ti - C->theta_r),
+                                    cfg->ice_impedance_omega) *
+              clmo_viscosity_factor(p->T[k], cfg->visc_gamma,
+                                    cfg->visc_gamma_T_ref) *
+              clmo_hydraulic_conductivity(
+                  C->vgm, C->K_sat,
+                  clmo_effective_saturation(C->nu, v, C->theta_r));
+    p->psi[k] = clmo_pressure_head(C->alpha, C->vgn, C->vgm, C->theta_r, v,
+                                   C->nu - ti, C->S_s);
+    /* :797-808 passes (_ρ_l, _ρ_i) into the (_ρ_ice, _ρ_liq) slots. */
+    p->Tf[k] = clmo_soil_Tf_depressed(tl, ti, C->nu, C->theta_r, C->alpha,
+                                      C->vgn, C->vgm, e->rho_l, e->rho_i,
+                                      e->T_freeze, e->grav, e->LH_f0);
+    /* :1282-1320 */
+    W += C->dzc[k] * (v + ti * e->rho_i / e->rho_l);
+    E += C->dzc[k] * Y->e[k];
+  }
+  p->total_water = W;
+  p->total_energy = E;
+}
+
+/* EnergyHydrology update_implicit_aux!: energy_hydrology.jl:427-445 */
+static void eh_update_implicit_aux(const col_t* C, const state_t* Y,
+                                   cache_t* p) {
+  const clm_earth_params* e = &C->cfg->earth;
+  for (int k = 0; k < C->n; ++k) {
+    double v = Y->v[k], ti = Y->ti[k];
+    p->T[k] = clmo_temperature_from_rho_e_int(
+        Y->e[k], ti,
+        clmo_volumetric_heat_capacity(fmin(C->nu - ti, v), ti, C->rhoc_ds, e),
+        e);
+    p->psi[k] = clmo_pressure_head(C->alpha, C->vgn, C->vgm, C->theta_r, v,
+                                   C->nu - ti, C->S_s);
+  }
+}
+
+/* shared_utilities/boundary_conditions.jl:63-65 */
+static double diffusive_flux(double K, double x2, double x1, double dz) {
+  return -K * (x2 - x1) / dz;
+}
+
+/* Boundary fluxes.
+ * Richards: rre.jl:111-149 with boundary_flux! methods
+ *   WaterFluxBC :168-180, MoistureStateBC top :227-264 / bottom :278-315,
+ *   FreeDrainage :340-353, set_dfluxBCdY! (MoistureStateBC top) :375-426.
+ * EnergyHydrology: energy_hydrology.jl:273-298 with WaterHeatBC :709-724,
+ *   HeatFluxBC :465-477, TemperatureStateBC :494-544,
+ *   EnergyWaterFreeDrainage :590-608. */
+static void update_boundary_fluxes(const col_t* C, const state_t* Y,
+                                   cache_t* p, double t) {
+  const clm_config* cfg = C->cfg;
+  const clmo_problem* P = C->P;
+  const clm_earth_params* e = &cfg->earth;
+  int n = C->n, c = C->c, ncol = P->ncol;
+  uint64_t seed = cfg->forcing_seed;
+  double f_tw = clmo_forcing_value(P->forcing[CLM_BC_TOP_WATER], ncol, c, t, seed);
+  double f_th = clmo_forcing_value(P->forcing[CLM_BC_TOP_HEAT], ncol, c, t, seed);
+  double f_bw = clmo_forcing_value(P->forcing[CLM_BC_BOTTOM_WATER], ncol, c, t, seed);
+  double f_bh = clmo_forcing_value(P->forcing[CLM_BC_BOTTOM_HEAT], ncol, c, t, seed);
+  double nu_top = C->nu, nu_bot = C->nu;
+
+  /* water, top */
+  switch (cfg->bc_top_water) {
+    case CLM_BC_STATE: {
+      double psi_bc = clmo_pressure_head(C->alpha, C->vgn, C->vgm, C->theta_r,
+                                         f_tw, nu_top, C->S_s);
+      p->top_w = diffusive_flux(p->K[n - 1], psi_bc + C->dz_top, p->psi[n - 1],
+                                C->dz_top);
+      break;
+    }
+    default:
+      p->top_w = f_tw;
+  }
+  /* water, bottom */
+  switch (cfg->bc_bottom_water) {
+    case CLM_BC_FREE_DRAINAGE:
+      p->bot_w = -1.0 * p->K[0];
+      break;
+    case CLM_BC_STATE: {
+      double psi_bc = clmo_pressure_head(C->alpha, C->vgn, C->vgm, C->theta_r,
+                                         f_bw, nu_bot, C->S_s);
+      p->bot_w = diffusive_flux(p->K[0], p->psi[0] + C->dz_bottom, psi_bc,
+                                C->dz_bottom);
+      break;
+    }
+    default:
+      p->bot_w = f_bw;
+  }
+  if (C->eh) {
+    switch (cfg->bc_top_heat) {
+      case CLM_BC_STATE:
+        p->top_h = diffusive_flux(p->kappa[n - 1], f_th, p->T[n - 1], C->dz_top);
+        break;
+      case CLM_BC_FLUX_ADVECTIVE: {
+        double T_adv = P->forcing[CLM_BC_TOP_HEAT]
+                           ? P->forcing[CLM_BC_TOP_HEAT][CLM_F_T_ADV * ncol + c]
+                           : e->T_0;
+        p->top_h = f_th + p->top_w * clmo_volumetric_internal_energy_liq(T_adv, e);
+        break;
+      }
+      default:
+        p->top_h = f_th;
+    }
+    switch (cfg->bc_bottom_heat) {
+      case CLM_BC_FREE_DRAINAGE: /* EnergyWaterFreeDrainage */
+        p->bot_h = -1.0 * p->K[0] * clmo_volumetric_internal_energy_liq(p->T[0], e);
+        break;
+      case CLM_BC_STATE:
+        p->bot_h = diffusive_flux(p->kappa[0], p->T[0], f_bh, C->dz_bottom);
+        break;
+      default:
+        p->bot_h = f_bh;
+    }
+  } else {
+    p->top_h = p->bot_h = 0.0;
+  }
+  /* set_dfluxBCdY! exists for RichardsModel + MoistureStateBC at the top */
+  p->has_dflux = (!C->eh && cfg->bc_top_water == CLM_BC_STATE);
+  if (p->has_dflux) {
+    p->dfluxBCdY = p->K[n - 1] *
+                   clmo_dpsidvartheta(C->alpha, C->vgn, C->vgm, Y->v[n - 1],
+                                      C->nu, C->theta_r, C->S_s) /
+                   C->dz_top;
+  }
+}
+
+/* make_update_cache = update_aux! + update_boundary_fluxes! */
+static void update_cache(const col_t* C, const state_t* Y, cache_t* p,
+                         double t) {
+  if (C->eh)
+    eh_update_aux(C, Y, p);
+  else
+    richards_update_aux(C, Y, p);
+  update_boundary_fluxes(C, Y, p, t);
+}
+
+/* make_update_implicit_cache (models.jl:238-246): implicit aux, then the
+ * boundary fluxes only if dfluxBCdY is in the cache (rre.jl:460-468,
+ * energy_hydrology.jl:447-455). Richards' implicit aux is the full aux
+ * (models.jl:207-210). */
+static void update_implicit_cache(const col_t* C, const state_t* Y,
+                                  cache_t* p, double t) {
+  if (C->eh)
+    eh_update_implicit_aux(C, Y, p);
+  else
+    richards_update_aux(C, Y, p);
+  if (p->has_dflux) update_boundary_fluxes(C, Y, p, t);
+}
+
+/* compute_exp_tendency!: rre.jl:214-243; energy_hydrology.jl:315-350 and
+ * the PhaseChange source!: energy_hydrology.jl:838-906. */
+static void exp_tendency(const col_t* C, const state_t* Y, cache_t* p,
+                         state_t* dY) {
+  int n = C->n;
+  for (int k = 0; k < n; ++k) dY->v[k] = dY->ti[k] = dY->e[k] = 0.0;
+  dY->Fw = dY->Fe = 0.0;
+  if (C->eh && C->cfg->phase_change) {
+    const clm_earth_params* e = &C->cfg->earth;
+    for (int k = 0; k < n; ++k) {
+      double tl = p->theta_l[k], ti = Y->ti[k];
+      double tau = clmo_thermal_time(
+          clmo_volumetric_heat_capacity(tl, ti, C->rhoc_ds, e), C->dzc[k],
+          p->kappa[k]);
+      int pp = 0;
+      double src = clmo_phase_change_source(
+          tl, ti, p->T[k], tau, C->nu, C->theta_r, C->alpha, C->vgn, C->vgm,
+          e->rho_i, e->rho_l, e->LH_f0, e->T_freeze, e->grav, &pp);
+      if (pp) p->psi_positive = 1;
+      dY->v[k] += -src;
+      dY->ti[k] += (e->rho_l / e->rho_i) * src;
+    }
+  }
+}
+
+/* Darcy + heat fluxes at faces and the divergence (ClimaCore
+ * DivergenceF2C(SetValue) of -interp(K) * grad(psi + z), etc.):
+ * rre.jl:161-203; energy_hydrology.jl:363-425. */
+static void imp_tendency(const col_t* C, const state_t* Y, const cache_t* p,
+                         state_t* dY) {
+  int n = C->n;
+  double Fw[MAXL + 1], Fe[MAXL + 1];
+  const clm_earth_params* e = &C->cfg->earth;
+  (void)Y;
+  dY->Fw = -(p->top_w - p->bot_w);
+  Fw[0] = p->bot_w;
+  Fw[n] = p->top_w;
+  for (int k = 1; k < n; ++k) {
+    double Kf = 0.5 * (p->K[k - 1] + p->K[k]);
+    double gh = ((p->psi[k] + C->z[k]) - (p->psi[k - 1] + C->z[k - 1])) / C->dzf[k];
+    Fw[k] = -Kf * gh;
+  }
+  for (int k = 0; k < n; ++k) dY->v[k] = -((Fw[k + 1] - Fw[k]) / C->dzc[k]);
+  if (C->eh) {
+    dY->Fe = -(p->top_h - p->bot_h);
+    Fe[0] = p->bot_h;
+    Fe[n] = p->top_h;
+    for (int k = 1; k < n; ++k) {
+      double kf = 0.5 * (p->kappa[k - 1] + p->kappa[k]);
+      double gT = (p->T[k] - p->T[k - 1]) / C->dzf[k];
+      double gh = ((p->psi[k] + C->z[k]) - (p->psi[k - 1] + C->z[k - 1])) / C->dzf[k];
+      double lk = 0.5 * (clmo_volumetric_internal_energy_liq(p->T[k - 1], e) * p->K[k - 1] +
+                         clmo_volumetric_internal_energy_liq(p->T[k], e) * p->K[k]);
+      Fe[k] = -kf * gT - lk * gh;
+    }
+    for (int k = 0; k < n; ++k) {
+      dY->e[k] = -((Fe[k + 1] - Fe[k]) / C->dzc[k]);
+      dY->ti[k] = 0.0;
+    }
+  } else {
+    dY->Fe = 0.0;
+  }
+}
+
+/* Assemble -dtγ * div * diag(coef_face) * grad * diag(d) - I as a
+ * tridiagonal (lower, diag, upper) given face coefficients a_f at
+ * interior faces (the MatrixFields.operator_matrix algebra of
+ * rre.jl:402-454). coef_face[k] for k = 1..n-1 multiplies the (SetGradient
+ * zero at the boundary) gradient at the face between centres k-1 and k. */
+static void assemble_block(const col_t* C, double dtgamma,
+                           const double* coef_face, const double* d,
+                           double* L, double* M, double* U) {
+  int n = C->n;
+  for (int k = 0; k < n; ++k) {
+    /* Row k of div * diag(-coef) * grad * diag(d):
+     *   (1/dzc_k) [-a_up (d_{k+1} x_{k+1} - d_k x_k)
+     *              + a_dn (d_k x_k - d_{k-1} x_{k-1})],
+     * a = coef / dzf at interior faces; boundary-face rows are zero
+     * (GradientC2F with SetGradient(0) at top and bottom). */
+    int has_up = (k + 1 <= n - 1), has_dn = (k >= 1);
+    double a_up = has_up ? coef_face[k + 1] / C->dzf[k + 1] : 0.0;
+    double a_dn = has_dn ? coef_face[k] / C->dzf[k] : 0.0;
+    double rowU = has_up ? -a_up * d[k + 1] / C->dzc[k] : 0.0;
+    double rowL = has_dn ? -a_dn * d[k - 1] / C->dzc[k] : 0.0;
+    double rowD = (a_up + a_dn) * d[k] / C->dzc[k];
+    U[k] = -dtgamma * rowU;
+    L[k] = -dtgamma * rowL;
+    M[k] = -dtgamma * rowD - 1.0;
+  }
+}
+
+/* Jacobian: Richards rre.jl:391-458, EnergyHydrology
+ * energy_hydrology.jl:466-576 (including the "- I" on ∂ρe/∂ϑ,
+ * :554-556). */
+static void jacobian(const col_t* C, const state_t* Y, const cache_t* p,
+                     double dtgamma, jac_t* J) {
+  int n = C->n;
+  const clm_earth_params* e = &C->cfg->earth;
+  double D[MAXL], cf[MAXL + 1];
+  for (int k = 0; k < n; ++k)
+    D[k] = clmo_dpsidvartheta(C->alpha, C->vgn, C->vgm, Y->v[k],
+                              C->nu - (C->eh ? Y->ti[k] : 0.0), C->theta_r,
+                              C->S_s);
+  cf[0] = cf[n] = 0.0;
+  for (int k = 1; k < n; ++k) cf[k] = 0.5 * (p->K[k - 1] + p->K[k]);
+  assemble_block(C, dtgamma, cf, D, J->vv[0], J->vv[1], J->vv[2]);
+  if (p->has_dflux) {
+    /* LowerDiagonalMatrixRow(topBC_scratch) at the top face: adds
+     * dfluxBCdY acting on the top cell, then -dtγ * div */
+    J->vv[1][n - 1] += -dtgamma * (p->dfluxBCdY / C->dzc[n - 1]);
+  }
+  if (!C->eh) return;
+  for (int k = 1; k < n; ++k)
+    cf[k] = 0.5 * (clmo_volumetric_internal_energy_liq(p->T[k - 1], e) * p->K[k - 1] +
+                   clmo_volumetric_internal_energy_liq(p->T[k], e) * p->K[k]);
+  assemble_block(C, dtgamma, cf, D, J->ev[0], J->ev[1], J->ev[2]);
+  double R[MAXL];
+  for (int k = 0; k < n; ++k)
+    R[k] = 1.0 / clmo_volumetric_heat_capacity(p->theta_l[k], Y->ti[k],
+                                               C->rhoc_ds, e);
+  for (int k = 1; k < n; ++k) cf[k] = 0.5 * (p->kappa[k - 1] + p->kappa[k]);
+  assemble_block(C, dtgamma, cf, R, J->ee[0], J->ee[1], J->ee[2]);
+}
+
+/* Thomas algorithm for one tridiagonal system (bottom to top). */
+static void thomas(int n, const double* L, const double* M, const double* U,
+                   const double* f, double* x) {
+  double cp[MAXL], dp[MAXL];
+  cp[0] = U[0] / M[0];
+  dp[0] = f[0] / M[0];
+  for (int k = 1; k < n; ++k) {
+    double den = M[k] - L[k] * cp[k - 1];
+    cp[k] = U[k] / den;
+    dp[k] = (f[k] - L[k] * dp[k - 1]) / den;
+  }
+  x[n - 1] = dp[n - 1];
+  for (int k = n - 2; k >= 0; --k) x[k] = dp[k] - cp[k] * x[k + 1];
+}
+
+/* FieldMatrixSolver: BlockDiagonalSolve (Richards) or
+ * BlockLowerTriangularSolve(soil.ϑ_l) (EnergyHydrology),
+ * implicit_timestepping.jl:160-171; explicit blocks are -I. */
+static void block_solve(const col_t* C, const jac_t* J, const state_t* f,
+                        state_t* d) {
+  int n = C->n;
+  thomas(n, J->vv[0], J->vv[1], J->vv[2], f->v, d->v);
+  d->Fw = -f->Fw;
+  if (C->eh) {
+    double g[MAXL] = {0};
+    for (int k = 0; k < n; ++k) {
+      double w = J->ev[1][k] * d->v[k];
+      if (k > 0) w += J->ev[0][k] * d->v[k - 1];
+      if (k < n - 1) w += J->ev[2][k] * d->v[k + 1];
+      g[k] = f->e[k] - w;
+    }
+    thomas(n, J->ee[0], J->ee[1], J->ee[2], g, d->e);
+    for (int k = 0; k < n; ++k) d->ti[k] = -f->ti[k];
+    d->Fe = -f->Fe;
+  }
+}
+
+static int state_finite(const col_t* C, const state_t* Y) {
+  for (int k = 0; k < C->n; ++k)
+    if (!isfinite(Y->v[k]) || !isfinite(Y->ti[k]) || !isfinite(Y->e[k])) return 0;
+  return isfinite(Y->Fw) && isfinite(Y->Fe);
+}
+
+/* One ARS111 step with NewtonsMethod (see the header comment). */
+static void column_step(const col_t* C, state_t* Y, double t, double dt,
+                        uint32_t* flag, int32_t* iters) {
+  const clm_config* cfg = C->cfg;
+  int n = C->n;
+  cache_t p;
+  memset(&p, 0, sizeof(p));
+  state_t Te, U, x, Ti, f, d;
+  jac_t J;
+  /* stage 1: T_exp!(T_exp[1], u, p, t) = update_cache! + compute_exp_tendency! */
+  update_cache(C, Y, &p, t);
+  exp_tendency(C, Y, &p, &Te);
+  /* stage 2: U = u + dt * a_exp[2,1] * T_exp[1] */
+  for (int k = 0; k < n; ++k) {
+    U.v[k] = Y->v[k] + dt * Te.v[k];
+    U.ti[k] = Y->ti[k] + dt * Te.ti[k];
+    U.e[k] = Y->e[k] + dt * Te.e[k];
+  }
+  U.Fw = Y->Fw + dt * Te.Fw;
+  U.Fe = Y->Fe + dt * Te.Fe;
+  x = U;
+  double t_imp = t + dt;
+  update_implicit_cache(C, &x, &p, t_imp);
+  int it = 0;
+  double prev_norm = INFINITY;
+  int maxit = cfg->max_iters;
+  for (it = 1; it <= maxit; ++it) {
+    imp_tendency(C, &x, &p, &Ti);
+    for (int k = 0; k < n; ++k) {
+      f.v[k] = U.v[k] + dt * Ti.v[k] - x.v[k];
+      f.ti[k] = U.ti[k] + dt * Ti.ti[k] - x.ti[k];
+      f.e[k] = U.e[k] + dt * Ti.e[k] - x.e[k];
+    }
+    f.Fw = U.Fw + dt * Ti.Fw - x.Fw;
+    f.Fe = U.Fe + dt * Ti.Fe - x.Fe;
+    jacobian(C, &x, &p, dt, &J);
+    block_solve(C, &J, &f, &d);
+    double s2 = 0.0, se = cfg->energy_norm_scale;
+    for (int k = 0; k < n; ++k) {
+      x.v[k] -= d.v[k];
+      x.ti[k] -= d.ti[k];
+      x.e[k] -= d.e[k];
+      s2 += d.v[k] * d.v[k] + d.ti[k] * d.ti[k] + (se * d.e[k]) * (se * d.e[k]);
+    }
+    x.Fw -= d.Fw;
+    x.Fe -= d.Fe;
+    s2 += d.Fw * d.Fw + d.Fe * d.Fe;
+    update_implicit_cache(C, &x, &p, t_imp);
+    double nrm = sqrt(s2);
+    if (cfg->newton_mode == CLM_NEWTON_TOL) {
+      if (nrm > prev_norm && it > 2) *flag |= CLM_COL_DIVERGED;
+      prev_norm = nrm;
+      if (nrm < cfg->newton_tol) break;
+      if (it == maxit) *flag |= CLM_COL_NOT_CONVERGED;
+    }
+  }
+  if (it > maxit) it = maxit;
+  *iters = it;
+  /* T_imp[2] = (U_2 - temp) / (dt * a_imp[2,2]);
+   * u += dt * b_exp[1] * T_exp[1]; u += dt * b_imp[2] * T_imp[2] */
+  for (int k = 0; k < n; ++k) {
+    Y->v[k] = (Y->v[k] + dt * Te.v[k]) + dt * ((x.v[k] - U.v[k]) / dt);
+    Y->ti[k] = (Y->ti[k] + dt * Te.ti[k]) + dt * ((x.ti[k] - U.ti[k]) / dt);
+    Y->e[k] = (Y->e[k] + dt * Te.e[k]) + dt * ((x.e[k] - U.e[k]) / dt);
+  }
+  Y->Fw = (Y->Fw + dt * Te.Fw) + dt * ((x.Fw - U.Fw) / dt);
+  Y->Fe = (Y->Fe + dt * Te.Fe) + dt * ((x.Fe - U.Fe) / dt);
+  if (p.psi_positive) *flag |= CLM_COL_PSI_POSITIVE;
+  if (!state_finite(C, Y)) *flag |= CLM_COL_NONFINITE;
+}
+
+/* ======================================================================
+ * Batch entry points
+ * ====================================================================== */
+
+static int check_problem(const clmo_problem* P) {
+  if (!P || P->ncol <= 0 || !P->offsets || !P->z_lo || !P->z_hi || !P->params)
+    return CLM_ERR_ARG;
+  int need = P->cfg.model == CLM_MODEL_ENERGY_HYDROLOGY ? CLM_NPARAM_EH
+                                                        : CLM_NPARAM_RICHARDS;
+  if (P->nparams < need) return CLM_ERR_ARG;
+  for (int c = 0; c < P->ncol; ++c) {
+    int n = P->offsets[c + 1] - P->offsets[c];
+    if (n < 2 || n > MAXL) return CLM_ERR_ARG;
+  }
+  return CLM_OK;
+}
+
+static void set_threads(const clmo_problem* P) {
+#ifdef _OPENMP
+  if (P->nthreads > 0) omp_set_num_threads(P->nthreads);
+#else
+  (void)P;
+#endif
+}
+
+int clmo_update_cache(const clmo_problem* P, const double* v, const double* ti,
+                      const double* e, double t, double* K, double* psi,
+                      double* theta_l, double* T, double* kappa, double* Tf,
+                      double* bc, double* total_water, double* total_energy) {
+  int rc = check_problem(P);
+  if (rc) return rc;
+  set_threads(P);
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < P->ncol; ++c) {
+    col_t C;
+    col_init(&C, P, c);
+    state_t Y;
+    cache_t p;
+    memset(&p, 0, sizeof(p));
+    state_load(&C, &Y, v, ti, e, NULL, NULL);
+    update_cache(&C, &Y, &p, t);
+    int o = P->offsets[c];
+    for (int k = 0; k < C.n; ++k) {
+      if (K) K[o + k] = p.K[k];
+      if (psi) psi[o + k] = p.psi[k];
+      if (C.eh) {
+        if (theta_l) theta_l[o + k] = p.theta_l[k];
+        if (T) T[o + k] = p.T[k];
+        if (kappa) kappa[o + k] = p.kappa[k];
+        if (Tf) Tf[o + k] = p.Tf[k];
+      }
+    }
+    if (bc) {
+      bc[0 * P->ncol + c] = p.top_w;
+      bc[1 * P->ncol + c] = p.top_h;
+      bc[2 * P->ncol + c] = p.bot_w;
+      bc[3 * P->ncol + c] = p.bot_h;
+    }
+    if (total_water) total_water[c] = p.total_water;
+    if (total_energy) total_energy[c] = p.total_energy;
+  }
+  return CLM_OK;
+}
+
+int clmo_exp_tendency(const clmo_problem* P, const double* v, const double* ti,
+                      const double* e, double t, double* dv, double* dti,
+                      double* de, double* dFw, double* dFe) {
+  int rc = check_problem(P);
+  if (rc) return rc;
+  set_threads(P);
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < P->ncol; ++c) {
+    col_t C;
+    col_init(&C, P, c);
+    state_t Y, dY;
+    cache_t p;
+    memset(&p, 0, sizeof(p));
+    state_load(&C, &Y, v, ti, e, NULL, NULL);
+    update_cache(&C, &Y, &p, t);
+    exp_tendency(&C, &Y, &p, &dY);
+    state_store(&C, &dY, dv, dti, de, dFw, dFe);
+  }
+  return CLM_OK;
+}
+
+int clmo_imp_tendency(const clmo_problem* P, const double* v, const double* ti,
+                      const double* e, double t, double* dv, double* dti,
+                      double* de, double* dFw, double* dFe) {
+  int rc = check_problem(P);
+  if (rc) return rc;
+  set_threads(P);
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < P->ncol; ++c) {
+    col_t C;
+    col_init(&C, P, c);
+    state_t Y, dY;
+    cache_t p;
+    memset(&p, 0, sizeof(p));
+    state_load(&C, &Y, v, ti, e, NULL, NULL);
+    update_cache(&C, &Y, &p, t);
+    imp_tendency(&C, &Y, &p, &dY);
+    state_store(&C, &dY, dv, dti, de, dFw, dFe);
+  }
+  return CLM_OK;
+}
+
+int clmo_jacobian(const clmo_problem* P, const double* v, const double* ti,
+                  const double* e, double t, double dtgamma, double* W_vv,
+                  double* W_ev, double* W_ee) {
+  int rc = check_problem(P);
+  if (rc) return rc;
+  set_threads(P);
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < P->ncol; ++c) {
+    col_t C;
+    col_init(&C, P, c);
+    state_t Y;
+    cache_t p;
+    jac_t J;
+    memset(&p, 0, sizeof(p));
+    memset(&J, 0, sizeof(J));
+    state_load(&C, &Y, v, ti, e, NULL, NULL);
+    update_cache(&C, &Y, &p, t);
+    jacobian(&C, &Y, &p, dtgamma, &J);
+    int o = P->offsets[c];
+    for (int k = 0; k < C.n; ++k)
+      for (int j = 0; j < 3; ++j) {
+        if (W_vv) W_vv[3 * (o + k) + j] = J.vv[j][k];
+        if (C.eh && W_ev) W_ev[3 * (o + k) + j] = J.ev[j][k];
+        if (C.eh && W_ee) W_ee[3 * (o + k) + j] = J.ee[j][k];
+      }
+  }
+  return CLM_OK;
+}
+
+int clmo_solve(const clmo_problem* P, const double* W_vv, const double* W_ev,
+               const double* W_ee, const double* f_v, const double* f_e,
+               double* delta_v, double* delta_e) {
+  int rc = check_problem(P);
+  if (rc) return rc;
+  set_threads(P);
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < P->ncol; ++c) {
+    col_t C;
+    col_init(&C, P, c);
+    jac_t J;
+    state_t f, d;
+    memset(&J, 0, sizeof(J));
+    memset(&f, 0, sizeof(f));
+    int o = P->offsets[c];
+    for (int k = 0; k < C.n; ++k) {
+      for (int j = 0; j < 3; ++j) {
+        J.vv[j][k] = W_vv[3 * (o + k) + j];
+        if (C.eh) {
+          J.ev[j][k] = W_ev[3 * (o + k) + j];
+          J.ee[j][k] = W_ee[3 * (o + k) + j];
+        }
+      }
+      f.v[k] = f_v[o + k];
+      if (C.eh) f.e[k] = f_e[o + k];
+    }
+    block_solve(&C, &J, &f, &d);
+    for (int k = 0; k < C.n; ++k) {
+      delta_v[o + k] = d.v[k];
+      if (C.eh && delta_e) delta_e[o + k] = d.e[k];
+    }
+  }
+  return CLM_OK;
+}
+
+int clmo_step(const clmo_problem* P, double* v, double* ti, double* e,
+              double* Fw, double* Fe, double t, double dt, int32_t nsteps,
+              uint32_t* flags, int32_t* iters) {
+  int rc = check_problem(P);
+  if (rc) return rc;
+  if (!(dt > 0) || nsteps < 0 || P->cfg.max_iters < 1) return CLM_ERR_ARG;
+  set_threads(P);
+  int bad = 0;
+#pragma omp parallel for schedule(dynamic, 16) reduction(| : bad)
+  for (int c = 0; c < P->ncol; ++c) {
+    col_t C;
+    col_init(&C, P, c);
+    state_t Y;
+    state_load(&C, &Y, v, ti, e, Fw, Fe);
+    uint32_t fl = 0;
+    int32_t it = 0;
+    for (int s = 0; s < nsteps; ++s)
+      column_step(&C, &Y, t + s * dt, dt, &fl, &it);
+    state_store(&C, &Y, v, ti, e, Fw, Fe);
+    if (flags) flags[c] = fl;
+    if (iters) iters[c] = it;
+    if (fl & CLM_COL_NONFINITE) bad = 1;
+  }
+  return bad ? CLM_ERR_NAN : CLM_OK;
+}
+
+int clmo_budgets(const clmo_problem* P, const double* v, const double* ti,
+                 const double* e, double* total_water, double* total_energy) {
+  int rc = check_problem(P);
+  if (rc) return rc;
+  const clm_earth_params* ep = &P->cfg.earth;
+  int eh = P->cfg.model == CLM_MODEL_ENERGY_HYDROLOGY;
+  for (int c = 0; c < P->ncol; ++c) {
+    col_t C;
+    col_init(&C, P, c);
+    int o = P->offsets[c];
+    double W = 0.0, E = 0.0;
+    for (int k = 0; k < C.n; ++k) {
+      W += C.dzc[k] * (v[o + k] + (eh ? ti[o + k] * ep->rho_i / ep->rho_l : 0.0));
+      if (eh) E += C.dzc[k] * e[o + k];
+    }
+    if (total_water) total_water[c] = W;
+    if (total_energy) total_energy[c] = eh ? E : 0.0;
+  }
+  return CLM_OK;
+}

@@ -1,0 +1,492 @@
+"""Pins the oracle against the reference's own known-answer tests.
+
+Each test restates one reference test case (cited) with the same inputs and
+the same expected expressions, evaluated here in numpy, and checks the
+oracle's output with the reference's tolerance (Julia `≈`: rtol = sqrt(eps)
+unless the reference states otherwise). The reference loops FT over Float32
+and Float64; the oracle is Float64 only.
+"""
+import ctypes
+import math
+
+import numpy as np
+import pytest
+
+import oracle as O
+from climaland_gb300 import _abi as A
+from climaland_gb300 import parameters as PR
+from climaland_gb300 import workloads as WL
+
+RTOL = math.sqrt(np.finfo(np.float64).eps)
+EPS = np.finfo(np.float64).eps
+
+
+def approx(a, b, rtol=RTOL, atol=0.0):
+    return np.allclose(a, b, rtol=rtol, atol=atol)
+
+
+@pytest.fixture(scope="module")
+def L():
+    return O.lib()
+
+
+@pytest.fixture(scope="module")
+def earth():
+    return O.earth()
+
+
+E = A.DEFAULT_EARTH
+RHO_L, RHO_I = E["rho_l"], E["rho_i"]
+RHOCP_L = E["cp_l"] * RHO_L
+RHOCP_I = E["cp_i"] * RHO_I
+T_REF = E["T_0"]
+LH_F0 = E["LH_f0"]
+GRAV = E["grav"]
+T_FREEZE = E["T_freeze"]
+
+
+# --- test/standalone/Soil/soil_parameterizations.jl:10-188 ------------------
+
+def test_preset_and_derived_params():
+    # :70-101
+    nu, om, q, g = 0.2, 0.1, 0.1, 0.1
+    p = PR.EnergyHydrologyParameters.from_composition(
+        nu=nu, nu_ss_om=om, nu_ss_quartz=q, nu_ss_gravel=g,
+        hydrology_cm=PR.vanGenuchten(alpha=2.0, n=1.4), K_sat=1e-5, S_s=1e-3, theta_r=0.1)
+    assert (p.alpha, p.beta, p.gamma, p.Omega, p.gamma_T_ref) == (0.24, 18.3, 2.64e-2, 7.0, 288.0)
+    c = PR.LAND_SOIL_CONSTANTS
+    ks = PR.kappa_solid(om, q, 0.25, 8.0, 2.5)
+    rho_p = om * 1.3e3 + q * 2.66e3 + g * 2.65e3 + (1 - om - q - g) * 2.65e3
+    rho_c_ss = om * 2.51e6 + q * 2.01e6 + g * 2.01e6 + (1 - om - q - g) * 2.01e6
+    assert p.kappa_dry == PR.kappa_dry(rho_p, nu, ks, c["K_therm"])
+    assert p.kappa_sat_frozen == PR.kappa_sat_frozen(ks, nu, 2.21)
+    assert p.kappa_sat_unfrozen == PR.kappa_sat_unfrozen(ks, nu, 0.57)
+    assert p.rho_c_ds == (1 - nu) * rho_c_ss
+    hcm = PR.vanGenuchten(alpha=2.0, n=1.4)
+    assert hcm.m == 1.0 - 1.0 / 1.4
+    assert hcm.S_c == (1 + ((1.4 - 1) / 1.4) ** (1 - 2 * 1.4)) ** (-hcm.m)
+
+
+def test_heat_pointwise(L, earth):
+    e = ctypes.byref(earth)
+    # :104-109 (exact equality in the reference)
+    assert L.clmo_temperature_from_rho_e_int(5.4e7, 0.05, 2.1415e6, e) == \
+        T_REF + (5.4e7 + 0.05 * RHO_I * LH_F0) / 2.1415e6
+    rho_c_ds = (1 - 0.2) * (0.1 * 2.51e6 + 0.9 * 2.01e6)
+    # :111-116
+    assert approx(L.clmo_volumetric_heat_capacity(0.25, 0.05, rho_c_ds, e),
+                  rho_c_ds + 0.25 * RHOCP_L + 0.05 * RHOCP_I)
+    # :118-123
+    assert L.clmo_volumetric_internal_energy(0.05, 2.1415e6, 300.0, e) == \
+        2.1415e6 * (300.0 - T_REF) - 0.05 * RHO_I * LH_F0
+    # :125-128
+    assert approx(L.clmo_kappa_sat(0.25, 0.05, 0.57, 2.29),
+                  0.57 ** (0.25 / 0.3) * 2.29 ** (0.05 / 0.3))
+    assert L.clmo_kappa_sat(0.0, 0.0, 0.57, 2.29) == 0.5 * (0.57 + 2.29)
+    # :130-131
+    assert L.clmo_relative_saturation(0.25, 0.05, 0.4) == (0.25 + 0.05) / 0.4
+    # :133-148 ice fraction = 0
+    exp_ke = 0.75 ** ((1 + 0.1 - 0.24 * 0.1 - 0.1) / 2) * (
+        (1 + math.exp(-18.3 * 0.75)) ** (-3) - ((1 - 0.75) / 2) ** 3) ** (1 - 0.1)
+    assert approx(L.clmo_kersten_number(0.0, 0.75, 0.24, 18.3, 0.1, 0.1, 0.1), exp_ke)
+    # :150-159 ice fraction > 0
+    assert L.clmo_kersten_number(0.05, 0.75, 0.24, 18.3, 0.1, 0.1, 0.1) == 0.75 ** 1.1
+    # :161-162
+    assert L.clmo_thermal_conductivity(1.5, 0.7287, 0.7187) == 0.7287 * 0.7187 + (1 - 0.7287) * 1.5
+    # :164-165
+    assert L.clmo_volumetric_internal_energy_liq(300.0, e) == RHOCP_L * (300.0 - T_REF)
+    # :167-179
+    assert approx(L.clmo_kappa_solid(0.5, 0.25, 2.0, 3.0, 2.0), 2 ** 0.5 * 2 ** 0.25 * 3.0 ** 0.25)
+    assert L.clmo_kappa_sat_frozen(0.5, 0.1, 0.4) == 0.5 ** 0.9 * 0.4 ** 0.1
+    assert L.clmo_kappa_sat_unfrozen(0.5, 0.1, 0.4) == 0.5 ** 0.9 * 0.4 ** 0.1
+    ks = PR.kappa_solid(0.1, 0.1, 0.25, 8.0, 2.5)
+    rho_p = 0.1 * 1.3e3 + 0.1 * 2.66e3 + 0.1 * 2.65e3 + 0.7 * 2.65e3
+    rho_b = (1 - 0.2) * rho_p
+    ka = 0.024
+    assert approx(L.clmo_kappa_dry(rho_p, 0.2, ks, ka),
+                  ((0.053 * ks - ka) * rho_b + ka * rho_p) / (rho_p - (1 - 0.053) * rho_b), rtol=1e-15)
+    # :180-186
+    assert approx(L.clmo_impedance_factor(1.0, 7.0), 1e-7)
+    for T in (278.0, 288.0, 298.0):
+        assert approx(L.clmo_viscosity_factor(T, 2.64e-2, 288.0), math.exp(2.64e-2 * (T - 288.0)))
+
+
+# --- :225-281 van Genuchten closures ----------------------------------------
+
+def test_van_genuchten(L):
+    theta_r, nu, S_s, a, n = 0.2, 0.4, 1e-2, 3.6, 1.56
+    m = 1.0 - 1.0 / n
+    K_sat = 2.9e-7
+    th = [0.3, 0.4, 0.5]
+    S = [L.clmo_effective_saturation(nu, t, theta_r) for t in th]
+    assert approx(S, [0.5, 1.0, 1.5])
+    va = -((S[0] ** (-1 / m) - 1) * a ** (-n)) ** (1 / n)
+    psi = [L.clmo_matric_potential(a, n, m, s) for s in S[:2]]
+    flag = ctypes.c_int(0)
+    inv = [L.clmo_inverse_matric_potential(a, n, m, p, ctypes.byref(flag)) for p in psi]
+    assert approx(inv, S[:2])
+    assert approx(psi, [va, 0.0], atol=0)
+    dpsi = [L.clmo_dpsidvartheta(a, n, m, t, nu, theta_r, S_s) for t in th]
+    va = 1.0 / (a * m * n) / (nu - theta_r) * (S[0] ** (-1 / m) - 1) ** (1 / n - 1) * S[0] ** (-1 / m - 1)
+    assert approx(dpsi, [va, 1 / S_s, 1 / S_s])
+    ph = [L.clmo_pressure_head(a, n, m, theta_r, t, nu, S_s) for t in th]
+    assert approx(ph, psi + [10.0])
+    k = [L.clmo_hydraulic_conductivity(m, K_sat, s) for s in S]
+    va = (math.sqrt(S[0]) * (1 - (1 - S[0] ** (1 / m)) ** m) ** 2) * K_sat
+    assert approx(k, [va, K_sat, K_sat])
+    vlf = [L.clmo_volumetric_liquid_fraction(t, 0.5, 0.0) for t in (0.25, 0.5, 0.75)]
+    assert approx(vlf, [0.25, 0.5, 0.5])
+    # inverse_matric_potential raises for psi > 0 (:73): reported as a flag
+    flag = ctypes.c_int(0)
+    L.clmo_inverse_matric_potential(a, n, m, 0.1, ctypes.byref(flag))
+    assert flag.value == 1
+
+
+# --- :283-495 freezing and thawing -----------------------------------------
+
+def _ft_case(L, earth, theta_l, theta_i, T):
+    nu, S_s, theta_r, a, n = 0.2, 1e-3, 0.1, 2.0, 1.4
+    m = 1 - 1 / n
+    p = PR.EnergyHydrologyParameters.from_composition(
+        nu=nu, nu_ss_om=0.1, nu_ss_quartz=0.1, nu_ss_gravel=0.1,
+        hydrology_cm=PR.vanGenuchten(alpha=a, n=n), K_sat=1e-5, S_s=S_s, theta_r=theta_r)
+    dz = 1.0
+    e = ctypes.byref(earth)
+    tau0 = L.clmo_thermal_time(p.rho_c_ds, dz, p.kappa_dry)
+    assert tau0 == 3 * p.rho_c_ds * dz ** 2 / p.kappa_dry
+    out, exp = [], []
+    for tl in np.atleast_1d(theta_l):
+        for ti in np.atleast_1d(theta_i):
+            th_tot = RHO_I / RHO_L * ti + tl
+            S = L.clmo_effective_saturation(nu, th_tot, theta_r)
+            psi0 = L.clmo_matric_potential(a, n, m, S)
+            Tf = T_FREEZE * math.exp(GRAV * psi0 / LH_F0)
+            psiT = LH_F0 / GRAV * math.log(T / Tf) * L.clmo_heaviside(Tf - T, 0.0)
+            flag = ctypes.c_int(0)
+            th_star = L.clmo_inverse_matric_potential(a, n, m, psi0 + psiT, ctypes.byref(flag)) * (nu - theta_r) + theta_r
+            rhoc = L.clmo_volumetric_heat_capacity(tl, ti, p.rho_c_ds, e)
+            tau = L.clmo_thermal_time(rhoc, dz, p.kappa_dry)
+            src = L.clmo_phase_change_source(tl, ti, T, tau, nu, theta_r, a, n, m, RHO_I, RHO_L,
+                                             LH_F0, T_FREEZE, GRAV, ctypes.byref(flag))
+            out.append(src)
+            exp.append((tl - th_star) / tau)
+    return np.array(out), np.array(exp)
+
+
+def test_freeze_thaw(L, earth):
+    # :326-364 : theta_i = 0, T = 270 -> all three freeze
+    src, exp = _ft_case(L, earth, [0.11, 0.15, 0.2], 0.0, 270.0)
+    assert approx(src, exp)
+    assert (src > 0).sum() == 3
+    # :366-404 : T = 274 -> no phase change, theta_star == theta_l
+    src, exp = _ft_case(L, earth, [0.11, 0.15, 0.2], 0.0, 274.0)
+    assert np.allclose(src, 0.0, atol=1e-30)
+    # :407-449 : ice present, T = 274 -> melts
+    src, exp = _ft_case(L, earth, 0.11, [0.05, 0.08], 274.0)
+    assert approx(src, exp)
+    assert (src < 0).sum() == 2
+    # :452-494 : ice present, T = 260 -> freezes
+    src, exp = _ft_case(L, earth, 0.11, [0.05, 0.08], 260.0)
+    assert approx(src, exp)
+    assert (src > 0).sum() == 2
+
+
+def test_heaviside_strict_eps(L):
+    # utils.jl:95-101 : strict `> eps(FT)`
+    assert L.clmo_heaviside(EPS, 0.0) == 0.0
+    assert L.clmo_heaviside(2 * EPS, 0.0) == 1.0
+    assert L.clmo_heaviside(0.0, 0.0) == 0.0
+
+
+# --- test/shared_utilities/implicit_timestepping/richards_model.jl ----------
+
+NU, KSAT, SS, VGN, VGA, THR = 0.495, 0.0443 / 3600 / 100, 1e-3, 1.43, 2.6, 0.124
+
+
+def _richards_column(top_state: bool, nelems=150):
+    cfg = A.default_config()
+    cfg.model = A.CLM_MODEL_RICHARDS
+    cfg.phase_change = 0
+    cfg.bc_bottom_water = A.CLM_BC_FREE_DRAINAGE
+    cfg.bc_top_water = A.CLM_BC_STATE if top_state else A.CLM_BC_FLUX
+    rp = PR.RichardsParameters(nu=NU, hydrology_cm=PR.vanGenuchten(VGA, VGN), K_sat=KSAT,
+                               S_s=SS, theta_r=THR)
+    f = WL.constant_forcing(1, NU - 1e-3 if top_state else -KSAT)
+    return WL.make_workload("jac", cfg, z_lo=-1.5, z_hi=0.0, nlayers=nelems,
+                            params=rp.soa(1), forcing={A.CLM_BC_TOP_WATER: f},
+                            vartheta_l=0.24)
+
+
+@pytest.mark.parametrize("top_state", [True, False])
+def test_richards_jacobian_entries(L, top_state):
+    # richards_model.jl:16-145 (MoistureStateBC) and :147-227 (WaterFluxBC)
+    w = _richards_column(top_state)
+    o = O.Oracle(w)
+    dtg = 1.0
+    Wvv, _, _ = o.jacobian(w.copy_state(), 0.0, dtg)
+    m = 1 - 1 / VGN
+    S = L.clmo_effective_saturation(NU, 0.24, THR)
+    K = L.clmo_hydraulic_conductivity(m, KSAT, S)
+    dpsi = L.clmo_dpsidvartheta(VGA, VGN, m, 0.24, NU, THR, SS)
+    dz = 0.01
+    lo, d, up = Wvv[:, 0], Wvv[:, 1], Wvv[:, 2]
+    assert np.allclose(lo[1:], up[:-1], rtol=RTOL)
+    assert lo[0] == 0.0 and up[-1] == 0.0
+    assert approx(lo[1:], dtg * (K / dz ** 2 * dpsi))
+    assert approx(d[0], dtg * (-K / dz ** 2 * dpsi) - 1)
+    assert approx(d[1:-1], dtg * (-2 * K / dz ** 2 * dpsi) - 1)
+    if top_state:
+        assert approx(d[-1], dtg * (-K / dz ** 2 * dpsi - K / (dz * dz / 2) * dpsi) - 1)
+    else:
+        assert approx(d[-1], dtg * (-K / dz ** 2 * dpsi) - 1)
+
+
+def _eh_column(nelems=150, phase_change=False):
+    cfg = A.default_config()
+    cfg.model = A.CLM_MODEL_ENERGY_HYDROLOGY
+    cfg.phase_change = int(phase_change)
+    for s in ("bc_top_water", "bc_top_heat", "bc_bottom_water", "bc_bottom_heat"):
+        setattr(cfg, s, A.CLM_BC_FLUX)
+    p = PR.EnergyHydrologyParameters.from_composition(
+        nu=NU, nu_ss_om=0.0, nu_ss_quartz=1.0, nu_ss_gravel=0.0,
+        hydrology_cm=PR.vanGenuchten(VGA, VGN), K_sat=KSAT, S_s=SS, theta_r=THR)
+    T = 280.0
+    rhoc = p.rho_c_ds + 0.24 * RHOCP_L
+    rho_e = rhoc * (T - T_REF)
+    w = WL.make_workload("jac_eh", cfg, z_lo=-1.5, z_hi=0.0, nlayers=nelems, params=p.soa(1),
+                         vartheta_l=0.24, theta_i=0.0, rho_e_int=rho_e)
+    return w, p
+
+
+def test_energy_hydrology_jacobian_entries(L, earth):
+    # energy_hydrology_model.jl:16-172 (flux BCs, zero fluxes)
+    w, p = _eh_column()
+    o = O.Oracle(w)
+    dtg = 1.0
+    Wvv, Wev, Wee = o.jacobian(w.copy_state(), 0.0, dtg)
+    m = 1 - 1 / VGN
+    e = ctypes.byref(earth)
+    K = (L.clmo_impedance_factor(0.0 / (0.24 + 0.0 - THR), 7.0)
+         * L.clmo_viscosity_factor(280.0, 2.64e-2, 288.0)
+         * L.clmo_hydraulic_conductivity(m, KSAT, L.clmo_effective_saturation(NU, 0.24, THR)))
+    dz = 0.01
+    dpsi = L.clmo_dpsidvartheta(VGA, VGN, m, 0.24, NU, THR, SS)
+    d = Wvv[:, 1]
+    assert approx(d[0], dtg * (-K / dz ** 2 * dpsi) - 1)
+    assert approx(d[1:-1], dtg * (-2 * K / dz ** 2 * dpsi) - 1)
+    assert approx(d[-1], dtg * (-K / dz ** 2 * dpsi) - 1)
+    kap = L.clmo_thermal_conductivity(
+        p.kappa_dry, L.clmo_kersten_number(0.0, L.clmo_relative_saturation(0.24, 0.0, NU),
+                                           0.24, 18.3, 0.0, 1.0, 0.0),
+        L.clmo_kappa_sat(0.24, 0.0, p.kappa_sat_unfrozen, p.kappa_sat_frozen))
+    dTdrho = 1.0 / L.clmo_volumetric_heat_capacity(0.24, 0.0, p.rho_c_ds, e)
+    d = Wee[:, 1]
+    assert approx(d[0], dtg * (-kap / dz ** 2 * dTdrho) - 1)
+    assert approx(d[1:-1], dtg * (-2 * kap / dz ** 2 * dTdrho) - 1)
+    assert approx(d[-1], dtg * (-kap / dz ** 2 * dTdrho) - 1)
+    # the "- I" on the off-diagonal block d(rho e)/d(vartheta) (:151-171)
+    rel = L.clmo_volumetric_internal_energy_liq(280.0, e)
+    d = Wev[:, 1]
+    assert approx(d[0], dtg * (-rel * K / dz ** 2 * dpsi) - 1)
+    assert approx(d[1:-1], dtg * (-2 * rel * K / dz ** 2 * dpsi) - 1)
+    assert approx(d[-1], dtg * (-rel * K / dz ** 2 * dpsi) - 1)
+
+
+# --- test/standalone/Soil/soiltest.jl ----------------------------------------
+
+def test_richards_hydrostatic_equilibrium(L):
+    # soiltest.jl:15-90: hydrostatic profile -> zero tendency, psi + z = -10
+    nu, ksat, ss, n, a, thr = 0.495, 0.0443 / 3600 / 100, 1e-3, 2.0, 2.6, 0.0
+    m = 1 - 1 / n
+    cfg = A.default_config()
+    cfg.model = A.CLM_MODEL_RICHARDS
+    cfg.bc_top_water = cfg.bc_bottom_water = A.CLM_BC_FLUX
+    rp = PR.RichardsParameters(nu=nu, hydrology_cm=PR.vanGenuchten(a, n), K_sat=ksat, S_s=ss, theta_r=thr)
+    nel = 50
+    zf = np.linspace(-10.0, 0.0, nel + 1)
+    z = 0.5 * (zf[1:] + zf[:-1])
+    S = (1 + (a * (z + 10.0)) ** n) ** (-m)
+    v = S * (nu - thr) + thr
+    w = WL.make_workload("hydrostatic", cfg, z_lo=-10.0, z_hi=0.0, nlayers=nel,
+                         params=rp.soa(1), vartheta_l=v)
+    o = O.Oracle(w)
+    st = w.copy_state()
+    de = o.exp_tendency(st, 0.0)
+    di = o.imp_tendency(st, 0.0)
+    assert np.mean(de[0] + di[0]) < EPS
+    c = o.update_cache(st, 0.0)
+    assert np.mean(c["psi"] + z + 10.0) < 2 * EPS
+
+
+def _eh_tendency_setup(ksat, kappa_zero):
+    nu, ss, n, a, thr = 0.495, 1e-3, 2.0, 2.6, 0.1
+    cfg = A.default_config()
+    cfg.model = A.CLM_MODEL_ENERGY_HYDROLOGY
+    cfg.phase_change = 0
+    for s in ("bc_top_water", "bc_top_heat", "bc_bottom_water", "bc_bottom_heat"):
+        setattr(cfg, s, A.CLM_BC_FLUX)
+    p = PR.EnergyHydrologyParameters.from_composition(
+        nu=nu, nu_ss_om=0.0, nu_ss_quartz=1.0, nu_ss_gravel=0.0,
+        hydrology_cm=PR.vanGenuchten(a, n), K_sat=ksat, S_s=ss, theta_r=thr)
+    p.rho_c_ds = 2e6 * (1.0 - nu)
+    if kappa_zero:
+        p.kappa_dry = p.kappa_sat_frozen = p.kappa_sat_unfrozen = 0.0
+    return cfg, p
+
+
+def test_eh_heat_only_tendency(L):
+    # soiltest.jl:133-199: K_sat = 0, T = 280 + 0.5 (z + 0.5)^2
+    cfg, p = _eh_tendency_setup(0.0, False)
+    nel = 200
+    zf = np.linspace(-1.0, 0.0, nel + 1)
+    z = 0.5 * (zf[1:] + zf[:-1])
+    dz = 1.0 / nel
+    v = p.nu / 2.0
+    T = 280.0 + 0.5 * (z + 0.5) ** 2
+    rhoc = p.rho_c_ds + v * RHOCP_L
+    rho_e = rhoc * (T - T_REF)
+    w = WL.make_workload("heat", cfg, z_lo=-1.0, z_hi=0.0, nlayers=nel, params=p.soa(1),
+                         vartheta_l=v, theta_i=0.0, rho_e_int=rho_e)
+    o = O.Oracle(w)
+    st = w.copy_state()
+    c = o.update_cache(st, 0.0)
+    kap = c["kappa"]
+    di = o.imp_tendency(st, 0.0)
+    F_face = 0.0
+    F_below = -0.5 * (kap[-1] + kap[-2]) * (-dz + 0.5)
+    dY_top = -(F_face - F_below) / dz
+    F_top = -0.5 * (kap[1] + kap[0]) * ((-1.0 + dz) + 0.5)
+    dY_bot = -(F_top - F_face) / dz
+    expected = kap.copy()
+    expected[0] = dY_bot
+    expected[-1] = dY_top
+    assert np.mean(np.abs(expected - di[2])) / np.median(rho_e) < EPS
+    assert np.max(np.abs(di[0])) == 0.0
+    assert np.max(np.abs(di[1])) == 0.0
+    de = o.exp_tendency(st, 0.0)
+    assert max(np.max(np.abs(x)) for x in de[:3]) == 0.0
+
+
+def test_eh_water_only_tendency(L, earth):
+    # soiltest.jl:200-341: kappa = 0, vartheta = nu/2 + nu/4 (z + 0.5)^2, T = 288
+    ksat = 0.0443 / 3600 / 100
+    cfg, p = _eh_tendency_setup(ksat, True)
+    nu, thr, n, a, ss = p.nu, p.theta_r, 2.0, 2.6, 1e-3
+    m = 1 - 1 / n
+    nel = 200
+    zf = np.linspace(-1.0, 0.0, nel + 1)
+    Z = 0.5 * (zf[1:] + zf[:-1])
+    dz = 1.0 / nel
+    th = nu / 2.0 + nu / 4.0 * (Z + 0.5) ** 2
+    rhoc = p.rho_c_ds + th * RHOCP_L
+    rho_e = rhoc * (288.0 - T_REF)
+    w = WL.make_workload("water", cfg, z_lo=-1.0, z_hi=0.0, nlayers=nel, params=p.soa(1),
+                         vartheta_l=th, theta_i=0.0, rho_e_int=rho_e)
+    o = O.Oracle(w)
+    st = w.copy_state()
+    de = o.exp_tendency(st, 0.0)
+    assert max(np.max(np.abs(x)) for x in de[:3]) == 0.0
+    di = o.imp_tendency(st, 0.0)
+    assert np.max(np.abs(di[1])) == 0.0
+
+    def Kf(t):
+        S = (t - thr) / (nu - thr)
+        f = 1.0 - (1.0 - S ** (1.0 / m)) ** m
+        return np.where(S < 1, ksat * f ** 2 * np.sqrt(S), ksat)
+
+    def dpsi(t):
+        S = (t - thr) / (nu - thr)
+        return 1.0 / (a * m * n) / (nu - thr) * (S ** (-1 / m) - 1) ** (1 / n - 1) * S ** (-1 / m - 1)
+
+    def dthdz(z):
+        return nu / 2.0 * (z + 0.5)
+
+    th_face = 0.5 * (th[1:] + th[:-1])
+    Z_face = 0.5 * (Z[1:] + Z[:-1])
+    K_face = 0.5 * (Kf(th[1:]) + Kf(th[:-1]))
+    flux = np.concatenate([[0.0], -K_face * (1.0 + dpsi(th_face) * dthdz(Z_face)), [0.0]])
+    expected = -(flux[1:] - flux[:-1]) / dz
+    # soiltest.jl:334-336 bound: 10^2 eps(FT)
+    assert np.mean(np.abs(expected - di[0])) / nu < 1e2 * EPS
+    c = o.update_cache(st, 0.0)
+    rel = RHOCP_L * (c["T"] - T_REF)
+    rel_face = 0.5 * (rel[1:] + rel[:-1])
+    flux_e = np.concatenate([[0.0], -K_face * rel_face * (1.0 + dpsi(th_face) * dthdz(Z_face)), [0.0]])
+    expected_e = -(flux_e[1:] - flux_e[:-1]) / dz
+    # soiltest.jl:303-304 bound: 10^2 eps(FT)
+    assert np.mean(np.abs(expected_e - di[2])) / np.median(rho_e) < 1e2 * EPS
+
+
+# --- test/standalone/Soil/soil_bc.jl:195-266 ---------------------------------
+
+def test_energy_water_free_drainage(L, earth):
+    nu, ksat, ss, n, a, thr = 0.495, 0.0443 / 3600 / 100, 1e-3, 2.0, 2.6, 0.1
+    cfg = A.default_config()
+    cfg.model = A.CLM_MODEL_ENERGY_HYDROLOGY
+    cfg.bc_top_water = cfg.bc_top_heat = A.CLM_BC_FLUX
+    cfg.bc_bottom_water = cfg.bc_bottom_heat = A.CLM_BC_FREE_DRAINAGE
+    p = PR.EnergyHydrologyParameters.from_composition(
+        nu=nu, nu_ss_om=0.0, nu_ss_quartz=1.0, nu_ss_gravel=0.0,
+        hydrology_cm=PR.vanGenuchten(a, n), K_sat=ksat, S_s=ss, theta_r=thr)
+    nel = 20
+    zf = np.linspace(-1.0, 0.0, nel + 1)
+    z = 0.5 * (zf[1:] + zf[:-1])
+    T = z * 10 + 290.0
+    rhoc = p.rho_c_ds + nu / 2 * RHOCP_L
+    w = WL.make_workload("fd", cfg, z_lo=-1.0, z_hi=0.0, nlayers=nel, params=p.soa(1),
+                         vartheta_l=nu / 2, theta_i=0.0, rho_e_int=rhoc * (T - T_REF))
+    c = O.Oracle(w).update_cache(w.copy_state(), 0.0)
+    fw = -1.0 * c["K"][0]
+    fe = fw * RHOCP_L * (c["T"][0] - T_REF)
+    assert approx(c["bc"][A.CLM_BC_BOTTOM_HEAT, 0], fe)
+    assert approx(c["bc"][A.CLM_BC_BOTTOM_WATER, 0], fw)
+
+
+# --- test/standalone/Soil/conservation.jl -----------------------------------
+
+def test_conservation_identities(L, earth):
+    """conservation.jl:222-258 identities without the FakeSource: the explicit
+    phase-change tendency conserves water (column integral of
+    dvartheta + rho_i/rho_l dtheta_i is zero) and leaves energy unchanged,
+    and the implicit tendencies integrate to -(F_top - F_bot)."""
+    w = WL.energy_hydrology_c1(ncol=64)
+    o = O.Oracle(w)
+    st = w.copy_state()
+    de = o.exp_tendency(st, 0.0)
+    dz = np.repeat((w.z_hi - w.z_lo) / w.nlayers, w.nlayers)
+    col = np.repeat(np.arange(w.ncol), w.nlayers)
+    water = np.bincount(col, dz * (de[0] + RHO_I / RHO_L * de[1]))
+    scale = np.bincount(col, dz * np.abs(de[0]))
+    assert np.all(np.abs(water) <= 10 * EPS * np.maximum(scale, 1e-300) + 1e-300)
+    assert np.all(de[2] == 0.0)
+    di = o.imp_tendency(st, 0.0)
+    c = o.update_cache(st, 0.0)
+    bc = c["bc"]
+    iw = np.bincount(col, dz * di[0])
+    ie = np.bincount(col, dz * di[2])
+    assert np.allclose(iw, -(bc[0] - bc[2]), rtol=1e-10, atol=1e-22)
+    assert np.allclose(ie, -(bc[1] - bc[3]), rtol=1e-10, atol=1e-9)
+    assert np.array_equal(di[3], -(bc[0] - bc[2]))
+    assert np.array_equal(di[4], -(bc[1] - bc[3]))
+
+
+def test_step_budgets_close():
+    """Budget closure after N steps: |dW - intF_w| / W and |dE - intF_e| / |E|
+    at 1e-12 (water closes every Newton iteration; energy from iteration 2 on)."""
+    for w in (WL.richards_c0(ncol=64), WL.energy_hydrology_c1(ncol=64)):
+        o = O.Oracle(w)
+        st = w.copy_state()
+        W0, E0 = o.budgets(st)
+        rc, flags, iters = o.step(st, w.t0, w.dt, 24)
+        assert rc == 0 and flags.max() == 0
+        W1, E1 = o.budgets(st)
+        assert np.max(np.abs((W1 - W0) - st[3]) / W0) < 1e-12
+        if w.cfg.model == A.CLM_MODEL_ENERGY_HYDROLOGY:
+            assert np.max(np.abs((E1 - E0) - st[4]) / np.abs(E0)) < 1e-12
+
+
+def test_forcing_hash_deterministic(L):
+    vals = [L.clm_forcing_hash01(7, c, k) for c in range(50) for k in range(20)]
+    assert all(0.0 <= v < 1.0 for v in vals)
+    assert abs(np.mean(vals) - 0.5) < 0.05
+    assert L.clm_forcing_hash01(7, 3, 5) == L.clm_forcing_hash01(7, 3, 5)
