@@ -1,0 +1,360 @@
+"""Benchmark of the fused soil column step on GB300.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                [--config c4] [--precision fp64|mixed] [--ncol NCOL]
+
+Workload (default): the full-scale EnergyHydrology configuration,
+1,048,576 columns x 20 layers (depth 1-5 m, diurnal heat flux, rain pulses,
+advective heat), seeded synthetic inputs. A step is one IMEX ARS111 step of
+every column (explicit stage, 3 Newton iterations, block Thomas solves),
+launched as one kernel that reads and writes the whole state in HBM
+(503 MB of state, larger than L2, so no flush is needed between steps).
+
+Prints one JSON line (rank 0). Metric: column-steps/s.
+  value     device-timed throughput, state resident in HBM (CUDA events on
+            the library's stream, max over ranks)
+  e2e       the same through the C ABI with host buffers: per step the
+            state is copied from pinned host memory, stepped, and copied back
+  roofline  dominant kernel (the step kernel) against the measured HBM peak
+  cpu_baseline  the FP64 CPU oracle on a bounded sample, all host threads
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO / "climaland.jl_gb300"))
+
+import numpy as np  # noqa: E402
+
+
+def algorithmic_bytes_per_column_step(model: int, nlayers: float) -> float:
+    """Unavoidable HBM traffic of one column-step with the state read and
+    written once. EnergyHydrology: 3 state arrays in + out (48 n) + intF_w,
+    intF_e in + out (32) + 13 parameters (104) + forcing (16) + geometry (16)
+    = 48 n + 168 bytes. Richards: 16 n + 16 + 48 + 8 + 8 = 16 n + 80."""
+    if model == 1:
+        return 48.0 * nlayers + 168.0
+    return 16.0 * nlayers + 80.0
+
+
+class ClockSampler:
+    """Samples SM clock and throttle reasons with nvidia-smi during a region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev_id: str | None):
+        self.dev_id = dev_id
+        self.proc = None
+        self.lines: list[str] = []
+        self._t = None
+
+    def __enter__(self):
+        cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"]
+        if self.dev_id:
+            cmd += ["-i", self.dev_id]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self._t:
+                self._t.join(timeout=2)
+
+    def summary(self) -> dict:
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d.get("hbm_gbs"), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def profile_traffic(kernel_key: str) -> dict | None:
+    """DRAM bytes per launch of the step kernel from the committed ncu
+    summary (profiles/<kernel_key>.json), if present."""
+    p = REPO / "profiles" / f"{kernel_key}.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return None
+
+
+def make_workload(name: str, ncol: int | None, rank: int):
+    from climaland_gb300 import workloads as WL
+
+    gen = WL.CONFIGS[name]
+    kw = {"seed": rank}
+    if ncol:
+        kw["ncol"] = ncol
+    return gen(**kw)
+
+
+def cpu_baseline(w, sample_cols: int, sample_steps: int) -> dict:
+    """The FP64 oracle (C, OpenMP) on a bounded sample of the workload."""
+    sys.path.insert(0, str(REPO / "oracle"))
+    import oracle as O
+
+    sub = w.subset(sample_cols)
+    threads = os.cpu_count() or 1
+    o = O.Oracle(sub, nthreads=threads)
+    st = sub.copy_state()
+    o.step(st, sub.t0, sub.dt, 1)  # warm-up (thread pool, page faults)
+    st = sub.copy_state()
+    t0 = time.perf_counter()
+    rc, _, _ = o.step(st, sub.t0, sub.dt, sample_steps)
+    el = time.perf_counter() - t0
+    return {"value": sub.ncol * sample_steps / el, "unit": "column-steps/s", "cores": threads,
+            "kind": "port",
+            "sample": f"{sub.ncol} of {w.ncol} columns x {sample_steps} steps, FP64 oracle "
+                      f"(C/OpenMP restatement; the Julia reference does not run here)",
+            "seconds": el}
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the reference's CPU path (the oracle port; Julia is
+    absent) on the host cores, same config and metric."""
+    if rank != 0:
+        return
+    w = make_workload(args.config, args.ncol, 0)
+    sys.path.insert(0, str(REPO / "oracle"))
+    import oracle as O
+
+    sample = min(w.ncol, args.ref_sample_cols)
+    sub = w.subset(sample)
+    threads = os.cpu_count() or 1
+    o = O.Oracle(sub, nthreads=threads)
+    st = sub.copy_state()
+    t = sub.t0
+    for _ in range(args.warmup):
+        o.step(st, t, sub.dt, 1)
+        t += sub.dt
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.step(st, t, sub.dt, 1)
+        t += sub.dt
+    el = time.perf_counter() - t0
+    value = sub.ncol * args.steps / el
+    line = {
+        "impl": "reference", "metric": "column-steps/s", "value": value, "unit": "column-steps/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": w.name, "columns_timed": sub.ncol, "layers": int(w.nlayers.max())},
+        "cpu_baseline": {"value": value, "unit": "column-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{sub.ncol} of {w.ncol} columns per step"},
+        "e2e": {"value": value, "unit": "column-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c4")
+    ap.add_argument("--ncol", type=int, default=None)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--cpu-sample-cols", type=int, default=16384)
+    ap.add_argument("--cpu-sample-steps", type=int, default=24)
+    ap.add_argument("--ref-sample-cols", type=int, default=32768)
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local_rank)
+
+    import __graft_entry__ as G
+
+    G.build()
+    from climaland_gb300 import _abi as A
+    from climaland_gb300 import device as D
+
+    w = make_workload(args.config, args.ncol, rank)
+    prec = A.CLM_PREC_MIXED if args.precision == "mixed" else A.CLM_PREC_FP64
+    nl = float(w.nlayers.mean())
+    g = D.SoilColumns(w, precision=prec)
+    stream = torch.cuda.Stream()
+    g.set_stream(stream.cuda_stream)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    # warm-up
+    t = w.t0
+    for _ in range(args.warmup):
+        g.step_async(t, w.dt, 1)
+        t += w.dt
+    stream.synchronize()
+
+    try:
+        uuid = str(torch.cuda.get_device_properties(local_rank).uuid)
+        dev_id = uuid if uuid.startswith("GPU-") else f"GPU-{uuid}"
+    except Exception:
+        dev_id = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0] or None
+
+    # ---- device-timed region: state resident in HBM ----------------------
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev_id) as clk:
+        ev[0].record(stream)
+        for i in range(args.steps):
+            g.step_async(t, w.dt, 1)
+            t += w.dt
+            ev[i + 1].record(stream)
+        stream.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    per_launch_ms = [ev[i].elapsed_time(ev[i + 1]) for i in range(args.steps)]
+    total_ms = ev[0].elapsed_time(ev[-1])
+    if dist is not None:
+        tt = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    value = w.ncol * world * args.steps / (total_ms / 1e3)
+    flags, iters = g.status()
+
+    # ---- end to end through the C ABI with host buffers ------------------
+    e2e_steps = args.e2e_steps or max(3, min(args.steps, 10))
+    pinned = []
+    for a in w.copy_state():
+        if a is None:
+            pinned.append(None)
+            continue
+        p = torch.empty(a.shape, dtype=torch.float64, pin_memory=True).numpy()
+        p[:] = a
+        pinned.append(p)
+    outs = [None if a is None else torch.empty(a.shape, dtype=torch.float64, pin_memory=True).numpy()
+            for a in pinned]
+    h2d = sum(a.nbytes for a in pinned if a is not None)
+    barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(e2e_steps):
+        g.set_state(*pinned)
+        g.step(t, w.dt, 1)
+        t += w.dt
+        g.get_state(out=outs)
+    e1.record(stream)
+    stream.synchronize()
+    wall_e2e_ms = e0.elapsed_time(e1)
+    if dist is not None:
+        tt = torch.tensor([wall_e2e_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        wall_e2e_ms = float(tt.item())
+    e2e = w.ncol * world * e2e_steps / (wall_e2e_ms / 1e3)
+
+    if rank != 0:
+        g.close()
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    peaks = measured_peaks()
+    bytes_per_launch = algorithmic_bytes_per_column_step(w.cfg.model, nl) * w.ncol
+    avg_launch_s = statistics.mean(per_launch_ms) / 1e3
+    achieved = bytes_per_launch / avg_launch_s / 1e9
+    key = f"{'eh' if w.cfg.model == 1 else 'richards'}_step_{args.precision}"
+    prof = profile_traffic(key)
+    traffic = None
+    if prof and prof.get("dram_bytes_per_column_step"):
+        traffic = prof["dram_bytes_per_column_step"] * w.ncol
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
+                "peak_source": peaks["source"], "kernel": key,
+                "bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_s * 1e3}
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_baseline(w, args.cpu_sample_cols, args.cpu_sample_steps)
+    line = {
+        "metric": "column-steps/s", "value": value, "unit": "column-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if prec == A.CLM_PREC_FP64 else "f64+f32",
+        "data": "synthetic",
+        "config": {"workload": w.name, "columns_per_gpu": w.ncol, "layers": int(w.nlayers.max()),
+                   "model": "EnergyHydrology" if w.cfg.model == 1 else "RichardsModel",
+                   "newton": f"fixed {w.cfg.max_iters} iterations", "precision": args.precision,
+                   "l2": "inputs larger than L2 (state 48 B x cells)", "dt_s": w.dt},
+        "e2e": {"value": e2e, "unit": "column-steps/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": h2d, "steps": e2e_steps},
+        "gpu_launches": args.steps,
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+        "status": {"flagged_columns": int(np.count_nonzero(flags)),
+                   "newton_iters_max": int(iters.max())},
+    }
+    print(json.dumps(line), flush=True)
+    g.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -213,6 +213,7 @@ SIGNATURES = [
     ("clm_step", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_double, ctypes.c_int32]),
     ("clm_step_async", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_double, ctypes.c_int32]),
     ("clm_sync", ctypes.c_int, [_H]),
+    ("clm_set_stream", ctypes.c_int, [_H, ctypes.c_void_p]),
     ("clm_get_budgets", ctypes.c_int, [_H, _DP, _DP]),
     ("clm_get_status", ctypes.c_int, [_H, _UP, _IP]),
     ("clm_update_aux", ctypes.c_int, [_H, ctypes.c_double, _DP, _DP, _DP, _DP, _DP, _DP, _DP]),

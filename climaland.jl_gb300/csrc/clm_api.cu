@@ -1,0 +1,636 @@
+// C ABI of libclimaland_cuda (include/climaland_cuda.h).
+//
+// The handle owns one CUDA stream, the device copies of the column layout,
+// parameters, forcing and state, and (lazily) the scratch buffers of the
+// closure-level entry points. No call throws, aborts or traps: CUDA errors
+// become CLM_ERR_CUDA with a message in clm_last_error().
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/climaland_cuda.h"
+#include "clm_internal.cuh"
+
+namespace clm {
+// clm_step.cu
+cudaError_t launch_step(const StepArgs& A, int model, int precision, int wpc, double t0,
+                        double dt, int nsteps, cudaStream_t stream);
+size_t step_smem_bytes(int model, int precision, int nmax, int wpc);
+// clm_layout.cu
+cudaError_t ref_to_internal(const Layout& L, const int32_t* ref_off, const double* src,
+                            double* dst, int ncomp, cudaStream_t st);
+cudaError_t internal_to_ref(const Layout& L, const int32_t* ref_off, const double* src,
+                            double* dst, int ncomp, cudaStream_t st);
+cudaError_t cols_to_sorted(const Layout& L, const double* src, double* dst, cudaStream_t st);
+cudaError_t cols_to_orig(const Layout& L, const double* src, double* dst, cudaStream_t st);
+// clm_budget.cu
+cudaError_t launch_budgets(const StepArgs& A, int model, double* W, double* E, cudaStream_t st);
+}  // namespace clm
+
+using namespace clm;
+
+struct clm_handle {
+  clm_config cfg{};
+  int device = 0;
+  cudaStream_t stream = nullptr;      // stream in use
+  cudaStream_t own_stream = nullptr;  // created by clm_create
+  std::string err;
+  // layout (host copies)
+  int ncol = 0, stride = 0, ntiles = 0, nmax = 0;
+  int64_t ncells_ref = 0, ncells_int = 0;
+  std::vector<int32_t> ref_off;
+  std::vector<int> perm, col_n, tile_n;
+  std::vector<int64_t> tile_off;
+  // device
+  int64_t* d_tile_off = nullptr;
+  int* d_tile_n = nullptr;
+  int* d_col_n = nullptr;
+  int* d_perm = nullptr;
+  int32_t* d_ref_off = nullptr;
+  double *d_zlo = nullptr, *d_zhi = nullptr, *d_prm = nullptr, *d_lkap = nullptr;
+  double* d_forc[4] = {nullptr, nullptr, nullptr, nullptr};
+  double *d_v = nullptr, *d_ti = nullptr, *d_e = nullptr, *d_Fw = nullptr, *d_Fe = nullptr;
+  uint32_t* d_flags = nullptr;
+  int32_t* d_iters = nullptr;
+  double* d_stage = nullptr;  // ncells_ref * 3 staging (reference layout)
+  double* d_colstage = nullptr;  // 4 * stride: upload staging, W, E, spare
+  float* d_guess = nullptr;
+  bool have_geometry = false, have_params = false, have_state = false;
+  int wpc = 1;
+  Earth E{};
+  EHScalars sc{};
+};
+
+namespace {
+
+int fail(clm_handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+int cuda_fail(clm_handle* h, cudaError_t e, const char* what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  cudaGetLastError();  // clear the (non-sticky) error state
+  return fail(h, CLM_ERR_CUDA, m);
+}
+
+#define CLM_CUDA(h, call)                                   \
+  do {                                                      \
+    cudaError_t _e = (call);                                \
+    if (_e != cudaSuccess) return cuda_fail((h), _e, #call); \
+  } while (0)
+
+template <typename T>
+void dfree(T*& p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+bool is_eh(const clm_handle* h) { return h->cfg.model == CLM_MODEL_ENERGY_HYDROLOGY; }
+
+Layout layout_of(const clm_handle* h) {
+  Layout L;
+  L.ncol = h->ncol;
+  L.stride = h->stride;
+  L.ntiles = h->ntiles;
+  L.nmax = h->nmax;
+  L.ncells_int = h->ncells_int;
+  L.tile_off = h->d_tile_off;
+  L.tile_n = h->d_tile_n;
+  L.col_n = h->d_col_n;
+  L.perm = h->d_perm;
+  return L;
+}
+
+StepArgs step_args(const clm_handle* h) {
+  StepArgs A;
+  A.L = layout_of(h);
+  A.z_lo = h->d_zlo;
+  A.z_hi = h->d_zhi;
+  A.prm = h->d_prm;
+  A.lkap = h->d_lkap;
+  for (int i = 0; i < 4; ++i) A.forc[i] = h->d_forc[i];
+  A.v = h->d_v;
+  A.ti = h->d_ti;
+  A.e = h->d_e;
+  A.Fw = h->d_Fw;
+  A.Fe = h->d_Fe;
+  A.flags = h->d_flags;
+  A.iters = h->d_iters;
+  A.guess = h->cfg.learned_guess ? h->d_guess : nullptr;
+  A.E = h->E;
+  A.sc = h->sc;
+  A.bc_tw = h->cfg.bc_top_water;
+  A.bc_th = h->cfg.bc_top_heat;
+  A.bc_bw = h->cfg.bc_bottom_water;
+  A.bc_bh = h->cfg.bc_bottom_heat;
+  A.phase_change = is_eh(h) ? h->cfg.phase_change : 0;
+  A.newton_mode = h->cfg.newton_mode;
+  A.max_iters = h->cfg.max_iters;
+  A.tol = h->cfg.newton_tol;
+  A.energy_scale = h->cfg.energy_norm_scale;
+  A.seed = h->cfg.forcing_seed;
+  return A;
+}
+
+// Build the sorted, tiled layout from per-column layer counts.
+int build_layout(clm_handle* h, const std::vector<int>& nl) {
+  const int ncol = h->ncol;
+  h->ref_off.assign(ncol + 1, 0);
+  for (int c = 0; c < ncol; ++c) {
+    if (nl[c] < 2 || nl[c] > kMaxLayers)
+      return fail(h, CLM_ERR_ARG, "layer count must be in [2, " + std::to_string(kMaxLayers) +
+                                      "], column " + std::to_string(c) + " has " +
+                                      std::to_string(nl[c]));
+    h->ref_off[c + 1] = h->ref_off[c] + nl[c];
+  }
+  h->ncells_ref = h->ref_off[ncol];
+  h->stride = (ncol + kTile - 1) / kTile * kTile;
+  h->ntiles = h->stride / kTile;
+  std::vector<int> order(ncol);
+  std::iota(order.begin(), order.end(), 0);
+  // deepest first: equal-depth columns share tiles, and the deep tiles are
+  // scheduled first (longest-processing-time order)
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return nl[a] > nl[b]; });
+  h->perm.assign(h->stride, -1);
+  h->col_n.assign(h->stride, 0);
+  for (int s = 0; s < ncol; ++s) {
+    h->perm[s] = order[s];
+    h->col_n[s] = nl[order[s]];
+  }
+  h->tile_n.assign(h->ntiles, 0);
+  h->tile_off.assign(h->ntiles, 0);
+  int64_t off = 0;
+  int nmax = 0;
+  for (int t = 0; t < h->ntiles; ++t) {
+    int m = 0;
+    for (int j = 0; j < kTile; ++j) m = std::max(m, h->col_n[t * kTile + j]);
+    h->tile_n[t] = m;
+    h->tile_off[t] = off;
+    off += (int64_t)m * kTile;
+    nmax = std::max(nmax, m);
+  }
+  h->ncells_int = off;
+  h->nmax = nmax;
+  // device copies
+  dfree(h->d_tile_off); dfree(h->d_tile_n); dfree(h->d_col_n); dfree(h->d_perm); dfree(h->d_ref_off);
+  cudaStream_t st = h->stream;
+  CLM_CUDA(h, cudaMalloc(&h->d_tile_off, sizeof(int64_t) * h->ntiles));
+  CLM_CUDA(h, cudaMalloc(&h->d_tile_n, sizeof(int) * h->ntiles));
+  CLM_CUDA(h, cudaMalloc(&h->d_col_n, sizeof(int) * h->stride));
+  CLM_CUDA(h, cudaMalloc(&h->d_perm, sizeof(int) * h->stride));
+  CLM_CUDA(h, cudaMalloc(&h->d_ref_off, sizeof(int32_t) * (ncol + 1)));
+  CLM_CUDA(h, cudaMemcpyAsync(h->d_tile_off, h->tile_off.data(), sizeof(int64_t) * h->ntiles, cudaMemcpyHostToDevice, st));
+  CLM_CUDA(h, cudaMemcpyAsync(h->d_tile_n, h->tile_n.data(), sizeof(int) * h->ntiles, cudaMemcpyHostToDevice, st));
+  CLM_CUDA(h, cudaMemcpyAsync(h->d_col_n, h->col_n.data(), sizeof(int) * h->stride, cudaMemcpyHostToDevice, st));
+  CLM_CUDA(h, cudaMemcpyAsync(h->d_perm, h->perm.data(), sizeof(int) * h->stride, cudaMemcpyHostToDevice, st));
+  CLM_CUDA(h, cudaMemcpyAsync(h->d_ref_off, h->ref_off.data(), sizeof(int32_t) * (ncol + 1), cudaMemcpyHostToDevice, st));
+  // per-layout buffers
+  dfree(h->d_v); dfree(h->d_ti); dfree(h->d_e); dfree(h->d_stage);
+  const int64_t ni = std::max<int64_t>(h->ncells_int, 1);
+  CLM_CUDA(h, cudaMalloc(&h->d_v, sizeof(double) * ni));
+  CLM_CUDA(h, cudaMemsetAsync(h->d_v, 0, sizeof(double) * ni, st));
+  if (is_eh(h)) {
+    CLM_CUDA(h, cudaMalloc(&h->d_ti, sizeof(double) * ni));
+    CLM_CUDA(h, cudaMalloc(&h->d_e, sizeof(double) * ni));
+    CLM_CUDA(h, cudaMemsetAsync(h->d_ti, 0, sizeof(double) * ni, st));
+    CLM_CUDA(h, cudaMemsetAsync(h->d_e, 0, sizeof(double) * ni, st));
+  }
+  CLM_CUDA(h, cudaMalloc(&h->d_stage, sizeof(double) * std::max<int64_t>(h->ncells_ref, 1) * 3));
+  // choose warps per CTA: as many tiles per CTA as fit in the shared memory
+  // budget, up to 4 (cfg->cols_per_cta overrides)
+  int dev_smem = 0;
+  cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+  int want = h->cfg.cols_per_cta > 0 ? std::max(1, h->cfg.cols_per_cta / kTile) : 1;
+  want = std::min(want, 4);
+  while (want > 1 && step_smem_bytes(h->cfg.model, h->cfg.precision, h->nmax, want) > (size_t)dev_smem) --want;
+  if (step_smem_bytes(h->cfg.model, h->cfg.precision, h->nmax, want) > (size_t)dev_smem)
+    return fail(h, CLM_ERR_ARG, "column depth " + std::to_string(h->nmax) +
+                                    " needs more shared memory than the device offers");
+  h->wpc = want;
+  return CLM_OK;
+}
+
+int upload_cols_sorted(clm_handle* h, const double* host, double* dst, int rows) {
+  // host rows of ncol (original order) -> device rows of stride (sorted)
+  cudaStream_t st = h->stream;
+  Layout L = layout_of(h);
+  for (int r = 0; r < rows; ++r) {
+    CLM_CUDA(h, cudaMemcpyAsync(h->d_colstage, host + (size_t)r * h->ncol, sizeof(double) * h->ncol,
+                                cudaMemcpyHostToDevice, st));
+    CLM_CUDA(h, cols_to_sorted(L, h->d_colstage, dst + (size_t)r * h->stride, st));
+  }
+  return CLM_OK;
+}
+
+int download_cols(clm_handle* h, const double* dsrc, double* host) {
+  cudaStream_t st = h->stream;
+  Layout L = layout_of(h);
+  CLM_CUDA(h, cols_to_orig(L, dsrc, h->d_colstage, st));
+  CLM_CUDA(h, cudaMemcpyAsync(host, h->d_colstage, sizeof(double) * h->ncol, cudaMemcpyDeviceToHost, st));
+  return CLM_OK;
+}
+
+int ready(clm_handle* h) {
+  if (!h) return CLM_ERR_ARG;
+  if (!h->have_geometry) return fail(h, CLM_ERR_STATE, "clm_set_geometry has not been called");
+  if (!h->have_params) return fail(h, CLM_ERR_STATE, "clm_set_params has not been called");
+  if (!h->have_state) return fail(h, CLM_ERR_STATE, "clm_set_state has not been called");
+  return CLM_OK;
+}
+
+int set_state_impl(clm_handle* h, const double* v, const double* ti, const double* e,
+                   const double* Fw, const double* Fe, cudaMemcpyKind kind) {
+  if (!h) return CLM_ERR_ARG;
+  if (!h->have_geometry) return fail(h, CLM_ERR_STATE, "clm_set_geometry has not been called");
+  if (!v || !Fw) return fail(h, CLM_ERR_ARG, "vartheta_l and intF_w are required");
+  const bool eh = is_eh(h);
+  if (eh && (!ti || !e || !Fe)) return fail(h, CLM_ERR_ARG, "EnergyHydrology needs theta_i, rho_e_int, intF_e");
+  cudaStream_t st = h->stream;
+  Layout L = layout_of(h);
+  const size_t nb = sizeof(double) * h->ncells_ref;
+  const double* src[3] = {v, ti, e};
+  double* dst[3] = {h->d_v, h->d_ti, h->d_e};
+  for (int i = 0; i < (eh ? 3 : 1); ++i) {
+    double* stg = h->d_stage + (size_t)i * h->ncells_ref;
+    CLM_CUDA(h, cudaMemcpyAsync(stg, src[i], nb, kind, st));
+    CLM_CUDA(h, ref_to_internal(L, h->d_ref_off, stg, dst[i], 1, st));
+  }
+  const double* cs[2] = {Fw, Fe};
+  double* cd[2] = {h->d_Fw, h->d_Fe};
+  for (int i = 0; i < (eh ? 2 : 1); ++i) {
+    CLM_CUDA(h, cudaMemcpyAsync(h->d_colstage, cs[i], sizeof(double) * h->ncol, kind, st));
+    CLM_CUDA(h, cols_to_sorted(L, h->d_colstage, cd[i], st));
+  }
+  CLM_CUDA(h, cudaStreamSynchronize(st));
+  h->have_state = true;
+  return CLM_OK;
+}
+
+int get_state_impl(clm_handle* h, double* v, double* ti, double* e, double* Fw, double* Fe,
+                   cudaMemcpyKind kind) {
+  if (!h) return CLM_ERR_ARG;
+  if (!h->have_state) return fail(h, CLM_ERR_STATE, "no state on the device");
+  const bool eh = is_eh(h);
+  cudaStream_t st = h->stream;
+  Layout L = layout_of(h);
+  const size_t nb = sizeof(double) * h->ncells_ref;
+  double* outs[3] = {v, ti, e};
+  const double* srcs[3] = {h->d_v, h->d_ti, h->d_e};
+  for (int i = 0; i < (eh ? 3 : 1); ++i) {
+    if (!outs[i]) continue;
+    double* stg = h->d_stage + (size_t)i * h->ncells_ref;
+    CLM_CUDA(h, internal_to_ref(L, h->d_ref_off, srcs[i], stg, 1, st));
+    CLM_CUDA(h, cudaMemcpyAsync(outs[i], stg, nb, kind, st));
+  }
+  double* co[2] = {Fw, Fe};
+  const double* cs[2] = {h->d_Fw, h->d_Fe};
+  for (int i = 0; i < (eh ? 2 : 1); ++i) {
+    if (!co[i]) continue;
+    CLM_CUDA(h, cols_to_orig(L, cs[i], h->d_colstage, st));
+    CLM_CUDA(h, cudaMemcpyAsync(co[i], h->d_colstage, sizeof(double) * h->ncol, kind, st));
+    CLM_CUDA(h, cudaStreamSynchronize(st));  // d_colstage is reused
+  }
+  CLM_CUDA(h, cudaStreamSynchronize(st));
+  return CLM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* clm_version(void) { return "libclimaland_cuda 0.1 (sm_103a)"; }
+
+double clm_forcing_hash01(uint64_t seed, uint64_t column, int64_t period) {
+  return hash01(seed, column, period);
+}
+
+void clm_config_default(clm_config* c) {
+  if (!c) return;
+  std::memset(c, 0, sizeof(*c));
+  c->model = CLM_MODEL_ENERGY_HYDROLOGY;
+  c->precision = CLM_PREC_FP64;
+  c->newton_mode = CLM_NEWTON_FIXED;
+  c->max_iters = 3;
+  c->newton_tol = 1e-8;
+  c->energy_norm_scale = 1.0;
+  c->bc_top_water = CLM_BC_FLUX;
+  c->bc_top_heat = CLM_BC_FLUX;
+  c->bc_bottom_water = CLM_BC_FREE_DRAINAGE;
+  c->bc_bottom_heat = CLM_BC_FREE_DRAINAGE;
+  c->kersten_alpha = 0.24;
+  c->kersten_beta = 18.3;
+  c->ice_impedance_omega = 7.0;
+  c->visc_gamma = 2.64e-2;
+  c->visc_gamma_T_ref = 288.0;
+  c->earth.rho_l = 1000.0;
+  c->earth.rho_i = 916.7;
+  c->earth.cp_l = 4181.0;
+  c->earth.cp_i = 2100.0;
+  c->earth.T_0 = 273.16;
+  c->earth.T_freeze = 273.15;
+  c->earth.LH_f0 = 2834400.0 - 2500800.0;
+  c->earth.grav = 9.81;
+  c->phase_change = 1;
+}
+
+int clm_create(const clm_config* cfg, clm_handle** out) {
+  if (!cfg || !out) return CLM_ERR_ARG;
+  *out = nullptr;
+  if (cfg->model != CLM_MODEL_RICHARDS && cfg->model != CLM_MODEL_ENERGY_HYDROLOGY) return CLM_ERR_ARG;
+  if (cfg->ncol <= 0 || cfg->nlayers < 0 || cfg->nlayers > kMaxLayers || cfg->max_iters < 1 ||
+      cfg->max_iters > 1000)
+    return CLM_ERR_ARG;
+  if (cfg->precision != CLM_PREC_FP64 && cfg->precision != CLM_PREC_MIXED) return CLM_ERR_ARG;
+  if (cfg->newton_mode != CLM_NEWTON_FIXED && cfg->newton_mode != CLM_NEWTON_TOL) return CLM_ERR_ARG;
+  const int kinds[4] = {cfg->bc_top_water, cfg->bc_top_heat, cfg->bc_bottom_water, cfg->bc_bottom_heat};
+  for (int k : kinds)
+    if (k < CLM_BC_FLUX || k > CLM_BC_FLUX_ADVECTIVE) return CLM_ERR_ARG;
+  if (cfg->bc_top_water == CLM_BC_FREE_DRAINAGE || cfg->bc_top_water == CLM_BC_FLUX_ADVECTIVE ||
+      cfg->bc_bottom_water == CLM_BC_FLUX_ADVECTIVE || cfg->bc_top_heat == CLM_BC_FREE_DRAINAGE ||
+      cfg->bc_bottom_heat == CLM_BC_FLUX_ADVECTIVE)
+    return CLM_ERR_ARG;
+  clm_handle* h = new (std::nothrow) clm_handle();
+  if (!h) return CLM_ERR_ARG;
+  h->cfg = *cfg;
+  h->ncol = cfg->ncol;
+  h->E = make_earth(cfg->earth);
+  h->sc.kersten_alpha = cfg->kersten_alpha;
+  h->sc.kersten_beta = cfg->kersten_beta;
+  h->sc.omega_ln10 = cfg->ice_impedance_omega * kLn10;
+  h->sc.visc_gamma = cfg->visc_gamma;
+  h->sc.visc_gamma_T_ref = cfg->visc_gamma_T_ref;
+  cudaError_t e = cudaGetDevice(&h->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
+  h->stream = h->own_stream;
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    delete h;
+    return CLM_ERR_CUDA;
+  }
+  const int stride = (h->ncol + kTile - 1) / kTile * kTile;
+  const size_t cb = sizeof(double) * stride;
+  bool ok = cudaMalloc(&h->d_zlo, cb) == cudaSuccess && cudaMalloc(&h->d_zhi, cb) == cudaSuccess &&
+            cudaMalloc(&h->d_prm, cb * CLM_NPARAM_EH) == cudaSuccess &&
+            cudaMalloc(&h->d_lkap, cb * 2) == cudaSuccess && cudaMalloc(&h->d_Fw, cb) == cudaSuccess &&
+            cudaMalloc(&h->d_Fe, cb) == cudaSuccess &&
+            cudaMalloc(&h->d_flags, sizeof(uint32_t) * stride) == cudaSuccess &&
+            cudaMalloc(&h->d_iters, sizeof(int32_t) * stride) == cudaSuccess &&
+            cudaMalloc(&h->d_colstage, cb * 4) == cudaSuccess;
+  if (ok) {
+    ok = cudaMemsetAsync(h->d_prm, 0, cb * CLM_NPARAM_EH, h->stream) == cudaSuccess &&
+         cudaMemsetAsync(h->d_lkap, 0, cb * 2, h->stream) == cudaSuccess &&
+         cudaMemsetAsync(h->d_Fw, 0, cb, h->stream) == cudaSuccess &&
+         cudaMemsetAsync(h->d_Fe, 0, cb, h->stream) == cudaSuccess &&
+         cudaMemsetAsync(h->d_flags, 0, sizeof(uint32_t) * stride, h->stream) == cudaSuccess &&
+         cudaMemsetAsync(h->d_iters, 0, sizeof(int32_t) * stride, h->stream) == cudaSuccess;
+  }
+  if (!ok) {
+    cudaGetLastError();
+    clm_destroy(h);
+    return CLM_ERR_CUDA;
+  }
+  if (cfg->nlayers > 0) {
+    std::vector<int> nl(h->ncol, cfg->nlayers);
+    int rc = build_layout(h, nl);
+    if (rc != CLM_OK) {
+      clm_destroy(h);
+      return rc;
+    }
+  }
+  *out = h;
+  return CLM_OK;
+}
+
+void clm_destroy(clm_handle* h) {
+  if (!h) return;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->own_stream && h->own_stream != h->stream) cudaStreamSynchronize(h->own_stream);
+  dfree(h->d_tile_off); dfree(h->d_tile_n); dfree(h->d_col_n); dfree(h->d_perm); dfree(h->d_ref_off);
+  dfree(h->d_zlo); dfree(h->d_zhi); dfree(h->d_prm); dfree(h->d_lkap);
+  for (auto& p : h->d_forc) dfree(p);
+  dfree(h->d_v); dfree(h->d_ti); dfree(h->d_e); dfree(h->d_Fw); dfree(h->d_Fe);
+  dfree(h->d_flags); dfree(h->d_iters); dfree(h->d_stage); dfree(h->d_colstage); dfree(h->d_guess);
+  if (h->own_stream) cudaStreamDestroy(h->own_stream);
+  cudaGetLastError();
+  delete h;
+}
+
+const char* clm_last_error(const clm_handle* h) {
+  if (!h) return "null handle";
+  return h->err.c_str();
+}
+
+int clm_set_geometry(clm_handle* h, const double* z_lo, const double* z_hi, const int32_t* offsets) {
+  if (!h || !z_lo || !z_hi) return h ? fail(h, CLM_ERR_ARG, "z_lo and z_hi are required") : CLM_ERR_ARG;
+  for (int c = 0; c < h->ncol; ++c)
+    if (!(z_hi[c] > z_lo[c]) || !std::isfinite(z_lo[c]) || !std::isfinite(z_hi[c]))
+      return fail(h, CLM_ERR_ARG, "column " + std::to_string(c) + " needs z_lo < z_hi");
+  if (h->cfg.nlayers == 0) {
+    if (!offsets) return fail(h, CLM_ERR_ARG, "offsets are required when cfg.nlayers == 0");
+    if (offsets[0] != 0) return fail(h, CLM_ERR_ARG, "offsets[0] must be 0");
+    std::vector<int> nl(h->ncol);
+    for (int c = 0; c < h->ncol; ++c) {
+      nl[c] = offsets[c + 1] - offsets[c];
+    }
+    int rc = build_layout(h, nl);
+    if (rc != CLM_OK) return rc;
+  } else if (offsets) {
+    for (int c = 0; c <= h->ncol; ++c)
+      if (offsets[c] != c * h->cfg.nlayers)
+        return fail(h, CLM_ERR_ARG, "offsets disagree with cfg.nlayers");
+  }
+  int rc = upload_cols_sorted(h, z_lo, h->d_zlo, 1);
+  if (rc == CLM_OK) rc = upload_cols_sorted(h, z_hi, h->d_zhi, 1);
+  if (rc != CLM_OK) return rc;
+  CLM_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->have_geometry = true;
+  return CLM_OK;
+}
+
+int clm_set_params(clm_handle* h, const double* p, int32_t nparams) {
+  if (!h) return CLM_ERR_ARG;
+  if (!h->have_geometry) return fail(h, CLM_ERR_STATE, "clm_set_geometry has not been called");
+  const int need = is_eh(h) ? CLM_NPARAM_EH : CLM_NPARAM_RICHARDS;
+  if (!p || nparams < need || nparams > CLM_NPARAM_EH)
+    return fail(h, CLM_ERR_ARG, "expected " + std::to_string(need) + " parameter rows");
+  const int ncol = h->ncol;
+  for (int c = 0; c < ncol; ++c) {
+    const double nu = p[CLM_P_NU * ncol + c], Ks = p[CLM_P_K_SAT * ncol + c];
+    const double Ss = p[CLM_P_S_S * ncol + c], tr = p[CLM_P_THETA_R * ncol + c];
+    const double a = p[CLM_P_VG_ALPHA * ncol + c], n = p[CLM_P_VG_N * ncol + c];
+    if (!(nu > 0 && nu <= 1) || !(Ks >= 0) || !(Ss > 0) || !(tr >= 0 && tr < nu) || !(a > 0) || !(n > 1))
+      return fail(h, CLM_ERR_ARG, "invalid hydraulic parameters in column " + std::to_string(c));
+    if (need == CLM_NPARAM_EH) {
+      const double kd = p[CLM_P_KAPPA_DRY * ncol + c], kf = p[CLM_P_KAPPA_SAT_FROZEN * ncol + c];
+      const double ku = p[CLM_P_KAPPA_SAT_UNFROZEN * ncol + c], rc = p[CLM_P_RHOC_DS * ncol + c];
+      if (!(kd >= 0) || !(kf > 0) || !(ku > 0) || !(rc > 0))
+        return fail(h, CLM_ERR_ARG, "invalid thermal parameters in column " + std::to_string(c));
+    }
+  }
+  int rc = upload_cols_sorted(h, p, h->d_prm, nparams);
+  if (rc != CLM_OK) return rc;
+  if (need == CLM_NPARAM_EH) {
+    std::vector<double> lk((size_t)2 * ncol);
+    for (int c = 0; c < ncol; ++c) {
+      lk[c] = std::log(p[CLM_P_KAPPA_SAT_UNFROZEN * ncol + c]);
+      lk[ncol + c] = std::log(p[CLM_P_KAPPA_SAT_FROZEN * ncol + c]);
+    }
+    rc = upload_cols_sorted(h, lk.data(), h->d_lkap, 2);
+    if (rc != CLM_OK) return rc;
+    CLM_CUDA(h, cudaStreamSynchronize(h->stream));
+  }
+  CLM_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->have_params = true;
+  return CLM_OK;
+}
+
+int clm_set_bc(clm_handle* h, int32_t slot, const double* f, int32_t nfields) {
+  if (!h) return CLM_ERR_ARG;
+  if (!h->have_geometry) return fail(h, CLM_ERR_STATE, "clm_set_geometry has not been called");
+  if (slot < 0 || slot > 3) return fail(h, CLM_ERR_ARG, "slot must be a clm_bc_slot");
+  if (!f) {
+    dfree(h->d_forc[slot]);
+    return CLM_OK;
+  }
+  if (nfields < 1 || nfields > CLM_F_NFIELDS) return fail(h, CLM_ERR_ARG, "nfields out of range");
+  for (int64_t i = 0; i < (int64_t)nfields * h->ncol; ++i)
+    if (!std::isfinite(f[i])) return fail(h, CLM_ERR_ARG, "non-finite forcing value");
+  if (!h->d_forc[slot]) {
+    CLM_CUDA(h, cudaMalloc(&h->d_forc[slot], sizeof(double) * h->stride * CLM_F_NFIELDS));
+  }
+  CLM_CUDA(h, cudaMemsetAsync(h->d_forc[slot], 0, sizeof(double) * h->stride * CLM_F_NFIELDS, h->stream));
+  int rc = upload_cols_sorted(h, f, h->d_forc[slot], nfields);
+  if (rc != CLM_OK) return rc;
+  CLM_CUDA(h, cudaStreamSynchronize(h->stream));
+  return CLM_OK;
+}
+
+int clm_set_state(clm_handle* h, const double* v, const double* ti, const double* e, const double* Fw,
+                  const double* Fe) {
+  return set_state_impl(h, v, ti, e, Fw, Fe, cudaMemcpyHostToDevice);
+}
+
+int clm_get_state(clm_handle* h, double* v, double* ti, double* e, double* Fw, double* Fe) {
+  return get_state_impl(h, v, ti, e, Fw, Fe, cudaMemcpyDeviceToHost);
+}
+
+int clm_set_state_device(clm_handle* h, const double* v, const double* ti, const double* e,
+                         const double* Fw, const double* Fe) {
+  return set_state_impl(h, v, ti, e, Fw, Fe, cudaMemcpyDeviceToDevice);
+}
+
+int clm_get_state_device(clm_handle* h, double* v, double* ti, double* e, double* Fw, double* Fe) {
+  return get_state_impl(h, v, ti, e, Fw, Fe, cudaMemcpyDeviceToDevice);
+}
+
+int clm_step_async(clm_handle* h, double t, double dt, int32_t nsteps) {
+  int rc = ready(h);
+  if (rc != CLM_OK) return rc;
+  if (!(dt > 0) || !std::isfinite(dt) || !std::isfinite(t) || nsteps < 0)
+    return fail(h, CLM_ERR_ARG, "need dt > 0, finite t, nsteps >= 0");
+  if (nsteps == 0) return CLM_OK;
+  StepArgs A = step_args(h);
+  // Steps are fused in one launch (the column stays in shared memory between
+  // steps); launches are chunked so that one launch stays short.
+  const int chunk = 64;
+  for (int s0 = 0; s0 < nsteps; s0 += chunk) {
+    const int ns = std::min(chunk, nsteps - s0);
+    CLM_CUDA(h, launch_step(A, h->cfg.model, h->cfg.precision, h->wpc, t + s0 * dt, dt, ns, h->stream));
+  }
+  return CLM_OK;
+}
+
+int clm_sync(clm_handle* h) {
+  if (!h) return CLM_ERR_ARG;
+  CLM_CUDA(h, cudaStreamSynchronize(h->stream));
+  return CLM_OK;
+}
+
+int clm_set_stream(clm_handle* h, void* cuda_stream) {
+  if (!h) return CLM_ERR_ARG;
+  CLM_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->stream = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : h->own_stream;
+  return CLM_OK;
+}
+
+int clm_step(clm_handle* h, double t, double dt, int32_t nsteps) {
+  int rc = clm_step_async(h, t, dt, nsteps);
+  if (rc != CLM_OK) return rc;
+  return clm_sync(h);
+}
+
+int clm_get_budgets(clm_handle* h, double* W, double* Eo) {
+  int rc = ready(h);
+  if (rc != CLM_OK) return rc;
+  StepArgs A = step_args(h);
+  double* dW = h->d_colstage + h->stride;
+  double* dE = h->d_colstage + 2 * (size_t)h->stride;
+  CLM_CUDA(h, launch_budgets(A, h->cfg.model, dW, dE, h->stream));
+  if (W) {
+    rc = download_cols(h, dW, W);
+    if (rc != CLM_OK) return rc;
+    CLM_CUDA(h, cudaStreamSynchronize(h->stream));
+  }
+  if (Eo) {
+    if (is_eh(h)) {
+      rc = download_cols(h, dE, Eo);
+      if (rc != CLM_OK) return rc;
+    } else {
+      std::fill(Eo, Eo + h->ncol, 0.0);
+    }
+  }
+  CLM_CUDA(h, cudaStreamSynchronize(h->stream));
+  return CLM_OK;
+}
+
+int clm_get_status(clm_handle* h, uint32_t* flags, int32_t* iters) {
+  if (!h) return CLM_ERR_ARG;
+  if (!h->have_geometry) return fail(h, CLM_ERR_STATE, "clm_set_geometry has not been called");
+  std::vector<uint32_t> f(h->stride);
+  std::vector<int32_t> it(h->stride);
+  CLM_CUDA(h, cudaMemcpyAsync(f.data(), h->d_flags, sizeof(uint32_t) * h->stride, cudaMemcpyDeviceToHost, h->stream));
+  CLM_CUDA(h, cudaMemcpyAsync(it.data(), h->d_iters, sizeof(int32_t) * h->stride, cudaMemcpyDeviceToHost, h->stream));
+  CLM_CUDA(h, cudaStreamSynchronize(h->stream));
+  for (int s = 0; s < h->ncol; ++s) {
+    const int c = h->perm[s];
+    if (flags) flags[c] = f[s];
+    if (iters) iters[c] = it[s];
+  }
+  return CLM_OK;
+}
+
+int clm_load_mlp(clm_handle* h, const void* weights, int64_t nbytes) {
+  if (!h) return CLM_ERR_ARG;
+  (void)weights;
+  (void)nbytes;
+  return fail(h, CLM_ERR_UNSUPPORTED, "learned Newton guess is not built in this library");
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// internal accessors for clm_closures_api.cu
+// ---------------------------------------------------------------------------
+namespace clm {
+StepArgs handle_step_args(clm_handle* h) { return step_args(h); }
+Layout handle_layout(clm_handle* h) { return layout_of(h); }
+int handle_ready(clm_handle* h) { return ready(h); }
+int handle_fail(clm_handle* h, int code, const char* msg) { return fail(h, code, msg); }
+int handle_cuda_fail(clm_handle* h, cudaError_t e, const char* what) { return cuda_fail(h, e, what); }
+cudaStream_t handle_stream(clm_handle* h) { return h->stream; }
+const int32_t* handle_ref_off(clm_handle* h) { return h->d_ref_off; }
+int64_t handle_ncells_ref(clm_handle* h) { return h->ncells_ref; }
+int handle_ncol(clm_handle* h) { return h->ncol; }
+int handle_model(clm_handle* h) { return h->cfg.model; }
+double* handle_state_ptr(clm_handle* h, int which) {
+  return which == 0 ? h->d_v : (which == 1 ? h->d_ti : h->d_e);
+}
+}  // namespace clm

@@ -1,0 +1,281 @@
+// Closure-level kernels: each reference closure evaluated on its own, for
+// per-closure parity checks and for callers that drive their own time
+// stepper. One thread per column; cell arrays in the reference layout
+// (cell = ref_off[c] + k), per-column arrays in sorted order (index s).
+//
+//   closure_kernel<AUX>  make_update_cache = update_aux! + boundary fluxes
+//                        (rre.jl:111-149, 368-380;
+//                         energy_hydrology.jl:273-298, 722-814)
+//   closure_kernel<EXP>  make_exp_tendency (models.jl:279-287; rre.jl:214-243;
+//                        energy_hydrology.jl:315-350, 838-906)
+//   closure_kernel<IMP>  make_compute_imp_tendency (rre.jl:161-203;
+//                        energy_hydrology.jl:363-425) after the cache update
+//   closure_kernel<JAC>  make_compute_jacobian (rre.jl:391-458;
+//                        energy_hydrology.jl:466-576) after the cache update
+//   solve_kernel         FieldMatrixSolver block solve
+//                        (implicit_timestepping.jl:160-171)
+
+#include <cuda_runtime.h>
+
+#include "clm_closures.cuh"
+
+namespace clm {
+
+template <int KIND>
+__global__ void closure_kernel(ClosureArgs C) {
+  const StepArgs& A = C.A;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= A.L.stride) return;
+  const int n = A.L.col_n[s];
+  if (n <= 0) return;
+  const int orig = A.L.perm[s];
+  const int64_t o = C.ref_off[orig];
+  const int st = A.L.stride;
+  const int ncol = A.L.ncol;
+  const bool eh = C.model == CLM_MODEL_ENERGY_HYDROLOGY;
+  const Earth& E = A.E;
+  const EHScalars& sc = A.sc;
+  const double* P = A.prm;
+  const double nu = P[CLM_P_NU * st + s], K_sat = P[CLM_P_K_SAT * st + s];
+  const double S_s = P[CLM_P_S_S * st + s], theta_r = P[CLM_P_THETA_R * st + s];
+  const VG g = make_vg(P[CLM_P_VG_ALPHA * st + s], P[CLM_P_VG_N * st + s]);
+  const double dz = (A.z_hi[s] - A.z_lo[s]) / n;
+  const double inv_dz = 1.0 / dz, half = 0.5 * dz;
+  double kdry = 0, ksf = 0, ksu = 0, rcds = 0, nuom = 0, nuq = 0, nug = 0, lku = 0, lkf = 0;
+  if (eh) {
+    kdry = P[CLM_P_KAPPA_DRY * st + s];
+    ksf = P[CLM_P_KAPPA_SAT_FROZEN * st + s];
+    ksu = P[CLM_P_KAPPA_SAT_UNFROZEN * st + s];
+    rcds = P[CLM_P_RHOC_DS * st + s];
+    nuom = P[CLM_P_NU_SS_OM * st + s];
+    nuq = P[CLM_P_NU_SS_QUARTZ * st + s];
+    nug = P[CLM_P_NU_SS_GRAVEL * st + s];
+    lku = A.lkap[s];
+    lkf = A.lkap[st + s];
+  }
+  double Kc[kMaxLayers], psic[kMaxLayers], Tc[kMaxLayers], kapc[kMaxLayers], tlc[kMaxLayers];
+  // ---- update_aux ----
+  for (int k = 0; k < n; ++k) {
+    const double Yv = C.v[o + k];
+    const double Yti = eh ? C.ti[o + k] : 0.0;
+    const double nu_eff = nu - Yti;
+    double d;
+    psi_dpsi<false>(g, nu_eff, Yv, theta_r, S_s, psic[k], d);
+    const Sat sK = saturation(nu, Yv, theta_r);
+    double K = conductivity(g, K_sat, sK.S);
+    if (eh) {
+      const double Ye = C.e[o + k];
+      const double v_safe = fmax(Yv, theta_r + kSqrtEps);
+      const double nu_safe = fmax(nu_eff, theta_r + kSqrtEps);
+      const double tl = (v_safe < nu_safe) ? v_safe : nu_safe;
+      tlc[k] = tl;
+      kapc[k] = conductivity_heat(sc, tl, Yti, nu, kdry, ksu, ksf, lku, lkf, nuom, nuq, nug);
+      Tc[k] = temperature(E, Ye, Yti, heat_capacity(E, tl, Yti, rcds));
+      const double fi = Yti / (tl + Yti - theta_r);
+      K *= exp(-sc.omega_ln10 * fi + sc.visc_gamma * (Tc[k] - sc.visc_gamma_T_ref));
+    }
+    Kc[k] = K;
+  }
+  // ---- boundary fluxes at t ----
+  const double t = C.t;
+  const double ftw = forcing_value(A.forc[CLM_BC_TOP_WATER], st, s, orig, t, A.seed);
+  const double fth = forcing_value(A.forc[CLM_BC_TOP_HEAT], st, s, orig, t, A.seed);
+  const double fbw = forcing_value(A.forc[CLM_BC_BOTTOM_WATER], st, s, orig, t, A.seed);
+  const double fbh = forcing_value(A.forc[CLM_BC_BOTTOM_HEAT], st, s, orig, t, A.seed);
+  double Ftw = ftw, Fth = 0, Fbw = fbw, Fbh = 0;
+  if (A.bc_tw == CLM_BC_STATE) {
+    double pb, d;
+    psi_dpsi<false>(g, nu, ftw, theta_r, S_s, pb, d);
+    Ftw = -Kc[n - 1] * ((pb + half) - psic[n - 1]) / half;
+  }
+  if (A.bc_bw == CLM_BC_FREE_DRAINAGE) {
+    Fbw = -1.0 * Kc[0];
+  } else if (A.bc_bw == CLM_BC_STATE) {
+    double pb, d;
+    psi_dpsi<false>(g, nu, fbw, theta_r, S_s, pb, d);
+    Fbw = -Kc[0] * ((psic[0] + half) - pb) / half;
+  }
+  if (eh) {
+    Fth = fth;
+    if (A.bc_th == CLM_BC_STATE) Fth = -kapc[n - 1] * (fth - Tc[n - 1]) / half;
+    else if (A.bc_th == CLM_BC_FLUX_ADVECTIVE) {
+      const double* F = A.forc[CLM_BC_TOP_HEAT];
+      Fth = fth + Ftw * rho_e_liq(E, F ? F[CLM_F_T_ADV * st + s] : E.T_0);
+    }
+    Fbh = fbh;
+    if (A.bc_bh == CLM_BC_FREE_DRAINAGE) Fbh = -1.0 * Kc[0] * rho_e_liq(E, Tc[0]);
+    else if (A.bc_bh == CLM_BC_STATE) Fbh = -kapc[0] * (Tc[0] - fbh) / half;
+  }
+  const bool dflux = !eh && A.bc_tw == CLM_BC_STATE;
+
+  if (KIND == CL_AUX) {
+    for (int k = 0; k < n; ++k) {
+      if (C.K) C.K[o + k] = Kc[k];
+      if (C.psi) C.psi[o + k] = psic[k];
+      if (eh) {
+        if (C.theta_l) C.theta_l[o + k] = tlc[k];
+        if (C.T) C.T[o + k] = Tc[k];
+        if (C.kappa) C.kappa[o + k] = kapc[k];
+        if (C.Tf) {
+          // energy_hydrology.jl:797-808 passes (rho_l, rho_i) into the
+          // (rho_ice, rho_liq) slots of soil_Tf_depressed (:35-52).
+          const double Yti = C.ti[o + k];
+          const double tt = fmin(E.rho_l / E.rho_i * Yti + tlc[k], nu);
+          const double pw = matric_of(g, nu, tt, theta_r);
+          C.Tf[o + k] = fmax(E.T_freeze * exp(E.grav_over_LH_f0 * pw), 1.0);
+        }
+      }
+    }
+    if (C.bc) {
+      C.bc[0 * ncol + orig] = Ftw;
+      C.bc[1 * ncol + orig] = Fth;
+      C.bc[2 * ncol + orig] = Fbw;
+      C.bc[3 * ncol + orig] = Fbh;
+    }
+    return;
+  }
+  if (KIND == CL_EXP) {
+    for (int k = 0; k < n; ++k) {
+      double dv = 0.0, dti = 0.0;
+      if (eh && A.phase_change) {
+        const double Yti = C.ti[o + k];
+        // phase_change_source with thermal_time(rho c(theta_l, theta_i), dz, kappa)
+        const double rc = heat_capacity(E, tlc[k], Yti, rcds);
+        const double theta_tot = fmin(E.rho_i_over_rho_l * Yti + tlc[k], nu);
+        const Sat ss = saturation(nu, theta_tot, theta_r);
+        const double pw = matric_of(g, nu, theta_tot, theta_r);
+        const double Tf = fmax(E.T_freeze * exp(E.grav_over_LH_f0 * pw), 1.0);
+        double th_star;
+        if (Tf - Tc[k] > kEps) {
+          const double p = pw + E.LH_f0_over_grav * log(Tc[k] / Tf);
+          const double x = exp(g.n * log(g.alpha * fabs(p)));
+          th_star = exp(-g.m * log1p(x)) * (nu - theta_r) + theta_r;
+        } else {
+          th_star = ss.S * (nu - theta_r) + theta_r;
+        }
+        const double tau = 3.0 * rc * (dz * dz) / kapc[k];
+        const double pc = (tlc[k] - th_star) / tau;
+        dv = -pc;
+        dti = E.rho_l_over_rho_i * pc;
+      }
+      if (C.dv) C.dv[o + k] = dv;
+      if (eh && C.dti) C.dti[o + k] = dti;
+      if (eh && C.de) C.de[o + k] = 0.0;
+    }
+    if (C.dFw) C.dFw[orig] = 0.0;
+    if (eh && C.dFe) C.dFe[orig] = 0.0;
+    return;
+  }
+  if (KIND == CL_IMP) {
+    double Fw_dn = Fbw, Fe_dn = Fbh;
+    for (int k = 0; k < n; ++k) {
+      double Fw_up, Fe_up = 0.0;
+      if (k < n - 1) {
+        const double dh = (psic[k + 1] - psic[k]) + dz;
+        Fw_up = -0.5 * (Kc[k] + Kc[k + 1]) * inv_dz * dh;
+        if (eh) {
+          const double ak = 0.5 * (kapc[k] + kapc[k + 1]) * inv_dz;
+          const double ae = 0.5 * (rho_e_liq(E, Tc[k]) * Kc[k] + rho_e_liq(E, Tc[k + 1]) * Kc[k + 1]) * inv_dz;
+          Fe_up = -ak * (Tc[k + 1] - Tc[k]) - ae * dh;
+        }
+      } else {
+        Fw_up = Ftw;
+        Fe_up = Fth;
+      }
+      if (C.dv) C.dv[o + k] = -((Fw_up - Fw_dn) * inv_dz);
+      if (eh) {
+        if (C.de) C.de[o + k] = -((Fe_up - Fe_dn) * inv_dz);
+        if (C.dti) C.dti[o + k] = 0.0;
+      }
+      Fw_dn = Fw_up;
+      Fe_dn = Fe_up;
+    }
+    if (C.dFw) C.dFw[orig] = -(Ftw - Fbw);
+    if (eh && C.dFe) C.dFe[orig] = -(Fth - Fbh);
+    return;
+  }
+  if (KIND == CL_JAC) {
+    const double rdz = C.dtgamma * inv_dz;
+    double D[kMaxLayers];
+    for (int k = 0; k < n; ++k) {
+      double p;
+      const double Yti = eh ? C.ti[o + k] : 0.0;
+      psi_dpsi<true>(g, nu - Yti, C.v[o + k], theta_r, S_s, p, D[k]);
+    }
+    for (int blk = 0; blk < (eh ? 3 : 1); ++blk) {
+      double* W = blk == 0 ? C.Wvv : (blk == 1 ? C.Wev : C.Wee);
+      if (!W) continue;
+      for (int k = 0; k < n; ++k) {
+        double cup = 0.0, cdn = 0.0, dm = 0.0, d0, dp = 0.0;
+        auto coef = [&](int a) -> double {  // face coefficient between a, a+1
+          if (blk == 0) return 0.5 * (Kc[a] + Kc[a + 1]);
+          if (blk == 1) return 0.5 * (rho_e_liq(E, Tc[a]) * Kc[a] + rho_e_liq(E, Tc[a + 1]) * Kc[a + 1]);
+          return 0.5 * (kapc[a] + kapc[a + 1]);
+        };
+        auto dd = [&](int a) -> double {
+          if (blk < 2) return D[a];
+          return 1.0 / heat_capacity(E, tlc[a], C.ti[o + a], rcds);
+        };
+        d0 = dd(k);
+        if (k < n - 1) { cup = coef(k) * inv_dz; dp = dd(k + 1); }
+        if (k > 0) { cdn = coef(k - 1) * inv_dz; dm = dd(k - 1); }
+        double L = (k > 0) ? rdz * cdn * dm : 0.0;
+        double U = (k < n - 1) ? rdz * cup * dp : 0.0;
+        double M = -rdz * (cup + cdn) * d0 - 1.0;
+        if (blk == 0 && dflux && k == n - 1) M += -C.dtgamma * ((Kc[n - 1] * D[n - 1] / half) * inv_dz);
+        W[3 * (o + k) + 0] = L;
+        W[3 * (o + k) + 1] = M;
+        W[3 * (o + k) + 2] = U;
+      }
+    }
+  }
+}
+
+__device__ void thomas_ref(int n, const double* W, const double* f, double* x) {
+  double cp[kMaxLayers], dp[kMaxLayers];
+  for (int k = 0; k < n; ++k) {
+    const double L = W[3 * k], M = W[3 * k + 1], U = W[3 * k + 2];
+    const double den = (k > 0) ? M - L * cp[k - 1] : M;
+    cp[k] = U / den;
+    dp[k] = (k > 0) ? (f[k] - L * dp[k - 1]) / den : f[k] / den;
+  }
+  x[n - 1] = dp[n - 1];
+  for (int k = n - 2; k >= 0; --k) x[k] = dp[k] - cp[k] * x[k + 1];
+}
+
+__global__ void solve_kernel(SolveArgs S) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= S.L.stride) return;
+  const int n = S.L.col_n[s];
+  if (n <= 0) return;
+  const int64_t o = S.ref_off[S.L.perm[s]];
+  thomas_ref(n, S.Wvv + 3 * o, S.fv + o, S.dv + o);
+  if (S.Wev && S.Wee && S.fe && S.de) {
+    double g[kMaxLayers];
+    for (int k = 0; k < n; ++k) {
+      double w = S.Wev[3 * (o + k) + 1] * S.dv[o + k];
+      if (k > 0) w += S.Wev[3 * (o + k)] * S.dv[o + k - 1];
+      if (k < n - 1) w += S.Wev[3 * (o + k) + 2] * S.dv[o + k + 1];
+      g[k] = S.fe[o + k] - w;
+    }
+    thomas_ref(n, S.Wee + 3 * o, g, S.de + o);
+  }
+}
+
+cudaError_t launch_closure(int kind, const ClosureArgs& C, cudaStream_t st) {
+  const int blocks = (C.A.L.stride + 127) / 128;
+  switch (kind) {
+    case CL_AUX: closure_kernel<CL_AUX><<<blocks, 128, 0, st>>>(C); break;
+    case CL_EXP: closure_kernel<CL_EXP><<<blocks, 128, 0, st>>>(C); break;
+    case CL_IMP: closure_kernel<CL_IMP><<<blocks, 128, 0, st>>>(C); break;
+    default: closure_kernel<CL_JAC><<<blocks, 128, 0, st>>>(C); break;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_solve(const SolveArgs& S, cudaStream_t st) {
+  solve_kernel<<<(S.L.stride + 127) / 128, 128, 0, st>>>(S);
+  return cudaGetLastError();
+}
+
+}  // namespace clm

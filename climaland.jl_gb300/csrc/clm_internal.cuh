@@ -1,0 +1,71 @@
+// Internal device layout and kernel argument blocks of libclimaland_cuda.
+//
+// Columns are processed one per thread, 32 columns (one warp) per "tile".
+// Cell arrays are stored tile by tile, layer-major inside a tile:
+//   cell(tile, k, lane) = tile_off[tile] + k * 32 + lane
+// so a warp's load of one layer is one contiguous 256-byte segment. Columns
+// are sorted by layer count (descending) before tiling, so a tile holds
+// columns of equal or nearly equal depth; tile_n is the deepest in the tile.
+// Per-column arrays (parameters, forcing, integrated fluxes, status) are
+// stored in the same sorted order with row stride `stride` (a multiple of 32).
+#pragma once
+
+#include <cstdint>
+
+#include "clm_physics.cuh"
+
+namespace clm {
+
+constexpr int kTile = 32;
+constexpr int kMaxLayers = 64;
+
+struct Layout {
+  int ncol;        // real columns
+  int stride;      // padded column count (multiple of 32)
+  int ntiles;      // stride / 32
+  int nmax;        // deepest column
+  int64_t ncells_int;  // cells in the internal layout (incl. padding)
+  const int64_t* tile_off;  // [ntiles]
+  const int* tile_n;        // [ntiles]
+  const int* col_n;         // [stride]  0 for padding lanes
+  const int* perm;          // [stride]  original column index, -1 padding
+};
+
+struct StepArgs {
+  Layout L;
+  const double* z_lo;   // [stride]
+  const double* z_hi;   // [stride]
+  const double* prm;    // [CLM_NPARAM_EH][stride]
+  const double* lkap;   // [2][stride] log kappa_sat_unfrozen, log kappa_sat_frozen
+  const double* forc[4];  // [CLM_F_NFIELDS][stride] per slot, or null
+  double* v;            // vartheta_l (internal layout)
+  double* ti;           // theta_i
+  double* e;            // rho_e_int
+  double* Fw;           // intF_w  [stride]
+  double* Fe;           // intF_e  [stride]
+  uint32_t* flags;      // [stride]
+  int32_t* iters;       // [stride]
+  const float* guess;   // learned Newton guess (internal layout, 2 per cell) or null
+  Earth E;
+  EHScalars sc;
+  int bc_tw, bc_th, bc_bw, bc_bh;
+  int phase_change;
+  int newton_mode;
+  int max_iters;
+  double tol;
+  double energy_scale;
+  uint64_t seed;
+};
+
+// Shared-memory view of one warp's column tile: array a, layer k.
+template <typename T>
+struct Tile {
+  T* base;
+  int nmax;
+  int lane;
+  __device__ __forceinline__ T& operator()(int a, int k) const {
+    return base[(a * nmax + k) * kTile + lane];
+  }
+};
+
+}  // namespace clm

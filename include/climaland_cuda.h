@@ -221,6 +221,12 @@ int clm_step(clm_handle* h, double t, double dt, int32_t nsteps);
 int clm_step_async(clm_handle* h, double t, double dt, int32_t nsteps);
 int clm_sync(clm_handle* h);
 
+/* Run the handle's work on a caller-owned cudaStream_t (NULL restores the
+ * handle's own stream). No reference counterpart: it lets a host that owns
+ * the CUDA context (CUDA.jl, PyTorch) order and time the library's kernels
+ * on its own stream. */
+int clm_set_stream(clm_handle* h, void* cuda_stream);
+
 /* Column budgets total_water / total_energy (rre.jl:502-511,
  * energy_hydrology.jl:1282-1320) of the current state, per column. */
 int clm_get_budgets(clm_handle* h, double* total_water, double* total_energy);

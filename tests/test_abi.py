@@ -1,0 +1,76 @@
+"""CPU checks of the C ABI: the library builds, loads without a GPU and
+exports every function include/climaland_cuda.h declares; the ctypes
+mirror agrees with the header; host-only entry points behave."""
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+import oracle as O
+from climaland_gb300 import _abi as A
+
+REPO = Path(__file__).resolve().parent.parent
+HEADER = REPO / "include" / "climaland_cuda.h"
+
+
+def header_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\*?\s*(clm_[a-z_0-9]+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import sys
+    sys.path.insert(0, str(REPO / "climaland.jl_gb300"))
+    import build as B
+    path = B.build()
+    return A.bind(ctypes.CDLL(str(path)))
+
+
+def test_header_and_mirror_agree():
+    assert header_functions() == sorted(A.declared_symbols())
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in header_functions():
+        assert hasattr(lib, name), name
+
+
+def test_config_struct_size_matches(lib):
+    # clm_config_default writes sizeof(clm_config) bytes; a larger guard
+    # buffer catches a size mismatch between ctypes and C.
+    buf = (ctypes.c_ubyte * (ctypes.sizeof(A.ClmConfig) + 64))()
+    for i in range(len(buf)):
+        buf[i] = 0xAB
+    lib.clm_config_default(ctypes.cast(buf, ctypes.POINTER(A.ClmConfig)))
+    tail = bytes(buf[ctypes.sizeof(A.ClmConfig):])
+    assert tail == b"\xab" * 64
+    c = A.ClmConfig.from_buffer_copy(bytes(buf[: ctypes.sizeof(A.ClmConfig)]))
+    d = A.default_config()
+    assert A.config_to_dict(c) == A.config_to_dict(d)
+
+
+def test_forcing_hash_matches_oracle(lib):
+    ol = O.lib()
+    for seed in (0, 7, 4000):
+        for c in (0, 1, 31, 1048575):
+            for k in (0, 1, 23, 191):
+                assert lib.clm_forcing_hash01(seed, c, k) == ol.clm_forcing_hash01(seed, c, k)
+
+
+def test_version(lib):
+    assert b"sm_103a" in lib.clm_version()
+
+
+def test_create_rejects_bad_config_before_touching_the_device(lib):
+    cfg = A.default_config()
+    cfg.ncol = 0
+    h = ctypes.c_void_p()
+    assert lib.clm_create(ctypes.byref(cfg), ctypes.byref(h)) == A.CLM_ERR_ARG
+    cfg.ncol = 10
+    cfg.bc_top_water = A.CLM_BC_FREE_DRAINAGE
+    assert lib.clm_create(ctypes.byref(cfg), ctypes.byref(h)) == A.CLM_ERR_ARG
+    assert lib.clm_last_error(None) == b"null handle"

@@ -1,0 +1,75 @@
+"""Closure-level GPU parity (clm_update_aux / clm_exp_tendency /
+clm_imp_tendency / clm_jacobian / clm_solve) against the oracle's closures."""
+import numpy as np
+import pytest
+
+import oracle as O
+from climaland_gb300 import _abi as A
+from climaland_gb300 import device as D
+from climaland_gb300 import workloads as WL
+from gpu_common import require_gpu
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-12  # pointwise closures: a few ulp of rearranged FP64 arithmetic
+
+
+@pytest.fixture(autouse=True)
+def _gpu():
+    require_gpu()
+
+
+def close(a, b, rtol=RTOL, atol=0.0):
+    a, b = np.asarray(a), np.asarray(b)
+    scale = np.maximum(np.abs(b), 1e-300)
+    bad = np.abs(a - b) > rtol * scale + atol
+    assert not bad.any(), f"max rel err {np.max(np.abs(a - b) / scale):.3e}"
+
+
+WORKLOADS = {
+    "richards": lambda: WL.richards_c0(ncol=256),
+    "eh": lambda: WL.energy_hydrology_c1(ncol=256),
+    "uneven": lambda: WL.uneven_c2(ncol=256),
+    "c4": lambda: WL.full_scale_c4(ncol=256),
+}
+
+
+@pytest.mark.parametrize("name", list(WORKLOADS))
+def test_closures(name):
+    w = WORKLOADS[name]()
+    eh = w.cfg.model == A.CLM_MODEL_ENERGY_HYDROLOGY
+    o = O.Oracle(w)
+    st = w.copy_state()
+    t = 3600.0 * 5.3
+    with D.SoilColumns(w) as g:
+        ag = g.update_aux(t)
+        ao = o.update_cache(st, t)
+        keys = ("K", "psi") + (("theta_l", "T", "kappa", "Tf") if eh else ())
+        for k in keys:
+            close(ag[k], ao[k], atol=1e-300)
+        close(ag["bc"], ao["bc"], atol=1e-25)
+        eg = g.exp_tendency(t)
+        eo = o.exp_tendency(st, t)
+        for a, b in zip(eg, eo):
+            # phase change of unfrozen cells is a rounding-level difference
+            sc = np.max(np.abs(b)) + 1e-300
+            assert np.max(np.abs(a - b)) <= 1e-9 * sc + 1e-18
+        ig = g.imp_tendency(t)
+        io = o.imp_tendency(st, t)
+        # face differences amplify rounding: compare against the flux scale
+        for a, b in zip(ig, io):
+            sc = np.max(np.abs(b)) + 1e-300
+            assert np.max(np.abs(a - b)) <= 1e-9 * sc
+        dtg = w.dt
+        Jg = g.jacobian(t, dtg)
+        Jo = o.jacobian(st, t, dtg)
+        for a, b in zip(Jg[: 3 if eh else 1], Jo[: 3 if eh else 1]):
+            close(a, b, rtol=1e-11, atol=1e-300)
+        rng = np.random.default_rng(0)
+        fv = rng.standard_normal(w.ncells)
+        fe = rng.standard_normal(w.ncells) * 1e5 if eh else None
+        dg = g.solve(Jo[0], Jo[1] if eh else None, Jo[2] if eh else None, fv, fe)
+        do = o.solve(Jo[0], Jo[1] if eh else None, Jo[2] if eh else None, fv, fe)
+        close(dg[0], do[0], rtol=1e-11, atol=1e-14)
+        if eh:
+            close(dg[1], do[1], rtol=1e-11, atol=1e-9)
