@@ -20,9 +20,11 @@
 
 namespace clm {
 // clm_step.cu
-cudaError_t launch_step(const StepArgs& A, int model, int precision, int wpc, double t0,
-                        double dt, int nsteps, cudaStream_t stream);
+cudaError_t launch_step(const StepArgs& A, int model, int precision, int wpc, int grid,
+                        double* scratch, double t0, double dt, int nsteps, cudaStream_t stream);
 size_t step_smem_bytes(int model, int precision, int nmax, int wpc);
+cudaError_t step_grid(int model, int precision, int nmax, int wpc, int ntiles, int* grid);
+size_t step_scratch_doubles(int model, int nmax, int wpc, int grid);
 // clm_layout.cu
 cudaError_t ref_to_internal(const Layout& L, const int32_t* ref_off, const double* src,
                             double* dst, int ncomp, cudaStream_t st);
@@ -63,7 +65,9 @@ struct clm_handle {
   double* d_colstage = nullptr;  // 4 * stride: upload staging, W, E, spare
   float* d_guess = nullptr;
   bool have_geometry = false, have_params = false, have_state = false;
-  int wpc = 1;
+  int wpc = 1;   // warps (32-column tiles) per CTA of the step kernel
+  int grid = 0;  // resident CTAs of the step kernel
+  double* d_scratch = nullptr;  // per-warp-slot frozen aux arrays
   Earth E{};
   EHScalars sc{};
 };
@@ -215,6 +219,10 @@ int build_layout(clm_handle* h, const std::vector<int>& nl) {
     return fail(h, CLM_ERR_ARG, "column depth " + std::to_string(h->nmax) +
                                     " needs more shared memory than the device offers");
   h->wpc = want;
+  CLM_CUDA(h, step_grid(h->cfg.model, h->cfg.precision, h->nmax, h->wpc, h->ntiles, &h->grid));
+  dfree(h->d_scratch);
+  const size_t nsc = step_scratch_doubles(h->cfg.model, h->nmax, h->wpc, h->grid);
+  if (nsc) CLM_CUDA(h, cudaMalloc(&h->d_scratch, sizeof(double) * nsc));
   return CLM_OK;
 }
 
@@ -418,6 +426,7 @@ void clm_destroy(clm_handle* h) {
   for (auto& p : h->d_forc) dfree(p);
   dfree(h->d_v); dfree(h->d_ti); dfree(h->d_e); dfree(h->d_Fw); dfree(h->d_Fe);
   dfree(h->d_flags); dfree(h->d_iters); dfree(h->d_stage); dfree(h->d_colstage); dfree(h->d_guess);
+  dfree(h->d_scratch);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   cudaGetLastError();
   delete h;
@@ -543,7 +552,8 @@ int clm_step_async(clm_handle* h, double t, double dt, int32_t nsteps) {
   const int chunk = 64;
   for (int s0 = 0; s0 < nsteps; s0 += chunk) {
     const int ns = std::min(chunk, nsteps - s0);
-    CLM_CUDA(h, launch_step(A, h->cfg.model, h->cfg.precision, h->wpc, t + s0 * dt, dt, ns, h->stream));
+    CLM_CUDA(h, launch_step(A, h->cfg.model, h->cfg.precision, h->wpc, h->grid, h->d_scratch,
+                            t + s0 * dt, dt, ns, h->stream));
   }
   return CLM_OK;
 }

@@ -23,6 +23,9 @@ namespace clm {
 
 template <int KIND>
 __global__ void closure_kernel(ClosureArgs C) {
+  __shared__ double tab[fm::TABLE_SIZE];
+  const Tables Tb = fm::stage_tables(tab);
+  __syncthreads();
   const StepArgs& A = C.A;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= A.L.stride) return;
@@ -60,19 +63,19 @@ __global__ void closure_kernel(ClosureArgs C) {
     const double Yti = eh ? C.ti[o + k] : 0.0;
     const double nu_eff = nu - Yti;
     double d;
-    psi_dpsi<false>(g, nu_eff, Yv, theta_r, S_s, psic[k], d);
+    psi_dpsi<false>(Tb, g, nu_eff, Yv, theta_r, S_s, psic[k], d);
     const Sat sK = saturation(nu, Yv, theta_r);
-    double K = conductivity(g, K_sat, sK.S);
+    double K = conductivity(Tb, g, K_sat, sK.S);
     if (eh) {
       const double Ye = C.e[o + k];
       const double v_safe = fmax(Yv, theta_r + kSqrtEps);
       const double nu_safe = fmax(nu_eff, theta_r + kSqrtEps);
       const double tl = (v_safe < nu_safe) ? v_safe : nu_safe;
       tlc[k] = tl;
-      kapc[k] = conductivity_heat(sc, tl, Yti, nu, kdry, ksu, ksf, lku, lkf, nuom, nuq, nug);
+      kapc[k] = conductivity_heat(Tb, sc, tl, Yti, nu, kdry, ksu, ksf, lku, lkf, nuom, nuq, nug);
       Tc[k] = temperature(E, Ye, Yti, heat_capacity(E, tl, Yti, rcds));
       const double fi = Yti / (tl + Yti - theta_r);
-      K *= exp(-sc.omega_ln10 * fi + sc.visc_gamma * (Tc[k] - sc.visc_gamma_T_ref));
+      K *= fm::exp(Tb, -sc.omega_ln10 * fi + sc.visc_gamma * (Tc[k] - sc.visc_gamma_T_ref));
     }
     Kc[k] = K;
   }
@@ -85,14 +88,14 @@ __global__ void closure_kernel(ClosureArgs C) {
   double Ftw = ftw, Fth = 0, Fbw = fbw, Fbh = 0;
   if (A.bc_tw == CLM_BC_STATE) {
     double pb, d;
-    psi_dpsi<false>(g, nu, ftw, theta_r, S_s, pb, d);
+    psi_dpsi<false>(Tb, g, nu, ftw, theta_r, S_s, pb, d);
     Ftw = -Kc[n - 1] * ((pb + half) - psic[n - 1]) / half;
   }
   if (A.bc_bw == CLM_BC_FREE_DRAINAGE) {
     Fbw = -1.0 * Kc[0];
   } else if (A.bc_bw == CLM_BC_STATE) {
     double pb, d;
-    psi_dpsi<false>(g, nu, fbw, theta_r, S_s, pb, d);
+    psi_dpsi<false>(Tb, g, nu, fbw, theta_r, S_s, pb, d);
     Fbw = -Kc[0] * ((psic[0] + half) - pb) / half;
   }
   if (eh) {
@@ -121,8 +124,8 @@ __global__ void closure_kernel(ClosureArgs C) {
           // (rho_ice, rho_liq) slots of soil_Tf_depressed (:35-52).
           const double Yti = C.ti[o + k];
           const double tt = fmin(E.rho_l / E.rho_i * Yti + tlc[k], nu);
-          const double pw = matric_of(g, nu, tt, theta_r);
-          C.Tf[o + k] = fmax(E.T_freeze * exp(E.grav_over_LH_f0 * pw), 1.0);
+          const double pw = matric_of(Tb, g, nu, tt, theta_r);
+          C.Tf[o + k] = fmax(E.T_freeze * fm::exp(Tb, E.grav_over_LH_f0 * pw), 1.0);
         }
       }
     }
@@ -139,22 +142,9 @@ __global__ void closure_kernel(ClosureArgs C) {
       double dv = 0.0, dti = 0.0;
       if (eh && A.phase_change) {
         const double Yti = C.ti[o + k];
-        // phase_change_source with thermal_time(rho c(theta_l, theta_i), dz, kappa)
+        uint32_t fl = 0;
         const double rc = heat_capacity(E, tlc[k], Yti, rcds);
-        const double theta_tot = fmin(E.rho_i_over_rho_l * Yti + tlc[k], nu);
-        const Sat ss = saturation(nu, theta_tot, theta_r);
-        const double pw = matric_of(g, nu, theta_tot, theta_r);
-        const double Tf = fmax(E.T_freeze * exp(E.grav_over_LH_f0 * pw), 1.0);
-        double th_star;
-        if (Tf - Tc[k] > kEps) {
-          const double p = pw + E.LH_f0_over_grav * log(Tc[k] / Tf);
-          const double x = exp(g.n * log(g.alpha * fabs(p)));
-          th_star = exp(-g.m * log1p(x)) * (nu - theta_r) + theta_r;
-        } else {
-          th_star = ss.S * (nu - theta_r) + theta_r;
-        }
-        const double tau = 3.0 * rc * (dz * dz) / kapc[k];
-        const double pc = (tlc[k] - th_star) / tau;
+        const double pc = phase_change(Tb, E, g, nu, theta_r, tlc[k], Yti, Tc[k], rc, kapc[k], dz, fl);
         dv = -pc;
         dti = E.rho_l_over_rho_i * pc;
       }
@@ -200,7 +190,7 @@ __global__ void closure_kernel(ClosureArgs C) {
     for (int k = 0; k < n; ++k) {
       double p;
       const double Yti = eh ? C.ti[o + k] : 0.0;
-      psi_dpsi<true>(g, nu - Yti, C.v[o + k], theta_r, S_s, p, D[k]);
+      psi_dpsi<true>(Tb, g, nu - Yti, C.v[o + k], theta_r, S_s, p, D[k]);
     }
     for (int blk = 0; blk < (eh ? 3 : 1); ++blk) {
       double* W = blk == 0 ? C.Wvv : (blk == 1 ? C.Wev : C.Wee);

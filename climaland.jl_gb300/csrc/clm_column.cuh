@@ -1,0 +1,516 @@
+// One soil column through nsteps IMEX ARS111 steps (host and device code).
+//
+// Reference path replaced (paths relative to the ClimaLand.jl tree):
+//   stage 1   make_exp_tendency = update_aux! + update_boundary_fluxes! +
+//             compute_exp_tendency! (models.jl:279-287; rre.jl:111-149,
+//             214-243, 368-380; energy_hydrology.jl:273-350, 722-906)
+//   stage 2   U = u + dt T_exp; Newton on U + dt T_imp(x) - x = 0 with
+//             W = dt dT_imp/dY - I from make_compute_jacobian (rre.jl:391-458;
+//             energy_hydrology.jl:466-576, including the "- I" on
+//             d(rho e)/d(vartheta)), cache_imp! = make_update_implicit_cache
+//             (models.jl:238-246; energy_hydrology.jl:427-455) run on U
+//             before the first iteration and after every update, and the
+//             block Thomas solve of initialize_jacobian
+//             (implicit_timestepping.jl:160-171)
+//   final     u_{n+1} = u + dt T_exp + dt (x - U) / dt
+//
+// Storage (accessed through Col<T>, a strided view; stride 32 on the
+// device where 32 columns are interleaved, 1 in a host replay):
+//   g*    state arrays in the internal layout. During a step they hold the
+//         stage value U (the explicit stage writes U over Y; U_e = Y_e), so
+//         U costs no on-chip storage; the final combination overwrites them.
+//   x*    Newton iterate, f_e residual, Thomas arrays: per-warp shared memory
+//   K, kappa, 1/rho c: frozen through the Newton solve, per-warp scratch
+//
+// Per Newton iteration, four sweeps:
+//   1 (up)    T, psi, dpsi at x in a rolling register window; face fluxes,
+//             residual, Jacobian rows and the Thomas forward elimination of
+//             the vartheta block, fused;
+//   2 (down)  back substitution: delta vartheta;
+//   3 (up)    energy right-hand side f_e - W_ev delta vartheta, forward
+//             elimination of the rho e block, x_v -= delta_v;
+//   4 (down)  back substitution: delta rho e, x_e -= delta_e.
+// JT is the Jacobian/Thomas type: double (plain path) or float (mixed path,
+// where an FP64 column-sum projection keeps the solve's exact budget identity).
+#pragma once
+
+#include "clm_internal.cuh"
+
+namespace clm {
+
+template <typename T>
+struct Col {
+  T* p;
+  int s;
+  CLM_HD T& operator[](int k) const { return p[(int64_t)k * s]; }
+};
+
+struct EHCol {
+  double nu, K_sat, S_s, theta_r;
+  VG g;
+  double kdry, ksf, ksu, rcds, nuom, nuq, nug, lku, lkf;
+  double dz, inv_dz;
+};
+
+CLM_HD EHCol load_eh_col(const StepArgs& A, int s, int n) {
+  const int st = A.L.stride;
+  const double* P = A.prm;
+  EHCol c;
+  c.nu = P[CLM_P_NU * st + s];
+  c.K_sat = P[CLM_P_K_SAT * st + s];
+  c.S_s = P[CLM_P_S_S * st + s];
+  c.theta_r = P[CLM_P_THETA_R * st + s];
+  c.g = make_vg(P[CLM_P_VG_ALPHA * st + s], P[CLM_P_VG_N * st + s]);
+  c.kdry = P[CLM_P_KAPPA_DRY * st + s];
+  c.ksf = P[CLM_P_KAPPA_SAT_FROZEN * st + s];
+  c.ksu = P[CLM_P_KAPPA_SAT_UNFROZEN * st + s];
+  c.rcds = P[CLM_P_RHOC_DS * st + s];
+  c.nuom = P[CLM_P_NU_SS_OM * st + s];
+  c.nuq = P[CLM_P_NU_SS_QUARTZ * st + s];
+  c.nug = P[CLM_P_NU_SS_GRAVEL * st + s];
+  c.lku = A.lkap[s];
+  c.lkf = A.lkap[st + s];
+  c.dz = (A.z_hi[s] - A.z_lo[s]) / n;
+  c.inv_dz = 1.0 / c.dz;
+  return c;
+}
+
+// T and psi at the Newton iterate (update_implicit_aux!,
+// energy_hydrology.jl:427-445) and dpsi/dvartheta for the Jacobian (:503-512).
+CLM_HD void eh_iterate_point(const Tables& Tb, const Earth& E, const EHCol& c, double xv,
+                             double xe, double ti, double& T, double& psi, double& D) {
+  const double nu_eff = c.nu - ti;
+  T = temperature(E, xe, ti, heat_capacity(E, fmin(nu_eff, xv), ti, c.rcds));
+  psi_dpsi<true>(Tb, c.g, nu_eff, xv, c.theta_r, c.S_s, psi, D);
+}
+
+struct EHBuffers {
+  Col<double> gv, gti, ge;          // state (holds U during a step)
+  Col<double> xv, xe, fe;           // iterate, energy residual
+  Col<double> K, kap, irc;          // frozen aux
+};
+
+template <typename JT>
+struct EHJac {
+  Col<JT> cp, dp, d, ae;            // Thomas c', d' (then delta_v, d''), dpsi, face coef
+};
+
+template <typename JT>
+CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int orig,
+                      const EHBuffers& B, const EHJac<JT>& J, double t0, double dt, int nsteps,
+                      double& Fw, double& Fe, uint32_t& flags, int& iters_done) {
+  const Earth& E = A.E;
+  const EHScalars& sc = A.sc;
+  const EHCol c = load_eh_col(A, s, n);
+  const int st = A.L.stride;
+  const double rdz = dt * c.inv_dz;
+  const double half = 0.5 * c.dz;
+  constexpr bool mixed = sizeof(JT) < sizeof(double);
+
+  for (int step = 0; step < nsteps; ++step) {
+    const double t = t0 + step * dt;
+    // ---------------- stage 1: aux at Y_n, explicit tendency, U ----------
+    double K0 = 0, T0 = 0, kap0 = 0, psi0 = 0;
+    double Kt = 0, Tt = 0, kapt = 0, psit = 0;
+    for (int k = 0; k < n; ++k) {
+      const double Yv = B.gv[k], Yti = B.gti[k], Ye = B.ge[k];
+      const double nu_eff = c.nu - Yti;
+      // volumetric_liquid_fraction (soil_hydrology_parameterizations.jl:22-31)
+      const double v_safe = fmax(Yv, c.theta_r + kSqrtEps);
+      const double nu_safe = fmax(nu_eff, c.theta_r + kSqrtEps);
+      const double tl = (v_safe < nu_safe) ? v_safe : nu_safe;
+      const double kap = conductivity_heat(Tb, sc, tl, Yti, c.nu, c.kdry, c.ksu, c.ksf, c.lku,
+                                           c.lkf, c.nuom, c.nuq, c.nug);
+      const double rc = heat_capacity(E, tl, Yti, c.rcds);
+      const double T = temperature(E, Ye, Yti, rc);
+      const Sat sK = saturation(c.nu, Yv, c.theta_r);
+      const double fi = Yti / (tl + Yti - c.theta_r);
+      // impedance_factor * viscosity_factor * hydraulic_conductivity
+      const double K =
+          fm::exp(Tb, -sc.omega_ln10 * fi + sc.visc_gamma * (T - sc.visc_gamma_T_ref)) *
+          conductivity(Tb, c.g, c.K_sat, sK.S);
+      double Uv = Yv, Uti = Yti;
+      if (A.phase_change) {
+        const double pc = phase_change(Tb, E, c.g, c.nu, c.theta_r, tl, Yti, T, rc, kap, c.dz, flags);
+        Uv = Yv + dt * (-pc);
+        Uti = Yti + dt * (E.rho_l_over_rho_i * pc);
+      }
+      B.gv[k] = Uv;
+      B.gti[k] = Uti;
+      B.xv[k] = Uv;
+      B.xe[k] = Ye;
+      B.K[k] = K;
+      B.kap[k] = kap;
+      B.irc[k] = 1.0 / heat_capacity(E, tl, Uti, c.rcds);
+      if (k == 0) {
+        K0 = K; T0 = T; kap0 = kap;
+        if (A.bc_bw == CLM_BC_STATE) {
+          double d;
+          psi_dpsi<false>(Tb, c.g, nu_eff, Yv, c.theta_r, c.S_s, psi0, d);
+        }
+      }
+      if (k == n - 1) {
+        Kt = K; Tt = T; kapt = kap;
+        if (A.bc_tw == CLM_BC_STATE) {
+          double d;
+          psi_dpsi<false>(Tb, c.g, nu_eff, Yv, c.theta_r, c.S_s, psit, d);
+        }
+      }
+    }
+    // boundary fluxes at t, frozen through the Newton solve
+    double Ftw, Fth, Fbw, Fbh;
+    {
+      const double ftw = forcing_value(A.forc[CLM_BC_TOP_WATER], st, s, orig, t, A.seed);
+      const double fth = forcing_value(A.forc[CLM_BC_TOP_HEAT], st, s, orig, t, A.seed);
+      const double fbw = forcing_value(A.forc[CLM_BC_BOTTOM_WATER], st, s, orig, t, A.seed);
+      const double fbh = forcing_value(A.forc[CLM_BC_BOTTOM_HEAT], st, s, orig, t, A.seed);
+      if (A.bc_tw == CLM_BC_STATE) {
+        double pb, d;
+        psi_dpsi<false>(Tb, c.g, c.nu, ftw, c.theta_r, c.S_s, pb, d);
+        Ftw = -Kt * ((pb + half) - psit) / half;  // diffusive_flux
+      } else {
+        Ftw = ftw;
+      }
+      if (A.bc_bw == CLM_BC_FREE_DRAINAGE) {
+        Fbw = -1.0 * K0;
+      } else if (A.bc_bw == CLM_BC_STATE) {
+        double pb, d;
+        psi_dpsi<false>(Tb, c.g, c.nu, fbw, c.theta_r, c.S_s, pb, d);
+        Fbw = -K0 * ((psi0 + half) - pb) / half;
+      } else {
+        Fbw = fbw;
+      }
+      if (A.bc_th == CLM_BC_STATE) {
+        Fth = -kapt * (fth - Tt) / half;
+      } else if (A.bc_th == CLM_BC_FLUX_ADVECTIVE) {
+        const double* F = A.forc[CLM_BC_TOP_HEAT];
+        const double Tadv = F ? F[CLM_F_T_ADV * st + s] : E.T_0;
+        Fth = fth + Ftw * rho_e_liq(E, Tadv);
+      } else {
+        Fth = fth;
+      }
+      if (A.bc_bh == CLM_BC_FREE_DRAINAGE) {
+        Fbh = -1.0 * K0 * rho_e_liq(E, T0);
+      } else if (A.bc_bh == CLM_BC_STATE) {
+        Fbh = -kap0 * (T0 - fbh) / half;
+      } else {
+        Fbh = fbh;
+      }
+    }
+    const double UFw = Fw, UFe = Fe;
+    double xFw = UFw, xFe = UFe;
+
+    // ---------------- stage 2: Newton ------------------------------------
+    double prev_norm = 1e300;
+    for (int it = 1; it <= A.max_iters; ++it) {
+      // sweep 1 (bottom -> top)
+      JT cp_prev = 0, dp_prev = 0;
+      double Fw_dn = Fbw, Fe_dn = Fbh;
+      double aw_dn = 0.0;
+      JT D_prev = 0;
+      double sum_fv = 0.0, sum_fe = 0.0;
+      double Tc, psic, Dc;
+      eh_iterate_point(Tb, E, c, B.xv[0], B.xe[0], B.gti[0], Tc, psic, Dc);
+      double Kc = B.K[0], kapc = B.kap[0];
+      double relKc = rho_e_liq(E, Tc) * Kc;
+      for (int k = 0; k < n; ++k) {
+        double Fw_up, Fe_up, aw_up = 0.0, ae_up = 0.0;
+        double Tn = 0, psin = 0, Dn = 0, Kn = 0, kapn = 0, relKn = 0;
+        if (k < n - 1) {
+          eh_iterate_point(Tb, E, c, B.xv[k + 1], B.xe[k + 1], B.gti[k + 1], Tn, psin, Dn);
+          Kn = B.K[k + 1];
+          kapn = B.kap[k + 1];
+          relKn = rho_e_liq(E, Tn) * Kn;
+          aw_up = 0.5 * (Kc + Kn) * c.inv_dz;
+          const double ak_up = 0.5 * (kapc + kapn) * c.inv_dz;
+          ae_up = 0.5 * (relKc + relKn) * c.inv_dz;
+          const double dh = (psin - psic) + c.dz;
+          Fw_up = -aw_up * dh;
+          Fe_up = -ak_up * (Tn - Tc) - ae_up * dh;
+        } else {
+          Fw_up = Ftw;
+          Fe_up = Fth;
+        }
+        const double Tv = -((Fw_up - Fw_dn) * c.inv_dz);
+        const double Tee = -((Fe_up - Fe_dn) * c.inv_dz);
+        const double fv = B.gv[k] + dt * Tv - B.xv[k];
+        const double fe = B.ge[k] + dt * Tee - B.xe[k];
+        sum_fv += fv;
+        sum_fe += fe;
+        const JT L = (JT)(rdz * aw_dn) * D_prev;
+        const JT U = (k < n - 1) ? (JT)(rdz * aw_up * Dn) : (JT)0;
+        const JT M = (JT)(-rdz * (aw_up + aw_dn) * Dc - 1.0);
+        const JT inv = (JT)1 / (M - L * cp_prev);
+        const JT cpk = U * inv;
+        const JT dpk = ((JT)fv - L * dp_prev) * inv;
+        J.cp[k] = cpk;
+        J.dp[k] = dpk;
+        J.d[k] = (JT)Dc;
+        J.ae[k] = (JT)ae_up;
+        B.fe[k] = fe;
+        cp_prev = cpk;
+        dp_prev = dpk;
+        Fw_dn = Fw_up;
+        Fe_dn = Fe_up;
+        aw_dn = aw_up;
+        D_prev = (JT)Dc;
+        Tc = Tn; psic = psin; Dc = Dn; Kc = Kn; kapc = kapn; relKc = relKn;
+      }
+      // integrated fluxes (their Jacobian block is -I): x += f
+      const double fFw = UFw + dt * (-(Ftw - Fbw)) - xFw;
+      const double fFe = UFe + dt * (-(Fth - Fbh)) - xFe;
+      xFw += fFw;
+      xFe += fFe;
+      // sweep 2 (top -> bottom): delta vartheta into dp
+      double sdv = 0.0;
+      {
+        JT nxt = 0;
+        for (int k = n - 1; k >= 0; --k) {
+          const JT d = J.dp[k] - J.cp[k] * nxt;
+          J.dp[k] = d;
+          nxt = d;
+          if (mixed) sdv += (double)d;
+        }
+      }
+      // FP64 column-sum projection (mixed path): sum(delta_v) = -sum(f_v)
+      const double corr_v = mixed ? (sdv + sum_fv) / n : 0.0;
+      double norm2 = fFw * fFw + fFe * fFe;
+      // sweep 3 (bottom -> top): energy right-hand side, rho e forward
+      // elimination (c'' into cp, d'' into dp behind the read of delta_v)
+      {
+        JT c_prev = 0, d_prev = 0;
+        double ak_dn = 0.0;
+        JT dvm = 0, Dm = 0;
+        JT dv0 = J.dp[0] - (JT)corr_v, D0 = J.d[0];
+        JT ae_dn = 0;
+        double kap_c = B.kap[0], irc_c = B.irc[0], irc_m = 0.0;
+        for (int k = 0; k < n; ++k) {
+          JT dvp = 0, Dp = 0, ae_up = 0;
+          double ak_up = 0.0, kap_n = 0.0, irc_n = 0.0;
+          if (k < n - 1) {
+            dvp = J.dp[k + 1] - (JT)corr_v;
+            Dp = J.d[k + 1];
+            ae_up = J.ae[k];
+            kap_n = B.kap[k + 1];
+            irc_n = B.irc[k + 1];
+            ak_up = 0.5 * (kap_c + kap_n) * c.inv_dz;
+          }
+          const JT Gup = (k < n - 1) ? (Dp * dvp - D0 * dv0) : (JT)0;
+          const JT Gdn = (k > 0) ? (D0 * dv0 - Dm * dvm) : (JT)0;
+          const JT wev = (JT)rdz * (ae_up * Gup - ae_dn * Gdn) - dv0;
+          const double g = B.fe[k] - (double)wev;
+          const JT L = (JT)(rdz * ak_dn * irc_m);
+          const JT U = (JT)(rdz * ak_up * irc_n);
+          const JT M = (JT)(-rdz * (ak_up + ak_dn) * irc_c - 1.0);
+          const JT inv = (JT)1 / (M - L * c_prev);
+          const JT ck = U * inv;
+          const JT dk = ((JT)g - L * d_prev) * inv;
+          J.cp[k] = ck;
+          J.dp[k] = dk;
+          c_prev = ck;
+          d_prev = dk;
+          const double dvd = (double)dv0;
+          B.xv[k] -= dvd;
+          norm2 += dvd * dvd;
+          dvm = dv0; Dm = D0; dv0 = dvp; D0 = Dp;
+          ae_dn = ae_up;
+          ak_dn = ak_up;
+          irc_m = irc_c; irc_c = irc_n; kap_c = kap_n;
+        }
+      }
+      // sweep 4 (top -> bottom): delta rho e
+      {
+        const double se = A.energy_scale;
+        JT nxt = 0;
+        if (mixed) {
+          double sde = 0.0;
+          for (int k = n - 1; k >= 0; --k) {
+            const JT d = J.dp[k] - J.cp[k] * nxt;
+            J.dp[k] = d;
+            sde += (double)d;
+            nxt = d;
+          }
+          // W_ee and W_ev + I have zero column sums:
+          // sum(delta_e) = -sum(f_e) - sum(delta_v) = -sum(f_e) + sum(f_v)
+          const double corr_e = (sde + sum_fe - sum_fv) / n;
+          for (int k = 0; k < n; ++k) {
+            const double d = (double)J.dp[k] - corr_e;
+            B.xe[k] -= d;
+            norm2 += (se * d) * (se * d);
+          }
+        } else {
+          for (int k = n - 1; k >= 0; --k) {
+            const JT d = J.dp[k] - J.cp[k] * nxt;
+            nxt = d;
+            B.xe[k] -= (double)d;
+            norm2 += (se * (double)d) * (se * (double)d);
+          }
+        }
+      }
+      iters_done = it;
+      if (A.newton_mode == CLM_NEWTON_TOL) {
+        const double nrm = sqrt(norm2);
+        if (nrm > prev_norm && it > 2) flags |= CLM_COL_DIVERGED;
+        prev_norm = nrm;
+        if (nrm < A.tol) break;
+        if (it == A.max_iters) flags |= CLM_COL_NOT_CONVERGED;
+      }
+    }
+    // ---------------- final combination ---------------------------------
+    const double inv_dt = 1.0 / dt;
+    for (int k = 0; k < n; ++k) {
+      const double Uv = B.gv[k], Ue = B.ge[k];
+      B.gv[k] = Uv + dt * ((B.xv[k] - Uv) * inv_dt);
+      B.ge[k] = Ue + dt * ((B.xe[k] - Ue) * inv_dt);
+    }
+    Fw = UFw + dt * ((xFw - UFw) * inv_dt);
+    Fe = UFe + dt * ((xFe - UFe) * inv_dt);
+  }
+  bool finite = isfinite(Fw) && isfinite(Fe);
+  for (int k = 0; k < n; ++k) finite = finite && isfinite(B.gv[k]) && isfinite(B.gti[k]) && isfinite(B.ge[k]);
+  if (!finite) flags |= CLM_COL_NONFINITE;
+}
+
+// ---------------------------------------------------------------------------
+// RichardsModel
+// ---------------------------------------------------------------------------
+
+struct RBuffers {
+  Col<double> gv;   // state (U = u during a step: no explicit tendency)
+  Col<double> xv;   // iterate
+};
+
+template <typename JT>
+struct RJac {
+  Col<JT> cp, dp;
+};
+
+template <typename JT>
+CLM_HD void richards_column(const StepArgs& A, const Tables& Tb, int s, int n, int orig,
+                            const RBuffers& B, const RJac<JT>& J, double t0, double dt,
+                            int nsteps, double& Fw, uint32_t& flags, int& iters_done) {
+  const int st = A.L.stride;
+  const double* P = A.prm;
+  const double nu = P[CLM_P_NU * st + s];
+  const double K_sat = P[CLM_P_K_SAT * st + s];
+  const double S_s = P[CLM_P_S_S * st + s];
+  const double theta_r = P[CLM_P_THETA_R * st + s];
+  const VG g = make_vg(P[CLM_P_VG_ALPHA * st + s], P[CLM_P_VG_N * st + s]);
+  const double dz = (A.z_hi[s] - A.z_lo[s]) / n;
+  const double inv_dz = 1.0 / dz;
+  const double half = 0.5 * dz;
+  const double rdz = dt * inv_dz;
+  constexpr bool mixed = sizeof(JT) < sizeof(double);
+  // MoistureStateBC at the top carries dfluxBCdY (rre.jl:137-146, 460-468):
+  // the boundary fluxes are then refreshed with the implicit cache.
+  const bool dflux = (A.bc_tw == CLM_BC_STATE);
+
+  for (int step = 0; step < nsteps; ++step) {
+    const double t = t0 + step * dt;
+    for (int k = 0; k < n; ++k) B.xv[k] = B.gv[k];
+    const double UFw = Fw;
+    double xFw = UFw;
+    const double t_bc = dflux ? t + dt : t;
+    const double ftw = forcing_value(A.forc[CLM_BC_TOP_WATER], st, s, orig, t_bc, A.seed);
+    const double fbw = forcing_value(A.forc[CLM_BC_BOTTOM_WATER], st, s, orig, t_bc, A.seed);
+    double psi_tb = 0.0, psi_bb = 0.0;
+    if (A.bc_tw == CLM_BC_STATE) { double d; psi_dpsi<false>(Tb, g, nu, ftw, theta_r, S_s, psi_tb, d); }
+    if (A.bc_bw == CLM_BC_STATE) { double d; psi_dpsi<false>(Tb, g, nu, fbw, theta_r, S_s, psi_bb, d); }
+    // without dfluxBCdY the fluxes are those of the explicit stage at (u, t);
+    // U = u, so iteration 1 (x = U) evaluates exactly those
+    double Ftw = ftw, Fbw = fbw;
+    double prev_norm = 1e300;
+    for (int it = 1; it <= A.max_iters; ++it) {
+      const bool refresh_bc = dflux || it == 1;
+      JT cp_prev = 0, dp_prev = 0;
+      double aw_dn = 0.0;
+      JT D_prev = 0;
+      double sum_f = 0.0;
+      double Kc, psic, Dc;
+      richards_point<true>(Tb, g, nu, B.xv[0], theta_r, S_s, K_sat, Kc, psic, Dc);
+      if (refresh_bc) {
+        if (A.bc_bw == CLM_BC_FREE_DRAINAGE) Fbw = -1.0 * Kc;
+        else if (A.bc_bw == CLM_BC_STATE) Fbw = -Kc * ((psic + half) - psi_bb) / half;
+      }
+      double Fw_dn = Fbw;
+      for (int k = 0; k < n; ++k) {
+        double Fw_up, aw_up = 0.0;
+        double Kn = 0, psin = 0, Dn = 0;
+        double Md_extra = 0.0;
+        if (k < n - 1) {
+          richards_point<true>(Tb, g, nu, B.xv[k + 1], theta_r, S_s, K_sat, Kn, psin, Dn);
+          aw_up = 0.5 * (Kc + Kn) * inv_dz;
+          Fw_up = -aw_up * ((psin - psic) + dz);
+        } else {
+          if (refresh_bc && A.bc_tw == CLM_BC_STATE) Ftw = -Kc * ((psi_tb + half) - psic) / half;
+          // set_dfluxBCdY! (boundary_conditions.jl:375-426): K_N dpsi_N / dz_top
+          if (dflux) Md_extra = -dt * ((Kc * Dc / half) * inv_dz);
+          Fw_up = Ftw;
+        }
+        const double Tv = -((Fw_up - Fw_dn) * inv_dz);
+        const double f = B.gv[k] + dt * Tv - B.xv[k];
+        sum_f += f;
+        const JT L = (JT)(rdz * aw_dn) * D_prev;
+        const JT U = (k < n - 1) ? (JT)(rdz * aw_up * Dn) : (JT)0;
+        const JT M = (JT)(-rdz * (aw_up + aw_dn) * Dc - 1.0 + Md_extra);
+        const JT inv = (JT)1 / (M - L * cp_prev);
+        const JT cpk = U * inv;
+        const JT dpk = ((JT)f - L * dp_prev) * inv;
+        J.cp[k] = cpk;
+        J.dp[k] = dpk;
+        cp_prev = cpk;
+        dp_prev = dpk;
+        Fw_dn = Fw_up;
+        aw_dn = aw_up;
+        D_prev = (JT)Dc;
+        Kc = Kn; psic = psin; Dc = Dn;
+      }
+      const double fFw = UFw + dt * (-(Ftw - Fbw)) - xFw;
+      xFw += fFw;
+      double norm2 = fFw * fFw;
+      if (mixed) {
+        JT nxt = 0;
+        double sd = 0.0;
+        for (int k = n - 1; k >= 0; --k) {
+          const JT d = J.dp[k] - J.cp[k] * nxt;
+          J.dp[k] = d;
+          sd += (double)d;
+          nxt = d;
+        }
+        const double corr = dflux ? 0.0 : (sd + sum_f) / n;
+        for (int k = 0; k < n; ++k) {
+          const double d = (double)J.dp[k] - corr;
+          B.xv[k] -= d;
+          norm2 += d * d;
+        }
+      } else {
+        JT nxt = 0;
+        for (int k = n - 1; k >= 0; --k) {
+          const JT d = J.dp[k] - J.cp[k] * nxt;
+          nxt = d;
+          B.xv[k] -= (double)d;
+          norm2 += (double)d * (double)d;
+        }
+      }
+      iters_done = it;
+      if (A.newton_mode == CLM_NEWTON_TOL) {
+        const double nrm = sqrt(norm2);
+        if (nrm > prev_norm && it > 2) flags |= CLM_COL_DIVERGED;
+        prev_norm = nrm;
+        if (nrm < A.tol) break;
+        if (it == A.max_iters) flags |= CLM_COL_NOT_CONVERGED;
+      }
+    }
+    const double inv_dt = 1.0 / dt;
+    for (int k = 0; k < n; ++k) {
+      const double Uv = B.gv[k];
+      B.gv[k] = Uv + dt * ((B.xv[k] - Uv) * inv_dt);
+    }
+    Fw = UFw + dt * ((xFw - UFw) * inv_dt);
+  }
+  bool finite = isfinite(Fw);
+  for (int k = 0; k < n; ++k) finite = finite && isfinite(B.gv[k]);
+  if (!finite) flags |= CLM_COL_NONFINITE;
+}
+
+}  // namespace clm

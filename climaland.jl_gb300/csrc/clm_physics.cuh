@@ -1,18 +1,20 @@
-// Pointwise soil physics on the device.
+// Pointwise soil physics (host and device).
 //
 // Same mathematics as the reference closures
 //   src/standalone/Soil/soil_hydrology_parameterizations.jl (a2-a9)
 //   src/standalone/Soil/soil_heat_parameterizations.jl      (a11-a15)
-// rearranged for the GPU: every power is exp(b * log(a)) and the logs and
-// exponentials that psi, dpsi/dvartheta and K have in common are computed
-// once per point (one S^(-1/m), one log(S^(-1/m) - 1) per evaluation instead
-// of the reference's five pow calls). Results agree with the reference
-// formulas to a few ulp; the oracle comparison in tests/ holds them to 1e-10.
+// rearranged for a GPU with a narrow FP64 pipe: every power a^b is
+// exp(b log a) with the table-driven exp/log of clm_fastmath.cuh, and the
+// logs and exponentials that psi, dpsi/dvartheta and K have in common are
+// computed once per point. Where the reference rounds an intermediate (for
+// example 1 - S^(1/m) before raising it to m) the same intermediate is
+// rounded here, so cancellation behaves the same way in both.
 #pragma once
 
 #include <cstdint>
 
 #include "../../include/climaland_cuda.h"
+#include "clm_fastmath.cuh"
 
 #ifndef CLM_HD
 #define CLM_HD __host__ __device__ __forceinline__
@@ -23,6 +25,8 @@ namespace clm {
 constexpr double kSqrtEps = 1.4901161193847656e-08;  // sqrt(eps(Float64))
 constexpr double kEps = 2.220446049250313e-16;       // eps(Float64)
 constexpr double kLn10 = 2.302585092994045684;
+
+using fm::Tables;
 
 // Physical constants, derived once per handle (LandParameters fields).
 struct Earth {
@@ -96,21 +100,18 @@ CLM_HD Sat saturation(double nu_eff, double vartheta, double theta_r) {
 
 // pressure_head (:109-127) and dpsidvartheta (:135-152) at one point,
 // sharing S^(-1/m) and log(S^(-1/m) - 1). want_d selects the derivative.
-//   psi = -(S^(-1/m) - 1)^(1/n) / alpha                      (S <= 1)
-//       = (vartheta_safe - nu_safe) / S_s                     (S > 1)
+//   psi  = -(S^(-1/m) - 1)^(1/n) / alpha                 (S <= 1)
+//        = (vartheta_safe - nu_safe) / S_s                (S > 1)
 //   dpsi = (S^(-1/m) - 1)^(1/n - 1) S^(-1/m - 1) / (alpha m n (nu_safe - theta_r))
-//        = 1 / S_s                                            (S >= 1)
+//        = 1 / S_s                                        (S >= 1)
 template <bool want_d>
-__device__ __forceinline__ void psi_dpsi(const VG& g, double nu_eff,
-                                         double vartheta, double theta_r,
-                                         double S_s, double& psi,
-                                         double& dpsi) {
+CLM_HD void psi_dpsi(const Tables& T, const VG& g, double nu_eff, double vartheta,
+                     double theta_r, double S_s, double& psi, double& dpsi) {
   Sat s = saturation(nu_eff, vartheta, theta_r);
   if (s.S < 1.0) {
-    double u = exp(-g.inv_m * log(s.S));  // S^(-1/m)
-    double w = u - 1.0;
-    double lw = log(w);
-    double w1n = exp(g.inv_n * lw);  // w^(1/n)
+    const double u = fm::exp(T, -g.inv_m * fm::log(T, s.S));  // S^(-1/m)
+    const double w = u - 1.0;
+    const double w1n = fm::exp(T, g.inv_n * fm::log(T, w));  // w^(1/n)
     psi = -w1n * g.inv_alpha;
     if (want_d) dpsi = g.coef_d * w1n * u / (w * s.S * (s.nu_safe - theta_r));
   } else {
@@ -120,36 +121,32 @@ __device__ __forceinline__ void psi_dpsi(const VG& g, double nu_eff,
   }
 }
 
-// hydraulic_conductivity (:161-173) of effective_saturation(nu, vartheta):
+// hydraulic_conductivity (:161-173) of an effective saturation S:
 //   K = K_sat sqrt(S) (1 - (1 - S^(1/m))^m)^2 (S < 1), K_sat otherwise.
-__device__ __forceinline__ double conductivity(const VG& g, double K_sat,
-                                               double S) {
+CLM_HD double conductivity(const Tables& T, const VG& g, double K_sat, double S) {
   if (!(S < 1.0)) return K_sat;
-  double s1m = exp(g.inv_m * log(S));          // S^(1/m)
-  double t = exp(g.m * log1p(-s1m));           // (1 - S^(1/m))^m
-  double f = 1.0 - t;
+  const double s1m = fm::exp(T, g.inv_m * fm::log(T, S));  // S^(1/m)
+  const double t = fm::exp(T, g.m * fm::log(T, 1.0 - s1m));  // (1 - S^(1/m))^m
+  const double f = 1.0 - t;
   return K_sat * (sqrt(S) * f * f);
 }
 
-// Richards: K and psi (and dpsi) sharing log(S) (nu_eff = nu).
+// Richards point: K, psi (and dpsi) sharing log(S) (nu_eff = nu).
 template <bool want_d>
-__device__ __forceinline__ void richards_point(const VG& g, double nu,
-                                               double vartheta, double theta_r,
-                                               double S_s, double K_sat,
-                                               double& K, double& psi,
-                                               double& dpsi) {
+CLM_HD void richards_point(const Tables& T, const VG& g, double nu, double vartheta,
+                           double theta_r, double S_s, double K_sat, double& K, double& psi,
+                           double& dpsi) {
   Sat s = saturation(nu, vartheta, theta_r);
   if (s.S < 1.0) {
-    double lS = log(s.S);
-    double u = exp(-g.inv_m * lS);  // S^(-1/m)
-    double w = u - 1.0;
-    double lw = log(w);
-    double w1n = exp(g.inv_n * lw);
+    const double lS = fm::log(T, s.S);
+    const double u = fm::exp(T, -g.inv_m * lS);  // S^(-1/m)
+    const double w = u - 1.0;
+    const double w1n = fm::exp(T, g.inv_n * fm::log(T, w));
     psi = -w1n * g.inv_alpha;
     if (want_d) dpsi = g.coef_d * w1n * u / (w * s.S * (s.nu_safe - theta_r));
-    double s1m = 1.0 / u;  // S^(1/m)
-    double t = exp(g.m * log1p(-s1m));
-    double f = 1.0 - t;
+    const double s1m = fm::exp(T, g.inv_m * lS);  // S^(1/m)
+    const double t = fm::exp(T, g.m * fm::log(T, 1.0 - s1m));
+    const double f = 1.0 - t;
     K = K_sat * (sqrt(s.S) * f * f);
   } else {
     psi = (s.S <= 1.0) ? -0.0 : (s.v_safe - s.nu_safe) / S_s;
@@ -158,60 +155,91 @@ __device__ __forceinline__ void richards_point(const VG& g, double nu,
   }
 }
 
-// matric_potential of effective_saturation(nu, theta_tot) (used by
-// soil_Tf_depressed and phase_change_source).
-__device__ __forceinline__ double matric_of(const VG& g, double nu,
-                                            double theta, double theta_r) {
+// matric_potential of effective_saturation(nu, theta) (soil_Tf_depressed,
+// phase_change_source). Returns S through *S_out.
+CLM_HD double matric_of(const Tables& T, const VG& g, double nu, double theta,
+                        double theta_r, double* S_out = nullptr) {
   Sat s = saturation(nu, theta, theta_r);
-  double u = exp(-g.inv_m * log(s.S));
-  double w = u - 1.0;
-  if (!(w > 0.0)) return -0.0;  // S >= 1 (theta_tot <= nu keeps S <= 1)
-  return -exp(g.inv_n * log(w)) * g.inv_alpha;
+  if (S_out) *S_out = s.S;
+  const double u = fm::exp(T, -g.inv_m * fm::log(T, s.S));
+  const double w = u - 1.0;
+  if (!(w > 0.0)) return -0.0;  // S >= 1 (theta <= nu keeps S <= 1)
+  return -fm::exp(T, g.inv_n * fm::log(T, w)) * g.inv_alpha;
 }
 
 // volumetric_heat_capacity (soil_heat_parameterizations.jl:157-171)
-CLM_HD double heat_capacity(const Earth& E, double theta_l, double theta_i,
-                            double rhoc_ds) {
+CLM_HD double heat_capacity(const Earth& E, double theta_l, double theta_i, double rhoc_ds) {
   return rhoc_ds + theta_l * E.rhocp_l + theta_i * E.rhocp_i;
 }
 
 // temperature_from_ρe_int (:180-192)
-CLM_HD double temperature(const Earth& E, double rho_e, double theta_i,
-                          double rhoc) {
+CLM_HD double temperature(const Earth& E, double rho_e, double theta_i, double rhoc) {
   return E.T_0 + (rho_e + theta_i * E.rho_i_LH_f0) / rhoc;
 }
 
 // volumetric_internal_energy_liq (:221-231)
-CLM_HD double rho_e_liq(const Earth& E, double T) {
-  return E.rhocp_l * (T - E.T_0);
-}
+CLM_HD double rho_e_liq(const Earth& E, double T) { return E.rhocp_l * (T - E.T_0); }
 
-// Thermal conductivity kappa (energy_hydrology.jl:756-768):
-// Balland-Arp Kersten number (:301-320) and kappa_sat (:243-256) with
-// log(kappa_sat_unfrozen), log(kappa_sat_frozen) precomputed per column.
-__device__ __forceinline__ double conductivity_heat(
-    const EHScalars& sc, double theta_l, double theta_i, double nu,
-    double kappa_dry, double k_unfrozen, double k_frozen, double lku,
-    double lkf, double nu_om, double nu_quartz, double nu_gravel) {
-  double S_r = (theta_l + theta_i) / nu;  // relative_saturation
+// Thermal conductivity kappa (energy_hydrology.jl:756-768): Balland-Arp
+// Kersten number (:301-320) and kappa_sat (:243-256), with
+// log(kappa_sat_unfrozen) and log(kappa_sat_frozen) precomputed per column.
+CLM_HD double conductivity_heat(const Tables& T, const EHScalars& sc, double theta_l,
+                                double theta_i, double nu, double kappa_dry, double k_unfrozen,
+                                double k_frozen, double lku, double lkf, double nu_om,
+                                double nu_quartz, double nu_gravel) {
+  const double S_r = (theta_l + theta_i) / nu;  // relative_saturation
   double K_e;
   if (theta_i < kEps) {
-    double a = (1.0 + nu_om - sc.kersten_alpha * nu_quartz - nu_gravel) * 0.5;
-    double t1 = 1.0 + exp(-sc.kersten_beta * S_r);
-    double t1m3 = 1.0 / (t1 * t1 * t1);
-    double h = (1.0 - S_r) * 0.5;
-    double base = t1m3 - h * h * h;
-    K_e = exp(a * log(S_r) + (1.0 - nu_om) * log(base));
+    const double a = (1.0 + nu_om - sc.kersten_alpha * nu_quartz - nu_gravel) * 0.5;
+    const double t1 = 1.0 + fm::exp(T, -sc.kersten_beta * S_r);
+    const double t1m3 = 1.0 / (t1 * t1 * t1);
+    const double h = (1.0 - S_r) * 0.5;
+    const double base = t1m3 - h * h * h;
+    K_e = fm::exp(T, a * fm::log(T, S_r) + (1.0 - nu_om) * fm::log(T, base));
   } else {
-    K_e = exp((1.0 + nu_om) * log(S_r));
+    K_e = fm::exp(T, (1.0 + nu_om) * fm::log(T, S_r));
   }
-  double theta_w = theta_l + theta_i;
+  const double theta_w = theta_l + theta_i;
   double ksat;
   if (theta_w < kEps)
     ksat = 0.5 * (k_unfrozen + k_frozen);
+  else if (theta_i == 0.0)
+    ksat = k_unfrozen;  // k_u^1 k_f^0
   else
-    ksat = exp((theta_l * lku + theta_i * lkf) / theta_w);
+    ksat = fm::exp(T, (theta_l * lku + theta_i * lkf) / theta_w);
   return K_e * ksat + (1.0 - K_e) * kappa_dry;
+}
+
+// Phase-change source (soil_heat_parameterizations.jl:89-122) including
+// thermal_time (:60-62): (theta_l - theta_star) / tau,
+// tau = 3 rho c dz^2 / kappa. For T >= T_freeze the heaviside factor is
+// zero without evaluating Tf (Tf <= T_freeze), and theta_star is then
+// inverse_matric_potential(matric_potential(S)) = S (nu - theta_r) + theta_r.
+CLM_HD double phase_change(const Tables& T, const Earth& E, const VG& g, double nu,
+                           double theta_r, double theta_l, double theta_i, double Tk,
+                           double rhoc, double kappa, double dz, uint32_t& flags) {
+  const double theta_tot = fmin(E.rho_i_over_rho_l * theta_i + theta_l, nu);
+  double theta_star;
+  double S;
+  if (Tk >= E.T_freeze) {
+    S = saturation(nu, theta_tot, theta_r).S;
+    theta_star = S * (nu - theta_r) + theta_r;
+  } else {
+    const double psi_w0 = matric_of(T, g, nu, theta_tot, theta_r, &S);
+    const double Tf = fmax(E.T_freeze * fm::exp(T, E.grav_over_LH_f0 * psi_w0), 1.0);
+    if (Tf - Tk > kEps) {  // heaviside(Tf - T)
+      const double psi = psi_w0 + E.LH_f0_over_grav * fm::log(T, Tk / Tf);
+      if (psi > 0.0) flags |= CLM_COL_PSI_POSITIVE;
+      const double x = fm::exp(T, g.n * fm::log(T, g.alpha * fabs(psi)));  // (alpha|psi|)^n
+      const double Sst = fm::exp(T, -g.m * fm::log(T, 1.0 + x));         // (1 + x)^(-m)
+      theta_star = Sst * (nu - theta_r) + theta_r;
+    } else {
+      if (psi_w0 > 0.0) flags |= CLM_COL_PSI_POSITIVE;
+      theta_star = S * (nu - theta_r) + theta_r;
+    }
+  }
+  const double tau = 3.0 * rhoc * (dz * dz) / kappa;
+  return (theta_l - theta_star) / tau;
 }
 
 // counter hash of the rain-pulse forcing (splitmix64 finaliser, Vigna):
@@ -230,17 +258,15 @@ CLM_HD double hash01(uint64_t seed, uint64_t column, int64_t period) {
 
 // Forcing descriptor value at time t for column `orig` (header comment of
 // enum clm_forcing_field). F points to row 0 of a [CLM_F_NFIELDS][stride] block.
-__device__ __forceinline__ double forcing_value(const double* F, int stride,
-                                                int col, int orig, double t,
-                                                uint64_t seed) {
+CLM_HD double forcing_value(const double* F, int stride, int col, int orig, double t,
+                            uint64_t seed) {
   if (F == nullptr) return 0.0;
   double v = F[CLM_F_BASE * stride + col];
-  double amp = F[CLM_F_AMP * stride + col];
-  if (amp != 0.0)
-    v += amp * sin(F[CLM_F_OMEGA * stride + col] * t + F[CLM_F_PHASE * stride + col]);
-  double pp = F[CLM_F_PULSE_PERIOD * stride + col];
+  const double amp = F[CLM_F_AMP * stride + col];
+  if (amp != 0.0) v += amp * sin(F[CLM_F_OMEGA * stride + col] * t + F[CLM_F_PHASE * stride + col]);
+  const double pp = F[CLM_F_PULSE_PERIOD * stride + col];
   if (pp > 0.0) {
-    int64_t k = (int64_t)floor(t / pp);
+    const int64_t k = (int64_t)floor(t / pp);
     if (hash01(seed, (uint64_t)orig, k) < F[CLM_F_PULSE_DUTY * stride + col])
       v += F[CLM_F_PULSE_AMP * stride + col];
   }

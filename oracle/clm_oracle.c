@@ -709,6 +709,8 @@ static void block_solve(const col_t* C, const jac_t* J, const state_t* f,
   int n = C->n;
   thomas(n, J->vv[0], J->vv[1], J->vv[2], f->v, d->v);
   d->Fw = -f->Fw;
+  for (int k = 0; k < n; ++k) d->ti[k] = d->e[k] = 0.0;
+  d->Fe = 0.0;
   if (C->eh) {
     double g[MAXL] = {0};
     for (int k = 0; k < n; ++k) {
