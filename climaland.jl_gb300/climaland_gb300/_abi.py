@@ -222,6 +222,12 @@ SIGNATURES = [
     ("clm_jacobian", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_double, _DP, _DP, _DP]),
     ("clm_solve", ctypes.c_int, [_H, _DP, _DP, _DP, _DP, _DP, _DP, _DP]),
     ("clm_load_mlp", ctypes.c_int, [_H, ctypes.c_void_p, ctypes.c_int64]),
+    ("clm_step_eh_noalloc", ctypes.c_int, [ctypes.POINTER(ClmConfig), ctypes.c_int32, ctypes.c_int32,
+                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.POINTER(ctypes.c_void_p), ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
+                                           ctypes.c_double, ctypes.c_int32, ctypes.c_void_p]),
     ("clm_forcing_hash01", ctypes.c_double, [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int64]),
     ("clm_version", ctypes.c_char_p, []),
 ]

@@ -52,7 +52,10 @@ struct EHCol {
   double dz, inv_dz;
 };
 
-CLM_HD EHCol load_eh_col(const StepArgs& A, int s, int n) {
+// kLogKappaHere: take log(kappa_sat_*) from the exp/log tables instead of
+// the handle's precomputed per-column array (for callers without a handle).
+template <bool kLogKappaHere = false>
+CLM_HD EHCol load_eh_col(const StepArgs& A, const Tables& Tb, int s, int n) {
   const int st = A.L.stride;
   const double* P = A.prm;
   EHCol c;
@@ -68,8 +71,13 @@ CLM_HD EHCol load_eh_col(const StepArgs& A, int s, int n) {
   c.nuom = P[CLM_P_NU_SS_OM * st + s];
   c.nuq = P[CLM_P_NU_SS_QUARTZ * st + s];
   c.nug = P[CLM_P_NU_SS_GRAVEL * st + s];
-  c.lku = A.lkap[s];
-  c.lkf = A.lkap[st + s];
+  if (kLogKappaHere) {
+    c.lku = fm::log(Tb, c.ksu);
+    c.lkf = fm::log(Tb, c.ksf);
+  } else {
+    c.lku = A.lkap[s];
+    c.lkf = A.lkap[st + s];
+  }
   c.dz = (A.z_hi[s] - A.z_lo[s]) / n;
   c.inv_dz = 1.0 / c.dz;
   return c;
@@ -95,13 +103,13 @@ struct EHJac {
   Col<JT> cp, dp, d, ae;            // Thomas c', d' (then delta_v, d''), dpsi, face coef
 };
 
-template <typename JT>
+template <typename JT, bool kLogKappaHere = false>
 CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int orig,
                       const EHBuffers& B, const EHJac<JT>& J, double t0, double dt, int nsteps,
                       double& Fw, double& Fe, uint32_t& flags, int& iters_done) {
   const Earth& E = A.E;
   const EHScalars& sc = A.sc;
-  const EHCol c = load_eh_col(A, s, n);
+  const EHCol c = load_eh_col<kLogKappaHere>(A, Tb, s, n);
   const int st = A.L.stride;
   const double rdz = dt * c.inv_dz;
   const double half = 0.5 * c.dz;

@@ -283,6 +283,32 @@ int clm_solve(clm_handle* h, const double* W_vv, const double* W_ev,
  * cfg->learned_guess = 1. */
 int clm_load_mlp(clm_handle* h, const void* weights, int64_t nbytes);
 
+/* ---- allocation-free step (no reference counterpart) -----------------
+ * The EnergyHydrology step for callers that cannot allocate device memory:
+ * hosts whose device heap belongs to another allocator (CUDA.jl or PyTorch
+ * caching allocators under a fixed budget), code running inside a CUDA
+ * graph capture, or embeddings that forbid allocation after start-up.
+ * Everything is caller-owned device memory in the reference layout: z_lo,
+ * z_hi (ncol), params (CLM_NPARAM_EH rows of ncol), the state (cell = c * nlayers + k) and intF_w / intF_e (ncol),
+ * updated in place; flags (ncol, CLM_COL_*) may be NULL. forcing is a
+ * host array of 4 device pointers, one per clm_bc_slot (CLM_F_NFIELDS rows
+ * of ncol each, or NULL); forcing itself may be NULL. cfg (host memory)
+ * supplies the model constants and must ask for EnergyHydrology in FP64.
+ * Limits: 2 <= nlayers <= 32, the same for every column; otherwise
+ * CLM_ERR_ARG. The kernel's working scratch is a fixed 24 MiB device array
+ * inside the library, held by every GPU that loads it until the process
+ * exits. All calls share it: calls that overlap on the GPU (other streams
+ * or host threads) race. The first call on each device looks up that
+ * array and configures the kernel, so make it before any stream capture.
+ * Runs asynchronously on cuda_stream (a cudaStream_t, NULL for the legacy
+ * default stream). */
+int clm_step_eh_noalloc(const clm_config* cfg, int32_t ncol, int32_t nlayers,
+                        const double* z_lo, const double* z_hi, const double* params,
+                        const double* const* forcing, double* vartheta_l,
+                        double* theta_i, double* rho_e_int, double* intF_w,
+                        double* intF_e, uint32_t* flags, double t, double dt,
+                        int32_t nsteps, void* cuda_stream);
+
 /* Counter hash used by the rain-pulse forcing: uniform in [0, 1). Plain
  * integer arithmetic, identical on host and device. */
 double clm_forcing_hash01(uint64_t seed, uint64_t column, int64_t period);

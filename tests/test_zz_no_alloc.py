@@ -1,0 +1,97 @@
+"""The allocation-free step (clm_step_eh_noalloc) against the handle path.
+
+Callers whose device memory belongs to another allocator, or who run inside
+a CUDA graph capture, cannot let the library call cudaMalloc; this entry
+point takes every buffer from the caller and keeps its working scratch in a
+fixed array inside the library. The test drives it through the C ABI on
+caller-owned device buffers for two calls in a row and compares each result
+with the handle API's clm_step on the same workload, at the parity
+tolerance of the other GPU tests (1e-10). This file is collected last so
+that a failure here comes after every other test has run.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from climaland_gb300 import _abi as A
+from climaland_gb300 import device as D
+from climaland_gb300 import workloads as WL
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+@pytest.fixture
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def _workload():
+    w = WL.energy_hydrology_c1(ncol=1000, nlayers=15, seed=7)
+    w.params[A.CLM_P_K_SAT] = np.minimum(w.params[A.CLM_P_K_SAT], 1e-5)
+    return w
+
+
+def test_noalloc_matches_handle_path_two_calls(torch_cuda):
+    torch = torch_cuda
+    lib = D.load_library()
+    w = _workload()
+    nsteps = 6
+    # reference: the handle API, two calls
+    with D.SoilColumns(w) as g:
+        g.step(w.t0, w.dt, nsteps)
+        ref1 = g.get_state()
+        g.step(w.t0 + nsteps * w.dt, w.dt, nsteps)
+        ref2 = g.get_state()
+    # caller-owned device buffers in the reference layout
+    dev = lambda a: torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
+    z_lo, z_hi, prm = dev(w.z_lo), dev(w.z_hi), dev(w.params)
+    forc = {s: dev(f) for s, f in w.forcing.items()}
+    fptr = (ctypes.c_void_p * 4)(*[forc[s].data_ptr() if s in forc else None for s in range(4)])
+    st = [dev(a) for a in w.copy_state()]
+    flags = torch.zeros(w.ncol, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def call(t):
+        return lib.clm_step_eh_noalloc(
+            ctypes.byref(w.cfg), w.ncol, int(w.nlayers[0]), z_lo.data_ptr(), z_hi.data_ptr(),
+            prm.data_ptr(), fptr, st[0].data_ptr(), st[1].data_ptr(), st[2].data_ptr(),
+            st[3].data_ptr(), st[4].data_ptr(), flags.data_ptr(), t, w.dt, nsteps,
+            ctypes.c_void_p(stream.cuda_stream))
+
+    assert call(w.t0) == A.CLM_OK
+    torch.cuda.synchronize()
+    got1 = [x.cpu().numpy() for x in st]
+    free_before, _ = torch.cuda.mem_get_info()
+    assert call(w.t0 + nsteps * w.dt) == A.CLM_OK
+    torch.cuda.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    got2 = [x.cpu().numpy() for x in st]
+    assert free_after == free_before  # the call allocated no device memory
+    for got, ref in ((got1, ref1), (got2, ref2)):
+        assert np.max(np.abs(got[0] - ref[0])) <= TOL
+        assert np.max(np.abs(got[1] - ref[1])) <= TOL
+        assert np.max(np.abs(got[2] - ref[2])) / np.max(np.abs(ref[2])) <= TOL
+        assert np.max(np.abs(got[3] - ref[3])) <= TOL * max(np.max(np.abs(ref[3])), 1.0)
+        assert np.max(np.abs(got[4] - ref[4])) / max(np.max(np.abs(ref[4])), 1.0) <= TOL
+    assert int(flags.max()) == 0
+
+
+def test_noalloc_rejects_sizes_beyond_its_maximum(torch_cuda):
+    lib = D.load_library()
+    w = _workload()
+    null = None
+    for nl in (1, 33, 64):
+        rc = lib.clm_step_eh_noalloc(ctypes.byref(w.cfg), w.ncol, nl, null, null, null, null,
+                                     null, null, null, null, null, null, 0.0, w.dt, 1, null)
+        assert rc == A.CLM_ERR_ARG
+    cfg = A.ClmConfig.from_buffer_copy(w.cfg)
+    cfg.precision = A.CLM_PREC_MIXED
+    rc = lib.clm_step_eh_noalloc(ctypes.byref(cfg), w.ncol, 15, null, null, null, null,
+                                 null, null, null, null, null, null, 0.0, w.dt, 1, null)
+    assert rc == A.CLM_ERR_ARG
