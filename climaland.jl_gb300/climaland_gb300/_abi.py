@@ -222,6 +222,21 @@ SIGNATURES = [
     ("clm_jacobian", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_double, _DP, _DP, _DP]),
     ("clm_solve", ctypes.c_int, [_H, _DP, _DP, _DP, _DP, _DP, _DP, _DP]),
     ("clm_load_mlp", ctypes.c_int, [_H, ctypes.c_void_p, ctypes.c_int64]),
+    ("clm_features", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_double, ctypes.c_void_p]),
+    ("clm_mlp_create", ctypes.c_int, [ctypes.c_uint64, ctypes.POINTER(ctypes.c_void_p)]),
+    ("clm_mlp_destroy", None, [ctypes.c_void_p]),
+    ("clm_mlp_set_normalization", ctypes.c_int, [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_float)] * 4),
+    ("clm_mlp_train", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                     ctypes.c_int32, ctypes.c_int32, ctypes.c_float,
+                                     ctypes.POINTER(ctypes.c_float), ctypes.c_void_p]),
+    ("clm_mlp_gradients", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                         ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
+    ("clm_mlp_predict", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                       ctypes.c_void_p]),
+    ("clm_mlp_blob_bytes", ctypes.c_int64, []),
+    ("clm_mlp_nparams", ctypes.c_int64, []),
+    ("clm_mlp_get", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]),
+    ("clm_mlp_set", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64]),
     ("clm_step_eh_noalloc", ctypes.c_int, [ctypes.POINTER(ClmConfig), ctypes.c_int32, ctypes.c_int32,
                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.POINTER(ctypes.c_void_p), ctypes.c_void_p,

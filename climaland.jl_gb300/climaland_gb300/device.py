@@ -48,7 +48,8 @@ class SoilColumns:
     """
 
     def __init__(self, w, *, precision=None, newton_mode=None, max_iters=None,
-                 newton_tol=None, energy_norm_scale=None, cols_per_cta=None, lib=None):
+                 newton_tol=None, energy_norm_scale=None, cols_per_cta=None, learned_guess=None,
+                 lib=None):
         self.lib = lib or load_library()
         self.w = w
         cfg = A.ClmConfig.from_buffer_copy(w.cfg)
@@ -64,6 +65,8 @@ class SoilColumns:
             cfg.energy_norm_scale = energy_norm_scale
         if cols_per_cta is not None:
             cfg.cols_per_cta = cols_per_cta
+        if learned_guess is not None:
+            cfg.learned_guess = int(learned_guess)
         self.cfg = cfg
         self.eh = cfg.model == A.CLM_MODEL_ENERGY_HYDROLOGY
         self.ncol = w.ncol
@@ -162,6 +165,15 @@ class SoilColumns:
         it = np.empty(self.ncol, np.int32)
         self._check(self.lib.clm_get_status(self.h, A.uptr(f), A.iptr(it)))
         return f, it
+
+    # -- learned Newton guess ---------------------------------------------------------
+    def load_mlp(self, blob: bytes):
+        buf = ctypes.create_string_buffer(bytes(blob), len(blob))
+        self._check(self.lib.clm_load_mlp(self.h, buf, len(blob)))
+
+    def features(self, t, dt, X_ptr):
+        """Raw network inputs (ncol x 67 floats) into the device array X_ptr."""
+        self._check(self.lib.clm_features(self.h, float(t), float(dt), ctypes.c_void_p(X_ptr)))
 
     # -- closures -----------------------------------------------------------------
     def update_aux(self, t):

@@ -34,7 +34,13 @@ cudaError_t cols_to_sorted(const Layout& L, const double* src, double* dst, cuda
 cudaError_t cols_to_orig(const Layout& L, const double* src, double* dst, cudaStream_t st);
 // clm_budget.cu
 cudaError_t launch_budgets(const StepArgs& A, int model, double* W, double* E, cudaStream_t st);
+// clm_mlp.cu
+cudaError_t mlp_features(const StepArgs& A, double t, double dt, float* X, cudaStream_t st);
+cudaError_t mlp_guess(const StepArgs& A, const float* P, const float* norm, double t, double dt,
+                      float* guess, cudaStream_t st);
 }  // namespace clm
+
+#include "clm_mlp.cuh"
 
 using namespace clm;
 
@@ -63,7 +69,8 @@ struct clm_handle {
   int32_t* d_iters = nullptr;
   double* d_stage = nullptr;  // ncells_ref * 3 staging (reference layout)
   double* d_colstage = nullptr;  // 4 * stride: upload staging, W, E, spare
-  float* d_guess = nullptr;
+  float* d_guess = nullptr;  // learned guess, 2 x ncells_int (NaN: none)
+  float* d_mlp = nullptr;    // network parameters then standardisation
   bool have_geometry = false, have_params = false, have_state = false;
   int wpc = 1;   // warps (32-column tiles) per CTA of the step kernel
   int grid = 0;  // resident CTAs of the step kernel
@@ -357,6 +364,8 @@ int clm_create(const clm_config* cfg, clm_handle** out) {
       cfg->max_iters > 1000)
     return CLM_ERR_ARG;
   if (cfg->precision != CLM_PREC_FP64 && cfg->precision != CLM_PREC_MIXED) return CLM_ERR_ARG;
+  if (cfg->learned_guess && (cfg->model != CLM_MODEL_ENERGY_HYDROLOGY || cfg->newton_mode != CLM_NEWTON_TOL))
+    return CLM_ERR_ARG;  // the guess only changes where tolerance-mode Newton starts
   if (cfg->newton_mode != CLM_NEWTON_FIXED && cfg->newton_mode != CLM_NEWTON_TOL) return CLM_ERR_ARG;
   const int kinds[4] = {cfg->bc_top_water, cfg->bc_top_heat, cfg->bc_bottom_water, cfg->bc_bottom_heat};
   for (int k : kinds)
@@ -427,6 +436,7 @@ void clm_destroy(clm_handle* h) {
   dfree(h->d_v); dfree(h->d_ti); dfree(h->d_e); dfree(h->d_Fw); dfree(h->d_Fe);
   dfree(h->d_flags); dfree(h->d_iters); dfree(h->d_stage); dfree(h->d_colstage); dfree(h->d_guess);
   dfree(h->d_scratch);
+  dfree(h->d_mlp);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   cudaGetLastError();
   delete h;
@@ -547,6 +557,20 @@ int clm_step_async(clm_handle* h, double t, double dt, int32_t nsteps) {
     return fail(h, CLM_ERR_ARG, "need dt > 0, finite t, nsteps >= 0");
   if (nsteps == 0) return CLM_OK;
   StepArgs A = step_args(h);
+  if (h->cfg.learned_guess) {
+    // the network predicts each step's increment from the state at its start:
+    // one guess launch, then one step launch, per step
+    if (!h->d_mlp || !h->d_guess) return fail(h, CLM_ERR_STATE, "clm_load_mlp has not been called");
+    const float* P = h->d_mlp;
+    const float* norm = h->d_mlp + kMlpParams;
+    for (int i = 0; i < nsteps; ++i) {
+      const double ti = t + i * dt;
+      CLM_CUDA(h, mlp_guess(A, P, norm, ti, dt, h->d_guess, h->stream));
+      CLM_CUDA(h, launch_step(A, h->cfg.model, h->cfg.precision, h->wpc, h->grid, h->d_scratch,
+                              ti, dt, 1, h->stream));
+    }
+    return CLM_OK;
+  }
   // Steps are fused in one launch (the column stays in shared memory between
   // steps); launches are chunked so that one launch stays short.
   const int chunk = 64;
@@ -619,9 +643,41 @@ int clm_get_status(clm_handle* h, uint32_t* flags, int32_t* iters) {
 
 int clm_load_mlp(clm_handle* h, const void* weights, int64_t nbytes) {
   if (!h) return CLM_ERR_ARG;
-  (void)weights;
-  (void)nbytes;
-  return fail(h, CLM_ERR_UNSUPPORTED, "learned Newton guess is not built in this library");
+  if (!is_eh(h)) return fail(h, CLM_ERR_UNSUPPORTED, "the learned guess is built for EnergyHydrology");
+  if (!h->have_geometry) return fail(h, CLM_ERR_STATE, "clm_set_geometry has not been called");
+  if (!weights || nbytes < kMlpBlobBytes) return fail(h, CLM_ERR_ARG, "weight blob too small");
+  MlpBlobHeader hd;
+  std::memcpy(&hd, weights, sizeof hd);
+  if (hd.magic != kMlpMagic || hd.nin != (uint32_t)kMlpIn || hd.nhidden != (uint32_t)kMlpHidden ||
+      hd.nout != (uint32_t)kMlpOut)
+    return fail(h, CLM_ERR_ARG, "weight blob header does not match this library's network");
+  const float* f = reinterpret_cast<const float*>(static_cast<const unsigned char*>(weights) + sizeof hd);
+  const int nnorm = 2 * kMlpIn + 2 * kMlpOut;
+  std::vector<float> buf((size_t)kMlpParams + nnorm);
+  std::memcpy(buf.data(), f + nnorm, sizeof(float) * kMlpParams);  // parameters first
+  std::memcpy(buf.data() + kMlpParams, f, sizeof(float) * nnorm);
+  for (float x : buf)
+    if (!std::isfinite(x)) return fail(h, CLM_ERR_ARG, "non-finite value in the weight blob");
+  if (!h->d_mlp) CLM_CUDA(h, cudaMalloc(&h->d_mlp, sizeof(float) * buf.size()));
+  CLM_CUDA(h, cudaMemcpyAsync(h->d_mlp, buf.data(), sizeof(float) * buf.size(), cudaMemcpyHostToDevice, h->stream));
+  if (!h->d_guess) {
+    const size_t gb = sizeof(float) * 2 * (size_t)std::max<int64_t>(h->ncells_int, 1);
+    CLM_CUDA(h, cudaMalloc(&h->d_guess, gb));
+    CLM_CUDA(h, cudaMemsetAsync(h->d_guess, 0xFF, gb, h->stream));  // NaN: no guess
+  }
+  CLM_CUDA(h, cudaStreamSynchronize(h->stream));
+  return CLM_OK;
+}
+
+int clm_features(clm_handle* h, double t, double dt, float* X) {
+  int rc = ready(h);
+  if (rc != CLM_OK) return rc;
+  if (!is_eh(h)) return fail(h, CLM_ERR_UNSUPPORTED, "features are defined for EnergyHydrology");
+  if (!X) return fail(h, CLM_ERR_ARG, "X is required");
+  StepArgs A = step_args(h);
+  CLM_CUDA(h, mlp_features(A, t, dt, X, h->stream));
+  CLM_CUDA(h, cudaStreamSynchronize(h->stream));
+  return CLM_OK;
 }
 
 }  // extern "C"

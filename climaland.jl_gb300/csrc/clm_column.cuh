@@ -96,6 +96,9 @@ struct EHBuffers {
   Col<double> gv, gti, ge;          // state (holds U during a step)
   Col<double> xv, xe, fe;           // iterate, energy residual
   Col<double> K, kap, irc;          // frozen aux
+  // learned Newton guess: predicted u_{n+1} - u_n of vartheta_l and rho_e_int
+  // (p == nullptr: no guess)
+  Col<const float> guess_v{nullptr, 0}, guess_e{nullptr, 0};
 };
 
 template <typename JT>
@@ -117,6 +120,12 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
 
   for (int step = 0; step < nsteps; ++step) {
     const double t = t0 + step * dt;
+    // learned guess (tolerance mode only): Newton starts from u_n + predicted
+    // increment instead of U, and falls back to U when its first increment
+    // is larger than the predicted one (the guess was worse than none)
+    bool use_guess = B.guess_v.p != nullptr && A.newton_mode == CLM_NEWTON_TOL &&
+                     isfinite(B.guess_v[0]) && isfinite(B.guess_e[0]);
+    double pred2 = 0.0;
     // ---------------- stage 1: aux at Y_n, explicit tendency, U ----------
     double K0 = 0, T0 = 0, kap0 = 0, psi0 = 0;
     double Kt = 0, Tt = 0, kapt = 0, psit = 0;
@@ -145,8 +154,16 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       }
       B.gv[k] = Uv;
       B.gti[k] = Uti;
-      B.xv[k] = Uv;
-      B.xe[k] = Ye;
+      if (use_guess) {
+        const double xv0 = Yv + (double)B.guess_v[k], xe0 = Ye + (double)B.guess_e[k];
+        B.xv[k] = xv0;
+        B.xe[k] = xe0;
+        const double dv = xv0 - Uv, de = A.energy_scale * (xe0 - Ye);
+        pred2 += dv * dv + de * de;
+      } else {
+        B.xv[k] = Uv;
+        B.xe[k] = Ye;
+      }
       B.K[k] = K;
       B.kap[k] = kap;
       B.irc[k] = 1.0 / heat_capacity(E, tl, Uti, c.rcds);
@@ -358,6 +375,17 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       iters_done = it;
       if (A.newton_mode == CLM_NEWTON_TOL) {
         const double nrm = sqrt(norm2);
+        if (use_guess && it == 1 && nrm * nrm > pred2) {
+          // restart from the zero guess x = U
+          for (int k = 0; k < n; ++k) {
+            B.xv[k] = B.gv[k];
+            B.xe[k] = B.ge[k];
+          }
+          use_guess = false;
+          flags |= CLM_COL_GUESS_FALLBACK;
+          prev_norm = 1e300;
+          continue;
+        }
         if (nrm > prev_norm && it > 2) flags |= CLM_COL_DIVERGED;
         prev_norm = nrm;
         if (nrm < A.tol) break;

@@ -38,6 +38,7 @@ constexpr int kNoAllocMaxLayers = 32;
 constexpr int kNoAllocSlots = 1024;  // warps (32-column tiles) resident at once
 constexpr size_t kNoAllocScratchDoubles = (size_t)kNoAllocSlots * 3 * kNoAllocMaxLayers * kTile;
 constexpr size_t kNoAllocScratchBytes = kNoAllocScratchDoubles * sizeof(double);
+static_assert(kNoAllocScratchBytes == 24u << 20, "the documented scratch size is 24 MiB");
 
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchDoubles];
 

@@ -64,6 +64,10 @@ __global__ void __launch_bounds__(128, 1)
     B.gv = Col<double>{A.v + base, kTile};
     B.gti = Col<double>{A.ti + base, kTile};
     B.ge = Col<double>{A.e + base, kTile};
+    if (A.guess) {
+      B.guess_v = Col<const float>{A.guess + base, kTile};
+      B.guess_e = Col<const float>{A.guess + A.L.ncells_int + base, kTile};
+    }
     double Fw = A.Fw[s], Fe = A.Fe[s];
     uint32_t flags = 0;
     int iters = 0;

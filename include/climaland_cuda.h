@@ -278,10 +278,47 @@ int clm_solve(clm_handle* h, const double* W_vv, const double* W_ev,
               const double* W_ee, const double* f_v, const double* f_e,
               double* delta_v, double* delta_e);
 
-/* ---- learned Newton guess (no reference counterpart) ------------------ */
-/* Load the MLP weights (layout in clm_mlp_layout) used when
- * cfg->learned_guess = 1. */
+/* ---- learned Newton guess (no reference counterpart) ------------------
+ * A small MLP (inputs: the 20-layer vartheta_l, theta_i, T profiles, top
+ * water and heat fluxes, alpha, n, nu, log10 K_sat, dt; two hidden layers
+ * of 64 with GELU; outputs: the step's increments of vartheta_l and
+ * rho_e_int) predicts where each column's Newton solve will end. With
+ * cfg->learned_guess = 1 (EnergyHydrology, tolerance mode, 20-layer
+ * columns) Newton starts from u_n + prediction; a column whose first Newton
+ * increment exceeds the predicted one restarts from the zero guess
+ * (CLM_COL_GUESS_FALLBACK). Weights are a blob of clm_mlp_blob_bytes()
+ * bytes written by clm_mlp_get. */
 int clm_load_mlp(clm_handle* h, const void* weights, int64_t nbytes);
+
+/* Raw network inputs of every 20-layer column at time t (device array of
+ * ncol x 67 floats, original column order; other columns untouched). */
+int clm_features(clm_handle* h, double t, double dt, float* X);
+
+/* Trainer: FP32 master weights + Adam on the GPU; forward and backward
+ * BF16 GEMMs on the tensor cores (FP32 accumulation). X (rows x 67) and
+ * Y (rows x 40) are device arrays of raw inputs and targets; the
+ * standardisation (per-feature mean and std, host arrays) is set first.
+ * clm_mlp_train runs nsteps minibatches of `batch` consecutive rows,
+ * wrapping at nrows, and returns each step's summed squared error (host
+ * array of nsteps, may be NULL). clm_mlp_gradients returns the gradient
+ * (host, clm_mlp_nparams() floats, parameter order W1 b1 W2 b2 W3 b3) of the
+ * mean over rows of the squared standardised error, without updating. */
+typedef struct clm_mlp clm_mlp;
+int clm_mlp_create(uint64_t seed, clm_mlp** out);
+void clm_mlp_destroy(clm_mlp* m);
+int clm_mlp_set_normalization(clm_mlp* m, const float* in_mean, const float* in_std,
+                              const float* out_mean, const float* out_std);
+int clm_mlp_train(clm_mlp* m, const float* X, const float* Y, int64_t nrows,
+                  int32_t batch, int32_t nsteps, float lr, float* loss,
+                  void* cuda_stream);
+int clm_mlp_gradients(clm_mlp* m, const float* X, const float* Y, int32_t nrows,
+                      float* grad, float* loss);
+int clm_mlp_predict(clm_mlp* m, const float* X, int64_t nrows, float* Y,
+                    void* cuda_stream);
+int64_t clm_mlp_blob_bytes(void);
+int64_t clm_mlp_nparams(void);
+int clm_mlp_get(const clm_mlp* m, void* blob, int64_t nbytes);
+int clm_mlp_set(clm_mlp* m, const void* blob, int64_t nbytes);
 
 /* ---- allocation-free step (no reference counterpart) -----------------
  * The EnergyHydrology step for callers that cannot allocate device memory:

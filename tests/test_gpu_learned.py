@@ -1,0 +1,142 @@
+"""Learned Newton initial guess: the network's GPU forward/backward kernels
+against the FP64 CPU restatement (oracle/mlp_oracle.py), training, the
+feature kernel, and the end-to-end effect on tolerance-mode Newton."""
+import json
+
+import numpy as np
+import pytest
+
+import mlp_oracle as MO
+from climaland_gb300 import _abi as A
+from climaland_gb300 import learned as LG
+from climaland_gb300 import workloads as WL
+from climaland_gb300.device import SoilColumns
+from gpu_common import require_gpu
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    require_gpu()
+    import torch
+    return torch
+
+
+def _random_problem(torch, n=512, seed=0):
+    rng = np.random.default_rng(seed)
+    X = rng.normal(size=(n, LG.N_IN)).astype(np.float32) * 3.0 + 1.0
+    Y = rng.normal(size=(n, LG.N_OUT)).astype(np.float32) * 2.0 - 0.5
+    norm = (rng.normal(size=LG.N_IN).astype(np.float32), rng.uniform(1, 4, LG.N_IN).astype(np.float32),
+            rng.normal(size=LG.N_OUT).astype(np.float32), rng.uniform(1, 3, LG.N_OUT).astype(np.float32))
+    return X, Y, norm
+
+
+def _blocks(g):
+    sizes = [80 * 64, 64, 64 * 64, 64, 64 * 40, 40]
+    out, o = [], 0
+    for s in sizes:
+        out.append(g[o:o + s])
+        o += s
+    return out
+
+
+def test_gradients_match_fp64_oracle(torch):
+    X, Y, norm = _random_problem(torch)
+    tr = LG.Trainer(seed=3)
+    tr.set_normalization(*norm)
+    Xd, Yd = torch.tensor(X, device="cuda"), torch.tensor(Y, device="cuda")
+    g_gpu, loss_gpu = tr.gradients(Xd, Yd)
+    loss_ref, g_ref, _ = MO.loss_and_grad(tr.params(), tr.normalization(), X, Y)
+    assert abs(loss_gpu - loss_ref) / loss_ref < 1e-2
+    for name, a, b in zip(["W1", "b1", "W2", "b2", "W3", "b3"], _blocks(g_gpu), _blocks(g_ref)):
+        b = b.astype(np.float64)
+        if name == "W1":  # padded input rows carry no gradient
+            a, b = a.reshape(80, 64)[:67].ravel(), b.reshape(80, 64)[:67].ravel()
+        rel = np.linalg.norm(a - b) / np.linalg.norm(b)
+        cos = float(a @ b / (np.linalg.norm(a) * np.linalg.norm(b)))
+        print(f"GRADCHECK {name} rel_l2={rel:.3e} cos={cos:.6f}")
+        # BF16 activations (2^-8 relative) bound the agreement
+        assert rel < 3e-2 and cos > 0.999, (name, rel, cos)
+
+
+def test_predict_matches_fp64_oracle(torch):
+    X, Y, norm = _random_problem(torch, n=1000, seed=1)
+    tr = LG.Trainer(seed=5)
+    tr.set_normalization(*norm)
+    Yp = tr.predict(torch.tensor(X, device="cuda")).cpu().numpy()
+    _, _, Yref = MO.loss_and_grad(tr.params(), tr.normalization(), X, Y)
+    rel = np.linalg.norm(Yp - Yref) / np.linalg.norm(Yref)
+    assert rel < 2e-2, rel
+
+
+def test_training_fits_a_smooth_map(torch):
+    rng = np.random.default_rng(2)
+    n = 65536
+    X = rng.normal(size=(n, LG.N_IN)).astype(np.float32)
+    M = rng.normal(size=(LG.N_IN, LG.N_OUT)).astype(np.float32) / np.sqrt(LG.N_IN)
+    Y = np.tanh(X @ M) + 0.1 * (X[:, :LG.N_OUT] ** 2)
+    Xd, Yd = torch.tensor(X, device="cuda"), torch.tensor(Y.astype(np.float32), device="cuda")
+    res = LG.train(Xd, Yd, steps=3000, batch=2048, lr=2e-3)
+    print(f"TRAIN loss {res.loss[:50].mean():.4f} -> {res.loss[-50:].mean():.4f} in {res.seconds:.2f}s")
+    assert res.loss[-50:].mean() < 0.1 * res.loss[:50].mean()
+
+
+def test_features_kernel_matches_host(torch):
+    w = WL.energy_hydrology_c1(ncol=300, nlayers=20, seed=1)
+    X = torch.zeros((w.ncol, LG.N_IN), dtype=torch.float32, device="cuda")
+    t = 3600.0 * 7
+    with SoilColumns(w) as g:
+        g.features(t, w.dt, X.data_ptr())
+    X = X.cpu().numpy()
+    v = w.vartheta_l.reshape(w.ncol, 20)
+    ti = w.theta_i.reshape(w.ncol, 20)
+    e = w.rho_e_int.reshape(w.ncol, 20)
+    E = A.DEFAULT_EARTH
+    nu = w.params[A.CLM_P_NU][:, None]
+    thr = w.params[A.CLM_P_THETA_R][:, None]
+    sq = np.sqrt(np.finfo(float).eps)
+    tl = np.minimum(np.maximum(v, thr + sq), np.maximum(nu - ti, thr + sq))
+    rc = w.params[A.CLM_P_RHOC_DS][:, None] + tl * E["cp_l"] * E["rho_l"] + ti * E["cp_i"] * E["rho_i"]
+    T = E["T_0"] + (e + ti * E["rho_i"] * E["LH_f0"]) / rc
+    assert np.allclose(X[:, :20], v, rtol=1e-6)
+    assert np.allclose(X[:, 20:40], ti, rtol=1e-6, atol=1e-7)
+    assert np.allclose(X[:, 40:60], T, rtol=1e-6)
+    fh = w.forcing[A.CLM_BC_TOP_HEAT]
+    assert np.allclose(X[:, 61], fh[A.CLM_F_AMP] * np.sin(fh[A.CLM_F_OMEGA] * t), rtol=1e-5, atol=1e-4)
+    assert np.allclose(X[:, 65], np.log10(w.params[A.CLM_P_K_SAT]), rtol=1e-6)
+    assert np.all(X[:, 66] == np.float32(w.dt))
+
+
+def test_learned_guess_saves_newton_iterations(torch):
+    """Train on the plain solver's trajectories, then solve unseen columns to
+    the same tolerance with and without the guess: fewer iterations, same
+    answer (the plain solve is the judge)."""
+    wtr = LG.training_workload(ncol=16384, seed=0)
+    X, Y = LG.generate(wtr, 24)
+    res = LG.train(X, Y, steps=3000, batch=4096, lr=2e-3)
+    wev = LG.eval_workload(ncol=8192, seed=1)
+    nsteps = 24
+    out = {}
+    for name, guess in (("plain", False), ("learned", True)):
+        with SoilColumns(wev, learned_guess=1 if guess else None, **LG.TOL) as g:
+            if guess:
+                g.load_mlp(res.blob)
+            iters = []
+            t = wev.t0
+            for i in range(nsteps):
+                g.step(t, wev.dt, 1)
+                t += wev.dt
+                f, it = g.status()
+                iters.append(it.astype(np.float64))
+            out[name] = (g.get_state(), np.mean(iters), f)
+    (sp, ip, fp), (sl, il, fl) = out["plain"], out["learned"]
+    colerr = np.max(np.abs(sp[0] - sl[0]).reshape(wev.ncol, 20), axis=1)
+    frac_ok = float(np.mean(colerr <= 1e-8))
+    stats = dict(train_rows=res.nrows, train_seconds=res.seconds, loss_first=float(res.loss[:50].mean()),
+                 loss_last=float(res.loss[-50:].mean()), iters_plain=ip, iters_learned=il,
+                 fallback_frac=float(np.mean((fl & A.CLM_COL_GUESS_FALLBACK) > 0)),
+                 frac_cols_within_1e8=frac_ok, max_err=float(colerr.max()))
+    print("LEARNED " + json.dumps(stats))
+    assert il < ip
+    assert frac_ok >= 0.99
