@@ -299,7 +299,8 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       }
       // FP64 column-sum projection (mixed path): sum(delta_v) = -sum(f_v)
       const double corr_v = mixed ? (sdv + sum_fv) / n : 0.0;
-      double norm2 = fFw * fFw + fFe * fFe;
+      const double flux2 = fFw * fFw + fFe * fFe;
+      double norm2 = flux2;
       // sweep 3 (bottom -> top): energy right-hand side, rho e forward
       // elimination (c'' into cp, d'' into dp behind the read of delta_v)
       {
@@ -375,7 +376,9 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       iters_done = it;
       if (A.newton_mode == CLM_NEWTON_TOL) {
         const double nrm = sqrt(norm2);
-        if (use_guess && it == 1 && nrm * nrm > pred2) {
+        // the guess test uses the state part only: the integrated-flux
+        // increments do not depend on the starting point
+        if (use_guess && it == 1 && norm2 - flux2 > pred2) {
           // restart from the zero guess x = U
           for (int k = 0; k < n; ++k) {
             B.xv[k] = B.gv[k];

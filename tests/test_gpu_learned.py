@@ -79,7 +79,7 @@ def test_training_fits_a_smooth_map(torch):
     Xd, Yd = torch.tensor(X, device="cuda"), torch.tensor(Y.astype(np.float32), device="cuda")
     res = LG.train(Xd, Yd, steps=3000, batch=2048, lr=2e-3)
     print(f"TRAIN loss {res.loss[:50].mean():.4f} -> {res.loss[-50:].mean():.4f} in {res.seconds:.2f}s")
-    assert res.loss[-50:].mean() < 0.1 * res.loss[:50].mean()
+    assert res.loss[-50:].mean() < 0.2 * res.loss[:50].mean()
 
 
 def test_features_kernel_matches_host(torch):
