@@ -155,7 +155,11 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       B.gv[k] = Uv;
       B.gti[k] = Uti;
       if (use_guess) {
-        const double xv0 = Yv + (double)B.guess_v[k], xe0 = Ye + (double)B.guess_e[k];
+        double xv0 = Yv + (double)B.guess_v[k], xe0 = Ye + (double)B.guess_e[k];
+        // a layer whose guess leaves the retention curve's domain
+        // (vartheta_l <= theta_r) or is not finite starts from U
+        if (!(xv0 > c.theta_r + kSqrtEps) || !isfinite(xv0)) xv0 = Uv;
+        if (!isfinite(xe0)) xe0 = Ye;
         B.xv[k] = xv0;
         B.xe[k] = xe0;
         const double dv = xv0 - Uv, de = A.energy_scale * (xe0 - Ye);
@@ -299,8 +303,8 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       }
       // FP64 column-sum projection (mixed path): sum(delta_v) = -sum(f_v)
       const double corr_v = mixed ? (sdv + sum_fv) / n : 0.0;
-      const double flux2 = fFw * fFw + fFe * fFe;
-      double norm2 = flux2;
+      const double flux2 = fFw * fFw + fFe * fFe;  // integrated fluxes
+      double state2 = 0.0;                           // state increments
       // sweep 3 (bottom -> top): energy right-hand side, rho e forward
       // elimination (c'' into cp, d'' into dp behind the read of delta_v)
       {
@@ -337,7 +341,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
           d_prev = dk;
           const double dvd = (double)dv0;
           B.xv[k] -= dvd;
-          norm2 += dvd * dvd;
+          state2 += dvd * dvd;
           dvm = dv0; Dm = D0; dv0 = dvp; D0 = Dp;
           ae_dn = ae_up;
           ak_dn = ak_up;
@@ -362,23 +366,23 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
           for (int k = 0; k < n; ++k) {
             const double d = (double)J.dp[k] - corr_e;
             B.xe[k] -= d;
-            norm2 += (se * d) * (se * d);
+            state2 += (se * d) * (se * d);
           }
         } else {
           for (int k = n - 1; k >= 0; --k) {
             const JT d = J.dp[k] - J.cp[k] * nxt;
             nxt = d;
             B.xe[k] -= (double)d;
-            norm2 += (se * (double)d) * (se * (double)d);
+            state2 += (se * (double)d) * (se * (double)d);
           }
         }
       }
       iters_done = it;
       if (A.newton_mode == CLM_NEWTON_TOL) {
-        const double nrm = sqrt(norm2);
+        const double nrm = sqrt(flux2 + state2);
         // the guess test uses the state part only: the integrated-flux
         // increments do not depend on the starting point
-        if (use_guess && it == 1 && norm2 - flux2 > pred2) {
+        if (use_guess && it == 1 && state2 > pred2) {
           // restart from the zero guess x = U
           for (int k = 0; k < n; ++k) {
             B.xv[k] = B.gv[k];
@@ -391,7 +395,11 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         }
         if (nrm > prev_norm && it > 2) flags |= CLM_COL_DIVERGED;
         prev_norm = nrm;
-        if (nrm < A.tol) break;
+        // with a guess, the integrated fluxes start from their value at the
+        // guessed state (U_F + dt T_F(x0)): their first increment is that
+        // start-up, not a Newton correction, and stays out of the test
+        const double conv = (use_guess && it == 1) ? sqrt(state2) : nrm;
+        if (conv < A.tol) break;
         if (it == A.max_iters) flags |= CLM_COL_NOT_CONVERGED;
       }
     }

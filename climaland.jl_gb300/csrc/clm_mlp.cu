@@ -49,28 +49,38 @@ __device__ __forceinline__ float gelu_grad(float x) {
 }
 
 // Shared-memory image of the weights: transposed (WT[n][k], k contiguous:
-// B operands of the forward GEMMs) and row-major (W[k][n], n contiguous: B
-// operands of the backward GEMMs dY W^T), BF16, padded rows.
-struct Smem {
+// B operands of the forward GEMMs), BF16, padded rows; biases and the
+// standardisation in FP32. Inference kernels stage only this.
+struct Weights {
   __nv_bfloat16 W1T[kMlpHidden][kMlpInPad + 8];
   __nv_bfloat16 W2T[kMlpHidden][kMlpHidden + 8];
   __nv_bfloat16 W3T[kMlpOut][kMlpHidden + 8];
-  __nv_bfloat16 W2r[kMlpHidden][kMlpHidden + 8];
-  __nv_bfloat16 W3r[kMlpHidden][kMlpOutPad + 8];
   float b1[kMlpHidden], b2[kMlpHidden], b3[kMlpOut];
   float in_mean[kMlpIn], in_istd[kMlpIn], out_mean[kMlpOut], out_std[kMlpOut];
-  // transposed activations of the CTA's 64 rows (training only)
+};
+
+// Training adds the row-major weights (W[k][n], n contiguous: B operands of
+// the backward GEMMs dY W^T) and the CTA's transposed activations.
+struct Smem : Weights {
+  __nv_bfloat16 W2r[kMlpHidden][kMlpHidden + 8];
+  __nv_bfloat16 W3r[kMlpHidden][kMlpOutPad + 8];
   __nv_bfloat16 XT[kMlpInPad][kSR];
   __nv_bfloat16 H1T[kMlpHidden][kSR];
   __nv_bfloat16 H2T[kMlpHidden][kSR];
   __nv_bfloat16 dA1T[kMlpHidden][kSR];
   __nv_bfloat16 dA2T[kMlpHidden][kSR];
   __nv_bfloat16 dYT[kMlpOutPad][kSR];
-  // per-warp staging of 16 rows of raw inputs (prediction / guess)
+  // per-warp staging of 16 rows of raw inputs
   float xs[kWarps][16][kMlpInPad];
 };
 
-__device__ void stage_weights(Smem& S, const float* __restrict__ P, const float* __restrict__ norm) {
+// Inference (prediction, in-step guess): eight warps of 16 rows each.
+constexpr int kInferWarps = 8;
+struct InferSmem : Weights {
+  float xs[kInferWarps][16][kMlpInPad];
+};
+
+__device__ void stage_forward(Weights& S, const float* __restrict__ P, const float* __restrict__ norm) {
   const int tid = threadIdx.x, nt = blockDim.x;
   for (int i = tid; i < kMlpInPad * kMlpHidden; i += nt) {
     const int k = i / kMlpHidden, n = i % kMlpHidden;
@@ -78,16 +88,11 @@ __device__ void stage_weights(Smem& S, const float* __restrict__ P, const float*
   }
   for (int i = tid; i < kMlpHidden * kMlpHidden; i += nt) {
     const int k = i / kMlpHidden, n = i % kMlpHidden;
-    const __nv_bfloat16 w = __float2bfloat16_rn(P[kMlpW2 + i]);
-    S.W2T[n][k] = w;
-    S.W2r[k][n] = w;
+    S.W2T[n][k] = __float2bfloat16_rn(P[kMlpW2 + i]);
   }
-  for (int i = tid; i < kMlpHidden * kMlpOutPad; i += nt) {
-    const int k = i / kMlpOutPad, n = i % kMlpOutPad;
-    const float w = n < kMlpOut ? P[kMlpW3 + k * kMlpOut + n] : 0.0f;
-    const __nv_bfloat16 wb = __float2bfloat16_rn(w);
-    S.W3r[k][n] = wb;
-    if (n < kMlpOut) S.W3T[n][k] = wb;
+  for (int i = tid; i < kMlpHidden * kMlpOut; i += nt) {
+    const int k = i / kMlpOut, n = i % kMlpOut;
+    S.W3T[n][k] = __float2bfloat16_rn(P[kMlpW3 + i]);
   }
   for (int i = tid; i < kMlpHidden; i += nt) {
     S.b1[i] = P[kMlpB1 + i];
@@ -105,6 +110,19 @@ __device__ void stage_weights(Smem& S, const float* __restrict__ P, const float*
   }
 }
 
+__device__ void stage_weights(Smem& S, const float* __restrict__ P, const float* __restrict__ norm) {
+  stage_forward(S, P, norm);
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int i = tid; i < kMlpHidden * kMlpHidden; i += nt) {
+    const int k = i / kMlpHidden, n = i % kMlpHidden;
+    S.W2r[k][n] = __float2bfloat16_rn(P[kMlpW2 + i]);
+  }
+  for (int i = tid; i < kMlpHidden * kMlpOutPad; i += nt) {
+    const int k = i / kMlpOutPad, n = i % kMlpOutPad;
+    S.W3r[k][n] = __float2bfloat16_rn(n < kMlpOut ? P[kMlpW3 + k * kMlpOut + n] : 0.0f);
+  }
+}
+
 // Forward pass of one warp's 16 rows given their A fragments (5 k-chunks of
 // the standardised inputs). Leaves the pre-activations in A1, A2 and the
 // standardised outputs in Y (accumulator layout).
@@ -112,7 +130,7 @@ struct Fwd {
   float A1[8][4], A2[8][4], Y[5][4];
 };
 
-__device__ __forceinline__ void forward16(const Smem& S, const uint32_t xf[5][4], Fwd& F,
+__device__ __forceinline__ void forward16(const Weights& S, const uint32_t xf[5][4], Fwd& F,
                                           uint32_t h1f[4][4], uint32_t h2f[4][4]) {
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   // layer 1
@@ -167,7 +185,7 @@ __device__ __forceinline__ void forward16(const Smem& S, const uint32_t xf[5][4]
 
 // A fragments of 16 staged rows xs[16][kMlpInPad] (raw features):
 // standardise and pack (feature columns >= kMlpIn are zero).
-__device__ __forceinline__ void input_fragments(const Smem& S, const float (*xs)[kMlpInPad],
+__device__ __forceinline__ void input_fragments(const Weights& S, const float (*xs)[kMlpInPad],
                                                 uint32_t xf[5][4]) {
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   auto val = [&](int r, int f) -> float {
@@ -374,16 +392,16 @@ __global__ void adam_kernel(float* __restrict__ P, float* __restrict__ G, float*
 // ---------------------------------------------------------------------------
 // prediction on raw feature rows (de-standardised outputs)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kWarps * 32)
+__global__ void __launch_bounds__(kInferWarps * 32)
     predict_kernel(const float* __restrict__ P, const float* __restrict__ norm,
                    const float* __restrict__ X, int64_t nrows, float* __restrict__ Yout) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  Smem& S = *reinterpret_cast<Smem*>(smem_raw);
-  stage_weights(S, P, norm);
+  InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
+  stage_forward(S, P, norm);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  for (int64_t r0 = (int64_t)(blockIdx.x * kWarps + warp) * 16; r0 < nrows;
-       r0 += (int64_t)gridDim.x * kWarps * 16) {
+  for (int64_t r0 = (int64_t)(blockIdx.x * kInferWarps + warp) * 16; r0 < nrows;
+       r0 += (int64_t)gridDim.x * kInferWarps * 16) {
     for (int i = lane; i < 16 * kMlpInPad; i += 32) {
       const int r = i / kMlpInPad, f = i % kMlpInPad;
       S.xs[warp][r][f] = (r0 + r < nrows && f < kMlpIn) ? X[(r0 + r) * kMlpIn + f] : 0.0f;
@@ -421,29 +439,35 @@ __global__ void features_kernel(StepArgs A, double t, double dt, float* __restri
 }
 
 // guess[0][cell] = delta vartheta_l, guess[1][cell] = delta rho_e_int
-// (internal layout), for every 20-layer column.
-__global__ void __launch_bounds__(kWarps * 32)
+// (internal layout), for every 20-layer column. A warp takes 16 columns;
+// its two half-warps build the features of layers 0-9 and 10-19.
+__global__ void __launch_bounds__(kInferWarps * 32)
     guess_kernel(StepArgs A, const float* __restrict__ P, const float* __restrict__ norm, double t,
                  double dt, float* __restrict__ guess) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  Smem& S = *reinterpret_cast<Smem*>(smem_raw);
-  stage_weights(S, P, norm);
+  InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
+  stage_forward(S, P, norm);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t4 = lane & 3;
   const int64_t nci = A.L.ncells_int;
   const int nrows = A.L.stride;
-  for (int r0 = (blockIdx.x * kWarps + warp) * 16; r0 < nrows; r0 += gridDim.x * kWarps * 16) {
-    if (lane < 16) {
-      const int s = r0 + lane;
-      float* xr = S.xs[warp][lane];
+  const int half = lane >> 4;
+  constexpr int kHalf = kMlpLayers / 2;
+  for (int r0 = (blockIdx.x * kInferWarps + warp) * 16; r0 < nrows;
+       r0 += gridDim.x * kInferWarps * 16) {
+    {
+      const int s = r0 + (lane & 15);
+      float* xr = S.xs[warp][lane & 15];
       if (A.L.col_n[s] == kMlpLayers) {
         const int64_t base = A.L.tile_off[s / kTile] + s % kTile;
         Col<double> v{A.v + base, kTile}, ti{A.ti + base, kTile}, e{A.e + base, kTile};
-        column_features(A, s, A.L.perm[s], v, ti, e, t, dt, xr);
+        column_features(A, s, A.L.perm[s], v, ti, e, t, dt, xr, half * kHalf, (half + 1) * kHalf,
+                        half == 1);
       } else {
-        for (int f = 0; f < kMlpIn; ++f) xr[f] = S.in_mean[f];
+        for (int f = half; f < kMlpIn; f += 2) xr[f] = S.in_mean[f];
       }
-      for (int f = kMlpIn; f < kMlpInPad; ++f) xr[f] = 0.0f;
+      if (half == 0)
+        for (int f = kMlpIn; f < kMlpInPad; ++f) xr[f] = 0.0f;
     }
     __syncwarp();
     uint32_t xf[5][4], h1f[4][4], h2f[4][4];
@@ -487,15 +511,26 @@ cudaError_t mlp_adam(float* P, float* G, float* M, float* V, int step, float lr,
   return cudaGetLastError();
 }
 
+// Persistent grid: resident CTAs of the inference kernels (all SMs).
+template <typename K>
+static int infer_grid(K kernel, size_t sm, int64_t rows) {
+  int dev = 0, nsm = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, mlp::kInferWarps * 32, sm);
+  const int64_t need = (rows + 16 * mlp::kInferWarps - 1) / (16 * mlp::kInferWarps);
+  int64_t grid = (int64_t)(per > 0 ? per : 1) * (nsm > 0 ? nsm : 1);
+  if (grid > need) grid = need;
+  return grid < 1 ? 1 : (int)grid;
+}
+
 cudaError_t mlp_predict(const float* P, const float* norm, const float* X, int64_t nrows, float* Y,
                         cudaStream_t st) {
-  const size_t sm = sizeof(mlp::Smem);
+  const size_t sm = sizeof(mlp::InferSmem);
   cudaError_t e = cudaFuncSetAttribute(mlp::predict_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  int grid = (int)((nrows + 63) / 64);
-  if (grid > 152 * 8) grid = 152 * 8;
-  if (grid < 1) grid = 1;
-  mlp::predict_kernel<<<grid, mlp::kWarps * 32, sm, st>>>(P, norm, X, nrows, Y);
+  const int grid = infer_grid(mlp::predict_kernel, sm, nrows);
+  mlp::predict_kernel<<<grid, mlp::kInferWarps * 32, sm, st>>>(P, norm, X, nrows, Y);
   return cudaGetLastError();
 }
 
@@ -506,12 +541,11 @@ cudaError_t mlp_features(const StepArgs& A, double t, double dt, float* X, cudaS
 
 cudaError_t mlp_guess(const StepArgs& A, const float* P, const float* norm, double t, double dt,
                       float* guess, cudaStream_t st) {
-  const size_t sm = sizeof(mlp::Smem);
+  const size_t sm = sizeof(mlp::InferSmem);
   cudaError_t e = cudaFuncSetAttribute(mlp::guess_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  int grid = (A.L.stride + 63) / 64;
-  if (grid > 152 * 8) grid = 152 * 8;
-  mlp::guess_kernel<<<grid, mlp::kWarps * 32, sm, st>>>(A, P, norm, t, dt, guess);
+  const int grid = infer_grid(mlp::guess_kernel, sm, A.L.stride);
+  mlp::guess_kernel<<<grid, mlp::kInferWarps * 32, sm, st>>>(A, P, norm, t, dt, guess);
   return cudaGetLastError();
 }
 

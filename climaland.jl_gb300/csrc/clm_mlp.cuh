@@ -50,15 +50,17 @@ constexpr int64_t kMlpBlobBytes = sizeof(MlpBlobHeader) + kMlpBlobFloats * sizeo
 
 // Raw features of one column (layer k of the column through the strided
 // views; n must be kMlpLayers). T from temperature_from_ρe_int with
-// θ_l = volumetric_liquid_fraction, as update_aux! computes it.
+// θ_l = volumetric_liquid_fraction, as update_aux! computes it. Layers
+// [k0, k1) are written, and the seven column scalars when `tail`.
 template <typename V>
 CLM_HD void column_features(const StepArgs& A, int s, int orig, V v, V ti, V e, double t,
-                            double dt, float* out) {
+                            double dt, float* out, int k0 = 0, int k1 = kMlpLayers,
+                            bool tail = true) {
   const int st = A.L.stride;
   const double* P = A.prm;
   const double nu = P[CLM_P_NU * st + s], thr = P[CLM_P_THETA_R * st + s];
   const double rcds = P[CLM_P_RHOC_DS * st + s];
-  for (int k = 0; k < kMlpLayers; ++k) {
+  for (int k = k0; k < k1; ++k) {
     const double Yv = v[k], Yti = ti[k], Ye = e[k];
     const double v_safe = fmax(Yv, thr + kSqrtEps);
     const double nu_safe = fmax(nu - Yti, thr + kSqrtEps);
@@ -67,6 +69,7 @@ CLM_HD void column_features(const StepArgs& A, int s, int orig, V v, V ti, V e, 
     out[kMlpLayers + k] = (float)Yti;
     out[2 * kMlpLayers + k] = (float)temperature(A.E, Ye, Yti, heat_capacity(A.E, tl, Yti, rcds));
   }
+  if (!tail) return;
   out[60] = (float)forcing_value(A.forc[CLM_BC_TOP_WATER], st, s, orig, t, A.seed);
   out[61] = (float)forcing_value(A.forc[CLM_BC_TOP_HEAT], st, s, orig, t, A.seed);
   out[62] = (float)P[CLM_P_VG_ALPHA * st + s];
