@@ -42,6 +42,8 @@ CLM_PREC_FP64 = 0
 CLM_PREC_MIXED = 1
 CLM_NEWTON_FIXED = 0
 CLM_NEWTON_TOL = 1
+CLM_SCHED_STATIC = 0
+CLM_SCHED_DYNAMIC = 1
 CLM_BC_FLUX = 0
 CLM_BC_FREE_DRAINAGE = 1
 CLM_BC_STATE = 2
@@ -117,7 +119,9 @@ class ClmConfig(ctypes.Structure):
         ("pad0", ctypes.c_int32),
         ("forcing_seed", ctypes.c_uint64),
         ("cols_per_cta", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 7),
+        ("schedule", ctypes.c_int32),
+        ("graph", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 5),
     ]
 
 
@@ -164,7 +168,19 @@ def default_config() -> ClmConfig:
     c.phase_change = 1
     c.forcing_seed = 0
     c.cols_per_cta = 0
+    c.schedule = CLM_SCHED_STATIC
+    c.graph = 0
     return c
+
+
+class ClmTuneEntry(ctypes.Structure):
+    _fields_ = [
+        ("cols_per_cta", ctypes.c_int32),
+        ("schedule", ctypes.c_int32),
+        ("grid", ctypes.c_int32),
+        ("chosen", ctypes.c_int32),
+        ("ms_per_step", ctypes.c_double),
+    ]
 
 
 def config_to_dict(c: ClmConfig) -> dict:
@@ -214,6 +230,9 @@ SIGNATURES = [
     ("clm_step_async", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_double, ctypes.c_int32]),
     ("clm_sync", ctypes.c_int, [_H]),
     ("clm_set_stream", ctypes.c_int, [_H, ctypes.c_void_p]),
+    ("clm_autotune", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_double, ctypes.c_int32,
+                                    ctypes.c_void_p, ctypes.c_int32, _IP]),
+    ("clm_get_launch_config", ctypes.c_int, [_H, _IP, _IP, _IP]),
     ("clm_get_budgets", ctypes.c_int, [_H, _DP, _DP]),
     ("clm_get_status", ctypes.c_int, [_H, _UP, _IP]),
     ("clm_update_aux", ctypes.c_int, [_H, ctypes.c_double, _DP, _DP, _DP, _DP, _DP, _DP, _DP]),

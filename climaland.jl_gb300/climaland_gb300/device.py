@@ -49,7 +49,7 @@ class SoilColumns:
 
     def __init__(self, w, *, precision=None, newton_mode=None, max_iters=None,
                  newton_tol=None, energy_norm_scale=None, cols_per_cta=None, learned_guess=None,
-                 lib=None):
+                 schedule=None, graph=None, lib=None):
         self.lib = lib or load_library()
         self.w = w
         cfg = A.ClmConfig.from_buffer_copy(w.cfg)
@@ -67,6 +67,10 @@ class SoilColumns:
             cfg.cols_per_cta = cols_per_cta
         if learned_guess is not None:
             cfg.learned_guess = int(learned_guess)
+        if schedule is not None:
+            cfg.schedule = int(schedule)
+        if graph is not None:
+            cfg.graph = int(bool(graph))
         self.cfg = cfg
         self.eh = cfg.model == A.CLM_MODEL_ENERGY_HYDROLOGY
         self.ncol = w.ncol
@@ -167,6 +171,21 @@ class SoilColumns:
         return f, it
 
     # -- learned Newton guess ---------------------------------------------------------
+    def autotune(self, t, dt, probe_steps=4):
+        """clm_autotune: time every launch configuration on probe_steps
+        steps from the current state (which is restored) and keep the
+        fastest. Returns the timed candidates as dicts."""
+        table = (A.ClmTuneEntry * 16)()
+        n = ctypes.c_int32(0)
+        self._check(self.lib.clm_autotune(self.h, float(t), float(dt), int(probe_steps),
+                                          ctypes.cast(table, ctypes.c_void_p), 16, ctypes.byref(n)))
+        return [{k: getattr(table[i], k) for k, _ in A.ClmTuneEntry._fields_} for i in range(min(n.value, 16))]
+
+    def launch_config(self):
+        c, s, g = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        self._check(self.lib.clm_get_launch_config(self.h, ctypes.byref(c), ctypes.byref(s), ctypes.byref(g)))
+        return {"cols_per_cta": c.value, "schedule": s.value, "grid": g.value}
+
     def load_mlp(self, blob: bytes):
         buf = ctypes.create_string_buffer(bytes(blob), len(blob))
         self._check(self.lib.clm_load_mlp(self.h, buf, len(blob)))

@@ -21,7 +21,7 @@
 namespace clm {
 // clm_step.cu
 cudaError_t launch_step(const StepArgs& A, int model, int precision, int wpc, int grid,
-                        double* scratch, double t0, double dt, int nsteps, cudaStream_t stream);
+                        double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream);
 size_t step_smem_bytes(int model, int precision, int nmax, int wpc);
 cudaError_t step_grid(int model, int precision, int nmax, int wpc, int ntiles, int* grid);
 size_t step_scratch_doubles(int model, int nmax, int wpc, int grid);
@@ -36,8 +36,9 @@ cudaError_t cols_to_orig(const Layout& L, const double* src, double* dst, cudaSt
 cudaError_t launch_budgets(const StepArgs& A, int model, double* W, double* E, cudaStream_t st);
 // clm_mlp.cu
 cudaError_t mlp_features(const StepArgs& A, double t, double dt, float* X, cudaStream_t st);
-cudaError_t mlp_guess(const StepArgs& A, const float* P, const float* norm, double t, double dt,
-                      float* guess, cudaStream_t st);
+cudaError_t mlp_guess_setup(int64_t rows, int* grid);
+cudaError_t mlp_guess(const StepArgs& A, const float* P, const float* norm, const StepClock& clk,
+                      float* guess, int grid, cudaStream_t st);
 }  // namespace clm
 
 #include "clm_mlp.cuh"
@@ -74,7 +75,26 @@ struct clm_handle {
   bool have_geometry = false, have_params = false, have_state = false;
   int wpc = 1;   // warps (32-column tiles) per CTA of the step kernel
   int grid = 0;  // resident CTAs of the step kernel
+  int sched = CLM_SCHED_STATIC;  // tile order of the step kernel
+  int* d_ctr = nullptr;          // dynamic tile order: [next tile, warps done]
   double* d_scratch = nullptr;  // per-warp-slot frozen aux arrays
+  size_t scratch_doubles = 0;
+  int guess_grid = 0;           // persistent grid of the guess kernel
+  // CUDA graph replay of clm_step_async: one executable graph per piece
+  // length, captured on cap_stream, launched on `stream`; t and dt reach the
+  // kernels through d_clock, filled from a pinned ring before each replay
+  static constexpr int kGraphs = 4, kRing = 4;
+  struct Graph {
+    cudaGraphExec_t exec = nullptr;
+    int nsteps = 0;
+    uint64_t used = 0;
+  } graphs[kGraphs];
+  uint64_t graph_tick = 0;
+  cudaStream_t cap_stream = nullptr;
+  double* d_clock = nullptr;   // kClockSlots + 1
+  double* h_clock = nullptr;   // pinned, kRing x (kClockSlots + 1)
+  cudaEvent_t clock_ev[kRing] = {};
+  int clock_next = 0;
   Earth E{};
   EHScalars sc{};
 };
@@ -106,6 +126,15 @@ void dfree(T*& p) {
 
 bool is_eh(const clm_handle* h) { return h->cfg.model == CLM_MODEL_ENERGY_HYDROLOGY; }
 
+// Captured graphs hold kernel arguments by value (buffer pointers, launch
+// shape): drop them whenever one of those changes.
+void drop_graphs(clm_handle* h) {
+  for (auto& g : h->graphs) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = clm_handle::Graph{};
+  }
+}
+
 Layout layout_of(const clm_handle* h) {
   Layout L;
   L.ncol = h->ncol;
@@ -136,6 +165,7 @@ StepArgs step_args(const clm_handle* h) {
   A.flags = h->d_flags;
   A.iters = h->d_iters;
   A.guess = h->cfg.learned_guess ? h->d_guess : nullptr;
+  A.tile_ctr = h->sched == CLM_SCHED_DYNAMIC ? h->d_ctr : nullptr;
   A.E = h->E;
   A.sc = h->sc;
   A.bc_tw = h->cfg.bc_top_water;
@@ -154,6 +184,7 @@ StepArgs step_args(const clm_handle* h) {
 // Build the sorted, tiled layout from per-column layer counts.
 int build_layout(clm_handle* h, const std::vector<int>& nl) {
   const int ncol = h->ncol;
+  drop_graphs(h);
   h->ref_off.assign(ncol + 1, 0);
   for (int c = 0; c < ncol; ++c) {
     if (nl[c] < 2 || nl[c] > kMaxLayers)
@@ -230,6 +261,109 @@ int build_layout(clm_handle* h, const std::vector<int>& nl) {
   dfree(h->d_scratch);
   const size_t nsc = step_scratch_doubles(h->cfg.model, h->nmax, h->wpc, h->grid);
   if (nsc) CLM_CUDA(h, cudaMalloc(&h->d_scratch, sizeof(double) * nsc));
+  h->scratch_doubles = nsc;
+  h->guess_grid = 0;
+  return CLM_OK;
+}
+
+// Start time of step s of a call that starts at t: the one expression both
+// the direct launches and the graph clock use, so both give the same bits.
+__attribute__((noinline)) double step_time(double t, int s, double dt) { return t + s * dt; }
+
+// One kernel launch of a step sequence: `nsteps` steps from step `step` of
+// the call, preceded by the guess kernel when `guess`.
+struct Launch {
+  int step, nsteps;
+  bool guess;
+};
+
+// Steps are fused in one launch (a column stays in shared memory between
+// steps), 64 per launch so that one launch stays short; with the learned
+// guess, the network predicts each step's increment from the state at its
+// start: one guess launch, then one step launch, per step.
+std::vector<Launch> launch_sequence(const clm_handle* h, int nsteps) {
+  std::vector<Launch> seq;
+  if (h->cfg.learned_guess) {
+    for (int i = 0; i < nsteps; ++i) seq.push_back({i, 1, true});
+  } else {
+    const int chunk = 64;
+    for (int s0 = 0; s0 < nsteps; s0 += chunk) seq.push_back({s0, std::min(chunk, nsteps - s0), false});
+  }
+  return seq;
+}
+
+int issue(clm_handle* h, const Launch& l, const StepClock& clk, cudaStream_t st) {
+  const StepArgs A = step_args(h);
+  if (l.guess) {
+    const float* P = h->d_mlp;
+    CLM_CUDA(h, mlp_guess(A, P, P + kMlpParams, clk, h->d_guess, h->guess_grid, st));
+  }
+  CLM_CUDA(h, launch_step(A, h->cfg.model, h->cfg.precision, h->wpc, h->grid, h->d_scratch, clk,
+                          l.nsteps, st));
+  return CLM_OK;
+}
+
+// Graph replay: the call is cut into pieces of at most kClockSlots launches;
+// each piece length has one captured graph whose kernels read their start
+// time from d_clock[slot] and dt from d_clock[kClockSlots].
+int step_graph(clm_handle* h, double t, double dt, int nsteps) {
+  if (!h->d_clock) {
+    CLM_CUDA(h, cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking));
+    CLM_CUDA(h, cudaMalloc(&h->d_clock, sizeof(double) * (kClockSlots + 1)));
+    CLM_CUDA(h, cudaMallocHost(&h->h_clock, sizeof(double) * (kClockSlots + 1) * clm_handle::kRing));
+    for (auto& ev : h->clock_ev) CLM_CUDA(h, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  }
+  const int per_launch = h->cfg.learned_guess ? 1 : 64;
+  const int piece_max = per_launch * kClockSlots;
+  for (int s_begin = 0; s_begin < nsteps; s_begin += piece_max) {
+    const int P = std::min(piece_max, nsteps - s_begin);
+    const std::vector<Launch> seq = launch_sequence(h, P);
+    clm_handle::Graph* g = nullptr;
+    for (auto& c : h->graphs)
+      if (c.exec && c.nsteps == P) g = &c;
+    if (!g) {
+      // evict the least recently used entry
+      g = &h->graphs[0];
+      for (auto& c : h->graphs)
+        if (c.used < g->used) g = &c;
+      if (g->exec) cudaGraphExecDestroy(g->exec);
+      *g = clm_handle::Graph{};
+      CLM_CUDA(h, cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal));
+      int rc = CLM_OK;
+      for (size_t j = 0; j < seq.size() && rc == CLM_OK; ++j) {
+        StepClock clk;
+        clk.dev = h->d_clock;
+        clk.slot = (int)j;
+        rc = issue(h, seq[j], clk, h->cap_stream);
+      }
+      cudaGraph_t graph = nullptr;
+      const cudaError_t ec = cudaStreamEndCapture(h->cap_stream, &graph);
+      if (rc != CLM_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+      }
+      if (ec != cudaSuccess) return cuda_fail(h, ec, "cudaStreamEndCapture");
+      const cudaError_t ei = cudaGraphInstantiate(&g->exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ei != cudaSuccess) {
+        g->exec = nullptr;
+        return cuda_fail(h, ei, "cudaGraphInstantiate");
+      }
+      g->nsteps = P;
+    }
+    g->used = ++h->graph_tick;
+    // the ring slot is free once the copy that last read it has run
+    const int r = h->clock_next;
+    h->clock_next = (r + 1) % clm_handle::kRing;
+    CLM_CUDA(h, cudaEventSynchronize(h->clock_ev[r]));
+    double* hc = h->h_clock + (size_t)r * (kClockSlots + 1);
+    for (size_t j = 0; j < seq.size(); ++j) hc[j] = step_time(t, s_begin + seq[j].step, dt);
+    hc[kClockSlots] = dt;
+    CLM_CUDA(h, cudaMemcpyAsync(h->d_clock, hc, sizeof(double) * (kClockSlots + 1),
+                                cudaMemcpyHostToDevice, h->stream));
+    CLM_CUDA(h, cudaEventRecord(h->clock_ev[r], h->stream));
+    CLM_CUDA(h, cudaGraphLaunch(g->exec, h->stream));
+  }
   return CLM_OK;
 }
 
@@ -367,6 +501,9 @@ int clm_create(const clm_config* cfg, clm_handle** out) {
   if (cfg->learned_guess && (cfg->model != CLM_MODEL_ENERGY_HYDROLOGY || cfg->newton_mode != CLM_NEWTON_TOL))
     return CLM_ERR_ARG;  // the guess only changes where tolerance-mode Newton starts
   if (cfg->newton_mode != CLM_NEWTON_FIXED && cfg->newton_mode != CLM_NEWTON_TOL) return CLM_ERR_ARG;
+  if (cfg->schedule != CLM_SCHED_STATIC && cfg->schedule != CLM_SCHED_DYNAMIC) return CLM_ERR_ARG;
+  if (cfg->graph != 0 && cfg->graph != 1) return CLM_ERR_ARG;
+  if (cfg->cols_per_cta < 0) return CLM_ERR_ARG;
   const int kinds[4] = {cfg->bc_top_water, cfg->bc_top_heat, cfg->bc_bottom_water, cfg->bc_bottom_heat};
   for (int k : kinds)
     if (k < CLM_BC_FLUX || k > CLM_BC_FLUX_ADVECTIVE) return CLM_ERR_ARG;
@@ -384,6 +521,7 @@ int clm_create(const clm_config* cfg, clm_handle** out) {
   h->sc.omega_ln10 = cfg->ice_impedance_omega * kLn10;
   h->sc.visc_gamma = cfg->visc_gamma;
   h->sc.visc_gamma_T_ref = cfg->visc_gamma_T_ref;
+  h->sched = cfg->schedule;
   cudaError_t e = cudaGetDevice(&h->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
   h->stream = h->own_stream;
@@ -400,14 +538,16 @@ int clm_create(const clm_config* cfg, clm_handle** out) {
             cudaMalloc(&h->d_Fe, cb) == cudaSuccess &&
             cudaMalloc(&h->d_flags, sizeof(uint32_t) * stride) == cudaSuccess &&
             cudaMalloc(&h->d_iters, sizeof(int32_t) * stride) == cudaSuccess &&
-            cudaMalloc(&h->d_colstage, cb * 4) == cudaSuccess;
+            cudaMalloc(&h->d_colstage, cb * 4) == cudaSuccess &&
+            cudaMalloc(&h->d_ctr, sizeof(int) * 2) == cudaSuccess;
   if (ok) {
     ok = cudaMemsetAsync(h->d_prm, 0, cb * CLM_NPARAM_EH, h->stream) == cudaSuccess &&
          cudaMemsetAsync(h->d_lkap, 0, cb * 2, h->stream) == cudaSuccess &&
          cudaMemsetAsync(h->d_Fw, 0, cb, h->stream) == cudaSuccess &&
          cudaMemsetAsync(h->d_Fe, 0, cb, h->stream) == cudaSuccess &&
          cudaMemsetAsync(h->d_flags, 0, sizeof(uint32_t) * stride, h->stream) == cudaSuccess &&
-         cudaMemsetAsync(h->d_iters, 0, sizeof(int32_t) * stride, h->stream) == cudaSuccess;
+         cudaMemsetAsync(h->d_iters, 0, sizeof(int32_t) * stride, h->stream) == cudaSuccess &&
+         cudaMemsetAsync(h->d_ctr, 0, sizeof(int) * 2, h->stream) == cudaSuccess;
   }
   if (!ok) {
     cudaGetLastError();
@@ -437,6 +577,13 @@ void clm_destroy(clm_handle* h) {
   dfree(h->d_flags); dfree(h->d_iters); dfree(h->d_stage); dfree(h->d_colstage); dfree(h->d_guess);
   dfree(h->d_scratch);
   dfree(h->d_mlp);
+  dfree(h->d_ctr);
+  drop_graphs(h);
+  dfree(h->d_clock);
+  if (h->h_clock) cudaFreeHost(h->h_clock);
+  for (auto& ev : h->clock_ev)
+    if (ev) cudaEventDestroy(ev);
+  if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   cudaGetLastError();
   delete h;
@@ -516,6 +663,7 @@ int clm_set_bc(clm_handle* h, int32_t slot, const double* f, int32_t nfields) {
   if (!h->have_geometry) return fail(h, CLM_ERR_STATE, "clm_set_geometry has not been called");
   if (slot < 0 || slot > 3) return fail(h, CLM_ERR_ARG, "slot must be a clm_bc_slot");
   if (!f) {
+    if (h->d_forc[slot]) drop_graphs(h);
     dfree(h->d_forc[slot]);
     return CLM_OK;
   }
@@ -523,6 +671,7 @@ int clm_set_bc(clm_handle* h, int32_t slot, const double* f, int32_t nfields) {
   for (int64_t i = 0; i < (int64_t)nfields * h->ncol; ++i)
     if (!std::isfinite(f[i])) return fail(h, CLM_ERR_ARG, "non-finite forcing value");
   if (!h->d_forc[slot]) {
+    drop_graphs(h);
     CLM_CUDA(h, cudaMalloc(&h->d_forc[slot], sizeof(double) * h->stride * CLM_F_NFIELDS));
   }
   CLM_CUDA(h, cudaMemsetAsync(h->d_forc[slot], 0, sizeof(double) * h->stride * CLM_F_NFIELDS, h->stream));
@@ -556,29 +705,161 @@ int clm_step_async(clm_handle* h, double t, double dt, int32_t nsteps) {
   if (!(dt > 0) || !std::isfinite(dt) || !std::isfinite(t) || nsteps < 0)
     return fail(h, CLM_ERR_ARG, "need dt > 0, finite t, nsteps >= 0");
   if (nsteps == 0) return CLM_OK;
-  StepArgs A = step_args(h);
-  if (h->cfg.learned_guess) {
-    // the network predicts each step's increment from the state at its start:
-    // one guess launch, then one step launch, per step
-    if (!h->d_mlp || !h->d_guess) return fail(h, CLM_ERR_STATE, "clm_load_mlp has not been called");
-    const float* P = h->d_mlp;
-    const float* norm = h->d_mlp + kMlpParams;
-    for (int i = 0; i < nsteps; ++i) {
-      const double ti = t + i * dt;
-      CLM_CUDA(h, mlp_guess(A, P, norm, ti, dt, h->d_guess, h->stream));
-      CLM_CUDA(h, launch_step(A, h->cfg.model, h->cfg.precision, h->wpc, h->grid, h->d_scratch,
-                              ti, dt, 1, h->stream));
+  if (h->cfg.learned_guess && (!h->d_mlp || !h->d_guess))
+    return fail(h, CLM_ERR_STATE, "clm_load_mlp has not been called");
+  if (h->cfg.graph) {
+    // a caller that is capturing the stream itself records the plain launches
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CLM_CUDA(h, cudaStreamIsCapturing(h->stream, &cs));
+    if (cs == cudaStreamCaptureStatusNone) return step_graph(h, t, dt, nsteps);
+  }
+  const std::vector<Launch> seq = launch_sequence(h, nsteps);
+  for (const Launch& l : seq) {
+    StepClock clk;
+    clk.t0 = step_time(t, l.step, dt);
+    clk.dt = dt;
+    rc = issue(h, l, clk, h->stream);
+    if (rc != CLM_OK) return rc;
+  }
+  return CLM_OK;
+}
+
+int clm_autotune(clm_handle* h, double t, double dt, int32_t probe_steps, clm_tune_entry* table,
+                 int32_t table_cap, int32_t* n_entries) {
+  int rc = ready(h);
+  if (rc != CLM_OK) return rc;
+  if (!(dt > 0) || !std::isfinite(dt) || !std::isfinite(t) || probe_steps < 1 || probe_steps > 64)
+    return fail(h, CLM_ERR_ARG, "need dt > 0, finite t, probe_steps in [1, 64]");
+  if (table_cap < 0 || (table_cap > 0 && !table)) return fail(h, CLM_ERR_ARG, "bad table");
+  // candidates: warps per CTA that fit the shared memory x tile order
+  int dev_smem = 0;
+  CLM_CUDA(h, cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
+  std::vector<clm_tune_entry> cand;
+  size_t need = 0;
+  for (int w = 1; w <= 4; ++w) {
+    if (step_smem_bytes(h->cfg.model, h->cfg.precision, h->nmax, w) > (size_t)dev_smem) break;
+    int grid = 0;
+    CLM_CUDA(h, step_grid(h->cfg.model, h->cfg.precision, h->nmax, w, h->ntiles, &grid));
+    need = std::max(need, step_scratch_doubles(h->cfg.model, h->nmax, w, grid));
+    for (int sch : {CLM_SCHED_STATIC, CLM_SCHED_DYNAMIC}) {
+      clm_tune_entry e{};
+      e.cols_per_cta = w * kTile;
+      e.schedule = sch;
+      e.grid = grid;
+      cand.push_back(e);
     }
-    return CLM_OK;
   }
-  // Steps are fused in one launch (the column stays in shared memory between
-  // steps); launches are chunked so that one launch stays short.
-  const int chunk = 64;
-  for (int s0 = 0; s0 < nsteps; s0 += chunk) {
-    const int ns = std::min(chunk, nsteps - s0);
-    CLM_CUDA(h, launch_step(A, h->cfg.model, h->cfg.precision, h->wpc, h->grid, h->d_scratch,
-                            t + s0 * dt, dt, ns, h->stream));
+  if (cand.empty()) return fail(h, CLM_ERR_ARG, "no launch configuration fits the shared memory");
+  CLM_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (need > h->scratch_doubles) {
+    dfree(h->d_scratch);
+    CLM_CUDA(h, cudaMalloc(&h->d_scratch, sizeof(double) * need));
+    h->scratch_doubles = need;
   }
+  drop_graphs(h);
+  // the probe advances the real state: keep a copy and put it back
+  const int64_t ni = std::max<int64_t>(h->ncells_int, 1);
+  const int nf = is_eh(h) ? 3 : 1;
+  double* keep = nullptr;
+  uint32_t* keep_fl = nullptr;
+  int32_t* keep_it = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  auto cleanup = [&]() {
+    if (keep) cudaFree(keep);
+    if (keep_fl) cudaFree(keep_fl);
+    if (keep_it) cudaFree(keep_it);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+  };
+  auto bail = [&](cudaError_t err, const char* what) {
+    cleanup();
+    return cuda_fail(h, err, what);
+  };
+#define CLM_TRY(call)                               \
+  do {                                              \
+    cudaError_t _e = (call);                        \
+    if (_e != cudaSuccess) return bail(_e, #call);  \
+  } while (0)
+  CLM_TRY(cudaMalloc(&keep, sizeof(double) * (nf * ni + 2 * h->stride)));
+  CLM_TRY(cudaMalloc(&keep_fl, sizeof(uint32_t) * h->stride));
+  CLM_TRY(cudaMalloc(&keep_it, sizeof(int32_t) * h->stride));
+  CLM_TRY(cudaEventCreate(&e0));
+  CLM_TRY(cudaEventCreate(&e1));
+  double* fields[3] = {h->d_v, h->d_ti, h->d_e};
+  auto save_restore = [&](bool save) -> cudaError_t {
+    cudaError_t err = cudaSuccess;
+    const cudaMemcpyKind k = cudaMemcpyDeviceToDevice;
+    for (int f = 0; f < nf && err == cudaSuccess; ++f)
+      err = save ? cudaMemcpyAsync(keep + f * ni, fields[f], sizeof(double) * ni, k, h->stream)
+                 : cudaMemcpyAsync(fields[f], keep + f * ni, sizeof(double) * ni, k, h->stream);
+    double* kf = keep + nf * ni;
+    const size_t cb = sizeof(double) * h->stride;
+    if (err == cudaSuccess)
+      err = save ? cudaMemcpyAsync(kf, h->d_Fw, cb, k, h->stream) : cudaMemcpyAsync(h->d_Fw, kf, cb, k, h->stream);
+    if (err == cudaSuccess && is_eh(h))
+      err = save ? cudaMemcpyAsync(kf + h->stride, h->d_Fe, cb, k, h->stream)
+                 : cudaMemcpyAsync(h->d_Fe, kf + h->stride, cb, k, h->stream);
+    if (err == cudaSuccess)
+      err = save ? cudaMemcpyAsync(keep_fl, h->d_flags, sizeof(uint32_t) * h->stride, k, h->stream)
+                 : cudaMemcpyAsync(h->d_flags, keep_fl, sizeof(uint32_t) * h->stride, k, h->stream);
+    if (err == cudaSuccess)
+      err = save ? cudaMemcpyAsync(keep_it, h->d_iters, sizeof(int32_t) * h->stride, k, h->stream)
+                 : cudaMemcpyAsync(h->d_iters, keep_it, sizeof(int32_t) * h->stride, k, h->stream);
+    return err;
+  };
+  CLM_TRY(save_restore(true));
+  const int wpc0 = h->wpc, grid0 = h->grid, sched0 = h->sched;
+  int best = -1;
+  for (size_t i = 0; i < cand.size(); ++i) {
+    clm_tune_entry& c = cand[i];
+    h->wpc = c.cols_per_cta / kTile;
+    h->grid = c.grid;
+    h->sched = c.schedule;
+    StepArgs A = step_args(h);
+    A.guess = nullptr;  // the probe times the step kernel alone
+    StepClock clk;
+    clk.t0 = t;
+    clk.dt = dt;
+    // one untimed step (first-touch of the scratch slots), then the probe
+    cudaError_t err = launch_step(A, h->cfg.model, h->cfg.precision, h->wpc, h->grid, h->d_scratch,
+                                  clk, 1, h->stream);
+    if (err == cudaSuccess) err = save_restore(false);
+    if (err == cudaSuccess) err = cudaEventRecord(e0, h->stream);
+    if (err == cudaSuccess)
+      err = launch_step(A, h->cfg.model, h->cfg.precision, h->wpc, h->grid, h->d_scratch, clk,
+                        probe_steps, h->stream);
+    if (err == cudaSuccess) err = cudaEventRecord(e1, h->stream);
+    if (err == cudaSuccess) err = save_restore(false);
+    if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+    if (err != cudaSuccess) {
+      h->wpc = wpc0;
+      h->grid = grid0;
+      h->sched = sched0;
+      return bail(err, "autotune probe");
+    }
+    c.ms_per_step = ms / probe_steps;
+    if (best < 0 || c.ms_per_step < cand[best].ms_per_step) best = (int)i;
+  }
+#undef CLM_TRY
+  h->wpc = cand[best].cols_per_cta / kTile;
+  h->grid = cand[best].grid;
+  h->sched = cand[best].schedule;
+  cand[best].chosen = 1;
+  const cudaError_t err = cudaStreamSynchronize(h->stream);
+  cleanup();
+  if (err != cudaSuccess) return cuda_fail(h, err, "autotune");
+  for (int i = 0; i < (int)cand.size() && i < table_cap; ++i) table[i] = cand[i];
+  if (n_entries) *n_entries = (int32_t)cand.size();
+  return CLM_OK;
+}
+
+int clm_get_launch_config(const clm_handle* h, int32_t* cols_per_cta, int32_t* schedule, int32_t* grid) {
+  if (!h) return CLM_ERR_ARG;
+  if (cols_per_cta) *cols_per_cta = h->wpc * kTile;
+  if (schedule) *schedule = h->sched;
+  if (grid) *grid = h->grid;
   return CLM_OK;
 }
 
@@ -658,7 +939,9 @@ int clm_load_mlp(clm_handle* h, const void* weights, int64_t nbytes) {
   std::memcpy(buf.data() + kMlpParams, f, sizeof(float) * nnorm);
   for (float x : buf)
     if (!std::isfinite(x)) return fail(h, CLM_ERR_ARG, "non-finite value in the weight blob");
+  if (!h->d_mlp || !h->d_guess) drop_graphs(h);
   if (!h->d_mlp) CLM_CUDA(h, cudaMalloc(&h->d_mlp, sizeof(float) * buf.size()));
+  if (!h->guess_grid) CLM_CUDA(h, mlp_guess_setup(h->stride, &h->guess_grid));
   CLM_CUDA(h, cudaMemcpyAsync(h->d_mlp, buf.data(), sizeof(float) * buf.size(), cudaMemcpyHostToDevice, h->stream));
   if (!h->d_guess) {
     const size_t gb = sizeof(float) * 2 * (size_t)std::max<int64_t>(h->ncells_int, 1);

@@ -45,7 +45,8 @@ struct StepArgs {
   double* Fe;           // intF_e  [stride]
   uint32_t* flags;      // [stride]
   int32_t* iters;       // [stride]
-  const float* guess;   // learned Newton guess (internal layout, 2 per cell) or null
+  const float* guess = nullptr;  // learned Newton guess (internal layout, 2 per cell) or null
+  int* tile_ctr = nullptr;       // dynamic tile order: [next tile, warps done], or null (static)
   Earth E;
   EHScalars sc;
   int bc_tw, bc_th, bc_bw, bc_bh;
@@ -56,6 +57,40 @@ struct StepArgs {
   double energy_scale;
   uint64_t seed;
 };
+
+// Start time and step of a launch: by value, or (CUDA graph replay) read
+// from a device array written before each replay: dev[slot] = t0 of this
+// launch, dev[kClockSlots] = dt.
+constexpr int kClockSlots = 64;
+struct StepClock {
+  double t0 = 0.0, dt = 0.0;
+  const double* dev = nullptr;
+  int slot = 0;
+  CLM_HD double start() const { return dev ? dev[slot] : t0; }
+  CLM_HD double step() const { return dev ? dev[kClockSlots] : dt; }
+};
+
+// Dynamic tile order: lane 0 claims the next tile for the warp. The last
+// warp of the launch to finish resets the counter pair, so every launch
+// (direct or replayed in a graph) starts from tile 0 without a memset.
+#ifdef __CUDACC__
+__device__ __forceinline__ int claim_tile(int* ctr) {
+  int t = 0;
+  if ((threadIdx.x & 31) == 0) t = atomicAdd(ctr, 1);
+  return __shfl_sync(0xffffffffu, t, 0);
+}
+
+__device__ __forceinline__ void release_tiles(int* ctr, int nwarps) {
+  if ((threadIdx.x & 31) == 0) {
+    __threadfence();
+    if (atomicAdd(ctr + 1, 1) == nwarps - 1) {
+      atomicExch(ctr, 0);
+      atomicExch(ctr + 1, 0);
+    }
+  }
+  __syncwarp();
+}
+#endif
 
 // Shared-memory view of one warp's column tile: array a, layer k.
 template <typename T>

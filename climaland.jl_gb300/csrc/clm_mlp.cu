@@ -442,12 +442,13 @@ __global__ void features_kernel(StepArgs A, double t, double dt, float* __restri
 // (internal layout), for every 20-layer column. A warp takes 16 columns;
 // its two half-warps build the features of layers 0-9 and 10-19.
 __global__ void __launch_bounds__(kInferWarps * 32)
-    guess_kernel(StepArgs A, const float* __restrict__ P, const float* __restrict__ norm, double t,
-                 double dt, float* __restrict__ guess) {
+    guess_kernel(StepArgs A, const float* __restrict__ P, const float* __restrict__ norm,
+                 StepClock clk, float* __restrict__ guess) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
   stage_forward(S, P, norm);
   __syncthreads();
+  const double t = clk.start(), dt = clk.step();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t4 = lane & 3;
   const int64_t nci = A.L.ncells_int;
   const int nrows = A.L.stride;
@@ -539,13 +540,20 @@ cudaError_t mlp_features(const StepArgs& A, double t, double dt, float* X, cudaS
   return cudaGetLastError();
 }
 
-cudaError_t mlp_guess(const StepArgs& A, const float* P, const float* norm, double t, double dt,
-                      float* guess, cudaStream_t st) {
+// Kernel attribute and persistent grid of the guess kernel: set up once
+// (clm_load_mlp), so the per-step launch makes no other runtime call and can
+// be captured in a CUDA graph.
+cudaError_t mlp_guess_setup(int64_t rows, int* grid) {
   const size_t sm = sizeof(mlp::InferSmem);
   cudaError_t e = cudaFuncSetAttribute(mlp::guess_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  const int grid = infer_grid(mlp::guess_kernel, sm, A.L.stride);
-  mlp::guess_kernel<<<grid, mlp::kInferWarps * 32, sm, st>>>(A, P, norm, t, dt, guess);
+  *grid = infer_grid(mlp::guess_kernel, sm, rows);
+  return cudaGetLastError();
+}
+
+cudaError_t mlp_guess(const StepArgs& A, const float* P, const float* norm, const StepClock& clk,
+                      float* guess, int grid, cudaStream_t st) {
+  mlp::guess_kernel<<<grid, mlp::kInferWarps * 32, sizeof(mlp::InferSmem), st>>>(A, P, norm, clk, guess);
   return cudaGetLastError();
 }
 

@@ -7,7 +7,9 @@
 // a per-warp-slot global scratch area (`scratch`, sized by the launch
 // grid, small enough to stay in L2). The grid is the number of CTAs that
 // fit on the device at once; each warp walks tiles w, w + W, w + 2W, ...
-// (tiles are sorted deepest first, so the walk is balanced).
+// (tiles are sorted deepest first, so the walk is balanced), or, with the
+// dynamic order, claims the next unprocessed tile from an atomic counter
+// (deepest first: longest-processing-time-first list scheduling).
 
 #include <cuda_runtime.h>
 
@@ -29,7 +31,7 @@ constexpr int kEHScratchArrays = 3;  // K, kappa, 1 / rho c
 
 template <typename JT>
 __global__ void __launch_bounds__(128, 1)
-    eh_step_kernel(StepArgs A, double* __restrict__ scratch, double t0, double dt, int nsteps) {
+    eh_step_kernel(StepArgs A, double* __restrict__ scratch, StepClock clk, int nsteps) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* tab = reinterpret_cast<double*>(smem_raw);
   const Tables Tb = fm::stage_tables(tab);
@@ -56,32 +58,38 @@ __global__ void __launch_bounds__(128, 1)
   J.dp = Col<JT>{jw + lay + lane, kTile};
   J.d = Col<JT>{jw + 2 * lay + lane, kTile};
   J.ae = Col<JT>{jw + 3 * lay + lane, kTile};
-  for (int tile = gwarp; tile < A.L.ntiles; tile += nwarps) {
+  const double t0 = clk.start(), dt = clk.step();
+  const bool dyn = A.tile_ctr != nullptr;
+  int tile = dyn ? claim_tile(A.tile_ctr) : gwarp;
+  while (tile < A.L.ntiles) {
     const int s = tile * kTile + lane;
     const int n = A.L.col_n[s];
-    if (n <= 0) continue;
-    const int64_t base = A.L.tile_off[tile] + lane;
-    B.gv = Col<double>{A.v + base, kTile};
-    B.gti = Col<double>{A.ti + base, kTile};
-    B.ge = Col<double>{A.e + base, kTile};
-    if (A.guess) {
-      B.guess_v = Col<const float>{A.guess + base, kTile};
-      B.guess_e = Col<const float>{A.guess + A.L.ncells_int + base, kTile};
+    if (n > 0) {
+      const int64_t base = A.L.tile_off[tile] + lane;
+      B.gv = Col<double>{A.v + base, kTile};
+      B.gti = Col<double>{A.ti + base, kTile};
+      B.ge = Col<double>{A.e + base, kTile};
+      if (A.guess) {
+        B.guess_v = Col<const float>{A.guess + base, kTile};
+        B.guess_e = Col<const float>{A.guess + A.L.ncells_int + base, kTile};
+      }
+      double Fw = A.Fw[s], Fe = A.Fe[s];
+      uint32_t flags = 0;
+      int iters = 0;
+      eh_column<JT>(A, Tb, s, n, A.L.perm[s], B, J, t0, dt, nsteps, Fw, Fe, flags, iters);
+      A.Fw[s] = Fw;
+      A.Fe[s] = Fe;
+      A.flags[s] = flags;
+      A.iters[s] = iters;
     }
-    double Fw = A.Fw[s], Fe = A.Fe[s];
-    uint32_t flags = 0;
-    int iters = 0;
-    eh_column<JT>(A, Tb, s, n, A.L.perm[s], B, J, t0, dt, nsteps, Fw, Fe, flags, iters);
-    A.Fw[s] = Fw;
-    A.Fe[s] = Fe;
-    A.flags[s] = flags;
-    A.iters[s] = iters;
+    tile = dyn ? claim_tile(A.tile_ctr) : tile + nwarps;
   }
+  if (dyn) release_tiles(A.tile_ctr, nwarps);
 }
 
 template <typename JT>
 __global__ void __launch_bounds__(128, 1)
-    richards_step_kernel(StepArgs A, double t0, double dt, int nsteps) {
+    richards_step_kernel(StepArgs A, StepClock clk, int nsteps) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* tab = reinterpret_cast<double*>(smem_raw);
   const Tables Tb = fm::stage_tables(tab);
@@ -99,19 +107,25 @@ __global__ void __launch_bounds__(128, 1)
   RJac<JT> J;
   J.cp = Col<JT>{jw + lane, kTile};
   J.dp = Col<JT>{jw + lay + lane, kTile};
-  for (int tile = gwarp; tile < A.L.ntiles; tile += nwarps) {
+  const double t0 = clk.start(), dt = clk.step();
+  const bool dyn = A.tile_ctr != nullptr;
+  int tile = dyn ? claim_tile(A.tile_ctr) : gwarp;
+  while (tile < A.L.ntiles) {
     const int s = tile * kTile + lane;
     const int n = A.L.col_n[s];
-    if (n <= 0) continue;
-    B.gv = Col<double>{A.v + A.L.tile_off[tile] + lane, kTile};
-    double Fw = A.Fw[s];
-    uint32_t flags = 0;
-    int iters = 0;
-    richards_column<JT>(A, Tb, s, n, A.L.perm[s], B, J, t0, dt, nsteps, Fw, flags, iters);
-    A.Fw[s] = Fw;
-    A.flags[s] = flags;
-    A.iters[s] = iters;
+    if (n > 0) {
+      B.gv = Col<double>{A.v + A.L.tile_off[tile] + lane, kTile};
+      double Fw = A.Fw[s];
+      uint32_t flags = 0;
+      int iters = 0;
+      richards_column<JT>(A, Tb, s, n, A.L.perm[s], B, J, t0, dt, nsteps, Fw, flags, iters);
+      A.Fw[s] = Fw;
+      A.flags[s] = flags;
+      A.iters[s] = iters;
+    }
+    tile = dyn ? claim_tile(A.tile_ctr) : tile + nwarps;
   }
+  if (dyn) release_tiles(A.tile_ctr, nwarps);
 }
 
 // ---------------------------------------------------------------------------
@@ -158,19 +172,19 @@ size_t step_scratch_doubles(int model, int nmax, int wpc, int grid) {
 }
 
 cudaError_t launch_step(const StepArgs& A, int model, int precision, int wpc, int grid,
-                        double* scratch, double t0, double dt, int nsteps, cudaStream_t stream) {
+                        double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream) {
   const size_t smem = step_smem_bytes(model, precision, A.L.nmax, wpc);
   const dim3 block(32 * wpc);
   if (model == CLM_MODEL_ENERGY_HYDROLOGY) {
     if (precision == CLM_PREC_MIXED)
-      eh_step_kernel<float><<<grid, block, smem, stream>>>(A, scratch, t0, dt, nsteps);
+      eh_step_kernel<float><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
     else
-      eh_step_kernel<double><<<grid, block, smem, stream>>>(A, scratch, t0, dt, nsteps);
+      eh_step_kernel<double><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
   } else {
     if (precision == CLM_PREC_MIXED)
-      richards_step_kernel<float><<<grid, block, smem, stream>>>(A, t0, dt, nsteps);
+      richards_step_kernel<float><<<grid, block, smem, stream>>>(A, clk, nsteps);
     else
-      richards_step_kernel<double><<<grid, block, smem, stream>>>(A, t0, dt, nsteps);
+      richards_step_kernel<double><<<grid, block, smem, stream>>>(A, clk, nsteps);
   }
   return cudaGetLastError();
 }

@@ -64,6 +64,14 @@ enum clm_newton_mode {
                            newton_tol (CTS MaximumError on the norm)       */
 };
 
+/* Tile order of the persistent step kernel (no reference counterpart: a
+ * launch-configuration choice). Tiles of 32 columns are sorted deepest
+ * first; results do not depend on the order. */
+enum clm_schedule {
+  CLM_SCHED_STATIC = 0,  /* warp w takes tiles w, w + W, w + 2W, ...        */
+  CLM_SCHED_DYNAMIC = 1  /* warps claim the next tile from an atomic counter */
+};
+
 /* Boundary-condition kinds (src/standalone/Soil/boundary_conditions.jl). */
 enum clm_bc_kind {
   CLM_BC_FLUX = 0,            /* WaterFluxBC / HeatFluxBC: F = f(t)        */
@@ -161,8 +169,13 @@ typedef struct clm_config {
                              in the explicit tendency (EnergyHydrology)    */
   int32_t pad0;
   uint64_t forcing_seed;  /* seed of the rain-pulse hash                   */
-  int32_t cols_per_cta;   /* 0: autotuned / default                        */
-  int32_t reserved[7];
+  int32_t cols_per_cta;   /* 0: default (32); clm_autotune may change it   */
+  int32_t schedule;       /* enum clm_schedule; clm_autotune may change it  */
+  int32_t graph;          /* 1: clm_step / clm_step_async replay their launch
+                             sequence as CUDA graphs captured on first use
+                             (t and dt go through a device array, so one
+                             graph serves every call with the same nsteps) */
+  int32_t reserved[5];
 } clm_config;
 
 typedef struct clm_handle clm_handle;
@@ -220,6 +233,27 @@ int clm_get_state_device(clm_handle* h, double* vartheta_l, double* theta_i,
 int clm_step(clm_handle* h, double t, double dt, int32_t nsteps);
 int clm_step_async(clm_handle* h, double t, double dt, int32_t nsteps);
 int clm_sync(clm_handle* h);
+
+/* Launch-configuration autotuner (no reference counterpart; ClimaLand's
+ * broadcasts are configured by ClimaCore). Times the step kernel on
+ * probe_steps steps (1-64) from the handle's current state at time t, for
+ * every columns-per-CTA (32 x warps, 1-4 warps that fit the shared memory)
+ * and tile order, restores the state, flags and iteration counts, and keeps
+ * the fastest configuration. `table` (may be NULL) receives up to
+ * table_cap entries; *n_entries the number of candidates timed. */
+typedef struct clm_tune_entry {
+  int32_t cols_per_cta;   /* 32 x warps per CTA                            */
+  int32_t schedule;       /* enum clm_schedule                              */
+  int32_t grid;           /* resident CTAs (persistent grid)                */
+  int32_t chosen;         /* 1 for the configuration kept                   */
+  double ms_per_step;     /* CUDA-event time of the probe / probe_steps     */
+} clm_tune_entry;
+int clm_autotune(clm_handle* h, double t, double dt, int32_t probe_steps,
+                 clm_tune_entry* table, int32_t table_cap, int32_t* n_entries);
+
+/* The step kernel's current launch configuration. */
+int clm_get_launch_config(const clm_handle* h, int32_t* cols_per_cta, int32_t* schedule,
+                          int32_t* grid);
 
 /* Run the handle's work on a caller-owned cudaStream_t (NULL restores the
  * handle's own stream). No reference counterpart: it lets a host that owns

@@ -1,0 +1,119 @@
+"""Launch machinery of the persistent step kernel: dynamic tile order, CUDA
+graph replay, capture by a caller (PyTorch) and the autotuner. None of them
+may change a single bit of the results: each column's arithmetic does not
+depend on which warp runs it, in which order, or how the launch was issued."""
+import numpy as np
+import pytest
+
+from climaland_gb300 import _abi as A
+from climaland_gb300 import learned as LG
+from climaland_gb300 import workloads as WL
+from climaland_gb300.device import SoilColumns
+from gpu_common import require_gpu
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    require_gpu()
+    import torch
+    return torch
+
+
+def _run(w, calls, **kw):
+    """Step through `calls` = [(t, nsteps), ...]; return state, flags, iters."""
+    with SoilColumns(w, **kw) as g:
+        for t, n in calls:
+            g.step(t, w.dt, n)
+        f, it = g.status()
+        return g.get_state(), f, it
+
+
+def _same(a, b):
+    (sa, fa, ia), (sb, fb, ib) = a, b
+    for x, y in zip(sa, sb):
+        if x is None:
+            assert y is None
+            continue
+        assert np.array_equal(x, y)
+    assert np.array_equal(fa, fb) and np.array_equal(ia, ib)
+
+
+def test_dynamic_tile_order_bitwise_equals_static(torch):
+    w = WL.uneven_c2(ncol=3000, seed=11)
+    calls = [(w.t0, 6)]
+    for prec in (A.CLM_PREC_FP64, A.CLM_PREC_MIXED):
+        _same(_run(w, calls, precision=prec, schedule=A.CLM_SCHED_STATIC),
+              _run(w, calls, precision=prec, schedule=A.CLM_SCHED_DYNAMIC))
+
+
+def test_graph_replay_bitwise_equals_direct_launches(torch):
+    # 70 steps = launches of 64 + 6 steps; the second call replays the graph
+    # with another start time
+    w = WL.uneven_c2(ncol=2048, seed=12)
+    calls = [(w.t0, 70), (w.t0 + 70 * w.dt, 70), (w.t0 + 140 * w.dt, 3)]
+    for sched in (A.CLM_SCHED_STATIC, A.CLM_SCHED_DYNAMIC):
+        _same(_run(w, calls, schedule=sched, graph=0), _run(w, calls, schedule=sched, graph=1))
+    r = WL.richards_c0(ncol=512, seed=3)
+    rc = [(r.t0, 5), (r.t0 + 5 * r.dt, 5)]
+    _same(_run(r, rc, graph=0), _run(r, rc, graph=1))
+
+
+def test_graph_replay_with_learned_guess(torch):
+    # an untrained network: the guess is poor, Newton still converges and
+    # the graph and direct launches give the same bits
+    w = WL.learned_eval_c3(ncol=1024, seed=5)
+    tr = LG.Trainer(seed=9)
+    tr.set_normalization(np.zeros(LG.N_IN), np.ones(LG.N_IN), np.zeros(LG.N_OUT), np.ones(LG.N_OUT) * 1e-4)
+    blob = tr.blob()
+    tr.close()
+    out = []
+    for graph in (0, 1):
+        with SoilColumns(w, learned_guess=1, graph=graph, **LG.TOL) as g:
+            g.load_mlp(blob)
+            g.step(w.t0, w.dt, 4)
+            g.step(w.t0 + 4 * w.dt, w.dt, 4)
+            f, it = g.status()
+            out.append((g.get_state(), f, it))
+    _same(*out)
+
+
+def test_caller_capture_records_plain_launches(torch):
+    # a host that captures its own stream (PyTorch here, CUDA.jl alike) gets
+    # the library's launches recorded in its graph
+    w = WL.uneven_c2(ncol=1024, seed=13)
+    ref = _run(w, [(w.t0, 3)])
+    s = torch.cuda.Stream()
+    with SoilColumns(w, graph=1) as g:
+        g.set_stream(s.cuda_stream)
+        cg = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(cg, stream=s):
+            g.step_async(w.t0, w.dt, 3)
+        g.set_state(*w.copy_state())  # capture does not run the kernels
+        cg.replay()
+        torch.cuda.synchronize()
+        f, it = g.status()
+        got = (g.get_state(), f, it)
+    _same(ref, got)
+
+
+def test_autotune_restores_state_and_changes_no_result(torch):
+    w = WL.uneven_c2(ncol=4096, seed=14)
+    ref = _run(w, [(w.t0, 5)])
+    with SoilColumns(w) as g:
+        before = g.get_state()
+        table = g.autotune(w.t0, w.dt, probe_steps=2)
+        assert len(table) >= 2
+        assert sum(e["chosen"] for e in table) == 1
+        best = min(table, key=lambda e: e["ms_per_step"])
+        assert best["chosen"] == 1
+        cfg = g.launch_config()
+        assert (cfg["cols_per_cta"], cfg["schedule"], cfg["grid"]) == (
+            best["cols_per_cta"], best["schedule"], best["grid"])
+        for x, y in zip(before, g.get_state()):
+            assert x is None or np.array_equal(x, y)
+        g.step(w.t0, w.dt, 5)
+        f, it = g.status()
+        got = (g.get_state(), f, it)
+    _same(ref, got)
