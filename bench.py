@@ -192,6 +192,104 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def _error_stats(a, b, ncol_cells):
+    """Per-column max |vartheta_l| difference statistics of state a vs b."""
+    d = np.abs(a[0] - b[0])
+    off = ncol_cells
+    col = np.maximum.reduceat(d, off[:-1]) if len(off) > 1 else d
+    return {"max_abs": float(col.max()), "q99": float(np.quantile(col, 0.99)),
+            "q999": float(np.quantile(col, 0.999)),
+            "frac_cols_le_1e-8": float(np.mean(col <= 1e-8)),
+            "frac_cols_le_1e-10": float(np.mean(col <= 1e-10))}
+
+
+def forms_block(args, torch, stream):
+    """The three forms beside the plain path, on subsets that finish in
+    seconds: mixed precision, uneven columns (autotuned, graph-replayed) and
+    learned guess + mixed precision in tolerance mode. Errors are per-column
+    max |vartheta_l| differences from the plain FP64 path on the same
+    columns and steps (the plain path itself is held to the FP64 oracle by
+    the parity tests)."""
+    from climaland_gb300 import _abi as A
+    from climaland_gb300 import device as D
+    from climaland_gb300 import learned as LG
+    from climaland_gb300 import workloads as WL
+
+    nst = args.forms_steps
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+
+    def run(w, tune=True, blob=None, **kw):
+        with D.SoilColumns(w, **kw) as g:
+            g.set_stream(stream.cuda_stream)
+            if tune:
+                g.autotune(w.t0, w.dt, probe_steps=2)
+            if blob is not None:
+                g.load_mlp(blob)
+            its = []
+            t = w.t0
+            for _ in range(nst):  # untimed pass: state, iterations, flags
+                g.step(t, w.dt, 1)
+                t += w.dt
+                f, it = g.status()
+                its.append(it)
+            state = g.get_state()
+            g.set_state(*w.copy_state())
+            g.step(w.t0, w.dt, nst)  # same call as timed: captures its graph if any
+            g.set_state(*w.copy_state())
+            torch.cuda.synchronize()
+            e0.record(stream)
+            g.step_async(w.t0, w.dt, nst)
+            e1.record(stream)
+            stream.synchronize()
+            ms = e0.elapsed_time(e1) / nst
+            its = np.asarray(its, np.float64)
+            return {"state": state, "ms_per_step": ms, "value": w.ncol / ms * 1e3,
+                    "newton_iters_mean": float(its.mean()),
+                    "fallback_frac": float(np.mean((f & A.CLM_COL_GUESS_FALLBACK) > 0)),
+                    "launch_config": g.launch_config()}
+
+    def pub(r, base, w):
+        out = {k: v for k, v in r.items() if k != "state"}
+        out["unit"] = "column-steps/s"
+        if base is not None:
+            out["speedup_vs_plain_fp64"] = r["value"] / base["value"]
+            out["err_vs_plain_fp64"] = _error_stats(r["state"], base["state"], w.offsets)
+        return out
+
+    out = {"steps": nst}
+    # full-scale distribution, 20 layers
+    w4 = WL.full_scale_c4(ncol=args.forms_ncol, seed=0)
+    plain = run(w4)
+    mixed = run(w4, precision=A.CLM_PREC_MIXED)
+    out["full_scale_subset"] = {"workload": w4.name, "plain_fp64": pub(plain, None, w4),
+                                "mixed": pub(mixed, plain, w4)}
+    # (1)+(4) learned guess + mixed precision, tolerance-stopped Newton:
+    # network trained on the plain solver's trajectories (another seed)
+    wtr = WL.full_scale_c4(ncol=65536, seed=7)
+    t0 = time.perf_counter()
+    X, Y = LG.generate(wtr, 32)
+    res = LG.train(X, Y, steps=20000, batch=4096, lr=2e-3)
+    gen_train_s = time.perf_counter() - t0
+    del X, Y
+    tol = dict(newton_mode=A.CLM_NEWTON_TOL, max_iters=20, newton_tol=1e-8, energy_norm_scale=1e-9)
+    plain_tol = run(w4, **tol)
+    learned = run(w4, blob=res.blob, learned_guess=1, precision=A.CLM_PREC_MIXED, **tol)
+    out["full_scale_subset"]["plain_fp64_tol1e-8"] = pub(plain_tol, plain, w4)
+    out["full_scale_subset"]["learned_mixed_tol1e-8"] = pub(learned, plain, w4)
+    out["full_scale_subset"]["learned_training"] = {
+        "pairs": res.nrows, "train_steps": 20000, "loss_first": float(res.loss[:50].mean()),
+        "loss_last": float(res.loss[-200:].mean()), "train_s": res.seconds, "gen_train_s": gen_train_s}
+    # (2) uneven columns, 4-30 layers, CSR: autotuned launch, CUDA graph replay
+    w2 = WL.uneven_c2(ncol=args.forms_ncol, seed=0)
+    u64 = run(w2, graph=1)
+    umx = run(w2, graph=1, precision=A.CLM_PREC_MIXED)
+    out["uneven_4_30"] = {"workload": w2.name, "cells": int(w2.ncells),
+                          "plain_fp64_graph_autotuned": pub(u64, None, w2),
+                          "mixed_graph_autotuned": pub(umx, u64, w2)}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -201,11 +299,15 @@ def main():
     ap.add_argument("--config", default="c4")
     ap.add_argument("--ncol", type=int, default=None)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
-    ap.add_argument("--cpu-sample-cols", type=int, default=16384)
-    ap.add_argument("--cpu-sample-steps", type=int, default=24)
+    ap.add_argument("--cpu-sample-cols", type=int, default=65536)
+    ap.add_argument("--cpu-sample-steps", type=int, default=128)
     ap.add_argument("--ref-sample-cols", type=int, default=32768)
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-forms", action="store_true")
+    ap.add_argument("--forms-ncol", type=int, default=262144)
+    ap.add_argument("--forms-steps", type=int, default=32)
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -237,6 +339,9 @@ def main():
     g = D.SoilColumns(w, precision=prec)
     stream = torch.cuda.Stream()
     g.set_stream(stream.cuda_stream)
+    tune = None
+    if not args.no_autotune:
+        tune = g.autotune(w.t0, w.dt, probe_steps=2)  # the state is restored
 
     def barrier():
         if dist is not None:
@@ -331,6 +436,9 @@ def main():
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(w, args.cpu_sample_cols, args.cpu_sample_steps)
+    forms = None
+    if not args.no_forms and world == 1:
+        forms = forms_block(args, torch, stream)
     line = {
         "metric": "column-steps/s", "value": value, "unit": "column-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
@@ -344,11 +452,13 @@ def main():
         "e2e": {"value": e2e, "unit": "column-steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": h2d, "steps": e2e_steps},
         "gpu_launches": args.steps,
+        "launch_config": dict(g.launch_config(), autotuned=tune is not None),
         "roofline": roofline,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "status": {"flagged_columns": int(np.count_nonzero(flags)),
                    "newton_iters_max": int(iters.max())},
+        "forms": forms,
     }
     print(json.dumps(line), flush=True)
     g.close()
