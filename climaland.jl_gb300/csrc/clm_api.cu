@@ -24,7 +24,7 @@ cudaError_t launch_step(const StepArgs& A, int model, int precision, int wpc, in
                         double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream);
 size_t step_smem_bytes(int model, int precision, int nmax, int wpc);
 cudaError_t step_grid(int model, int precision, int nmax, int wpc, int ntiles, int* grid);
-size_t step_scratch_doubles(int model, int nmax, int wpc, int grid);
+size_t step_scratch_doubles(int model, int precision, int nmax, int wpc, int grid);
 // clm_layout.cu
 cudaError_t ref_to_internal(const Layout& L, const int32_t* ref_off, const double* src,
                             double* dst, int ncomp, cudaStream_t st);
@@ -259,7 +259,7 @@ int build_layout(clm_handle* h, const std::vector<int>& nl) {
   h->wpc = want;
   CLM_CUDA(h, step_grid(h->cfg.model, h->cfg.precision, h->nmax, h->wpc, h->ntiles, &h->grid));
   dfree(h->d_scratch);
-  const size_t nsc = step_scratch_doubles(h->cfg.model, h->nmax, h->wpc, h->grid);
+  const size_t nsc = step_scratch_doubles(h->cfg.model, h->cfg.precision, h->nmax, h->wpc, h->grid);
   if (nsc) CLM_CUDA(h, cudaMalloc(&h->d_scratch, sizeof(double) * nsc));
   h->scratch_doubles = nsc;
   h->guess_grid = 0;
@@ -740,7 +740,7 @@ int clm_autotune(clm_handle* h, double t, double dt, int32_t probe_steps, clm_tu
     if (step_smem_bytes(h->cfg.model, h->cfg.precision, h->nmax, w) > (size_t)dev_smem) break;
     int grid = 0;
     CLM_CUDA(h, step_grid(h->cfg.model, h->cfg.precision, h->nmax, w, h->ntiles, &grid));
-    need = std::max(need, step_scratch_doubles(h->cfg.model, h->nmax, w, grid));
+    need = std::max(need, step_scratch_doubles(h->cfg.model, h->cfg.precision, h->nmax, w, grid));
     for (int sch : {CLM_SCHED_STATIC, CLM_SCHED_DYNAMIC}) {
       clm_tune_entry e{};
       e.cols_per_cta = w * kTile;

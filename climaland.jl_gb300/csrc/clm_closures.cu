@@ -142,8 +142,8 @@ __global__ void closure_kernel(ClosureArgs C) {
       double dv = 0.0, dti = 0.0;
       if (eh && A.phase_change) {
         const double Yti = C.ti[o + k];
-        uint32_t fl = 0;
         const double rc = heat_capacity(E, tlc[k], Yti, rcds);
+        uint32_t fl = 0;
         const double pc = phase_change(Tb, E, g, nu, theta_r, tlc[k], Yti, Tc[k], rc, kapc[k], dz, fl);
         dv = -pc;
         dti = E.rho_l_over_rho_i * pc;

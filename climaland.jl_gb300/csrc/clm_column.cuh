@@ -35,6 +35,7 @@
 #pragma once
 
 #include "clm_internal.cuh"
+#include "clm_physics_ff.cuh"
 
 namespace clm {
 
@@ -92,10 +93,61 @@ CLM_HD void eh_iterate_point(const Tables& Tb, const Earth& E, const EHCol& c, d
   psi_dpsi<true>(Tb, c.g, nu_eff, xv, c.theta_r, c.S_s, psi, D);
 }
 
+// Mixed path: T and psi in double-float (FP64 results), dpsi in float; points
+// outside the double-float range fall back to the FP64 closure.
+struct EHMixed {
+  ff::Tables FT;
+  ColFF cf;
+  EarthFF Ef;
+  F2 rcds, K_sat, omega_ln10, visc_gamma, visc_T_ref;
+  KappaFF kf;
+};
+
+CLM_HD EHMixed make_eh_mixed(const Tables& Tb, const Earth& E, const EHScalars& sc, const EHCol& c) {
+  EHMixed m;
+  m.FT = ff::Tables{Tb.ff};
+  m.cf = make_col_ff(c.nu, c.theta_r, c.g);
+  m.Ef = make_earth_ff(E);
+  m.rcds = ff::from_double(c.rcds);
+  m.K_sat = ff::from_double(c.K_sat);
+  m.omega_ln10 = ff::from_double(sc.omega_ln10);
+  m.visc_gamma = ff::from_double(sc.visc_gamma);
+  m.visc_T_ref = ff::from_double(sc.visc_gamma_T_ref);
+  m.kf = make_kappa_ff(sc, c.nu, c.kdry, c.ksu, c.ksf, c.lku, c.lkf, c.nuom, c.nuq, c.nug);
+  return m;
+}
+
+CLM_HD void eh_iterate_point_mixed(const Tables& Tb, const EHCol& c, const EHMixed& M, double xv,
+                                   double xe, double ti, double& T, double& psi, float& D) {
+  const F2 ti_f = ff::from_double(ti);
+  const F2 v = ff::from_double(xv);
+  const F2 nu_eff = ff::sub(M.cf.nu, ti_f);
+  T = temperature_ff(M.Ef, ff::from_double(xe), ti_f, ff_min(nu_eff, v), M.rcds);
+  if (!psi_dpsi_ff(M.FT, M.cf, nu_eff, v, psi, D)) {
+    double d;
+    psi_dpsi<true>(Tb, c.g, c.nu - ti, xv, c.theta_r, c.S_s, psi, d);
+    D = (float)d;
+  }
+}
+
+// T, psi and dpsi at the iterate on either path (dpsi in the Jacobian type).
+template <typename JT>
+CLM_HD void eh_point(const Tables& Tb, const Earth& E, const EHCol& c, const EHMixed& M, double xv,
+                     double xe, double ti, double& T, double& psi, JT& D) {
+  if constexpr (sizeof(JT) < sizeof(double)) {
+    eh_iterate_point_mixed(Tb, c, M, xv, xe, ti, T, psi, D);
+  } else {
+    eh_iterate_point(Tb, E, c, xv, xe, ti, T, psi, D);
+  }
+}
+
 struct EHBuffers {
   Col<double> gv, gti, ge;          // state (holds U during a step)
   Col<double> xv, xe, fe;           // iterate, energy residual
-  Col<double> K, kap, irc;          // frozen aux
+  Col<double> K, kap, irc;          // frozen aux: K, face kappa / dz (after stage 1), 1 / rho c
+  // mixed path: the Jacobian's face products dt K_face / dz^2, dt kappa_face /
+  // dz^2 and 1 / rho c in float (p == nullptr on the FP64 path)
+  Col<float> awr{nullptr, 0}, akr{nullptr, 0}, ircf{nullptr, 0};
   // learned Newton guess: predicted u_{n+1} - u_n of vartheta_l and rho_e_int
   // (p == nullptr: no guess)
   Col<const float> guess_v{nullptr, 0}, guess_e{nullptr, 0};
@@ -117,6 +169,8 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
   const double rdz = dt * c.inv_dz;
   const double half = 0.5 * c.dz;
   constexpr bool mixed = sizeof(JT) < sizeof(double);
+  EHMixed MX;
+  if constexpr (mixed) MX = make_eh_mixed(Tb, E, sc, c);
 
   for (int step = 0; step < nsteps; ++step) {
     const double t = t0 + step * dt;
@@ -129,6 +183,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
     // ---------------- stage 1: aux at Y_n, explicit tendency, U ----------
     double K0 = 0, T0 = 0, kap0 = 0, psi0 = 0;
     double Kt = 0, Tt = 0, kapt = 0, psit = 0;
+    double kap_prev = 0.0, K_prev = 0.0;
     for (int k = 0; k < n; ++k) {
       const double Yv = B.gv[k], Yti = B.gti[k], Ye = B.ge[k];
       const double nu_eff = c.nu - Yti;
@@ -136,19 +191,44 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       const double v_safe = fmax(Yv, c.theta_r + kSqrtEps);
       const double nu_safe = fmax(nu_eff, c.theta_r + kSqrtEps);
       const double tl = (v_safe < nu_safe) ? v_safe : nu_safe;
-      const double kap = conductivity_heat(Tb, sc, tl, Yti, c.nu, c.kdry, c.ksu, c.ksf, c.lku,
-                                           c.lkf, c.nuom, c.nuq, c.nug);
       const double rc = heat_capacity(E, tl, Yti, c.rcds);
       const double T = temperature(E, Ye, Yti, rc);
-      const Sat sK = saturation(c.nu, Yv, c.theta_r);
-      const double fi = Yti / (tl + Yti - c.theta_r);
-      // impedance_factor * viscosity_factor * hydraulic_conductivity
-      const double K =
-          fm::exp(Tb, -sc.omega_ln10 * fi + sc.visc_gamma * (T - sc.visc_gamma_T_ref)) *
-          conductivity(Tb, c.g, c.K_sat, sK.S);
+      double kap = 0.0, K = 0.0;
+      bool aux_ff = false;
+      if constexpr (mixed) {
+        // kappa and K in double-float
+        const F2 tl_f = ff::from_double(tl), ti_f = ff::from_double(Yti);
+        const F2 guard = ff::add_f(MX.cf.theta_r, 1.4901161193847656e-08f);
+        const F2 S = ff::div(ff::sub(ff_max(ff::from_double(Yv), guard), MX.cf.theta_r),
+                             ff::sub(ff_max(MX.cf.nu, guard), MX.cf.theta_r));
+        const F2 fi = Yti > 0.0 ? ff::div(ti_f, ff::sub(ff::add(tl_f, ti_f), MX.cf.theta_r))
+                                : ff::make(0.0f);
+        const F2 lnf = ff::add(ff::neg(ff::mul(MX.omega_ln10, fi)),
+                               ff::mul(MX.visc_gamma, ff::sub(ff::from_double(T), MX.visc_T_ref)));
+        aux_ff = kappa_ff(MX.FT, MX.kf, tl, Yti, tl_f, ti_f, kap) &&
+                 conductivity_ff(MX.FT, MX.cf, MX.K_sat, S, lnf, K);
+      }
+      if (!aux_ff) {
+        kap = conductivity_heat(Tb, sc, tl, Yti, c.nu, c.kdry, c.ksu, c.ksf, c.lku, c.lkf, c.nuom,
+                                c.nuq, c.nug);
+        const Sat sK = saturation(c.nu, Yv, c.theta_r);
+        const double fi = Yti > 0.0 ? Yti / (tl + Yti - c.theta_r) : 0.0;
+        // impedance_factor * viscosity_factor * hydraulic_conductivity, with
+        // the sqrt(S) of the van Genuchten K inside the same exponential
+        const double lnf = -sc.omega_ln10 * fi + sc.visc_gamma * (T - sc.visc_gamma_T_ref);
+        if (sK.S < 1.0) {
+          const double lS = fm::log(Tb, sK.S);
+          const double s1m = fm::exp(Tb, c.g.inv_m * lS);                  // S^(1/m)
+          const double tm = fm::exp(Tb, c.g.m * fm::log(Tb, 1.0 - s1m));   // (1 - S^(1/m))^m
+          const double f = 1.0 - tm;
+          K = c.K_sat * (f * f) * fm::exp(Tb, lnf + 0.5 * lS);
+        } else {
+          K = c.K_sat * fm::exp(Tb, lnf);
+        }
+      }
       double Uv = Yv, Uti = Yti;
       if (A.phase_change) {
-        const double pc = phase_change(Tb, E, c.g, c.nu, c.theta_r, tl, Yti, T, rc, kap, c.dz, flags);
+        const double pc = phase_change<!mixed>(Tb, E, c.g, c.nu, c.theta_r, tl, Yti, T, rc, kap, c.dz, flags);
         Uv = Yv + dt * (-pc);
         Uti = Yti + dt * (E.rho_l_over_rho_i * pc);
       }
@@ -169,8 +249,22 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         B.xe[k] = Ye;
       }
       B.K[k] = K;
-      B.kap[k] = kap;
-      B.irc[k] = 1.0 / heat_capacity(E, tl, Uti, c.rcds);
+      // face conductances k-1|k, frozen through the Newton solve: kappa on
+      // the face into kappa's slot (the cell value is not used after stage 1)
+      if (k > 0) {
+        const double ak = 0.5 * (kap_prev + kap) * c.inv_dz;
+        B.kap[k - 1] = ak;
+        if constexpr (mixed) {
+          B.awr[k - 1] = (float)(rdz * (0.5 * (K_prev + K) * c.inv_dz));
+          B.akr[k - 1] = (float)(rdz * ak);
+        }
+      }
+      kap_prev = kap;
+      K_prev = K;
+      if constexpr (mixed)
+        B.ircf[k] = 1.0f / (float)heat_capacity(E, tl, Uti, c.rcds);
+      else
+        B.irc[k] = 1.0 / heat_capacity(E, tl, Uti, c.rcds);
       if (k == 0) {
         K0 = K; T0 = T; kap0 = kap;
         if (A.bc_bw == CLM_BC_STATE) {
@@ -236,26 +330,29 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       JT cp_prev = 0, dp_prev = 0;
       double Fw_dn = Fbw, Fe_dn = Fbh;
       double aw_dn = 0.0;
+      JT awr_dn = 0;  // mixed: dt K_face / dz^2 of the face below
       JT D_prev = 0;
       double sum_fv = 0.0, sum_fe = 0.0;
-      double Tc, psic, Dc;
-      eh_iterate_point(Tb, E, c, B.xv[0], B.xe[0], B.gti[0], Tc, psic, Dc);
-      double Kc = B.K[0], kapc = B.kap[0];
+      double Tc, psic;
+      JT Dc;
+      eh_point<JT>(Tb, E, c, MX, B.xv[0], B.xe[0], B.gti[0], Tc, psic, Dc);
+      double Kc = B.K[0];
       double relKc = rho_e_liq(E, Tc) * Kc;
       for (int k = 0; k < n; ++k) {
         double Fw_up, Fe_up, aw_up = 0.0, ae_up = 0.0;
-        double Tn = 0, psin = 0, Dn = 0, Kn = 0, kapn = 0, relKn = 0;
+        double Tn = 0, psin = 0, Kn = 0, relKn = 0;
+        JT Dn = 0, awr_up = 0;
         if (k < n - 1) {
-          eh_iterate_point(Tb, E, c, B.xv[k + 1], B.xe[k + 1], B.gti[k + 1], Tn, psin, Dn);
+          eh_point<JT>(Tb, E, c, MX, B.xv[k + 1], B.xe[k + 1], B.gti[k + 1], Tn, psin, Dn);
           Kn = B.K[k + 1];
-          kapn = B.kap[k + 1];
           relKn = rho_e_liq(E, Tn) * Kn;
           aw_up = 0.5 * (Kc + Kn) * c.inv_dz;
-          const double ak_up = 0.5 * (kapc + kapn) * c.inv_dz;
+          const double ak_up = B.kap[k];  // face k|k+1 (stage 1)
           ae_up = 0.5 * (relKc + relKn) * c.inv_dz;
           const double dh = (psin - psic) + c.dz;
           Fw_up = -aw_up * dh;
           Fe_up = -ak_up * (Tn - Tc) - ae_up * dh;
+          if constexpr (mixed) awr_up = B.awr[k];
         } else {
           Fw_up = Ftw;
           Fe_up = Fth;
@@ -266,15 +363,22 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         const double fe = B.ge[k] + dt * Tee - B.xe[k];
         sum_fv += fv;
         sum_fe += fe;
-        const JT L = (JT)(rdz * aw_dn) * D_prev;
-        const JT U = (k < n - 1) ? (JT)(rdz * aw_up * Dn) : (JT)0;
-        const JT M = (JT)(-rdz * (aw_up + aw_dn) * Dc - 1.0);
-        const JT inv = (JT)1 / (M - L * cp_prev);
+        JT L, U, Md;
+        if constexpr (mixed) {  // rows from the float face products
+          L = awr_dn * D_prev;
+          U = awr_up * Dn;
+          Md = -(awr_up + awr_dn) * Dc - 1.0f;
+        } else {
+          L = (JT)(rdz * aw_dn) * D_prev;
+          U = (k < n - 1) ? (JT)(rdz * aw_up * Dn) : (JT)0;
+          Md = (JT)(-rdz * (aw_up + aw_dn) * Dc - 1.0);
+        }
+        const JT inv = (JT)1 / (Md - L * cp_prev);
         const JT cpk = U * inv;
         const JT dpk = ((JT)fv - L * dp_prev) * inv;
         J.cp[k] = cpk;
         J.dp[k] = dpk;
-        J.d[k] = (JT)Dc;
+        J.d[k] = Dc;
         J.ae[k] = (JT)ae_up;
         B.fe[k] = fe;
         cp_prev = cpk;
@@ -282,8 +386,9 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         Fw_dn = Fw_up;
         Fe_dn = Fe_up;
         aw_dn = aw_up;
-        D_prev = (JT)Dc;
-        Tc = Tn; psic = psin; Dc = Dn; Kc = Kn; kapc = kapn; relKc = relKn;
+        awr_dn = awr_up;
+        D_prev = Dc;
+        Tc = Tn; psic = psin; Dc = Dn; Kc = Kn; relKc = relKn;
       }
       // integrated fluxes (their Jacobian block is -I): x += f
       const double fFw = UFw + dt * (-(Ftw - Fbw)) - xFw;
@@ -310,42 +415,68 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       {
         JT c_prev = 0, d_prev = 0;
         double ak_dn = 0.0;
+        JT akr_dn = 0;
         JT dvm = 0, Dm = 0;
         JT dv0 = J.dp[0] - (JT)corr_v, D0 = J.d[0];
+        // the applied increment in FP64, so that the increments sum to
+        // -sum(f_v) to FP64 rounding (the water budget identity)
+        double dvd0 = (double)J.dp[0] - corr_v;
         JT ae_dn = 0;
-        double kap_c = B.kap[0], irc_c = B.irc[0], irc_m = 0.0;
+        double irc_c = 0.0, irc_m = 0.0;
+        JT ircf_c = 0, ircf_m = 0;
+        if constexpr (mixed)
+          ircf_c = B.ircf[0];
+        else
+          irc_c = B.irc[0];
         for (int k = 0; k < n; ++k) {
           JT dvp = 0, Dp = 0, ae_up = 0;
-          double ak_up = 0.0, kap_n = 0.0, irc_n = 0.0;
+          double dvdp = 0.0;
+          double ak_up = 0.0, irc_n = 0.0;
+          JT akr_up = 0, ircf_n = 0;
           if (k < n - 1) {
             dvp = J.dp[k + 1] - (JT)corr_v;
+            dvdp = (double)J.dp[k + 1] - corr_v;
             Dp = J.d[k + 1];
             ae_up = J.ae[k];
-            kap_n = B.kap[k + 1];
-            irc_n = B.irc[k + 1];
-            ak_up = 0.5 * (kap_c + kap_n) * c.inv_dz;
+            if constexpr (mixed) {
+              akr_up = B.akr[k];
+              ircf_n = B.ircf[k + 1];
+            } else {
+              ak_up = B.kap[k];  // face k|k+1 (stage 1)
+              irc_n = B.irc[k + 1];
+            }
           }
           const JT Gup = (k < n - 1) ? (Dp * dvp - D0 * dv0) : (JT)0;
           const JT Gdn = (k > 0) ? (D0 * dv0 - Dm * dvm) : (JT)0;
           const JT wev = (JT)rdz * (ae_up * Gup - ae_dn * Gdn) - dv0;
           const double g = B.fe[k] - (double)wev;
-          const JT L = (JT)(rdz * ak_dn * irc_m);
-          const JT U = (JT)(rdz * ak_up * irc_n);
-          const JT M = (JT)(-rdz * (ak_up + ak_dn) * irc_c - 1.0);
-          const JT inv = (JT)1 / (M - L * c_prev);
+          JT L, U, Md;
+          if constexpr (mixed) {
+            L = akr_dn * ircf_m;
+            U = akr_up * ircf_n;
+            Md = -(akr_up + akr_dn) * ircf_c - 1.0f;
+          } else {
+            L = (JT)(rdz * ak_dn * irc_m);
+            U = (JT)(rdz * ak_up * irc_n);
+            Md = (JT)(-rdz * (ak_up + ak_dn) * irc_c - 1.0);
+          }
+          const JT inv = (JT)1 / (Md - L * c_prev);
           const JT ck = U * inv;
           const JT dk = ((JT)g - L * d_prev) * inv;
           J.cp[k] = ck;
           J.dp[k] = dk;
           c_prev = ck;
           d_prev = dk;
-          const double dvd = (double)dv0;
+          const double dvd = dvd0;
           B.xv[k] -= dvd;
           state2 += dvd * dvd;
           dvm = dv0; Dm = D0; dv0 = dvp; D0 = Dp;
+          dvd0 = dvdp;
           ae_dn = ae_up;
           ak_dn = ak_up;
-          irc_m = irc_c; irc_c = irc_n; kap_c = kap_n;
+          akr_dn = akr_up;
+          irc_m = irc_c; irc_c = irc_n;
+          ircf_m = ircf_c; ircf_c = ircf_n;
         }
       }
       // sweep 4 (top -> bottom): delta rho e

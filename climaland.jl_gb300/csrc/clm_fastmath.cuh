@@ -34,24 +34,52 @@ struct Tables {
   const double* invc;
   const double* logc_hi;
   const double* logc_lo;
+  const float* ff;  // 2^(j/64) as float pairs (hi[64], lo[64]) for clm_ff.cuh
 };
+
+// Staged size in doubles: the FP64 tables, then 128 floats of pairs.
+constexpr int kStageDoubles = TABLE_SIZE + 64;
 
 static const double kTableHost[TABLE_SIZE] = CLM_FM_TABLE_INIT;
 
 inline Tables host_tables() {
-  return Tables{kTableHost, kTableHost + 64, kTableHost + 128, kTableHost + 192};
+  static float pairs[128];
+  static bool filled = false;
+  if (!filled) {
+    for (int j = 0; j < 64; ++j) {
+      const float hi = (float)kTableHost[j];
+      pairs[j] = hi;
+      pairs[64 + j] = (float)(kTableHost[j] - (double)hi);
+    }
+    filled = true;
+  }
+  return Tables{kTableHost, kTableHost + 64, kTableHost + 128, kTableHost + 192, pairs};
 }
 
 #ifdef __CUDACC__
 static __constant__ double kTableConst[TABLE_SIZE] = CLM_FM_TABLE_INIT;
 
-// Copy the tables into shared memory (TABLE_SIZE doubles at `sm`); the
-// caller synchronises the block before use. Lanes look up data-dependent
-// entries, which shared memory serves without the serialisation that
-// divergent constant-memory reads incur.
+// Copy the tables into shared memory (stage_doubles<kPairs>() doubles at
+// `sm`); the caller synchronises the block before use. Lanes look up
+// data-dependent entries, which shared memory serves without the
+// serialisation that divergent constant-memory reads incur. kPairs: also the
+// float pairs of the double-float code (mixed path only).
+template <bool kPairs>
+__host__ __device__ constexpr int stage_doubles() { return kPairs ? kStageDoubles : TABLE_SIZE; }
+
+template <bool kPairs = false>
 __device__ __forceinline__ Tables stage_tables(double* sm) {
   for (int i = threadIdx.x; i < TABLE_SIZE; i += blockDim.x) sm[i] = kTableConst[i];
-  return Tables{sm, sm + 64, sm + 128, sm + 192};
+  float* pairs = nullptr;
+  if (kPairs) {
+    pairs = reinterpret_cast<float*>(sm + TABLE_SIZE);
+    for (int j = threadIdx.x; j < 64; j += blockDim.x) {
+      const float hi = (float)kTableConst[j];
+      pairs[j] = hi;
+      pairs[64 + j] = (float)(kTableConst[j] - (double)hi);
+    }
+  }
+  return Tables{sm, sm + 64, sm + 128, sm + 192, pairs};
 }
 #endif
 

@@ -1,0 +1,258 @@
+// Double-float ("ff") arithmetic on the FP32 pipe for the mixed path.
+//
+// GB300 issues FP32 at many times its FP64 rate. The mixed path evaluates the
+// transcendental soil closures (van Genuchten powers, hydraulic and thermal
+// conductivity, temperature) on unevaluated pairs hi + lo of floats, which
+// carry about 48 significant bits (relative error near 2^-44 after a few
+// operations); IEEE FP64 stays for the Newton residual assembly, the state
+// increments, the phase partition and the budgets.
+//
+// Algorithms (published; written here from their descriptions):
+//   two_sum            Knuth, TAOCP vol. 2, 4.2.2 (6 flops, any order)
+//   fast_two_sum       Dekker 1971 (|a| >= |b|)
+//   two_prod           with a fused multiply-add (exact product error)
+//   add, mul, div      Joldes, Muller, Popescu, "Tight and rigorous error
+//                      bounds for basic building blocks of double-word
+//                      arithmetic", ACM TOMS 44(2) 2017: AccurateDWPlusDW,
+//                      DWTimesDW (FMA variant), DWDivDW
+//   exp                table-driven (2^(j/64), Tang 1989) with a short
+//                      polynomial on a double-word reduced argument
+//   log                one Newton step y + x e^(-y) - 1 from the float log
+// Every routine compiles for host and device, so the CPU tests check the
+// same code; host builds must not contract a*b+c (-ffp-contract=off).
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+#ifndef CLM_HD
+#define CLM_HD __host__ __device__ __forceinline__
+#endif
+
+namespace clm {
+namespace ff {
+
+struct F2 {
+  float hi, lo;
+};
+
+CLM_HD uint32_t fbits(float x) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(x);
+#else
+  uint32_t b;
+  std::memcpy(&b, &x, sizeof b);
+  return b;
+#endif
+}
+
+CLM_HD float ffrom(uint32_t b) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(b);
+#else
+  float x;
+  std::memcpy(&x, &b, sizeof x);
+  return x;
+#endif
+}
+
+CLM_HD uint64_t dbits(double x) {
+#ifdef __CUDA_ARCH__
+  return (uint64_t)__double_as_longlong(x);
+#else
+  uint64_t b;
+  std::memcpy(&b, &x, sizeof b);
+  return b;
+#endif
+}
+
+CLM_HD double dfrom(uint64_t b) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)b);
+#else
+  double x;
+  std::memcpy(&x, &b, sizeof x);
+  return x;
+#endif
+}
+
+// ---- error-free transformations -------------------------------------------
+CLM_HD F2 two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  const float e = (a - (s - bb)) + (b - bb);
+  return F2{s, e};
+}
+
+CLM_HD F2 fast_two_sum(float a, float b) {
+  const float s = a + b;
+  const float e = b - (s - a);
+  return F2{s, e};
+}
+
+CLM_HD F2 two_prod(float a, float b) {
+  const float p = a * b;
+  const float e = fmaf(a, b, -p);
+  return F2{p, e};
+}
+
+// ---- double-word operations ---------------------------------------------------
+CLM_HD F2 make(float x) { return F2{x, 0.0f}; }
+CLM_HD F2 neg(F2 x) { return F2{-x.hi, -x.lo}; }
+
+// AccurateDWPlusDW (relative error <= 3u^2 + 13u^3, u = 2^-24)
+CLM_HD F2 add(F2 x, F2 y) {
+  F2 s = two_sum(x.hi, y.hi);
+  const F2 t = two_sum(x.lo, y.lo);
+  float c = s.lo + t.hi;
+  const F2 v = fast_two_sum(s.hi, c);
+  const float w = t.lo + v.lo;
+  return fast_two_sum(v.hi, w);
+}
+
+CLM_HD F2 sub(F2 x, F2 y) { return add(x, neg(y)); }
+
+// DWPlusFP (relative error <= 2u^2)
+CLM_HD F2 add_f(F2 x, float y) {
+  const F2 s = two_sum(x.hi, y);
+  const float v = x.lo + s.lo;
+  return fast_two_sum(s.hi, v);
+}
+
+// DWTimesDW with FMA (relative error <= 4u^2)
+CLM_HD F2 mul(F2 x, F2 y) {
+  const F2 c = two_prod(x.hi, y.hi);
+  float tl = x.hi * y.lo;
+  tl = fmaf(x.lo, y.hi, tl);
+  const float cl = c.lo + tl;
+  return fast_two_sum(c.hi, cl);
+}
+
+// DWTimesFP with FMA (relative error <= 2u^2)
+CLM_HD F2 mul_f(F2 x, float y) {
+  const F2 c = two_prod(x.hi, y);
+  const float cl = fmaf(x.lo, y, c.lo);
+  return fast_two_sum(c.hi, cl);
+}
+
+// DWDivDW (relative error <= 15u^2 + 56u^3)
+CLM_HD F2 div(F2 x, F2 y) {
+  const float th = x.hi / y.hi;
+  const F2 r = mul_f(y, th);
+  const float ph = x.hi - r.hi;
+  const float dl = x.lo - r.lo;
+  const float d = ph + dl;
+  const float tl = d / y.hi;
+  return fast_two_sum(th, tl);
+}
+
+// ---- conversions ----------------------------------------------------------------
+// double -> hi + lo by splitting the significand with integer operations (no
+// FP64 instruction): hi keeps the leading 24 bits, lo the next 24 (rounded),
+// then renormalised. For |d| in [2^-70, 2^100] (both parts stay normal);
+// outside that range (and for 0, non-finite) through float conversions.
+CLM_HD F2 from_double(double d) {
+  const uint64_t b = dbits(d);
+  const int e = (int)((b >> 52) & 0x7FF);
+  if (e < 1023 - 70 || e > 1023 + 100) {
+    const float hi = (float)d;
+    return F2{hi, (float)(d - (double)hi)};
+  }
+  const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+  const uint64_t m = b & 0x000FFFFFFFFFFFFFull;
+  // hi: exponent e, top 23 fraction bits (truncated)
+  const uint32_t hib = sign | ((uint32_t)(e - 1023 + 127) << 23) | (uint32_t)(m >> 29);
+  const float hi = ffrom(hib);
+  // lo: the remaining 29 fraction bits, value rem * 2^(e - 1023 - 52)
+  const uint32_t rem = (uint32_t)(m & 0x1FFFFFFFu);
+  const float scale = ffrom((uint32_t)(e - 1023 - 52 + 127) << 23);  // 2^(e-1075), normal
+  const float lo = (float)rem * scale;  // rounds rem to 24 bits
+  return fast_two_sum(hi, sign ? -lo : lo);
+}
+
+// float -> double by re-biasing the exponent (normal floats; zero, subnormal
+// and non-finite values through the conversion instruction).
+CLM_HD double widen(float x) {
+  const uint32_t b = fbits(x);
+  const uint32_t e = (b >> 23) & 0xFF;
+  if (e == 0 || e == 0xFF) return (double)x;
+  const uint64_t s = (uint64_t)(b & 0x80000000u) << 32;
+  return dfrom(s | ((uint64_t)(e - 127 + 1023) << 52) | ((uint64_t)(b & 0x7FFFFFu) << 29));
+}
+
+// hi + lo -> double: both are exact in double; one FP64 addition.
+CLM_HD double to_double(F2 x) { return widen(x.hi) + widen(x.lo); }
+
+// ---- tables -----------------------------------------------------------------------
+// 2^(j/64), j = 0..63, as double-float pairs (hi[64] then lo[64]).
+struct Tables {
+  const float* t;  // 128 floats
+};
+
+// ---- exp and log ------------------------------------------------------------------
+// Argument range of exp at full double-float precision: [kExpMin, kExpMax]
+// (the result's lo word stays normal; 2^k stays normal).
+constexpr float kExpMin = -65.0f;
+constexpr float kExpMax = 80.0f;
+
+// exp(x) for x.hi in [kExpMin, kExpMax] (the caller checks). x = k ln2/64 + r,
+// |r| <= ln2/128, with ln2/64 split as C1 (11 bits: k C1 is exact for
+// |k| < 2^13) + C2 (24 bits) + C3; e^r - 1 = r + r^2 (1/2 + r c(r)), c(r) =
+// 1/6 + r/24 + r^2/120 in float (its error enters below 2^-48).
+CLM_HD F2 exp(const Tables& T, F2 x) {
+  const float kInvL = 92.33248138427734f;          // 64 / ln2
+  const float C1 = 0.010833740234375f;             // ln2/64 to 11 significant bits
+  const float C2 = -3.3155381515825866e-06f;       // ln2/64 - C1 to 24 bits
+  const float C3 = 2.572804640231345e-14f;         // remainder
+  const float kf = rintf(x.hi * kInvL);
+  const float t = fmaf(-kf, C1, x.hi);  // exact
+  const F2 p = two_prod(kf, C2);
+  F2 r = two_sum(t, -p.hi);  // exact
+  r = add_f(r, x.lo);        // x.lo kept to the last bit
+  r = fast_two_sum(r.hi, r.lo - (p.lo + kf * C3));
+  const int k = (int)kf;
+  const int j = k & 63;
+  const int m = (k - j) / 64;
+  const float c = fmaf(fmaf(r.hi, 1.0f / 120.0f, 1.0f / 24.0f), r.hi, 1.0f / 6.0f);
+  const F2 s = two_sum(0.5f, r.hi * c);
+  const F2 q = mul(mul(r, r), s);
+  const F2 em1 = add(r, q);  // e^r - 1
+  const F2 tj = F2{T.t[j], T.t[64 + j]};
+  const F2 y = add(tj, mul(tj, em1));
+  const float sc = ffrom((uint32_t)(m + 127) << 23);  // 2^m
+  return F2{y.hi * sc, y.lo * sc};
+}
+
+// log(x) for x > 0 (normal float hi): x = 2^k xm with xm in [1, 2) (exact
+// scaling), y0 = logf(xm.hi), t = xm e^(-y0) - 1 (|t| ~ 1e-7, exp argument
+// within +-0.7), log x = k ln2 + y0 + t - t^2/2 (+ O(t^3)); ln2 split as
+// L1 (16 bits: k L1 exact for |k| < 2^8) + L2 + L3.
+CLM_HD F2 log(const Tables& T, F2 x) {
+  const float L1 = 0.693145751953125f;
+  const float L2 = 1.428606765330187e-06f;
+  const float L3 = 5.497923148104107e-14f;
+  const int k = (int)((fbits(x.hi) >> 23) & 0xFF) - 127;
+  const float sc = ffrom((uint32_t)(127 - k) << 23);  // 2^-k
+  const F2 xm = F2{x.hi * sc, x.lo * sc};
+  const float y0 = logf(xm.hi);
+  const F2 e = exp(T, make(-y0));
+  const F2 t = add_f(mul(xm, e), -1.0f);
+  const float kf = (float)k;
+  F2 y = add(two_sum(kf * L1, y0), t);  // k L1 exact
+  y = add(y, two_prod(kf, L2));
+  return add_f(y, fmaf(kf, L3, -0.5f * t.hi * t.hi));
+}
+
+// ---- table staging -------------------------------------------------------------------
+// From the FP64 table of 2^(j/64): hi = float(v), lo = float(v - hi).
+CLM_HD void fill_table(const double* exp2j, float* out) {
+  for (int j = 0; j < 64; ++j) {
+    const float hi = (float)exp2j[j];
+    out[j] = hi;
+    out[64 + j] = (float)(exp2j[j] - (double)hi);
+  }
+}
+
+}  // namespace ff
+}  // namespace clm

@@ -37,6 +37,7 @@ struct Earth {
   double rho_i_LH_f0;           // latent energy per unit ice fraction
   double grav_over_LH_f0;       // Tf_depressed exponent
   double LH_f0_over_grav;       // psi_T prefactor
+  double inv_T_freeze;          // 1 / T_freeze
 };
 
 inline Earth make_earth(const clm_earth_params& e) {
@@ -54,6 +55,7 @@ inline Earth make_earth(const clm_earth_params& e) {
   E.rho_i_LH_f0 = e.rho_i * e.LH_f0;
   E.grav_over_LH_f0 = e.grav / e.LH_f0;
   E.LH_f0_over_grav = e.LH_f0 / e.grav;
+  E.inv_T_freeze = 1.0 / e.T_freeze;
   return E;
 }
 
@@ -211,13 +213,47 @@ CLM_HD double conductivity_heat(const Tables& T, const EHScalars& sc, double the
 }
 
 // Phase-change source (soil_heat_parameterizations.jl:89-122) including
-// thermal_time (:60-62): (theta_l - theta_star) / tau,
-// tau = 3 rho c dz^2 / kappa. For T >= T_freeze the heaviside factor is
-// zero without evaluating Tf (Tf <= T_freeze), and theta_star is then
-// inverse_matric_potential(matric_potential(S)) = S (nu - theta_r) + theta_r.
+// thermal_time (:60-62): (theta_l - theta_star) / tau, tau = 3 rho c dz^2 /
+// kappa.
+//
+// kRefForm (the plain FP64 path) evaluates the reference's own sequence:
+// psi_w0 = matric_potential(S(theta_tot)), Tf = max(T_freeze exp(g psi_w0 /
+// L_f), 1), psi_T = L_f/g log(T/Tf) heaviside(Tf - T), theta_star =
+// inverse_matric_potential(psi_w0 + psi_T). For T >= T_freeze the heaviside
+// factor is zero without evaluating Tf (Tf <= T_freeze), and theta_star is
+// then inverse_matric_potential(matric_potential(S)) = S (nu - theta_r) +
+// theta_r.
+//
+// The reduced form (mixed path) uses that with this Tf,
+//   psi_w0 + L_f/g log(T/Tf) = L_f/g log(T/T_freeze) =: psi_T,
+// independent of psi_w0, and Tf > T <=> psi_w0 > psi_T <=> S(theta_tot) > S_T
+// with S_T = inverse_matric_potential(psi_T) (the matric potential increases
+// with S). So theta_star = min(S(theta_tot), S_T) (nu - theta_r) + theta_r:
+// one log and the two powers of inverse_matric_potential, no matric_potential
+// and no Tf. The Tf >= 1 K clamp acts only where psi_w0 < -L_f/g
+// log(T_freeze), where S(theta_tot) < S_T for every T > 1 K, so the min keeps
+// S(theta_tot) as the clamped reference does; both branches agree at
+// S(theta_tot) = S_T. It avoids the reference's cancellation of psi_w0
+// against itself, which leaves up to ~1e-11 of theta_l / tau: columns whose
+// trajectory switches a discontinuous closure (the Kersten number at
+// theta_i = eps) follow that rounding, so the plain path keeps the
+// reference's sequence.
+template <bool kRefForm = true>
 CLM_HD double phase_change(const Tables& T, const Earth& E, const VG& g, double nu,
                            double theta_r, double theta_l, double theta_i, double Tk,
                            double rhoc, double kappa, double dz, uint32_t& flags) {
+  if (!kRefForm) {
+    const double theta_tot = fmin(E.rho_i_over_rho_l * theta_i + theta_l, nu);
+    double S = saturation(nu, theta_tot, theta_r).S;
+    if (Tk < E.T_freeze) {
+      const double psi_T = E.LH_f0_over_grav * fm::log(T, Tk * E.inv_T_freeze);
+      const double x = fm::exp(T, g.n * fm::log(T, g.alpha * fabs(psi_T)));  // (alpha|psi|)^n
+      const double S_T = fm::exp(T, -g.m * fm::log(T, 1.0 + x));             // (1 + x)^(-m)
+      S = fmin(S, S_T);
+    }
+    const double theta_star = S * (nu - theta_r) + theta_r;
+    return (theta_l - theta_star) * kappa / (3.0 * rhoc * (dz * dz));
+  }
   const double theta_tot = fmin(E.rho_i_over_rho_l * theta_i + theta_l, nu);
   double theta_star;
   double S;

@@ -1,9 +1,9 @@
 // Step kernels: persistent warps over 32-column tiles, one thread per
 // column, running the column code of clm_column.cuh.
 //
-// Shared memory per CTA: the exp/log tables (2 KB), then per warp the
-// Newton iterate, the energy residual and the Jacobian/Thomas arrays of its
-// tile. The frozen aux arrays (K, kappa, 1/rho c) of EnergyHydrology live in
+// Shared memory per CTA: the exp/log tables (2 KB; the mixed EnergyHydrology
+// kernel also 0.5 KB of double-float pairs), then per warp the Newton
+// iterate, the energy residual and the Jacobian/Thomas arrays of its tile. The frozen aux arrays (K, kappa, 1/rho c) of EnergyHydrology live in
 // a per-warp-slot global scratch area (`scratch`, sized by the launch
 // grid, small enough to stay in L2). The grid is the number of CTAs that
 // fit on the device at once; each warp walks tiles w, w + W, w + 2W, ...
@@ -27,32 +27,44 @@ __host__ __device__ constexpr size_t richards_smem_per_layer() {
   return sizeof(double) + 2 * sizeof(JT);  // xv | cp, dp
 }
 
-constexpr int kEHScratchArrays = 3;  // K, kappa, 1 / rho c
+// Per-warp scratch slots of nmax x 32 doubles: K, face kappa and 1 / rho c
+// (FP64 path); K, face kappa and the float Jacobian arrays 1 / rho c,
+// dt K_face / dz^2 and dt kappa_face / dz^2 packed into two slots (mixed).
+__host__ __device__ constexpr int eh_scratch_slots(bool mixed) { return mixed ? 4 : 3; }
 
 template <typename JT>
 __global__ void __launch_bounds__(128, 1)
     eh_step_kernel(StepArgs A, double* __restrict__ scratch, StepClock clk, int nsteps) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* tab = reinterpret_cast<double*>(smem_raw);
-  const Tables Tb = fm::stage_tables(tab);
+  constexpr bool kMixed = sizeof(JT) < sizeof(double);
+  constexpr int kTab = fm::stage_doubles<kMixed>();
+  const Tables Tb = fm::stage_tables<kMixed>(tab);
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const int wpc = blockDim.x >> 5;
   const int nmax = A.L.nmax;
   const int64_t lay = (int64_t)nmax * kTile;
-  double* dw = tab + fm::TABLE_SIZE + (int64_t)warp * 3 * lay;
-  JT* jw = reinterpret_cast<JT*>(tab + fm::TABLE_SIZE + (int64_t)wpc * 3 * lay) + (int64_t)warp * 4 * lay;
+  double* dw = tab + kTab + (int64_t)warp * 3 * lay;
+  JT* jw = reinterpret_cast<JT*>(tab + kTab + (int64_t)wpc * 3 * lay) + (int64_t)warp * 4 * lay;
   const int gwarp = blockIdx.x * wpc + warp;
   const int nwarps = gridDim.x * wpc;
-  double* sw = scratch + (int64_t)gwarp * kEHScratchArrays * lay;
+  double* sw = scratch + (int64_t)gwarp * eh_scratch_slots(kMixed) * lay;
   EHBuffers B;
   B.xv = Col<double>{dw + lane, kTile};
   B.xe = Col<double>{dw + lay + lane, kTile};
   B.fe = Col<double>{dw + 2 * lay + lane, kTile};
   B.K = Col<double>{sw + lane, kTile};
   B.kap = Col<double>{sw + lay + lane, kTile};
-  B.irc = Col<double>{sw + 2 * lay + lane, kTile};
+  if constexpr (kMixed) {
+    float* fw = reinterpret_cast<float*>(sw + 2 * lay);
+    B.ircf = Col<float>{fw + lane, kTile};
+    B.awr = Col<float>{fw + lay + lane, kTile};
+    B.akr = Col<float>{fw + 2 * lay + lane, kTile};
+  } else {
+    B.irc = Col<double>{sw + 2 * lay + lane, kTile};
+  }
   EHJac<JT> J;
   J.cp = Col<JT>{jw + lane, kTile};
   J.dp = Col<JT>{jw + lay + lane, kTile};
@@ -139,7 +151,10 @@ size_t step_smem_bytes(int model, int precision, int nmax, int wpc) {
   else
     per_layer = precision == CLM_PREC_MIXED ? richards_smem_per_layer<float>()
                                             : richards_smem_per_layer<double>();
-  return fm::TABLE_SIZE * sizeof(double) + per_layer * (size_t)nmax * kTile * wpc;
+  const int tab = (model == CLM_MODEL_ENERGY_HYDROLOGY && precision == CLM_PREC_MIXED)
+                      ? fm::stage_doubles<true>()
+                      : fm::stage_doubles<false>();
+  return tab * sizeof(double) + per_layer * (size_t)nmax * kTile * wpc;
 }
 
 static void* step_fn(int model, int precision) {
@@ -166,9 +181,9 @@ cudaError_t step_grid(int model, int precision, int nmax, int wpc, int ntiles, i
   return cudaSuccess;
 }
 
-size_t step_scratch_doubles(int model, int nmax, int wpc, int grid) {
+size_t step_scratch_doubles(int model, int precision, int nmax, int wpc, int grid) {
   if (model != CLM_MODEL_ENERGY_HYDROLOGY) return 0;
-  return (size_t)grid * wpc * kEHScratchArrays * nmax * kTile;
+  return (size_t)grid * wpc * eh_scratch_slots(precision == CLM_PREC_MIXED) * nmax * kTile;
 }
 
 cudaError_t launch_step(const StepArgs& A, int model, int precision, int wpc, int grid,

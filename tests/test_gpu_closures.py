@@ -54,9 +54,13 @@ def test_closures(name):
         eg = g.exp_tendency(t)
         eo = o.exp_tendency(st, t)
         for a, b in zip(eg, eo):
-            # phase change of unfrozen cells is a rounding-level difference
+            # At freezing-curve equilibrium the phase-change source is
+            # rounding noise. The reference form psi_w0 + L_f/g log(T/Tf)
+            # cancels psi_w0 against itself (the kernel evaluates the equal
+            # L_f/g log(T/T_freeze)), which leaves up to ~1e-11 of theta_l/tau
+            # (~1e-17 1/s here): 1e-16 1/s is 5e-14 of vartheta per step.
             sc = np.max(np.abs(b)) + 1e-300
-            assert np.max(np.abs(a - b)) <= 1e-9 * sc + 1e-18
+            assert np.max(np.abs(a - b)) <= 1e-9 * sc + 1e-16
         ig = g.imp_tendency(t)
         io = o.imp_tendency(st, t)
         # face differences amplify rounding: compare against the flux scale

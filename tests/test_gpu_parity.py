@@ -64,6 +64,27 @@ def test_full_scale_c4_tolerance_mode():
     report("full_scale_c4_tol", check_parity(w, 96, oracle_cfg=TOL_MODE, **TOL_MODE))
 
 
+# Mixed path (FP32 Jacobian and Thomas; double-float closures; FP64 residual
+# assembly, increments, phase partition and budgets): 1e-8 wherever the
+# oracle reproduces itself under perturbations of the double-float closures'
+# size (2^-44 relative per step), budgets as the plain path.
+MIXED = dict(tol_state=1e-8, noise=2.0 ** -44, precision=A.CLM_PREC_MIXED)
+
+
+@pytest.mark.parametrize("name,make,nsteps", [
+    ("full_scale", lambda: WL.full_scale_c4(ncol=1024), 48),
+    ("energy_hydrology", lambda: WL.energy_hydrology_c1().subset(1024), 48),
+    ("uneven", lambda: WL.uneven_c2().subset(1024), 48),
+])
+def test_mixed_precision_within_1e8(name, make, nsteps):
+    report(f"mixed_{name}", check_parity(make(), nsteps, **MIXED))
+
+
+def test_mixed_precision_tolerance_mode():
+    w = WL.full_scale_c4(ncol=512)
+    report("mixed_full_scale_tol", check_parity(w, 48, oracle_cfg=TOL_MODE, **TOL_MODE, **MIXED))
+
+
 def test_richards_tolerance_mode():
     w = WL.richards_c0(ncol=512)
     st = check_parity(w, 48, oracle_cfg=TOL_MODE, **TOL_MODE)
