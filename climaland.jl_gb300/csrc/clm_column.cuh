@@ -148,6 +148,9 @@ struct EHBuffers {
   // mixed path: the Jacobian's face products dt K_face / dz^2, dt kappa_face /
   // dz^2 and 1 / rho c in float (p == nullptr on the FP64 path)
   Col<float> awr{nullptr, 0}, akr{nullptr, 0}, ircf{nullptr, 0};
+  // face water conductance K_face / dz, precomputed per step (p == nullptr:
+  // computed in every Newton iteration, the same value)
+  Col<double> aw{nullptr, 0};
   // learned Newton guess: predicted u_{n+1} - u_n of vartheta_l and rho_e_int
   // (p == nullptr: no guess)
   Col<const float> guess_v{nullptr, 0}, guess_e{nullptr, 0};
@@ -254,6 +257,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       if (k > 0) {
         const double ak = 0.5 * (kap_prev + kap) * c.inv_dz;
         B.kap[k - 1] = ak;
+        if (B.aw.p) B.aw[k - 1] = 0.5 * (K_prev + K) * c.inv_dz;
         if constexpr (mixed) {
           B.awr[k - 1] = (float)(rdz * (0.5 * (K_prev + K) * c.inv_dz));
           B.akr[k - 1] = (float)(rdz * ak);
@@ -346,7 +350,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
           eh_point<JT>(Tb, E, c, MX, B.xv[k + 1], B.xe[k + 1], B.gti[k + 1], Tn, psin, Dn);
           Kn = B.K[k + 1];
           relKn = rho_e_liq(E, Tn) * Kn;
-          aw_up = 0.5 * (Kc + Kn) * c.inv_dz;
+          aw_up = B.aw.p ? B.aw[k] : 0.5 * (Kc + Kn) * c.inv_dz;
           const double ak_up = B.kap[k];  // face k|k+1 (stage 1)
           ae_up = 0.5 * (relKc + relKn) * c.inv_dz;
           const double dh = (psin - psic) + c.dz;

@@ -27,10 +27,11 @@ __host__ __device__ constexpr size_t richards_smem_per_layer() {
   return sizeof(double) + 2 * sizeof(JT);  // xv | cp, dp
 }
 
-// Per-warp scratch slots of nmax x 32 doubles: K, face kappa and 1 / rho c
-// (FP64 path); K, face kappa and the float Jacobian arrays 1 / rho c,
-// dt K_face / dz^2 and dt kappa_face / dz^2 packed into two slots (mixed).
-__host__ __device__ constexpr int eh_scratch_slots(bool mixed) { return mixed ? 4 : 3; }
+// Per-warp scratch slots of nmax x 32 doubles: K, face kappa / dz, face
+// K / dz and 1 / rho c (FP64 path); K, face kappa / dz, face K / dz and the
+// float Jacobian arrays 1 / rho c, dt K_face / dz^2 and dt kappa_face / dz^2
+// packed into two slots (mixed).
+__host__ __device__ constexpr int eh_scratch_slots(bool mixed) { return mixed ? 5 : 4; }
 
 template <typename JT>
 __global__ void __launch_bounds__(128, 1)
@@ -57,6 +58,7 @@ __global__ void __launch_bounds__(128, 1)
   B.fe = Col<double>{dw + 2 * lay + lane, kTile};
   B.K = Col<double>{sw + lane, kTile};
   B.kap = Col<double>{sw + lay + lane, kTile};
+  B.aw = Col<double>{sw + (kMixed ? 4 : 3) * lay + lane, kTile};
   if constexpr (kMixed) {
     float* fw = reinterpret_cast<float*>(sw + 2 * lay);
     B.ircf = Col<float>{fw + lane, kTile};
