@@ -130,7 +130,11 @@ def make_workload(name: str, ncol: int | None, rank: int):
     kw = {"seed": rank}
     if ncol:
         kw["ncol"] = ncol
-    return gen(**kw)
+    w = gen(**kw)
+    # rank r holds columns [r ncol, (r + 1) ncol) of one domain: the
+    # rain-pulse hash sees global column indices
+    w.cfg.column_offset = rank * w.ncol
+    return w
 
 
 def cpu_baseline(w, sample_cols: int, sample_steps: int) -> dict:

@@ -121,7 +121,9 @@ class ClmConfig(ctypes.Structure):
         ("cols_per_cta", ctypes.c_int32),
         ("schedule", ctypes.c_int32),
         ("graph", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 5),
+        ("pad1", ctypes.c_int32),
+        ("column_offset", ctypes.c_int64),
+        ("reserved", ctypes.c_int32 * 2),
     ]
 
 
@@ -189,7 +191,7 @@ def config_to_dict(c: ClmConfig) -> dict:
         v = getattr(c, name)
         if name == "earth":
             v = {k: getattr(v, k) for k, _ in ClmEarthParams._fields_}
-        elif name == "reserved":
+        elif name in ("reserved", "pad1"):
             continue
         out[name] = v
     return out

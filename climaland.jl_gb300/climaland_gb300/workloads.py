@@ -67,22 +67,29 @@ class Workload:
 
     def subset(self, ncol: int) -> "Workload":
         """First `ncol` columns (a bounded sample of the same workload)."""
-        ncol = min(ncol, self.ncol)
-        nc = int(self.offsets[ncol])
+        return self.columns(0, min(ncol, self.ncol), name=f"{self.name}[:{min(ncol, self.ncol)}]")
 
-        def cells(a):
-            return None if a is None else a[:nc].copy()
+    def columns(self, c0: int, c1: int, name: str | None = None) -> "Workload":
+        """Columns [c0, c1) as a workload of their own. Its config's
+        column_offset keeps the global column indices (the rain-pulse hash),
+        so stepping the parts gives the same bits as stepping the whole."""
+        assert 0 <= c0 < c1 <= self.ncol
+        a, b = int(self.offsets[c0]), int(self.offsets[c1])
 
-        def cols(a):
-            return None if a is None else a[:ncol].copy()
+        def cells(x):
+            return None if x is None else x[a:b].copy()
+
+        def cols(x):
+            return None if x is None else x[c0:c1].copy()
 
         cfg = A.ClmConfig.from_buffer_copy(self.cfg)
-        cfg.ncol = ncol
+        cfg.ncol = c1 - c0
+        cfg.column_offset = self.cfg.column_offset + c0
         return Workload(
-            name=f"{self.name}[:{ncol}]", cfg=cfg, ncol=ncol,
-            offsets=self.offsets[: ncol + 1].copy(), z_lo=cols(self.z_lo),
-            z_hi=cols(self.z_hi), params=np.ascontiguousarray(self.params[:, :ncol]),
-            forcing={k: np.ascontiguousarray(v[:, :ncol]) for k, v in self.forcing.items()},
+            name=name or f"{self.name}[{c0}:{c1}]", cfg=cfg, ncol=c1 - c0,
+            offsets=(self.offsets[c0: c1 + 1] - a).astype(np.int32), z_lo=cols(self.z_lo),
+            z_hi=cols(self.z_hi), params=np.ascontiguousarray(self.params[:, c0:c1]),
+            forcing={k: np.ascontiguousarray(v[:, c0:c1]) for k, v in self.forcing.items()},
             vartheta_l=cells(self.vartheta_l), theta_i=cells(self.theta_i),
             rho_e_int=cells(self.rho_e_int), intF_w=cols(self.intF_w),
             intF_e=cols(self.intF_e), t0=self.t0, dt=self.dt,

@@ -178,6 +178,7 @@ StepArgs step_args(const clm_handle* h) {
   A.tol = h->cfg.newton_tol;
   A.energy_scale = h->cfg.energy_norm_scale;
   A.seed = h->cfg.forcing_seed;
+  A.col0 = h->cfg.column_offset;
   return A;
 }
 

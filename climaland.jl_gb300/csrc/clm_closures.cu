@@ -81,10 +81,10 @@ __global__ void closure_kernel(ClosureArgs C) {
   }
   // ---- boundary fluxes at t ----
   const double t = C.t;
-  const double ftw = forcing_value(A.forc[CLM_BC_TOP_WATER], st, s, orig, t, A.seed);
-  const double fth = forcing_value(A.forc[CLM_BC_TOP_HEAT], st, s, orig, t, A.seed);
-  const double fbw = forcing_value(A.forc[CLM_BC_BOTTOM_WATER], st, s, orig, t, A.seed);
-  const double fbh = forcing_value(A.forc[CLM_BC_BOTTOM_HEAT], st, s, orig, t, A.seed);
+  const double ftw = forcing_value(A.forc[CLM_BC_TOP_WATER], st, s, A.col0 + orig, t, A.seed);
+  const double fth = forcing_value(A.forc[CLM_BC_TOP_HEAT], st, s, A.col0 + orig, t, A.seed);
+  const double fbw = forcing_value(A.forc[CLM_BC_BOTTOM_WATER], st, s, A.col0 + orig, t, A.seed);
+  const double fbh = forcing_value(A.forc[CLM_BC_BOTTOM_HEAT], st, s, A.col0 + orig, t, A.seed);
   double Ftw = ftw, Fth = 0, Fbw = fbw, Fbh = 0;
   if (A.bc_tw == CLM_BC_STATE) {
     double pb, d;

@@ -287,10 +287,10 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
     // boundary fluxes at t, frozen through the Newton solve
     double Ftw, Fth, Fbw, Fbh;
     {
-      const double ftw = forcing_value(A.forc[CLM_BC_TOP_WATER], st, s, orig, t, A.seed);
-      const double fth = forcing_value(A.forc[CLM_BC_TOP_HEAT], st, s, orig, t, A.seed);
-      const double fbw = forcing_value(A.forc[CLM_BC_BOTTOM_WATER], st, s, orig, t, A.seed);
-      const double fbh = forcing_value(A.forc[CLM_BC_BOTTOM_HEAT], st, s, orig, t, A.seed);
+      const double ftw = forcing_value(A.forc[CLM_BC_TOP_WATER], st, s, A.col0 + orig, t, A.seed);
+      const double fth = forcing_value(A.forc[CLM_BC_TOP_HEAT], st, s, A.col0 + orig, t, A.seed);
+      const double fbw = forcing_value(A.forc[CLM_BC_BOTTOM_WATER], st, s, A.col0 + orig, t, A.seed);
+      const double fbh = forcing_value(A.forc[CLM_BC_BOTTOM_HEAT], st, s, A.col0 + orig, t, A.seed);
       if (A.bc_tw == CLM_BC_STATE) {
         double pb, d;
         psi_dpsi<false>(Tb, c.g, c.nu, ftw, c.theta_r, c.S_s, pb, d);
@@ -593,8 +593,8 @@ CLM_HD void richards_column(const StepArgs& A, const Tables& Tb, int s, int n, i
     const double UFw = Fw;
     double xFw = UFw;
     const double t_bc = dflux ? t + dt : t;
-    const double ftw = forcing_value(A.forc[CLM_BC_TOP_WATER], st, s, orig, t_bc, A.seed);
-    const double fbw = forcing_value(A.forc[CLM_BC_BOTTOM_WATER], st, s, orig, t_bc, A.seed);
+    const double ftw = forcing_value(A.forc[CLM_BC_TOP_WATER], st, s, A.col0 + orig, t_bc, A.seed);
+    const double fbw = forcing_value(A.forc[CLM_BC_BOTTOM_WATER], st, s, A.col0 + orig, t_bc, A.seed);
     double psi_tb = 0.0, psi_bb = 0.0;
     if (A.bc_tw == CLM_BC_STATE) { double d; psi_dpsi<false>(Tb, g, nu, ftw, theta_r, S_s, psi_tb, d); }
     if (A.bc_bw == CLM_BC_STATE) { double d; psi_dpsi<false>(Tb, g, nu, fbw, theta_r, S_s, psi_bb, d); }

@@ -56,6 +56,7 @@ struct StepArgs {
   double tol;
   double energy_scale;
   uint64_t seed;
+  int64_t col0 = 0;     // global index of column 0 (rain-pulse hash)
 };
 
 // Start time and step of a launch: by value, or (CUDA graph replay) read

@@ -70,8 +70,8 @@ CLM_HD void column_features(const StepArgs& A, int s, int orig, V v, V ti, V e, 
     out[2 * kMlpLayers + k] = (float)temperature(A.E, Ye, Yti, heat_capacity(A.E, tl, Yti, rcds));
   }
   if (!tail) return;
-  out[60] = (float)forcing_value(A.forc[CLM_BC_TOP_WATER], st, s, orig, t, A.seed);
-  out[61] = (float)forcing_value(A.forc[CLM_BC_TOP_HEAT], st, s, orig, t, A.seed);
+  out[60] = (float)forcing_value(A.forc[CLM_BC_TOP_WATER], st, s, A.col0 + orig, t, A.seed);
+  out[61] = (float)forcing_value(A.forc[CLM_BC_TOP_HEAT], st, s, A.col0 + orig, t, A.seed);
   out[62] = (float)P[CLM_P_VG_ALPHA * st + s];
   out[63] = (float)P[CLM_P_VG_N * st + s];
   out[64] = (float)nu;

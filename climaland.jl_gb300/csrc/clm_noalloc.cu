@@ -185,6 +185,7 @@ extern "C" int clm_step_eh_noalloc(const clm_config* cfg, int32_t ncol, int32_t 
   A.tol = cfg->newton_tol;
   A.energy_scale = cfg->energy_norm_scale;
   A.seed = cfg->forcing_seed;
+  A.col0 = cfg->column_offset;
   const int ntiles = (ncol + kTile - 1) / kTile;
   const int grid = S.grid < ntiles ? S.grid : ntiles;
   eh_step_noalloc_kernel<<<grid, 32, noalloc_smem(nlayers), static_cast<cudaStream_t>(cuda_stream)>>>(

@@ -294,7 +294,8 @@ CLM_HD double hash01(uint64_t seed, uint64_t column, int64_t period) {
 
 // Forcing descriptor value at time t for column `orig` (header comment of
 // enum clm_forcing_field). F points to row 0 of a [CLM_F_NFIELDS][stride] block.
-CLM_HD double forcing_value(const double* F, int stride, int col, int orig, double t,
+// col: the column's row in F; hash_col: its global index (rain-pulse hash).
+CLM_HD double forcing_value(const double* F, int stride, int col, int64_t hash_col, double t,
                             uint64_t seed) {
   if (F == nullptr) return 0.0;
   double v = F[CLM_F_BASE * stride + col];
@@ -303,7 +304,7 @@ CLM_HD double forcing_value(const double* F, int stride, int col, int orig, doub
   const double pp = F[CLM_F_PULSE_PERIOD * stride + col];
   if (pp > 0.0) {
     const int64_t k = (int64_t)floor(t / pp);
-    if (hash01(seed, (uint64_t)orig, k) < F[CLM_F_PULSE_DUTY * stride + col])
+    if (hash01(seed, (uint64_t)hash_col, k) < F[CLM_F_PULSE_DUTY * stride + col])
       v += F[CLM_F_PULSE_AMP * stride + col];
   }
   return v;

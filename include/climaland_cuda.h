@@ -175,7 +175,11 @@ typedef struct clm_config {
                              sequence as CUDA graphs captured on first use
                              (t and dt go through a device array, so one
                              graph serves every call with the same nsteps) */
-  int32_t reserved[5];
+  int32_t pad1;
+  int64_t column_offset;  /* global index of this handle's column 0 when a
+                             domain is split across handles or GPUs: the
+                             rain-pulse hash uses the global column index  */
+  int32_t reserved[2];
 } clm_config;
 
 typedef struct clm_handle clm_handle;

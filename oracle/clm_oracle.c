@@ -261,8 +261,9 @@ double clm_forcing_hash01(uint64_t seed, uint64_t column, int64_t period) {
   return (double)(h >> 11) * (1.0 / 9007199254740992.0);
 }
 
+/* forcing row c; the rain-pulse hash uses the global column c + col0 */
 double clmo_forcing_value(const double* F, int32_t ncol, int32_t c, double t,
-                          uint64_t seed) {
+                          uint64_t seed, int64_t col0) {
   if (!F) return 0.0;
   double v = F[CLM_F_BASE * ncol + c];
   double amp = F[CLM_F_AMP * ncol + c];
@@ -271,7 +272,7 @@ double clmo_forcing_value(const double* F, int32_t ncol, int32_t c, double t,
   double pp = F[CLM_F_PULSE_PERIOD * ncol + c];
   if (pp > 0.0) {
     int64_t k = (int64_t)floor(t / pp);
-    if (clm_forcing_hash01(seed, (uint64_t)c, k) < F[CLM_F_PULSE_DUTY * ncol + c])
+    if (clm_forcing_hash01(seed, (uint64_t)(c + col0), k) < F[CLM_F_PULSE_DUTY * ncol + c])
       v += F[CLM_F_PULSE_AMP * ncol + c];
   }
   return v;
@@ -468,10 +469,11 @@ static void update_boundary_fluxes(const col_t* C, const state_t* Y,
   const clm_earth_params* e = &cfg->earth;
   int n = C->n, c = C->c, ncol = P->ncol;
   uint64_t seed = cfg->forcing_seed;
-  double f_tw = clmo_forcing_value(P->forcing[CLM_BC_TOP_WATER], ncol, c, t, seed);
-  double f_th = clmo_forcing_value(P->forcing[CLM_BC_TOP_HEAT], ncol, c, t, seed);
-  double f_bw = clmo_forcing_value(P->forcing[CLM_BC_BOTTOM_WATER], ncol, c, t, seed);
-  double f_bh = clmo_forcing_value(P->forcing[CLM_BC_BOTTOM_HEAT], ncol, c, t, seed);
+  int64_t col0 = cfg->column_offset;
+  double f_tw = clmo_forcing_value(P->forcing[CLM_BC_TOP_WATER], ncol, c, t, seed, col0);
+  double f_th = clmo_forcing_value(P->forcing[CLM_BC_TOP_HEAT], ncol, c, t, seed, col0);
+  double f_bw = clmo_forcing_value(P->forcing[CLM_BC_BOTTOM_WATER], ncol, c, t, seed, col0);
+  double f_bh = clmo_forcing_value(P->forcing[CLM_BC_BOTTOM_HEAT], ncol, c, t, seed, col0);
   double nu_top = C->nu, nu_bot = C->nu;
 
   /* water, top */

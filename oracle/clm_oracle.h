@@ -83,7 +83,7 @@ double clmo_kappa_sat_unfrozen(double kappa_solid, double nu, double kappa_l);
 double clmo_kappa_dry(double rho_p, double nu, double kappa_solid,
                       double kappa_air);
 double clmo_forcing_value(const double* forcing, int32_t ncol, int32_t c,
-                          double t, uint64_t seed);
+                          double t, uint64_t seed, int64_t col0);
 
 /* ---- closure level, whole batch --------------------------------------- *
  * State pointers: vartheta_l, theta_i, rho_e_int per cell; intF_w, intF_e

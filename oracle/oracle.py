@@ -96,7 +96,8 @@ def lib():
         L.clm_forcing_hash01.restype = _D
         L.clm_forcing_hash01.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int64]
         L.clmo_forcing_value.restype = _D
-        L.clmo_forcing_value.argtypes = [_DP, ctypes.c_int32, ctypes.c_int32, _D, ctypes.c_uint64]
+        L.clmo_forcing_value.argtypes = [_DP, ctypes.c_int32, ctypes.c_int32, _D, ctypes.c_uint64,
+                                         ctypes.c_int64]
         L.clmo_update_cache.restype = ctypes.c_int
         L.clmo_update_cache.argtypes = [_PP, _DP, _DP, _DP, _D] + [_DP] * 9
         for nm in ("clmo_exp_tendency", "clmo_imp_tendency"):

@@ -117,3 +117,17 @@ def test_autotune_restores_state_and_changes_no_result(torch):
         f, it = g.status()
         got = (g.get_state(), f, it)
     _same(ref, got)
+
+
+def test_column_ranges_with_offset_equal_the_whole(torch):
+    # the multi-GPU split on one device: two handles over [0, 500) and
+    # [500, 1024) (column_offset keeps the rain-pulse hash global) give the
+    # whole run's bits
+    w = WL.full_scale_c4(ncol=1024, seed=6)
+    whole = _run(w, [(w.t0, 10)])
+    parts = [_run(w.columns(a, b), [(w.t0, 10)]) for a, b in ((0, 500), (500, 1024))]
+    for i in range(5):
+        if whole[0][i] is None:
+            continue
+        assert np.array_equal(whole[0][i], np.concatenate([p[0][i] for p in parts]))
+    assert np.array_equal(whole[1], np.concatenate([p[1] for p in parts]))
