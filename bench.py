@@ -13,8 +13,9 @@ launched as one kernel that reads and writes the whole state in HBM
 Prints one JSON line (rank 0). Metric: column-steps/s.
   value     device-timed throughput, state resident in HBM (CUDA events on
             the library's stream, max over ranks)
-  e2e       the same through the C ABI with host buffers: per step the
-            state is copied from pinned host memory, stepped, and copied back
+  e2e       the same through the C ABI with host buffers (clm_step_host,
+            wall clock): per step the state is copied in from pinned host
+            memory, stepped, and copied back, pipelined over column chunks
   roofline  dominant kernel (the step kernel) against the measured HBM peak
   cpu_baseline  the FP64 CPU oracle on a bounded sample, all host threads
 """
@@ -396,22 +397,19 @@ def main():
         p = torch.empty(a.shape, dtype=torch.float64, pin_memory=True).numpy()
         p[:] = a
         pinned.append(p)
-    outs = [None if a is None else torch.empty(a.shape, dtype=torch.float64, pin_memory=True).numpy()
-            for a in pinned]
     h2d = sum(a.nbytes for a in pinned if a is not None)
+    g.step_host([None if a is None else a.copy() for a in pinned], t, w.dt, 1)  # warm: streams, events
     barrier()
     torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
+    # wall clock: clm_step_host is synchronous and spans three streams
+    w0 = time.perf_counter()
     for i in range(e2e_steps):
-        g.set_state(*pinned)
-        g.step(t, w.dt, 1)
+        # clm_step_host: the state goes in from pinned host memory, is
+        # stepped, and comes back in place, copies pipelined with the kernels
+        g.step_host(pinned, t, w.dt, 1)
         t += w.dt
-        g.get_state(out=outs)
-    e1.record(stream)
-    stream.synchronize()
-    wall_e2e_ms = e0.elapsed_time(e1)
+    torch.cuda.synchronize()
+    wall_e2e_ms = (time.perf_counter() - w0) * 1e3
     if dist is not None:
         tt = torch.tensor([wall_e2e_ms], device="cuda")
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)

@@ -123,7 +123,8 @@ class ClmConfig(ctypes.Structure):
         ("graph", ctypes.c_int32),
         ("pad1", ctypes.c_int32),
         ("column_offset", ctypes.c_int64),
-        ("reserved", ctypes.c_int32 * 2),
+        ("host_chunks", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 1),
     ]
 
 
@@ -232,6 +233,8 @@ SIGNATURES = [
     ("clm_step_async", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_double, ctypes.c_int32]),
     ("clm_sync", ctypes.c_int, [_H]),
     ("clm_set_stream", ctypes.c_int, [_H, ctypes.c_void_p]),
+    ("clm_step_host", ctypes.c_int, [_H, _DP, _DP, _DP, _DP, _DP, ctypes.c_double, ctypes.c_double,
+                                     ctypes.c_int32]),
     ("clm_autotune", ctypes.c_int, [_H, ctypes.c_double, ctypes.c_double, ctypes.c_int32,
                                     ctypes.c_void_p, ctypes.c_int32, _IP]),
     ("clm_get_launch_config", ctypes.c_int, [_H, _IP, _IP, _IP]),

@@ -49,7 +49,7 @@ class SoilColumns:
 
     def __init__(self, w, *, precision=None, newton_mode=None, max_iters=None,
                  newton_tol=None, energy_norm_scale=None, cols_per_cta=None, learned_guess=None,
-                 schedule=None, graph=None, lib=None):
+                 schedule=None, graph=None, host_chunks=None, lib=None):
         self.lib = lib or load_library()
         self.w = w
         cfg = A.ClmConfig.from_buffer_copy(w.cfg)
@@ -71,6 +71,8 @@ class SoilColumns:
             cfg.schedule = int(schedule)
         if graph is not None:
             cfg.graph = int(bool(graph))
+        if host_chunks is not None:
+            cfg.host_chunks = int(host_chunks)
         self.cfg = cfg
         self.eh = cfg.model == A.CLM_MODEL_ENERGY_HYDROLOGY
         self.ncol = w.ncol
@@ -144,6 +146,16 @@ class SoilColumns:
         self._check(self.lib.clm_get_state_device(self.h, *[ctypes.c_void_p(p) if p else None for p in ptrs]))
 
     # -- stepping -----------------------------------------------------------------
+    def step_host(self, state, t, dt, nsteps=1):
+        """clm_step_host: `state` (v, ti, e, Fw, Fe; float64 C-contiguous
+        host arrays in the C ABI layout, pinned for overlap) is copied in,
+        advanced and copied back in place, pipelined over column chunks."""
+        v, ti, e, fw, fe = state
+        for a in (v, ti, e, fw, fe):
+            assert a is None or (a.dtype == np.float64 and a.flags.c_contiguous)
+        self._check(self.lib.clm_step_host(self.h, A.dptr(v), A.dptr(ti), A.dptr(e), A.dptr(fw),
+                                           A.dptr(fe), float(t), float(dt), int(nsteps)))
+
     def step(self, t, dt, nsteps=1):
         self._check(self.lib.clm_step(self.h, float(t), float(dt), int(nsteps)))
 

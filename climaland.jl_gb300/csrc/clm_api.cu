@@ -27,9 +27,9 @@ cudaError_t step_grid(int model, int precision, int nmax, int wpc, int ntiles, i
 size_t step_scratch_doubles(int model, int precision, int nmax, int wpc, int grid);
 // clm_layout.cu
 cudaError_t ref_to_internal(const Layout& L, const int32_t* ref_off, const double* src,
-                            double* dst, int ncomp, cudaStream_t st);
+                            double* dst, int ncomp, cudaStream_t st, int tile0 = 0, int ntl = -1);
 cudaError_t internal_to_ref(const Layout& L, const int32_t* ref_off, const double* src,
-                            double* dst, int ncomp, cudaStream_t st);
+                            double* dst, int ncomp, cudaStream_t st, int tile0 = 0, int ntl = -1);
 cudaError_t cols_to_sorted(const Layout& L, const double* src, double* dst, cudaStream_t st);
 cudaError_t cols_to_orig(const Layout& L, const double* src, double* dst, cudaStream_t st);
 // clm_budget.cu
@@ -80,6 +80,10 @@ struct clm_handle {
   double* d_scratch = nullptr;  // per-warp-slot frozen aux arrays
   size_t scratch_doubles = 0;
   int guess_grid = 0;           // persistent grid of the guess kernel
+  bool perm_identity = false;   // columns already in depth order
+  // clm_step_host pipeline: copy streams and one event pair per chunk
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  std::vector<cudaEvent_t> host_ev;
   // CUDA graph replay of clm_step_async: one executable graph per piece
   // length, captured on cap_stream, launched on `stream`; t and dt reach the
   // kernels through d_clock, filled from a pinned ring before each replay
@@ -221,6 +225,8 @@ int build_layout(clm_handle* h, const std::vector<int>& nl) {
     nmax = std::max(nmax, m);
   }
   h->ncells_int = off;
+  h->perm_identity = true;
+  for (int s = 0; s < ncol; ++s) h->perm_identity = h->perm_identity && h->perm[s] == s;
   h->nmax = nmax;
   // device copies
   dfree(h->d_tile_off); dfree(h->d_tile_n); dfree(h->d_col_n); dfree(h->d_perm); dfree(h->d_ref_off);
@@ -585,6 +591,9 @@ void clm_destroy(clm_handle* h) {
   for (auto& ev : h->clock_ev)
     if (ev) cudaEventDestroy(ev);
   if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
+  for (auto& ev : h->host_ev) cudaEventDestroy(ev);
+  if (h->copy_in) cudaStreamDestroy(h->copy_in);
+  if (h->copy_out) cudaStreamDestroy(h->copy_out);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   cudaGetLastError();
   delete h;
@@ -722,6 +731,99 @@ int clm_step_async(clm_handle* h, double t, double dt, int32_t nsteps) {
     rc = issue(h, l, clk, h->stream);
     if (rc != CLM_OK) return rc;
   }
+  return CLM_OK;
+}
+
+int clm_step_host(clm_handle* h, double* v, double* ti, double* e, double* Fw, double* Fe,
+                  double t, double dt, int32_t nsteps) {
+  if (!h) return CLM_ERR_ARG;
+  if (!h->have_geometry) return fail(h, CLM_ERR_STATE, "clm_set_geometry has not been called");
+  if (!h->have_params) return fail(h, CLM_ERR_STATE, "clm_set_params has not been called");
+  if (!(dt > 0) || !std::isfinite(dt) || !std::isfinite(t) || nsteps < 0)
+    return fail(h, CLM_ERR_ARG, "need dt > 0, finite t, nsteps >= 0");
+  const bool eh = is_eh(h);
+  if (!v || !Fw || (eh && (!ti || !e || !Fe)))
+    return fail(h, CLM_ERR_ARG, "every state array of the model is required");
+  if (h->cfg.learned_guess || !h->perm_identity) {
+    int rc = set_state_impl(h, v, ti, e, Fw, Fe, cudaMemcpyHostToDevice);
+    if (rc == CLM_OK) rc = clm_step(h, t, dt, nsteps);
+    if (rc == CLM_OK) rc = get_state_impl(h, v, ti, e, Fw, Fe, cudaMemcpyDeviceToHost);
+    return rc;
+  }
+  if (!h->copy_in) {
+    CLM_CUDA(h, cudaStreamCreateWithFlags(&h->copy_in, cudaStreamNonBlocking));
+    CLM_CUDA(h, cudaStreamCreateWithFlags(&h->copy_out, cudaStreamNonBlocking));
+  }
+  const int nf = eh ? 3 : 1, nc = eh ? 2 : 1;
+  const int64_t bytes = (int64_t)h->ncells_ref * nf * (int64_t)sizeof(double);
+  // about 128 MB per chunk, at most 4 (each chunk's persistent launch ends
+  // with a partial wave; measured on the 1,048,576 x 20 state: 4 chunks
+  // 41.9 ms, 16 chunks 49.1 ms, unchunked 45.7 ms), chunks a whole number of
+  // waves of the step grid's warps
+  int nch = h->cfg.host_chunks > 0
+                ? h->cfg.host_chunks
+                : (int)std::min<int64_t>(4, std::max<int64_t>(1, (bytes + (64 << 20)) >> 27));
+  nch = std::max(1, std::min(nch, h->ntiles));
+  const int wave = std::max(1, h->grid * h->wpc);
+  int per = (h->ntiles + nch - 1) / nch;
+  if (per > wave) per = (per + wave - 1) / wave * wave;
+  while ((int)h->host_ev.size() < 2 * nch) {
+    cudaEvent_t ev;
+    CLM_CUDA(h, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    h->host_ev.push_back(ev);
+  }
+  const Layout L = layout_of(h);
+  StepArgs A = step_args(h);
+  double* hf[3] = {v, ti, e};
+  double* df[3] = {h->d_v, h->d_ti, h->d_e};
+  double* hc[2] = {Fw, Fe};
+  double* dc[2] = {h->d_Fw, h->d_Fe};
+  for (int k = 0; k * per < h->ntiles; ++k) {
+    const int T0 = k * per, T1 = std::min(h->ntiles, T0 + per);
+    const int c0 = T0 * kTile, c1 = std::min(T1 * kTile, h->ncol);
+    if (c0 >= c1) break;
+    const int64_t a = h->ref_off[c0], b = h->ref_off[c1];
+    cudaEvent_t ev_in = h->host_ev[2 * k], ev_done = h->host_ev[2 * k + 1];
+    // in: this chunk's cells and per-column values (identity order: the
+    // sorted index of a column is its own)
+    for (int f = 0; f < nf; ++f)
+      CLM_CUDA(h, cudaMemcpyAsync(h->d_stage + f * h->ncells_ref + a, hf[f] + a,
+                                  sizeof(double) * (b - a), cudaMemcpyHostToDevice, h->copy_in));
+    for (int f = 0; f < nc; ++f)
+      CLM_CUDA(h, cudaMemcpyAsync(dc[f] + c0, hc[f] + c0, sizeof(double) * (c1 - c0),
+                                  cudaMemcpyHostToDevice, h->copy_in));
+    CLM_CUDA(h, cudaEventRecord(ev_in, h->copy_in));
+    // transpose, step, transpose back on the handle's stream (step kernels
+    // share the per-warp scratch, so they stay in one stream)
+    CLM_CUDA(h, cudaStreamWaitEvent(h->stream, ev_in, 0));
+    for (int f = 0; f < nf; ++f)
+      CLM_CUDA(h, ref_to_internal(L, h->d_ref_off, h->d_stage + f * h->ncells_ref, df[f], 1, h->stream,
+                                  T0, T1 - T0));
+    A.tile_begin = T0;
+    A.tile_end = T1;
+    for (int s0 = 0; s0 < nsteps; s0 += 64) {
+      StepClock clk;
+      clk.t0 = step_time(t, s0, dt);
+      clk.dt = dt;
+      CLM_CUDA(h, launch_step(A, h->cfg.model, h->cfg.precision, h->wpc, h->grid, h->d_scratch, clk,
+                              std::min(64, nsteps - s0), h->stream));
+    }
+    for (int f = 0; f < nf; ++f)
+      CLM_CUDA(h, internal_to_ref(L, h->d_ref_off, df[f], h->d_stage + f * h->ncells_ref, 1, h->stream,
+                                  T0, T1 - T0));
+    CLM_CUDA(h, cudaEventRecord(ev_done, h->stream));
+    // out
+    CLM_CUDA(h, cudaStreamWaitEvent(h->copy_out, ev_done, 0));
+    for (int f = 0; f < nf; ++f)
+      CLM_CUDA(h, cudaMemcpyAsync(hf[f] + a, h->d_stage + f * h->ncells_ref + a, sizeof(double) * (b - a),
+                                  cudaMemcpyDeviceToHost, h->copy_out));
+    for (int f = 0; f < nc; ++f)
+      CLM_CUDA(h, cudaMemcpyAsync(hc[f] + c0, dc[f] + c0, sizeof(double) * (c1 - c0),
+                                  cudaMemcpyDeviceToHost, h->copy_out));
+  }
+  CLM_CUDA(h, cudaStreamSynchronize(h->copy_out));
+  CLM_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->have_state = true;
   return CLM_OK;
 }
 

@@ -18,7 +18,7 @@ struct clm_handle;
 
 namespace clm {
 cudaError_t internal_to_ref(const Layout& L, const int32_t* ref_off, const double* src,
-                            double* dst, int ncomp, cudaStream_t st);
+                            double* dst, int ncomp, cudaStream_t st, int tile0 = 0, int ntl = -1);
 StepArgs handle_step_args(clm_handle* h);
 Layout handle_layout(clm_handle* h);
 int handle_ready(clm_handle* h);

@@ -57,6 +57,8 @@ struct StepArgs {
   double energy_scale;
   uint64_t seed;
   int64_t col0 = 0;     // global index of column 0 (rain-pulse hash)
+  int tile_begin = 0;   // the launch's tiles: [tile_begin, tile_end)
+  int tile_end = -1;    // -1: through the last tile
 };
 
 // Start time and step of a launch: by value, or (CUDA graph replay) read

@@ -17,9 +17,9 @@ constexpr int kXposePad = kTile + 1;  // padded row (in doubles) of the staging 
 __global__ void __launch_bounds__(kXposeThreads)
     ref_to_internal_kernel(Layout L, const int32_t* __restrict__ ref_off,
                            const double* __restrict__ src, double* __restrict__ dst,
-                           int ncomp) {
+                           int ncomp, int tile0) {
   extern __shared__ double tileb[];  // [nmax * ncomp][kXposePad]
-  const int tile = blockIdx.x;
+  const int tile = tile0 + blockIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nw = blockDim.x >> 5;
   const int nt = L.tile_n[tile];
@@ -43,9 +43,9 @@ __global__ void __launch_bounds__(kXposeThreads)
 __global__ void __launch_bounds__(kXposeThreads)
     internal_to_ref_kernel(Layout L, const int32_t* __restrict__ ref_off,
                            const double* __restrict__ src, double* __restrict__ dst,
-                           int ncomp) {
+                           int ncomp, int tile0) {
   extern __shared__ double tileb[];
-  const int tile = blockIdx.x;
+  const int tile = tile0 + blockIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nw = blockDim.x >> 5;
   const int nt = L.tile_n[tile];
@@ -87,23 +87,28 @@ size_t xpose_smem(const Layout& L, int ncomp) {
   return (size_t)L.nmax * ncomp * kXposePad * sizeof(double);
 }
 
+// tiles [tile0, tile0 + ntl) (ntl < 0: through the last tile)
 cudaError_t ref_to_internal(const Layout& L, const int32_t* ref_off, const double* src,
-                            double* dst, int ncomp, cudaStream_t st) {
+                            double* dst, int ncomp, cudaStream_t st, int tile0, int ntl) {
   const size_t sm = xpose_smem(L, ncomp);
   cudaError_t e = cudaFuncSetAttribute(ref_to_internal_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  ref_to_internal_kernel<<<L.ntiles, kXposeThreads, sm, st>>>(L, ref_off, src, dst, ncomp);
+  const int grid = ntl < 0 ? L.ntiles - tile0 : ntl;
+  if (grid <= 0) return cudaSuccess;
+  ref_to_internal_kernel<<<grid, kXposeThreads, sm, st>>>(L, ref_off, src, dst, ncomp, tile0);
   return cudaGetLastError();
 }
 
 cudaError_t internal_to_ref(const Layout& L, const int32_t* ref_off, const double* src,
-                            double* dst, int ncomp, cudaStream_t st) {
+                            double* dst, int ncomp, cudaStream_t st, int tile0, int ntl) {
   const size_t sm = xpose_smem(L, ncomp);
   cudaError_t e = cudaFuncSetAttribute(internal_to_ref_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  internal_to_ref_kernel<<<L.ntiles, kXposeThreads, sm, st>>>(L, ref_off, src, dst, ncomp);
+  const int grid = ntl < 0 ? L.ntiles - tile0 : ntl;
+  if (grid <= 0) return cudaSuccess;
+  internal_to_ref_kernel<<<grid, kXposeThreads, sm, st>>>(L, ref_off, src, dst, ncomp, tile0);
   return cudaGetLastError();
 }
 

@@ -74,8 +74,9 @@ __global__ void __launch_bounds__(128, 1)
   J.ae = Col<JT>{jw + 3 * lay + lane, kTile};
   const double t0 = clk.start(), dt = clk.step();
   const bool dyn = A.tile_ctr != nullptr;
-  int tile = dyn ? claim_tile(A.tile_ctr) : gwarp;
-  while (tile < A.L.ntiles) {
+  const int tend = A.tile_end < 0 ? A.L.ntiles : A.tile_end;
+  int tile = A.tile_begin + (dyn ? claim_tile(A.tile_ctr) : gwarp);
+  while (tile < tend) {
     const int s = tile * kTile + lane;
     const int n = A.L.col_n[s];
     if (n > 0) {
@@ -96,7 +97,7 @@ __global__ void __launch_bounds__(128, 1)
       A.flags[s] = flags;
       A.iters[s] = iters;
     }
-    tile = dyn ? claim_tile(A.tile_ctr) : tile + nwarps;
+    tile = dyn ? A.tile_begin + claim_tile(A.tile_ctr) : tile + nwarps;
   }
   if (dyn) release_tiles(A.tile_ctr, nwarps);
 }
@@ -123,8 +124,9 @@ __global__ void __launch_bounds__(128, 1)
   J.dp = Col<JT>{jw + lay + lane, kTile};
   const double t0 = clk.start(), dt = clk.step();
   const bool dyn = A.tile_ctr != nullptr;
-  int tile = dyn ? claim_tile(A.tile_ctr) : gwarp;
-  while (tile < A.L.ntiles) {
+  const int tend = A.tile_end < 0 ? A.L.ntiles : A.tile_end;
+  int tile = A.tile_begin + (dyn ? claim_tile(A.tile_ctr) : gwarp);
+  while (tile < tend) {
     const int s = tile * kTile + lane;
     const int n = A.L.col_n[s];
     if (n > 0) {
@@ -137,7 +139,7 @@ __global__ void __launch_bounds__(128, 1)
       A.flags[s] = flags;
       A.iters[s] = iters;
     }
-    tile = dyn ? claim_tile(A.tile_ctr) : tile + nwarps;
+    tile = dyn ? A.tile_begin + claim_tile(A.tile_ctr) : tile + nwarps;
   }
   if (dyn) release_tiles(A.tile_ctr, nwarps);
 }

@@ -179,7 +179,8 @@ typedef struct clm_config {
   int64_t column_offset;  /* global index of this handle's column 0 when a
                              domain is split across handles or GPUs: the
                              rain-pulse hash uses the global column index  */
-  int32_t reserved[2];
+  int32_t host_chunks;    /* clm_step_host pipeline depth (0: by size)      */
+  int32_t reserved[1];
 } clm_config;
 
 typedef struct clm_handle clm_handle;
@@ -237,6 +238,16 @@ int clm_get_state_device(clm_handle* h, double* vartheta_l, double* theta_i,
 int clm_step(clm_handle* h, double t, double dt, int32_t nsteps);
 int clm_step_async(clm_handle* h, double t, double dt, int32_t nsteps);
 int clm_sync(clm_handle* h);
+
+/* Host-buffer step: the state in host memory (reference layout, updated in
+ * place; pinned memory lets the copies overlap) is copied in, advanced
+ * nsteps and copied back, pipelined over chunks of columns so that each
+ * chunk's copies overlap the kernels of its neighbours. Replaces
+ * step!(landsim) (Simulations.jl:312-314) for a host-resident Y.soil; the
+ * same bits as clm_set_state + clm_step + clm_get_state (which it becomes
+ * when columns are not already in depth order or the learned guess is on). */
+int clm_step_host(clm_handle* h, double* vartheta_l, double* theta_i, double* rho_e_int,
+                  double* intF_w, double* intF_e, double t, double dt, int32_t nsteps);
 
 /* Launch-configuration autotuner (no reference counterpart; ClimaLand's
  * broadcasts are configured by ClimaCore). Times the step kernel on

@@ -131,3 +131,20 @@ def test_column_ranges_with_offset_equal_the_whole(torch):
             continue
         assert np.array_equal(whole[0][i], np.concatenate([p[0][i] for p in parts]))
     assert np.array_equal(whole[1], np.concatenate([p[1] for p in parts]))
+
+
+@pytest.mark.parametrize("name,make,chunks,nsteps", [
+    ("full_scale", lambda: WL.full_scale_c4(ncol=1000, seed=7), 5, 70),     # pipelined
+    ("richards", lambda: WL.richards_c0(ncol=300, seed=2), 3, 4),           # pipelined
+    ("uneven", lambda: WL.uneven_c2(ncol=262144, seed=8).subset(700), 4, 5),  # reorders: fallback
+])
+def test_host_step_equals_set_step_get(torch, name, make, chunks, nsteps):
+    w = make()
+    ref = _run(w, [(w.t0, nsteps)])
+    st = w.copy_state()
+    with SoilColumns(w, host_chunks=chunks) as g:
+        g.step_host(st, w.t0, w.dt, nsteps)
+        f, it = g.status()
+        dev = g.get_state()
+    _same(ref, (st, f, it))
+    _same(ref, (dev, f, it))
