@@ -106,8 +106,13 @@ CLM_HD double from_bits(int64_t b) {
 // exp(x): x = (64 k' + j) ln2/64 + r, |r| <= ln2/128;
 // exp(x) = 2^k' 2^(j/64) (1 + expm1(r)), expm1 by its degree-5 Taylor
 // polynomial (truncation < 4e-17).
+// Range checks compare the bit patterns as integers (the FP64 pipe is the
+// scarce one): |x| <= 700 <=> (bits & ~sign) <= bits(700), NaN included in
+// the slow path since its magnitude bits exceed those of any finite value.
+constexpr int64_t kBits700 = 0x4085E00000000000LL;  // 700.0
+
 CLM_HD double exp(const Tables& T, double x) {
-  if (!(fabs(x) <= 700.0)) return ::exp(x);
+  if ((bits_of(x) & 0x7FFFFFFFFFFFFFFFLL) > kBits700) return ::exp(x);
   const double shifter = 6755399441055744.0;  // 1.5 * 2^52: round to integer
   const double kd = fma(x, INV_LNN, shifter);
   const int64_t k = bits_of(kd) - bits_of(shifter);
@@ -130,8 +135,8 @@ CLM_HD double exp(const Tables& T, double x) {
 // log1p(r), log1p by its degree-9 Taylor polynomial (truncation < 1e-19).
 CLM_HD double log(const Tables& T, double x) {
   int64_t b = bits_of(x);
-  // positive normal finite only
-  if (!(x > 2.2250738585072014e-308) || !(x < 1.7976931348623157e308)) return ::log(x);
+  // positive normal finite only: bits in [0x0010000000000000, 0x7FF0000000000000)
+  if ((uint64_t)(b - 0x0010000000000000LL) >= (uint64_t)0x7FE0000000000000LL) return ::log(x);
   int e = (int)((b >> 52) & 0x7FF) - 1023;
   const int j = (int)((b >> 46) & 63);
   const double mant = from_bits((b & 0x000FFFFFFFFFFFFFLL) | 0x3FF0000000000000LL);
