@@ -77,6 +77,45 @@ CLM_HD double dfrom(uint64_t b) {
 #endif
 }
 
+// ---- conversion-free helpers ------------------------------------------------
+// Float <-> integer conversions and rounding instructions share the FP64
+// pipe on GB300; these use FP32 and integer arithmetic instead.
+constexpr float kShift = 12582912.0f;  // 1.5 * 2^23
+
+// nearest integer of x (|x| < 2^22), as a float and as an int
+CLM_HD float round_f(float x, int& k) {
+  const float s = x + kShift;
+  k = (int)(fbits(s) - fbits(kShift));
+  return s - kShift;
+}
+
+// (float)k for |k| < 2^22
+CLM_HD float int_to_float(int k) { return ffrom(fbits(kShift) + (uint32_t)k) - kShift; }
+
+// (float)r, correctly rounded, for r < 2^29: two exact 23-bit halves, one rounding
+CLM_HD float u29_to_float(uint32_t r) {
+  const float lo = ffrom(0x4B000000u | (r & 0x7FFFFFu)) - 8388608.0f;
+  const float hi = ffrom(0x4B000000u | (r >> 23)) - 8388608.0f;
+  return fmaf(hi, 8388608.0f, lo);
+}
+
+// first approximations (multi-function unit on the device)
+CLM_HD float log_approx(float x) {
+#ifdef __CUDA_ARCH__
+  return __logf(x);
+#else
+  return std::log(x);
+#endif
+}
+
+CLM_HD float exp_approx(float x) {
+#ifdef __CUDA_ARCH__
+  return __expf(x);
+#else
+  return std::exp(x);
+#endif
+}
+
 // ---- error-free transformations -------------------------------------------
 CLM_HD F2 two_sum(float a, float b) {
   const float s = a + b;
@@ -167,7 +206,7 @@ CLM_HD F2 from_double(double d) {
   // lo: the remaining 29 fraction bits, value rem * 2^(e - 1023 - 52)
   const uint32_t rem = (uint32_t)(m & 0x1FFFFFFFu);
   const float scale = ffrom((uint32_t)(e - 1023 - 52 + 127) << 23);  // 2^(e-1075), normal
-  const float lo = (float)rem * scale;  // rounds rem to 24 bits
+  const float lo = u29_to_float(rem) * scale;  // rem rounded to 24 bits
   return fast_two_sum(hi, sign ? -lo : lo);
 }
 
@@ -205,13 +244,13 @@ CLM_HD F2 exp(const Tables& T, F2 x) {
   const float C1 = 0.010833740234375f;             // ln2/64 to 11 significant bits
   const float C2 = -3.3155381515825866e-06f;       // ln2/64 - C1 to 24 bits
   const float C3 = 2.572804640231345e-14f;         // remainder
-  const float kf = rintf(x.hi * kInvL);
+  int k;
+  const float kf = round_f(x.hi * kInvL, k);
   const float t = fmaf(-kf, C1, x.hi);  // exact
   const F2 p = two_prod(kf, C2);
   F2 r = two_sum(t, -p.hi);  // exact
   r = add_f(r, x.lo);        // x.lo kept to the last bit
   r = fast_two_sum(r.hi, r.lo - (p.lo + kf * C3));
-  const int k = (int)kf;
   const int j = k & 63;
   const int m = (k - j) / 64;
   const float c = fmaf(fmaf(r.hi, 1.0f / 120.0f, 1.0f / 24.0f), r.hi, 1.0f / 6.0f);
@@ -225,9 +264,10 @@ CLM_HD F2 exp(const Tables& T, F2 x) {
 }
 
 // log(x) for x > 0 (normal float hi): x = 2^k xm with xm in [1, 2) (exact
-// scaling), y0 = logf(xm.hi), t = xm e^(-y0) - 1 (|t| ~ 1e-7, exp argument
-// within +-0.7), log x = k ln2 + y0 + t - t^2/2 (+ O(t^3)); ln2 split as
-// L1 (16 bits: k L1 exact for |k| < 2^8) + L2 + L3.
+// scaling), y0 = log_approx(xm.hi) (absolute error below 2^-21), t =
+// xm e^(-y0) - 1 (|t| < 1e-6, exp argument within +-0.7), log x = k ln2 +
+// y0 + t - t^2/2 (+ O(t^3) < 1e-18); ln2 split as L1 (16 bits: k L1 exact
+// for |k| < 2^8) + L2 + L3.
 CLM_HD F2 log(const Tables& T, F2 x) {
   const float L1 = 0.693145751953125f;
   const float L2 = 1.428606765330187e-06f;
@@ -235,10 +275,10 @@ CLM_HD F2 log(const Tables& T, F2 x) {
   const int k = (int)((fbits(x.hi) >> 23) & 0xFF) - 127;
   const float sc = ffrom((uint32_t)(127 - k) << 23);  // 2^-k
   const F2 xm = F2{x.hi * sc, x.lo * sc};
-  const float y0 = logf(xm.hi);
+  const float y0 = log_approx(xm.hi);
   const F2 e = exp(T, make(-y0));
   const F2 t = add_f(mul(xm, e), -1.0f);
-  const float kf = (float)k;
+  const float kf = int_to_float(k);
   F2 y = add(two_sum(kf * L1, y0), t);  // k L1 exact
   y = add(y, two_prod(kf, L2));
   return add_f(y, fmaf(kf, L3, -0.5f * t.hi * t.hi));
