@@ -48,6 +48,10 @@ CLM_BC_FLUX = 0
 CLM_BC_FREE_DRAINAGE = 1
 CLM_BC_STATE = 2
 CLM_BC_FLUX_ADVECTIVE = 3
+CLM_BC_PRECIP_RUNOFF = 4
+CLM_RUNOFF_NONE = 0
+CLM_RUNOFF_SURFACE = 1
+CLM_RUNOFF_TOPMODEL = 2
 
 CLM_P_NU = 0
 CLM_P_K_SAT = 1
@@ -64,6 +68,10 @@ CLM_P_NU_SS_OM = 10
 CLM_P_NU_SS_QUARTZ = 11
 CLM_P_NU_SS_GRAVEL = 12
 CLM_NPARAM_EH = 13
+CLM_P_F_MAX = 13
+CLM_P_F_OVER = 14
+CLM_P_R_SB = 15
+CLM_NPARAM_MAX = 16
 
 CLM_F_BASE = 0
 CLM_F_AMP = 1
@@ -124,7 +132,7 @@ class ClmConfig(ctypes.Structure):
         ("pad1", ctypes.c_int32),
         ("column_offset", ctypes.c_int64),
         ("host_chunks", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 1),
+        ("runoff", ctypes.c_int32),
     ]
 
 

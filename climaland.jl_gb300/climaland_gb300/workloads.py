@@ -323,6 +323,59 @@ def learned_eval_c3(ncol: int = 262144, nlayers: int = 20, seed: int = 0) -> Wor
     return w
 
 
+def richards_runoff(ncol: int = 1024, nlayers: int = 20, seed: int = 0,
+                    runoff: int = A.CLM_RUNOFF_TOPMODEL) -> Workload:
+    """RichardsModel driven by precipitation through a runoff model
+    (RichardsAtmosDrivenFluxBC): the hydraulics of the 1024 x 20 Richards
+    configuration over 2 m, water that rises from theta_r + 0.1 at the top to
+    nu + 0.05 (saturated) at the bottom, no-flux bottom, precipitation
+    -1e-6 + 5e-7 sin(2 pi t / day) m/s with hourly storms of -2e-5 m/s on 20 % of
+    hours (heavier than most columns' K_sat), TOPMODEL f_max U[0.3, 0.7],
+    f_over 3.28 1/m, R_sb 1.484e-7 m/s (the reference runoff tests' values),
+    dt = 900 s."""
+    rng = np.random.Generator(np.random.PCG64(7000 + seed))
+    cfg = A.default_config()
+    cfg.model = A.CLM_MODEL_RICHARDS
+    cfg.ncol = ncol
+    cfg.nlayers = nlayers
+    cfg.bc_top_water = A.CLM_BC_PRECIP_RUNOFF
+    cfg.bc_bottom_water = A.CLM_BC_FLUX
+    cfg.runoff = runoff
+    cfg.phase_change = 0
+    cfg.forcing_seed = 7000 + seed
+    hyd = _hydraulics(rng, ncol)
+    offsets = (np.arange(ncol + 1) * nlayers).astype(np.int32)
+    z_lo = np.full(ncol, -2.0)
+    z_hi = np.zeros(ncol)
+    frac = (np.arange(nlayers) + 0.5) / nlayers  # 0 at the bottom, 1 at the top
+    lo = hyd["theta_r"][:, None] + 0.1
+    hi = hyd["nu"][:, None] + 0.05
+    v = (hi + (lo - hi) * frac[None, :]).ravel()
+    params = np.zeros((A.CLM_NPARAM_MAX, ncol))
+    params[A.CLM_P_NU] = hyd["nu"]
+    params[A.CLM_P_K_SAT] = hyd["K_sat"]
+    params[A.CLM_P_S_S] = hyd["S_s"]
+    params[A.CLM_P_THETA_R] = hyd["theta_r"]
+    params[A.CLM_P_VG_ALPHA] = hyd["alpha"]
+    params[A.CLM_P_VG_N] = hyd["n"]
+    params[A.CLM_P_F_MAX] = rng.uniform(0.3, 0.7, ncol)
+    params[A.CLM_P_F_OVER] = 3.28
+    params[A.CLM_P_R_SB] = 1.484e-4 / 1000.0
+    ftw = _forcing(ncol)
+    ftw[A.CLM_F_BASE] = -1e-6
+    ftw[A.CLM_F_AMP] = 5e-7
+    ftw[A.CLM_F_OMEGA] = 2.0 * np.pi / DAY
+    ftw[A.CLM_F_PULSE_AMP] = -2e-5
+    ftw[A.CLM_F_PULSE_PERIOD] = 3600.0
+    ftw[A.CLM_F_PULSE_DUTY] = 0.2
+    return Workload(
+        name=f"richards_runoff_{ncol}x{nlayers}", cfg=cfg, ncol=ncol, offsets=offsets,
+        z_lo=z_lo, z_hi=z_hi, params=params,
+        forcing={A.CLM_BC_TOP_WATER: ftw}, vartheta_l=v, theta_i=None,
+        rho_e_int=None, intF_w=np.zeros(ncol), intF_e=None, t0=0.0, dt=900.0,
+        nsteps=96)
+
+
 CONFIGS = {
     "c0": richards_c0,
     "c1": energy_hydrology_c1,

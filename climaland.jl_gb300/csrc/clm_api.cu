@@ -178,6 +178,7 @@ StepArgs step_args(const clm_handle* h) {
   A.bc_bh = h->cfg.bc_bottom_heat;
   A.phase_change = is_eh(h) ? h->cfg.phase_change : 0;
   A.newton_mode = h->cfg.newton_mode;
+  A.runoff = h->cfg.runoff;
   A.max_iters = h->cfg.max_iters;
   A.tol = h->cfg.newton_tol;
   A.energy_scale = h->cfg.energy_norm_scale;
@@ -512,8 +513,14 @@ int clm_create(const clm_config* cfg, clm_handle** out) {
   if (cfg->graph != 0 && cfg->graph != 1) return CLM_ERR_ARG;
   if (cfg->cols_per_cta < 0) return CLM_ERR_ARG;
   const int kinds[4] = {cfg->bc_top_water, cfg->bc_top_heat, cfg->bc_bottom_water, cfg->bc_bottom_heat};
-  for (int k : kinds)
-    if (k < CLM_BC_FLUX || k > CLM_BC_FLUX_ADVECTIVE) return CLM_ERR_ARG;
+  for (int i = 0; i < 4; ++i) {
+    const int k = kinds[i];
+    const bool runoff_top = (i == 0 && k == CLM_BC_PRECIP_RUNOFF);
+    if (!runoff_top && (k < CLM_BC_FLUX || k > CLM_BC_FLUX_ADVECTIVE)) return CLM_ERR_ARG;
+  }
+  if (cfg->bc_top_water == CLM_BC_PRECIP_RUNOFF &&
+      (cfg->model != CLM_MODEL_RICHARDS || cfg->runoff < CLM_RUNOFF_NONE || cfg->runoff > CLM_RUNOFF_TOPMODEL))
+    return CLM_ERR_ARG;  // the EnergyHydrology atmosphere-driven BC is not built
   if (cfg->bc_top_water == CLM_BC_FREE_DRAINAGE || cfg->bc_top_water == CLM_BC_FLUX_ADVECTIVE ||
       cfg->bc_bottom_water == CLM_BC_FLUX_ADVECTIVE || cfg->bc_top_heat == CLM_BC_FREE_DRAINAGE ||
       cfg->bc_bottom_heat == CLM_BC_FLUX_ADVECTIVE)
@@ -540,7 +547,7 @@ int clm_create(const clm_config* cfg, clm_handle** out) {
   const int stride = (h->ncol + kTile - 1) / kTile * kTile;
   const size_t cb = sizeof(double) * stride;
   bool ok = cudaMalloc(&h->d_zlo, cb) == cudaSuccess && cudaMalloc(&h->d_zhi, cb) == cudaSuccess &&
-            cudaMalloc(&h->d_prm, cb * CLM_NPARAM_EH) == cudaSuccess &&
+            cudaMalloc(&h->d_prm, cb * CLM_NPARAM_MAX) == cudaSuccess &&
             cudaMalloc(&h->d_lkap, cb * 2) == cudaSuccess && cudaMalloc(&h->d_Fw, cb) == cudaSuccess &&
             cudaMalloc(&h->d_Fe, cb) == cudaSuccess &&
             cudaMalloc(&h->d_flags, sizeof(uint32_t) * stride) == cudaSuccess &&
@@ -548,7 +555,7 @@ int clm_create(const clm_config* cfg, clm_handle** out) {
             cudaMalloc(&h->d_colstage, cb * 4) == cudaSuccess &&
             cudaMalloc(&h->d_ctr, sizeof(int) * 2) == cudaSuccess;
   if (ok) {
-    ok = cudaMemsetAsync(h->d_prm, 0, cb * CLM_NPARAM_EH, h->stream) == cudaSuccess &&
+    ok = cudaMemsetAsync(h->d_prm, 0, cb * CLM_NPARAM_MAX, h->stream) == cudaSuccess &&
          cudaMemsetAsync(h->d_lkap, 0, cb * 2, h->stream) == cudaSuccess &&
          cudaMemsetAsync(h->d_Fw, 0, cb, h->stream) == cudaSuccess &&
          cudaMemsetAsync(h->d_Fe, 0, cb, h->stream) == cudaSuccess &&
@@ -634,8 +641,9 @@ int clm_set_geometry(clm_handle* h, const double* z_lo, const double* z_hi, cons
 int clm_set_params(clm_handle* h, const double* p, int32_t nparams) {
   if (!h) return CLM_ERR_ARG;
   if (!h->have_geometry) return fail(h, CLM_ERR_STATE, "clm_set_geometry has not been called");
-  const int need = is_eh(h) ? CLM_NPARAM_EH : CLM_NPARAM_RICHARDS;
-  if (!p || nparams < need || nparams > CLM_NPARAM_EH)
+  const bool topmodel = h->cfg.bc_top_water == CLM_BC_PRECIP_RUNOFF && h->cfg.runoff == CLM_RUNOFF_TOPMODEL;
+  const int need = topmodel ? CLM_NPARAM_MAX : (is_eh(h) ? CLM_NPARAM_EH : CLM_NPARAM_RICHARDS);
+  if (!p || nparams < need || nparams > CLM_NPARAM_MAX)
     return fail(h, CLM_ERR_ARG, "expected " + std::to_string(need) + " parameter rows");
   const int ncol = h->ncol;
   for (int c = 0; c < ncol; ++c) {
@@ -644,7 +652,12 @@ int clm_set_params(clm_handle* h, const double* p, int32_t nparams) {
     const double a = p[CLM_P_VG_ALPHA * ncol + c], n = p[CLM_P_VG_N * ncol + c];
     if (!(nu > 0 && nu <= 1) || !(Ks >= 0) || !(Ss > 0) || !(tr >= 0 && tr < nu) || !(a > 0) || !(n > 1))
       return fail(h, CLM_ERR_ARG, "invalid hydraulic parameters in column " + std::to_string(c));
-    if (need == CLM_NPARAM_EH) {
+    if (topmodel) {
+      const double fm = p[CLM_P_F_MAX * ncol + c], fo = p[CLM_P_F_OVER * ncol + c], rs = p[CLM_P_R_SB * ncol + c];
+      if (!(fm >= 0 && fm <= 1) || !(fo >= 0) || !(rs >= 0))
+        return fail(h, CLM_ERR_ARG, "invalid TOPMODEL parameters in column " + std::to_string(c));
+    }
+    if (is_eh(h)) {
       const double kd = p[CLM_P_KAPPA_DRY * ncol + c], kf = p[CLM_P_KAPPA_SAT_FROZEN * ncol + c];
       const double ku = p[CLM_P_KAPPA_SAT_UNFROZEN * ncol + c], rc = p[CLM_P_RHOC_DS * ncol + c];
       if (!(kd >= 0) || !(kf > 0) || !(ku > 0) || !(rc > 0))
@@ -653,7 +666,7 @@ int clm_set_params(clm_handle* h, const double* p, int32_t nparams) {
   }
   int rc = upload_cols_sorted(h, p, h->d_prm, nparams);
   if (rc != CLM_OK) return rc;
-  if (need == CLM_NPARAM_EH) {
+  if (is_eh(h)) {
     std::vector<double> lk((size_t)2 * ncol);
     for (int c = 0; c < ncol; ++c) {
       lk[c] = std::log(p[CLM_P_KAPPA_SAT_UNFROZEN * ncol + c]);

@@ -86,6 +86,17 @@ ClosureArgs base_args(clm_handle* h) {
   return C;
 }
 
+// The closures evaluate the boundary fluxes without a runoff model: the
+// precipitation-driven top boundary is available through clm_step only.
+int closure_ready(clm_handle* h) {
+  const int rc = handle_ready(h);
+  if (rc != CLM_OK) return rc;
+  if (handle_step_args(h).bc_tw == CLM_BC_PRECIP_RUNOFF)
+    return handle_fail(h, CLM_ERR_UNSUPPORTED,
+                       "closure entry points do not evaluate the runoff boundary condition");
+  return CLM_OK;
+}
+
 int copy_out(clm_handle* h, double* host, const double* dev, size_t n) {
   if (!host) return CLM_OK;
   CLM_CUDA(h, cudaMemcpyAsync(host, dev, sizeof(double) * n, cudaMemcpyDeviceToHost, handle_stream(h)));
@@ -94,7 +105,7 @@ int copy_out(clm_handle* h, double* host, const double* dev, size_t n) {
 
 int tendency(clm_handle* h, int kind, double t, double* dv, double* dti, double* de, double* dFw,
              double* dFe) {
-  int rc = handle_ready(h);
+  int rc = closure_ready(h);
   if (rc != CLM_OK) return rc;
   Scratch S;
   ClosureArgs C = base_args(h);
@@ -129,7 +140,7 @@ extern "C" {
 
 int clm_update_aux(clm_handle* h, double t, double* K, double* psi, double* theta_l, double* T,
                    double* kappa, double* Tf, double* bc) {
-  int rc = handle_ready(h);
+  int rc = closure_ready(h);
   if (rc != CLM_OK) return rc;
   Scratch S;
   ClosureArgs C = base_args(h);
@@ -176,7 +187,7 @@ int clm_imp_tendency(clm_handle* h, double t, double* dv, double* dti, double* d
 }
 
 int clm_jacobian(clm_handle* h, double t, double dtgamma, double* Wvv, double* Wev, double* Wee) {
-  int rc = handle_ready(h);
+  int rc = closure_ready(h);
   if (rc != CLM_OK) return rc;
   if (!Wvv) return handle_fail(h, CLM_ERR_ARG, "W_vv is required");
   Scratch S;

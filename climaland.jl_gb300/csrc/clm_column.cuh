@@ -32,6 +32,17 @@
 //   4 (down)  back substitution: delta rho e, x_e -= delta_e.
 // JT is the Jacobian/Thomas type: double (plain path) or float (mixed path,
 // where an FP64 column-sum projection keeps the solve's exact budget identity).
+//
+// Mixed-path elimination. Every column of the water and energy blocks of
+// W = dt dT_imp/dY - I sums to -1 (the face fluxes telescope), plus the
+// MoistureStateBC term at the top. In stiff cells (saturated soil: dpsi =
+// 1/S_s) the diagonal is -(off-diagonals) - 1 with off-diagonals near 1e7, and
+// the "- 1" is below float resolution, so the textbook pivot M_k - L_k c'_{k-1}
+// cancels. The float path therefore carries the reduced column sums s'_k of
+// the Schur complement (Grassmann-Taksar-Heyman style): s'_k = s_k -
+// U_{k-1} s'_{k-1} / piv_{k-1} and piv_k = s'_k - L_{k+1}, where every term
+// has one sign (U, L >= 0; s', piv < 0): no cancellation at any stiffness.
+// The FP64 path keeps the reference's Thomas recurrence.
 #pragma once
 
 #include "clm_internal.cuh"
@@ -332,6 +343,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
     for (int it = 1; it <= A.max_iters; ++it) {
       // sweep 1 (bottom -> top)
       JT cp_prev = 0, dp_prev = 0;
+      JT U_prev = 0, sp_prev = -1, piv_prev = -1;  // mixed: reduced column sums
       double Fw_dn = Fbw, Fe_dn = Fbh;
       double aw_dn = 0.0;
       JT awr_dn = 0;  // mixed: dt K_face / dz^2 of the face below
@@ -377,7 +389,17 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
           U = (k < n - 1) ? (JT)(rdz * aw_up * Dn) : (JT)0;
           Md = (JT)(-rdz * (aw_up + aw_dn) * Dc - 1.0);
         }
-        const JT inv = (JT)1 / (Md - L * cp_prev);
+        JT piv;
+        if constexpr (mixed) {
+          const JT sp = (k == 0) ? (JT)-1 : (JT)-1 - U_prev * (sp_prev / piv_prev);
+          piv = sp - awr_up * Dc;  // L_{k+1} = dt K_face(k|k+1) / dz^2 dpsi_k
+          U_prev = U;
+          sp_prev = sp;
+          piv_prev = piv;
+        } else {
+          piv = Md - L * cp_prev;
+        }
+        const JT inv = (JT)1 / piv;
         const JT cpk = U * inv;
         const JT dpk = ((JT)fv - L * dp_prev) * inv;
         J.cp[k] = cpk;
@@ -418,6 +440,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       // elimination (c'' into cp, d'' into dp behind the read of delta_v)
       {
         JT c_prev = 0, d_prev = 0;
+        JT U_prev = 0, sp_prev = -1, piv_prev = -1;  // mixed: reduced column sums
         double ak_dn = 0.0;
         JT akr_dn = 0;
         JT dvm = 0, Dm = 0;
@@ -464,7 +487,17 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
             U = (JT)(rdz * ak_up * irc_n);
             Md = (JT)(-rdz * (ak_up + ak_dn) * irc_c - 1.0);
           }
-          const JT inv = (JT)1 / (Md - L * c_prev);
+          JT piv;
+          if constexpr (mixed) {
+            const JT sp = (k == 0) ? (JT)-1 : (JT)-1 - U_prev * (sp_prev / piv_prev);
+            piv = sp - akr_up * ircf_c;  // L_{k+1} = dt kappa_face(k|k+1) / dz^2 / rho c_k
+            U_prev = U;
+            sp_prev = sp;
+            piv_prev = piv;
+          } else {
+            piv = Md - L * c_prev;
+          }
+          const JT inv = (JT)1 / piv;
           const JT ck = U * inv;
           const JT dk = ((JT)g - L * d_prev) * inv;
           J.cp[k] = ck;
@@ -565,6 +598,10 @@ struct RBuffers {
 template <typename JT>
 struct RJac {
   Col<JT> cp, dp;
+  // mixed path: low words of the double-float right-hand side recurrence
+  // (the residual is not rounded to float: in stiff columns it is far
+  // larger than the smooth modes of the solution)
+  Col<JT> dpl{nullptr, 0};
 };
 
 template <typename JT>
@@ -601,10 +638,38 @@ CLM_HD void richards_column(const StepArgs& A, const Tables& Tb, int s, int n, i
     // without dfluxBCdY the fluxes are those of the explicit stage at (u, t);
     // U = u, so iteration 1 (x = U) evaluates exactly those
     double Ftw = ftw, Fbw = fbw;
+    // RichardsAtmosDrivenFluxBC (boundary_conditions.jl:200-212): the runoff
+    // model (Runoff.jl) turns the precipitation ftw into the infiltration at
+    // (u, t); TOPMODEL adds the implicit subsurface sink (Runoff.jl:321-345)
+    // R_ss / max(h_sat, eps) on the saturated layers, not in the Jacobian.
+    // All of it is frozen through the Newton solve.
+    double R_ss = 0.0, q_sink = 0.0;
+    const double nr = nu - theta_r;
+    if (A.bc_tw == CLM_BC_PRECIP_RUNOFF) {
+      const double ic = -1.0 * K_sat;  // soil_infiltration_capacity (Runoff.jl:386-399)
+      if (A.runoff == CLM_RUNOFF_SURFACE) {
+        const double is_sat = ((B.gv[n - 1] + 0.0) - nu) > kEps ? 1.0 : 0.0;
+        Ftw = (1.0 - is_sat) * fmax(ic, ftw);
+      } else if (A.runoff == CLM_RUNOFF_TOPMODEL) {
+        double h = 0.0;  // column_integral_definite of the saturation weights
+        for (int k = 0; k < n; ++k) {
+          const double twc = B.gv[k] + 0.0 - theta_r;
+          h += dz * ((twc - nr > kEps ? 1.0 : 0.0) * twc / nr);
+        }
+        const double zwt = (A.z_hi[s] - A.z_lo[s]) - h;
+        const double f_sat = fmin(P[CLM_P_F_MAX * st + s] *
+                                      fm::exp(Tb, -P[CLM_P_F_OVER * st + s] / 2.0 * zwt), 1.0);
+        Ftw = (1.0 - f_sat) * fmax(ic, ftw);
+        R_ss = P[CLM_P_R_SB * st + s] * fm::exp(Tb, -P[CLM_P_F_OVER * st + s] * zwt);
+        q_sink = R_ss / fmax(h, kEps);
+      }
+    }
     double prev_norm = 1e300;
     for (int it = 1; it <= A.max_iters; ++it) {
       const bool refresh_bc = dflux || it == 1;
       JT cp_prev = 0, dp_prev = 0;
+      JT U_prev = 0, sp_prev = -1, piv_prev = -1;  // mixed: reduced column sums
+      F2 dpf_prev = ff::make(0.0f);                // mixed: double-float d'
       double aw_dn = 0.0;
       JT D_prev = 0;
       double sum_f = 0.0;
@@ -629,39 +694,63 @@ CLM_HD void richards_column(const StepArgs& A, const Tables& Tb, int s, int n, i
           if (dflux) Md_extra = -dt * ((Kc * Dc / half) * inv_dz);
           Fw_up = Ftw;
         }
-        const double Tv = -((Fw_up - Fw_dn) * inv_dz);
+        double Tv = -((Fw_up - Fw_dn) * inv_dz);
+        if (q_sink != 0.0) {
+          const double twc = B.gv[k] + 0.0 - theta_r;  // U = u for Richards
+          Tv -= q_sink * ((twc - nr > kEps ? 1.0 : 0.0) * twc / nr);
+        }
         const double f = B.gv[k] + dt * Tv - B.xv[k];
         sum_f += f;
         const JT L = (JT)(rdz * aw_dn) * D_prev;
         const JT U = (k < n - 1) ? (JT)(rdz * aw_up * Dn) : (JT)0;
         const JT M = (JT)(-rdz * (aw_up + aw_dn) * Dc - 1.0 + Md_extra);
-        const JT inv = (JT)1 / (M - L * cp_prev);
+        JT piv;
+        if constexpr (mixed) {
+          // column sum -1 (+ the MoistureStateBC term of the top column)
+          const JT s_k = (JT)(-1.0 + Md_extra);
+          const JT sp = (k == 0) ? s_k : s_k - U_prev * (sp_prev / piv_prev);
+          piv = sp - ((k < n - 1) ? (JT)(rdz * aw_up) * (JT)Dc : (JT)0);  // L_{k+1}
+          U_prev = U;
+          sp_prev = sp;
+          piv_prev = piv;
+        } else {
+          piv = M - L * cp_prev;
+        }
+        const JT inv = (JT)1 / piv;
         const JT cpk = U * inv;
-        const JT dpk = ((JT)f - L * dp_prev) * inv;
         J.cp[k] = cpk;
-        J.dp[k] = dpk;
+        if constexpr (mixed) {
+          const F2 dpf = ff::mul_f(ff::sub(ff::from_double(f), ff::mul_f(dpf_prev, L)), inv);
+          J.dp[k] = dpf.hi;
+          J.dpl[k] = dpf.lo;
+          dpf_prev = dpf;
+        } else {
+          const JT dpk = ((JT)f - L * dp_prev) * inv;
+          J.dp[k] = dpk;
+          dp_prev = dpk;
+        }
         cp_prev = cpk;
-        dp_prev = dpk;
         Fw_dn = Fw_up;
         aw_dn = aw_up;
         D_prev = (JT)Dc;
         Kc = Kn; psic = psin; Dc = Dn;
       }
-      const double fFw = UFw + dt * (-(Ftw - Fbw)) - xFw;
+      const double fFw = UFw + dt * ((-(Ftw - Fbw)) - R_ss) - xFw;
       xFw += fFw;
       double norm2 = fFw * fFw;
-      if (mixed) {
-        JT nxt = 0;
+      if constexpr (mixed) {
+        F2 nxt = ff::make(0.0f);
         double sd = 0.0;
         for (int k = n - 1; k >= 0; --k) {
-          const JT d = J.dp[k] - J.cp[k] * nxt;
-          J.dp[k] = d;
-          sd += (double)d;
+          const F2 d = ff::sub(F2{J.dp[k], J.dpl[k]}, ff::mul_f(nxt, J.cp[k]));
+          J.dp[k] = d.hi;
+          J.dpl[k] = d.lo;
+          sd += ff::to_double(d);
           nxt = d;
         }
         const double corr = dflux ? 0.0 : (sd + sum_f) / n;
         for (int k = 0; k < n; ++k) {
-          const double d = (double)J.dp[k] - corr;
+          const double d = ff::to_double(F2{J.dp[k], J.dpl[k]}) - corr;
           B.xv[k] -= d;
           norm2 += d * d;
         }

@@ -35,7 +35,7 @@ struct StepArgs {
   Layout L;
   const double* z_lo;   // [stride]
   const double* z_hi;   // [stride]
-  const double* prm;    // [CLM_NPARAM_EH][stride]
+  const double* prm;    // [CLM_NPARAM_MAX][stride]
   const double* lkap;   // [2][stride] log kappa_sat_unfrozen, log kappa_sat_frozen
   const double* forc[4];  // [CLM_F_NFIELDS][stride] per slot, or null
   double* v;            // vartheta_l (internal layout)
@@ -51,6 +51,7 @@ struct StepArgs {
   EHScalars sc;
   int bc_tw, bc_th, bc_bw, bc_bh;
   int phase_change;
+  int runoff;           // enum clm_runoff (CLM_BC_PRECIP_RUNOFF)
   int newton_mode;
   int max_iters;
   double tol;

@@ -23,8 +23,13 @@ __host__ __device__ constexpr size_t eh_smem_per_layer() {
 }
 
 template <typename JT>
+__host__ __device__ constexpr int richards_jac_arrays() {
+  return sizeof(JT) < sizeof(double) ? 3 : 2;  // cp, dp (| low words of dp)
+}
+
+template <typename JT>
 __host__ __device__ constexpr size_t richards_smem_per_layer() {
-  return sizeof(double) + 2 * sizeof(JT);  // xv | cp, dp
+  return sizeof(double) + richards_jac_arrays<JT>() * sizeof(JT);  // xv | cp, dp (, dp low)
 }
 
 // Per-warp scratch slots of nmax x 32 doubles: K, face kappa / dz, face
@@ -114,7 +119,8 @@ __global__ void __launch_bounds__(128, 1)
   const int wpc = blockDim.x >> 5;
   const int64_t lay = (int64_t)A.L.nmax * kTile;
   double* dw = tab + fm::TABLE_SIZE + (int64_t)warp * lay;
-  JT* jw = reinterpret_cast<JT*>(tab + fm::TABLE_SIZE + (int64_t)wpc * lay) + (int64_t)warp * 2 * lay;
+  constexpr int kJA = richards_jac_arrays<JT>();
+  JT* jw = reinterpret_cast<JT*>(tab + fm::TABLE_SIZE + (int64_t)wpc * lay) + (int64_t)warp * kJA * lay;
   const int gwarp = blockIdx.x * wpc + warp;
   const int nwarps = gridDim.x * wpc;
   RBuffers B;
@@ -122,6 +128,7 @@ __global__ void __launch_bounds__(128, 1)
   RJac<JT> J;
   J.cp = Col<JT>{jw + lane, kTile};
   J.dp = Col<JT>{jw + lay + lane, kTile};
+  if (kJA > 2) J.dpl = Col<JT>{jw + 2 * lay + lane, kTile};
   const double t0 = clk.start(), dt = clk.step();
   const bool dyn = A.tile_ctr != nullptr;
   const int tend = A.tile_end < 0 ? A.L.ntiles : A.tile_end;

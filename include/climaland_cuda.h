@@ -79,14 +79,35 @@ enum clm_bc_kind {
                                  as heat BC: EnergyWaterFreeDrainage
                                  F_e = -K_1 rho e_liq(T_1)                 */
   CLM_BC_STATE = 2,           /* MoistureStateBC / TemperatureStateBC      */
-  CLM_BC_FLUX_ADVECTIVE = 3   /* heat only: F_e = f(t) + F_w,top(t) *
+  CLM_BC_FLUX_ADVECTIVE = 3,  /* heat only: F_e = f(t) + F_w,top(t) *
                                  rho e_liq(T_adv), T_adv per column        */
+  CLM_BC_PRECIP_RUNOFF = 4    /* water, top, RichardsModel:
+                                 RichardsAtmosDrivenFluxBC
+                                 (boundary_conditions.jl:64-100, :200-212):
+                                 the top-water forcing row is the liquid
+                                 precipitation P(t) (< 0 into the soil),
+                                 cfg->runoff turns it into the infiltration
+                                 flux at the explicit stage               */
 };
 
 /* Per-column parameter rows for clm_set_params (SoA, row p of ncol). The
  * first CLM_NPARAM_RICHARDS rows are RichardsParameters (rre.jl:7-21); all
  * CLM_NPARAM_EH rows are the per-point EnergyHydrologyParameters
  * (energy_hydrology.jl:21-78). */
+/* Runoff model of CLM_BC_PRECIP_RUNOFF (src/standalone/Soil/Runoff/Runoff.jl). */
+enum clm_runoff {
+  CLM_RUNOFF_NONE = 0,     /* NoRunoff: infiltration = P (:56-80)            */
+  CLM_RUNOFF_SURFACE = 1,  /* SurfaceRunoff: (1 - H(theta_top - nu)) max(-K_sat, P)
+                              (:85-145)                                      */
+  CLM_RUNOFF_TOPMODEL = 2  /* TOPMODELRunoff (:198-270, :373-440): h_sat = sum dz
+                              H(vartheta - nu) (vartheta - theta_r)/(nu - theta_r),
+                              f_sat = min(f_max exp(-f_over z_wt / 2), 1),
+                              infiltration (1 - f_sat) max(-K_sat, P), and the
+                              TOPMODELSubsurfaceRunoff sink (:321-345) of
+                              R_ss = R_sb exp(-f_over z_wt) spread over the
+                              saturated layers, z_wt = depth - h_sat        */
+};
+
 enum clm_param {
   CLM_P_NU = 0,            /* porosity nu                                 */
   CLM_P_K_SAT = 1,         /* saturated hydraulic conductivity (m/s)      */
@@ -102,7 +123,13 @@ enum clm_param {
   CLM_P_NU_SS_OM = 10,
   CLM_P_NU_SS_QUARTZ = 11,
   CLM_P_NU_SS_GRAVEL = 12,
-  CLM_NPARAM_EH = 13
+  CLM_NPARAM_EH = 13,
+  /* TOPMODEL rows (CLM_RUNOFF_TOPMODEL; the reference's f_over and R_sb are
+   * scalars, f_max a surface field) */
+  CLM_P_F_MAX = 13,        /* maximum saturated fraction                      */
+  CLM_P_F_OVER = 14,       /* 1/m                                             */
+  CLM_P_R_SB = 15,         /* m/s                                             */
+  CLM_NPARAM_MAX = 16
 };
 
 /* Forcing descriptor rows for clm_set_bc (SoA, row f of ncol). A boundary
@@ -180,7 +207,7 @@ typedef struct clm_config {
                              domain is split across handles or GPUs: the
                              rain-pulse hash uses the global column index  */
   int32_t host_chunks;    /* clm_step_host pipeline depth (0: by size)      */
-  int32_t reserved[1];
+  int32_t runoff;         /* enum clm_runoff (CLM_BC_PRECIP_RUNOFF)         */
 } clm_config;
 
 typedef struct clm_handle clm_handle;

@@ -294,6 +294,8 @@ typedef struct {
   double nu, K_sat, S_s, theta_r, alpha, vgn, vgm;
   double kappa_dry, kappa_sat_frozen, kappa_sat_unfrozen, rhoc_ds;
   double nu_om, nu_quartz, nu_gravel;
+  double f_max, f_over, R_sb; /* TOPMODEL (Runoff.jl:198-232)          */
+  double depth;               /* model.domain.depth: z_hi - z_lo       */
   const clm_config* cfg;
   const clmo_problem* P;
   int c;
@@ -303,6 +305,11 @@ typedef struct { /* p.soil */
   double K[MAXL], psi[MAXL], theta_l[MAXL], T[MAXL], kappa[MAXL], Tf[MAXL];
   double top_w, top_h, bot_w, bot_h;
   int has_dflux;
+  /* runoff (Runoff.jl): infiltration, surface runoff R_s, subsurface runoff
+   * R_ss, saturated height h_sat, per-layer saturation weights */
+  double infiltration, R_s, R_ss, h_sat;
+  double sat_w[MAXL];
+  int runoff_sink;
   double dfluxBCdY;
   double total_water, total_energy;
   int psi_positive;
@@ -346,6 +353,13 @@ static void col_init(col_t* C, const clmo_problem* P, int c) {
   C->alpha = p[CLM_P_VG_ALPHA * ncol + c];
   C->vgn = p[CLM_P_VG_N * ncol + c];
   C->vgm = 1.0 - 1.0 / C->vgn; /* retention_models.jl:364-368 */
+  C->depth = zhi - zlo;
+  C->f_max = C->f_over = C->R_sb = 0.0;
+  if (P->nparams >= CLM_NPARAM_MAX) {
+    C->f_max = p[CLM_P_F_MAX * ncol + c];
+    C->f_over = p[CLM_P_F_OVER * ncol + c];
+    C->R_sb = p[CLM_P_R_SB * ncol + c];
+  }
   if (C->eh) {
     C->kappa_dry = p[CLM_P_KAPPA_DRY * ncol + c];
     C->kappa_sat_frozen = p[CLM_P_KAPPA_SAT_FROZEN * ncol + c];
@@ -455,6 +469,51 @@ static double diffusive_flux(double K, double x2, double x1, double dz) {
   return -K * (x2 - x1) / dz;
 }
 
+/* Runoff of RichardsAtmosDrivenFluxBC (src/standalone/Soil/Runoff/Runoff.jl):
+ * update_infiltration_water_flux! for NoRunoff (:69-80), SurfaceRunoff
+ * (:129-145) and TOPMODELRunoff (:234-270) on a RichardsModel column (no ice:
+ * model_agnostic_volumetric_ice_content is zero). precip is P_liq (m/s). */
+static double runoff_heaviside(double x) { return (x - 0.0 > EPS64) ? 1.0 : 0.0; } /* utils.jl:83-100 */
+
+static void richards_runoff(const col_t* C, const state_t* Y, cache_t* p, double precip) {
+  const int n = C->n;
+  const double ic = -1.0 * C->K_sat; /* soil_infiltration_capacity (Richards): -K_sat (:386-399) */
+  switch (C->cfg->runoff) {
+    case CLM_RUNOFF_SURFACE: {
+      /* is_saturated(vartheta_l + theta_i, nu) at the top centre */
+      const double is_sat = runoff_heaviside((Y->v[n - 1] + 0.0) - C->nu);
+      p->infiltration = (1.0 - is_sat) * fmax(ic, precip); /* surface_infiltration (:107-109) */
+      p->R_s = fabs(precip - p->infiltration);
+      break;
+    }
+    case CLM_RUNOFF_TOPMODEL: {
+      /* is_saturated(vartheta_l + theta_i - theta_r, nu - theta_r) weighted
+       * by (vartheta_l + theta_i - theta_r) / (nu - theta_r); h_sat is its
+       * column_integral_definite (sum of dz f, bottom to top) */
+      double h = 0.0;
+      for (int k = 0; k < n; ++k) {
+        const double twc = Y->v[k] + 0.0 - C->theta_r, nr = C->nu - C->theta_r;
+        p->sat_w[k] = runoff_heaviside(twc - nr) * twc / nr;
+        h += C->dzc[k] * p->sat_w[k];
+      }
+      p->h_sat = h;
+      const double zwt = C->depth - h;
+      /* topmodel_surface_infiltration (:373-376) */
+      const double f_sat = fmin(C->f_max * exp(-C->f_over / 2.0 * zwt), 1.0);
+      p->infiltration = (1.0 - f_sat) * fmax(ic, precip);
+      p->R_s = fabs(precip - p->infiltration);
+      /* the liquid-only repetition gives the same weights without ice;
+       * topmodel_ss_flux (:427-429) */
+      p->R_ss = C->R_sb * exp(-C->f_over * zwt);
+      p->runoff_sink = 1;
+      break;
+    }
+    default: /* NoRunoff */
+      p->infiltration = precip;
+      p->R_s = 0.0;
+  }
+}
+
 /* Boundary fluxes.
  * Richards: rre.jl:111-149 with boundary_flux! methods
  *   WaterFluxBC :168-180, MoistureStateBC top :227-264 / bottom :278-315,
@@ -477,7 +536,12 @@ static void update_boundary_fluxes(const col_t* C, const state_t* Y,
   double nu_top = C->nu, nu_bot = C->nu;
 
   /* water, top */
+  p->runoff_sink = 0;
   switch (cfg->bc_top_water) {
+    case CLM_BC_PRECIP_RUNOFF: /* RichardsAtmosDrivenFluxBC: boundary_conditions.jl:200-212 */
+      richards_runoff(C, Y, p, f_tw);
+      p->top_w = p->infiltration;
+      break;
     case CLM_BC_STATE: {
       double psi_bc = clmo_pressure_head(C->alpha, C->vgn, C->vgm, C->theta_r,
                                          f_tw, nu_top, C->S_s);
@@ -607,6 +671,12 @@ static void imp_tendency(const col_t* C, const state_t* Y, const cache_t* p,
     Fw[k] = -Kf * gh;
   }
   for (int k = 0; k < n; ++k) dY->v[k] = -((Fw[k + 1] - Fw[k]) / C->dzc[k]);
+  if (p->runoff_sink) {
+    /* TOPMODELSubsurfaceRunoff source! (Runoff.jl:321-345), an implicit
+     * source with the cached R_ss, h_sat and saturation weights */
+    for (int k = 0; k < n; ++k) dY->v[k] -= (p->R_ss / fmax(p->h_sat, EPS64)) * p->sat_w[k];
+    dY->Fw -= p->R_ss;
+  }
   if (C->eh) {
     dY->Fe = -(p->top_h - p->bot_h);
     Fe[0] = p->bot_h;
@@ -814,6 +884,11 @@ static int check_problem(const clmo_problem* P) {
   int need = P->cfg.model == CLM_MODEL_ENERGY_HYDROLOGY ? CLM_NPARAM_EH
                                                         : CLM_NPARAM_RICHARDS;
   if (P->nparams < need) return CLM_ERR_ARG;
+  if (P->cfg.bc_top_water == CLM_BC_PRECIP_RUNOFF) {
+    if (P->cfg.model != CLM_MODEL_RICHARDS) return CLM_ERR_ARG;
+    if (P->cfg.runoff < CLM_RUNOFF_NONE || P->cfg.runoff > CLM_RUNOFF_TOPMODEL) return CLM_ERR_ARG;
+    if (P->cfg.runoff == CLM_RUNOFF_TOPMODEL && P->nparams < CLM_NPARAM_MAX) return CLM_ERR_ARG;
+  }
   for (int c = 0; c < P->ncol; ++c) {
     int n = P->offsets[c + 1] - P->offsets[c];
     if (n < 2 || n > MAXL) return CLM_ERR_ARG;
@@ -998,6 +1073,32 @@ int clmo_step(const clmo_problem* P, double* v, double* ti, double* e,
     if (fl & CLM_COL_NONFINITE) bad = 1;
   }
   return bad ? CLM_ERR_NAN : CLM_OK;
+}
+
+/* Runoff diagnostics of the explicit-stage cache (per column): the
+ * infiltration (the top water flux), R_s, R_ss and h_sat (p.soil.infiltration,
+ * R_s, R_ss, h_grad of Runoff.jl). */
+int clmo_runoff(const clmo_problem* P, const double* v, double t, double* infiltration,
+                double* R_s, double* R_ss, double* h_sat) {
+  int rc = check_problem(P);
+  if (rc) return rc;
+  if (P->cfg.bc_top_water != CLM_BC_PRECIP_RUNOFF) return CLM_ERR_ARG;
+  set_threads(P);
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < P->ncol; ++c) {
+    col_t C;
+    col_init(&C, P, c);
+    state_t Y;
+    cache_t p;
+    memset(&p, 0, sizeof(p));
+    state_load(&C, &Y, v, NULL, NULL, NULL, NULL);
+    update_cache(&C, &Y, &p, t);
+    infiltration[c] = p.infiltration;
+    R_s[c] = p.R_s;
+    R_ss[c] = p.R_ss;
+    h_sat[c] = p.h_sat;
+  }
+  return CLM_OK;
 }
 
 int clmo_budgets(const clmo_problem* P, const double* v, const double* ti,

@@ -90,6 +90,9 @@ double clmo_forcing_value(const double* forcing, int32_t ncol, int32_t c,
  * per column. theta_i / rho_e_int / intF_e are ignored for Richards. */
 
 /* update_aux + update_boundary_fluxes at (state, t) (make_update_cache). */
+/* runoff diagnostics of CLM_BC_PRECIP_RUNOFF (RichardsModel) */
+int clmo_runoff(const clmo_problem* P, const double* vartheta_l, double t,
+                double* infiltration, double* R_s, double* R_ss, double* h_sat);
 int clmo_update_cache(const clmo_problem* P, const double* vartheta_l,
                       const double* theta_i, const double* rho_e_int,
                       double t, double* K, double* psi, double* theta_l,

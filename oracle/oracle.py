@@ -113,6 +113,8 @@ def lib():
                                 ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_int32)]
         L.clmo_budgets.restype = ctypes.c_int
         L.clmo_budgets.argtypes = [_PP, _DP, _DP, _DP, _DP, _DP]
+        L.clmo_runoff.restype = ctypes.c_int
+        L.clmo_runoff.argtypes = [_PP, _DP, _D] + [_DP] * 4
         _lib = L
     return _lib
 
@@ -218,6 +220,14 @@ class Oracle:
                               A.dptr(c(fe) if fe is not None else None), A.dptr(dv), A.dptr(de))
         assert rc == 0, rc
         return dv, de
+
+    def runoff(self, state, t):
+        """Runoff diagnostics of the explicit stage (CLM_BC_PRECIP_RUNOFF):
+        infiltration, R_s, R_ss, h_sat per column."""
+        out = [np.zeros(self.w.ncol) for _ in range(4)]
+        rc = lib().clmo_runoff(ctypes.byref(self.P), A.dptr(state[0]), float(t), *[A.dptr(a) for a in out])
+        assert rc == 0, rc
+        return dict(zip(("infiltration", "R_s", "R_ss", "h_sat"), out))
 
     def budgets(self, state):
         W = np.zeros(self.w.ncol)

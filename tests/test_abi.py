@@ -74,3 +74,23 @@ def test_create_rejects_bad_config_before_touching_the_device(lib):
     cfg.bc_top_water = A.CLM_BC_FREE_DRAINAGE
     assert lib.clm_create(ctypes.byref(cfg), ctypes.byref(h)) == A.CLM_ERR_ARG
     assert lib.clm_last_error(None) == b"null handle"
+
+
+def test_create_rejects_runoff_outside_richards(lib):
+    # the precipitation/runoff top boundary is RichardsAtmosDrivenFluxBC: an
+    # EnergyHydrology handle (whose atmosphere-driven BC is not built), the
+    # heat or bottom slots and unknown runoff kinds are refused before any
+    # device work
+    h = ctypes.c_void_p()
+    cfg = A.default_config()
+    cfg.ncol = 10
+    cfg.nlayers = 5
+    cfg.bc_top_water = A.CLM_BC_PRECIP_RUNOFF
+    assert lib.clm_create(ctypes.byref(cfg), ctypes.byref(h)) == A.CLM_ERR_ARG  # EnergyHydrology
+    cfg.model = A.CLM_MODEL_RICHARDS
+    cfg.runoff = 7
+    assert lib.clm_create(ctypes.byref(cfg), ctypes.byref(h)) == A.CLM_ERR_ARG
+    cfg.runoff = A.CLM_RUNOFF_TOPMODEL
+    cfg.bc_top_water = A.CLM_BC_FLUX
+    cfg.bc_bottom_water = A.CLM_BC_PRECIP_RUNOFF
+    assert lib.clm_create(ctypes.byref(cfg), ctypes.byref(h)) == A.CLM_ERR_ARG

@@ -85,6 +85,26 @@ def test_mixed_precision_tolerance_mode():
     report("mixed_full_scale_tol", check_parity(w, 48, oracle_cfg=TOL_MODE, **TOL_MODE, **MIXED))
 
 
+@pytest.mark.parametrize("kind", [A.CLM_RUNOFF_NONE, A.CLM_RUNOFF_SURFACE, A.CLM_RUNOFF_TOPMODEL])
+def test_richards_precipitation_runoff(kind):
+    """RichardsAtmosDrivenFluxBC with each runoff model: hourly storms above
+    K_sat, saturated deep layers (TOPMODEL's saturated height and subsurface
+    sink); budgets against the oracle's (the reference keeps subtracting R_ss
+    from the integrated flux when no layer is saturated). FP64 path only: in
+    saturated layers dpsi = 1/S_s makes the Jacobian's off-diagonals ~1e7
+    against its "- I", which a float Jacobian cannot represent."""
+    w = WL.richards_runoff(ncol=1024, runoff=kind)
+    report(f"richards_runoff_{kind}", check_parity(w, 48))
+
+
+def test_runoff_handles_refuse_closures():
+    w = WL.richards_runoff(ncol=64)
+    with D.SoilColumns(w) as g:
+        with pytest.raises(D.ClmError) as e:
+            g.update_aux(w.t0)
+        assert e.value.code == A.CLM_ERR_UNSUPPORTED
+
+
 def test_richards_tolerance_mode():
     w = WL.richards_c0(ncol=512)
     st = check_parity(w, 48, oracle_cfg=TOL_MODE, **TOL_MODE)

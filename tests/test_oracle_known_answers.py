@@ -490,3 +490,91 @@ def test_forcing_hash_deterministic(L):
     assert all(0.0 <= v < 1.0 for v in vals)
     assert abs(np.mean(vals) - 0.5) < 0.05
     assert L.clm_forcing_hash01(7, 3, 5) == L.clm_forcing_hash01(7, 3, 5)
+
+
+# ---- runoff (test/standalone/Soil/runoff.jl) ---------------------------------
+
+def _runoff_state(kind):
+    w = WL.richards_runoff(ncol=32, runoff=kind, seed=3)
+    return w, w.copy_state()
+
+
+def test_topmodel_runoff_diagnostics():
+    # runoff.jl:173-213: h_grad = column integral of H(vartheta - nu) (vartheta -
+    # theta_r) / (nu - theta_r); R_ss = topmodel_ss_flux(R_sb, f_over, depth -
+    # h_grad); infiltration = topmodel_surface_infiltration(f_max, f_over, depth
+    # - h_grad, -K_sat, P); R_s = |P - infiltration|
+    w, st = _runoff_state(A.CLM_RUNOFF_TOPMODEL)
+    o = O.Oracle(w)
+    r = o.runoff(st, w.t0)
+    P = w.params
+    nl = w.nlayers
+    v = st[0].reshape(w.ncol, nl[0])
+    nu, tr = P[A.CLM_P_NU][:, None], P[A.CLM_P_THETA_R][:, None]
+    dz = ((w.z_hi - w.z_lo) / nl)[:, None]
+    h = np.sum(dz * (((v - nu) > np.finfo(float).eps) * (v - tr) / (nu - tr)), axis=1)
+    assert np.allclose(r["h_sat"], h, rtol=1e-14, atol=0)
+    assert np.all(r["h_sat"] > 0)  # the bottom layers start saturated
+    depth = w.z_hi - w.z_lo
+    precip = w.forcing[A.CLM_BC_TOP_WATER][A.CLM_F_BASE] + 0.0  # t = 0: sin term zero
+    pulses = O.lib().clm_forcing_hash01
+    storm = np.array([pulses(w.cfg.forcing_seed, c, 0) < 0.2 for c in range(w.ncol)])
+    precip = precip + np.where(storm, -2e-5, 0.0)
+    fo, fm, rsb = P[A.CLM_P_F_OVER], P[A.CLM_P_F_MAX], P[A.CLM_P_R_SB]
+    f_sat = np.minimum(fm * np.exp(-fo / 2 * (depth - h)), 1.0)
+    infil = (1 - f_sat) * np.maximum(-P[A.CLM_P_K_SAT], precip)
+    assert np.allclose(r["R_ss"], rsb * np.exp(-fo * (depth - h)), rtol=1e-13, atol=0)
+    assert np.allclose(r["infiltration"], infil, rtol=1e-13, atol=1e-22)
+    assert np.allclose(r["R_s"], np.abs(precip - infil), rtol=1e-12, atol=1e-22)
+
+
+def test_surface_and_no_runoff():
+    # runoff.jl:355-383 (SurfaceRunoff) and :26-90 (NoRunoff: infiltration = P)
+    for kind in (A.CLM_RUNOFF_SURFACE, A.CLM_RUNOFF_NONE):
+        w, st = _runoff_state(kind)
+        r = O.Oracle(w).runoff(st, w.t0)
+        P = w.params
+        top = st[0].reshape(w.ncol, -1)[:, -1]
+        precip = w.forcing[A.CLM_BC_TOP_WATER][A.CLM_F_BASE] + np.where(
+            np.array([O.lib().clm_forcing_hash01(w.cfg.forcing_seed, c, 0) < 0.2 for c in range(w.ncol)]),
+            -2e-5, 0.0)
+        if kind == A.CLM_RUNOFF_NONE:
+            assert np.array_equal(r["infiltration"], precip)
+        else:
+            sat = (top - P[A.CLM_P_NU]) > np.finfo(float).eps
+            expect = (1 - sat) * np.maximum(-P[A.CLM_P_K_SAT], precip)
+            assert np.allclose(r["infiltration"], expect, rtol=1e-15, atol=0)
+            assert np.allclose(r["R_s"], np.abs(precip - expect), rtol=1e-13, atol=1e-22)
+
+
+def test_topmodel_sink_in_implicit_tendency():
+    # Runoff.jl:321-345: d(vartheta_l) -= R_ss / max(h_grad, eps) H(...) w; the
+    # integrated flux loses R_ss; the sink leaves the tendency's water budget
+    # identity (sum dz d(vartheta) = d(intF_w)) intact where h_grad > 0
+    w, st = _runoff_state(A.CLM_RUNOFF_TOPMODEL)
+    o = O.Oracle(w)
+    d = o.imp_tendency(st, w.t0)
+    w0 = WL.richards_runoff(ncol=32, runoff=A.CLM_RUNOFF_NONE, seed=3)
+    o0 = O.Oracle(w0)
+    r = o.runoff(st, w.t0)
+    r0 = o0.runoff(st, w.t0)
+    # the same infiltration through a flux BC isolates the sink
+    w1 = WL.richards_runoff(ncol=32, runoff=A.CLM_RUNOFF_NONE, seed=3)
+    w1.cfg.bc_top_water = A.CLM_BC_FLUX
+    w1.forcing[A.CLM_BC_TOP_WATER] = np.zeros_like(w1.forcing[A.CLM_BC_TOP_WATER])
+    w1.forcing[A.CLM_BC_TOP_WATER][A.CLM_F_BASE] = r["infiltration"]
+    d1 = O.Oracle(w1).imp_tendency(st, w.t0)
+    P = w.params
+    v = st[0].reshape(w.ncol, -1)
+    nu, tr = P[A.CLM_P_NU][:, None], P[A.CLM_P_THETA_R][:, None]
+    wgt = ((v - tr) - (nu - tr) > np.finfo(float).eps) * (v - tr) / (nu - tr)
+    sink = (r["R_ss"] / np.maximum(r["h_sat"], np.finfo(float).eps))[:, None] * wgt
+    assert np.allclose(d[0].reshape(w.ncol, -1), d1[0].reshape(w.ncol, -1) - sink, rtol=0, atol=1e-20)
+    assert np.allclose(d[3], d1[3] - r["R_ss"], rtol=0, atol=1e-22)
+    dz = ((w.z_hi - w.z_lo) / w.nlayers)
+    dv = d[0].reshape(w.ncol, -1)
+    # the layer terms reach 0.1 in supersaturated cells (S_s = 1e-3) and
+    # cancel to ~1e-6: the bound scales with them
+    bound = 1e-14 * np.abs(dv).max(axis=1) * dz * dv.shape[1]
+    assert np.all(np.abs(np.sum(dv, axis=1) * dz - d[3]) <= bound)
+    assert np.array_equal(r0["R_ss"], np.zeros(w.ncol))
