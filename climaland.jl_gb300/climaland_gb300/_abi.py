@@ -52,6 +52,8 @@ CLM_BC_PRECIP_RUNOFF = 4
 CLM_RUNOFF_NONE = 0
 CLM_RUNOFF_SURFACE = 1
 CLM_RUNOFF_TOPMODEL = 2
+CLM_CM_VAN_GENUCHTEN = 0
+CLM_CM_BROOKS_COREY = 1
 
 CLM_P_NU = 0
 CLM_P_K_SAT = 1
@@ -59,6 +61,8 @@ CLM_P_S_S = 2
 CLM_P_THETA_R = 3
 CLM_P_VG_ALPHA = 4
 CLM_P_VG_N = 5
+CLM_P_BC_PSI_B = 4
+CLM_P_BC_C = 5
 CLM_NPARAM_RICHARDS = 6
 CLM_P_KAPPA_DRY = 6
 CLM_P_KAPPA_SAT_FROZEN = 7
@@ -129,7 +133,7 @@ class ClmConfig(ctypes.Structure):
         ("cols_per_cta", ctypes.c_int32),
         ("schedule", ctypes.c_int32),
         ("graph", ctypes.c_int32),
-        ("pad1", ctypes.c_int32),
+        ("hydrology_cm", ctypes.c_int32),
         ("column_offset", ctypes.c_int64),
         ("host_chunks", ctypes.c_int32),
         ("runoff", ctypes.c_int32),
@@ -200,7 +204,7 @@ def config_to_dict(c: ClmConfig) -> dict:
         v = getattr(c, name)
         if name == "earth":
             v = {k: getattr(v, k) for k, _ in ClmEarthParams._fields_}
-        elif name in ("reserved", "pad1"):
+        elif name == "reserved":
             continue
         out[name] = v
     return out

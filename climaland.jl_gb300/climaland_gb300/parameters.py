@@ -64,9 +64,32 @@ class vanGenuchten:
 
 
 @dataclass
+class BrooksCorey:
+    """Brooks-Corey closure (retention_models.jl:47-67): c, psi_b (m, < 0)
+    and the critical saturation S_c = (1 + 1/c)^(-c). Its rows go where the
+    van Genuchten alpha and n go (CLM_P_BC_PSI_B, CLM_P_BC_C) with
+    cfg.hydrology_cm = CLM_CM_BROOKS_COREY."""
+
+    c: np.ndarray
+    psib: np.ndarray
+
+    @property
+    def S_c(self):
+        c = np.asarray(self.c, dtype=np.float64)
+        return (1.0 + 1.0 / c) ** (-c)
+
+
+def closure_rows(hcm):
+    """(row 4, row 5, cfg.hydrology_cm) for a closure object."""
+    if isinstance(hcm, BrooksCorey):
+        return hcm.psib, hcm.c, A.CLM_CM_BROOKS_COREY
+    return hcm.alpha, hcm.n, A.CLM_CM_VAN_GENUCHTEN
+
+
+@dataclass
 class RichardsParameters:
     nu: np.ndarray
-    hydrology_cm: vanGenuchten
+    hydrology_cm: vanGenuchten | BrooksCorey
     K_sat: np.ndarray
     S_s: np.ndarray
     theta_r: np.ndarray
@@ -77,8 +100,7 @@ class RichardsParameters:
         p[A.CLM_P_K_SAT] = self.K_sat
         p[A.CLM_P_S_S] = self.S_s
         p[A.CLM_P_THETA_R] = self.theta_r
-        p[A.CLM_P_VG_ALPHA] = self.hydrology_cm.alpha
-        p[A.CLM_P_VG_N] = self.hydrology_cm.n
+        p[A.CLM_P_VG_ALPHA], p[A.CLM_P_VG_N], _ = closure_rows(self.hydrology_cm)
         return p
 
 
@@ -112,7 +134,7 @@ class EnergyHydrologyParameters:
     nu_ss_om: np.ndarray
     nu_ss_quartz: np.ndarray
     nu_ss_gravel: np.ndarray
-    hydrology_cm: vanGenuchten
+    hydrology_cm: vanGenuchten | BrooksCorey
     K_sat: np.ndarray
     S_s: np.ndarray
     theta_r: np.ndarray
@@ -151,8 +173,7 @@ class EnergyHydrologyParameters:
         p[A.CLM_P_K_SAT] = self.K_sat
         p[A.CLM_P_S_S] = self.S_s
         p[A.CLM_P_THETA_R] = self.theta_r
-        p[A.CLM_P_VG_ALPHA] = self.hydrology_cm.alpha
-        p[A.CLM_P_VG_N] = self.hydrology_cm.n
+        p[A.CLM_P_VG_ALPHA], p[A.CLM_P_VG_N], _ = closure_rows(self.hydrology_cm)
         p[A.CLM_P_KAPPA_DRY] = self.kappa_dry
         p[A.CLM_P_KAPPA_SAT_FROZEN] = self.kappa_sat_frozen
         p[A.CLM_P_KAPPA_SAT_UNFROZEN] = self.kappa_sat_unfrozen

@@ -174,6 +174,7 @@ class RichardsModel:
         cfg = A.default_config()
         cfg.model = A.CLM_MODEL_RICHARDS
         cfg.phase_change = 0
+        cfg.hydrology_cm = PR.closure_rows(self.parameters.hydrology_cm)[2]
         top, bot = self.boundary_conditions["top"], self.boundary_conditions["bottom"]
         cfg.bc_top_water = top.kind
         cfg.bc_bottom_water = bot.kind
@@ -220,6 +221,7 @@ class EnergyHydrology:
         cfg = A.default_config()
         cfg.model = A.CLM_MODEL_ENERGY_HYDROLOGY
         cfg.phase_change = int(any(isinstance(s, PhaseChange) for s in self.sources))
+        cfg.hydrology_cm = PR.closure_rows(self.parameters.hydrology_cm)[2]
         for k, v in self.earth.items():
             setattr(cfg.earth, k, v)
         self.parameters.apply_scalars(cfg)

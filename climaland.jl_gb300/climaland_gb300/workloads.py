@@ -134,19 +134,31 @@ def _frozen_equilibrium(theta_tot, T, hyd_c, earth):
     """theta_l = min(theta_star(T), theta_tot), theta_i from the remainder:
     the phase-change equilibrium of phase_change_source
     (soil_heat_parameterizations.jl:89-122) for a given liquid-equivalent
-    water content theta_tot."""
-    alpha, n, nu, theta_r = hyd_c["alpha"], hyd_c["n"], hyd_c["nu"], hyd_c["theta_r"]
-    m = 1.0 - 1.0 / n
+    water content theta_tot. hyd_c holds van Genuchten (alpha, n) or
+    Brooks-Corey (psib, c) per cell."""
+    nu, theta_r = hyd_c["nu"], hyd_c["theta_r"]
+    bc = "psib" in hyd_c
+    if bc:
+        psib, c = hyd_c["psib"], hyd_c["c"]
+    else:
+        alpha, n = hyd_c["alpha"], hyd_c["n"]
+        m = 1.0 - 1.0 / n
     rho_l, rho_i = earth["rho_l"], earth["rho_i"]
     LH_f0, grav, T_freeze = earth["LH_f0"], earth["grav"], earth["T_freeze"]
     sq = np.sqrt(np.finfo(np.float64).eps)
     tt = np.minimum(theta_tot, nu)
     S = (np.maximum(tt, theta_r + sq) - theta_r) / (np.maximum(nu, theta_r + sq) - theta_r)
-    psi_w0 = -(((S ** (-1.0 / m) - 1.0) * alpha ** (-n)) ** (1.0 / n))
+    if bc:
+        psi_w0 = psib * S ** (-1.0 / c)
+    else:
+        psi_w0 = -(((S ** (-1.0 / m) - 1.0) * alpha ** (-n)) ** (1.0 / n))
     Tf = np.maximum(T_freeze * np.exp(grav * psi_w0 / LH_f0), 1.0)
     H = (Tf - T > np.finfo(np.float64).eps).astype(np.float64)
     psi_T = LH_f0 / grav * np.log(T / Tf) * H
-    S_star = (1.0 + (alpha * np.abs(psi_w0 + psi_T)) ** n) ** (-m)
+    if bc:
+        S_star = ((psi_w0 + psi_T) / psib) ** (-c)
+    else:
+        S_star = (1.0 + (alpha * np.abs(psi_w0 + psi_T)) ** n) ** (-m)
     theta_star = S_star * (nu - theta_r) + theta_r
     theta_l = np.minimum(theta_star, theta_tot)
     theta_i = np.maximum(theta_tot - theta_l, 0.0) * rho_l / rho_i
@@ -374,6 +386,40 @@ def richards_runoff(ncol: int = 1024, nlayers: int = 20, seed: int = 0,
         forcing={A.CLM_BC_TOP_WATER: ftw}, vartheta_l=v, theta_i=None,
         rho_e_int=None, intF_w=np.zeros(ncol), intF_e=None, t0=0.0, dt=900.0,
         nsteps=96)
+
+
+def brooks_corey(w: Workload, seed: int = 0) -> Workload:
+    """The workload with a per-column Brooks-Corey closure instead of van
+    Genuchten (cfg.hydrology_cm = CLM_CM_BROOKS_COREY): psi_b uniform in
+    [-0.9, -0.05] m and c in [0.2, 0.6], around the reference's values
+    (psi_b = -0.09, c = 0.228 in test/standalone/Soil/soil_parameterizations.jl:191;
+    psi_b = -0.6, c = 0.43 in docs/src/tutorials/standalone/Soil/freezing_front.jl:106-108).
+    EnergyHydrology states are re-partitioned into the Brooks-Corey freezing
+    equilibrium at the same temperature and total water."""
+    rng = np.random.Generator(np.random.PCG64(9000 + seed))
+    cfg = A.ClmConfig.from_buffer_copy(w.cfg)
+    cfg.hydrology_cm = A.CLM_CM_BROOKS_COREY
+    params = w.params.copy()
+    params[A.CLM_P_BC_PSI_B] = rng.uniform(-0.9, -0.05, w.ncol)
+    params[A.CLM_P_BC_C] = rng.uniform(0.2, 0.6, w.ncol)
+    v, ti, e = w.vartheta_l.copy(), None, None
+    if cfg.model == A.CLM_MODEL_ENERGY_HYDROLOGY:
+        earth = _earth_dict(cfg)
+        col = np.repeat(np.arange(w.ncol), w.nlayers)
+        rhoc_ds = params[A.CLM_P_RHOC_DS][col]
+        rhoc = rhoc_ds + w.vartheta_l * earth["cp_l"] * earth["rho_l"] + w.theta_i * earth["cp_i"] * earth["rho_i"]
+        T = earth["T_0"] + (w.rho_e_int + w.theta_i * earth["rho_i"] * earth["LH_f0"]) / rhoc
+        theta_tot = w.vartheta_l + w.theta_i * earth["rho_i"] / earth["rho_l"]
+        hyd_c = dict(psib=params[A.CLM_P_BC_PSI_B][col], c=params[A.CLM_P_BC_C][col],
+                     nu=params[A.CLM_P_NU][col], theta_r=params[A.CLM_P_THETA_R][col])
+        v, ti = _frozen_equilibrium(theta_tot, T, hyd_c, earth)
+        e = _rho_e(v, ti, T, rhoc_ds, earth)
+    return Workload(
+        name=f"{w.name}_bc", cfg=cfg, ncol=w.ncol, offsets=w.offsets, z_lo=w.z_lo,
+        z_hi=w.z_hi, params=params, forcing=w.forcing, vartheta_l=v, theta_i=ti,
+        rho_e_int=e, intF_w=w.intF_w.copy(),
+        intF_e=None if w.intF_e is None else w.intF_e.copy(), t0=w.t0, dt=w.dt,
+        nsteps=w.nsteps, meta=dict(w.meta))
 
 
 CONFIGS = {

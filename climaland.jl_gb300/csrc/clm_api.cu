@@ -23,7 +23,7 @@ namespace clm {
 cudaError_t launch_step(const StepArgs& A, int model, int precision, int wpc, int grid,
                         double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream);
 size_t step_smem_bytes(int model, int precision, int nmax, int wpc);
-cudaError_t step_grid(int model, int precision, int nmax, int wpc, int ntiles, int* grid);
+cudaError_t step_grid(int model, int precision, int cm, int nmax, int wpc, int ntiles, int* grid);
 size_t step_scratch_doubles(int model, int precision, int nmax, int wpc, int grid);
 // clm_layout.cu
 cudaError_t ref_to_internal(const Layout& L, const int32_t* ref_off, const double* src,
@@ -179,6 +179,7 @@ StepArgs step_args(const clm_handle* h) {
   A.phase_change = is_eh(h) ? h->cfg.phase_change : 0;
   A.newton_mode = h->cfg.newton_mode;
   A.runoff = h->cfg.runoff;
+  A.cm = h->cfg.hydrology_cm;
   A.max_iters = h->cfg.max_iters;
   A.tol = h->cfg.newton_tol;
   A.energy_scale = h->cfg.energy_norm_scale;
@@ -265,7 +266,7 @@ int build_layout(clm_handle* h, const std::vector<int>& nl) {
     return fail(h, CLM_ERR_ARG, "column depth " + std::to_string(h->nmax) +
                                     " needs more shared memory than the device offers");
   h->wpc = want;
-  CLM_CUDA(h, step_grid(h->cfg.model, h->cfg.precision, h->nmax, h->wpc, h->ntiles, &h->grid));
+  CLM_CUDA(h, step_grid(h->cfg.model, h->cfg.precision, h->cfg.hydrology_cm, h->nmax, h->wpc, h->ntiles, &h->grid));
   dfree(h->d_scratch);
   const size_t nsc = step_scratch_doubles(h->cfg.model, h->cfg.precision, h->nmax, h->wpc, h->grid);
   if (nsc) CLM_CUDA(h, cudaMalloc(&h->d_scratch, sizeof(double) * nsc));
@@ -512,6 +513,8 @@ int clm_create(const clm_config* cfg, clm_handle** out) {
   if (cfg->schedule != CLM_SCHED_STATIC && cfg->schedule != CLM_SCHED_DYNAMIC) return CLM_ERR_ARG;
   if (cfg->graph != 0 && cfg->graph != 1) return CLM_ERR_ARG;
   if (cfg->cols_per_cta < 0) return CLM_ERR_ARG;
+  if (cfg->hydrology_cm != CLM_CM_VAN_GENUCHTEN && cfg->hydrology_cm != CLM_CM_BROOKS_COREY)
+    return CLM_ERR_ARG;
   const int kinds[4] = {cfg->bc_top_water, cfg->bc_top_heat, cfg->bc_bottom_water, cfg->bc_bottom_heat};
   for (int i = 0; i < 4; ++i) {
     const int k = kinds[i];
@@ -650,7 +653,9 @@ int clm_set_params(clm_handle* h, const double* p, int32_t nparams) {
     const double nu = p[CLM_P_NU * ncol + c], Ks = p[CLM_P_K_SAT * ncol + c];
     const double Ss = p[CLM_P_S_S * ncol + c], tr = p[CLM_P_THETA_R * ncol + c];
     const double a = p[CLM_P_VG_ALPHA * ncol + c], n = p[CLM_P_VG_N * ncol + c];
-    if (!(nu > 0 && nu <= 1) || !(Ks >= 0) || !(Ss > 0) || !(tr >= 0 && tr < nu) || !(a > 0) || !(n > 1))
+    // van Genuchten alpha > 0, n > 1; Brooks-Corey psi_b < 0, c > 0
+    const bool closure_ok = h->cfg.hydrology_cm == CLM_CM_BROOKS_COREY ? (a < 0 && n > 0) : (a > 0 && n > 1);
+    if (!(nu > 0 && nu <= 1) || !(Ks >= 0) || !(Ss > 0) || !(tr >= 0 && tr < nu) || !closure_ok)
       return fail(h, CLM_ERR_ARG, "invalid hydraulic parameters in column " + std::to_string(c));
     if (topmodel) {
       const double fm = p[CLM_P_F_MAX * ncol + c], fo = p[CLM_P_F_OVER * ncol + c], rs = p[CLM_P_R_SB * ncol + c];
@@ -855,7 +860,7 @@ int clm_autotune(clm_handle* h, double t, double dt, int32_t probe_steps, clm_tu
   for (int w = 1; w <= 4; ++w) {
     if (step_smem_bytes(h->cfg.model, h->cfg.precision, h->nmax, w) > (size_t)dev_smem) break;
     int grid = 0;
-    CLM_CUDA(h, step_grid(h->cfg.model, h->cfg.precision, h->nmax, w, h->ntiles, &grid));
+    CLM_CUDA(h, step_grid(h->cfg.model, h->cfg.precision, h->cfg.hydrology_cm, h->nmax, w, h->ntiles, &grid));
     need = std::max(need, step_scratch_doubles(h->cfg.model, h->cfg.precision, h->nmax, w, grid));
     for (int sch : {CLM_SCHED_STATIC, CLM_SCHED_DYNAMIC}) {
       clm_tune_entry e{};

@@ -21,11 +21,8 @@
 
 namespace clm {
 
-template <int KIND>
-__global__ void closure_kernel(ClosureArgs C) {
-  __shared__ double tab[fm::TABLE_SIZE];
-  const Tables Tb = fm::stage_tables(tab);
-  __syncthreads();
+template <int KIND, class CM>
+__device__ void closure_column(const ClosureArgs& C, const Tables& Tb) {
   const StepArgs& A = C.A;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= A.L.stride) return;
@@ -41,7 +38,7 @@ __global__ void closure_kernel(ClosureArgs C) {
   const double* P = A.prm;
   const double nu = P[CLM_P_NU * st + s], K_sat = P[CLM_P_K_SAT * st + s];
   const double S_s = P[CLM_P_S_S * st + s], theta_r = P[CLM_P_THETA_R * st + s];
-  const VG g = make_vg(P[CLM_P_VG_ALPHA * st + s], P[CLM_P_VG_N * st + s]);
+  const CM g = make_cm<CM>(P[CLM_P_VG_ALPHA * st + s], P[CLM_P_VG_N * st + s]);
   const double dz = (A.z_hi[s] - A.z_lo[s]) / n;
   const double inv_dz = 1.0 / dz, half = 0.5 * dz;
   double kdry = 0, ksf = 0, ksu = 0, rcds = 0, nuom = 0, nuq = 0, nug = 0, lku = 0, lkf = 0;
@@ -219,6 +216,17 @@ __global__ void closure_kernel(ClosureArgs C) {
       }
     }
   }
+}
+
+template <int KIND>
+__global__ void closure_kernel(ClosureArgs C) {
+  __shared__ double tab[fm::TABLE_SIZE];
+  const Tables Tb = fm::stage_tables(tab);
+  __syncthreads();
+  if (C.A.cm == CLM_CM_BROOKS_COREY)
+    closure_column<KIND, BC>(C, Tb);
+  else
+    closure_column<KIND, VG>(C, Tb);
 }
 
 __device__ void thomas_ref(int n, const double* W, const double* f, double* x) {

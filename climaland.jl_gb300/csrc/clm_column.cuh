@@ -57,25 +57,26 @@ struct Col {
   CLM_HD T& operator[](int k) const { return p[(int64_t)k * s]; }
 };
 
+template <class CM>
 struct EHCol {
   double nu, K_sat, S_s, theta_r;
-  VG g;
+  CM g;  // hydrology closure (VG or BC)
   double kdry, ksf, ksu, rcds, nuom, nuq, nug, lku, lkf;
   double dz, inv_dz;
 };
 
 // kLogKappaHere: take log(kappa_sat_*) from the exp/log tables instead of
 // the handle's precomputed per-column array (for callers without a handle).
-template <bool kLogKappaHere = false>
-CLM_HD EHCol load_eh_col(const StepArgs& A, const Tables& Tb, int s, int n) {
+template <class CM, bool kLogKappaHere = false>
+CLM_HD EHCol<CM> load_eh_col(const StepArgs& A, const Tables& Tb, int s, int n) {
   const int st = A.L.stride;
   const double* P = A.prm;
-  EHCol c;
+  EHCol<CM> c;
   c.nu = P[CLM_P_NU * st + s];
   c.K_sat = P[CLM_P_K_SAT * st + s];
   c.S_s = P[CLM_P_S_S * st + s];
   c.theta_r = P[CLM_P_THETA_R * st + s];
-  c.g = make_vg(P[CLM_P_VG_ALPHA * st + s], P[CLM_P_VG_N * st + s]);
+  c.g = make_cm<CM>(P[CLM_P_VG_ALPHA * st + s], P[CLM_P_VG_N * st + s]);
   c.kdry = P[CLM_P_KAPPA_DRY * st + s];
   c.ksf = P[CLM_P_KAPPA_SAT_FROZEN * st + s];
   c.ksu = P[CLM_P_KAPPA_SAT_UNFROZEN * st + s];
@@ -97,7 +98,8 @@ CLM_HD EHCol load_eh_col(const StepArgs& A, const Tables& Tb, int s, int n) {
 
 // T and psi at the Newton iterate (update_implicit_aux!,
 // energy_hydrology.jl:427-445) and dpsi/dvartheta for the Jacobian (:503-512).
-CLM_HD void eh_iterate_point(const Tables& Tb, const Earth& E, const EHCol& c, double xv,
+template <class CM>
+CLM_HD void eh_iterate_point(const Tables& Tb, const Earth& E, const EHCol<CM>& c, double xv,
                              double xe, double ti, double& T, double& psi, double& D) {
   const double nu_eff = c.nu - ti;
   T = temperature(E, xe, ti, heat_capacity(E, fmin(nu_eff, xv), ti, c.rcds));
@@ -106,16 +108,19 @@ CLM_HD void eh_iterate_point(const Tables& Tb, const Earth& E, const EHCol& c, d
 
 // Mixed path: T and psi in double-float (FP64 results), dpsi in float; points
 // outside the double-float range fall back to the FP64 closure.
+template <class CM>
 struct EHMixed {
   ff::Tables FT;
-  ColFF cf;
+  typename ColFFOf<CM>::type cf;
   EarthFF Ef;
   F2 rcds, K_sat, omega_ln10, visc_gamma, visc_T_ref;
   KappaFF kf;
 };
 
-CLM_HD EHMixed make_eh_mixed(const Tables& Tb, const Earth& E, const EHScalars& sc, const EHCol& c) {
-  EHMixed m;
+template <class CM>
+CLM_HD EHMixed<CM> make_eh_mixed(const Tables& Tb, const Earth& E, const EHScalars& sc,
+                                 const EHCol<CM>& c) {
+  EHMixed<CM> m;
   m.FT = ff::Tables{Tb.ff};
   m.cf = make_col_ff(c.nu, c.theta_r, c.g);
   m.Ef = make_earth_ff(E);
@@ -128,7 +133,8 @@ CLM_HD EHMixed make_eh_mixed(const Tables& Tb, const Earth& E, const EHScalars& 
   return m;
 }
 
-CLM_HD void eh_iterate_point_mixed(const Tables& Tb, const EHCol& c, const EHMixed& M, double xv,
+template <class CM>
+CLM_HD void eh_iterate_point_mixed(const Tables& Tb, const EHCol<CM>& c, const EHMixed<CM>& M, double xv,
                                    double xe, double ti, double& T, double& psi, float& D) {
   const F2 ti_f = ff::from_double(ti);
   const F2 v = ff::from_double(xv);
@@ -142,8 +148,8 @@ CLM_HD void eh_iterate_point_mixed(const Tables& Tb, const EHCol& c, const EHMix
 }
 
 // T, psi and dpsi at the iterate on either path (dpsi in the Jacobian type).
-template <typename JT>
-CLM_HD void eh_point(const Tables& Tb, const Earth& E, const EHCol& c, const EHMixed& M, double xv,
+template <typename JT, class CM>
+CLM_HD void eh_point(const Tables& Tb, const Earth& E, const EHCol<CM>& c, const EHMixed<CM>& M, double xv,
                      double xe, double ti, double& T, double& psi, JT& D) {
   if constexpr (sizeof(JT) < sizeof(double)) {
     eh_iterate_point_mixed(Tb, c, M, xv, xe, ti, T, psi, D);
@@ -172,18 +178,18 @@ struct EHJac {
   Col<JT> cp, dp, d, ae;            // Thomas c', d' (then delta_v, d''), dpsi, face coef
 };
 
-template <typename JT, bool kLogKappaHere = false>
+template <typename JT, class CM, bool kLogKappaHere = false>
 CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int orig,
                       const EHBuffers& B, const EHJac<JT>& J, double t0, double dt, int nsteps,
                       double& Fw, double& Fe, uint32_t& flags, int& iters_done) {
   const Earth& E = A.E;
   const EHScalars& sc = A.sc;
-  const EHCol c = load_eh_col<kLogKappaHere>(A, Tb, s, n);
+  const EHCol<CM> c = load_eh_col<CM, kLogKappaHere>(A, Tb, s, n);
   const int st = A.L.stride;
   const double rdz = dt * c.inv_dz;
   const double half = 0.5 * c.dz;
   constexpr bool mixed = sizeof(JT) < sizeof(double);
-  EHMixed MX;
+  EHMixed<CM> MX;
   if constexpr (mixed) MX = make_eh_mixed(Tb, E, sc, c);
 
   for (int step = 0; step < nsteps; ++step) {
@@ -230,15 +236,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         // impedance_factor * viscosity_factor * hydraulic_conductivity, with
         // the sqrt(S) of the van Genuchten K inside the same exponential
         const double lnf = -sc.omega_ln10 * fi + sc.visc_gamma * (T - sc.visc_gamma_T_ref);
-        if (sK.S < 1.0) {
-          const double lS = fm::log(Tb, sK.S);
-          const double s1m = fm::exp(Tb, c.g.inv_m * lS);                  // S^(1/m)
-          const double tm = fm::exp(Tb, c.g.m * fm::log(Tb, 1.0 - s1m));   // (1 - S^(1/m))^m
-          const double f = 1.0 - tm;
-          K = c.K_sat * (f * f) * fm::exp(Tb, lnf + 0.5 * lS);
-        } else {
-          K = c.K_sat * fm::exp(Tb, lnf);
-        }
+        K = conductivity_scaled(Tb, c.g, c.K_sat, sK.S, lnf);
       }
       double Uv = Yv, Uti = Yti;
       if (A.phase_change) {
@@ -351,7 +349,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       double sum_fv = 0.0, sum_fe = 0.0;
       double Tc, psic;
       JT Dc;
-      eh_point<JT>(Tb, E, c, MX, B.xv[0], B.xe[0], B.gti[0], Tc, psic, Dc);
+      eh_point<JT, CM>(Tb, E, c, MX, B.xv[0], B.xe[0], B.gti[0], Tc, psic, Dc);
       double Kc = B.K[0];
       double relKc = rho_e_liq(E, Tc) * Kc;
       for (int k = 0; k < n; ++k) {
@@ -359,7 +357,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         double Tn = 0, psin = 0, Kn = 0, relKn = 0;
         JT Dn = 0, awr_up = 0;
         if (k < n - 1) {
-          eh_point<JT>(Tb, E, c, MX, B.xv[k + 1], B.xe[k + 1], B.gti[k + 1], Tn, psin, Dn);
+          eh_point<JT, CM>(Tb, E, c, MX, B.xv[k + 1], B.xe[k + 1], B.gti[k + 1], Tn, psin, Dn);
           Kn = B.K[k + 1];
           relKn = rho_e_liq(E, Tn) * Kn;
           aw_up = B.aw.p ? B.aw[k] : 0.5 * (Kc + Kn) * c.inv_dz;
@@ -604,7 +602,7 @@ struct RJac {
   Col<JT> dpl{nullptr, 0};
 };
 
-template <typename JT>
+template <typename JT, class CM>
 CLM_HD void richards_column(const StepArgs& A, const Tables& Tb, int s, int n, int orig,
                             const RBuffers& B, const RJac<JT>& J, double t0, double dt,
                             int nsteps, double& Fw, uint32_t& flags, int& iters_done) {
@@ -614,7 +612,7 @@ CLM_HD void richards_column(const StepArgs& A, const Tables& Tb, int s, int n, i
   const double K_sat = P[CLM_P_K_SAT * st + s];
   const double S_s = P[CLM_P_S_S * st + s];
   const double theta_r = P[CLM_P_THETA_R * st + s];
-  const VG g = make_vg(P[CLM_P_VG_ALPHA * st + s], P[CLM_P_VG_N * st + s]);
+  const CM g = make_cm<CM>(P[CLM_P_VG_ALPHA * st + s], P[CLM_P_VG_N * st + s]);
   const double dz = (A.z_hi[s] - A.z_lo[s]) / n;
   const double inv_dz = 1.0 / dz;
   const double half = 0.5 * dz;

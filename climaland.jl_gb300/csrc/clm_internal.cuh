@@ -52,6 +52,7 @@ struct StepArgs {
   int bc_tw, bc_th, bc_bw, bc_bh;
   int phase_change;
   int runoff;           // enum clm_runoff (CLM_BC_PRECIP_RUNOFF)
+  int cm = CLM_CM_VAN_GENUCHTEN;  // enum clm_hydrology_cm
   int newton_mode;
   int max_iters;
   double tol;

@@ -56,6 +56,7 @@ size_t noalloc_smem(int n) {
 
 // One warp per CTA; columns are read in the reference layout (cell =
 // c * n + k), which the column code accesses through stride-1 views.
+template <class CM>
 __global__ void __launch_bounds__(32, 1)
     eh_step_noalloc_kernel(StepArgs A, double* __restrict__ scratch, int ncol, int n, double t0,
                            double dt, int nsteps, uint32_t* __restrict__ flags_out) {
@@ -90,7 +91,7 @@ __global__ void __launch_bounds__(32, 1)
     double Fw = A.Fw[c], Fe = A.Fe[c];
     uint32_t fl = 0;
     int it = 0;
-    eh_column<double, true>(A, Tb, c, n, c, B, J, t0, dt, nsteps, Fw, Fe, fl, it);
+    eh_column<double, CM, true>(A, Tb, c, n, c, B, J, t0, dt, nsteps, Fw, Fe, fl, it);
     A.Fw[c] = Fw;
     A.Fe[c] = Fe;
     if (flags_out) flags_out[c] = fl;
@@ -108,16 +109,21 @@ int setup_device(int dev, DeviceSetup* out) {
       return CLM_ERR_CUDA;
     }
     const size_t smem = noalloc_smem(kNoAllocMaxLayers);
-    int nsm = 0, per_sm = 0;
-    if (cudaFuncSetAttribute(eh_step_noalloc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    int nsm = 0, per_vg = 0, per_bc = 0;
+    if (cudaFuncSetAttribute(eh_step_noalloc_kernel<VG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess ||
+        cudaFuncSetAttribute(eh_step_noalloc_kernel<BC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem) != cudaSuccess ||
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, eh_step_noalloc_kernel, 32, smem) !=
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_vg, eh_step_noalloc_kernel<VG>, 32, smem) !=
             cudaSuccess ||
-        per_sm < 1) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_bc, eh_step_noalloc_kernel<BC>, 32, smem) !=
+            cudaSuccess ||
+        per_vg < 1 || per_bc < 1) {
       cudaGetLastError();
       return CLM_ERR_CUDA;
     }
+    const int per_sm = per_vg < per_bc ? per_vg : per_bc;  // one grid for either closure
     s.grid = per_sm * nsm < kNoAllocSlots ? per_sm * nsm : kNoAllocSlots;
     s.scratch = static_cast<double*>(p);
   }
@@ -142,6 +148,8 @@ extern "C" int clm_step_eh_noalloc(const clm_config* cfg, int32_t ncol, int32_t 
   if (!z_lo || !z_hi || !params || !vartheta_l || !theta_i || !rho_e_int || !intF_w || !intF_e)
     return CLM_ERR_ARG;
   if (!(dt > 0) || nsteps < 0 || cfg->max_iters < 1) return CLM_ERR_ARG;
+  if (cfg->hydrology_cm != CLM_CM_VAN_GENUCHTEN && cfg->hydrology_cm != CLM_CM_BROOKS_COREY)
+    return CLM_ERR_ARG;
   const int kinds[4] = {cfg->bc_top_water, cfg->bc_top_heat, cfg->bc_bottom_water, cfg->bc_bottom_heat};
   for (int k : kinds)
     if (k < CLM_BC_FLUX || k > CLM_BC_FLUX_ADVECTIVE) return CLM_ERR_ARG;
@@ -186,10 +194,16 @@ extern "C" int clm_step_eh_noalloc(const clm_config* cfg, int32_t ncol, int32_t 
   A.energy_scale = cfg->energy_norm_scale;
   A.seed = cfg->forcing_seed;
   A.col0 = cfg->column_offset;
+  A.cm = cfg->hydrology_cm;
   const int ntiles = (ncol + kTile - 1) / kTile;
   const int grid = S.grid < ntiles ? S.grid : ntiles;
-  eh_step_noalloc_kernel<<<grid, 32, noalloc_smem(nlayers), static_cast<cudaStream_t>(cuda_stream)>>>(
-      A, S.scratch, ncol, nlayers, t, dt, nsteps, flags);
+  const cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+  if (A.cm == CLM_CM_BROOKS_COREY)
+    eh_step_noalloc_kernel<BC><<<grid, 32, noalloc_smem(nlayers), st>>>(A, S.scratch, ncol, nlayers, t,
+                                                                          dt, nsteps, flags);
+  else
+    eh_step_noalloc_kernel<VG><<<grid, 32, noalloc_smem(nlayers), st>>>(A, S.scratch, ncol, nlayers, t,
+                                                                          dt, nsteps, flags);
   if (cudaGetLastError() != cudaSuccess) return CLM_ERR_CUDA;
   return CLM_OK;
 }

@@ -86,6 +86,34 @@ CLM_HD VG make_vg(double alpha, double n) {
   return g;
 }
 
+// Brooks-Corey closure of one column (retention_models.jl:47-67).
+struct BC {
+  double psib, c;
+  double neg_inv_c;  // -1/c
+  double k_exp;      // 2/c + 3
+  double coef_d;     // -psi_b / c
+};
+
+CLM_HD BC make_bc(double psib, double c) {
+  BC g;
+  g.psib = psib;
+  g.c = c;
+  g.neg_inv_c = -1.0 / c;
+  g.k_exp = 2.0 / c + 3.0;
+  g.coef_d = -psib / c;
+  return g;
+}
+
+// The closure from parameter rows CLM_P_VG_ALPHA / CLM_P_VG_N
+// (CLM_P_BC_PSI_B / CLM_P_BC_C): the reference dispatches on the type of
+// hydrology_cm, the kernels on a template argument.
+template <class CM>
+CLM_HD CM make_cm(double row_a, double row_b);
+template <>
+CLM_HD VG make_cm<VG>(double alpha, double n) { return make_vg(alpha, n); }
+template <>
+CLM_HD BC make_cm<BC>(double psib, double c) { return make_bc(psib, c); }
+
 // effective_saturation (soil_hydrology_parameterizations.jl:45-50), also
 // returning the clipped vartheta and the clipped denominator.
 struct Sat {
@@ -123,6 +151,27 @@ CLM_HD void psi_dpsi(const Tables& T, const VG& g, double nu_eff, double varthet
   }
 }
 
+// Brooks-Corey pressure_head (:268-287) and dpsidvartheta (:219-230),
+// sharing S^(-1/c):
+//   psi  = psi_b S^(-1/c)                                  (S <= 1)
+//        = (vartheta_safe - nu_safe) / S_s + psi_b          (S > 1)
+//   dpsi = -psi_b / (c (nu_safe - theta_r)) S^(-1/c) / S   (S < 1)
+//        = 1 / S_s                                         (S >= 1)
+template <bool want_d>
+CLM_HD void psi_dpsi(const Tables& T, const BC& g, double nu_eff, double vartheta,
+                     double theta_r, double S_s, double& psi, double& dpsi) {
+  Sat s = saturation(nu_eff, vartheta, theta_r);
+  if (s.S < 1.0) {
+    const double u = fm::exp(T, g.neg_inv_c * fm::log(T, s.S));  // S^(-1/c)
+    psi = g.psib * u;
+    if (want_d) dpsi = g.coef_d * u / (s.S * (s.nu_safe - theta_r));
+  } else {
+    // S == 1: matric_potential(1) = psi_b
+    psi = (s.S <= 1.0) ? g.psib : (s.v_safe - s.nu_safe) / S_s + g.psib;
+    if (want_d) dpsi = 1.0 / S_s;
+  }
+}
+
 // hydraulic_conductivity (:161-173) of an effective saturation S:
 //   K = K_sat sqrt(S) (1 - (1 - S^(1/m))^m)^2 (S < 1), K_sat otherwise.
 CLM_HD double conductivity(const Tables& T, const VG& g, double K_sat, double S) {
@@ -131,6 +180,32 @@ CLM_HD double conductivity(const Tables& T, const VG& g, double K_sat, double S)
   const double t = fm::exp(T, g.m * fm::log(T, 1.0 - s1m));  // (1 - S^(1/m))^m
   const double f = 1.0 - t;
   return K_sat * (sqrt(S) * f * f);
+}
+
+// Brooks-Corey hydraulic_conductivity (:239-251): K_sat S^(2/c + 3) (S < 1).
+CLM_HD double conductivity(const Tables& T, const BC& g, double K_sat, double S) {
+  if (!(S < 1.0)) return K_sat;
+  return K_sat * fm::exp(T, g.k_exp * fm::log(T, S));
+}
+
+// K_sat exp(lnf) k_r(S): the hydraulic conductivity times the impedance and
+// viscosity factors exp(lnf) (EnergyHydrology update_aux!,
+// energy_hydrology.jl:776-790), with the S-power of k_r inside the same
+// exponential (sqrt(S) for van Genuchten, S^(2/c + 3) for Brooks-Corey).
+CLM_HD double conductivity_scaled(const Tables& T, const VG& g, double K_sat, double S,
+                                  double lnf) {
+  if (!(S < 1.0)) return K_sat * fm::exp(T, lnf);
+  const double lS = fm::log(T, S);
+  const double s1m = fm::exp(T, g.inv_m * lS);                 // S^(1/m)
+  const double tm = fm::exp(T, g.m * fm::log(T, 1.0 - s1m));   // (1 - S^(1/m))^m
+  const double f = 1.0 - tm;
+  return K_sat * (f * f) * fm::exp(T, lnf + 0.5 * lS);
+}
+
+CLM_HD double conductivity_scaled(const Tables& T, const BC& g, double K_sat, double S,
+                                  double lnf) {
+  if (!(S < 1.0)) return K_sat * fm::exp(T, lnf);
+  return K_sat * fm::exp(T, lnf + g.k_exp * fm::log(T, S));
 }
 
 // Richards point: K, psi (and dpsi) sharing log(S) (nu_eff = nu).
@@ -157,6 +232,25 @@ CLM_HD void richards_point(const Tables& T, const VG& g, double nu, double varth
   }
 }
 
+// Brooks-Corey Richards point: K, psi (and dpsi) sharing log(S).
+template <bool want_d>
+CLM_HD void richards_point(const Tables& T, const BC& g, double nu, double vartheta,
+                           double theta_r, double S_s, double K_sat, double& K, double& psi,
+                           double& dpsi) {
+  Sat s = saturation(nu, vartheta, theta_r);
+  if (s.S < 1.0) {
+    const double lS = fm::log(T, s.S);
+    const double u = fm::exp(T, g.neg_inv_c * lS);  // S^(-1/c)
+    psi = g.psib * u;
+    if (want_d) dpsi = g.coef_d * u / (s.S * (s.nu_safe - theta_r));
+    K = K_sat * fm::exp(T, g.k_exp * lS);
+  } else {
+    psi = (s.S <= 1.0) ? g.psib : (s.v_safe - s.nu_safe) / S_s + g.psib;
+    if (want_d) dpsi = 1.0 / S_s;
+    K = K_sat;
+  }
+}
+
 // matric_potential of effective_saturation(nu, theta) (soil_Tf_depressed,
 // phase_change_source). Returns S through *S_out.
 CLM_HD double matric_of(const Tables& T, const VG& g, double nu, double theta,
@@ -167,6 +261,25 @@ CLM_HD double matric_of(const Tables& T, const VG& g, double nu, double theta,
   const double w = u - 1.0;
   if (!(w > 0.0)) return -0.0;  // S >= 1 (theta <= nu keeps S <= 1)
   return -fm::exp(T, g.inv_n * fm::log(T, w)) * g.inv_alpha;
+}
+
+// Brooks-Corey: psi_b S^(-1/c) (matric_potential, :182-185).
+CLM_HD double matric_of(const Tables& T, const BC& g, double nu, double theta,
+                        double theta_r, double* S_out = nullptr) {
+  Sat s = saturation(nu, theta, theta_r);
+  if (S_out) *S_out = s.S;
+  return g.psib * fm::exp(T, g.neg_inv_c * fm::log(T, s.S));
+}
+
+// inverse_matric_potential (:72-77, :195-200) for psi <= 0:
+//   van Genuchten (1 + (alpha |psi|)^n)^(-m), Brooks-Corey (psi / psi_b)^(-c).
+CLM_HD double inverse_sat(const Tables& T, const VG& g, double psi) {
+  const double x = fm::exp(T, g.n * fm::log(T, g.alpha * fabs(psi)));  // (alpha|psi|)^n
+  return fm::exp(T, -g.m * fm::log(T, 1.0 + x));                     // (1 + x)^(-m)
+}
+
+CLM_HD double inverse_sat(const Tables& T, const BC& g, double psi) {
+  return fm::exp(T, -g.c * fm::log(T, psi / g.psib));
 }
 
 // volumetric_heat_capacity (soil_heat_parameterizations.jl:157-171)
@@ -228,9 +341,9 @@ CLM_HD double conductivity_heat(const Tables& T, const EHScalars& sc, double the
 //   psi_w0 + L_f/g log(T/Tf) = L_f/g log(T/T_freeze) =: psi_T,
 // independent of psi_w0, and Tf > T <=> psi_w0 > psi_T <=> S(theta_tot) > S_T
 // with S_T = inverse_matric_potential(psi_T) (the matric potential increases
-// with S). So theta_star = min(S(theta_tot), S_T) (nu - theta_r) + theta_r:
-// one log and the two powers of inverse_matric_potential, no matric_potential
-// and no Tf. The Tf >= 1 K clamp acts only where psi_w0 < -L_f/g
+// with S, for either closure). So theta_star = min(S(theta_tot), S_T) (nu -
+// theta_r) + theta_r: one log and inverse_matric_potential, no
+// matric_potential and no Tf. The Tf >= 1 K clamp acts only where psi_w0 < -L_f/g
 // log(T_freeze), where S(theta_tot) < S_T for every T > 1 K, so the min keeps
 // S(theta_tot) as the clamped reference does; both branches agree at
 // S(theta_tot) = S_T. It avoids the reference's cancellation of psi_w0
@@ -238,8 +351,8 @@ CLM_HD double conductivity_heat(const Tables& T, const EHScalars& sc, double the
 // trajectory switches a discontinuous closure (the Kersten number at
 // theta_i = eps) follow that rounding, so the plain path keeps the
 // reference's sequence.
-template <bool kRefForm = true>
-CLM_HD double phase_change(const Tables& T, const Earth& E, const VG& g, double nu,
+template <bool kRefForm = true, class CM>
+CLM_HD double phase_change(const Tables& T, const Earth& E, const CM& g, double nu,
                            double theta_r, double theta_l, double theta_i, double Tk,
                            double rhoc, double kappa, double dz, uint32_t& flags) {
   if (!kRefForm) {
@@ -247,9 +360,7 @@ CLM_HD double phase_change(const Tables& T, const Earth& E, const VG& g, double 
     double S = saturation(nu, theta_tot, theta_r).S;
     if (Tk < E.T_freeze) {
       const double psi_T = E.LH_f0_over_grav * fm::log(T, Tk * E.inv_T_freeze);
-      const double x = fm::exp(T, g.n * fm::log(T, g.alpha * fabs(psi_T)));  // (alpha|psi|)^n
-      const double S_T = fm::exp(T, -g.m * fm::log(T, 1.0 + x));             // (1 + x)^(-m)
-      S = fmin(S, S_T);
+      S = fmin(S, inverse_sat(T, g, psi_T));
     }
     const double theta_star = S * (nu - theta_r) + theta_r;
     return (theta_l - theta_star) * kappa / (3.0 * rhoc * (dz * dz));
@@ -266,9 +377,7 @@ CLM_HD double phase_change(const Tables& T, const Earth& E, const VG& g, double 
     if (Tf - Tk > kEps) {  // heaviside(Tf - T)
       const double psi = psi_w0 + E.LH_f0_over_grav * fm::log(T, Tk / Tf);
       if (psi > 0.0) flags |= CLM_COL_PSI_POSITIVE;
-      const double x = fm::exp(T, g.n * fm::log(T, g.alpha * fabs(psi)));  // (alpha|psi|)^n
-      const double Sst = fm::exp(T, -g.m * fm::log(T, 1.0 + x));         // (1 + x)^(-m)
-      theta_star = Sst * (nu - theta_r) + theta_r;
+      theta_star = inverse_sat(T, g, psi) * (nu - theta_r) + theta_r;
     } else {
       if (psi_w0 > 0.0) flags |= CLM_COL_PSI_POSITIVE;
       theta_star = S * (nu - theta_r) + theta_r;

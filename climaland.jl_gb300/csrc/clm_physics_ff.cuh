@@ -77,6 +77,50 @@ CLM_HD bool psi_dpsi_ff(const ff::Tables& T, const ColFF& c, F2 nu_eff, F2 v, do
   return true;
 }
 
+// Brooks-Corey constants of the mixed-path closures.
+struct ColFFBC {
+  F2 nu, theta_r, neg_inv_c, k_exp, psib;
+  float coef_d;  // -psi_b / c for the FP32 Jacobian
+};
+
+CLM_HD ColFFBC make_col_ff(double nu, double theta_r, const BC& g) {
+  ColFFBC c;
+  c.nu = ff::from_double(nu);
+  c.theta_r = ff::from_double(theta_r);
+  c.neg_inv_c = ff::from_double(g.neg_inv_c);
+  c.k_exp = ff::from_double(g.k_exp);
+  c.psib = ff::from_double(g.psib);
+  c.coef_d = (float)g.coef_d;
+  return c;
+}
+
+// Per-column closure constants of the mixed path for closure CM.
+template <class CM>
+struct ColFFOf;
+template <>
+struct ColFFOf<VG> { using type = ColFF; };
+template <>
+struct ColFFOf<BC> { using type = ColFFBC; };
+
+// Brooks-Corey pressure_head (S < 1) and dpsidvartheta (:219-230, :268-287):
+//   psi = psi_b u, dpsi = -psi_b u / (c S (nu_safe - theta_r)), u = S^(-1/c).
+CLM_HD bool psi_dpsi_ff(const ff::Tables& T, const ColFFBC& c, F2 nu_eff, F2 v, double& psi,
+                        float& dpsi) {
+  using namespace ff;
+  const F2 guard = add_f(c.theta_r, 1.4901161193847656e-08f);  // theta_r + sqrt(eps)
+  const F2 vs = ff_max(v, guard);
+  const F2 ns = ff_max(nu_eff, guard);
+  const F2 den = sub(ns, c.theta_r);
+  const F2 S = div(sub(vs, c.theta_r), den);
+  if (!(S.hi < 1.0f) || !(S.hi > 1e-30f)) return false;
+  const F2 L = log(T, S);
+  const F2 a = mul(L, c.neg_inv_c);  // log u
+  if (!(a.hi <= kExpMax)) return false;
+  psi = to_double(mul(exp(T, a), c.psib));
+  dpsi = c.coef_d * ff::exp_approx(a.hi - L.hi) / den.hi;
+  return true;
+}
+
 // temperature_from_ρe_int with volumetric_heat_capacity
 // (soil_heat_parameterizations.jl:157-192) at theta_l = tl.
 CLM_HD double temperature_ff(const EarthFF& E, F2 rho_e, F2 ti, F2 tl, F2 rhoc_ds) {
@@ -89,10 +133,13 @@ CLM_HD double temperature_ff(const EarthFF& E, F2 rho_e, F2 ti, F2 tl, F2 rhoc_d
 // impedance_factor * viscosity_factor * hydraulic_conductivity
 // (:161-173, :302-323): K_sat (1 - (1 - S^(1/m))^m)^2 exp(lnf + log(S)/2)
 // with lnf = -Omega ln10 f_i + gamma (T - gamma_T_ref).
+//
+// Saturation is tested on the pair (S = 1 - 2^-26 rounds its high word to
+// 1.0f; k_r is far from 1 there).
 CLM_HD bool conductivity_ff(const ff::Tables& T, const ColFF& c, F2 K_sat, F2 S, F2 lnf,
                             double& K) {
   using namespace ff;
-  if (!(S.hi < 1.0f)) {
+  if (!ff_lt(S, make(1.0f))) {
     if (!(lnf.hi >= kExpMin && lnf.hi <= kExpMax)) return false;
     K = to_double(mul(K_sat, exp(T, lnf)));
     return true;
@@ -108,6 +155,22 @@ CLM_HD bool conductivity_ff(const ff::Tables& T, const ColFF& c, F2 K_sat, F2 S,
   const F2 e = add(lnf, mul_f(L, 0.5f));
   if (!(e.hi >= kExpMin && e.hi <= kExpMax)) return false;
   K = to_double(mul(mul(K_sat, mul(f, f)), exp(T, e)));
+  return true;
+}
+
+// Brooks-Corey (:239-251): K_sat exp(lnf + (2/c + 3) log(S)).
+CLM_HD bool conductivity_ff(const ff::Tables& T, const ColFFBC& c, F2 K_sat, F2 S, F2 lnf,
+                            double& K) {
+  using namespace ff;
+  if (!ff_lt(S, make(1.0f))) {
+    if (!(lnf.hi >= kExpMin && lnf.hi <= kExpMax)) return false;
+    K = to_double(mul(K_sat, exp(T, lnf)));
+    return true;
+  }
+  if (!(S.hi > 1e-30f)) return false;
+  const F2 e = add(lnf, mul(log(T, S), c.k_exp));
+  if (!(e.hi >= kExpMin && e.hi <= kExpMax)) return false;
+  K = to_double(mul(K_sat, exp(T, e)));
   return true;
 }
 

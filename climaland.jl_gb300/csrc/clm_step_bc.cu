@@ -1,0 +1,16 @@
+// Brooks-Corey instantiations of the step kernels (clm_step_kernels.cuh),
+// in their own translation unit so that they compile in parallel with the
+// van Genuchten ones.
+
+#include "clm_step_kernels.cuh"
+
+namespace clm {
+
+void* step_fn_bc(int model, int precision) { return step_fn_t<BC>(model, precision); }
+
+void launch_step_bc(const StepArgs& A, int model, int precision, int grid, dim3 block, size_t smem,
+                    double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream) {
+  launch_step_t<BC>(A, model, precision, grid, block, smem, scratch, clk, nsteps, stream);
+}
+
+}  // namespace clm

@@ -1,0 +1,182 @@
+// Step kernels: persistent warps over 32-column tiles, one thread per
+// column, running the column code of clm_column.cuh.
+//
+// Shared memory per CTA: the exp/log tables (2 KB; the mixed EnergyHydrology
+// kernel also 0.5 KB of double-float pairs), then per warp the Newton
+// iterate, the energy residual and the Jacobian/Thomas arrays of its tile. The frozen aux arrays (K, kappa, 1/rho c) of EnergyHydrology live in
+// a per-warp-slot global scratch area (`scratch`, sized by the launch
+// grid, small enough to stay in L2). The grid is the number of CTAs that
+// fit on the device at once; each warp walks tiles w, w + W, w + 2W, ...
+// (tiles are sorted deepest first, so the walk is balanced), or, with the
+// dynamic order, claims the next unprocessed tile from an atomic counter
+// (deepest first: longest-processing-time-first list scheduling).
+
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "clm_column.cuh"
+
+namespace clm {
+
+template <typename JT>
+__host__ __device__ constexpr size_t eh_smem_per_layer() {
+  return 3 * sizeof(double) + 4 * sizeof(JT);  // xv, xe, fe | cp, dp, d, ae
+}
+
+template <typename JT>
+__host__ __device__ constexpr int richards_jac_arrays() {
+  return sizeof(JT) < sizeof(double) ? 3 : 2;  // cp, dp (| low words of dp)
+}
+
+template <typename JT>
+__host__ __device__ constexpr size_t richards_smem_per_layer() {
+  return sizeof(double) + richards_jac_arrays<JT>() * sizeof(JT);  // xv | cp, dp (, dp low)
+}
+
+// Per-warp scratch slots of nmax x 32 doubles: K, face kappa / dz, face
+// K / dz and 1 / rho c (FP64 path); K, face kappa / dz, face K / dz and the
+// float Jacobian arrays 1 / rho c, dt K_face / dz^2 and dt kappa_face / dz^2
+// packed into two slots (mixed).
+__host__ __device__ constexpr int eh_scratch_slots(bool mixed) { return mixed ? 5 : 4; }
+
+template <typename JT, class CM>
+__global__ void __launch_bounds__(128, 1)
+    eh_step_kernel(StepArgs A, double* __restrict__ scratch, StepClock clk, int nsteps) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* tab = reinterpret_cast<double*>(smem_raw);
+  constexpr bool kMixed = sizeof(JT) < sizeof(double);
+  constexpr int kTab = fm::stage_doubles<kMixed>();
+  const Tables Tb = fm::stage_tables<kMixed>(tab);
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int wpc = blockDim.x >> 5;
+  const int nmax = A.L.nmax;
+  const int64_t lay = (int64_t)nmax * kTile;
+  double* dw = tab + kTab + (int64_t)warp * 3 * lay;
+  JT* jw = reinterpret_cast<JT*>(tab + kTab + (int64_t)wpc * 3 * lay) + (int64_t)warp * 4 * lay;
+  const int gwarp = blockIdx.x * wpc + warp;
+  const int nwarps = gridDim.x * wpc;
+  double* sw = scratch + (int64_t)gwarp * eh_scratch_slots(kMixed) * lay;
+  EHBuffers B;
+  B.xv = Col<double>{dw + lane, kTile};
+  B.xe = Col<double>{dw + lay + lane, kTile};
+  B.fe = Col<double>{dw + 2 * lay + lane, kTile};
+  B.K = Col<double>{sw + lane, kTile};
+  B.kap = Col<double>{sw + lay + lane, kTile};
+  B.aw = Col<double>{sw + (kMixed ? 4 : 3) * lay + lane, kTile};
+  if constexpr (kMixed) {
+    float* fw = reinterpret_cast<float*>(sw + 2 * lay);
+    B.ircf = Col<float>{fw + lane, kTile};
+    B.awr = Col<float>{fw + lay + lane, kTile};
+    B.akr = Col<float>{fw + 2 * lay + lane, kTile};
+  } else {
+    B.irc = Col<double>{sw + 2 * lay + lane, kTile};
+  }
+  EHJac<JT> J;
+  J.cp = Col<JT>{jw + lane, kTile};
+  J.dp = Col<JT>{jw + lay + lane, kTile};
+  J.d = Col<JT>{jw + 2 * lay + lane, kTile};
+  J.ae = Col<JT>{jw + 3 * lay + lane, kTile};
+  const double t0 = clk.start(), dt = clk.step();
+  const bool dyn = A.tile_ctr != nullptr;
+  const int tend = A.tile_end < 0 ? A.L.ntiles : A.tile_end;
+  int tile = A.tile_begin + (dyn ? claim_tile(A.tile_ctr) : gwarp);
+  while (tile < tend) {
+    const int s = tile * kTile + lane;
+    const int n = A.L.col_n[s];
+    if (n > 0) {
+      const int64_t base = A.L.tile_off[tile] + lane;
+      B.gv = Col<double>{A.v + base, kTile};
+      B.gti = Col<double>{A.ti + base, kTile};
+      B.ge = Col<double>{A.e + base, kTile};
+      if (A.guess) {
+        B.guess_v = Col<const float>{A.guess + base, kTile};
+        B.guess_e = Col<const float>{A.guess + A.L.ncells_int + base, kTile};
+      }
+      double Fw = A.Fw[s], Fe = A.Fe[s];
+      uint32_t flags = 0;
+      int iters = 0;
+      eh_column<JT, CM>(A, Tb, s, n, A.L.perm[s], B, J, t0, dt, nsteps, Fw, Fe, flags, iters);
+      A.Fw[s] = Fw;
+      A.Fe[s] = Fe;
+      A.flags[s] = flags;
+      A.iters[s] = iters;
+    }
+    tile = dyn ? A.tile_begin + claim_tile(A.tile_ctr) : tile + nwarps;
+  }
+  if (dyn) release_tiles(A.tile_ctr, nwarps);
+}
+
+template <typename JT, class CM>
+__global__ void __launch_bounds__(128, 1)
+    richards_step_kernel(StepArgs A, StepClock clk, int nsteps) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* tab = reinterpret_cast<double*>(smem_raw);
+  const Tables Tb = fm::stage_tables(tab);
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int wpc = blockDim.x >> 5;
+  const int64_t lay = (int64_t)A.L.nmax * kTile;
+  double* dw = tab + fm::TABLE_SIZE + (int64_t)warp * lay;
+  constexpr int kJA = richards_jac_arrays<JT>();
+  JT* jw = reinterpret_cast<JT*>(tab + fm::TABLE_SIZE + (int64_t)wpc * lay) + (int64_t)warp * kJA * lay;
+  const int gwarp = blockIdx.x * wpc + warp;
+  const int nwarps = gridDim.x * wpc;
+  RBuffers B;
+  B.xv = Col<double>{dw + lane, kTile};
+  RJac<JT> J;
+  J.cp = Col<JT>{jw + lane, kTile};
+  J.dp = Col<JT>{jw + lay + lane, kTile};
+  if (kJA > 2) J.dpl = Col<JT>{jw + 2 * lay + lane, kTile};
+  const double t0 = clk.start(), dt = clk.step();
+  const bool dyn = A.tile_ctr != nullptr;
+  const int tend = A.tile_end < 0 ? A.L.ntiles : A.tile_end;
+  int tile = A.tile_begin + (dyn ? claim_tile(A.tile_ctr) : gwarp);
+  while (tile < tend) {
+    const int s = tile * kTile + lane;
+    const int n = A.L.col_n[s];
+    if (n > 0) {
+      B.gv = Col<double>{A.v + A.L.tile_off[tile] + lane, kTile};
+      double Fw = A.Fw[s];
+      uint32_t flags = 0;
+      int iters = 0;
+      richards_column<JT, CM>(A, Tb, s, n, A.L.perm[s], B, J, t0, dt, nsteps, Fw, flags, iters);
+      A.Fw[s] = Fw;
+      A.flags[s] = flags;
+      A.iters[s] = iters;
+    }
+    tile = dyn ? A.tile_begin + claim_tile(A.tile_ctr) : tile + nwarps;
+  }
+  if (dyn) release_tiles(A.tile_ctr, nwarps);
+}
+
+// The kernel of (model, precision) for closure CM, and its launch.
+template <class CM>
+void* step_fn_t(int model, int precision) {
+  if (model == CLM_MODEL_ENERGY_HYDROLOGY)
+    return precision == CLM_PREC_MIXED ? (void*)eh_step_kernel<float, CM>
+                                       : (void*)eh_step_kernel<double, CM>;
+  return precision == CLM_PREC_MIXED ? (void*)richards_step_kernel<float, CM>
+                                     : (void*)richards_step_kernel<double, CM>;
+}
+
+template <class CM>
+void launch_step_t(const StepArgs& A, int model, int precision, int grid, dim3 block, size_t smem,
+                   double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream) {
+  if (model == CLM_MODEL_ENERGY_HYDROLOGY) {
+    if (precision == CLM_PREC_MIXED)
+      eh_step_kernel<float, CM><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
+    else
+      eh_step_kernel<double, CM><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
+  } else {
+    if (precision == CLM_PREC_MIXED)
+      richards_step_kernel<float, CM><<<grid, block, smem, stream>>>(A, clk, nsteps);
+    else
+      richards_step_kernel<double, CM><<<grid, block, smem, stream>>>(A, clk, nsteps);
+  }
+}
+
+}  // namespace clm

@@ -108,6 +108,15 @@ enum clm_runoff {
                               saturated layers, z_wt = depth - h_sat        */
 };
 
+/* Hydrology closure (src/standalone/Soil/retention_models.jl): how rows
+ * 4 and 5 of the parameters are read. */
+enum clm_hydrology_cm {
+  CLM_CM_VAN_GENUCHTEN = 0, /* vanGenuchten{FT}(; alpha, n) (:354-368)          */
+  CLM_CM_BROOKS_COREY = 1   /* BrooksCorey{FT}(; c, psi_b) (:47-67):
+                               psi = psi_b S^(-1/c), K = K_sat S^(2/c + 3)
+                               (soil_hydrology_parameterizations.jl:182-289) */
+};
+
 enum clm_param {
   CLM_P_NU = 0,            /* porosity nu                                 */
   CLM_P_K_SAT = 1,         /* saturated hydraulic conductivity (m/s)      */
@@ -115,6 +124,8 @@ enum clm_param {
   CLM_P_THETA_R = 3,       /* residual water fraction                     */
   CLM_P_VG_ALPHA = 4,      /* van Genuchten alpha (1/m)                   */
   CLM_P_VG_N = 5,          /* van Genuchten n                             */
+  CLM_P_BC_PSI_B = 4,      /* Brooks-Corey psi_b (m, < 0)                 */
+  CLM_P_BC_C = 5,          /* Brooks-Corey c (> 0)                        */
   CLM_NPARAM_RICHARDS = 6,
   CLM_P_KAPPA_DRY = 6,          /* W/m/K                                   */
   CLM_P_KAPPA_SAT_FROZEN = 7,   /* W/m/K                                   */
@@ -202,7 +213,7 @@ typedef struct clm_config {
                              sequence as CUDA graphs captured on first use
                              (t and dt go through a device array, so one
                              graph serves every call with the same nsteps) */
-  int32_t pad1;
+  int32_t hydrology_cm;   /* enum clm_hydrology_cm                          */
   int64_t column_offset;  /* global index of this handle's column 0 when a
                              domain is split across handles or GPUs: the
                              rain-pulse hash uses the global column index  */

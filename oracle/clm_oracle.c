@@ -102,6 +102,83 @@ double clmo_hydraulic_conductivity(double m, double K_sat, double S) {
   return K * K_sat;
 }
 
+/* Brooks-Corey closure (retention_models.jl:47-67), :182-185 */
+double clmo_bc_matric_potential(double c, double psib, double S) {
+  return psib * pow(S, -1.0 / c);
+}
+
+/* :195-200 (the reference raises an error for psi > 0; here a flag) */
+double clmo_bc_inverse_matric_potential(double c, double psib, double psi,
+                                        int* psi_positive) {
+  if (psi > 0 && psi_positive) *psi_positive = 1;
+  return pow(psi / psib, -c);
+}
+
+/* :219-230 */
+double clmo_bc_dpsidvartheta(double c, double psib, double vartheta,
+                             double nu_eff, double theta_r, double S_s) {
+  double nu_safe = fmax(nu_eff, theta_r + SQRT_EPS);
+  double S = clmo_effective_saturation(nu_safe, vartheta, theta_r);
+  if (S < 1.0) return -psib / (c * (nu_safe - theta_r)) * pow(S, -(1.0 + 1.0 / c));
+  return 1.0 / S_s;
+}
+
+/* :239-251 */
+double clmo_bc_hydraulic_conductivity(double c, double K_sat, double S) {
+  double K = (S < 1.0) ? pow(S, 2.0 / c + 3.0) : 1.0;
+  return K * K_sat;
+}
+
+/* :268-287: for Brooks-Corey S = 1 is psi = psi_b, not 0 */
+double clmo_bc_pressure_head(double c, double psib, double theta_r,
+                             double vartheta_l, double nu_eff, double S_s) {
+  double S = clmo_effective_saturation(nu_eff, vartheta_l, theta_r);
+  double v_safe = fmax(vartheta_l, theta_r + SQRT_EPS);
+  double nu_safe = fmax(nu_eff, theta_r + SQRT_EPS);
+  if (S <= 1.0) return clmo_bc_matric_potential(c, psib, S);
+  return (v_safe - nu_safe) / S_s + psib;
+}
+
+/* The closure of one column: the reference dispatches on the type of
+ * hydrology_cm (vanGenuchten / BrooksCorey). */
+typedef struct {
+  int bc;             /* CLM_CM_BROOKS_COREY?   */
+  double alpha, n, m; /* vanGenuchten           */
+  double c, psib;     /* BrooksCorey            */
+} hcm_t;
+
+static hcm_t hcm_vg(double alpha, double n, double m) {
+  hcm_t h = {0, alpha, n, m, 0.0, 0.0};
+  return h;
+}
+
+static double hcm_matric_potential(const hcm_t* h, double S) {
+  return h->bc ? clmo_bc_matric_potential(h->c, h->psib, S)
+               : clmo_matric_potential(h->alpha, h->n, h->m, S);
+}
+
+static double hcm_inverse_matric_potential(const hcm_t* h, double psi, int* pos) {
+  return h->bc ? clmo_bc_inverse_matric_potential(h->c, h->psib, psi, pos)
+               : clmo_inverse_matric_potential(h->alpha, h->n, h->m, psi, pos);
+}
+
+static double hcm_pressure_head(const hcm_t* h, double theta_r, double v,
+                                double nu_eff, double S_s) {
+  return h->bc ? clmo_bc_pressure_head(h->c, h->psib, theta_r, v, nu_eff, S_s)
+               : clmo_pressure_head(h->alpha, h->n, h->m, theta_r, v, nu_eff, S_s);
+}
+
+static double hcm_dpsidvartheta(const hcm_t* h, double v, double nu_eff,
+                                double theta_r, double S_s) {
+  return h->bc ? clmo_bc_dpsidvartheta(h->c, h->psib, v, nu_eff, theta_r, S_s)
+               : clmo_dpsidvartheta(h->alpha, h->n, h->m, v, nu_eff, theta_r, S_s);
+}
+
+static double hcm_hydraulic_conductivity(const hcm_t* h, double K_sat, double S) {
+  return h->bc ? clmo_bc_hydraulic_conductivity(h->c, K_sat, S)
+               : clmo_hydraulic_conductivity(h->m, K_sat, S);
+}
+
 /* :302-305 */
 double clmo_impedance_factor(double f_i, double Omega) {
   return pow(10.0, -Omega * f_i);
@@ -122,14 +199,23 @@ double clmo_heaviside(double x, double a) {
  * ====================================================================== */
 
 /* :35-52 (argument order as the reference signature: rho_ice, rho_liq) */
+static double tf_depressed(double theta_l, double theta_i, double nu,
+                           double theta_r, const hcm_t* h, double rho_ice,
+                           double rho_liq, double T_freeze, double grav,
+                           double LH_f0) {
+  double theta_tot = fmin(rho_ice / rho_liq * theta_i + theta_l, nu);
+  double psi_w0 = hcm_matric_potential(
+      h, clmo_effective_saturation(nu, theta_tot, theta_r));
+  return fmax(T_freeze * exp(grav * psi_w0 / LH_f0), 1.0);
+}
+
 double clmo_soil_Tf_depressed(double theta_l, double theta_i, double nu,
                               double theta_r, double alpha, double n,
                               double m, double rho_ice, double rho_liq,
                               double T_freeze, double grav, double LH_f0) {
-  double theta_tot = fmin(rho_ice / rho_liq * theta_i + theta_l, nu);
-  double psi_w0 = clmo_matric_potential(
-      alpha, n, m, clmo_effective_saturation(nu, theta_tot, theta_r));
-  return fmax(T_freeze * exp(grav * psi_w0 / LH_f0), 1.0);
+  hcm_t h = hcm_vg(alpha, n, m);
+  return tf_depressed(theta_l, theta_i, nu, theta_r, &h, rho_ice, rho_liq,
+                      T_freeze, grav, LH_f0);
 }
 
 /* :60-62 */
@@ -138,24 +224,33 @@ double clmo_thermal_time(double rhoc, double dz, double kappa) {
 }
 
 /* :89-122 */
+static double phase_change_source(double theta_l, double theta_i, double T,
+                                  double tau, double nu, double theta_r,
+                                  const hcm_t* h, double rho_i, double rho_l,
+                                  double LH_f0, double T_freeze, double grav,
+                                  int* psi_positive) {
+  double Tf = tf_depressed(theta_l, theta_i, nu, theta_r, h, rho_i, rho_l,
+                           T_freeze, grav, LH_f0);
+  double psi_T = LH_f0 / grav * log(T / Tf) * clmo_heaviside(Tf - T, 0.0);
+  double theta_tot = fmin(rho_i / rho_l * theta_i + theta_l, nu);
+  double psi_w0 = hcm_matric_potential(
+      h, clmo_effective_saturation(nu, theta_tot, theta_r));
+  double theta_star =
+      hcm_inverse_matric_potential(h, psi_w0 + psi_T, psi_positive) *
+          (nu - theta_r) +
+      theta_r;
+  return (theta_l - theta_star) / tau;
+}
+
 double clmo_phase_change_source(double theta_l, double theta_i, double T,
                                 double tau, double nu, double theta_r,
                                 double alpha, double n, double m,
                                 double rho_i, double rho_l, double LH_f0,
                                 double T_freeze, double grav,
                                 int* psi_positive) {
-  double Tf = clmo_soil_Tf_depressed(theta_l, theta_i, nu, theta_r, alpha, n,
-                                     m, rho_i, rho_l, T_freeze, grav, LH_f0);
-  double psi_T = LH_f0 / grav * log(T / Tf) * clmo_heaviside(Tf - T, 0.0);
-  double theta_tot = fmin(rho_i / rho_l * theta_i + theta_l, nu);
-  double psi_w0 = clmo_matric_potential(
-      alpha, n, m, clmo_effective_saturation(nu, theta_tot, theta_r));
-  double theta_star =
-      clmo_inverse_matric_potential(alpha, n, m, psi_w0 + psi_T,
-                                    psi_positive) *
-          (nu - theta_r) +
-      theta_r;
-  return (theta_l - theta_star) / tau;
+  hcm_t h = hcm_vg(alpha, n, m);
+  return phase_change_source(theta_l, theta_i, T, tau, nu, theta_r, &h, rho_i,
+                             rho_l, LH_f0, T_freeze, grav, psi_positive);
 }
 
 /* :157-171 */
@@ -291,7 +386,8 @@ typedef struct {
   double dzf[MAXL];   /* dzf[k]: centre spacing between k-1, k  */
   double dz_top, dz_bottom; /* centre-to-boundary distances      */
   /* parameters */
-  double nu, K_sat, S_s, theta_r, alpha, vgn, vgm;
+  double nu, K_sat, S_s, theta_r;
+  hcm_t hcm; /* hydrology_cm */
   double kappa_dry, kappa_sat_frozen, kappa_sat_unfrozen, rhoc_ds;
   double nu_om, nu_quartz, nu_gravel;
   double f_max, f_over, R_sb; /* TOPMODEL (Runoff.jl:198-232)          */
@@ -350,9 +446,16 @@ static void col_init(col_t* C, const clmo_problem* P, int c) {
   C->K_sat = p[CLM_P_K_SAT * ncol + c];
   C->S_s = p[CLM_P_S_S * ncol + c];
   C->theta_r = p[CLM_P_THETA_R * ncol + c];
-  C->alpha = p[CLM_P_VG_ALPHA * ncol + c];
-  C->vgn = p[CLM_P_VG_N * ncol + c];
-  C->vgm = 1.0 - 1.0 / C->vgn; /* retention_models.jl:364-368 */
+  if (cfg->hydrology_cm == CLM_CM_BROOKS_COREY) {
+    memset(&C->hcm, 0, sizeof C->hcm);
+    C->hcm.bc = 1;
+    C->hcm.psib = p[CLM_P_BC_PSI_B * ncol + c];
+    C->hcm.c = p[CLM_P_BC_C * ncol + c];
+  } else {
+    double vgn = p[CLM_P_VG_N * ncol + c];
+    /* m = 1 - 1/n: retention_models.jl:364-368 */
+    C->hcm = hcm_vg(p[CLM_P_VG_ALPHA * ncol + c], vgn, 1.0 - 1.0 / vgn);
+  }
   C->depth = zhi - zlo;
   C->f_max = C->f_over = C->R_sb = 0.0;
   if (P->nparams >= CLM_NPARAM_MAX) {
@@ -401,11 +504,10 @@ static void richards_update_aux(const col_t* C, const state_t* Y,
                                  cache_t* p) {
   double W = 0.0;
   for (int k = 0; k < C->n; ++k) {
-    p->K[k] = clmo_hydraulic_conductivity(
-        C->vgm, C->K_sat,
+    p->K[k] = hcm_hydraulic_conductivity(
+        &C->hcm, C->K_sat,
         clmo_effective_saturation(C->nu, Y->v[k], C->theta_r));
-    p->psi[k] = clmo_pressure_head(C->alpha, C->vgn, C->vgm, C->theta_r,
-                                   Y->v[k], C->nu, C->S_s);
+    p->psi[k] = hcm_pressure_head(&C->hcm, C->theta_r, Y->v[k], C->nu, C->S_s);
     W += C->dzc[k] * Y->v[k]; /* rre.jl:502-511 */
   }
   p->total_water = W;
@@ -432,15 +534,13 @@ static void eh_update_aux(const col_t* C, const state_t* Y, cache_t* p) {
                                     cfg->ice_impedance_omega) *
               clmo_viscosity_factor(p->T[k], cfg->visc_gamma,
                                     cfg->visc_gamma_T_ref) *
-              clmo_hydraulic_conductivity(
-                  C->vgm, C->K_sat,
+              hcm_hydraulic_conductivity(
+                  &C->hcm, C->K_sat,
                   clmo_effective_saturation(C->nu, v, C->theta_r));
-    p->psi[k] = clmo_pressure_head(C->alpha, C->vgn, C->vgm, C->theta_r, v,
-                                   C->nu - ti, C->S_s);
+    p->psi[k] = hcm_pressure_head(&C->hcm, C->theta_r, v, C->nu - ti, C->S_s);
     /* :797-808 passes (_ρ_l, _ρ_i) into the (_ρ_ice, _ρ_liq) slots. */
-    p->Tf[k] = clmo_soil_Tf_depressed(tl, ti, C->nu, C->theta_r, C->alpha,
-                                      C->vgn, C->vgm, e->rho_l, e->rho_i,
-                                      e->T_freeze, e->grav, e->LH_f0);
+    p->Tf[k] = tf_depressed(tl, ti, C->nu, C->theta_r, &C->hcm, e->rho_l,
+                            e->rho_i, e->T_freeze, e->grav, e->LH_f0);
     /* :1282-1320 */
     W += C->dzc[k] * (v + ti * e->rho_i / e->rho_l);
     E += C->dzc[k] * Y->e[k];
@@ -459,8 +559,7 @@ static void eh_update_implicit_aux(const col_t* C, const state_t* Y,
         Y->e[k], ti,
         clmo_volumetric_heat_capacity(fmin(C->nu - ti, v), ti, C->rhoc_ds, e),
         e);
-    p->psi[k] = clmo_pressure_head(C->alpha, C->vgn, C->vgm, C->theta_r, v,
-                                   C->nu - ti, C->S_s);
+    p->psi[k] = hcm_pressure_head(&C->hcm, C->theta_r, v, C->nu - ti, C->S_s);
   }
 }
 
@@ -543,8 +642,7 @@ static void update_boundary_fluxes(const col_t* C, const state_t* Y,
       p->top_w = p->infiltration;
       break;
     case CLM_BC_STATE: {
-      double psi_bc = clmo_pressure_head(C->alpha, C->vgn, C->vgm, C->theta_r,
-                                         f_tw, nu_top, C->S_s);
+      double psi_bc = hcm_pressure_head(&C->hcm, C->theta_r, f_tw, nu_top, C->S_s);
       p->top_w = diffusive_flux(p->K[n - 1], psi_bc + C->dz_top, p->psi[n - 1],
                                 C->dz_top);
       break;
@@ -558,8 +656,7 @@ static void update_boundary_fluxes(const col_t* C, const state_t* Y,
       p->bot_w = -1.0 * p->K[0];
       break;
     case CLM_BC_STATE: {
-      double psi_bc = clmo_pressure_head(C->alpha, C->vgn, C->vgm, C->theta_r,
-                                         f_bw, nu_bot, C->S_s);
+      double psi_bc = hcm_pressure_head(&C->hcm, C->theta_r, f_bw, nu_bot, C->S_s);
       p->bot_w = diffusive_flux(p->K[0], p->psi[0] + C->dz_bottom, psi_bc,
                                 C->dz_bottom);
       break;
@@ -599,8 +696,8 @@ static void update_boundary_fluxes(const col_t* C, const state_t* Y,
   p->has_dflux = (!C->eh && cfg->bc_top_water == CLM_BC_STATE);
   if (p->has_dflux) {
     p->dfluxBCdY = p->K[n - 1] *
-                   clmo_dpsidvartheta(C->alpha, C->vgn, C->vgm, Y->v[n - 1],
-                                      C->nu, C->theta_r, C->S_s) /
+                   hcm_dpsidvartheta(&C->hcm, Y->v[n - 1], C->nu, C->theta_r,
+                                     C->S_s) /
                    C->dz_top;
   }
 }
@@ -643,9 +740,9 @@ static void exp_tendency(const col_t* C, const state_t* Y, cache_t* p,
           clmo_volumetric_heat_capacity(tl, ti, C->rhoc_ds, e), C->dzc[k],
           p->kappa[k]);
       int pp = 0;
-      double src = clmo_phase_change_source(
-          tl, ti, p->T[k], tau, C->nu, C->theta_r, C->alpha, C->vgn, C->vgm,
-          e->rho_i, e->rho_l, e->LH_f0, e->T_freeze, e->grav, &pp);
+      double src = phase_change_source(
+          tl, ti, p->T[k], tau, C->nu, C->theta_r, &C->hcm, e->rho_i, e->rho_l,
+          e->LH_f0, e->T_freeze, e->grav, &pp);
       if (pp) p->psi_positive = 1;
       dY->v[k] += -src;
       dY->ti[k] += (e->rho_l / e->rho_i) * src;
@@ -734,9 +831,9 @@ static void jacobian(const col_t* C, const state_t* Y, const cache_t* p,
   const clm_earth_params* e = &C->cfg->earth;
   double D[MAXL], cf[MAXL + 1];
   for (int k = 0; k < n; ++k)
-    D[k] = clmo_dpsidvartheta(C->alpha, C->vgn, C->vgm, Y->v[k],
-                              C->nu - (C->eh ? Y->ti[k] : 0.0), C->theta_r,
-                              C->S_s);
+    D[k] = hcm_dpsidvartheta(&C->hcm, Y->v[k],
+                             C->nu - (C->eh ? Y->ti[k] : 0.0), C->theta_r,
+                             C->S_s);
   cf[0] = cf[n] = 0.0;
   for (int k = 1; k < n; ++k) cf[k] = 0.5 * (p->K[k - 1] + p->K[k]);
   assemble_block(C, dtgamma, cf, D, J->vv[0], J->vv[1], J->vv[2]);
@@ -884,6 +981,9 @@ static int check_problem(const clmo_problem* P) {
   int need = P->cfg.model == CLM_MODEL_ENERGY_HYDROLOGY ? CLM_NPARAM_EH
                                                         : CLM_NPARAM_RICHARDS;
   if (P->nparams < need) return CLM_ERR_ARG;
+  if (P->cfg.hydrology_cm != CLM_CM_VAN_GENUCHTEN &&
+      P->cfg.hydrology_cm != CLM_CM_BROOKS_COREY)
+    return CLM_ERR_ARG;
   if (P->cfg.bc_top_water == CLM_BC_PRECIP_RUNOFF) {
     if (P->cfg.model != CLM_MODEL_RICHARDS) return CLM_ERR_ARG;
     if (P->cfg.runoff < CLM_RUNOFF_NONE || P->cfg.runoff > CLM_RUNOFF_TOPMODEL) return CLM_ERR_ARG;

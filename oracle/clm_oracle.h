@@ -45,6 +45,15 @@ double clmo_pressure_head(double alpha, double n, double m, double theta_r,
 double clmo_dpsidvartheta(double alpha, double n, double m, double vartheta,
                           double nu_eff, double theta_r, double S_s);
 double clmo_hydraulic_conductivity(double m, double K_sat, double S);
+/* Brooks-Corey closure (soil_hydrology_parameterizations.jl:182-289) */
+double clmo_bc_matric_potential(double c, double psib, double S);
+double clmo_bc_inverse_matric_potential(double c, double psib, double psi,
+                                        int* psi_positive);
+double clmo_bc_pressure_head(double c, double psib, double theta_r,
+                             double vartheta_l, double nu_eff, double S_s);
+double clmo_bc_dpsidvartheta(double c, double psib, double vartheta,
+                             double nu_eff, double theta_r, double S_s);
+double clmo_bc_hydraulic_conductivity(double c, double K_sat, double S);
 double clmo_impedance_factor(double f_i, double Omega);
 double clmo_viscosity_factor(double T, double gamma, double gamma_T_ref);
 double clmo_heaviside(double x, double a);

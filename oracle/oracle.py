@@ -70,6 +70,11 @@ def lib():
             "clmo_pressure_head": [_D] * 7,
             "clmo_dpsidvartheta": [_D] * 7,
             "clmo_hydraulic_conductivity": [_D] * 3,
+            "clmo_bc_matric_potential": [_D] * 3,
+            "clmo_bc_inverse_matric_potential": [_D] * 3 + [ip],
+            "clmo_bc_pressure_head": [_D] * 6,
+            "clmo_bc_dpsidvartheta": [_D] * 6,
+            "clmo_bc_hydraulic_conductivity": [_D] * 3,
             "clmo_impedance_factor": [_D] * 2,
             "clmo_viscosity_factor": [_D] * 3,
             "clmo_heaviside": [_D] * 2,

@@ -15,11 +15,13 @@ state arrays at every step (several seeds), and requires on every column
 i.e. the bar wherever the oracle reproduces itself; at most 5 % of the
 columns may need the widened bound (error above 1e-10).
 
-Budgets: water and energy close to 1e-12 relative on the GPU state, except
-where the reference itself does not close them (MoistureStateBC with a fixed
-number of Newton iterations: the integrated flux uses the boundary flux of
-the iterate before the last update); there the GPU's defect must equal the
-oracle's.
+Budgets, per column: water and energy close to 1e-12 relative on the GPU
+state, except where the reference itself does not close them
+(MoistureStateBC with a fixed number of Newton iterations: the integrated
+flux uses the boundary flux of the iterate before the last update; columns
+whose three Newton iterations do not converge); there the GPU's defect must
+equal the oracle's to 1e-8 of it, or to 1000 x the spread of the oracle's
+own defect under the same perturbations.
 """
 import numpy as np
 import pytest
@@ -79,14 +81,20 @@ def oracle_run(w, nsteps, oracle_cfg=None, perturb_seed=None, noise=None):
 
 
 def oracle_spread(w, nsteps, ref_state, oracle_cfg=None, nseeds=NSEEDS, noise=None):
-    """Per-column max difference between the oracle and its perturbed runs."""
+    """Per-column max difference between the oracle and its perturbed runs:
+    of each state field, and of the water and energy budget defects."""
     ref = _fields(w, ref_state)
     spread = [np.zeros(w.ncol) for _ in ref]
+    bref = budget_defects(w, w.copy_state(), ref_state, *O.Oracle(w).budgets(ref_state))
+    bspread = [np.zeros(w.ncol), np.zeros(w.ncol)]
     for seed in range(nseeds):
         st, _, _ = oracle_run(w, nsteps, oracle_cfg, perturb_seed=seed, noise=noise)
         for i, f in enumerate(_fields(w, st)):
             spread[i] = np.maximum(spread[i], _colmax(w, ref[i], f))
-    return spread
+        b = budget_defects(w, w.copy_state(), st, *O.Oracle(w).budgets(st))
+        for i in (0, 1):
+            bspread[i] = np.maximum(bspread[i], np.abs(b[i] - bref[i]))
+    return spread, bspread
 
 
 def gpu_run(w, nsteps, **dev_kw):
@@ -107,9 +115,10 @@ def check_parity(w, nsteps, oracle_cfg=None, spread=True, tol_state=TOL_STATE, n
     errs = [_colmax(w, r, g) for r, g in zip(ref, got)]
     names = ["vartheta_l", "theta_i", "rho_e_int_rel"][: len(errs)]
     if spread:
-        spr = oracle_spread(w, nsteps, so, oracle_cfg, noise=noise)
+        spr, bspr = oracle_spread(w, nsteps, so, oracle_cfg, noise=noise)
     else:
         spr = [np.zeros(w.ncol) for _ in errs]
+        bspr = [np.zeros(w.ncol), np.zeros(w.ncol)]
     total_spread = np.max(np.stack(spr), axis=0)
     sensitive = total_spread > SENSITIVE
     stats = {"columns": w.ncol, "sensitive": int(sensitive.sum())}
@@ -128,12 +137,14 @@ def check_parity(w, nsteps, oracle_cfg=None, spread=True, tol_state=TOL_STATE, n
     assert excused.mean() <= MAX_SENSITIVE, stats
     err_fw = float(np.max(np.abs(so[3] - sg[3])) / max(np.max(np.abs(so[3])), 1e-30))
     stats["intF_w_rel"] = err_fw
-    ew, ee = budget_errors(w, w.copy_state(), sg, Wg, Eg)
-    Wo, Eo = O.Oracle(w).budgets(so)
-    ewo, eeo = budget_errors(w, w.copy_state(), so, Wo, Eo)
-    stats.update(budget_water=ew, budget_energy=ee, oracle_budget_water=ewo, oracle_budget_energy=eeo)
-    assert ew < TOL_BUDGET or abs(ew - ewo) <= 1e-8 * max(ewo, 1e-300) + 1e-12, stats
-    assert ee < TOL_BUDGET or abs(ee - eeo) <= 1e-8 * max(eeo, 1e-300) + 1e-12, stats
+    bg = budget_defects(w, w.copy_state(), sg, Wg, Eg)
+    bo = budget_defects(w, w.copy_state(), so, *O.Oracle(w).budgets(so))
+    stats.update(budget_water=float(bg[0].max()), budget_energy=float(bg[1].max()),
+                 oracle_budget_water=float(bo[0].max()), oracle_budget_energy=float(bo[1].max()))
+    for nm, g, o, sp in zip(("water", "energy"), bg, bo, bspr):
+        allowed = np.maximum(1e-8 * o + 1e-12, SPREAD_FACTOR * sp)
+        bad = (g >= TOL_BUDGET) & (np.abs(g - o) > allowed)
+        assert not bad.any(), (nm, np.nonzero(bad)[0][:8], g[bad][:4], o[bad][:4], stats)
     stats["oracle_iters_max"] = int(io.max())
     stats["gpu_iters_max"] = int(ig.max())
     stats["iters_agree"] = float(np.mean(io == ig))
@@ -141,13 +152,15 @@ def check_parity(w, nsteps, oracle_cfg=None, spread=True, tol_state=TOL_STATE, n
     return stats
 
 
-def budget_errors(w, state0, state1, W1, E1):
+def budget_defects(w, state0, state1, W1, E1):
+    """Per column |(W1 - W0) - (intF_w1 - intF_w0)| / |W0| and the same for
+    energy (zeros for RichardsModel)."""
     o = O.Oracle(w)
     W0, E0 = o.budgets(state0)
-    ew = float(np.max(np.abs((W1 - W0) - (state1[3] - state0[3])) / np.abs(W0)))
-    ee = 0.0
+    ew = np.abs((W1 - W0) - (state1[3] - state0[3])) / np.abs(W0)
+    ee = np.zeros(w.ncol)
     if w.cfg.model == A.CLM_MODEL_ENERGY_HYDROLOGY:
-        ee = float(np.max(np.abs((E1 - E0) - (state1[4] - state0[4])) / np.abs(E0)))
+        ee = np.abs((E1 - E0) - (state1[4] - state0[4])) / np.abs(E0)
     return ew, ee
 
 

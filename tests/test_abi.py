@@ -94,3 +94,14 @@ def test_create_rejects_runoff_outside_richards(lib):
     cfg.bc_top_water = A.CLM_BC_FLUX
     cfg.bc_bottom_water = A.CLM_BC_PRECIP_RUNOFF
     assert lib.clm_create(ctypes.byref(cfg), ctypes.byref(h)) == A.CLM_ERR_ARG
+
+
+def test_create_rejects_unknown_hydrology_closure(lib):
+    h = ctypes.c_void_p()
+    cfg = A.default_config()
+    cfg.ncol = 10
+    cfg.nlayers = 5
+    cfg.hydrology_cm = 2
+    assert lib.clm_create(ctypes.byref(cfg), ctypes.byref(h)) == A.CLM_ERR_ARG
+    cfg.hydrology_cm = -1
+    assert lib.clm_create(ctypes.byref(cfg), ctypes.byref(h)) == A.CLM_ERR_ARG

@@ -32,6 +32,8 @@ WORKLOADS = {
     "eh": lambda: WL.energy_hydrology_c1(ncol=256),
     "uneven": lambda: WL.uneven_c2(ncol=256),
     "c4": lambda: WL.full_scale_c4(ncol=256),
+    "richards_bc": lambda: WL.brooks_corey(WL.richards_c0(ncol=256)),
+    "c4_bc": lambda: WL.brooks_corey(WL.full_scale_c4(ncol=256)),
 }
 
 

@@ -85,6 +85,30 @@ def test_mixed_precision_tolerance_mode():
     report("mixed_full_scale_tol", check_parity(w, 48, oracle_cfg=TOL_MODE, **TOL_MODE, **MIXED))
 
 
+# Brooks-Corey closure (cfg.hydrology_cm = CLM_CM_BROOKS_COREY): sandy columns
+# with |psi_b| ~ 0.05 m and K_sat ~ 1e-4 m/s are stiff enough that three
+# Newton iterations diverge (the reference's trajectory there is not
+# reproducible: those columns fall under the oracle-spread bound). The mixed
+# path runs on the EnergyHydrology configurations only, as for van Genuchten.
+BROOKS_COREY = {
+    "richards": (lambda: WL.brooks_corey(WL.richards_c0(ncol=1024)), 96, {}),
+    "energy_hydrology": (lambda: WL.brooks_corey(WL.energy_hydrology_c1().subset(1024)), 96, {}),
+    "uneven": (lambda: WL.brooks_corey(WL.uneven_c2().subset(1024)), 48, {}),
+    "full_scale": (lambda: WL.brooks_corey(WL.full_scale_c4(ncol=1024)), 48, {}),
+    "full_scale_tol": (lambda: WL.brooks_corey(WL.full_scale_c4(ncol=512)), 48,
+                       dict(oracle_cfg=TOL_MODE, **TOL_MODE)),
+    "mixed_energy_hydrology": (lambda: WL.brooks_corey(WL.energy_hydrology_c1().subset(1024)), 48, MIXED),
+    "mixed_full_scale": (lambda: WL.brooks_corey(WL.full_scale_c4(ncol=1024)), 48, MIXED),
+    "mixed_uneven": (lambda: WL.brooks_corey(WL.uneven_c2().subset(1024)), 48, MIXED),
+}
+
+
+@pytest.mark.parametrize("name", list(BROOKS_COREY))
+def test_brooks_corey(name):
+    make, nsteps, kw = BROOKS_COREY[name]
+    report(f"brooks_corey_{name}", check_parity(make(), nsteps, **kw))
+
+
 @pytest.mark.parametrize("kind", [A.CLM_RUNOFF_NONE, A.CLM_RUNOFF_SURFACE, A.CLM_RUNOFF_TOPMODEL])
 def test_richards_precipitation_runoff(kind):
     """RichardsAtmosDrivenFluxBC with each runoff model: hourly storms above
@@ -217,6 +241,11 @@ def test_nonfinite_state_flagged():
 def test_invalid_arguments_rejected():
     w = WL.richards_c0(ncol=32, nlayers=5)
     w.params[A.CLM_P_VG_N][3] = 0.9  # n must exceed 1
+    with pytest.raises(D.ClmError) as e:
+        D.SoilColumns(w)
+    assert e.value.code == A.CLM_ERR_ARG
+    w = WL.brooks_corey(WL.richards_c0(ncol=32, nlayers=5))
+    w.params[A.CLM_P_BC_PSI_B][3] = 0.1  # psi_b must be negative
     with pytest.raises(D.ClmError) as e:
         D.SoilColumns(w)
     assert e.value.code == A.CLM_ERR_ARG

@@ -142,6 +142,55 @@ def test_van_genuchten(L):
     assert flag.value == 1
 
 
+# --- :190-222 Brooks and Corey closures ------------------------------------
+
+def test_brooks_corey(L):
+    c, psib = 0.228, -0.09
+    hcm = PR.BrooksCorey(c=c, psib=psib)
+    assert hcm.S_c == (1 + 1 / 0.228) ** (-0.228)
+    S = [0.5, 1.0, 1.5]
+    th = [0.3, 0.4, 0.5]
+    theta_r, nu, K_sat, S_s = 0.2, 0.4, 2.9e-7, 1e-2
+    va = S[0] ** (-1 / c) * psib
+    psi = [L.clmo_bc_matric_potential(c, psib, s) for s in S[:2]]
+    flag = ctypes.c_int(0)
+    inv = [L.clmo_bc_inverse_matric_potential(c, psib, p, ctypes.byref(flag)) for p in psi]
+    assert approx(inv, S[:2]) and flag.value == 0
+    assert approx(psi, [va, psib])
+    # pressure head: saturated soil continues from psi_b, not from 0
+    ph = [L.clmo_bc_pressure_head(c, psib, theta_r, t, nu, S_s) for t in th]
+    assert approx(ph, psi + [0.1 / 1e-2 + psib])
+    dpsi = [L.clmo_bc_dpsidvartheta(c, psib, t, nu, theta_r, S_s) for t in th]
+    va = [-psib / (c * (nu - theta_r)) * s ** (-(1 + 1 / c)) for s in S]
+    assert approx(dpsi, [va[0], 1 / S_s, 1 / S_s])
+    k = [L.clmo_bc_hydraulic_conductivity(c, K_sat, s) for s in S]
+    assert approx(k, [S[0] ** (2 / c + 3) * K_sat, K_sat, K_sat])
+    # inverse_matric_potential raises for psi > 0 (:196): reported as a flag
+    L.clmo_bc_inverse_matric_potential(c, psib, 0.1, ctypes.byref(flag))
+    assert flag.value == 1
+
+
+def test_brooks_corey_columns_use_the_closure(L):
+    """A Brooks-Corey handle evaluates psi and K of every cell with the
+    Brooks-Corey functions (RichardsModel update_aux!, rre.jl:368-380), and
+    the oracle refuses an unknown closure."""
+    w = WL.brooks_corey(WL.richards_c0(ncol=16, nlayers=6))
+    aux = O.Oracle(w).update_cache(w.copy_state(), 0.0)
+    col = np.repeat(np.arange(w.ncol), w.nlayers)
+    P = w.params[:, col]
+    nu, K_sat, S_s, theta_r = P[A.CLM_P_NU], P[A.CLM_P_K_SAT], P[A.CLM_P_S_S], P[A.CLM_P_THETA_R]
+    psib, c = P[A.CLM_P_BC_PSI_B], P[A.CLM_P_BC_C]
+    v = w.vartheta_l
+    S = (np.maximum(v, theta_r + math.sqrt(EPS)) - theta_r) / (np.maximum(nu, theta_r + math.sqrt(EPS)) - theta_r)
+    assert np.all(S < 1)
+    assert approx(aux["psi"], psib * S ** (-1 / c))
+    assert approx(aux["K"], K_sat * S ** (2 / c + 3))
+    w.cfg.hydrology_cm = 2
+    o = O.Oracle(w)
+    rc, _, _ = o.step(w.copy_state(), 0.0, 1.0, 1)
+    assert rc == A.CLM_ERR_ARG
+
+
 # --- :283-495 freezing and thawing -----------------------------------------
 
 def _ft_case(L, earth, theta_l, theta_i, T):

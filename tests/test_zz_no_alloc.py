@@ -31,16 +31,17 @@ def torch_cuda():
     return torch
 
 
-def _workload():
+def _workload(brooks_corey=False):
     w = WL.energy_hydrology_c1(ncol=1000, nlayers=15, seed=7)
     w.params[A.CLM_P_K_SAT] = np.minimum(w.params[A.CLM_P_K_SAT], 1e-5)
-    return w
+    return WL.brooks_corey(w) if brooks_corey else w
 
 
-def test_noalloc_matches_handle_path_two_calls(torch_cuda):
+@pytest.mark.parametrize("brooks_corey", [False, True])
+def test_noalloc_matches_handle_path_two_calls(torch_cuda, brooks_corey):
     torch = torch_cuda
     lib = D.load_library()
-    w = _workload()
+    w = _workload(brooks_corey)
     nsteps = 6
     # reference: the handle API, two calls
     with D.SoilColumns(w) as g:
