@@ -26,6 +26,9 @@ const CLM_BC_FLUX = Int32(0)
 const CLM_BC_FREE_DRAINAGE = Int32(1)
 const CLM_BC_STATE = Int32(2)
 const CLM_BC_FLUX_ADVECTIVE = Int32(3)
+const CLM_BC_PRECIP_RUNOFF = Int32(4)
+const CLM_CM_VAN_GENUCHTEN = Int32(0)
+const CLM_CM_BROOKS_COREY = Int32(1)
 const CLM_F_NFIELDS = 8
 
 struct ClmEarthParams
@@ -64,7 +67,12 @@ mutable struct ClmConfig
     pad0::Int32
     forcing_seed::UInt64
     cols_per_cta::Int32
-    reserved::NTuple{7, Int32}
+    schedule::Int32
+    graph::Int32
+    hydrology_cm::Int32
+    column_offset::Int64
+    host_chunks::Int32
+    runoff::Int32
     ClmConfig() = new()
 end
 
@@ -115,6 +123,20 @@ set_geometry!(h::Handle, z_lo::Vector{Float64}, z_hi::Vector{Float64}, offsets::
     check(h, ccall((:clm_set_geometry, libclm), Cint,
         (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Int32}),
         h.ptr, z_lo, z_hi, offsets === nothing ? C_NULL : offsets))
+
+"""
+    closure_rows(hcm)
+
+Rows 5 and 6 of the parameter matrix and `cfg.hydrology_cm` for a
+`vanGenuchten` (α, n) or `BrooksCorey` (ψb, c) closure
+(src/standalone/Soil/retention_models.jl).
+"""
+function closure_rows(hcm)
+    if hasproperty(hcm, :ψb)
+        return hcm.ψb, hcm.c, CLM_CM_BROOKS_COREY
+    end
+    return hcm.α, hcm.n, CLM_CM_VAN_GENUCHTEN
+end
 
 "Per-column parameters as a (nparams × ncol) matrix, rows in `enum clm_param` order."
 set_params!(h::Handle, p::Matrix{Float64}) =

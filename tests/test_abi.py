@@ -105,3 +105,16 @@ def test_create_rejects_unknown_hydrology_closure(lib):
     assert lib.clm_create(ctypes.byref(cfg), ctypes.byref(h)) == A.CLM_ERR_ARG
     cfg.hydrology_cm = -1
     assert lib.clm_create(ctypes.byref(cfg), ctypes.byref(h)) == A.CLM_ERR_ARG
+
+
+def test_julia_binding_config_matches_the_header_layout():
+    # the Julia mirror of clm_config must list the ctypes fields in order
+    # with the same widths (ccall passes the struct by reference)
+    text = (REPO / "climaland.jl_gb300" / "julia" / "ClimaLandGB300.jl").read_text()
+    body = re.search(r"mutable struct ClmConfig\n(.*?)\n\s*ClmConfig\(\) = new\(\)", text, re.S).group(1)
+    fields = re.findall(r"^\s*([A-Za-z_0-9]+)::([A-Za-z0-9]+)", body, re.M)
+    jl = {"Int32": ctypes.c_int32, "Int64": ctypes.c_int64, "UInt64": ctypes.c_uint64,
+          "Float64": ctypes.c_double, "ClmEarthParams": A.ClmEarthParams}
+    assert [n for n, _ in fields] == [n for n, _ in A.ClmConfig._fields_]
+    for (n, t), (_, ct) in zip(fields, A.ClmConfig._fields_):
+        assert ctypes.sizeof(jl[t]) == ctypes.sizeof(ct), n
