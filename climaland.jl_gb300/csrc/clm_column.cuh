@@ -191,6 +191,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
   constexpr bool mixed = sizeof(JT) < sizeof(double);
   EHMixed<CM> MX;
   if constexpr (mixed) MX = make_eh_mixed(Tb, E, sc, c);
+  const bool tol = A.newton_mode == CLM_NEWTON_TOL;  // the increment norms are needed only then
 
   for (int step = 0; step < nsteps; ++step) {
     const double t = t0 + step * dt;
@@ -504,7 +505,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
           d_prev = dk;
           const double dvd = dvd0;
           B.xv[k] -= dvd;
-          state2 += dvd * dvd;
+          if (tol) state2 += dvd * dvd;
           dvm = dv0; Dm = D0; dv0 = dvp; D0 = Dp;
           dvd0 = dvdp;
           ae_dn = ae_up;
@@ -532,19 +533,19 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
           for (int k = 0; k < n; ++k) {
             const double d = (double)J.dp[k] - corr_e;
             B.xe[k] -= d;
-            state2 += (se * d) * (se * d);
+            if (tol) state2 += (se * d) * (se * d);
           }
         } else {
           for (int k = n - 1; k >= 0; --k) {
             const JT d = J.dp[k] - J.cp[k] * nxt;
             nxt = d;
             B.xe[k] -= (double)d;
-            state2 += (se * (double)d) * (se * (double)d);
+            if (tol) state2 += (se * (double)d) * (se * (double)d);
           }
         }
       }
       iters_done = it;
-      if (A.newton_mode == CLM_NEWTON_TOL) {
+      if (tol) {
         const double nrm = sqrt(flux2 + state2);
         // the guess test uses the state part only: the integrated-flux
         // increments do not depend on the starting point
@@ -621,6 +622,7 @@ CLM_HD void richards_column(const StepArgs& A, const Tables& Tb, int s, int n, i
   // MoistureStateBC at the top carries dfluxBCdY (rre.jl:137-146, 460-468):
   // the boundary fluxes are then refreshed with the implicit cache.
   const bool dflux = (A.bc_tw == CLM_BC_STATE);
+  const bool tol = A.newton_mode == CLM_NEWTON_TOL;  // the increment norm is needed only then
 
   for (int step = 0; step < nsteps; ++step) {
     const double t = t0 + step * dt;
@@ -750,7 +752,7 @@ CLM_HD void richards_column(const StepArgs& A, const Tables& Tb, int s, int n, i
         for (int k = 0; k < n; ++k) {
           const double d = ff::to_double(F2{J.dp[k], J.dpl[k]}) - corr;
           B.xv[k] -= d;
-          norm2 += d * d;
+          if (tol) norm2 += d * d;
         }
       } else {
         JT nxt = 0;
@@ -758,11 +760,11 @@ CLM_HD void richards_column(const StepArgs& A, const Tables& Tb, int s, int n, i
           const JT d = J.dp[k] - J.cp[k] * nxt;
           nxt = d;
           B.xv[k] -= (double)d;
-          norm2 += (double)d * (double)d;
+          if (tol) norm2 += (double)d * (double)d;
         }
       }
       iters_done = it;
-      if (A.newton_mode == CLM_NEWTON_TOL) {
+      if (tol) {
         const double nrm = sqrt(norm2);
         if (nrm > prev_norm && it > 2) flags |= CLM_COL_DIVERGED;
         prev_norm = nrm;

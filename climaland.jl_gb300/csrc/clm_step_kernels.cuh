@@ -3,9 +3,14 @@
 //
 // Shared memory per CTA: the exp/log tables (2 KB; the mixed EnergyHydrology
 // kernel also 0.5 KB of double-float pairs), then per warp the Newton
-// iterate, the energy residual and the Jacobian/Thomas arrays of its tile. The frozen aux arrays (K, kappa, 1/rho c) of EnergyHydrology live in
-// a per-warp-slot global scratch area (`scratch`, sized by the launch
-// grid, small enough to stay in L2). The grid is the number of CTAs that
+// iterate and the Thomas arrays of its tile. The arrays of EnergyHydrology
+// that are written once per sweep and read once in a later sweep (the frozen
+// aux K, kappa, 1/rho c, the face coefficients, the energy residual and the
+// energy-advection face coefficient) live in a per-warp-slot global scratch
+// area (`scratch`, sized by the launch grid, small enough to stay in L2):
+// the smaller shared footprint leaves room for more resident warps when
+// columns are deep (up to 30 layers: 8 instead of 5 warps per SM on the
+// mixed path). The grid is the number of CTAs that
 // fit on the device at once; each warp walks tiles w, w + W, w + 2W, ...
 // (tiles are sorted deepest first, so the walk is balanced), or, with the
 // dynamic order, claims the next unprocessed tile from an atomic counter
@@ -21,7 +26,7 @@ namespace clm {
 
 template <typename JT>
 __host__ __device__ constexpr size_t eh_smem_per_layer() {
-  return 3 * sizeof(double) + 4 * sizeof(JT);  // xv, xe, fe | cp, dp, d, ae
+  return 2 * sizeof(double) + 3 * sizeof(JT);  // xv, xe | cp, dp, d
 }
 
 template <typename JT>
@@ -34,11 +39,12 @@ __host__ __device__ constexpr size_t richards_smem_per_layer() {
   return sizeof(double) + richards_jac_arrays<JT>() * sizeof(JT);  // xv | cp, dp (, dp low)
 }
 
-// Per-warp scratch slots of nmax x 32 doubles: K, face kappa / dz, face
-// K / dz and 1 / rho c (FP64 path); K, face kappa / dz, face K / dz and the
-// float Jacobian arrays 1 / rho c, dt K_face / dz^2 and dt kappa_face / dz^2
-// packed into two slots (mixed).
-__host__ __device__ constexpr int eh_scratch_slots(bool mixed) { return mixed ? 5 : 4; }
+// Per-warp scratch slots of nmax x 32 doubles. FP64 path: K, face kappa / dz,
+// 1 / rho c, face K / dz, the energy residual, the energy-advection face
+// coefficient. Mixed: K, face kappa / dz, then the floats 1 / rho c,
+// dt K_face / dz^2, dt kappa_face / dz^2 and the energy-advection face
+// coefficient packed into two slots, face K / dz, the energy residual.
+__host__ __device__ constexpr int eh_scratch_slots(bool) { return 6; }
 
 template <typename JT, class CM>
 __global__ void __launch_bounds__(128, 1)
@@ -54,15 +60,15 @@ __global__ void __launch_bounds__(128, 1)
   const int wpc = blockDim.x >> 5;
   const int nmax = A.L.nmax;
   const int64_t lay = (int64_t)nmax * kTile;
-  double* dw = tab + kTab + (int64_t)warp * 3 * lay;
-  JT* jw = reinterpret_cast<JT*>(tab + kTab + (int64_t)wpc * 3 * lay) + (int64_t)warp * 4 * lay;
+  double* dw = tab + kTab + (int64_t)warp * 2 * lay;
+  JT* jw = reinterpret_cast<JT*>(tab + kTab + (int64_t)wpc * 2 * lay) + (int64_t)warp * 3 * lay;
   const int gwarp = blockIdx.x * wpc + warp;
   const int nwarps = gridDim.x * wpc;
   double* sw = scratch + (int64_t)gwarp * eh_scratch_slots(kMixed) * lay;
   EHBuffers B;
   B.xv = Col<double>{dw + lane, kTile};
   B.xe = Col<double>{dw + lay + lane, kTile};
-  B.fe = Col<double>{dw + 2 * lay + lane, kTile};
+  B.fe = Col<double>{sw + (kMixed ? 5 : 4) * lay + lane, kTile};
   B.K = Col<double>{sw + lane, kTile};
   B.kap = Col<double>{sw + lay + lane, kTile};
   B.aw = Col<double>{sw + (kMixed ? 4 : 3) * lay + lane, kTile};
@@ -78,7 +84,10 @@ __global__ void __launch_bounds__(128, 1)
   J.cp = Col<JT>{jw + lane, kTile};
   J.dp = Col<JT>{jw + lay + lane, kTile};
   J.d = Col<JT>{jw + 2 * lay + lane, kTile};
-  J.ae = Col<JT>{jw + 3 * lay + lane, kTile};
+  if constexpr (kMixed)
+    J.ae = Col<JT>{reinterpret_cast<JT*>(sw + 2 * lay) + 3 * lay + lane, kTile};
+  else
+    J.ae = Col<JT>{reinterpret_cast<JT*>(sw + 5 * lay) + lane, kTile};
   const double t0 = clk.start(), dt = clk.step();
   const bool dyn = A.tile_ctr != nullptr;
   const int tend = A.tile_end < 0 ? A.L.ntiles : A.tile_end;
