@@ -173,6 +173,24 @@ struct EHBuffers {
   Col<const float> guess_v{nullptr, 0}, guess_e{nullptr, 0};
 };
 
+// FP64 <-> Jacobian-type conversions: identities on the FP64 path; on the
+// mixed path integer-only ones (clm_ff.cuh), which keep the FP64 pipe for
+// the arithmetic.
+template <typename JT>
+CLM_HD JT to_jt(double x) {
+  if constexpr (sizeof(JT) < sizeof(double))
+    return ff::narrow_trunc(x);
+  else
+    return x;
+}
+template <typename JT>
+CLM_HD double from_jt(JT x) {
+  if constexpr (sizeof(JT) < sizeof(double))
+    return ff::widen_fast(x);
+  else
+    return x;
+}
+
 template <typename JT>
 struct EHJac {
   Col<JT> cp, dp, d, ae;            // Thomas c', d' (then delta_v, d''), dpsi, face coef
@@ -188,9 +206,14 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
   const int st = A.L.stride;
   const double rdz = dt * c.inv_dz;
   const double half = 0.5 * c.dz;
+  const double hinv_dz = 0.5 * c.inv_dz;  // face means: 0.5 (a + b) / dz, exactly (a + b) hinv_dz
   constexpr bool mixed = sizeof(JT) < sizeof(double);
   EHMixed<CM> MX;
-  if constexpr (mixed) MX = make_eh_mixed(Tb, E, sc, c);
+  PCCol pcc;
+  if constexpr (mixed) {
+    MX = make_eh_mixed(Tb, E, sc, c);
+    pcc = make_pc_col(c.nu, c.theta_r, c.dz);
+  }
   const bool tol = A.newton_mode == CLM_NEWTON_TOL;  // the increment norms are needed only then
 
   for (int step = 0; step < nsteps; ++step) {
@@ -213,7 +236,9 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       const double nu_safe = fmax(nu_eff, c.theta_r + kSqrtEps);
       const double tl = (v_safe < nu_safe) ? v_safe : nu_safe;
       const double rc = heat_capacity(E, tl, Yti, c.rcds);
-      const double T = temperature(E, Ye, Yti, rc);
+      // mixed: one reciprocal of rho c for T and the phase change
+      const double inv_rc = mixed ? 1.0 / rc : 0.0;
+      const double T = mixed ? E.T_0 + (Ye + Yti * E.rho_i_LH_f0) * inv_rc : temperature(E, Ye, Yti, rc);
       double kap = 0.0, K = 0.0;
       bool aux_ff = false;
       if constexpr (mixed) {
@@ -241,7 +266,9 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       }
       double Uv = Yv, Uti = Yti;
       if (A.phase_change) {
-        const double pc = phase_change<!mixed>(Tb, E, c.g, c.nu, c.theta_r, tl, Yti, T, rc, kap, c.dz, flags);
+        const double pc =
+            mixed ? phase_change_reduced(Tb, E, c.g, c.nu, c.theta_r, pcc, tl, Yti, T, inv_rc, kap)
+                  : phase_change(Tb, E, c.g, c.nu, c.theta_r, tl, Yti, T, rc, kap, c.dz, flags);
         Uv = Yv + dt * (-pc);
         Uti = Yti + dt * (E.rho_l_over_rho_i * pc);
       }
@@ -265,18 +292,19 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       // face conductances k-1|k, frozen through the Newton solve: kappa on
       // the face into kappa's slot (the cell value is not used after stage 1)
       if (k > 0) {
-        const double ak = 0.5 * (kap_prev + kap) * c.inv_dz;
+        const double ak = (kap_prev + kap) * hinv_dz;
+        const double aw = (K_prev + K) * hinv_dz;
         B.kap[k - 1] = ak;
-        if (B.aw.p) B.aw[k - 1] = 0.5 * (K_prev + K) * c.inv_dz;
+        if (B.aw.p) B.aw[k - 1] = aw;
         if constexpr (mixed) {
-          B.awr[k - 1] = (float)(rdz * (0.5 * (K_prev + K) * c.inv_dz));
-          B.akr[k - 1] = (float)(rdz * ak);
+          B.awr[k - 1] = ff::narrow_trunc(rdz * aw);
+          B.akr[k - 1] = ff::narrow_trunc(rdz * ak);
         }
       }
       kap_prev = kap;
       K_prev = K;
       if constexpr (mixed)
-        B.ircf[k] = 1.0f / (float)heat_capacity(E, tl, Uti, c.rcds);
+        B.ircf[k] = 1.0f / ff::narrow_trunc(heat_capacity(E, tl, Uti, c.rcds));
       else
         B.irc[k] = 1.0 / heat_capacity(E, tl, Uti, c.rcds);
       if (k == 0) {
@@ -361,9 +389,9 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
           eh_point<JT, CM>(Tb, E, c, MX, B.xv[k + 1], B.xe[k + 1], B.gti[k + 1], Tn, psin, Dn);
           Kn = B.K[k + 1];
           relKn = rho_e_liq(E, Tn) * Kn;
-          aw_up = B.aw.p ? B.aw[k] : 0.5 * (Kc + Kn) * c.inv_dz;
+          aw_up = B.aw.p ? B.aw[k] : (Kc + Kn) * hinv_dz;
           const double ak_up = B.kap[k];  // face k|k+1 (stage 1)
-          ae_up = 0.5 * (relKc + relKn) * c.inv_dz;
+          ae_up = (relKc + relKn) * hinv_dz;
           const double dh = (psin - psic) + c.dz;
           Fw_up = -aw_up * dh;
           Fe_up = -ak_up * (Tn - Tc) - ae_up * dh;
@@ -372,10 +400,17 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
           Fw_up = Ftw;
           Fe_up = Fth;
         }
-        const double Tv = -((Fw_up - Fw_dn) * c.inv_dz);
-        const double Tee = -((Fe_up - Fe_dn) * c.inv_dz);
-        const double fv = B.gv[k] + dt * Tv - B.xv[k];
-        const double fe = B.ge[k] + dt * Tee - B.xe[k];
+        double fv, fe;
+        if constexpr (mixed) {
+          // U + dt T - x with dt T = rdz (F_dn - F_up): one rounding fewer
+          fv = (B.gv[k] - B.xv[k]) + rdz * (Fw_dn - Fw_up);
+          fe = (B.ge[k] - B.xe[k]) + rdz * (Fe_dn - Fe_up);
+        } else {
+          const double Tv = -((Fw_up - Fw_dn) * c.inv_dz);
+          const double Tee = -((Fe_up - Fe_dn) * c.inv_dz);
+          fv = B.gv[k] + dt * Tv - B.xv[k];
+          fe = B.ge[k] + dt * Tee - B.xe[k];
+        }
         sum_fv += fv;
         sum_fe += fe;
         JT L, U, Md;
@@ -400,11 +435,11 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         }
         const JT inv = (JT)1 / piv;
         const JT cpk = U * inv;
-        const JT dpk = ((JT)fv - L * dp_prev) * inv;
+        const JT dpk = (to_jt<JT>(fv) - L * dp_prev) * inv;
         J.cp[k] = cpk;
         J.dp[k] = dpk;
         J.d[k] = Dc;
-        J.ae[k] = (JT)ae_up;
+        J.ae[k] = to_jt<JT>(ae_up);
         B.fe[k] = fe;
         cp_prev = cpk;
         dp_prev = dpk;
@@ -428,7 +463,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
           const JT d = J.dp[k] - J.cp[k] * nxt;
           J.dp[k] = d;
           nxt = d;
-          if (mixed) sdv += (double)d;
+          if (mixed) sdv += from_jt<JT>(d);
         }
       }
       // FP64 column-sum projection (mixed path): sum(delta_v) = -sum(f_v)
@@ -446,7 +481,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         JT dv0 = J.dp[0] - (JT)corr_v, D0 = J.d[0];
         // the applied increment in FP64, so that the increments sum to
         // -sum(f_v) to FP64 rounding (the water budget identity)
-        double dvd0 = (double)J.dp[0] - corr_v;
+        double dvd0 = from_jt<JT>(J.dp[0]) - corr_v;
         JT ae_dn = 0;
         double irc_c = 0.0, irc_m = 0.0;
         JT ircf_c = 0, ircf_m = 0;
@@ -461,7 +496,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
           JT akr_up = 0, ircf_n = 0;
           if (k < n - 1) {
             dvp = J.dp[k + 1] - (JT)corr_v;
-            dvdp = (double)J.dp[k + 1] - corr_v;
+            dvdp = from_jt<JT>(J.dp[k + 1]) - corr_v;
             Dp = J.d[k + 1];
             ae_up = J.ae[k];
             if constexpr (mixed) {
@@ -475,7 +510,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
           const JT Gup = (k < n - 1) ? (Dp * dvp - D0 * dv0) : (JT)0;
           const JT Gdn = (k > 0) ? (D0 * dv0 - Dm * dvm) : (JT)0;
           const JT wev = (JT)rdz * (ae_up * Gup - ae_dn * Gdn) - dv0;
-          const double g = B.fe[k] - (double)wev;
+          const double g = B.fe[k] - from_jt<JT>(wev);
           JT L, U, Md;
           if constexpr (mixed) {
             L = akr_dn * ircf_m;
@@ -498,7 +533,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
           }
           const JT inv = (JT)1 / piv;
           const JT ck = U * inv;
-          const JT dk = ((JT)g - L * d_prev) * inv;
+          const JT dk = (to_jt<JT>(g) - L * d_prev) * inv;
           J.cp[k] = ck;
           J.dp[k] = dk;
           c_prev = ck;
@@ -524,14 +559,14 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
           for (int k = n - 1; k >= 0; --k) {
             const JT d = J.dp[k] - J.cp[k] * nxt;
             J.dp[k] = d;
-            sde += (double)d;
+            sde += from_jt<JT>(d);
             nxt = d;
           }
           // W_ee and W_ev + I have zero column sums:
           // sum(delta_e) = -sum(f_e) - sum(delta_v) = -sum(f_e) + sum(f_v)
           const double corr_e = (sde + sum_fe - sum_fv) / n;
           for (int k = 0; k < n; ++k) {
-            const double d = (double)J.dp[k] - corr_e;
+            const double d = from_jt<JT>(J.dp[k]) - corr_e;
             B.xe[k] -= d;
             if (tol) state2 += (se * d) * (se * d);
           }

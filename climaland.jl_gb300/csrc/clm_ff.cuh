@@ -223,6 +223,39 @@ CLM_HD double widen(float x) {
 // hi + lo -> double: both are exact in double; one FP64 addition.
 CLM_HD double to_double(F2 x) { return widen(x.hi) + widen(x.lo); }
 
+// float -> double with integer operations only and no branch: exact for
+// normal floats; zero and subnormal floats give a signed zero; infinities
+// and NaN keep their class. For the mixed path's float increments and
+// right-hand sides, which are never subnormal in magnitude that matters.
+CLM_HD double widen_fast(float x) {
+  const uint32_t b = fbits(x);
+  const uint32_t e = (b >> 23) & 0xFF;
+  const uint64_t sign = (uint64_t)(b & 0x80000000u) << 32;
+  const uint64_t mant = (uint64_t)(b & 0x7FFFFFu) << 29;
+  uint64_t r = sign | ((uint64_t)(e + 896) << 52) | mant;
+  r = (e == 0) ? sign : r;
+  r = (e == 0xFF) ? (sign | 0x7FF0000000000000ull | mant) : r;
+  return dfrom(r);
+}
+
+// double -> float by truncating the significand (relative error below
+// 2^-23), integer operations only: the mixed path's float Jacobian entries
+// and right-hand sides. Magnitudes below the float normal range give a
+// signed zero; above it, and infinities, an infinity; NaN stays NaN.
+CLM_HD float narrow_trunc(double d) {
+  const uint64_t b = dbits(d);
+  const uint32_t h = (uint32_t)(b >> 32);
+  const uint32_t sign = h & 0x80000000u;
+  const int E = (int)((h >> 20) & 0x7FF);
+  const int e = E - 896;  // float biased exponent
+  const uint32_t mant = (uint32_t)(b >> 29) & 0x7FFFFFu;
+  uint32_t r = sign | ((uint32_t)e << 23) | mant;
+  r = (e <= 0) ? sign : r;
+  const bool nan = E == 0x7FF && (b & 0x000FFFFFFFFFFFFFull) != 0;
+  r = (e >= 255) ? (sign | 0x7F800000u | (nan ? 0x400000u : 0u)) : r;
+  return ffrom(r);
+}
+
 // ---- tables -----------------------------------------------------------------------
 // 2^(j/64), j = 0..63, as double-float pairs (hi[64] then lo[64]).
 struct Tables {

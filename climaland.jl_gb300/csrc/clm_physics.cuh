@@ -329,7 +329,7 @@ CLM_HD double conductivity_heat(const Tables& T, const EHScalars& sc, double the
 // thermal_time (:60-62): (theta_l - theta_star) / tau, tau = 3 rho c dz^2 /
 // kappa.
 //
-// kRefForm (the plain FP64 path) evaluates the reference's own sequence:
+// phase_change (the FP64 path) evaluates the reference's own sequence:
 // psi_w0 = matric_potential(S(theta_tot)), Tf = max(T_freeze exp(g psi_w0 /
 // L_f), 1), psi_T = L_f/g log(T/Tf) heaviside(Tf - T), theta_star =
 // inverse_matric_potential(psi_w0 + psi_T). For T >= T_freeze the heaviside
@@ -337,7 +337,7 @@ CLM_HD double conductivity_heat(const Tables& T, const EHScalars& sc, double the
 // then inverse_matric_potential(matric_potential(S)) = S (nu - theta_r) +
 // theta_r.
 //
-// The reduced form (mixed path) uses that with this Tf,
+// phase_change_reduced (the mixed path) uses that with this Tf,
 //   psi_w0 + L_f/g log(T/Tf) = L_f/g log(T/T_freeze) =: psi_T,
 // independent of psi_w0, and Tf > T <=> psi_w0 > psi_T <=> S(theta_tot) > S_T
 // with S_T = inverse_matric_potential(psi_T) (the matric potential increases
@@ -351,20 +351,10 @@ CLM_HD double conductivity_heat(const Tables& T, const EHScalars& sc, double the
 // trajectory switches a discontinuous closure (the Kersten number at
 // theta_i = eps) follow that rounding, so the plain path keeps the
 // reference's sequence.
-template <bool kRefForm = true, class CM>
+template <class CM>
 CLM_HD double phase_change(const Tables& T, const Earth& E, const CM& g, double nu,
                            double theta_r, double theta_l, double theta_i, double Tk,
                            double rhoc, double kappa, double dz, uint32_t& flags) {
-  if (!kRefForm) {
-    const double theta_tot = fmin(E.rho_i_over_rho_l * theta_i + theta_l, nu);
-    double S = saturation(nu, theta_tot, theta_r).S;
-    if (Tk < E.T_freeze) {
-      const double psi_T = E.LH_f0_over_grav * fm::log(T, Tk * E.inv_T_freeze);
-      S = fmin(S, inverse_sat(T, g, psi_T));
-    }
-    const double theta_star = S * (nu - theta_r) + theta_r;
-    return (theta_l - theta_star) * kappa / (3.0 * rhoc * (dz * dz));
-  }
   const double theta_tot = fmin(E.rho_i_over_rho_l * theta_i + theta_l, nu);
   double theta_star;
   double S;
@@ -385,6 +375,34 @@ CLM_HD double phase_change(const Tables& T, const Earth& E, const CM& g, double 
   }
   const double tau = 3.0 * rhoc * (dz * dz) / kappa;
   return (theta_l - theta_star) / tau;
+}
+
+// Per-column constants of phase_change_reduced.
+struct PCCol {
+  double nr;        // nu - theta_r
+  double inv_den;   // 1 / (max(nu, theta_r + sqrt(eps)) - theta_r): effective_saturation(nu, .)
+  double inv_3dz2;  // 1 / (3 dz^2): thermal_time
+};
+
+CLM_HD PCCol make_pc_col(double nu, double theta_r, double dz) {
+  return PCCol{nu - theta_r, 1.0 / (fmax(nu, theta_r + kSqrtEps) - theta_r), 1.0 / (3.0 * (dz * dz))};
+}
+
+// The reduced form, with the divisions turned into products by reciprocals:
+// the per-column ones above and inv_rhoc = 1 / rho c, which the caller also
+// uses for the temperature.
+template <class CM>
+CLM_HD double phase_change_reduced(const Tables& T, const Earth& E, const CM& g, double nu,
+                                   double theta_r, const PCCol& pcc, double theta_l,
+                                   double theta_i, double Tk, double inv_rhoc, double kappa) {
+  const double theta_tot = fmin(E.rho_i_over_rho_l * theta_i + theta_l, nu);
+  double S = (fmax(theta_tot, theta_r + kSqrtEps) - theta_r) * pcc.inv_den;
+  if (Tk < E.T_freeze) {
+    const double psi_T = E.LH_f0_over_grav * fm::log(T, Tk * E.inv_T_freeze);
+    S = fmin(S, inverse_sat(T, g, psi_T));
+  }
+  const double theta_star = S * pcc.nr + theta_r;
+  return (theta_l - theta_star) * kappa * inv_rhoc * pcc.inv_3dz2;
 }
 
 // counter hash of the rain-pulse forcing (splitmix64 finaliser, Vigna):
