@@ -63,6 +63,7 @@ struct EHCol {
   CM g;  // hydrology closure (VG or BC)
   double kdry, ksf, ksu, rcds, nuom, nuq, nug, lku, lkf;
   double dz, inv_dz;
+  double inv_S_s;  // 1 / S_s
 };
 
 // kLogKappaHere: take log(kappa_sat_*) from the exp/log tables instead of
@@ -93,17 +94,20 @@ CLM_HD EHCol<CM> load_eh_col(const StepArgs& A, const Tables& Tb, int s, int n) 
   }
   c.dz = (A.z_hi[s] - A.z_lo[s]) / n;
   c.inv_dz = 1.0 / c.dz;
+  c.inv_S_s = 1.0 / c.S_s;
   return c;
 }
 
 // T and psi at the Newton iterate (update_implicit_aux!,
 // energy_hydrology.jl:427-445) and dpsi/dvartheta for the Jacobian (:503-512).
+// inv: sat_inv(nu - ti, theta_r), fixed through the Newton solve.
 template <class CM>
 CLM_HD void eh_iterate_point(const Tables& Tb, const Earth& E, const EHCol<CM>& c, double xv,
-                             double xe, double ti, double& T, double& psi, double& D) {
+                             double xe, double ti, double inv, double& T, double& psi,
+                             double& D) {
   const double nu_eff = c.nu - ti;
   T = temperature(E, xe, ti, heat_capacity(E, fmin(nu_eff, xv), ti, c.rcds));
-  psi_dpsi<true>(Tb, c.g, nu_eff, xv, c.theta_r, c.S_s, psi, D);
+  psi_dpsi_r<true>(Tb, c.g, nu_eff, inv, xv, c.theta_r, c.inv_S_s, psi, D);
 }
 
 // Mixed path: T and psi in double-float (FP64 results), dpsi in float; points
@@ -150,11 +154,11 @@ CLM_HD void eh_iterate_point_mixed(const Tables& Tb, const EHCol<CM>& c, const E
 // T, psi and dpsi at the iterate on either path (dpsi in the Jacobian type).
 template <typename JT, class CM>
 CLM_HD void eh_point(const Tables& Tb, const Earth& E, const EHCol<CM>& c, const EHMixed<CM>& M, double xv,
-                     double xe, double ti, double& T, double& psi, JT& D) {
+                     double xe, double ti, double inv, double& T, double& psi, JT& D) {
   if constexpr (sizeof(JT) < sizeof(double)) {
     eh_iterate_point_mixed(Tb, c, M, xv, xe, ti, T, psi, D);
   } else {
-    eh_iterate_point(Tb, E, c, xv, xe, ti, T, psi, D);
+    eh_iterate_point(Tb, E, c, xv, xe, ti, inv, T, psi, D);
   }
 }
 
@@ -168,6 +172,9 @@ struct EHBuffers {
   // face water conductance K_face / dz, precomputed per step (p == nullptr:
   // computed in every Newton iteration, the same value)
   Col<double> aw{nullptr, 0};
+  // FP64 path: sat_inv(nu - theta_i, theta_r) per layer for the Newton solve
+  // (p == nullptr: computed at each use)
+  Col<double> iden{nullptr, 0};
   // learned Newton guess: predicted u_{n+1} - u_n of vartheta_l and rho_e_int
   // (p == nullptr: no guess)
   Col<const float> guess_v{nullptr, 0}, guess_e{nullptr, 0};
@@ -209,11 +216,8 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
   const double hinv_dz = 0.5 * c.inv_dz;  // face means: 0.5 (a + b) / dz, exactly (a + b) hinv_dz
   constexpr bool mixed = sizeof(JT) < sizeof(double);
   EHMixed<CM> MX;
-  PCCol pcc;
-  if constexpr (mixed) {
-    MX = make_eh_mixed(Tb, E, sc, c);
-    pcc = make_pc_col(c.nu, c.theta_r, c.dz);
-  }
+  const PCCol pcc = make_pc_col(c.nu, c.theta_r, c.dz);
+  if constexpr (mixed) MX = make_eh_mixed(Tb, E, sc, c);
   const bool tol = A.newton_mode == CLM_NEWTON_TOL;  // the increment norms are needed only then
 
   for (int step = 0; step < nsteps; ++step) {
@@ -236,9 +240,9 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       const double nu_safe = fmax(nu_eff, c.theta_r + kSqrtEps);
       const double tl = (v_safe < nu_safe) ? v_safe : nu_safe;
       const double rc = heat_capacity(E, tl, Yti, c.rcds);
-      // mixed: one reciprocal of rho c for T and the phase change
-      const double inv_rc = mixed ? 1.0 / rc : 0.0;
-      const double T = mixed ? E.T_0 + (Ye + Yti * E.rho_i_LH_f0) * inv_rc : temperature(E, Ye, Yti, rc);
+      // one reciprocal of rho c for T and the phase change
+      const double inv_rc = 1.0 / rc;
+      const double T = E.T_0 + (Ye + Yti * E.rho_i_LH_f0) * inv_rc;
       double kap = 0.0, K = 0.0;
       bool aux_ff = false;
       if constexpr (mixed) {
@@ -257,23 +261,25 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       if (!aux_ff) {
         kap = conductivity_heat(Tb, sc, tl, Yti, c.nu, c.kdry, c.ksu, c.ksf, c.lku, c.lkf, c.nuom,
                                 c.nuq, c.nug);
-        const Sat sK = saturation(c.nu, Yv, c.theta_r);
+        const double SK = saturation_r(pcc.inv_den, Yv, c.theta_r);
         const double fi = Yti > 0.0 ? Yti / (tl + Yti - c.theta_r) : 0.0;
         // impedance_factor * viscosity_factor * hydraulic_conductivity, with
         // the sqrt(S) of the van Genuchten K inside the same exponential
         const double lnf = -sc.omega_ln10 * fi + sc.visc_gamma * (T - sc.visc_gamma_T_ref);
-        K = conductivity_scaled(Tb, c.g, c.K_sat, sK.S, lnf);
+        K = conductivity_scaled(Tb, c.g, c.K_sat, SK, lnf);
       }
       double Uv = Yv, Uti = Yti;
       if (A.phase_change) {
         const double pc =
             mixed ? phase_change_reduced(Tb, E, c.g, c.nu, c.theta_r, pcc, tl, Yti, T, inv_rc, kap)
-                  : phase_change(Tb, E, c.g, c.nu, c.theta_r, tl, Yti, T, rc, kap, c.dz, flags);
+                  : phase_change_r(Tb, E, c.g, c.nu, c.theta_r, pcc, tl, Yti, T, inv_rc, kap, flags);
         Uv = Yv + dt * (-pc);
         Uti = Yti + dt * (E.rho_l_over_rho_i * pc);
       }
       B.gv[k] = Uv;
       B.gti[k] = Uti;
+      if constexpr (!mixed)
+        if (B.iden.p) B.iden[k] = sat_inv(c.nu - Uti, c.theta_r);
       if (use_guess) {
         double xv0 = Yv + (double)B.guess_v[k], xe0 = Ye + (double)B.guess_e[k];
         // a layer whose guess leaves the retention curve's domain
@@ -378,7 +384,11 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       double sum_fv = 0.0, sum_fe = 0.0;
       double Tc, psic;
       JT Dc;
-      eh_point<JT, CM>(Tb, E, c, MX, B.xv[0], B.xe[0], B.gti[0], Tc, psic, Dc);
+      auto inv_of = [&](int k) {  // FP64 path: the layer's sat_inv
+        if constexpr (mixed) return 0.0;
+        else return B.iden.p ? B.iden[k] : sat_inv(c.nu - B.gti[k], c.theta_r);
+      };
+      eh_point<JT, CM>(Tb, E, c, MX, B.xv[0], B.xe[0], B.gti[0], inv_of(0), Tc, psic, Dc);
       double Kc = B.K[0];
       double relKc = rho_e_liq(E, Tc) * Kc;
       for (int k = 0; k < n; ++k) {
@@ -386,7 +396,8 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         double Tn = 0, psin = 0, Kn = 0, relKn = 0;
         JT Dn = 0, awr_up = 0;
         if (k < n - 1) {
-          eh_point<JT, CM>(Tb, E, c, MX, B.xv[k + 1], B.xe[k + 1], B.gti[k + 1], Tn, psin, Dn);
+          eh_point<JT, CM>(Tb, E, c, MX, B.xv[k + 1], B.xe[k + 1], B.gti[k + 1], inv_of(k + 1), Tn,
+                           psin, Dn);
           Kn = B.K[k + 1];
           relKn = rho_e_liq(E, Tn) * Kn;
           aw_up = B.aw.p ? B.aw[k] : (Kc + Kn) * hinv_dz;
@@ -649,6 +660,7 @@ CLM_HD void richards_column(const StepArgs& A, const Tables& Tb, int s, int n, i
   const double S_s = P[CLM_P_S_S * st + s];
   const double theta_r = P[CLM_P_THETA_R * st + s];
   const CM g = make_cm<CM>(P[CLM_P_VG_ALPHA * st + s], P[CLM_P_VG_N * st + s]);
+  const double inv = sat_inv(nu, theta_r), inv_S_s = 1.0 / S_s;
   const double dz = (A.z_hi[s] - A.z_lo[s]) / n;
   const double inv_dz = 1.0 / dz;
   const double half = 0.5 * dz;
@@ -709,7 +721,7 @@ CLM_HD void richards_column(const StepArgs& A, const Tables& Tb, int s, int n, i
       JT D_prev = 0;
       double sum_f = 0.0;
       double Kc, psic, Dc;
-      richards_point<true>(Tb, g, nu, B.xv[0], theta_r, S_s, K_sat, Kc, psic, Dc);
+      richards_point<true>(Tb, g, nu, inv, B.xv[0], theta_r, inv_S_s, K_sat, Kc, psic, Dc);
       if (refresh_bc) {
         if (A.bc_bw == CLM_BC_FREE_DRAINAGE) Fbw = -1.0 * Kc;
         else if (A.bc_bw == CLM_BC_STATE) Fbw = -Kc * ((psic + half) - psi_bb) / half;
@@ -720,7 +732,7 @@ CLM_HD void richards_column(const StepArgs& A, const Tables& Tb, int s, int n, i
         double Kn = 0, psin = 0, Dn = 0;
         double Md_extra = 0.0;
         if (k < n - 1) {
-          richards_point<true>(Tb, g, nu, B.xv[k + 1], theta_r, S_s, K_sat, Kn, psin, Dn);
+          richards_point<true>(Tb, g, nu, inv, B.xv[k + 1], theta_r, inv_S_s, K_sat, Kn, psin, Dn);
           aw_up = 0.5 * (Kc + Kn) * inv_dz;
           Fw_up = -aw_up * ((psin - psic) + dz);
         } else {

@@ -128,6 +128,19 @@ CLM_HD Sat saturation(double nu_eff, double vartheta, double theta_r) {
   return s;
 }
 
+// 1 / (max(nu_eff, theta_r + sqrt(eps)) - theta_r): the reciprocal of the
+// clipped denominator of effective_saturation, constant over a column
+// (nu_eff = nu) or over a Newton solve (nu_eff = nu - theta_i, theta_i fixed).
+// With it S = (vartheta_safe - theta_r) inv costs a product instead of a
+// division (within an ulp of the quotient).
+CLM_HD double sat_inv(double nu_eff, double theta_r) {
+  return 1.0 / (fmax(nu_eff, theta_r + kSqrtEps) - theta_r);
+}
+
+CLM_HD double saturation_r(double inv, double vartheta, double theta_r) {
+  return (fmax(vartheta, theta_r + kSqrtEps) - theta_r) * inv;
+}
+
 // pressure_head (:109-127) and dpsidvartheta (:135-152) at one point,
 // sharing S^(-1/m) and log(S^(-1/m) - 1). want_d selects the derivative.
 //   psi  = -(S^(-1/m) - 1)^(1/n) / alpha                 (S <= 1)
@@ -151,6 +164,27 @@ CLM_HD void psi_dpsi(const Tables& T, const VG& g, double nu_eff, double varthet
   }
 }
 
+// psi_dpsi with the reciprocal inv = sat_inv(nu_eff, theta_r) and 1/S_s given:
+// no division on the unsaturated branch but dpsi's, whose factor
+// S (nu_safe - theta_r) is vartheta_safe - theta_r itself.
+template <bool want_d>
+CLM_HD void psi_dpsi_r(const Tables& T, const VG& g, double nu_eff, double inv, double vartheta,
+                       double theta_r, double inv_S_s, double& psi, double& dpsi) {
+  const double vs = fmax(vartheta, theta_r + kSqrtEps);
+  const double a = vs - theta_r;
+  const double S = a * inv;
+  if (S < 1.0) {
+    const double u = fm::exp(T, -g.inv_m * fm::log(T, S));  // S^(-1/m)
+    const double w = u - 1.0;
+    const double w1n = fm::exp(T, g.inv_n * fm::log(T, w));  // w^(1/n)
+    psi = -w1n * g.inv_alpha;
+    if (want_d) dpsi = g.coef_d * w1n * u / (w * a);
+  } else {
+    psi = (S <= 1.0) ? -0.0 : (vs - fmax(nu_eff, theta_r + kSqrtEps)) * inv_S_s;
+    if (want_d) dpsi = inv_S_s;
+  }
+}
+
 // Brooks-Corey pressure_head (:268-287) and dpsidvartheta (:219-230),
 // sharing S^(-1/c):
 //   psi  = psi_b S^(-1/c)                                  (S <= 1)
@@ -169,6 +203,22 @@ CLM_HD void psi_dpsi(const Tables& T, const BC& g, double nu_eff, double varthet
     // S == 1: matric_potential(1) = psi_b
     psi = (s.S <= 1.0) ? g.psib : (s.v_safe - s.nu_safe) / S_s + g.psib;
     if (want_d) dpsi = 1.0 / S_s;
+  }
+}
+
+template <bool want_d>
+CLM_HD void psi_dpsi_r(const Tables& T, const BC& g, double nu_eff, double inv, double vartheta,
+                       double theta_r, double inv_S_s, double& psi, double& dpsi) {
+  const double vs = fmax(vartheta, theta_r + kSqrtEps);
+  const double a = vs - theta_r;
+  const double S = a * inv;
+  if (S < 1.0) {
+    const double u = fm::exp(T, g.neg_inv_c * fm::log(T, S));  // S^(-1/c)
+    psi = g.psib * u;
+    if (want_d) dpsi = g.coef_d * u / a;
+  } else {
+    psi = (S <= 1.0) ? g.psib : (vs - fmax(nu_eff, theta_r + kSqrtEps)) * inv_S_s + g.psib;
+    if (want_d) dpsi = inv_S_s;
   }
 }
 
@@ -208,45 +258,50 @@ CLM_HD double conductivity_scaled(const Tables& T, const BC& g, double K_sat, do
   return K_sat * fm::exp(T, lnf + g.k_exp * fm::log(T, S));
 }
 
-// Richards point: K, psi (and dpsi) sharing log(S) (nu_eff = nu).
+// Richards point: K, psi (and dpsi) sharing log(S) (nu_eff = nu), with the
+// column's inv = sat_inv(nu, theta_r) and 1/S_s (as psi_dpsi_r).
 template <bool want_d>
-CLM_HD void richards_point(const Tables& T, const VG& g, double nu, double vartheta,
-                           double theta_r, double S_s, double K_sat, double& K, double& psi,
+CLM_HD void richards_point(const Tables& T, const VG& g, double nu, double inv, double vartheta,
+                           double theta_r, double inv_S_s, double K_sat, double& K, double& psi,
                            double& dpsi) {
-  Sat s = saturation(nu, vartheta, theta_r);
-  if (s.S < 1.0) {
-    const double lS = fm::log(T, s.S);
+  const double vs = fmax(vartheta, theta_r + kSqrtEps);
+  const double a = vs - theta_r;
+  const double S = a * inv;
+  if (S < 1.0) {
+    const double lS = fm::log(T, S);
     const double u = fm::exp(T, -g.inv_m * lS);  // S^(-1/m)
     const double w = u - 1.0;
     const double w1n = fm::exp(T, g.inv_n * fm::log(T, w));
     psi = -w1n * g.inv_alpha;
-    if (want_d) dpsi = g.coef_d * w1n * u / (w * s.S * (s.nu_safe - theta_r));
+    if (want_d) dpsi = g.coef_d * w1n * u / (w * a);
     const double s1m = fm::exp(T, g.inv_m * lS);  // S^(1/m)
     const double t = fm::exp(T, g.m * fm::log(T, 1.0 - s1m));
     const double f = 1.0 - t;
-    K = K_sat * (sqrt(s.S) * f * f);
+    K = K_sat * (sqrt(S) * f * f);
   } else {
-    psi = (s.S <= 1.0) ? -0.0 : (s.v_safe - s.nu_safe) / S_s;
-    if (want_d) dpsi = 1.0 / S_s;
+    psi = (S <= 1.0) ? -0.0 : (vs - fmax(nu, theta_r + kSqrtEps)) * inv_S_s;
+    if (want_d) dpsi = inv_S_s;
     K = K_sat;
   }
 }
 
 // Brooks-Corey Richards point: K, psi (and dpsi) sharing log(S).
 template <bool want_d>
-CLM_HD void richards_point(const Tables& T, const BC& g, double nu, double vartheta,
-                           double theta_r, double S_s, double K_sat, double& K, double& psi,
+CLM_HD void richards_point(const Tables& T, const BC& g, double nu, double inv, double vartheta,
+                           double theta_r, double inv_S_s, double K_sat, double& K, double& psi,
                            double& dpsi) {
-  Sat s = saturation(nu, vartheta, theta_r);
-  if (s.S < 1.0) {
-    const double lS = fm::log(T, s.S);
+  const double vs = fmax(vartheta, theta_r + kSqrtEps);
+  const double a = vs - theta_r;
+  const double S = a * inv;
+  if (S < 1.0) {
+    const double lS = fm::log(T, S);
     const double u = fm::exp(T, g.neg_inv_c * lS);  // S^(-1/c)
     psi = g.psib * u;
-    if (want_d) dpsi = g.coef_d * u / (s.S * (s.nu_safe - theta_r));
+    if (want_d) dpsi = g.coef_d * u / a;
     K = K_sat * fm::exp(T, g.k_exp * lS);
   } else {
-    psi = (s.S <= 1.0) ? g.psib : (s.v_safe - s.nu_safe) / S_s + g.psib;
-    if (want_d) dpsi = 1.0 / S_s;
+    psi = (S <= 1.0) ? g.psib : (vs - fmax(nu, theta_r + kSqrtEps)) * inv_S_s + g.psib;
+    if (want_d) dpsi = inv_S_s;
     K = K_sat;
   }
 }
@@ -269,6 +324,18 @@ CLM_HD double matric_of(const Tables& T, const BC& g, double nu, double theta,
   Sat s = saturation(nu, theta, theta_r);
   if (S_out) *S_out = s.S;
   return g.psib * fm::exp(T, g.neg_inv_c * fm::log(T, s.S));
+}
+
+// matric_potential of a given effective saturation S <= 1.
+CLM_HD double matric_S(const Tables& T, const VG& g, double S) {
+  const double u = fm::exp(T, -g.inv_m * fm::log(T, S));
+  const double w = u - 1.0;
+  if (!(w > 0.0)) return -0.0;
+  return -fm::exp(T, g.inv_n * fm::log(T, w)) * g.inv_alpha;
+}
+
+CLM_HD double matric_S(const Tables& T, const BC& g, double S) {
+  return g.psib * fm::exp(T, g.neg_inv_c * fm::log(T, S));
 }
 
 // inverse_matric_potential (:72-77, :195-200) for psi <= 0:
@@ -325,6 +392,17 @@ CLM_HD double conductivity_heat(const Tables& T, const EHScalars& sc, double the
   return K_e * ksat + (1.0 - K_e) * kappa_dry;
 }
 
+// Per-column constants of phase_change_r and phase_change_reduced.
+struct PCCol {
+  double nr;        // nu - theta_r
+  double inv_den;   // 1 / (max(nu, theta_r + sqrt(eps)) - theta_r): effective_saturation(nu, .)
+  double inv_3dz2;  // 1 / (3 dz^2): thermal_time
+};
+
+CLM_HD PCCol make_pc_col(double nu, double theta_r, double dz) {
+  return PCCol{nu - theta_r, 1.0 / (fmax(nu, theta_r + kSqrtEps) - theta_r), 1.0 / (3.0 * (dz * dz))};
+}
+
 // Phase-change source (soil_heat_parameterizations.jl:89-122) including
 // thermal_time (:60-62): (theta_l - theta_star) / tau, tau = 3 rho c dz^2 /
 // kappa.
@@ -351,6 +429,10 @@ CLM_HD double conductivity_heat(const Tables& T, const EHScalars& sc, double the
 // trajectory switches a discontinuous closure (the Kersten number at
 // theta_i = eps) follow that rounding, so the plain path keeps the
 // reference's sequence.
+//
+// The column step passes the reciprocals it shares (PCCol below, and
+// inv_rhoc = 1 / rho c, also used for T): products replace the divisions
+// of S, tau and (theta_l - theta_star) / tau (each within an ulp or two).
 template <class CM>
 CLM_HD double phase_change(const Tables& T, const Earth& E, const CM& g, double nu,
                            double theta_r, double theta_l, double theta_i, double Tk,
@@ -377,15 +459,26 @@ CLM_HD double phase_change(const Tables& T, const Earth& E, const CM& g, double 
   return (theta_l - theta_star) / tau;
 }
 
-// Per-column constants of phase_change_reduced.
-struct PCCol {
-  double nr;        // nu - theta_r
-  double inv_den;   // 1 / (max(nu, theta_r + sqrt(eps)) - theta_r): effective_saturation(nu, .)
-  double inv_3dz2;  // 1 / (3 dz^2): thermal_time
-};
 
-CLM_HD PCCol make_pc_col(double nu, double theta_r, double dz) {
-  return PCCol{nu - theta_r, 1.0 / (fmax(nu, theta_r + kSqrtEps) - theta_r), 1.0 / (3.0 * (dz * dz))};
+template <class CM>
+CLM_HD double phase_change_r(const Tables& T, const Earth& E, const CM& g, double nu,
+                             double theta_r, const PCCol& pcc, double theta_l, double theta_i,
+                             double Tk, double inv_rhoc, double kappa, uint32_t& flags) {
+  const double theta_tot = fmin(E.rho_i_over_rho_l * theta_i + theta_l, nu);
+  const double S = (fmax(theta_tot, theta_r + kSqrtEps) - theta_r) * pcc.inv_den;
+  double theta_star = S * pcc.nr + theta_r;
+  if (Tk < E.T_freeze) {
+    const double psi_w0 = matric_S(T, g, S);
+    const double Tf = fmax(E.T_freeze * fm::exp(T, E.grav_over_LH_f0 * psi_w0), 1.0);
+    if (Tf - Tk > kEps) {  // heaviside(Tf - T)
+      const double psi = psi_w0 + E.LH_f0_over_grav * fm::log(T, Tk / Tf);
+      if (psi > 0.0) flags |= CLM_COL_PSI_POSITIVE;
+      theta_star = inverse_sat(T, g, psi) * pcc.nr + theta_r;
+    } else if (psi_w0 > 0.0) {
+      flags |= CLM_COL_PSI_POSITIVE;
+    }
+  }
+  return (theta_l - theta_star) * kappa * inv_rhoc * pcc.inv_3dz2;
 }
 
 // The reduced form, with the divisions turned into products by reciprocals:

@@ -41,10 +41,11 @@ __host__ __device__ constexpr size_t richards_smem_per_layer() {
 
 // Per-warp scratch slots of nmax x 32 doubles. FP64 path: K, face kappa / dz,
 // 1 / rho c, face K / dz, the energy residual, the energy-advection face
-// coefficient. Mixed: K, face kappa / dz, then the floats 1 / rho c,
-// dt K_face / dz^2, dt kappa_face / dz^2 and the energy-advection face
-// coefficient packed into two slots, face K / dz, the energy residual.
-__host__ __device__ constexpr int eh_scratch_slots(bool) { return 6; }
+// coefficient, the layer's saturation reciprocal. Mixed: K, face kappa / dz,
+// then the floats 1 / rho c, dt K_face / dz^2, dt kappa_face / dz^2 and the
+// energy-advection face coefficient packed into two slots, face K / dz, the
+// energy residual.
+__host__ __device__ constexpr int eh_scratch_slots(bool mixed) { return mixed ? 6 : 7; }
 
 template <typename JT, class CM>
 __global__ void __launch_bounds__(128, 1)
@@ -88,6 +89,7 @@ __global__ void __launch_bounds__(128, 1)
     J.ae = Col<JT>{reinterpret_cast<JT*>(sw + 2 * lay) + 3 * lay + lane, kTile};
   else
     J.ae = Col<JT>{reinterpret_cast<JT*>(sw + 5 * lay) + lane, kTile};
+  if constexpr (!kMixed) B.iden = Col<double>{sw + 6 * lay + lane, kTile};
   const double t0 = clk.start(), dt = clk.step();
   const bool dyn = A.tile_ctr != nullptr;
   const int tend = A.tile_end < 0 ? A.L.ntiles : A.tile_end;
