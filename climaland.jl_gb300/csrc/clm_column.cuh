@@ -139,11 +139,11 @@ CLM_HD EHMixed<CM> make_eh_mixed(const Tables& Tb, const Earth& E, const EHScala
 
 template <class CM>
 CLM_HD void eh_iterate_point_mixed(const Tables& Tb, const EHCol<CM>& c, const EHMixed<CM>& M, double xv,
-                                   double xe, double ti, double& T, double& psi, float& D) {
+                                   double xe, double ti, double& q, double& psi, float& D) {
   const F2 ti_f = ff::from_double(ti);
   const F2 v = ff::from_double(xv);
   const F2 nu_eff = ff::sub(M.cf.nu, ti_f);
-  T = temperature_ff(M.Ef, ff::from_double(xe), ti_f, ff_min(nu_eff, v), M.rcds);
+  q = temperature_rel_ff(M.Ef, ff::from_double(xe), ti_f, ff_min(nu_eff, v), M.rcds);
   if (!psi_dpsi_ff(M.FT, M.cf, nu_eff, v, psi, D)) {
     double d;
     psi_dpsi<true>(Tb, c.g, c.nu - ti, xv, c.theta_r, c.S_s, psi, d);
@@ -151,7 +151,14 @@ CLM_HD void eh_iterate_point_mixed(const Tables& Tb, const EHCol<CM>& c, const E
   }
 }
 
-// T, psi and dpsi at the iterate on either path (dpsi in the Jacobian type).
+// The temperature, psi and dpsi at the iterate (dpsi in the Jacobian type).
+// The FP64 path returns T as the reference computes it; the mixed path
+// returns q = T - T_0: the residual needs only temperature differences and
+// volumetric_internal_energy_liq(T) = rho c_l (T - T_0), so the mixed
+// iterate's temperature is carried relative to T_0 (no rounding of T to the
+// ulp of ~273 K and no subtraction of T_0). The FP64 path keeps the
+// reference's sequence: columns whose phase change sits on an unstable mode
+// follow differences of a few ulp in rho e_int.
 template <typename JT, class CM>
 CLM_HD void eh_point(const Tables& Tb, const Earth& E, const EHCol<CM>& c, const EHMixed<CM>& M, double xv,
                      double xe, double ti, double inv, double& T, double& psi, JT& D) {
@@ -214,6 +221,9 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
   const double rdz = dt * c.inv_dz;
   const double half = 0.5 * c.dz;
   const double hinv_dz = 0.5 * c.inv_dz;  // face means: 0.5 (a + b) / dz, exactly (a + b) hinv_dz
+  // mixed: the energy advection coefficient at a face, 0.5 (rho e_l(T_k) K_k
+  // + rho e_l(T_k+1) K_k+1) / dz, as the sum of the layers' q K (rho c_l 0.5 / dz)
+  const double c_adv = E.rhocp_l * hinv_dz;
   constexpr bool mixed = sizeof(JT) < sizeof(double);
   EHMixed<CM> MX;
   const PCCol pcc = make_pc_col(c.nu, c.theta_r, c.dz);
@@ -382,7 +392,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       JT awr_dn = 0;  // mixed: dt K_face / dz^2 of the face below
       JT D_prev = 0;
       double sum_fv = 0.0, sum_fe = 0.0;
-      double Tc, psic;
+      double Tc, psic;  // Tc, Tn: T (FP64 path) or T - T_0 (mixed) at the iterate
       JT Dc;
       auto inv_of = [&](int k) {  // FP64 path: the layer's sat_inv
         if constexpr (mixed) return 0.0;
@@ -390,7 +400,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       };
       eh_point<JT, CM>(Tb, E, c, MX, B.xv[0], B.xe[0], B.gti[0], inv_of(0), Tc, psic, Dc);
       double Kc = B.K[0];
-      double relKc = rho_e_liq(E, Tc) * Kc;
+      double relKc = mixed ? Tc * (Kc * c_adv) : rho_e_liq(E, Tc) * Kc;
       for (int k = 0; k < n; ++k) {
         double Fw_up, Fe_up, aw_up = 0.0, ae_up = 0.0;
         double Tn = 0, psin = 0, Kn = 0, relKn = 0;
@@ -399,10 +409,10 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
           eh_point<JT, CM>(Tb, E, c, MX, B.xv[k + 1], B.xe[k + 1], B.gti[k + 1], inv_of(k + 1), Tn,
                            psin, Dn);
           Kn = B.K[k + 1];
-          relKn = rho_e_liq(E, Tn) * Kn;
+          relKn = mixed ? Tn * (Kn * c_adv) : rho_e_liq(E, Tn) * Kn;
           aw_up = B.aw.p ? B.aw[k] : (Kc + Kn) * hinv_dz;
           const double ak_up = B.kap[k];  // face k|k+1 (stage 1)
-          ae_up = (relKc + relKn) * hinv_dz;
+          ae_up = mixed ? relKc + relKn : (relKc + relKn) * hinv_dz;
           const double dh = (psin - psic) + c.dz;
           Fw_up = -aw_up * dh;
           Fe_up = -ak_up * (Tn - Tc) - ae_up * dh;

@@ -122,12 +122,14 @@ CLM_HD bool psi_dpsi_ff(const ff::Tables& T, const ColFFBC& c, F2 nu_eff, F2 v, 
 }
 
 // temperature_from_ρe_int with volumetric_heat_capacity
-// (soil_heat_parameterizations.jl:157-192) at theta_l = tl.
-CLM_HD double temperature_ff(const EarthFF& E, F2 rho_e, F2 ti, F2 tl, F2 rhoc_ds) {
+// (soil_heat_parameterizations.jl:157-192) at theta_l = tl, relative to T_0:
+// (rho_e + theta_i rho_i L_f) / rho c, as a double (the Newton residual uses
+// T - T_0 only).
+CLM_HD double temperature_rel_ff(const EarthFF& E, F2 rho_e, F2 ti, F2 tl, F2 rhoc_ds) {
   using namespace ff;
   const F2 rc = add(add(rhoc_ds, mul(tl, E.rhocp_l)), mul(ti, E.rhocp_i));
   const F2 num = add(rho_e, mul(ti, E.rho_i_LH_f0));
-  return to_double(add(E.T_0, div(num, rc)));
+  return to_double(div(num, rc));
 }
 
 // impedance_factor * viscosity_factor * hydraulic_conductivity
