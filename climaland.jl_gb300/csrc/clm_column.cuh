@@ -19,8 +19,11 @@
 //   g*    state arrays in the internal layout. During a step they hold the
 //         stage value U (the explicit stage writes U over Y; U_e = Y_e), so
 //         U costs no on-chip storage; the final combination overwrites them.
-//   x*    Newton iterate, f_e residual, Thomas arrays: per-warp shared memory
-//   K, kappa, 1/rho c: frozen through the Newton solve, per-warp scratch
+//   x*    Newton iterate and Thomas arrays: per-warp shared memory
+//   K, kappa, 1/rho c, face coefficients (frozen through the Newton solve),
+//         the f_e residual: per-warp scratch (L2-resident global memory).
+//         The last step's state writes are evict-first (Col::store_last) so
+//         that the state streaming through L2 does not push the scratch out.
 //
 // Per Newton iteration, four sweeps:
 //   1 (up)    T, psi, dpsi at x in a rolling register window; face fluxes,
@@ -55,6 +58,14 @@ struct Col {
   T* p;
   int s;
   CLM_HD T& operator[](int k) const { return p[(int64_t)k * s]; }
+  // a store this launch does not read back: cache-streaming (evict-first)
+  CLM_HD void store_last(int k, T v) const {
+#ifdef __CUDA_ARCH__
+    __stcs(p + (int64_t)k * s, v);
+#else
+    p[(int64_t)k * s] = v;
+#endif
+  }
 };
 
 template <class CM>
@@ -230,6 +241,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
   if constexpr (mixed) MX = make_eh_mixed(Tb, E, sc, c);
   const bool tol = A.newton_mode == CLM_NEWTON_TOL;  // the increment norms are needed only then
 
+  bool finite = true;  // the last step's state, checked as it is stored
   for (int step = 0; step < nsteps; ++step) {
     const double t = t0 + step * dt;
     // learned guess (tolerance mode only): Newton starts from u_n + predicted
@@ -628,16 +640,24 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
     }
     // ---------------- final combination ---------------------------------
     const double inv_dt = 1.0 / dt;
+    const bool last = step == nsteps - 1;
     for (int k = 0; k < n; ++k) {
       const double Uv = B.gv[k], Ue = B.ge[k];
-      B.gv[k] = Uv + dt * ((B.xv[k] - Uv) * inv_dt);
-      B.ge[k] = Ue + dt * ((B.xe[k] - Ue) * inv_dt);
+      const double v = Uv + dt * ((B.xv[k] - Uv) * inv_dt);
+      const double e = Ue + dt * ((B.xe[k] - Ue) * inv_dt);
+      if (last) {
+        B.gv.store_last(k, v);
+        B.ge.store_last(k, e);
+        finite = finite && isfinite(v) && isfinite(B.gti[k]) && isfinite(e);
+      } else {
+        B.gv[k] = v;
+        B.ge[k] = e;
+      }
     }
     Fw = UFw + dt * ((xFw - UFw) * inv_dt);
     Fe = UFe + dt * ((xFe - UFe) * inv_dt);
   }
-  bool finite = isfinite(Fw) && isfinite(Fe);
-  for (int k = 0; k < n; ++k) finite = finite && isfinite(B.gv[k]) && isfinite(B.gti[k]) && isfinite(B.ge[k]);
+  finite = finite && isfinite(Fw) && isfinite(Fe);
   if (!finite) flags |= CLM_COL_NONFINITE;
 }
 
