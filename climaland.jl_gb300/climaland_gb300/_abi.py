@@ -52,6 +52,15 @@ CLM_BC_PRECIP_RUNOFF = 4
 CLM_RUNOFF_NONE = 0
 CLM_RUNOFF_SURFACE = 1
 CLM_RUNOFF_TOPMODEL = 2
+CLM_RX_PSI_CANOPY = 0
+CLM_RX_LAI = 1
+CLM_RX_RAI = 2
+CLM_RX_HEIGHT = 3
+CLM_RX_ROOT_DEPTH = 4
+CLM_RX_K_SAT = 5
+CLM_RX_PSI63 = 6
+CLM_RX_WEIBULL_C = 7
+CLM_RX_NFIELDS = 8
 CLM_CM_VAN_GENUCHTEN = 0
 CLM_CM_BROOKS_COREY = 1
 
@@ -234,6 +243,7 @@ SIGNATURES = [
     ("clm_last_error", ctypes.c_char_p, [_H]),
     ("clm_set_geometry", ctypes.c_int, [_H, _DP, _DP, _IP]),
     ("clm_set_params", ctypes.c_int, [_H, _DP, ctypes.c_int32]),
+    ("clm_set_root_extraction", ctypes.c_int, [_H, _DP, ctypes.c_int32]),
     ("clm_set_bc", ctypes.c_int, [_H, ctypes.c_int32, _DP, ctypes.c_int32]),
     ("clm_set_state", ctypes.c_int, [_H, _DP, _DP, _DP, _DP, _DP]),
     ("clm_get_state", ctypes.c_int, [_H, _DP, _DP, _DP, _DP, _DP]),

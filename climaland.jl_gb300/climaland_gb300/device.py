@@ -89,7 +89,18 @@ class SoilColumns:
         for slot, f in w.forcing.items():
             f = _c(f)
             self._check(self.lib.clm_set_bc(self.h, int(slot), A.dptr(f), f.shape[0]))
+        if getattr(w, "root", None) is not None:
+            self.set_root_extraction(w.root)
         self.set_state(w.vartheta_l, w.theta_i, w.rho_e_int, w.intF_w, w.intF_e)
+
+    def set_root_extraction(self, root):
+        """RootExtraction canopy values (CLM_RX_NFIELDS rows of ncol), or None
+        to remove the source."""
+        if root is None:
+            self._check(self.lib.clm_set_root_extraction(self.h, None, 0))
+            return
+        r = _c(root)
+        self._check(self.lib.clm_set_root_extraction(self.h, A.dptr(r), r.shape[0]))
 
     # -- plumbing -----------------------------------------------------------
     def _check(self, rc):

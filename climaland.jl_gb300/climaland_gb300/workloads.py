@@ -49,6 +49,8 @@ class Workload:
     dt: float
     nsteps: int
     meta: dict = field(default_factory=dict)
+    # root-extraction canopy values (CLM_RX_NFIELDS, ncol), or None
+    root: np.ndarray | None = None
 
     @property
     def ncells(self) -> int:
@@ -93,7 +95,8 @@ class Workload:
             vartheta_l=cells(self.vartheta_l), theta_i=cells(self.theta_i),
             rho_e_int=cells(self.rho_e_int), intF_w=cols(self.intF_w),
             intF_e=cols(self.intF_e), t0=self.t0, dt=self.dt,
-            nsteps=self.nsteps, meta=dict(self.meta))
+            nsteps=self.nsteps, meta=dict(self.meta),
+            root=None if self.root is None else np.ascontiguousarray(self.root[:, c0:c1]))
 
 
 def _forcing(ncol: int) -> np.ndarray:
@@ -419,7 +422,31 @@ def brooks_corey(w: Workload, seed: int = 0) -> Workload:
         z_hi=w.z_hi, params=params, forcing=w.forcing, vartheta_l=v, theta_i=ti,
         rho_e_int=e, intF_w=w.intF_w.copy(),
         intF_e=None if w.intF_e is None else w.intF_e.copy(), t0=w.t0, dt=w.dt,
-        nsteps=w.nsteps, meta=dict(w.meta))
+        nsteps=w.nsteps, meta=dict(w.meta), root=None if w.root is None else w.root.copy())
+
+
+def with_root_extraction(w: Workload, seed: int = 0) -> Workload:
+    """The EnergyHydrology workload with the RootExtraction source: per-column
+    canopy values around the reference's plant-functional-type table
+    (src/standalone/Vegetation/pfts.jl: K_sat_plant = 5e-9 m/s, psi63 =
+    -4 MPa = -408 m, rooting depths 2-3.9 m): canopy psi U[-150, -10] m,
+    LAI U[0.5, 5], RAI U[0.5, 3], height U[1, 20] m, rooting depth
+    U[0.5, 4] m, K_sat_plant 10^U[-9, -8] m/s, psi63 U[-600, -200] m, Weibull
+    c U[2, 5]."""
+    assert w.cfg.model == A.CLM_MODEL_ENERGY_HYDROLOGY
+    rng = np.random.Generator(np.random.PCG64(11000 + seed))
+    r = np.zeros((A.CLM_RX_NFIELDS, w.ncol))
+    r[A.CLM_RX_PSI_CANOPY] = rng.uniform(-150.0, -10.0, w.ncol)
+    r[A.CLM_RX_LAI] = rng.uniform(0.5, 5.0, w.ncol)
+    r[A.CLM_RX_RAI] = rng.uniform(0.5, 3.0, w.ncol)
+    r[A.CLM_RX_HEIGHT] = rng.uniform(1.0, 20.0, w.ncol)
+    r[A.CLM_RX_ROOT_DEPTH] = rng.uniform(0.5, 4.0, w.ncol)
+    r[A.CLM_RX_K_SAT] = 10.0 ** rng.uniform(-9.0, -8.0, w.ncol)
+    r[A.CLM_RX_PSI63] = rng.uniform(-600.0, -200.0, w.ncol)
+    r[A.CLM_RX_WEIBULL_C] = rng.uniform(2.0, 5.0, w.ncol)
+    out = w.columns(0, w.ncol, name=f"{w.name}_roots")
+    out.root = r
+    return out
 
 
 CONFIGS = {

@@ -65,6 +65,7 @@ struct clm_handle {
   int32_t* d_ref_off = nullptr;
   double *d_zlo = nullptr, *d_zhi = nullptr, *d_prm = nullptr, *d_lkap = nullptr;
   double* d_forc[4] = {nullptr, nullptr, nullptr, nullptr};
+  double* d_rx = nullptr;  // root-extraction canopy rows (sorted), or null
   double *d_v = nullptr, *d_ti = nullptr, *d_e = nullptr, *d_Fw = nullptr, *d_Fe = nullptr;
   uint32_t* d_flags = nullptr;
   int32_t* d_iters = nullptr;
@@ -161,6 +162,7 @@ StepArgs step_args(const clm_handle* h) {
   A.prm = h->d_prm;
   A.lkap = h->d_lkap;
   for (int i = 0; i < 4; ++i) A.forc[i] = h->d_forc[i];
+  A.rx = h->d_rx;
   A.v = h->d_v;
   A.ti = h->d_ti;
   A.e = h->d_e;
@@ -590,6 +592,7 @@ void clm_destroy(clm_handle* h) {
   dfree(h->d_tile_off); dfree(h->d_tile_n); dfree(h->d_col_n); dfree(h->d_perm); dfree(h->d_ref_off);
   dfree(h->d_zlo); dfree(h->d_zhi); dfree(h->d_prm); dfree(h->d_lkap);
   for (auto& p : h->d_forc) dfree(p);
+  dfree(h->d_rx);
   dfree(h->d_v); dfree(h->d_ti); dfree(h->d_e); dfree(h->d_Fw); dfree(h->d_Fe);
   dfree(h->d_flags); dfree(h->d_iters); dfree(h->d_stage); dfree(h->d_colstage); dfree(h->d_guess);
   dfree(h->d_scratch);
@@ -704,6 +707,39 @@ int clm_set_bc(clm_handle* h, int32_t slot, const double* f, int32_t nfields) {
   }
   CLM_CUDA(h, cudaMemsetAsync(h->d_forc[slot], 0, sizeof(double) * h->stride * CLM_F_NFIELDS, h->stream));
   int rc = upload_cols_sorted(h, f, h->d_forc[slot], nfields);
+  if (rc != CLM_OK) return rc;
+  CLM_CUDA(h, cudaStreamSynchronize(h->stream));
+  return CLM_OK;
+}
+
+int clm_set_root_extraction(clm_handle* h, const double* r, int32_t nfields) {
+  if (!h) return CLM_ERR_ARG;
+  if (!h->have_geometry) return fail(h, CLM_ERR_STATE, "clm_set_geometry has not been called");
+  if (!r) {
+    if (h->d_rx) drop_graphs(h);
+    dfree(h->d_rx);
+    return CLM_OK;
+  }
+  if (!is_eh(h))
+    return fail(h, CLM_ERR_ARG, "root extraction is an EnergyHydrology source");
+  if (nfields != CLM_RX_NFIELDS) return fail(h, CLM_ERR_ARG, "expected CLM_RX_NFIELDS rows");
+  const int ncol = h->ncol;
+  for (int64_t i = 0; i < (int64_t)nfields * ncol; ++i)
+    if (!std::isfinite(r[i])) return fail(h, CLM_ERR_ARG, "non-finite root-extraction value");
+  for (int c = 0; c < ncol; ++c) {
+    const double lai = r[CLM_RX_LAI * ncol + c], rai = r[CLM_RX_RAI * ncol + c];
+    const double ht = r[CLM_RX_HEIGHT * ncol + c], d = r[CLM_RX_ROOT_DEPTH * ncol + c];
+    const double ks = r[CLM_RX_K_SAT * ncol + c], p63 = r[CLM_RX_PSI63 * ncol + c];
+    const double wc = r[CLM_RX_WEIBULL_C * ncol + c];
+    if (!(lai >= 0) || !(rai >= 0) || !(ht > 0) || !(d > 0) || !(ks >= 0) || !(p63 < 0) || !(wc > 0))
+      return fail(h, CLM_ERR_ARG, "invalid root-extraction values in column " + std::to_string(c));
+  }
+  if (!h->d_rx) {
+    drop_graphs(h);
+    CLM_CUDA(h, cudaMalloc(&h->d_rx, sizeof(double) * h->stride * CLM_RX_NFIELDS));
+    CLM_CUDA(h, cudaMemsetAsync(h->d_rx, 0, sizeof(double) * h->stride * CLM_RX_NFIELDS, h->stream));
+  }
+  int rc = upload_cols_sorted(h, r, h->d_rx, nfields);
   if (rc != CLM_OK) return rc;
   CLM_CUDA(h, cudaStreamSynchronize(h->stream));
   return CLM_OK;

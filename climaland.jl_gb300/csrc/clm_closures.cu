@@ -135,8 +135,13 @@ __device__ void closure_column(const ClosureArgs& C, const Tables& Tb) {
     return;
   }
   if (KIND == CL_EXP) {
+    // PhaseChange, then RootExtraction (soil_canopy_root_interactions.jl:139-159)
+    const bool roots = eh && A.rx;
+    RootCol rcol;
+    if (roots) rcol = load_root_col(Tb, A.rx, st, s);
+    double root_w = 0.0, root_e = 0.0;
     for (int k = 0; k < n; ++k) {
-      double dv = 0.0, dti = 0.0;
+      double dv = 0.0, dti = 0.0, de = 0.0;
       if (eh && A.phase_change) {
         const double Yti = C.ti[o + k];
         const double rc = heat_capacity(E, tlc[k], Yti, rcds);
@@ -145,12 +150,23 @@ __device__ void closure_column(const ClosureArgs& C, const Tables& Tb) {
         dv = -pc;
         dti = E.rho_l_over_rho_i * pc;
       }
+      if (roots) {
+        const double zlo = A.z_lo[s], zhi = A.z_hi[s];
+        const double zc = 0.5 * ((zlo + (zhi - zlo) * ((double)k / n)) +
+                                 (k + 1 == n ? zhi : zlo + (zhi - zlo) * ((double)(k + 1) / n)));
+        const double re = root_rate(Tb, rcol, zc, psic[k], Kc[k]);
+        const double ree = re * rho_e_liq(E, Tc[k]);
+        dv += -1.0 * re;
+        de += -1.0 * ree;
+        root_e += dz * ree;
+        root_w += dz * re;
+      }
       if (C.dv) C.dv[o + k] = dv;
       if (eh && C.dti) C.dti[o + k] = dti;
-      if (eh && C.de) C.de[o + k] = 0.0;
+      if (eh && C.de) C.de[o + k] = de;
     }
-    if (C.dFw) C.dFw[orig] = 0.0;
-    if (eh && C.dFe) C.dFe[orig] = 0.0;
+    if (C.dFw) C.dFw[orig] = root_w;
+    if (eh && C.dFe) C.dFe[orig] = root_e;
     return;
   }
   if (KIND == CL_IMP) {

@@ -254,6 +254,11 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
     double K0 = 0, T0 = 0, kap0 = 0, psi0 = 0;
     double Kt = 0, Tt = 0, kapt = 0, psit = 0;
     double kap_prev = 0.0, K_prev = 0.0;
+    // RootExtraction (soil_canopy_root_interactions.jl:8-39, 139-159): the
+    // explicit source at Y_n and its column integrals for intF_w / intF_e
+    RootCol rcol;
+    if (A.rx) rcol = load_root_col(Tb, A.rx, st, s);
+    double root_w = 0.0, root_e = 0.0;
     for (int k = 0; k < n; ++k) {
       const double Yv = B.gv[k], Yti = B.gti[k], Ye = B.ge[k];
       const double nu_eff = c.nu - Yti;
@@ -290,13 +295,28 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         const double lnf = -sc.omega_ln10 * fi + sc.visc_gamma * (T - sc.visc_gamma_T_ref);
         K = conductivity_scaled(Tb, c.g, c.K_sat, SK, lnf);
       }
-      double Uv = Yv, Uti = Yti;
+      double Uv = Yv, Uti = Yti, Ue = Ye;
+      double pc = 0.0;
       if (A.phase_change) {
-        const double pc =
-            mixed ? phase_change_reduced(Tb, E, c.g, c.nu, c.theta_r, pcc, tl, Yti, T, inv_rc, kap)
-                  : phase_change_r(Tb, E, c.g, c.nu, c.theta_r, pcc, tl, Yti, T, inv_rc, kap, flags);
+        pc = mixed ? phase_change_reduced(Tb, E, c.g, c.nu, c.theta_r, pcc, tl, Yti, T, inv_rc, kap)
+                   : phase_change_r(Tb, E, c.g, c.nu, c.theta_r, pcc, tl, Yti, T, inv_rc, kap, flags);
         Uv = Yv + dt * (-pc);
         Uti = Yti + dt * (E.rho_l_over_rho_i * pc);
+      }
+      if (A.rx) {
+        // psi at Y_n (update_aux!), the layer centre z, K and T of this stage
+        double psi_n, d;
+        psi_dpsi<false>(Tb, c.g, nu_eff, Yv, c.theta_r, c.S_s, psi_n, d);
+        const double zc = 0.5 * ((A.z_lo[s] + (A.z_hi[s] - A.z_lo[s]) * ((double)k / n)) +
+                                 (k + 1 == n ? A.z_hi[s]
+                                             : A.z_lo[s] + (A.z_hi[s] - A.z_lo[s]) * ((double)(k + 1) / n)));
+        const double re = root_rate(Tb, rcol, zc, psi_n, K);
+        const double ree = re * rho_e_liq(E, T);
+        Uv = Yv + dt * ((-pc) + (-1.0 * re));  // sources in the reference's order
+        Ue = Ye + dt * (-1.0 * ree);
+        root_e += c.dz * ree;
+        root_w += c.dz * re;
+        B.ge[k] = Ue;
       }
       B.gv[k] = Uv;
       B.gti[k] = Uti;
@@ -307,14 +327,14 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         // a layer whose guess leaves the retention curve's domain
         // (vartheta_l <= theta_r) or is not finite starts from U
         if (!(xv0 > c.theta_r + kSqrtEps) || !isfinite(xv0)) xv0 = Uv;
-        if (!isfinite(xe0)) xe0 = Ye;
+        if (!isfinite(xe0)) xe0 = Ue;
         B.xv[k] = xv0;
         B.xe[k] = xe0;
-        const double dv = xv0 - Uv, de = A.energy_scale * (xe0 - Ye);
+        const double dv = xv0 - Uv, de = A.energy_scale * (xe0 - Ue);
         pred2 += dv * dv + de * de;
       } else {
         B.xv[k] = Uv;
-        B.xe[k] = Ye;
+        B.xe[k] = Ue;
       }
       B.K[k] = K;
       // face conductances k-1|k, frozen through the Newton solve: kappa on
@@ -390,7 +410,8 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         Fbh = fbh;
       }
     }
-    const double UFw = Fw, UFe = Fe;
+    const double UFw = A.rx ? Fw + dt * root_w : Fw;
+    const double UFe = A.rx ? Fe + dt * root_e : Fe;
     double xFw = UFw, xFe = UFe;
 
     // ---------------- stage 2: Newton ------------------------------------

@@ -53,6 +53,7 @@ struct StepArgs {
   int phase_change;
   int runoff;           // enum clm_runoff (CLM_BC_PRECIP_RUNOFF)
   int cm = CLM_CM_VAN_GENUCHTEN;  // enum clm_hydrology_cm
+  const double* rx = nullptr;     // root-extraction canopy rows [CLM_RX_NFIELDS][stride], or null
   int newton_mode;
   int max_iters;
   double tol;

@@ -498,6 +498,40 @@ CLM_HD double phase_change_reduced(const Tables& T, const Earth& E, const CM& g,
   return (theta_l - theta_star) * kappa * inv_rhoc * pcc.inv_3dz2;
 }
 
+// Root extraction of one column (src/integrated/soil_canopy_root_interactions.jl:8-39):
+// the per-column canopy factors and the per-layer rate
+//   re = hm(LAI, RAI) water_flux(z, h/2, psi_soil, psi_c, K_soil, K_c) root_distribution(z, d)
+// with hm(x, y) = x y / max(x + y, eps) (plant_hydraulics.jl:170), water_flux =
+// -hm(K1, K2) ((psi2 - psi1) / (z2 - z1) + 1) (:197-201), the Weibull plant
+// conductivity K_c (:256-267) and root_distribution = exp(z / d) / d
+// (biomass.jl:362-364).
+CLM_HD double harmonic_mean(double x, double y) { return x * y / fmax(x + y, kEps); }
+
+struct RootCol {
+  double psi_c, hm_LR, z2, inv_d, K_c;
+};
+
+CLM_HD RootCol load_root_col(const Tables& T, const double* R, int stride, int s) {
+  RootCol r;
+  r.psi_c = R[CLM_RX_PSI_CANOPY * stride + s];
+  r.hm_LR = harmonic_mean(R[CLM_RX_LAI * stride + s], R[CLM_RX_RAI * stride + s]);
+  r.z2 = R[CLM_RX_HEIGHT * stride + s] / 2.0;
+  r.inv_d = 1.0 / R[CLM_RX_ROOT_DEPTH * stride + s];
+  const double Ksat = R[CLM_RX_K_SAT * stride + s];
+  r.K_c = (r.psi_c <= 0.0)
+              ? fm::exp(T, -fm::exp(T, R[CLM_RX_WEIBULL_C * stride + s] *
+                                           fm::log(T, r.psi_c / R[CLM_RX_PSI63 * stride + s]))) *
+                    Ksat
+              : Ksat;
+  return r;
+}
+
+CLM_HD double root_rate(const Tables& T, const RootCol& r, double z, double psi_soil,
+                        double K_soil) {
+  const double flux = -harmonic_mean(K_soil, r.K_c) * ((r.psi_c - psi_soil) / (r.z2 - z) + 1.0);
+  return r.hm_LR * flux * (r.inv_d * fm::exp(T, z * r.inv_d));
+}
+
 // counter hash of the rain-pulse forcing (splitmix64 finaliser, Vigna):
 // identical integer arithmetic on host and device.
 CLM_HD uint64_t mix64(uint64_t z) {

@@ -172,6 +172,35 @@ enum clm_bc_slot {
   CLM_BC_BOTTOM_HEAT = 3
 };
 
+/* Root extraction (EnergyHydrology with the RootExtraction source:
+ * src/integrated/soil_canopy_root_interactions.jl:8-39, 139-159). Per-column
+ * canopy values for clm_set_root_extraction (SoA, row f of ncol), held by
+ * the caller's canopy model and frozen through a step. Each layer at centre
+ * z loses (explicit stage)
+ *   re = hm(LAI, RAI) water_flux(z, h/2, psi_soil, psi_canopy, K_soil,
+ *        K_canopy(psi_canopy)) root_distribution(z, rooting_depth)     (1/s)
+ * with hm(x, y) = x y / max(x + y, eps), water_flux = -hm(K1, K2) ((psi2 -
+ * psi1) / (z2 - z1) + 1) (plant_hydraulics.jl:170, 197-201), the Weibull
+ * conductivity K_sat exp(-(psi / psi63)^c) for psi <= 0, K_sat otherwise
+ * (:256-267), root_distribution = exp(z / d) / d (biomass.jl:362-364), and
+ * psi_soil, K_soil, T_soil the update_aux values at the step's start; rho e_int
+ * loses re rho c_l (T_soil - T_0). As in the reference, the integrated fluxes
+ * gain the column integrals of both (d intF_w += sum dz re, d intF_e += sum dz
+ * re rho e_l): the reference adds the water extraction to intF_w with the
+ * sign opposite to the state's change, so its water budget drifts by
+ * 2 dt sum dz re per step; the library reproduces that. */
+enum clm_root_field {
+  CLM_RX_PSI_CANOPY = 0,  /* p.canopy.hydraulics.psi (m)                    */
+  CLM_RX_LAI = 1,         /* leaf area index                                */
+  CLM_RX_RAI = 2,         /* root area index                                */
+  CLM_RX_HEIGHT = 3,      /* canopy height (m); the flux runs to h / 2      */
+  CLM_RX_ROOT_DEPTH = 4,  /* rooting depth (m)                              */
+  CLM_RX_K_SAT = 5,       /* Weibull K_sat of the plant (m/s)               */
+  CLM_RX_PSI63 = 6,       /* Weibull psi63 (m, < 0)                         */
+  CLM_RX_WEIBULL_C = 7,   /* Weibull c (> 0)                                */
+  CLM_RX_NFIELDS = 8
+};
+
 /* Physical constants (ClimaLand.Parameters.LandParameters,
  * src/shared_utilities/Parameters.jl:11-115). The Julia caller passes the
  * values of its own earth_param_set; clm_config_default fills ClimaParams
@@ -249,6 +278,13 @@ int clm_set_params(clm_handle* h, const double* soa_params, int32_t nparams);
  * bc closures evaluated by boundary_flux! (boundary_conditions.jl:168-608). */
 int clm_set_bc(clm_handle* h, int32_t slot, const double* soa_forcing,
                int32_t nfields);
+
+/* Root-extraction canopy values, CLM_RX_NFIELDS rows of ncol (enum
+ * clm_root_field), or NULL to remove the source. Replaces the RootExtraction
+ * source and update_root_extraction! (soil_canopy_root_interactions.jl:8-39,
+ * 123-159). EnergyHydrology only (the reference defines the source for it
+ * alone); the caller refreshes the values when its canopy state changes. */
+int clm_set_root_extraction(clm_handle* h, const double* soa, int32_t nfields);
 
 /* Prognostic state Y.soil (energy_hydrology.jl:624-625, rre.jl:282).
  * theta_i, rho_e, intF_e may be NULL for RichardsModel. */

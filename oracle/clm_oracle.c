@@ -179,6 +179,34 @@ static double hcm_hydraulic_conductivity(const hcm_t* h, double K_sat, double S)
                : clmo_hydraulic_conductivity(h->m, K_sat, S);
 }
 
+/* ======================================================================
+ * Root extraction helpers: src/standalone/Vegetation
+ * ====================================================================== */
+
+/* plant_hydraulics.jl:170 */
+double clmo_harmonic_mean(double x, double y) {
+  return x * y / fmax(x + y, EPS64);
+}
+
+/* plant_hydraulics.jl:197-201 */
+double clmo_plant_water_flux(double z1, double z2, double psi1, double psi2,
+                             double K1, double K2) {
+  double K_eff = clmo_harmonic_mean(K1, K2);
+  return -K_eff * ((psi2 - psi1) / (z2 - z1) + 1.0);
+}
+
+/* plant_hydraulics.jl:256-267 (Weibull) */
+double clmo_weibull_conductivity(double K_sat, double psi63, double c,
+                                 double psi) {
+  double K = (psi <= 0.0) ? exp(-pow(psi / psi63, c)) : 1.0;
+  return K * K_sat;
+}
+
+/* biomass.jl:362-364 */
+double clmo_root_distribution(double z, double rooting_depth) {
+  return (1.0 / rooting_depth) * exp(z / rooting_depth);
+}
+
 /* :302-305 */
 double clmo_impedance_factor(double f_i, double Omega) {
   return pow(10.0, -Omega * f_i);
@@ -409,6 +437,8 @@ typedef struct { /* p.soil */
   double dfluxBCdY;
   double total_water, total_energy;
   int psi_positive;
+  /* RootExtraction (soil_canopy_root_interactions.jl:8-39) */
+  double root_extraction[MAXL], root_energy_extraction[MAXL];
 } cache_t;
 
 typedef struct {
@@ -703,12 +733,15 @@ static void update_boundary_fluxes(const col_t* C, const state_t* Y,
 }
 
 /* make_update_cache = update_aux! + update_boundary_fluxes! */
+static void root_extraction(const col_t* C, cache_t* p);
+
 static void update_cache(const col_t* C, const state_t* Y, cache_t* p,
                          double t) {
   if (C->eh)
     eh_update_aux(C, Y, p);
   else
     richards_update_aux(C, Y, p);
+  if (C->eh && C->P->root) root_extraction(C, p);
   update_boundary_fluxes(C, Y, p, t);
 }
 
@@ -727,6 +760,31 @@ static void update_implicit_cache(const col_t* C, const state_t* Y,
 
 /* compute_exp_tendency!: rre.jl:214-243; energy_hydrology.jl:315-350 and
  * the PhaseChange source!: energy_hydrology.jl:838-906. */
+/* update_root_extraction! (soil_canopy_root_interactions.jl:8-39), part of
+ * the land model's update_boundary_fluxes! (soil_canopy_model.jl:266-268):
+ * at the explicit stage only, from the soil aux psi, K, T of update_aux!. */
+static void root_extraction(const col_t* C, cache_t* p) {
+  const clmo_problem* P = C->P;
+  const clm_earth_params* e = &C->cfg->earth;
+  int ncol = P->ncol, c = C->c;
+  const double* R = P->root;
+  double psi_c = R[CLM_RX_PSI_CANOPY * ncol + c];
+  double LAI = R[CLM_RX_LAI * ncol + c], RAI = R[CLM_RX_RAI * ncol + c];
+  double h = R[CLM_RX_HEIGHT * ncol + c], rd = R[CLM_RX_ROOT_DEPTH * ncol + c];
+  double K_can = clmo_weibull_conductivity(R[CLM_RX_K_SAT * ncol + c],
+                                           R[CLM_RX_PSI63 * ncol + c],
+                                           R[CLM_RX_WEIBULL_C * ncol + c], psi_c);
+  for (int k = 0; k < C->n; ++k) {
+    double re = clmo_harmonic_mean(LAI, RAI) *
+                clmo_plant_water_flux(C->z[k], h / 2.0, p->psi[k], psi_c,
+                                      p->K[k], K_can) *
+                clmo_root_distribution(C->z[k], rd);
+    p->root_extraction[k] = re;
+    p->root_energy_extraction[k] =
+        re * clmo_volumetric_internal_energy_liq(p->T[k], e);
+  }
+}
+
 static void exp_tendency(const col_t* C, const state_t* Y, cache_t* p,
                          state_t* dY) {
   int n = C->n;
@@ -747,6 +805,19 @@ static void exp_tendency(const col_t* C, const state_t* Y, cache_t* p,
       dY->v[k] += -src;
       dY->ti[k] += (e->rho_l / e->rho_i) * src;
     }
+  }
+  /* RootExtraction source! (soil_canopy_root_interactions.jl:139-159), after
+   * PhaseChange in the sources tuple */
+  if (C->eh && C->P->root) {
+    double sw = 0.0, se = 0.0;
+    for (int k = 0; k < n; ++k) {
+      dY->v[k] += -1.0 * p->root_extraction[k];
+      dY->e[k] += -1.0 * p->root_energy_extraction[k];
+    }
+    for (int k = 0; k < n; ++k) se += C->dzc[k] * p->root_energy_extraction[k];
+    dY->Fe += se;
+    for (int k = 0; k < n; ++k) sw += C->dzc[k] * p->root_extraction[k];
+    dY->Fw += sw;
   }
 }
 
@@ -981,6 +1052,7 @@ static int check_problem(const clmo_problem* P) {
   int need = P->cfg.model == CLM_MODEL_ENERGY_HYDROLOGY ? CLM_NPARAM_EH
                                                         : CLM_NPARAM_RICHARDS;
   if (P->nparams < need) return CLM_ERR_ARG;
+  if (P->root && P->cfg.model != CLM_MODEL_ENERGY_HYDROLOGY) return CLM_ERR_ARG;
   if (P->cfg.hydrology_cm != CLM_CM_VAN_GENUCHTEN &&
       P->cfg.hydrology_cm != CLM_CM_BROOKS_COREY)
     return CLM_ERR_ARG;

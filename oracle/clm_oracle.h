@@ -30,6 +30,8 @@ typedef struct clmo_problem {
   int32_t nparams;
   const double* forcing[4];/* CLM_F_NFIELDS x ncol per slot (NULL: zero)  */
   int32_t nthreads;        /* OpenMP threads (<= 0: library default)      */
+  const double* root;      /* CLM_RX_NFIELDS x ncol root-extraction canopy
+                              values (EnergyHydrology), or NULL            */
 } clmo_problem;
 
 /* ---- pointwise physics (names follow the reference functions) -------- */
@@ -55,6 +57,13 @@ double clmo_bc_dpsidvartheta(double c, double psib, double vartheta,
                              double nu_eff, double theta_r, double S_s);
 double clmo_bc_hydraulic_conductivity(double c, double K_sat, double S);
 double clmo_impedance_factor(double f_i, double Omega);
+/* canopy helpers of root extraction (src/standalone/Vegetation) */
+double clmo_harmonic_mean(double x, double y);
+double clmo_plant_water_flux(double z1, double z2, double psi1, double psi2,
+                             double K1, double K2);
+double clmo_weibull_conductivity(double K_sat, double psi63, double c,
+                                 double psi);
+double clmo_root_distribution(double z, double rooting_depth);
 double clmo_viscosity_factor(double T, double gamma, double gamma_T_ref);
 double clmo_heaviside(double x, double a);
 double clmo_soil_Tf_depressed(double theta_l, double theta_i, double nu,

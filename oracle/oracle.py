@@ -45,6 +45,7 @@ class _Problem(ctypes.Structure):
         ("nparams", ctypes.c_int32),
         ("forcing", ctypes.POINTER(ctypes.c_double) * 4),
         ("nthreads", ctypes.c_int32),
+        ("root", ctypes.POINTER(ctypes.c_double)),
     ]
 
 
@@ -76,6 +77,10 @@ def lib():
             "clmo_bc_dpsidvartheta": [_D] * 6,
             "clmo_bc_hydraulic_conductivity": [_D] * 3,
             "clmo_impedance_factor": [_D] * 2,
+            "clmo_harmonic_mean": [_D] * 2,
+            "clmo_plant_water_flux": [_D] * 6,
+            "clmo_weibull_conductivity": [_D] * 4,
+            "clmo_root_distribution": [_D] * 2,
             "clmo_viscosity_factor": [_D] * 3,
             "clmo_heaviside": [_D] * 2,
             "clmo_soil_Tf_depressed": [_D] * 12,
@@ -157,6 +162,8 @@ class Oracle:
             f = w.forcing.get(slot)
             P.forcing[slot] = A.dptr(keep(f)) if f is not None else None
         P.nthreads = int(nthreads if nthreads else (os.cpu_count() or 1))
+        root = getattr(w, "root", None)
+        P.root = A.dptr(keep(root)) if root is not None else None
         self.P = P
         self.eh = w.cfg.model == A.CLM_MODEL_ENERGY_HYDROLOGY
 

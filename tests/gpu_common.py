@@ -106,7 +106,8 @@ def gpu_run(w, nsteps, **dev_kw):
     return sg, fg, ig, Wg, Eg
 
 
-def check_parity(w, nsteps, oracle_cfg=None, spread=True, tol_state=TOL_STATE, noise=None, **dev_kw):
+def check_parity(w, nsteps, oracle_cfg=None, spread=True, tol_state=TOL_STATE, noise=None,
+                 nseeds=NSEEDS, **dev_kw):
     """Run the oracle and the GPU on the same workload and apply the
     criterion above. Returns a stats dict."""
     so, fo, io = oracle_run(w, nsteps, oracle_cfg)
@@ -115,7 +116,7 @@ def check_parity(w, nsteps, oracle_cfg=None, spread=True, tol_state=TOL_STATE, n
     errs = [_colmax(w, r, g) for r, g in zip(ref, got)]
     names = ["vartheta_l", "theta_i", "rho_e_int_rel"][: len(errs)]
     if spread:
-        spr, bspr = oracle_spread(w, nsteps, so, oracle_cfg, noise=noise)
+        spr, bspr = oracle_spread(w, nsteps, so, oracle_cfg, nseeds=nseeds, noise=noise)
     else:
         spr = [np.zeros(w.ncol) for _ in errs]
         bspr = [np.zeros(w.ncol), np.zeros(w.ncol)]

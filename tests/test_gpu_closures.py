@@ -34,6 +34,7 @@ WORKLOADS = {
     "c4": lambda: WL.full_scale_c4(ncol=256),
     "richards_bc": lambda: WL.brooks_corey(WL.richards_c0(ncol=256)),
     "c4_bc": lambda: WL.brooks_corey(WL.full_scale_c4(ncol=256)),
+    "c4_roots": lambda: WL.with_root_extraction(WL.full_scale_c4(ncol=256)),
 }
 
 

@@ -191,6 +191,73 @@ def test_brooks_corey_columns_use_the_closure(L):
     assert rc == A.CLM_ERR_ARG
 
 
+# --- root extraction: test/standalone/Vegetation/plant_hydraulics_test.jl ---
+
+def test_weibull_plant_conductivity(L):
+    # :17-44: psi from the linear retention curve (plant_hydraulics.jl:301-316)
+    # at S_l = 0.7, 0.9, 1.0, 1.1; K = min(K_sat exp(-(psi/psi63)^c), K_sat)
+    # to 2 eps
+    nu, S_s, K_sat, psi63, c, a = 0.5, 1e-2, 1.8e-8, -4 / 0.0098, 4.0, 0.05 * 0.0098
+    for S_l in (0.7, 0.9, 1.0, 1.1):
+        psi = (S_l - 1.0) / a if S_l <= 1.0 else (S_l * nu - nu) / S_s
+        got = L.clmo_weibull_conductivity(K_sat, psi63, c, psi)
+        assert abs(got - min(K_sat * math.exp(-(psi / psi63) ** c), K_sat)) < 2 * EPS
+
+
+def test_root_extraction_helpers(L):
+    # plant_hydraulics.jl:170 (zero when either argument is), :197-201;
+    # biomass.jl:362-364
+    assert L.clmo_harmonic_mean(2.0, 3.0) == 2.0 * 3.0 / 5.0
+    assert L.clmo_harmonic_mean(0.0, 0.0) == 0.0 and L.clmo_harmonic_mean(0.0, 4.0) == 0.0
+    K1, K2, z1, z2, p1, p2 = 1e-6, 5e-9, -0.4, 2.5, -3.0, -80.0
+    Keff = K1 * K2 / (K1 + K2)
+    assert approx(L.clmo_plant_water_flux(z1, z2, p1, p2, K1, K2), -Keff * ((p2 - p1) / (z2 - z1) + 1.0))
+    # hydrostatic: psi2 - psi1 = -(z2 - z1) gives no flux
+    assert abs(L.clmo_plant_water_flux(z1, z2, p1, p1 - (z2 - z1), K1, K2)) < 1e-22
+    assert approx(L.clmo_root_distribution(-0.5, 2.0), math.exp(-0.25) / 2.0)
+
+
+def test_root_extraction_source_in_the_step(L):
+    """RootExtraction (soil_canopy_root_interactions.jl:8-39, 139-159): the
+    explicit tendency loses re = hm(LAI, RAI) water_flux(z, h/2, psi, psi_c,
+    K, K_c) root_distribution(z, d) in vartheta_l and re rho e_l(T) in
+    rho e_int, with psi, K, T of update_aux at the same state, and the
+    integrated fluxes gain their column integrals (the reference's sign)."""
+    w = WL.with_root_extraction(WL.energy_hydrology_c1(ncol=8, nlayers=6))
+    w0 = WL.energy_hydrology_c1(ncol=8, nlayers=6)
+    st = w.copy_state()
+    o, o0 = O.Oracle(w), O.Oracle(w0)
+    aux = o.update_cache(st, 0.0)
+    d, d0 = o.exp_tendency(st, 0.0), o0.exp_tendency(w0.copy_state(), 0.0)
+    n = int(w.nlayers[0])
+    E_ = A.DEFAULT_EARTH
+    for c in range(w.ncol):
+        R = w.root[:, c]
+        zlo, zhi = w.z_lo[c], w.z_hi[c]
+        zf = zlo + (zhi - zlo) * np.arange(n + 1) / n
+        zf[-1] = zhi
+        z = 0.5 * (zf[:-1] + zf[1:])
+        sl = slice(c * n, (c + 1) * n)
+        psi_c = R[A.CLM_RX_PSI_CANOPY]
+        Kc = R[A.CLM_RX_K_SAT] * math.exp(-(psi_c / R[A.CLM_RX_PSI63]) ** R[A.CLM_RX_WEIBULL_C])
+        hm = lambda x, y: x * y / max(x + y, EPS)
+        K = aux["K"][sl]
+        Keff = K * Kc / np.maximum(K + Kc, EPS)
+        re = (hm(R[A.CLM_RX_LAI], R[A.CLM_RX_RAI]) * (-Keff * ((psi_c - aux["psi"][sl]) / (R[A.CLM_RX_HEIGHT] / 2 - z) + 1.0))
+              * np.exp(z / R[A.CLM_RX_ROOT_DEPTH]) / R[A.CLM_RX_ROOT_DEPTH])
+        ree = re * E_["cp_l"] * E_["rho_l"] * (aux["T"][sl] - E_["T_0"])
+        assert approx(d[0][sl] - d0[0][sl], -re, rtol=1e-9, atol=1e-22)
+        assert approx(d[2][sl] - d0[2][sl], -ree, rtol=1e-9, atol=1e-12)
+        dz = (zhi - zlo) / n
+        assert approx(d[3][c] - d0[3][c], np.sum(dz * re), rtol=1e-9, atol=1e-25)
+        assert approx(d[4][c] - d0[4][c], np.sum(dz * ree), rtol=1e-9, atol=1e-15)
+    # the reference defines the source for EnergyHydrology only
+    r = WL.richards_c0(ncol=4, nlayers=5)
+    r.root = np.ones((A.CLM_RX_NFIELDS, 4))
+    rc, _, _ = O.Oracle(r).step(r.copy_state(), 0.0, 1.0, 1)
+    assert rc == A.CLM_ERR_ARG
+
+
 # --- :283-495 freezing and thawing -----------------------------------------
 
 def _ft_case(L, earth, theta_l, theta_i, T):
