@@ -30,6 +30,7 @@ const CLM_BC_PRECIP_RUNOFF = Int32(4)
 const CLM_CM_VAN_GENUCHTEN = Int32(0)
 const CLM_CM_BROOKS_COREY = Int32(1)
 const CLM_F_NFIELDS = 8
+const CLM_RX_NFIELDS = 8
 
 struct ClmEarthParams
     rho_l::Float64
@@ -142,6 +143,19 @@ end
 set_params!(h::Handle, p::Matrix{Float64}) =
     check(h, ccall((:clm_set_params, libclm), Cint, (Ptr{Cvoid}, Ptr{Float64}, Int32),
         h.ptr, permutedims(p), size(p, 1)))
+
+"""
+    set_root_extraction!(h, r)
+
+Root-extraction canopy values as a (CLM_RX_NFIELDS × ncol) matrix (rows:
+canopy ψ, LAI, RAI, height, rooting depth, Weibull K_sat, ψ63, c), or
+`nothing` to remove the source. From a ClimaLand `CanopyModel`: `p.canopy.hydraulics.ψ`,
+`p.canopy.biomass.area_index.leaf` / `.root`, `canopy.biomass.height`,
+`canopy.biomass.rooting_depth` and `canopy.hydraulics.parameters.conductivity_model`.
+"""
+set_root_extraction!(h::Handle, r::Union{Nothing, Matrix{Float64}}) =
+    check(h, ccall((:clm_set_root_extraction, libclm), Cint, (Ptr{Cvoid}, Ptr{Float64}, Int32),
+        h.ptr, r === nothing ? C_NULL : permutedims(r), r === nothing ? 0 : size(r, 1)))
 
 "Forcing descriptor for one boundary slot as a (CLM_F_NFIELDS × ncol) matrix."
 set_bc!(h::Handle, slot::Integer, f::Matrix{Float64}) =
