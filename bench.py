@@ -17,6 +17,7 @@ Prints one JSON line (rank 0). Metric: column-steps/s.
             wall clock): per step the state is copied in from pinned host
             memory, stepped, and copied back, pipelined over column chunks
   roofline  dominant kernel (the step kernel) against the measured HBM peak
+  compute_bound  the FP64 pipe's busy fraction for that kernel (committed ncu capture)
   cpu_baseline  the FP64 CPU oracle on a bounded sample, all host threads
 """
 from __future__ import annotations
@@ -435,6 +436,14 @@ def main():
                 "frac": achieved / peaks["hbm_gbs"], "traffic": traffic,
                 "peak_source": peaks["source"], "kernel": key,
                 "bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_s * 1e3}
+    # the resource that bounds the step kernel (its HBM fraction is small by
+    # arithmetic intensity): the FP64 pipe's busy fraction and FP64
+    # instructions per cell-step from the committed ncu capture
+    compute = None
+    if prof and prof.get("fp64_pipe_pct_active"):
+        compute = {"pipe": "fp64", "active_frac": prof["fp64_pipe_pct_active"] / 100.0,
+                   "fp64_inst_per_cell_step": prof.get("fp64_inst_per_cell_step"),
+                   "source": f"profiles/{key}.json (ncu, 262,144-column launch)"}
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_baseline(w, args.cpu_sample_cols, args.cpu_sample_steps)
@@ -456,6 +465,7 @@ def main():
         "gpu_launches": args.steps,
         "launch_config": dict(g.launch_config(), autotuned=tune is not None),
         "roofline": roofline,
+        "compute_bound": compute,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "status": {"flagged_columns": int(np.count_nonzero(flags)),
