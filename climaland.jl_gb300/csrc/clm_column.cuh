@@ -117,7 +117,7 @@ CLM_HD void eh_iterate_point(const Tables& Tb, const Earth& E, const EHCol<CM>& 
                              double xe, double ti, double inv, double& T, double& psi,
                              double& D) {
   const double nu_eff = c.nu - ti;
-  T = temperature(E, xe, ti, heat_capacity(E, fmin(nu_eff, xv), ti, c.rcds));
+  T = E.T_0 + (xe + ti * E.rho_i_LH_f0) * fm::rcp(heat_capacity(E, fmin(nu_eff, xv), ti, c.rcds));
   psi_dpsi_r<true>(Tb, c.g, nu_eff, inv, xv, c.theta_r, c.inv_S_s, psi, D);
 }
 
@@ -216,12 +216,22 @@ CLM_HD double from_jt(JT x) {
     return x;
 }
 
+// 1 / pivot of the Thomas recurrences: the Newton-Raphson FP64 reciprocal,
+// or the float quotient on the mixed path.
+template <typename JT>
+CLM_HD JT rcp_jt(JT x) {
+  if constexpr (sizeof(JT) < sizeof(double))
+    return 1.0f / x;
+  else
+    return fm::rcp(x);
+}
+
 template <typename JT>
 struct EHJac {
   Col<JT> cp, dp, d, ae;            // Thomas c', d' (then delta_v, d''), dpsi, face coef
 };
 
-template <typename JT, class CM, bool kLogKappaHere = false>
+template <typename JT, class CM, bool kLogKappaHere = false, bool kRoots = false>
 CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int orig,
                       const EHBuffers& B, const EHJac<JT>& J, double t0, double dt, int nsteps,
                       double& Fw, double& Fe, uint32_t& flags, int& iters_done) {
@@ -257,7 +267,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
     // RootExtraction (soil_canopy_root_interactions.jl:8-39, 139-159): the
     // explicit source at Y_n and its column integrals for intF_w / intF_e
     RootCol rcol;
-    if (A.rx) rcol = load_root_col(Tb, A.rx, st, s);
+    if constexpr (kRoots) rcol = load_root_col(Tb, A.rx, st, s);
     double root_w = 0.0, root_e = 0.0;
     for (int k = 0; k < n; ++k) {
       const double Yv = B.gv[k], Yti = B.gti[k], Ye = B.ge[k];
@@ -268,7 +278,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       const double tl = (v_safe < nu_safe) ? v_safe : nu_safe;
       const double rc = heat_capacity(E, tl, Yti, c.rcds);
       // one reciprocal of rho c for T and the phase change
-      const double inv_rc = 1.0 / rc;
+      const double inv_rc = fm::rcp(rc);
       const double T = E.T_0 + (Ye + Yti * E.rho_i_LH_f0) * inv_rc;
       double kap = 0.0, K = 0.0;
       bool aux_ff = false;
@@ -303,7 +313,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         Uv = Yv + dt * (-pc);
         Uti = Yti + dt * (E.rho_l_over_rho_i * pc);
       }
-      if (A.rx) {
+      if constexpr (kRoots) {
         // psi at Y_n (update_aux!), the layer centre z, K and T of this stage
         double psi_n, d;
         psi_dpsi<false>(Tb, c.g, nu_eff, Yv, c.theta_r, c.S_s, psi_n, d);
@@ -354,7 +364,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       if constexpr (mixed)
         B.ircf[k] = 1.0f / ff::narrow_trunc(heat_capacity(E, tl, Uti, c.rcds));
       else
-        B.irc[k] = 1.0 / heat_capacity(E, tl, Uti, c.rcds);
+        B.irc[k] = fm::rcp(heat_capacity(E, tl, Uti, c.rcds));
       if (k == 0) {
         K0 = K; T0 = T; kap0 = kap;
         if (A.bc_bw == CLM_BC_STATE) {
@@ -410,8 +420,8 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         Fbh = fbh;
       }
     }
-    const double UFw = A.rx ? Fw + dt * root_w : Fw;
-    const double UFe = A.rx ? Fe + dt * root_e : Fe;
+    const double UFw = kRoots ? Fw + dt * root_w : Fw;
+    const double UFe = kRoots ? Fe + dt * root_e : Fe;
     double xFw = UFw, xFe = UFe;
 
     // ---------------- stage 2: Newton ------------------------------------
@@ -487,7 +497,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         } else {
           piv = Md - L * cp_prev;
         }
-        const JT inv = (JT)1 / piv;
+        const JT inv = rcp_jt(piv);
         const JT cpk = U * inv;
         const JT dpk = (to_jt<JT>(fv) - L * dp_prev) * inv;
         J.cp[k] = cpk;
@@ -585,7 +595,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
           } else {
             piv = Md - L * c_prev;
           }
-          const JT inv = (JT)1 / piv;
+          const JT inv = rcp_jt(piv);
           const JT ck = U * inv;
           const JT dk = (to_jt<JT>(g) - L * d_prev) * inv;
           J.cp[k] = ck;
@@ -814,7 +824,7 @@ CLM_HD void richards_column(const StepArgs& A, const Tables& Tb, int s, int n, i
         } else {
           piv = M - L * cp_prev;
         }
-        const JT inv = (JT)1 / piv;
+        const JT inv = rcp_jt(piv);
         const JT cpk = U * inv;
         J.cp[k] = cpk;
         if constexpr (mixed) {

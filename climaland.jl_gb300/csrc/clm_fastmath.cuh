@@ -159,5 +159,43 @@ CLM_HD double log(const Tables& T, double x) {
 // a^b = exp(b log a) for a > 0 (the van Genuchten powers).
 CLM_HD double pow_pos(const Tables& T, double a, double b) { return exp(T, b * log(T, a)); }
 
+// 1/x by Newton-Raphson iteration r <- r + r (1 - x r) from a
+// single-precision seed (each step squares the relative error: 2^-22 ->
+// 2^-44 -> below 2^-53 before the final rounding; the residual 1 - x r is
+// exact in one FMA). Within one ulp of the correctly rounded quotient, for
+// four FP64 FMAs; the seed comes from integer re-biasing of x's exponent and
+// top significand bits (no conversion instruction) and a float reciprocal.
+// |x| outside [2^-120, 2^120], zero, infinities and NaN: the IEEE division.
+CLM_HD float rcp_seed(float x) {
+#ifdef __CUDA_ARCH__
+  return __fdividef(1.0f, x);
+#else
+  return 1.0f / x;
+#endif
+}
+
+CLM_HD double rcp(double x) {
+  const int64_t b = bits_of(x);
+  const int e = (int)((b >> 52) & 0x7FF);
+  if (e < 1023 - 120 || e > 1023 + 120) return 1.0 / x;
+  // x as a float with its significand truncated to 24 bits
+  const uint32_t fb = (uint32_t)((uint64_t)b >> 32 & 0x80000000u) |
+                      ((uint32_t)(e - 1023 + 127) << 23) | (uint32_t)((b >> 29) & 0x7FFFFF);
+  float xf;
+  std::memcpy(&xf, &fb, sizeof xf);
+  const float rf = rcp_seed(xf);
+  uint32_t rb;
+  std::memcpy(&rb, &rf, sizeof rb);
+  // the float seed widened to double (normal: |1/x| within [2^-121, 2^121])
+  const int64_t db = ((int64_t)(rb & 0x80000000u) << 32) |
+                     ((int64_t)(((rb >> 23) & 0xFF) - 127 + 1023) << 52) |
+                     ((int64_t)(rb & 0x7FFFFF) << 29);
+  double r = from_bits(db);
+  double t = fma(-x, r, 1.0);
+  r = fma(r, t, r);
+  t = fma(-x, r, 1.0);
+  return fma(r, t, r);
+}
+
 }  // namespace fm
 }  // namespace clm

@@ -134,7 +134,7 @@ CLM_HD Sat saturation(double nu_eff, double vartheta, double theta_r) {
 // With it S = (vartheta_safe - theta_r) inv costs a product instead of a
 // division (within an ulp of the quotient).
 CLM_HD double sat_inv(double nu_eff, double theta_r) {
-  return 1.0 / (fmax(nu_eff, theta_r + kSqrtEps) - theta_r);
+  return fm::rcp(fmax(nu_eff, theta_r + kSqrtEps) - theta_r);
 }
 
 CLM_HD double saturation_r(double inv, double vartheta, double theta_r) {
@@ -178,7 +178,7 @@ CLM_HD void psi_dpsi_r(const Tables& T, const VG& g, double nu_eff, double inv, 
     const double w = u - 1.0;
     const double w1n = fm::exp(T, g.inv_n * fm::log(T, w));  // w^(1/n)
     psi = -w1n * g.inv_alpha;
-    if (want_d) dpsi = g.coef_d * w1n * u / (w * a);
+    if (want_d) dpsi = g.coef_d * w1n * u * fm::rcp(w * a);
   } else {
     psi = (S <= 1.0) ? -0.0 : (vs - fmax(nu_eff, theta_r + kSqrtEps)) * inv_S_s;
     if (want_d) dpsi = inv_S_s;
@@ -215,7 +215,7 @@ CLM_HD void psi_dpsi_r(const Tables& T, const BC& g, double nu_eff, double inv, 
   if (S < 1.0) {
     const double u = fm::exp(T, g.neg_inv_c * fm::log(T, S));  // S^(-1/c)
     psi = g.psib * u;
-    if (want_d) dpsi = g.coef_d * u / a;
+    if (want_d) dpsi = g.coef_d * u * fm::rcp(a);
   } else {
     psi = (S <= 1.0) ? g.psib : (vs - fmax(nu_eff, theta_r + kSqrtEps)) * inv_S_s + g.psib;
     if (want_d) dpsi = inv_S_s;
@@ -273,7 +273,7 @@ CLM_HD void richards_point(const Tables& T, const VG& g, double nu, double inv, 
     const double w = u - 1.0;
     const double w1n = fm::exp(T, g.inv_n * fm::log(T, w));
     psi = -w1n * g.inv_alpha;
-    if (want_d) dpsi = g.coef_d * w1n * u / (w * a);
+    if (want_d) dpsi = g.coef_d * w1n * u * fm::rcp(w * a);
     const double s1m = fm::exp(T, g.inv_m * lS);  // S^(1/m)
     const double t = fm::exp(T, g.m * fm::log(T, 1.0 - s1m));
     const double f = 1.0 - t;
@@ -297,7 +297,7 @@ CLM_HD void richards_point(const Tables& T, const BC& g, double nu, double inv, 
     const double lS = fm::log(T, S);
     const double u = fm::exp(T, g.neg_inv_c * lS);  // S^(-1/c)
     psi = g.psib * u;
-    if (want_d) dpsi = g.coef_d * u / a;
+    if (want_d) dpsi = g.coef_d * u * fm::rcp(a);
     K = K_sat * fm::exp(T, g.k_exp * lS);
   } else {
     psi = (S <= 1.0) ? g.psib : (vs - fmax(nu, theta_r + kSqrtEps)) * inv_S_s + g.psib;

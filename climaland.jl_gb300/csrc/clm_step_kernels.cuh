@@ -47,7 +47,9 @@ __host__ __device__ constexpr size_t richards_smem_per_layer() {
 // energy residual.
 __host__ __device__ constexpr int eh_scratch_slots(bool mixed) { return mixed ? 6 : 7; }
 
-template <typename JT, class CM>
+// kRoots: the RootExtraction source (A.rx) compiled in; a separate kernel so
+// that its registers do not weigh on the step without it.
+template <typename JT, class CM, bool kRoots>
 __global__ void __launch_bounds__(128, 1)
     eh_step_kernel(StepArgs A, double* __restrict__ scratch, StepClock clk, int nsteps) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -109,7 +111,7 @@ __global__ void __launch_bounds__(128, 1)
       double Fw = A.Fw[s], Fe = A.Fe[s];
       uint32_t flags = 0;
       int iters = 0;
-      eh_column<JT, CM>(A, Tb, s, n, A.L.perm[s], B, J, t0, dt, nsteps, Fw, Fe, flags, iters);
+      eh_column<JT, CM, false, kRoots>(A, Tb, s, n, A.L.perm[s], B, J, t0, dt, nsteps, Fw, Fe, flags, iters);
       A.Fw[s] = Fw;
       A.Fe[s] = Fe;
       A.flags[s] = flags;
@@ -166,10 +168,14 @@ __global__ void __launch_bounds__(128, 1)
 
 // The kernel of (model, precision) for closure CM, and its launch.
 template <class CM>
-void* step_fn_t(int model, int precision) {
-  if (model == CLM_MODEL_ENERGY_HYDROLOGY)
-    return precision == CLM_PREC_MIXED ? (void*)eh_step_kernel<float, CM>
-                                       : (void*)eh_step_kernel<double, CM>;
+void* step_fn_t(int model, int precision, bool roots = false) {
+  if (model == CLM_MODEL_ENERGY_HYDROLOGY) {
+    if (roots)
+      return precision == CLM_PREC_MIXED ? (void*)eh_step_kernel<float, CM, true>
+                                         : (void*)eh_step_kernel<double, CM, true>;
+    return precision == CLM_PREC_MIXED ? (void*)eh_step_kernel<float, CM, false>
+                                       : (void*)eh_step_kernel<double, CM, false>;
+  }
   return precision == CLM_PREC_MIXED ? (void*)richards_step_kernel<float, CM>
                                      : (void*)richards_step_kernel<double, CM>;
 }
@@ -178,10 +184,17 @@ template <class CM>
 void launch_step_t(const StepArgs& A, int model, int precision, int grid, dim3 block, size_t smem,
                    double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream) {
   if (model == CLM_MODEL_ENERGY_HYDROLOGY) {
-    if (precision == CLM_PREC_MIXED)
-      eh_step_kernel<float, CM><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
-    else
-      eh_step_kernel<double, CM><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
+    if (A.rx) {
+      if (precision == CLM_PREC_MIXED)
+        eh_step_kernel<float, CM, true><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
+      else
+        eh_step_kernel<double, CM, true><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
+    } else {
+      if (precision == CLM_PREC_MIXED)
+        eh_step_kernel<float, CM, false><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
+      else
+        eh_step_kernel<double, CM, false><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
+    }
   } else {
     if (precision == CLM_PREC_MIXED)
       richards_step_kernel<float, CM><<<grid, block, smem, stream>>>(A, clk, nsteps);
