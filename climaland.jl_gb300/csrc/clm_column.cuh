@@ -221,7 +221,7 @@ CLM_HD double from_jt(JT x) {
 template <typename JT>
 CLM_HD JT rcp_jt(JT x) {
   if constexpr (sizeof(JT) < sizeof(double))
-    return 1.0f / x;
+    return ff::fast_div(1.0f, x);
   else
     return fm::rcp(x);
 }

@@ -116,6 +116,17 @@ CLM_HD float exp_approx(float x) {
 #endif
 }
 
+// a / b with the multi-function unit's reciprocal on the device (within 2
+// ulps for |b| below 2^126; IEEE division on the host). The double-float
+// division below recovers its error in the remainder term.
+CLM_HD float fast_div(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fdividef(a, b);
+#else
+  return a / b;
+#endif
+}
+
 // ---- error-free transformations -------------------------------------------
 CLM_HD F2 two_sum(float a, float b) {
   const float s = a + b;
@@ -176,13 +187,16 @@ CLM_HD F2 mul_f(F2 x, float y) {
 }
 
 // DWDivDW (relative error <= 15u^2 + 56u^3)
+// The quotient estimate th need not be correctly rounded: the remainder
+// x - th y is exact (two_prod, and Sterbenz for the subtraction of the high
+// words) and its quotient tl corrects th to the pair's precision.
 CLM_HD F2 div(F2 x, F2 y) {
-  const float th = x.hi / y.hi;
+  const float th = fast_div(x.hi, y.hi);
   const F2 r = mul_f(y, th);
   const float ph = x.hi - r.hi;
   const float dl = x.lo - r.lo;
   const float d = ph + dl;
-  const float tl = d / y.hi;
+  const float tl = fast_div(d, y.hi);
   return fast_two_sum(th, tl);
 }
 
