@@ -163,6 +163,16 @@ CLM_HD F2 add(F2 x, F2 y) {
 
 CLM_HD F2 sub(F2 x, F2 y) { return add(x, neg(y)); }
 
+// SloppyDWPlusDW (Joldes, Muller, Popescu, Algorithm 5): relative error
+// 2^-46 or better when no cancellation occurs, here |y| <= |x| / 128 (the
+// callers below), so the accurate variant's second two_sum is not needed.
+CLM_HD F2 add_small(F2 x, F2 y) {
+  const F2 s = two_sum(x.hi, y.hi);
+  const float v = x.lo + y.lo;
+  const float w = s.lo + v;
+  return fast_two_sum(s.hi, w);
+}
+
 // DWPlusFP (relative error <= 2u^2)
 CLM_HD F2 add_f(F2 x, float y) {
   const F2 s = two_sum(x.hi, y);
@@ -303,9 +313,9 @@ CLM_HD F2 exp(const Tables& T, F2 x) {
   const float c = fmaf(fmaf(r.hi, 1.0f / 120.0f, 1.0f / 24.0f), r.hi, 1.0f / 6.0f);
   const F2 s = two_sum(0.5f, r.hi * c);
   const F2 q = mul(mul(r, r), s);
-  const F2 em1 = add(r, q);  // e^r - 1
+  const F2 em1 = add_small(r, q);  // e^r - 1 (|q| <= |r| |r| / 2, |r| <= ln2/128)
   const F2 tj = F2{T.t[j], T.t[64 + j]};
-  const F2 y = add(tj, mul(tj, em1));
+  const F2 y = add_small(tj, mul(tj, em1));  // tj >= 1, |tj em1| <= 2 |em1|
   const float sc = ffrom((uint32_t)(m + 127) << 23);  // 2^m
   return F2{y.hi * sc, y.lo * sc};
 }

@@ -73,7 +73,7 @@ CLM_HD bool psi_dpsi_ff(const ff::Tables& T, const ColFF& c, F2 nu_eff, F2 v, do
   const F2 b = mul(lw, c.inv_n);  // log w^(1/n)
   if (!(b.hi >= kExpMin && b.hi <= kExpMax)) return false;
   psi = -to_double(mul(exp(T, b), c.inv_alpha));
-  dpsi = c.coef_d * ff::exp_approx((b.hi - lw.hi) + (a.hi - L.hi)) / den.hi;
+  dpsi = ff::fast_div(c.coef_d * ff::exp_approx((b.hi - lw.hi) + (a.hi - L.hi)), den.hi);
   return true;
 }
 
@@ -117,7 +117,7 @@ CLM_HD bool psi_dpsi_ff(const ff::Tables& T, const ColFFBC& c, F2 nu_eff, F2 v, 
   const F2 a = mul(L, c.neg_inv_c);  // log u
   if (!(a.hi <= kExpMax)) return false;
   psi = to_double(mul(exp(T, a), c.psib));
-  dpsi = c.coef_d * ff::exp_approx(a.hi - L.hi) / den.hi;
+  dpsi = ff::fast_div(c.coef_d * ff::exp_approx(a.hi - L.hi), den.hi);
   return true;
 }
 
