@@ -163,9 +163,10 @@ CLM_HD F2 add(F2 x, F2 y) {
 
 CLM_HD F2 sub(F2 x, F2 y) { return add(x, neg(y)); }
 
-// SloppyDWPlusDW (Joldes, Muller, Popescu, Algorithm 5): relative error
-// 2^-46 or better when no cancellation occurs, here |y| <= |x| / 128 (the
-// callers below), so the accurate variant's second two_sum is not needed.
+// SloppyDWPlusDW (Joldes, Muller, Popescu, Algorithm 5): relative error of
+// order 2^-46 when the operands cannot cancel (same signs, or |y| much
+// smaller than |x|; every caller states which), so the accurate variant's
+// second two_sum is not needed.
 CLM_HD F2 add_small(F2 x, F2 y) {
   const F2 s = two_sum(x.hi, y.hi);
   const float v = x.lo + y.lo;
@@ -296,7 +297,8 @@ constexpr float kExpMax = 80.0f;
 // |r| <= ln2/128, with ln2/64 split as C1 (11 bits: k C1 is exact for
 // |k| < 2^13) + C2 (24 bits) + C3; e^r - 1 = r + r^2 (1/2 + r c(r)), c(r) =
 // 1/6 + r/24 + r^2/120 in float (its error enters below 2^-48).
-CLM_HD F2 exp(const Tables& T, F2 x) {
+template <bool kLo>
+CLM_HD F2 exp_impl(const Tables& T, F2 x) {
   const float kInvL = 92.33248138427734f;          // 64 / ln2
   const float C1 = 0.010833740234375f;             // ln2/64 to 11 significant bits
   const float C2 = -3.3155381515825866e-06f;       // ln2/64 - C1 to 24 bits
@@ -306,7 +308,7 @@ CLM_HD F2 exp(const Tables& T, F2 x) {
   const float t = fmaf(-kf, C1, x.hi);  // exact
   const F2 p = two_prod(kf, C2);
   F2 r = two_sum(t, -p.hi);  // exact
-  r = add_f(r, x.lo);        // x.lo kept to the last bit
+  if (kLo) r = add_f(r, x.lo);  // x.lo kept to the last bit
   r = fast_two_sum(r.hi, r.lo - (p.lo + kf * C3));
   const int j = k & 63;
   const int m = (k - j) / 64;
@@ -319,6 +321,11 @@ CLM_HD F2 exp(const Tables& T, F2 x) {
   const float sc = ffrom((uint32_t)(m + 127) << 23);  // 2^m
   return F2{y.hi * sc, y.lo * sc};
 }
+
+CLM_HD F2 exp(const Tables& T, F2 x) { return exp_impl<true>(T, x); }
+
+// exp of a single float (the reduction skips the low word)
+CLM_HD F2 exp1(const Tables& T, float x) { return exp_impl<false>(T, make(x)); }
 
 // log(x) for x > 0 (normal float hi): x = 2^k xm with xm in [1, 2) (exact
 // scaling), y0 = log_approx(xm.hi) (absolute error below 2^-21), t =
@@ -333,7 +340,7 @@ CLM_HD F2 log(const Tables& T, F2 x) {
   const float sc = ffrom((uint32_t)(127 - k) << 23);  // 2^-k
   const F2 xm = F2{x.hi * sc, x.lo * sc};
   const float y0 = log_approx(xm.hi);
-  const F2 e = exp(T, make(-y0));
+  const F2 e = exp1(T, -y0);
   const F2 t = add_f(mul(xm, e), -1.0f);
   const float kf = int_to_float(k);
   F2 y = add(two_sum(kf * L1, y0), t);  // k L1 exact

@@ -127,7 +127,9 @@ CLM_HD bool psi_dpsi_ff(const ff::Tables& T, const ColFFBC& c, F2 nu_eff, F2 v, 
 // T - T_0 only).
 CLM_HD double temperature_rel_ff(const EarthFF& E, F2 rho_e, F2 ti, F2 tl, F2 rhoc_ds) {
   using namespace ff;
-  const F2 rc = add(add(rhoc_ds, mul(tl, E.rhocp_l)), mul(ti, E.rhocp_i));
+  // rho c: three non-negative terms (no cancellation: the sloppy sum); the
+  // numerator can cancel (T near T_0) and keeps the accurate one
+  const F2 rc = add_small(add_small(rhoc_ds, mul(tl, E.rhocp_l)), mul(ti, E.rhocp_i));
   const F2 num = add(rho_e, mul(ti, E.rho_i_LH_f0));
   return to_double(div(num, rc));
 }
