@@ -727,6 +727,24 @@ CLM_HD void richards_column(const StepArgs& A, const Tables& Tb, int s, int n, i
   const double half = 0.5 * dz;
   const double rdz = dt * inv_dz;
   constexpr bool mixed = sizeof(JT) < sizeof(double);
+  // mixed path: K, psi and dpsi in double-float (FP64 closure where it declines)
+  typename ColFFOf<CM>::type cf;
+  F2 K_sat_f;
+  if constexpr (mixed) {
+    cf = make_col_ff(nu, theta_r, g);
+    K_sat_f = ff::from_double(K_sat);
+  }
+  const ff::Tables FT{Tb.ff};
+  auto point = [&](double xv, double& K, double& psi, double& D) {
+    if constexpr (mixed) {
+      float d;
+      if (richards_point_ff(FT, cf, K_sat_f, ff::from_double(xv), K, psi, d)) {
+        D = d;
+        return;
+      }
+    }
+    richards_point<true>(Tb, g, nu, inv, xv, theta_r, inv_S_s, K_sat, K, psi, D);
+  };
   // MoistureStateBC at the top carries dfluxBCdY (rre.jl:137-146, 460-468):
   // the boundary fluxes are then refreshed with the implicit cache.
   const bool dflux = (A.bc_tw == CLM_BC_STATE);
@@ -782,7 +800,7 @@ CLM_HD void richards_column(const StepArgs& A, const Tables& Tb, int s, int n, i
       JT D_prev = 0;
       double sum_f = 0.0;
       double Kc, psic, Dc;
-      richards_point<true>(Tb, g, nu, inv, B.xv[0], theta_r, inv_S_s, K_sat, Kc, psic, Dc);
+      point(B.xv[0], Kc, psic, Dc);
       if (refresh_bc) {
         if (A.bc_bw == CLM_BC_FREE_DRAINAGE) Fbw = -1.0 * Kc;
         else if (A.bc_bw == CLM_BC_STATE) Fbw = -Kc * ((psic + half) - psi_bb) / half;
@@ -793,7 +811,7 @@ CLM_HD void richards_column(const StepArgs& A, const Tables& Tb, int s, int n, i
         double Kn = 0, psin = 0, Dn = 0;
         double Md_extra = 0.0;
         if (k < n - 1) {
-          richards_point<true>(Tb, g, nu, inv, B.xv[k + 1], theta_r, inv_S_s, K_sat, Kn, psin, Dn);
+          point(B.xv[k + 1], Kn, psin, Dn);
           aw_up = 0.5 * (Kc + Kn) * inv_dz;
           Fw_up = -aw_up * ((psin - psic) + dz);
         } else {

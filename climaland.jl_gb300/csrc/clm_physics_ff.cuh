@@ -121,6 +121,60 @@ CLM_HD bool psi_dpsi_ff(const ff::Tables& T, const ColFFBC& c, F2 nu_eff, F2 v, 
   return true;
 }
 
+// RichardsModel point on the mixed path (update_aux! and dpsidvartheta at
+// the iterate, rre.jl:368-380, 402-454): K and psi (FP64 results) and dpsi
+// (float) sharing log S; van Genuchten's S^(1/m) is 1/S^(-1/m) (one
+// division instead of an exponential) and sqrt(S) is exp(log(S)/2). False
+// for saturated cells and outside the double-float range: the caller then
+// evaluates the FP64 closure.
+CLM_HD bool richards_point_ff(const ff::Tables& T, const ColFF& c, F2 K_sat, F2 v, double& K,
+                              double& psi, float& dpsi) {
+  using namespace ff;
+  const F2 guard = add_f(c.theta_r, 1.4901161193847656e-08f);  // theta_r + sqrt(eps)
+  const F2 vs = ff_max(v, guard);
+  const F2 ns = ff_max(c.nu, guard);
+  const F2 den = sub(ns, c.theta_r);
+  const F2 S = div(sub(vs, c.theta_r), den);
+  if (!(S.hi < 1.0f) || !(S.hi > 1e-30f)) return false;
+  const F2 L = log(T, S);
+  const F2 a = mul(L, c.neg_inv_m);  // log u, u = S^(-1/m)
+  if (!(a.hi <= kExpMax)) return false;
+  const F2 u = exp(T, a);
+  const F2 w = add_f(u, -1.0f);
+  if (!(w.hi > 1e-30f)) return false;
+  const F2 lw = log(T, w);
+  const F2 b = mul(lw, c.inv_n);  // log w^(1/n)
+  if (!(b.hi >= kExpMin && b.hi <= kExpMax)) return false;
+  psi = -to_double(mul(exp(T, b), c.inv_alpha));
+  dpsi = fast_div(c.coef_d * exp_approx((b.hi - lw.hi) + (a.hi - L.hi)), den.hi);
+  const F2 om = add_f(neg(div(make(1.0f), u)), 1.0f);  // 1 - S^(1/m)
+  if (!(om.hi > 1e-30f)) return false;
+  const F2 f = add_f(neg(exp(T, mul(log(T, om), c.m))), 1.0f);  // 1 - (1 - S^(1/m))^m
+  const F2 h = mul_f(L, 0.5f);                                   // log sqrt(S)
+  if (!(h.hi >= kExpMin)) return false;
+  K = to_double(mul(mul(K_sat, mul(f, f)), exp(T, h)));
+  return true;
+}
+
+CLM_HD bool richards_point_ff(const ff::Tables& T, const ColFFBC& c, F2 K_sat, F2 v, double& K,
+                              double& psi, float& dpsi) {
+  using namespace ff;
+  const F2 guard = add_f(c.theta_r, 1.4901161193847656e-08f);
+  const F2 vs = ff_max(v, guard);
+  const F2 ns = ff_max(c.nu, guard);
+  const F2 den = sub(ns, c.theta_r);
+  const F2 S = div(sub(vs, c.theta_r), den);
+  if (!(S.hi < 1.0f) || !(S.hi > 1e-30f)) return false;
+  const F2 L = log(T, S);
+  const F2 a = mul(L, c.neg_inv_c);  // log S^(-1/c)
+  const F2 ek = mul(L, c.k_exp);     // log S^(2/c + 3)
+  if (!(a.hi <= kExpMax) || !(ek.hi >= kExpMin)) return false;
+  psi = to_double(mul(exp(T, a), c.psib));
+  dpsi = fast_div(c.coef_d * exp_approx(a.hi - L.hi), den.hi);
+  K = to_double(mul(K_sat, exp(T, ek)));
+  return true;
+}
+
 // temperature_from_ρe_int with volumetric_heat_capacity
 // (soil_heat_parameterizations.jl:157-192) at theta_l = tl, relative to T_0:
 // (rho_e + theta_i rho_i L_f) / rho c, as a double (the Newton residual uses

@@ -21,9 +21,7 @@ size_t step_smem_bytes(int model, int precision, int nmax, int wpc) {
   else
     per_layer = precision == CLM_PREC_MIXED ? richards_smem_per_layer<float>()
                                             : richards_smem_per_layer<double>();
-  const int tab = (model == CLM_MODEL_ENERGY_HYDROLOGY && precision == CLM_PREC_MIXED)
-                      ? fm::stage_doubles<true>()
-                      : fm::stage_doubles<false>();
+  const int tab = precision == CLM_PREC_MIXED ? fm::stage_doubles<true>() : fm::stage_doubles<false>();
   return tab * sizeof(double) + per_layer * (size_t)nmax * kTile * wpc;
 }
 

@@ -127,15 +127,17 @@ __global__ void __launch_bounds__(128, 1)
     richards_step_kernel(StepArgs A, StepClock clk, int nsteps) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* tab = reinterpret_cast<double*>(smem_raw);
-  const Tables Tb = fm::stage_tables(tab);
+  constexpr bool kMixed = sizeof(JT) < sizeof(double);
+  constexpr int kTab = fm::stage_doubles<kMixed>();
+  const Tables Tb = fm::stage_tables<kMixed>(tab);
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const int wpc = blockDim.x >> 5;
   const int64_t lay = (int64_t)A.L.nmax * kTile;
-  double* dw = tab + fm::TABLE_SIZE + (int64_t)warp * lay;
+  double* dw = tab + kTab + (int64_t)warp * lay;
   constexpr int kJA = richards_jac_arrays<JT>();
-  JT* jw = reinterpret_cast<JT*>(tab + fm::TABLE_SIZE + (int64_t)wpc * lay) + (int64_t)warp * kJA * lay;
+  JT* jw = reinterpret_cast<JT*>(tab + kTab + (int64_t)wpc * lay) + (int64_t)warp * kJA * lay;
   const int gwarp = blockIdx.x * wpc + warp;
   const int nwarps = gridDim.x * wpc;
   RBuffers B;

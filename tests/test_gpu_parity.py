@@ -79,6 +79,7 @@ MIXED = dict(tol_state=1e-8, noise=2.0 ** -44, nseeds=16, precision=A.CLM_PREC_M
     ("full_scale", lambda: WL.full_scale_c4(ncol=1024), 48),
     ("energy_hydrology", lambda: WL.energy_hydrology_c1().subset(1024), 48),
     ("uneven", lambda: WL.uneven_c2().subset(1024), 48),
+    ("richards", lambda: WL.richards_c0(ncol=1024), 96),
 ])
 def test_mixed_precision_within_1e8(name, make, nsteps):
     report(f"mixed_{name}", check_parity(make(), nsteps, **MIXED))
@@ -92,8 +93,7 @@ def test_mixed_precision_tolerance_mode():
 # Brooks-Corey closure (cfg.hydrology_cm = CLM_CM_BROOKS_COREY): sandy columns
 # with |psi_b| ~ 0.05 m and K_sat ~ 1e-4 m/s are stiff enough that three
 # Newton iterations diverge (the reference's trajectory there is not
-# reproducible: those columns fall under the oracle-spread bound). The mixed
-# path runs on the EnergyHydrology configurations only, as for van Genuchten.
+# reproducible: those columns fall under the oracle-spread bound).
 BROOKS_COREY = {
     "richards": (lambda: WL.brooks_corey(WL.richards_c0(ncol=1024)), 96, {}),
     "energy_hydrology": (lambda: WL.brooks_corey(WL.energy_hydrology_c1().subset(1024)), 96, {}),
@@ -104,6 +104,7 @@ BROOKS_COREY = {
     "mixed_energy_hydrology": (lambda: WL.brooks_corey(WL.energy_hydrology_c1().subset(1024)), 48, MIXED),
     "mixed_full_scale": (lambda: WL.brooks_corey(WL.full_scale_c4(ncol=1024)), 48, MIXED),
     "mixed_uneven": (lambda: WL.brooks_corey(WL.uneven_c2().subset(1024)), 48, MIXED),
+    "mixed_richards": (lambda: WL.brooks_corey(WL.richards_c0(ncol=1024)), 96, MIXED),
 }
 
 
