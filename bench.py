@@ -211,7 +211,7 @@ def _error_stats(a, b, ncol_cells):
 
 def forms_block(args, torch, stream):
     """The three forms beside the plain path, on subsets that finish in
-    seconds: mixed precision, uneven columns (autotuned, graph-replayed) and
+    seconds: mixed precision (EnergyHydrology and RichardsModel), uneven columns (autotuned, graph-replayed) and
     learned guess + mixed precision in tolerance mode. Errors are per-column
     max |vartheta_l| differences from the plain FP64 path on the same
     columns and steps (the plain path itself is held to the FP64 oracle by
@@ -293,6 +293,12 @@ def forms_block(args, torch, stream):
     out["uneven_4_30"] = {"workload": w2.name, "cells": int(w2.ncells),
                           "plain_fp64_graph_autotuned": pub(u64, None, w2),
                           "mixed_graph_autotuned": pub(umx, u64, w2)}
+    # (1) on the RichardsModel: the 1024 x 20 configuration's distributions
+    w0 = WL.richards_c0(ncol=args.forms_ncol, seed=0)
+    r64 = run(w0)
+    rmx = run(w0, precision=A.CLM_PREC_MIXED)
+    out["richards_subset"] = {"workload": w0.name, "plain_fp64": pub(r64, None, w0),
+                              "mixed": pub(rmx, r64, w0)}
     return out
 
 
