@@ -111,7 +111,7 @@ def test_features_kernel_matches_host(torch):
 def test_learned_guess_saves_newton_iterations(torch):
     """Train on the plain solver's trajectories, then solve unseen columns to
     the same tolerance with and without the guess: fewer iterations, same
-    answer (the plain solve is the judge)."""
+    answer (the plain solve is the reference for its error)."""
     wtr = LG.training_workload(ncol=16384, seed=0)
     X, Y = LG.generate(wtr, 24)
     res = LG.train(X, Y, steps=3000, batch=4096, lr=2e-3)
