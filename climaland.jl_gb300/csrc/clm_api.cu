@@ -26,10 +26,10 @@ size_t step_smem_bytes(int model, int precision, int nmax, int wpc);
 cudaError_t step_grid(int model, int precision, int cm, int nmax, int wpc, int ntiles, int* grid);
 size_t step_scratch_doubles(int model, int precision, int nmax, int wpc, int grid);
 // clm_layout.cu
-cudaError_t ref_to_internal(const Layout& L, const int32_t* ref_off, const double* src,
-                            double* dst, int ncomp, cudaStream_t st, int tile0 = 0, int ntl = -1);
-cudaError_t internal_to_ref(const Layout& L, const int32_t* ref_off, const double* src,
-                            double* dst, int ncomp, cudaStream_t st, int tile0 = 0, int ntl = -1);
+cudaError_t ref_to_internal(const Layout& L, const double* src, double* dst, cudaStream_t st,
+                            int tile0 = 0, int ntl = -1);
+cudaError_t internal_to_ref(const Layout& L, const double* src, double* dst, cudaStream_t st,
+                            int tile0 = 0, int ntl = -1);
 cudaError_t cols_to_sorted(const Layout& L, const double* src, double* dst, cudaStream_t st);
 cudaError_t cols_to_orig(const Layout& L, const double* src, double* dst, cudaStream_t st);
 // clm_budget.cu
@@ -63,6 +63,7 @@ struct clm_handle {
   int* d_col_n = nullptr;
   int* d_perm = nullptr;
   int32_t* d_ref_off = nullptr;
+  int64_t* d_slot_ref = nullptr;
   double *d_zlo = nullptr, *d_zhi = nullptr, *d_prm = nullptr, *d_lkap = nullptr;
   double* d_forc[4] = {nullptr, nullptr, nullptr, nullptr};
   double* d_rx = nullptr;  // root-extraction canopy rows (sorted), or null
@@ -151,6 +152,7 @@ Layout layout_of(const clm_handle* h) {
   L.tile_n = h->d_tile_n;
   L.col_n = h->d_col_n;
   L.perm = h->d_perm;
+  L.slot_ref = h->d_slot_ref;
   return L;
 }
 
@@ -233,7 +235,12 @@ int build_layout(clm_handle* h, const std::vector<int>& nl) {
   for (int s = 0; s < ncol; ++s) h->perm_identity = h->perm_identity && h->perm[s] == s;
   h->nmax = nmax;
   // device copies
+  // per-slot reference offsets (what the layout transposes read instead of
+  // chasing perm -> ref_off)
+  std::vector<int64_t> slot_ref(h->stride, 0);
+  for (int s = 0; s < ncol; ++s) slot_ref[s] = h->ref_off[h->perm[s]];
   dfree(h->d_tile_off); dfree(h->d_tile_n); dfree(h->d_col_n); dfree(h->d_perm); dfree(h->d_ref_off);
+  dfree(h->d_slot_ref);
   cudaStream_t st = h->stream;
   CLM_CUDA(h, cudaMalloc(&h->d_tile_off, sizeof(int64_t) * h->ntiles));
   CLM_CUDA(h, cudaMalloc(&h->d_tile_n, sizeof(int) * h->ntiles));
@@ -245,6 +252,10 @@ int build_layout(clm_handle* h, const std::vector<int>& nl) {
   CLM_CUDA(h, cudaMemcpyAsync(h->d_col_n, h->col_n.data(), sizeof(int) * h->stride, cudaMemcpyHostToDevice, st));
   CLM_CUDA(h, cudaMemcpyAsync(h->d_perm, h->perm.data(), sizeof(int) * h->stride, cudaMemcpyHostToDevice, st));
   CLM_CUDA(h, cudaMemcpyAsync(h->d_ref_off, h->ref_off.data(), sizeof(int32_t) * (ncol + 1), cudaMemcpyHostToDevice, st));
+  CLM_CUDA(h, cudaMalloc(&h->d_slot_ref, sizeof(int64_t) * h->stride));
+  CLM_CUDA(h, cudaMemcpyAsync(h->d_slot_ref, slot_ref.data(), sizeof(int64_t) * h->stride, cudaMemcpyHostToDevice, st));
+  // the host vector above goes out of scope: wait for its copy
+  CLM_CUDA(h, cudaStreamSynchronize(st));
   // per-layout buffers
   dfree(h->d_v); dfree(h->d_ti); dfree(h->d_e); dfree(h->d_stage);
   const int64_t ni = std::max<int64_t>(h->ncells_int, 1);
@@ -421,7 +432,7 @@ int set_state_impl(clm_handle* h, const double* v, const double* ti, const doubl
   for (int i = 0; i < (eh ? 3 : 1); ++i) {
     double* stg = h->d_stage + (size_t)i * h->ncells_ref;
     CLM_CUDA(h, cudaMemcpyAsync(stg, src[i], nb, kind, st));
-    CLM_CUDA(h, ref_to_internal(L, h->d_ref_off, stg, dst[i], 1, st));
+    CLM_CUDA(h, ref_to_internal(L, stg, dst[i], st));
   }
   const double* cs[2] = {Fw, Fe};
   double* cd[2] = {h->d_Fw, h->d_Fe};
@@ -447,7 +458,7 @@ int get_state_impl(clm_handle* h, double* v, double* ti, double* e, double* Fw, 
   for (int i = 0; i < (eh ? 3 : 1); ++i) {
     if (!outs[i]) continue;
     double* stg = h->d_stage + (size_t)i * h->ncells_ref;
-    CLM_CUDA(h, internal_to_ref(L, h->d_ref_off, srcs[i], stg, 1, st));
+    CLM_CUDA(h, internal_to_ref(L, srcs[i], stg, st));
     CLM_CUDA(h, cudaMemcpyAsync(outs[i], stg, nb, kind, st));
   }
   double* co[2] = {Fw, Fe};
@@ -590,6 +601,7 @@ void clm_destroy(clm_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->own_stream && h->own_stream != h->stream) cudaStreamSynchronize(h->own_stream);
   dfree(h->d_tile_off); dfree(h->d_tile_n); dfree(h->d_col_n); dfree(h->d_perm); dfree(h->d_ref_off);
+  dfree(h->d_slot_ref);
   dfree(h->d_zlo); dfree(h->d_zhi); dfree(h->d_prm); dfree(h->d_lkap);
   for (auto& p : h->d_forc) dfree(p);
   dfree(h->d_rx);
@@ -851,8 +863,7 @@ int clm_step_host(clm_handle* h, double* v, double* ti, double* e, double* Fw, d
     // share the per-warp scratch, so they stay in one stream)
     CLM_CUDA(h, cudaStreamWaitEvent(h->stream, ev_in, 0));
     for (int f = 0; f < nf; ++f)
-      CLM_CUDA(h, ref_to_internal(L, h->d_ref_off, h->d_stage + f * h->ncells_ref, df[f], 1, h->stream,
-                                  T0, T1 - T0));
+      CLM_CUDA(h, ref_to_internal(L, h->d_stage + f * h->ncells_ref, df[f], h->stream, T0, T1 - T0));
     A.tile_begin = T0;
     A.tile_end = T1;
     for (int s0 = 0; s0 < nsteps; s0 += 64) {
@@ -863,8 +874,7 @@ int clm_step_host(clm_handle* h, double* v, double* ti, double* e, double* Fw, d
                               std::min(64, nsteps - s0), h->stream));
     }
     for (int f = 0; f < nf; ++f)
-      CLM_CUDA(h, internal_to_ref(L, h->d_ref_off, df[f], h->d_stage + f * h->ncells_ref, 1, h->stream,
-                                  T0, T1 - T0));
+      CLM_CUDA(h, internal_to_ref(L, df[f], h->d_stage + f * h->ncells_ref, h->stream, T0, T1 - T0));
     CLM_CUDA(h, cudaEventRecord(ev_done, h->stream));
     // out
     CLM_CUDA(h, cudaStreamWaitEvent(h->copy_out, ev_done, 0));

@@ -29,6 +29,7 @@ struct Layout {
   const int* tile_n;        // [ntiles]
   const int* col_n;         // [stride]  0 for padding lanes
   const int* perm;          // [stride]  original column index, -1 padding
+  const int64_t* slot_ref;  // [stride]  first cell of the slot's column in the reference layout (0: padding)
 };
 
 struct StepArgs {
