@@ -49,6 +49,7 @@ CLM_BC_FREE_DRAINAGE = 1
 CLM_BC_STATE = 2
 CLM_BC_FLUX_ADVECTIVE = 3
 CLM_BC_PRECIP_RUNOFF = 4
+CLM_BC_ATMOS = 5
 CLM_RUNOFF_NONE = 0
 CLM_RUNOFF_SURFACE = 1
 CLM_RUNOFF_TOPMODEL = 2
@@ -61,6 +62,20 @@ CLM_RX_K_SAT = 5
 CLM_RX_PSI63 = 6
 CLM_RX_WEIBULL_C = 7
 CLM_RX_NFIELDS = 8
+
+# clm_atmos_field: rows of clm_set_atmos
+ATMOS_FIELDS = ("P_LIQ", "T_AIR", "U_AIR", "Q_AIR", "P_AIR", "SW_D", "LW_D", "H_AIR", "GUSTINESS",
+                "PAR_ALBEDO_DRY", "NIR_ALBEDO_DRY", "PAR_ALBEDO_WET", "NIR_ALBEDO_WET",
+                "ALBEDO_TOP_THICKNESS", "EMISSIVITY", "Z_0M", "Z_0B", "D_DS", "EVAP_P", "EVAP_ALPHA")
+for _i, _n in enumerate(ATMOS_FIELDS):
+    globals()["CLM_AT_" + _n] = _i
+CLM_AT_NFIELDS = len(ATMOS_FIELDS)
+
+# clm_atmos_flux: rows of clm_atmos_fluxes
+ATMOS_FLUXES = ("LHF", "SHF", "VAPOR_LIQ", "VAPOR_ICE", "R_N", "Q_SFC", "TOP_WATER", "TOP_HEAT")
+for _i, _n in enumerate(ATMOS_FLUXES):
+    globals()["CLM_AF_" + _n] = _i
+CLM_AF_NFIELDS = len(ATMOS_FLUXES)
 CLM_CM_VAN_GENUCHTEN = 0
 CLM_CM_BROOKS_COREY = 1
 
@@ -113,6 +128,29 @@ class ClmEarthParams(ctypes.Structure):
         ("LH_f0", ctypes.c_double),
         ("grav", ctypes.c_double),
     ]
+
+
+class ClmAtmosParams(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in (
+        "stefan", "gas_constant", "molmass_dryair", "molmass_water", "D_vapor", "LH_v0", "LH_s0",
+        "cp_d", "cp_v", "T_triple", "press_triple", "von_karman", "Pr_0", "a_m", "a_h", "b_m", "b_h",
+        "zeta_max")] + [("iterations", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+
+# Python twin of clm_atmos_params_default (ClimaParams values; Businger-Dyer).
+DEFAULT_ATMOS = dict(
+    stefan=5.670374419e-8, gas_constant=8.3144598, molmass_dryair=0.02897,
+    molmass_water=0.01801528, D_vapor=2.5e-5, LH_v0=2500800.0, LH_s0=2834400.0, cp_d=1004.5,
+    cp_v=1859.0, T_triple=273.16, press_triple=611.657, von_karman=0.4, Pr_0=0.74, a_m=4.7,
+    a_h=4.7, b_m=15.0, b_h=9.0, zeta_max=100.0, iterations=10,
+)
+
+
+def default_atmos_params() -> "ClmAtmosParams":
+    a = ClmAtmosParams()
+    for k, v in DEFAULT_ATMOS.items():
+        setattr(a, k, v)
+    return a
 
 
 class ClmConfig(ctypes.Structure):
@@ -244,6 +282,9 @@ SIGNATURES = [
     ("clm_set_geometry", ctypes.c_int, [_H, _DP, _DP, _IP]),
     ("clm_set_params", ctypes.c_int, [_H, _DP, ctypes.c_int32]),
     ("clm_set_root_extraction", ctypes.c_int, [_H, _DP, ctypes.c_int32]),
+    ("clm_atmos_params_default", None, [ctypes.POINTER(ClmAtmosParams)]),
+    ("clm_set_atmos", ctypes.c_int, [_H, ctypes.POINTER(ClmAtmosParams), _DP, ctypes.c_int32]),
+    ("clm_atmos_fluxes", ctypes.c_int, [_H, _DP, ctypes.c_int32]),
     ("clm_set_bc", ctypes.c_int, [_H, ctypes.c_int32, _DP, ctypes.c_int32]),
     ("clm_set_state", ctypes.c_int, [_H, _DP, _DP, _DP, _DP, _DP]),
     ("clm_get_state", ctypes.c_int, [_H, _DP, _DP, _DP, _DP, _DP]),

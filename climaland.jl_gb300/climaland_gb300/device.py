@@ -91,6 +91,8 @@ class SoilColumns:
             self._check(self.lib.clm_set_bc(self.h, int(slot), A.dptr(f), f.shape[0]))
         if getattr(w, "root", None) is not None:
             self.set_root_extraction(w.root)
+        if getattr(w, "atmos", None) is not None:
+            self.set_atmos(w.atmos, getattr(w, "atmos_params", None))
         self.set_state(w.vartheta_l, w.theta_i, w.rho_e_int, w.intF_w, w.intF_e)
 
     def set_root_extraction(self, root):
@@ -101,6 +103,23 @@ class SoilColumns:
             return
         r = _c(root)
         self._check(self.lib.clm_set_root_extraction(self.h, A.dptr(r), r.shape[0]))
+
+    def set_atmos(self, drivers, params=None):
+        """Drivers of the atmosphere-driven top boundary (CLM_AT_NFIELDS rows
+        of ncol) and its constants (ClmAtmosParams; None: the defaults), or
+        drivers None to remove them."""
+        if drivers is None:
+            self._check(self.lib.clm_set_atmos(self.h, None, None, 0))
+            return
+        d = _c(drivers)
+        pp = ctypes.byref(params) if params is not None else None
+        self._check(self.lib.clm_set_atmos(self.h, pp, A.dptr(d), d.shape[0]))
+
+    def atmos_fluxes(self):
+        """The boundary's diagnostics at the current state: (CLM_AF_NFIELDS, ncol)."""
+        out = np.zeros((A.CLM_AF_NFIELDS, self.ncol))
+        self._check(self.lib.clm_atmos_fluxes(self.h, A.dptr(out), A.CLM_AF_NFIELDS))
+        return out
 
     # -- plumbing -----------------------------------------------------------
     def _check(self, rc):

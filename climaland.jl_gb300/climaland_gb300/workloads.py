@@ -51,6 +51,10 @@ class Workload:
     meta: dict = field(default_factory=dict)
     # root-extraction canopy values (CLM_RX_NFIELDS, ncol), or None
     root: np.ndarray | None = None
+    # drivers of the atmosphere-driven top boundary (CLM_AT_NFIELDS, ncol)
+    # and its constants (ClmAtmosParams; None: the defaults), or None
+    atmos: np.ndarray | None = None
+    atmos_params: object = None
 
     @property
     def ncells(self) -> int:
@@ -96,7 +100,9 @@ class Workload:
             rho_e_int=cells(self.rho_e_int), intF_w=cols(self.intF_w),
             intF_e=cols(self.intF_e), t0=self.t0, dt=self.dt,
             nsteps=self.nsteps, meta=dict(self.meta),
-            root=None if self.root is None else np.ascontiguousarray(self.root[:, c0:c1]))
+            root=None if self.root is None else np.ascontiguousarray(self.root[:, c0:c1]),
+            atmos=None if self.atmos is None else np.ascontiguousarray(self.atmos[:, c0:c1]),
+            atmos_params=self.atmos_params)
 
 
 def _forcing(ncol: int) -> np.ndarray:
@@ -422,7 +428,8 @@ def brooks_corey(w: Workload, seed: int = 0) -> Workload:
         z_hi=w.z_hi, params=params, forcing=w.forcing, vartheta_l=v, theta_i=ti,
         rho_e_int=e, intF_w=w.intF_w.copy(),
         intF_e=None if w.intF_e is None else w.intF_e.copy(), t0=w.t0, dt=w.dt,
-        nsteps=w.nsteps, meta=dict(w.meta), root=None if w.root is None else w.root.copy())
+        nsteps=w.nsteps, meta=dict(w.meta), root=None if w.root is None else w.root.copy(),
+        atmos=None if w.atmos is None else w.atmos.copy(), atmos_params=w.atmos_params)
 
 
 def with_root_extraction(w: Workload, seed: int = 0) -> Workload:
@@ -446,6 +453,70 @@ def with_root_extraction(w: Workload, seed: int = 0) -> Workload:
     r[A.CLM_RX_WEIBULL_C] = rng.uniform(2.0, 5.0, w.ncol)
     out = w.columns(0, w.ncol, name=f"{w.name}_roots")
     out.root = r
+    return out
+
+
+def with_atmos(w: Workload, seed: int = 0) -> Workload:
+    """The EnergyHydrology workload under the atmosphere-driven top boundary
+    (AtmosDrivenFluxBC, prescribed atmosphere and radiation, NoRunoff) with
+    per-column drivers: air temperature within U[-8, 8] K of the top
+    layer's temperature (the soil's own T_0 + (rho e + theta_i rho_i LH_f0) /
+    rho c, so that frozen columns meet sub-freezing air), relative humidity
+    U[0.2, 1], pressure U[80, 103] kPa, wind U[0.5, 10] m/s at U[2, 30] m,
+    gustiness 1 m/s, liquid precipitation 0 (half the columns) or
+    -U[1e-8, 5e-7] m/s, shortwave U[0, 900] W/m^2, longwave
+    U[0.7, 1] sigma T_air^4; surface parameters: dry PAR / NIR albedo
+    U[0.1, 0.3] / U[0.2, 0.45] and wet albedo U[0.5, 0.8] of the dry,
+    albedo thickness U[0.01, 0.4] m (from the top layer alone to a mean over
+    several), emissivity U[0.9, 1], z_0m U[1e-3, 5e-2] m, z_0b U[0.05, 1]
+    z_0m, dry-layer depth U[0.01, 0.02] m, evaporation exponent U[1, 3] and
+    scalar U[0.5, 2]."""
+    assert w.cfg.model == A.CLM_MODEL_ENERGY_HYDROLOGY
+    rng = np.random.Generator(np.random.PCG64(12000 + seed))
+    n = w.ncol
+    d = np.zeros((A.CLM_AT_NFIELDS, n))
+    e = w.cfg.earth
+    top = w.offsets[1:].astype(np.int64) - 1
+    ti = w.theta_i[top]
+    nu = w.params[A.CLM_P_NU]
+    tl = np.minimum(w.vartheta_l[top], nu - ti)
+    rhoc = w.params[A.CLM_P_RHOC_DS] + tl * e.rho_l * e.cp_l + ti * e.rho_i * e.cp_i
+    T_top = e.T_0 + (w.rho_e_int[top] + ti * e.rho_i * e.LH_f0) / rhoc
+    T = T_top + rng.uniform(-8.0, 8.0, n)
+    P = rng.uniform(80000.0, 103000.0, n)
+    # Magnus saturation vapour pressure (Pa), only to place q below saturation
+    e_s = 610.94 * np.exp(17.625 * (T - 273.15) / (T - 30.11))
+    q_s = 0.622 * e_s / (P - 0.378 * e_s)
+    d[A.CLM_AT_T_AIR] = T
+    d[A.CLM_AT_P_AIR] = P
+    d[A.CLM_AT_Q_AIR] = rng.uniform(0.2, 1.0, n) * q_s
+    d[A.CLM_AT_U_AIR] = rng.uniform(0.5, 10.0, n)
+    d[A.CLM_AT_H_AIR] = rng.uniform(2.0, 30.0, n)
+    d[A.CLM_AT_GUSTINESS] = 1.0
+    d[A.CLM_AT_P_LIQ] = np.where(rng.random(n) < 0.5, 0.0, -rng.uniform(1e-8, 5e-7, n))
+    d[A.CLM_AT_SW_D] = rng.uniform(0.0, 900.0, n)
+    d[A.CLM_AT_LW_D] = rng.uniform(0.7, 1.0, n) * 5.670374419e-8 * T ** 4
+    par = rng.uniform(0.1, 0.3, n)
+    nir = rng.uniform(0.2, 0.45, n)
+    d[A.CLM_AT_PAR_ALBEDO_DRY] = par
+    d[A.CLM_AT_NIR_ALBEDO_DRY] = nir
+    d[A.CLM_AT_PAR_ALBEDO_WET] = par * rng.uniform(0.5, 0.8, n)
+    d[A.CLM_AT_NIR_ALBEDO_WET] = nir * rng.uniform(0.5, 0.8, n)
+    d[A.CLM_AT_ALBEDO_TOP_THICKNESS] = rng.uniform(0.01, 0.4, n)
+    d[A.CLM_AT_EMISSIVITY] = rng.uniform(0.9, 1.0, n)
+    z0m = 10.0 ** rng.uniform(-3.0, np.log10(5e-2), n)
+    d[A.CLM_AT_Z_0M] = z0m
+    d[A.CLM_AT_Z_0B] = z0m * rng.uniform(0.05, 1.0, n)
+    d[A.CLM_AT_D_DS] = rng.uniform(0.01, 0.02, n)
+    d[A.CLM_AT_EVAP_P] = rng.uniform(1.0, 3.0, n)
+    d[A.CLM_AT_EVAP_ALPHA] = rng.uniform(0.5, 2.0, n)
+    out = w.columns(0, w.ncol, name=f"{w.name}_atmos")
+    out.cfg.bc_top_water = A.CLM_BC_ATMOS
+    out.cfg.bc_top_heat = A.CLM_BC_ATMOS
+    out.cfg.runoff = A.CLM_RUNOFF_NONE
+    out.forcing = {k: v for k, v in out.forcing.items()
+                   if k not in (A.CLM_BC_TOP_WATER, A.CLM_BC_TOP_HEAT)}
+    out.atmos = d
     return out
 
 

@@ -67,6 +67,8 @@ struct clm_handle {
   double *d_zlo = nullptr, *d_zhi = nullptr, *d_prm = nullptr, *d_lkap = nullptr;
   double* d_forc[4] = {nullptr, nullptr, nullptr, nullptr};
   double* d_rx = nullptr;  // root-extraction canopy rows (sorted), or null
+  double* d_atm = nullptr; // atmosphere drivers of CLM_BC_ATMOS (sorted), or null
+  AtmosK ak{};             // constants of CLM_BC_ATMOS
   double *d_v = nullptr, *d_ti = nullptr, *d_e = nullptr, *d_Fw = nullptr, *d_Fe = nullptr;
   uint32_t* d_flags = nullptr;
   int32_t* d_iters = nullptr;
@@ -165,6 +167,8 @@ StepArgs step_args(const clm_handle* h) {
   A.lkap = h->d_lkap;
   for (int i = 0; i < 4; ++i) A.forc[i] = h->d_forc[i];
   A.rx = h->d_rx;
+  A.atm = h->cfg.bc_top_water == CLM_BC_ATMOS ? h->d_atm : nullptr;
+  A.ak = h->ak;
   A.v = h->d_v;
   A.ti = h->d_ti;
   A.e = h->d_e;
@@ -414,6 +418,8 @@ int ready(clm_handle* h) {
   if (!h->have_geometry) return fail(h, CLM_ERR_STATE, "clm_set_geometry has not been called");
   if (!h->have_params) return fail(h, CLM_ERR_STATE, "clm_set_params has not been called");
   if (!h->have_state) return fail(h, CLM_ERR_STATE, "clm_set_state has not been called");
+  if (h->cfg.bc_top_water == CLM_BC_ATMOS && !h->d_atm)
+    return fail(h, CLM_ERR_STATE, "clm_set_atmos has not been called");
   return CLM_OK;
 }
 
@@ -532,11 +538,17 @@ int clm_create(const clm_config* cfg, clm_handle** out) {
   for (int i = 0; i < 4; ++i) {
     const int k = kinds[i];
     const bool runoff_top = (i == 0 && k == CLM_BC_PRECIP_RUNOFF);
-    if (!runoff_top && (k < CLM_BC_FLUX || k > CLM_BC_FLUX_ADVECTIVE)) return CLM_ERR_ARG;
+    const bool atmos_top = (i < 2 && k == CLM_BC_ATMOS);
+    if (!runoff_top && !atmos_top && (k < CLM_BC_FLUX || k > CLM_BC_FLUX_ADVECTIVE)) return CLM_ERR_ARG;
   }
   if (cfg->bc_top_water == CLM_BC_PRECIP_RUNOFF &&
       (cfg->model != CLM_MODEL_RICHARDS || cfg->runoff < CLM_RUNOFF_NONE || cfg->runoff > CLM_RUNOFF_TOPMODEL))
-    return CLM_ERR_ARG;  // the EnergyHydrology atmosphere-driven BC is not built
+    return CLM_ERR_ARG;
+  // AtmosDrivenFluxBC sets both top fluxes of EnergyHydrology (NoRunoff)
+  if ((cfg->bc_top_water == CLM_BC_ATMOS) != (cfg->bc_top_heat == CLM_BC_ATMOS)) return CLM_ERR_ARG;
+  if (cfg->bc_top_water == CLM_BC_ATMOS &&
+      (cfg->model != CLM_MODEL_ENERGY_HYDROLOGY || cfg->runoff != CLM_RUNOFF_NONE))
+    return CLM_ERR_ARG;
   if (cfg->bc_top_water == CLM_BC_FREE_DRAINAGE || cfg->bc_top_water == CLM_BC_FLUX_ADVECTIVE ||
       cfg->bc_bottom_water == CLM_BC_FLUX_ADVECTIVE || cfg->bc_top_heat == CLM_BC_FREE_DRAINAGE ||
       cfg->bc_bottom_heat == CLM_BC_FLUX_ADVECTIVE)
@@ -605,6 +617,7 @@ void clm_destroy(clm_handle* h) {
   dfree(h->d_zlo); dfree(h->d_zhi); dfree(h->d_prm); dfree(h->d_lkap);
   for (auto& p : h->d_forc) dfree(p);
   dfree(h->d_rx);
+  dfree(h->d_atm);
   dfree(h->d_v); dfree(h->d_ti); dfree(h->d_e); dfree(h->d_Fw); dfree(h->d_Fe);
   dfree(h->d_flags); dfree(h->d_iters); dfree(h->d_stage); dfree(h->d_colstage); dfree(h->d_guess);
   dfree(h->d_scratch);
@@ -734,6 +747,9 @@ int clm_set_root_extraction(clm_handle* h, const double* r, int32_t nfields) {
   }
   if (!is_eh(h))
     return fail(h, CLM_ERR_ARG, "root extraction is an EnergyHydrology source");
+  if (h->cfg.bc_top_water == CLM_BC_ATMOS)
+    return fail(h, CLM_ERR_UNSUPPORTED,
+                "root extraction with the standalone-soil atmosphere-driven boundary");
   if (nfields != CLM_RX_NFIELDS) return fail(h, CLM_ERR_ARG, "expected CLM_RX_NFIELDS rows");
   const int ncol = h->ncol;
   for (int64_t i = 0; i < (int64_t)nfields * ncol; ++i)
@@ -752,6 +768,80 @@ int clm_set_root_extraction(clm_handle* h, const double* r, int32_t nfields) {
     CLM_CUDA(h, cudaMemsetAsync(h->d_rx, 0, sizeof(double) * h->stride * CLM_RX_NFIELDS, h->stream));
   }
   int rc = upload_cols_sorted(h, r, h->d_rx, nfields);
+  if (rc != CLM_OK) return rc;
+  CLM_CUDA(h, cudaStreamSynchronize(h->stream));
+  return CLM_OK;
+}
+
+void clm_atmos_params_default(clm_atmos_params* a) {
+  if (!a) return;
+  std::memset(a, 0, sizeof *a);
+  a->stefan = 5.670374419e-8;
+  a->gas_constant = 8.3144598;
+  a->molmass_dryair = 0.02897;
+  a->molmass_water = 0.01801528;
+  a->D_vapor = 2.5e-5;
+  a->LH_v0 = 2500800.0;
+  a->LH_s0 = 2834400.0;
+  a->cp_d = 1004.5;
+  a->cp_v = 1859.0;
+  a->T_triple = 273.16;
+  a->press_triple = 611.657;
+  a->von_karman = 0.4;
+  a->Pr_0 = 0.74;
+  a->a_m = 4.7;
+  a->a_h = 4.7;
+  a->b_m = 15.0;
+  a->b_h = 9.0;
+  a->zeta_max = 100.0;
+  a->iterations = 10;
+}
+
+int clm_set_atmos(clm_handle* h, const clm_atmos_params* prm, const double* d, int32_t nfields) {
+  if (!h) return CLM_ERR_ARG;
+  if (!h->have_geometry) return fail(h, CLM_ERR_STATE, "clm_set_geometry has not been called");
+  if (!d) {
+    if (h->d_atm) drop_graphs(h);
+    dfree(h->d_atm);
+    return CLM_OK;
+  }
+  if (h->cfg.bc_top_water != CLM_BC_ATMOS)
+    return fail(h, CLM_ERR_ARG, "the top boundary is not CLM_BC_ATMOS");
+  if (nfields != CLM_AT_NFIELDS) return fail(h, CLM_ERR_ARG, "expected CLM_AT_NFIELDS rows");
+  clm_atmos_params a;
+  if (prm) a = *prm; else clm_atmos_params_default(&a);
+  const double pos[] = {a.stefan, a.gas_constant, a.molmass_dryair, a.molmass_water, a.D_vapor,
+                        a.cp_d, a.cp_v, a.T_triple, a.press_triple, a.von_karman, a.Pr_0,
+                        a.zeta_max};
+  for (double x : pos)
+    if (!(x > 0) || !std::isfinite(x)) return fail(h, CLM_ERR_ARG, "invalid clm_atmos_params constant");
+  const double fin[] = {a.LH_v0, a.LH_s0, a.a_m, a.a_h, a.b_m, a.b_h};
+  for (double x : fin)
+    if (!std::isfinite(x) || x < 0) return fail(h, CLM_ERR_ARG, "invalid clm_atmos_params constant");
+  if (a.iterations < 1 || a.iterations > 1000) return fail(h, CLM_ERR_ARG, "iterations must be in [1, 1000]");
+  const int ncol = h->ncol;
+  for (int64_t i = 0; i < (int64_t)nfields * ncol; ++i)
+    if (!std::isfinite(d[i])) return fail(h, CLM_ERR_ARG, "non-finite atmosphere driver");
+  for (int c = 0; c < ncol; ++c) {
+    auto at = [&](int f) { return d[(int64_t)f * ncol + c]; };
+    bool ok = at(CLM_AT_T_AIR) > 0 && at(CLM_AT_P_AIR) > 0 && at(CLM_AT_Q_AIR) >= 0 &&
+              at(CLM_AT_Q_AIR) < 1 && at(CLM_AT_GUSTINESS) >= 0 &&
+              (std::fabs(at(CLM_AT_U_AIR)) > 0 || at(CLM_AT_GUSTINESS) > 0) && at(CLM_AT_Z_0M) > 0 &&
+              at(CLM_AT_Z_0B) > 0 && at(CLM_AT_H_AIR) > at(CLM_AT_Z_0M) && at(CLM_AT_H_AIR) > at(CLM_AT_Z_0B) &&
+              at(CLM_AT_ALBEDO_TOP_THICKNESS) > 0 && at(CLM_AT_D_DS) >= 0 && at(CLM_AT_EVAP_ALPHA) >= 0 &&
+              at(CLM_AT_EMISSIVITY) >= 0 && at(CLM_AT_EMISSIVITY) <= 1;
+    for (int f = CLM_AT_PAR_ALBEDO_DRY; f <= CLM_AT_NIR_ALBEDO_WET; ++f) ok = ok && at(f) >= 0 && at(f) <= 1;
+    if (!ok) return fail(h, CLM_ERR_ARG, "invalid atmosphere drivers in column " + std::to_string(c));
+  }
+  if (!h->d_atm) {
+    drop_graphs(h);
+    CLM_CUDA(h, cudaMalloc(&h->d_atm, sizeof(double) * h->stride * CLM_AT_NFIELDS));
+    CLM_CUDA(h, cudaMemsetAsync(h->d_atm, 0, sizeof(double) * h->stride * CLM_AT_NFIELDS, h->stream));
+  }
+  // graphs hold StepArgs (with the constants) by value
+  drop_graphs(h);
+  h->ak = make_atmos_k(a, h->cfg.earth);
+  int rc = upload_cols_sorted(h, d, h->d_atm, nfields);
   if (rc != CLM_OK) return rc;
   CLM_CUDA(h, cudaStreamSynchronize(h->stream));
   return CLM_OK;

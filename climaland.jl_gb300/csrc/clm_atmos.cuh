@@ -1,0 +1,258 @@
+// Atmosphere-driven top boundary of EnergyHydrology (CLM_BC_ATMOS):
+// AtmosDrivenFluxBC with a prescribed atmosphere and radiation on a
+// standalone soil column (src/standalone/Soil/boundary_conditions.jl:610-677,
+// 870-936; energy_hydrology.jl:910-1368; shared_utilities/drivers.jl:
+// 369-382, 699-716). Evaluated once per column and step at the explicit
+// stage, in FP64 on both precision paths, from the update_aux values of the
+// top layers:
+//
+//   surface state      T_sfc, psi_sfc, Tf_depressed_sfc of the top centre;
+//                      theta_l extrapolated to the surface from the top two
+//                      centres (Domains.jl:883-895);
+//   humidity           q_vap_saturation (Clausius-Clapeyron with latent heat
+//                      linear in T) over liquid, times the Kelvin factor
+//                      exp(g min(psi, 0) M_w / (R T)), or over ice
+//                      (energy_hydrology.jl:1037-1060);
+//   soil conductance   D_vapor / max(dsl, eps), dsl the dry-layer thickness
+//                      of Swenson et al. 2012 (:1338-1368);
+//   turbulent fluxes   Monin-Obukhov similarity at point values with the
+//                      Businger-Dyer functions, a fixed number of
+//                      fixed-point steps on zeta = dz / L_MO with the
+//                      surface humidity re-evaluated from the heat
+//                      conductance in each (update_q_vap_sfc_at_a_point,
+//                      :1066-1099);
+//   radiation          R_n = -(1 - alpha) SW_d - eps (LW_d - sigma T^4), the
+//                      CLM two-band albedo over the top layers
+//                      (soil_albedo.jl:146-198);
+//   top fluxes         water P_liq + E_liq, energy R_n + LHF + SHF +
+//                      P_liq rho e_liq(T_air) (NoRunoff); the sublimation
+//                      part of E leaves theta_i (SoilSublimation, :931-947).
+//
+// SurfaceFluxes.jl and Thermodynamics.jl are not among the reference
+// sources; the saturation humidity and the similarity solve restate the
+// published formulations (constants in clm_atmos_params).
+
+#pragma once
+
+#include "clm_physics.cuh"
+
+namespace clm {
+
+constexpr double kHalfPi = 1.57079632679489661923;
+
+// Constants of the boundary, derived once per handle.
+struct AtmosK {
+  double stefan, D_vapor, LH_v0, cp_d, cp_v, von_karman;
+  double R_d, R_v, delta;    // delta = R_v / R_d - 1
+  double Mw_over_R;          // M_w / R (Kelvin factor)
+  double Pr_0, a_m, a_h_over_Pr, b_m, b_h, zeta_max;
+  int iterations;
+  // saturation vapour pressure, liquid [0] / ice [1]:
+  // p_v = p_tr exp(ex ln(T / T_tr) + cc (1 / T_tr - 1 / T))
+  double ex[2], cc[2];
+  double inv_T_tr, p_tr_over_R_v;
+};
+
+inline AtmosK make_atmos_k(const clm_atmos_params& a, const clm_earth_params& e) {
+  AtmosK K;
+  K.stefan = a.stefan;
+  K.D_vapor = a.D_vapor;
+  K.LH_v0 = a.LH_v0;
+  K.cp_d = a.cp_d;
+  K.cp_v = a.cp_v;
+  K.von_karman = a.von_karman;
+  K.R_d = a.gas_constant / a.molmass_dryair;
+  K.R_v = a.gas_constant / a.molmass_water;
+  K.delta = K.R_v / K.R_d - 1.0;
+  K.Mw_over_R = a.molmass_water / a.gas_constant;
+  K.Pr_0 = a.Pr_0;
+  K.a_m = a.a_m;
+  K.a_h_over_Pr = a.a_h / a.Pr_0;
+  K.b_m = a.b_m;
+  K.b_h = a.b_h;
+  K.zeta_max = a.zeta_max;
+  K.iterations = a.iterations;
+  const double LH0[2] = {a.LH_v0, a.LH_s0};
+  const double cpc[2] = {e.cp_l, e.cp_i};
+  for (int i = 0; i < 2; ++i) {
+    const double dcp = a.cp_v - cpc[i];
+    K.ex[i] = dcp / K.R_v;
+    K.cc[i] = (LH0[i] - dcp * e.T_0) / K.R_v;
+  }
+  K.inv_T_tr = 1.0 / a.T_triple;
+  K.p_tr_over_R_v = a.press_triple / K.R_v;
+  return K;
+}
+
+// x^y for x > 0
+CLM_HD double powp(const Tables& Tb, double x, double y) { return fm::exp(Tb, y * fm::log(Tb, x)); }
+
+// q_vap_saturation(T, rho, phase) = p_v,sat(T) / (rho R_v T)
+CLM_HD double q_sat(const Tables& Tb, const AtmosK& K, double T, double rho, int ice) {
+  const double pv_over_Rv =
+      K.p_tr_over_R_v * fm::exp(Tb, K.ex[ice] * fm::log(Tb, T * K.inv_T_tr) + K.cc[ice] * (K.inv_T_tr - 1.0 / T));
+  return pv_over_Rv / (rho * T);
+}
+
+// Businger-Dyer integrated stability functions
+CLM_HD double psi_m(const Tables& Tb, const AtmosK& K, double zeta) {
+  if (zeta >= 0.0) return -K.a_m * zeta;
+  const double x = sqrt(sqrt(1.0 - K.b_m * zeta));
+  return 2.0 * fm::log(Tb, (1.0 + x) * 0.5) + fm::log(Tb, (1.0 + x * x) * 0.5) - 2.0 * atan(x) + kHalfPi;
+}
+
+CLM_HD double psi_h(const Tables& Tb, const AtmosK& K, double zeta) {
+  if (zeta >= 0.0) return -K.a_h_over_Pr * zeta;
+  return 2.0 * fm::log(Tb, (1.0 + sqrt(1.0 - K.b_h * zeta)) * 0.5);
+}
+
+// S_c of the closure (retention_models.jl:42, :64)
+CLM_HD double closure_S_c(const Tables& Tb, const VG& g) {
+  return powp(Tb, 1.0 + powp(Tb, (g.n - 1.0) * g.inv_n, 1.0 - 2.0 * g.n), -g.m);
+}
+CLM_HD double closure_S_c(const Tables& Tb, const BC& g) { return powp(Tb, 1.0 + 1.0 / g.c, -g.c); }
+
+// The update_aux values the boundary reads.
+struct AtmosSfc {
+  double T, Tf, psi;    // top centre
+  double th1, th2;      // theta_l of the top two centres
+  double z1, z2;        // their coordinates
+  double dz_top;        // top centre to the surface
+  double th_alb;        // theta_l for the albedo (top-thickness mean or top centre)
+  double ti;            // theta_i of the top centre
+};
+
+struct AtmosOut {
+  double top_w, top_h;  // top_bc.water, top_bc.heat
+  double vice;          // turbulent_fluxes.vapor_flux_ice (sublimation source)
+  double lhf, shf, vliq, R_n, q_sfc;
+};
+
+// Field f of slot s in the per-slot driver rows.
+struct AtmosRow {
+  const double* a;
+  int st, s;
+  CLM_HD double operator()(int f) const { return a[(int64_t)f * st + s]; }
+};
+
+template <class CM>
+CLM_HD AtmosOut atmos_bc(const Tables& Tb, const AtmosK& K, const Earth& E, const AtmosRow& D,
+                         const CM& g, double nu, double theta_r, const AtmosSfc& sf) {
+  const double T_air = D(CLM_AT_T_AIR), q_air = D(CLM_AT_Q_AIR), h_air = D(CLM_AT_H_AIR);
+  const double P_liq = D(CLM_AT_P_LIQ);
+  const double grav = E.grav;
+  // air and surface densities (ideal gas; adiabatic extrapolation to T_sfc)
+  const double R_m = K.R_d + (K.R_v - K.R_d) * q_air;
+  const double cv_d = K.cp_d - K.R_d;
+  const double cv_m = cv_d + ((K.cp_v - K.R_v) - cv_d) * q_air;
+  const double cp_m = K.cp_d + (K.cp_v - K.cp_d) * q_air;
+  const double rho_air = D(CLM_AT_P_AIR) / (R_m * T_air);
+  const double rho_sfc = rho_air * powp(Tb, sf.T / T_air, cv_m / R_m);
+  // saturated surface humidity (component_specific_humidity)
+  double qsat;
+  if (sf.T > sf.Tf)
+    qsat = q_sat(Tb, K, sf.T, rho_sfc, 0) *
+           fm::exp(Tb, grav * fmin(sf.psi, 0.0) * K.Mw_over_R / sf.T);
+  else
+    qsat = q_sat(Tb, K, sf.T, rho_sfc, 1);
+  // soil vapour conductance from the surface liquid fraction
+  double th_sfc = (sf.th1 - sf.th2) / (sf.z1 - sf.z2) * (sf.dz_top + sf.z1 - sf.z2) + sf.th2;
+  th_sfc = fmax(th_sfc, theta_r + kEps);
+  const double S_l = saturation(nu, th_sfc, theta_r).S;
+  const double aSc = fmin(fmax(D(CLM_AT_EVAP_ALPHA) * closure_S_c(Tb, g), 0.0), 1.0);
+  const double dsl = S_l < aSc ? D(CLM_AT_D_DS) * powp(Tb, (aSc - S_l) / S_l, D(CLM_AT_EVAP_P)) : 0.0;
+  const double g_soil = K.D_vapor / fmax(dsl, kEps);
+  const double r = sf.ti / nu;
+  const double beta_ice = (r * r) * (r * r);
+  const bool subl = sf.T < sf.Tf;
+  // Monin-Obukhov similarity
+  const double dz = h_air;
+  const double U = fmax(fabs(D(CLM_AT_U_AIR)), D(CLM_AT_GUSTINESS));
+  const double z0m = D(CLM_AT_Z_0M), z0b = D(CLM_AT_Z_0B);
+  const double lm = fm::log(Tb, dz / z0m), lh = fm::log(Tb, dz / z0b);
+  const double thv_air = (T_air + grav * dz / K.cp_d) * (1.0 + K.delta * q_air);
+  const double gU = grav * dz / (U * U);
+  double zeta = 0.0, g_h = 0.0, q_sfc = qsat;
+  for (int it = 0;; ++it) {
+    const double F_m = lm - psi_m(Tb, K, zeta) + psi_m(Tb, K, zeta * z0m / dz);
+    const double F_h = K.Pr_0 * (lh - psi_h(Tb, K, zeta) + psi_h(Tb, K, zeta * z0b / dz));
+    const double ustar = K.von_karman * U / F_m;
+    g_h = K.von_karman * ustar / F_h;
+    if (subl)
+      q_sfc = q_air < qsat ? beta_ice * qsat + (1.0 - beta_ice) * q_air : qsat;
+    else
+      q_sfc = (g_soil / g_h * qsat + q_air) / (1.0 + g_soil / g_h);
+    if (it >= K.iterations) break;
+    const double thv_sfc = sf.T * (1.0 + K.delta * q_sfc);
+    const double Ri = gU * (thv_air - thv_sfc) / thv_sfc;
+    zeta = fmin(fmax(Ri * F_m * F_m / F_h, -K.zeta_max), K.zeta_max);
+  }
+  AtmosOut o;
+  const double Ev = -rho_sfc * g_h * (q_air - q_sfc);
+  o.lhf = K.LH_v0 * Ev;
+  o.shf = -rho_sfc * cp_m * g_h * (T_air + grav * dz / cp_m - sf.T);
+  const double Et = Ev / E.rho_l;
+  const double is_liq = (sf.T - sf.Tf > kEps) ? 1.0 : 0.0;
+  o.vliq = Et * is_liq;
+  o.vice = Et * (1.0 - is_liq);
+  // net radiation with the two-band albedo
+  const double S_a = saturation(nu, sf.th_alb, theta_r).S;
+  const double a_par = (1.0 - S_a) * D(CLM_AT_PAR_ALBEDO_DRY) + S_a * D(CLM_AT_PAR_ALBEDO_WET);
+  const double a_nir = (1.0 - S_a) * D(CLM_AT_NIR_ALBEDO_DRY) + S_a * D(CLM_AT_NIR_ALBEDO_WET);
+  const double alpha = a_par * 0.5 + a_nir * 0.5;
+  const double T2 = sf.T * sf.T;
+  o.R_n = -(1.0 - alpha) * D(CLM_AT_SW_D) - D(CLM_AT_EMISSIVITY) * (D(CLM_AT_LW_D) - K.stefan * (T2 * T2));
+  o.q_sfc = q_sfc;
+  o.top_w = P_liq + o.vliq;
+  o.top_h = ((o.R_n + o.lhf) + o.shf) + P_liq * rho_e_liq(E, T_air);
+  return o;
+}
+
+// Tf_depressed as update_aux computes it (energy_hydrology.jl:797-808 passes
+// (rho_l, rho_i) into the (rho_ice, rho_liq) slots of soil_Tf_depressed).
+template <class CM>
+CLM_HD double tf_depressed_aux(const Tables& Tb, const Earth& E, const CM& g, double nu,
+                               double theta_r, double theta_l, double theta_i) {
+  const double tt = fmin(E.rho_l / E.rho_i * theta_i + theta_l, nu);
+  const double pw = matric_of(Tb, g, nu, tt, theta_r);
+  return fmax(E.T_freeze * fm::exp(Tb, E.grav_over_LH_f0 * pw), 1.0);
+}
+
+// Layer geometry of a uniform column [z_lo, z_hi] with n layers, as the
+// reference's domain builds it: faces z_lo + (z_hi - z_lo) k / n (the top
+// face z_hi), centres the face midpoints.
+struct ColGeom {
+  double zlo, zhi;
+  int n;
+  CLM_HD double face(int k) const { return k == n ? zhi : zlo + (zhi - zlo) * ((double)k / n); }
+  CLM_HD double centre(int k) const { return 0.5 * (face(k) + face(k + 1)); }
+  CLM_HD double width(int k) const { return face(k + 1) - face(k); }
+};
+
+// theta_l for the albedo: the mean over the layers centred within
+// `thick` of the surface when the thinnest layer is thinner than it
+// (column_integral_definite of H theta_l / N), else the top centre's.
+template <class ThetaL>
+CLM_HD double albedo_theta(const ColGeom& G, double thick, ThetaL theta_l) {
+  double dz_min = G.width(0);
+  for (int k = 1; k < G.n; ++k) dz_min = fmin(dz_min, G.width(k));
+  if (!(dz_min < thick)) return theta_l(G.n - 1);
+  const double z_sfc = G.zhi;
+  double N = 0.0;
+  for (int k = 0; k < G.n; ++k)
+    N += G.width(k) * (((thick + kSqrtEps) - (z_sfc - G.centre(k)) > kEps) ? 1.0 : 0.0);
+  double I = 0.0;
+  for (int k = 0; k < G.n; ++k) {
+    const double H = ((thick + kSqrtEps) - (z_sfc - G.centre(k)) > kEps) ? 1.0 : 0.0;
+    if (H != 0.0) I += G.width(k) * (H * theta_l(k) / N);
+  }
+  return I;
+}
+
+// SoilSublimation's factor for layer k: H(z_k + 2 dz_top) / (2 dz_top), with
+// the reference's absolute coordinates.
+CLM_HD double sublimation_weight(const ColGeom& G, int k, double dz_top) {
+  return (((G.centre(k) + 2.0 * dz_top) - 0.0 > kEps) ? 1.0 : 0.0) / (2.0 * dz_top);
+}
+
+}  // namespace clm

@@ -107,6 +107,36 @@ __device__ void closure_column(const ClosureArgs& C, const Tables& Tb) {
     else if (A.bc_bh == CLM_BC_STATE) Fbh = -kapc[0] * (Tc[0] - fbh) / half;
   }
   const bool dflux = !eh && A.bc_tw == CLM_BC_STATE;
+  // atmosphere-driven top boundary (CLM_BC_ATMOS) from the aux values above
+  const ColGeom G{A.z_lo[s], A.z_hi[s], n};
+  AtmosOut ab{};
+  double dz_top = 0.0;
+  const bool atmos = eh && A.atm && A.bc_tw == CLM_BC_ATMOS;
+  if (atmos) {
+    AtmosSfc sf;
+    sf.T = Tc[n - 1];
+    sf.psi = psic[n - 1];
+    sf.ti = C.ti[o + n - 1];
+    sf.th1 = tlc[n - 1];
+    sf.th2 = tlc[n - 2];
+    sf.Tf = tf_depressed_aux(Tb, E, g, nu, theta_r, sf.th1, sf.ti);
+    sf.z1 = G.centre(n - 1);
+    sf.z2 = G.centre(n - 2);
+    dz_top = G.zhi - sf.z1;
+    sf.dz_top = dz_top;
+    const AtmosRow D{A.atm, st, s};
+    sf.th_alb = albedo_theta(G, D(CLM_AT_ALBEDO_TOP_THICKNESS), [&](int k) { return tlc[k]; });
+    ab = atmos_bc(Tb, A.ak, E, D, g, nu, theta_r, sf);
+    Ftw = ab.top_w;
+    Fth = ab.top_h;
+  }
+  if (KIND == CL_ATM) {
+    if (atmos && C.atm_out) {
+      const double vals[CLM_AF_NFIELDS] = {ab.lhf, ab.shf, ab.vliq, ab.vice, ab.R_n, ab.q_sfc, ab.top_w, ab.top_h};
+      for (int f = 0; f < CLM_AF_NFIELDS; ++f) C.atm_out[(int64_t)f * ncol + orig] = vals[f];
+    }
+    return;
+  }
 
   if (KIND == CL_AUX) {
     for (int k = 0; k < n; ++k) {
@@ -150,6 +180,7 @@ __device__ void closure_column(const ClosureArgs& C, const Tables& Tb) {
         dv = -pc;
         dti = E.rho_l_over_rho_i * pc;
       }
+      if (atmos) dti += -ab.vice * E.rho_l / E.rho_i * sublimation_weight(G, k, dz_top);
       if (roots) {
         const double zlo = A.z_lo[s], zhi = A.z_hi[s];
         const double zc = 0.5 * ((zlo + (zhi - zlo) * ((double)k / n)) +
@@ -165,7 +196,7 @@ __device__ void closure_column(const ClosureArgs& C, const Tables& Tb) {
       if (eh && C.dti) C.dti[o + k] = dti;
       if (eh && C.de) C.de[o + k] = de;
     }
-    if (C.dFw) C.dFw[orig] = root_w;
+    if (C.dFw) C.dFw[orig] = atmos ? 0.0 + -ab.vice : root_w;
     if (eh && C.dFe) C.dFe[orig] = root_e;
     return;
   }
@@ -282,6 +313,7 @@ cudaError_t launch_closure(int kind, const ClosureArgs& C, cudaStream_t st) {
     case CL_AUX: closure_kernel<CL_AUX><<<blocks, 128, 0, st>>>(C); break;
     case CL_EXP: closure_kernel<CL_EXP><<<blocks, 128, 0, st>>>(C); break;
     case CL_IMP: closure_kernel<CL_IMP><<<blocks, 128, 0, st>>>(C); break;
+    case CL_ATM: closure_kernel<CL_ATM><<<blocks, 128, 0, st>>>(C); break;
     default: closure_kernel<CL_JAC><<<blocks, 128, 0, st>>>(C); break;
   }
   return cudaGetLastError();

@@ -8,7 +8,7 @@
 
 namespace clm {
 
-enum ClosureKind { CL_AUX = 0, CL_EXP = 1, CL_IMP = 2, CL_JAC = 3 };
+enum ClosureKind { CL_AUX = 0, CL_EXP = 1, CL_IMP = 2, CL_JAC = 3, CL_ATM = 4 };
 
 struct ClosureArgs {
   StepArgs A;              // parameters, forcing, config (state pointers unused)
@@ -24,6 +24,7 @@ struct ClosureArgs {
   double* bc;                                  // [4][ncol] original column order
   double *dv, *dti, *de, *dFw, *dFe;           // EXP / IMP
   double *Wvv, *Wev, *Wee;                     // JAC: 3 per cell
+  double* atm_out;                             // ATM: [CLM_AF_NFIELDS][ncol] original order
 };
 
 struct SolveArgs {

@@ -176,6 +176,26 @@ int clm_update_aux(clm_handle* h, double t, double* K, double* psi, double* thet
   return CLM_OK;
 }
 
+int clm_atmos_fluxes(clm_handle* h, double* out, int32_t nfields) {
+  int rc = closure_ready(h);
+  if (rc != CLM_OK) return rc;
+  if (handle_step_args(h).bc_tw != CLM_BC_ATMOS)
+    return handle_fail(h, CLM_ERR_ARG, "the top boundary is not CLM_BC_ATMOS");
+  if (!out || nfields != CLM_AF_NFIELDS) return handle_fail(h, CLM_ERR_ARG, "expected CLM_AF_NFIELDS rows");
+  Scratch S;
+  ClosureArgs C = base_args(h);
+  rc = state_ref(h, S, &C.v, &C.ti, &C.e);
+  if (rc != CLM_OK) return rc;
+  const int ncol = handle_ncol(h);
+  cudaError_t err = cudaSuccess;
+  C.atm_out = S.get((size_t)CLM_AF_NFIELDS * ncol, err);
+  if (err != cudaSuccess) return handle_cuda_fail(h, err, "cudaMalloc");
+  CLM_CUDA(h, launch_closure(CL_ATM, C, handle_stream(h)));
+  if ((rc = copy_out(h, out, C.atm_out, (size_t)CLM_AF_NFIELDS * ncol))) return rc;
+  CLM_CUDA(h, cudaStreamSynchronize(handle_stream(h)));
+  return CLM_OK;
+}
+
 int clm_exp_tendency(clm_handle* h, double t, double* dv, double* dti, double* de, double* dFw,
                      double* dFe) {
   return tendency(h, CL_EXP, t, dv, dti, de, dFw, dFe);

@@ -50,6 +50,7 @@
 
 #include "clm_internal.cuh"
 #include "clm_physics_ff.cuh"
+#include "clm_atmos.cuh"
 
 namespace clm {
 
@@ -231,7 +232,12 @@ struct EHJac {
   Col<JT> cp, dp, d, ae;            // Thomas c', d' (then delta_v, d''), dpsi, face coef
 };
 
-template <typename JT, class CM, bool kLogKappaHere = false, bool kRoots = false>
+// Explicit sources and top boundaries compiled into a step kernel.
+constexpr int kSrcNone = 0;
+constexpr int kSrcRoots = 1;  // RootExtraction (A.rx)
+constexpr int kSrcAtmos = 2;  // atmosphere-driven top boundary + SoilSublimation (A.atm)
+
+template <typename JT, class CM, bool kLogKappaHere = false, int kSrc = kSrcNone>
 CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int orig,
                       const EHBuffers& B, const EHJac<JT>& J, double t0, double dt, int nsteps,
                       double& Fw, double& Fe, uint32_t& flags, int& iters_done) {
@@ -250,6 +256,9 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
   const PCCol pcc = make_pc_col(c.nu, c.theta_r, c.dz);
   if constexpr (mixed) MX = make_eh_mixed(Tb, E, sc, c);
   const bool tol = A.newton_mode == CLM_NEWTON_TOL;  // the increment norms are needed only then
+  constexpr bool kRoots = kSrc == kSrcRoots;
+  constexpr bool kAtmos = kSrc == kSrcAtmos;
+  const ColGeom G{A.z_lo[s], A.z_hi[s], n};
 
   bool finite = true;  // the last step's state, checked as it is stored
   for (int step = 0; step < nsteps; ++step) {
@@ -269,6 +278,35 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
     RootCol rcol;
     if constexpr (kRoots) rcol = load_root_col(Tb, A.rx, st, s);
     double root_w = 0.0, root_e = 0.0;
+    // atmosphere-driven top boundary at Y_n (update_aux values of the top
+    // layers), frozen through the Newton solve
+    AtmosOut ab{};
+    double dz_top = 0.0;
+    if constexpr (kAtmos) {
+      auto theta_l_of = [&](int k) {
+        const double Yv = B.gv[k], nu_eff = c.nu - B.gti[k];
+        const double v_safe = fmax(Yv, c.theta_r + kSqrtEps);
+        const double nu_safe = fmax(nu_eff, c.theta_r + kSqrtEps);
+        return (v_safe < nu_safe) ? v_safe : nu_safe;
+      };
+      const int k1 = n - 1;
+      const double Yv = B.gv[k1], Yti = B.gti[k1], Ye = B.ge[k1];
+      AtmosSfc sf;
+      sf.th1 = theta_l_of(k1);
+      sf.th2 = theta_l_of(k1 - 1);
+      sf.T = E.T_0 + (Ye + Yti * E.rho_i_LH_f0) * fm::rcp(heat_capacity(E, sf.th1, Yti, c.rcds));
+      double d;
+      psi_dpsi<false>(Tb, c.g, c.nu - Yti, Yv, c.theta_r, c.S_s, sf.psi, d);
+      sf.Tf = tf_depressed_aux(Tb, E, c.g, c.nu, c.theta_r, sf.th1, Yti);
+      sf.z1 = G.centre(k1);
+      sf.z2 = G.centre(k1 - 1);
+      dz_top = G.zhi - sf.z1;
+      sf.dz_top = dz_top;
+      sf.ti = Yti;
+      const AtmosRow D{A.atm, st, s};
+      sf.th_alb = albedo_theta(G, D(CLM_AT_ALBEDO_TOP_THICKNESS), theta_l_of);
+      ab = atmos_bc(Tb, A.ak, E, D, c.g, c.nu, c.theta_r, sf);
+    }
     for (int k = 0; k < n; ++k) {
       const double Yv = B.gv[k], Yti = B.gti[k], Ye = B.ge[k];
       const double nu_eff = c.nu - Yti;
@@ -312,6 +350,11 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
                    : phase_change_r(Tb, E, c.g, c.nu, c.theta_r, pcc, tl, Yti, T, inv_rc, kap, flags);
         Uv = Yv + dt * (-pc);
         Uti = Yti + dt * (E.rho_l_over_rho_i * pc);
+      }
+      if constexpr (kAtmos) {
+        // SoilSublimation after PhaseChange in the sources tuple
+        const double sub = -ab.vice * E.rho_l / E.rho_i * sublimation_weight(G, k, dz_top);
+        Uti = Yti + dt * ((A.phase_change ? E.rho_l_over_rho_i * pc : 0.0) + sub);
       }
       if constexpr (kRoots) {
         // psi at Y_n (update_aux!), the layer centre z, K and T of this stage
@@ -387,7 +430,9 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       const double fth = forcing_value(A.forc[CLM_BC_TOP_HEAT], st, s, A.col0 + orig, t, A.seed);
       const double fbw = forcing_value(A.forc[CLM_BC_BOTTOM_WATER], st, s, A.col0 + orig, t, A.seed);
       const double fbh = forcing_value(A.forc[CLM_BC_BOTTOM_HEAT], st, s, A.col0 + orig, t, A.seed);
-      if (A.bc_tw == CLM_BC_STATE) {
+      if (kAtmos) {
+        Ftw = ab.top_w;
+      } else if (A.bc_tw == CLM_BC_STATE) {
         double pb, d;
         psi_dpsi<false>(Tb, c.g, c.nu, ftw, c.theta_r, c.S_s, pb, d);
         Ftw = -Kt * ((pb + half) - psit) / half;  // diffusive_flux
@@ -403,7 +448,9 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       } else {
         Fbw = fbw;
       }
-      if (A.bc_th == CLM_BC_STATE) {
+      if (kAtmos) {
+        Fth = ab.top_h;
+      } else if (A.bc_th == CLM_BC_STATE) {
         Fth = -kapt * (fth - Tt) / half;
       } else if (A.bc_th == CLM_BC_FLUX_ADVECTIVE) {
         const double* F = A.forc[CLM_BC_TOP_HEAT];
@@ -420,7 +467,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         Fbh = fbh;
       }
     }
-    const double UFw = kRoots ? Fw + dt * root_w : Fw;
+    const double UFw = kRoots ? Fw + dt * root_w : kAtmos ? Fw + dt * (0.0 + -ab.vice) : Fw;
     const double UFe = kRoots ? Fe + dt * root_e : Fe;
     double xFw = UFw, xFe = UFe;
 

@@ -12,6 +12,7 @@
 
 #include <cstdint>
 
+#include "clm_atmos.cuh"
 #include "clm_physics.cuh"
 
 namespace clm {
@@ -55,6 +56,8 @@ struct StepArgs {
   int runoff;           // enum clm_runoff (CLM_BC_PRECIP_RUNOFF)
   int cm = CLM_CM_VAN_GENUCHTEN;  // enum clm_hydrology_cm
   const double* rx = nullptr;     // root-extraction canopy rows [CLM_RX_NFIELDS][stride], or null
+  const double* atm = nullptr;    // atmosphere drivers [CLM_AT_NFIELDS][stride] (CLM_BC_ATMOS), or null
+  AtmosK ak;                      // constants of CLM_BC_ATMOS
   int newton_mode;
   int max_iters;
   double tol;

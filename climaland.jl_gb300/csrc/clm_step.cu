@@ -6,7 +6,7 @@
 
 namespace clm {
 
-void* step_fn_bc(int model, int precision, bool roots);
+void* step_fn_bc(int model, int precision, int src);
 void launch_step_bc(const StepArgs& A, int model, int precision, int grid, dim3 block, size_t smem,
                     double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream);
 
@@ -25,8 +25,8 @@ size_t step_smem_bytes(int model, int precision, int nmax, int wpc) {
   return tab * sizeof(double) + per_layer * (size_t)nmax * kTile * wpc;
 }
 
-static void* step_fn(int model, int precision, int cm) {
-  return cm == CLM_CM_BROOKS_COREY ? step_fn_bc(model, precision, false) : step_fn_t<VG>(model, precision);
+static void* step_fn(int model, int precision, int cm, int src = kSrcNone) {
+  return cm == CLM_CM_BROOKS_COREY ? step_fn_bc(model, precision, src) : step_fn_t<VG>(model, precision, src);
 }
 
 // CTAs of `wpc` warps that can be resident on the whole device.
@@ -35,11 +35,11 @@ cudaError_t step_grid(int model, int precision, int cm, int nmax, int wpc, int n
   void* fn = step_fn(model, precision, cm);
   cudaError_t err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
-  if (model == CLM_MODEL_ENERGY_HYDROLOGY) {  // the same launch shape with root extraction
-    void* fr = cm == CLM_CM_BROOKS_COREY ? step_fn_bc(model, precision, true)
-                                         : step_fn_t<VG>(model, precision, true);
-    if ((err = cudaFuncSetAttribute(fr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
-      return err;
+  if (model == CLM_MODEL_ENERGY_HYDROLOGY) {  // the same launch shape with a source variant
+    for (int src : {kSrcRoots, kSrcAtmos})
+      if ((err = cudaFuncSetAttribute(step_fn(model, precision, cm, src),
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+        return err;
   }
   int dev = 0, nsm = 0, per_sm = 0;
   if ((err = cudaGetDevice(&dev)) != cudaSuccess) return err;

@@ -6,7 +6,7 @@
 
 namespace clm {
 
-void* step_fn_bc(int model, int precision, bool roots) { return step_fn_t<BC>(model, precision, roots); }
+void* step_fn_bc(int model, int precision, int src) { return step_fn_t<BC>(model, precision, src); }
 
 void launch_step_bc(const StepArgs& A, int model, int precision, int grid, dim3 block, size_t smem,
                     double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream) {

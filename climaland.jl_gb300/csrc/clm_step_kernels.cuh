@@ -47,9 +47,10 @@ __host__ __device__ constexpr size_t richards_smem_per_layer() {
 // energy residual.
 __host__ __device__ constexpr int eh_scratch_slots(bool mixed) { return mixed ? 6 : 7; }
 
-// kRoots: the RootExtraction source (A.rx) compiled in; a separate kernel so
-// that its registers do not weigh on the step without it.
-template <typename JT, class CM, bool kRoots>
+// kSrc: the RootExtraction source (A.rx) or the atmosphere-driven top
+// boundary (A.atm) compiled in; separate kernels so that their registers do
+// not weigh on the step without them.
+template <typename JT, class CM, int kSrc>
 __global__ void __launch_bounds__(128, 1)
     eh_step_kernel(StepArgs A, double* __restrict__ scratch, StepClock clk, int nsteps) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -111,7 +112,7 @@ __global__ void __launch_bounds__(128, 1)
       double Fw = A.Fw[s], Fe = A.Fe[s];
       uint32_t flags = 0;
       int iters = 0;
-      eh_column<JT, CM, false, kRoots>(A, Tb, s, n, A.L.perm[s], B, J, t0, dt, nsteps, Fw, Fe, flags, iters);
+      eh_column<JT, CM, false, kSrc>(A, Tb, s, n, A.L.perm[s], B, J, t0, dt, nsteps, Fw, Fe, flags, iters);
       A.Fw[s] = Fw;
       A.Fe[s] = Fe;
       A.flags[s] = flags;
@@ -168,35 +169,49 @@ __global__ void __launch_bounds__(128, 1)
   if (dyn) release_tiles(A.tile_ctr, nwarps);
 }
 
-// The kernel of (model, precision) for closure CM, and its launch.
+// The explicit source / top boundary kernel variant of a launch.
+inline int step_src(const StepArgs& A) {
+  return A.atm ? kSrcAtmos : A.rx ? kSrcRoots : kSrcNone;
+}
+
+// The kernel of (model, precision, source variant) for closure CM, and its launch.
 template <class CM>
-void* step_fn_t(int model, int precision, bool roots = false) {
+void* step_fn_t(int model, int precision, int src = kSrcNone) {
   if (model == CLM_MODEL_ENERGY_HYDROLOGY) {
-    if (roots)
-      return precision == CLM_PREC_MIXED ? (void*)eh_step_kernel<float, CM, true>
-                                         : (void*)eh_step_kernel<double, CM, true>;
-    return precision == CLM_PREC_MIXED ? (void*)eh_step_kernel<float, CM, false>
-                                       : (void*)eh_step_kernel<double, CM, false>;
+    const bool mx = precision == CLM_PREC_MIXED;
+    if (src == kSrcRoots)
+      return mx ? (void*)eh_step_kernel<float, CM, kSrcRoots> : (void*)eh_step_kernel<double, CM, kSrcRoots>;
+    if (src == kSrcAtmos)
+      return mx ? (void*)eh_step_kernel<float, CM, kSrcAtmos> : (void*)eh_step_kernel<double, CM, kSrcAtmos>;
+    return mx ? (void*)eh_step_kernel<float, CM, kSrcNone> : (void*)eh_step_kernel<double, CM, kSrcNone>;
   }
   return precision == CLM_PREC_MIXED ? (void*)richards_step_kernel<float, CM>
                                      : (void*)richards_step_kernel<double, CM>;
+}
+
+template <typename JT, class CM>
+void launch_eh_t(const StepArgs& A, int grid, dim3 block, size_t smem, double* scratch,
+                 const StepClock& clk, int nsteps, cudaStream_t stream) {
+  switch (step_src(A)) {
+    case kSrcRoots:
+      eh_step_kernel<JT, CM, kSrcRoots><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
+      break;
+    case kSrcAtmos:
+      eh_step_kernel<JT, CM, kSrcAtmos><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
+      break;
+    default:
+      eh_step_kernel<JT, CM, kSrcNone><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
+  }
 }
 
 template <class CM>
 void launch_step_t(const StepArgs& A, int model, int precision, int grid, dim3 block, size_t smem,
                    double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream) {
   if (model == CLM_MODEL_ENERGY_HYDROLOGY) {
-    if (A.rx) {
-      if (precision == CLM_PREC_MIXED)
-        eh_step_kernel<float, CM, true><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
-      else
-        eh_step_kernel<double, CM, true><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
-    } else {
-      if (precision == CLM_PREC_MIXED)
-        eh_step_kernel<float, CM, false><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
-      else
-        eh_step_kernel<double, CM, false><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
-    }
+    if (precision == CLM_PREC_MIXED)
+      launch_eh_t<float, CM>(A, grid, block, smem, scratch, clk, nsteps, stream);
+    else
+      launch_eh_t<double, CM>(A, grid, block, smem, scratch, clk, nsteps, stream);
   } else {
     if (precision == CLM_PREC_MIXED)
       richards_step_kernel<float, CM><<<grid, block, smem, stream>>>(A, clk, nsteps);

@@ -81,13 +81,20 @@ enum clm_bc_kind {
   CLM_BC_STATE = 2,           /* MoistureStateBC / TemperatureStateBC      */
   CLM_BC_FLUX_ADVECTIVE = 3,  /* heat only: F_e = f(t) + F_w,top(t) *
                                  rho e_liq(T_adv), T_adv per column        */
-  CLM_BC_PRECIP_RUNOFF = 4    /* water, top, RichardsModel:
+  CLM_BC_PRECIP_RUNOFF = 4,   /* water, top, RichardsModel:
                                  RichardsAtmosDrivenFluxBC
                                  (boundary_conditions.jl:64-100, :200-212):
                                  the top-water forcing row is the liquid
                                  precipitation P(t) (< 0 into the soil),
                                  cfg->runoff turns it into the infiltration
                                  flux at the explicit stage               */
+  CLM_BC_ATMOS = 5            /* water and heat, top, EnergyHydrology:
+                                 AtmosDrivenFluxBC with a prescribed
+                                 atmosphere and radiation, standalone soil
+                                 (boundary_conditions.jl:610-677, 870-936):
+                                 the drivers of clm_set_atmos; both top
+                                 kinds must be CLM_BC_ATMOS, cfg->runoff
+                                 CLM_RUNOFF_NONE                          */
 };
 
 /* Per-column parameter rows for clm_set_params (SoA, row p of ncol). The
@@ -201,6 +208,94 @@ enum clm_root_field {
   CLM_RX_NFIELDS = 8
 };
 
+/* Atmosphere-driven top boundary (CLM_BC_ATMOS). Per-column drivers and
+ * surface parameters for clm_set_atmos (SoA, row f of ncol), frozen through
+ * a step (the reference refreshes its drivers in a callback between steps).
+ * At the explicit stage, from the update_aux values of the top layer:
+ *   T_sfc = T_top, q_sfc from q_vap_saturation(T_sfc, rho_sfc) (liquid,
+ *   times exp(g min(psi_top, 0) M_w / (R T_sfc)), when T_sfc > Tf_depressed_top;
+ *   else ice) (energy_hydrology.jl:995-1060); the soil's vapour conductance
+ *   D_vapor / max(dsl, eps) from the surface liquid fraction linearly
+ *   extrapolated from the top two centres (:1062-1145, 1322-1368,
+ *   Domains.jl:883-895); CLMTwoBandSoilAlbedo over the top
+ *   ALBEDO_TOP_THICKNESS (soil_albedo.jl:146-198); net radiation
+ *   -(1 - alpha) SW_d - eps (LW_d - sigma T_sfc^4) (drivers.jl:699-716);
+ *   turbulent fluxes by Monin-Obukhov similarity (see clm_atmos_params);
+ *   top water flux = P_liq + E / rho_l (liquid part), top energy flux =
+ *   R_n + LHF + SHF + P_liq rho e_liq(T_air) (boundary_conditions.jl:
+ *   908-936, 988-1003); the sublimation part of E leaves theta_i of the
+ *   layers with z + 2 dz_top > eps (the top layer for a surface at z = 0) and
+ *   enters intF_w (SoilSublimation, energy_hydrology.jl:910-947). */
+enum clm_atmos_field {
+  CLM_AT_P_LIQ = 0,              /* liquid precipitation (m/s, < 0 downward)  */
+  CLM_AT_T_AIR = 1,              /* air temperature (K)                       */
+  CLM_AT_U_AIR = 2,              /* wind speed (m/s)                          */
+  CLM_AT_Q_AIR = 3,              /* specific humidity (kg/kg)                 */
+  CLM_AT_P_AIR = 4,              /* air pressure (Pa)                         */
+  CLM_AT_SW_D = 5,               /* downwelling shortwave (W/m^2)             */
+  CLM_AT_LW_D = 6,               /* downwelling longwave (W/m^2)              */
+  CLM_AT_H_AIR = 7,              /* height of the atmospheric values (m)      */
+  CLM_AT_GUSTINESS = 8,          /* gustiness (m/s): minimum wind speed       */
+  CLM_AT_PAR_ALBEDO_DRY = 9,
+  CLM_AT_NIR_ALBEDO_DRY = 10,
+  CLM_AT_PAR_ALBEDO_WET = 11,
+  CLM_AT_NIR_ALBEDO_WET = 12,    /* ConstantTwoBandSoilAlbedo: dry = wet      */
+  CLM_AT_ALBEDO_TOP_THICKNESS = 13, /* m (CLMTwoBandSoilAlbedo default 0.02) */
+  CLM_AT_EMISSIVITY = 14,
+  CLM_AT_Z_0M = 15,              /* momentum roughness length (m)             */
+  CLM_AT_Z_0B = 16,              /* scalar roughness length (m)               */
+  CLM_AT_D_DS = 17,              /* maximum dry soil layer depth (m)          */
+  CLM_AT_EVAP_P = 18,            /* evaporation exponent                      */
+  CLM_AT_EVAP_ALPHA = 19,        /* evaporation scalar                        */
+  CLM_AT_NFIELDS = 20
+};
+
+/* Constants of the atmosphere-driven boundary (ClimaParams names). The
+ * turbulent fluxes follow Monin-Obukhov similarity theory at point values
+ * with the Businger-Dyer stability functions (Businger et al. 1971; as
+ * restated here, since SurfaceFluxes.jl is not part of the reference
+ * sources):
+ *   U = max(|u|, gustiness), dz = h_air, zeta = dz / L_MO,
+ *   F_m = ln(dz/z_0m) - psi_m(zeta) + psi_m(zeta z_0m/dz),
+ *   F_h = Pr_0 (ln(dz/z_0b) - psi_h(zeta) + psi_h(zeta z_0b/dz)),
+ *   psi_m = -a_m zeta, psi_h = -a_h zeta / Pr_0 (zeta >= 0);
+ *   psi_m = 2 ln((1+x)/2) + ln((1+x^2)/2) - 2 atan x + pi/2, x = (1 - b_m zeta)^(1/4),
+ *   psi_h = 2 ln((1+y)/2), y = (1 - b_h zeta)^(1/2) (zeta < 0);
+ *   u* = kappa U / F_m, g_h = kappa u* / F_h, and zeta <- Ri_b F_m^2 / F_h
+ *   (clamped to +-zeta_max) for `iterations` fixed-point steps from 0, with
+ *   Ri_b = g dz (theta_v,air - theta_v,sfc) / (theta_v,sfc U^2),
+ *   theta_v,air = (T_air + g dz / cp_d)(1 + (R_v/R_d - 1) q_air),
+ *   theta_v,sfc = T_sfc (1 + (R_v/R_d - 1) q_sfc), and q_sfc updated from g_h
+ *   in every step by the reference's update_q_vap_sfc_at_a_point
+ *   (energy_hydrology.jl:1066-1099). Then
+ *   E = -rho_sfc g_h (q_air - q_sfc), LHF = LH_v0 E,
+ *   SHF = -rho_sfc cp_m g_h (T_air + g dz / cp_m - T_sfc),
+ *   rho_sfc = rho_air (T_sfc / T_air)^(cv_m / R_m), rho_air = P / (R_m T_air). */
+typedef struct clm_atmos_params {
+  double stefan;          /* Stefan-Boltzmann constant (W/m^2/K^4)         */
+  double gas_constant;    /* J/mol/K                                       */
+  double molmass_dryair;  /* kg/mol                                        */
+  double molmass_water;   /* kg/mol                                        */
+  double D_vapor;         /* diffusivity of water vapour in air (m^2/s)    */
+  double LH_v0, LH_s0;    /* latent heats at T_0 (J/kg)                    */
+  double cp_d, cp_v;      /* isobaric specific heats (J/kg/K)              */
+  double T_triple;        /* K                                             */
+  double press_triple;    /* Pa                                            */
+  double von_karman;
+  double Pr_0, a_m, a_h, b_m, b_h; /* Businger-Dyer                        */
+  double zeta_max;        /* |zeta| bound of the iteration                 */
+  int32_t iterations;     /* fixed-point steps (>= 1)                      */
+  int32_t pad;
+} clm_atmos_params;
+
+/* Diagnostics of clm_atmos_fluxes (row f of ncol): the reference's
+ * p.soil.turbulent_fluxes, R_n, q_sfc and top_bc at the current state. */
+enum clm_atmos_flux {
+  CLM_AF_LHF = 0, CLM_AF_SHF = 1, CLM_AF_VAPOR_LIQ = 2, CLM_AF_VAPOR_ICE = 3,
+  CLM_AF_R_N = 4, CLM_AF_Q_SFC = 5, CLM_AF_TOP_WATER = 6, CLM_AF_TOP_HEAT = 7,
+  CLM_AF_NFIELDS = 8
+};
+
 /* Physical constants (ClimaLand.Parameters.LandParameters,
  * src/shared_utilities/Parameters.jl:11-115). The Julia caller passes the
  * values of its own earth_param_set; clm_config_default fills ClimaParams
@@ -285,6 +380,21 @@ int clm_set_bc(clm_handle* h, int32_t slot, const double* soa_forcing,
  * 123-159). EnergyHydrology only (the reference defines the source for it
  * alone); the caller refreshes the values when its canopy state changes. */
 int clm_set_root_extraction(clm_handle* h, const double* soa, int32_t nfields);
+
+/* Drivers of the atmosphere-driven top boundary (CLM_BC_ATMOS): constants
+ * `prm` (NULL: clm_atmos_params_default) and CLM_AT_NFIELDS x ncol values
+ * (host pointer, SoA). Replaces the reference's update_drivers! of the
+ * PrescribedAtmosphere / PrescribedRadiativeFluxes (drivers.jl) for the
+ * soil; call again whenever the drivers change. soa = NULL removes them. */
+void clm_atmos_params_default(clm_atmos_params* prm);
+int clm_set_atmos(clm_handle* h, const clm_atmos_params* prm, const double* soa,
+                  int32_t nfields);
+
+/* The boundary's diagnostics at the current state (turbulent_fluxes!,
+ * net_radiation!, component_specific_humidity, top_bc:
+ * boundary_conditions.jl:908-936): CLM_AF_NFIELDS x ncol doubles written to
+ * the host pointer `out` (SoA, original column order). */
+int clm_atmos_fluxes(clm_handle* h, double* out, int32_t nfields);
 
 /* Prognostic state Y.soil (energy_hydrology.jl:624-625, rre.jl:282).
  * theta_i, rho_e, intF_e may be NULL for RichardsModel. */

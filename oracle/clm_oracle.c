@@ -35,6 +35,7 @@
 #define MAXL 256
 
 static const double SQRT_EPS = 1.4901161193847656e-08; /* sqrt(eps(Float64)) */
+static const double HALF_PI = 1.57079632679489661923;
 static const double EPS64 = 2.220446049250313e-16;     /* eps(Float64)        */
 
 /* ======================================================================
@@ -439,6 +440,9 @@ typedef struct { /* p.soil */
   int psi_positive;
   /* RootExtraction (soil_canopy_root_interactions.jl:8-39) */
   double root_extraction[MAXL], root_energy_extraction[MAXL];
+  /* AtmosDrivenFluxBC: turbulent_fluxes, R_n, q_sfc (CLM_AF_* order) */
+  double atmos[CLM_AF_NFIELDS];
+  int atmos_on;
 } cache_t;
 
 typedef struct {
@@ -643,6 +647,206 @@ static void richards_runoff(const col_t* C, const state_t* Y, cache_t* p, double
   }
 }
 
+/* ======================================================================
+ * Atmosphere-driven top boundary (CLM_BC_ATMOS): AtmosDrivenFluxBC with a
+ * PrescribedAtmosphere and PrescribedRadiativeFluxes on a standalone
+ * EnergyHydrology column (boundary_conditions.jl:610-677, 870-936).
+ * SurfaceFluxes.jl and Thermodynamics.jl are not among the reference
+ * sources: the saturation humidity and the Monin-Obukhov solve below are
+ * restatements of the published formulations (Clausius-Clapeyron with a
+ * latent heat linear in T; Businger et al. 1971 stability functions at
+ * point values), not of those packages' code; the declaration of
+ * clm_atmos_params spells them out.
+ * ====================================================================== */
+
+void clmo_atmos_params_default(clm_atmos_params* a) {
+  memset(a, 0, sizeof *a);
+  a->stefan = 5.670374419e-8;
+  a->gas_constant = 8.3144598;
+  a->molmass_dryair = 0.02897;
+  a->molmass_water = 0.01801528;
+  a->D_vapor = 2.5e-5;
+  a->LH_v0 = 2500800.0;
+  a->LH_s0 = 2834400.0;
+  a->cp_d = 1004.5;
+  a->cp_v = 1859.0;
+  a->T_triple = 273.16;
+  a->press_triple = 611.657;
+  a->von_karman = 0.4;
+  a->Pr_0 = 0.74;
+  a->a_m = 4.7;
+  a->a_h = 4.7;
+  a->b_m = 15.0;
+  a->b_h = 9.0;
+  a->zeta_max = 100.0;
+  a->iterations = 10;
+}
+
+/* q_vap_saturation(T, rho, Liquid() / Ice()): p_v,sat / (rho R_v T) with
+ * p_v,sat = p_tr (T / T_tr)^(dcp / R_v) exp((LH_0 - dcp T_0) / R_v (1/T_tr - 1/T)),
+ * dcp = cp_v - cp_l (cp_i), LH_0 = LH_v0 (LH_s0). */
+double clmo_q_vap_saturation(double T, double rho, int ice,
+                             const clm_atmos_params* a,
+                             const clm_earth_params* e) {
+  double R_v = a->gas_constant / a->molmass_water;
+  double LH_0 = ice ? a->LH_s0 : a->LH_v0;
+  double dcp = a->cp_v - (ice ? e->cp_i : e->cp_l);
+  double p_v = a->press_triple * pow(T / a->T_triple, dcp / R_v) *
+               exp((LH_0 - dcp * e->T_0) / R_v * (1.0 / a->T_triple - 1.0 / T));
+  return p_v / (rho * R_v * T);
+}
+
+/* energy_hydrology.jl:1352-1368 */
+double clmo_dry_soil_layer_thickness(double S_l, double aS_c, double d_ds,
+                                     double p) {
+  aS_c = fmin(fmax(aS_c, 0.0), 1.0);
+  return S_l < aS_c ? d_ds * pow((aS_c - S_l) / S_l, p) : 0.0;
+}
+
+/* energy_hydrology.jl:1338-1350 */
+double clmo_soil_conductance(double S_l, double S_c, double d_ds, double p,
+                             double alpha, double D_vapor) {
+  double dsl = clmo_dry_soil_layer_thickness(S_l, alpha * S_c, d_ds, p);
+  return D_vapor / fmax(dsl, EPS64);
+}
+
+/* Businger-Dyer integrated stability functions */
+double clmo_businger_psi_m(double zeta, const clm_atmos_params* a) {
+  if (zeta >= 0.0) return -a->a_m * zeta;
+  double x = sqrt(sqrt(1.0 - a->b_m * zeta));
+  return 2.0 * log((1.0 + x) / 2.0) + log((1.0 + x * x) / 2.0) - 2.0 * atan(x) +
+         HALF_PI;
+}
+
+double clmo_businger_psi_h(double zeta, const clm_atmos_params* a) {
+  if (zeta >= 0.0) return -a->a_h * zeta / a->Pr_0;
+  double y = sqrt(1.0 - a->b_h * zeta);
+  return 2.0 * log((1.0 + y) / 2.0);
+}
+
+/* S_c of the closure (retention_models.jl:42, :64) */
+static double hcm_S_c(const hcm_t* h) {
+  if (h->bc) return pow(1.0 + 1.0 / h->c, -h->c);
+  return pow(1.0 + pow((h->n - 1.0) / h->n, 1.0 - 2.0 * h->n), -h->m);
+}
+
+/* update_q_vap_sfc_at_a_point (energy_hydrology.jl:1066-1099) */
+static double q_sfc_update(double g_h, double q_air, double T_sfc, double Tf,
+                           double g_soil, double beta_ice, double qsat) {
+  if (T_sfc < Tf) {
+    if (q_air < qsat) return beta_ice * qsat + (1.0 - beta_ice) * q_air;
+    return qsat;
+  }
+  return (g_soil / g_h * qsat + q_air) / (1.0 + g_soil / g_h);
+}
+
+/* soil_boundary_fluxes!(::AtmosDrivenFluxBC, ::Val{(:soil,)}, ...) at the
+ * update_aux values of Y: turbulent_fluxes!, net_radiation!, NoRunoff
+ * infiltration and its energy, top_bc (boundary_conditions.jl:908-936). */
+static void atmos_top_bc(const col_t* C, const state_t* Y, cache_t* p) {
+  const clmo_problem* P = C->P;
+  const clm_atmos_params* a = &P->atm;
+  const clm_earth_params* e = &C->cfg->earth;
+  const int ncol = P->ncol, c = C->c, n = C->n;
+  const double* D = P->atmos;
+#define AT(f) D[(f) * ncol + c]
+  const double P_liq = AT(CLM_AT_P_LIQ), T_air = AT(CLM_AT_T_AIR);
+  const double u_air = AT(CLM_AT_U_AIR), q_air = AT(CLM_AT_Q_AIR);
+  const double P_air = AT(CLM_AT_P_AIR), h_air = AT(CLM_AT_H_AIR);
+  /* surface values: the top centre (component_temperature etc.) */
+  const double T_sfc = p->T[n - 1], Tf_sfc = p->Tf[n - 1], psi_sfc = p->psi[n - 1];
+  const double grav = e->grav;
+  const double R_d = a->gas_constant / a->molmass_dryair;
+  const double R_v = a->gas_constant / a->molmass_water;
+  /* air density and surface density (ideal gas; adiabatic extrapolation) */
+  const double R_m = R_d + (R_v - R_d) * q_air;
+  const double cv_m = (a->cp_d - R_d) + ((a->cp_v - R_v) - (a->cp_d - R_d)) * q_air;
+  const double cp_m = a->cp_d + (a->cp_v - a->cp_d) * q_air;
+  const double rho_air = P_air / (R_m * T_air);
+  const double rho_sfc = rho_air * pow(T_sfc / T_air, cv_m / R_m);
+  /* component_specific_humidity (:995-1060) */
+  double qsat;
+  if (T_sfc > Tf_sfc)
+    qsat = clmo_q_vap_saturation(T_sfc, rho_sfc, 0, a, e) *
+           exp(grav * fmin(psi_sfc, 0.0) * a->molmass_water / (a->gas_constant * T_sfc));
+  else
+    qsat = clmo_q_vap_saturation(T_sfc, rho_sfc, 1, a, e);
+  /* surface liquid fraction extrapolated from the top two centres
+   * (linear_interpolation_to_surface!, Domains.jl:883-895) */
+  const double f1 = p->theta_l[n - 1], f2 = p->theta_l[n - 2];
+  const double z1 = C->z[n - 1], z2 = C->z[n - 2];
+  double th_sfc = (f1 - f2) / (z1 - z2) * (C->dz_top + z1 - z2) + f2;
+  th_sfc = fmax(th_sfc, C->theta_r + EPS64);
+  const double S_l_sfc = clmo_effective_saturation(C->nu, th_sfc, C->theta_r);
+  const double g_soil = clmo_soil_conductance(S_l_sfc, hcm_S_c(&C->hcm), AT(CLM_AT_D_DS),
+                                              AT(CLM_AT_EVAP_P), AT(CLM_AT_EVAP_ALPHA),
+                                              a->D_vapor);
+  const double r = Y->ti[n - 1] / C->nu;
+  const double beta_ice = (r * r) * (r * r);
+  /* Monin-Obukhov solve */
+  const double dz = h_air;
+  const double U = fmax(fabs(u_air), AT(CLM_AT_GUSTINESS));
+  const double z0m = AT(CLM_AT_Z_0M), z0b = AT(CLM_AT_Z_0B);
+  const double lm = log(dz / z0m), lh = log(dz / z0b);
+  const double delta = R_v / R_d - 1.0;
+  const double thv_air = (T_air + grav * dz / a->cp_d) * (1.0 + delta * q_air);
+  double zeta = 0.0, F_m = 0.0, F_h = 0.0, g_h = 0.0, q_sfc = qsat;
+  for (int it = 0;; ++it) {
+    F_m = lm - clmo_businger_psi_m(zeta, a) + clmo_businger_psi_m(zeta * z0m / dz, a);
+    F_h = a->Pr_0 * (lh - clmo_businger_psi_h(zeta, a) + clmo_businger_psi_h(zeta * z0b / dz, a));
+    const double ustar = a->von_karman * U / F_m;
+    g_h = a->von_karman * ustar / F_h;
+    q_sfc = q_sfc_update(g_h, q_air, T_sfc, Tf_sfc, g_soil, beta_ice, qsat);
+    if (it >= a->iterations) break;
+    const double thv_sfc = T_sfc * (1.0 + delta * q_sfc);
+    const double Ri = grav * dz * (thv_air - thv_sfc) / (thv_sfc * U * U);
+    zeta = fmin(fmax(Ri * F_m * F_m / F_h, -a->zeta_max), a->zeta_max);
+  }
+  const double E = -rho_sfc * g_h * (q_air - q_sfc);
+  const double lhf = a->LH_v0 * E;
+  const double shf = -rho_sfc * cp_m * g_h * (T_air + grav * dz / cp_m - T_sfc);
+  const double Et = E / e->rho_l;
+  const double is_liq = clmo_heaviside(T_sfc, Tf_sfc);
+  const double vliq = Et * is_liq, vice = Et * (1.0 - is_liq);
+  /* CLMTwoBandSoilAlbedo (soil_albedo.jl:146-198) */
+  const double thick = AT(CLM_AT_ALBEDO_TOP_THICKNESS);
+  double dz_min = C->dzc[0];
+  for (int k = 1; k < n; ++k) dz_min = fmin(dz_min, C->dzc[k]);
+  double th_alb;
+  if (dz_min < thick) {
+    const double z_sfc = P->z_hi[c]; /* the top face (Domains.jl:1054) */
+    double N = 0.0, I = 0.0;
+    for (int k = 0; k < n; ++k)
+      N += C->dzc[k] * clmo_heaviside(thick + SQRT_EPS, z_sfc - C->z[k]);
+    for (int k = 0; k < n; ++k)
+      I += C->dzc[k] * (clmo_heaviside(thick + SQRT_EPS, z_sfc - C->z[k]) * p->theta_l[k] / N);
+    th_alb = I;
+  } else {
+    th_alb = p->theta_l[n - 1];
+  }
+  const double S_sfc = clmo_effective_saturation(C->nu, th_alb, C->theta_r);
+  const double a_par = (1.0 - S_sfc) * AT(CLM_AT_PAR_ALBEDO_DRY) + S_sfc * AT(CLM_AT_PAR_ALBEDO_WET);
+  const double a_nir = (1.0 - S_sfc) * AT(CLM_AT_NIR_ALBEDO_DRY) + S_sfc * AT(CLM_AT_NIR_ALBEDO_WET);
+  const double alpha = a_par / 2.0 + a_nir / 2.0;
+  const double T2 = T_sfc * T_sfc;
+  const double R_n = -(1.0 - alpha) * AT(CLM_AT_SW_D) -
+                     AT(CLM_AT_EMISSIVITY) * (AT(CLM_AT_LW_D) - a->stefan * (T2 * T2));
+  /* NoRunoff: infiltration = P_liq; its energy at the air temperature */
+  p->infiltration = P_liq;
+  p->top_w = P_liq + vliq;
+  p->top_h = R_n + lhf + shf + P_liq * clmo_volumetric_internal_energy_liq(T_air, e);
+  p->atmos[CLM_AF_LHF] = lhf;
+  p->atmos[CLM_AF_SHF] = shf;
+  p->atmos[CLM_AF_VAPOR_LIQ] = vliq;
+  p->atmos[CLM_AF_VAPOR_ICE] = vice;
+  p->atmos[CLM_AF_R_N] = R_n;
+  p->atmos[CLM_AF_Q_SFC] = q_sfc;
+  p->atmos[CLM_AF_TOP_WATER] = p->top_w;
+  p->atmos[CLM_AF_TOP_HEAT] = p->top_h;
+  p->atmos_on = 1;
+#undef AT
+}
+
 /* Boundary fluxes.
  * Richards: rre.jl:111-149 with boundary_flux! methods
  *   WaterFluxBC :168-180, MoistureStateBC top :227-264 / bottom :278-315,
@@ -666,7 +870,11 @@ static void update_boundary_fluxes(const col_t* C, const state_t* Y,
 
   /* water, top */
   p->runoff_sink = 0;
+  p->atmos_on = 0;
+  if (cfg->bc_top_water == CLM_BC_ATMOS) atmos_top_bc(C, Y, p);
   switch (cfg->bc_top_water) {
+    case CLM_BC_ATMOS:
+      break; /* set with the heat flux by atmos_top_bc */
     case CLM_BC_PRECIP_RUNOFF: /* RichardsAtmosDrivenFluxBC: boundary_conditions.jl:200-212 */
       richards_runoff(C, Y, p, f_tw);
       p->top_w = p->infiltration;
@@ -696,6 +904,8 @@ static void update_boundary_fluxes(const col_t* C, const state_t* Y,
   }
   if (C->eh) {
     switch (cfg->bc_top_heat) {
+      case CLM_BC_ATMOS:
+        break;
       case CLM_BC_STATE:
         p->top_h = diffusive_flux(p->kappa[n - 1], f_th, p->T[n - 1], C->dz_top);
         break;
@@ -805,6 +1015,16 @@ static void exp_tendency(const col_t* C, const state_t* Y, cache_t* p,
       dY->v[k] += -src;
       dY->ti[k] += (e->rho_l / e->rho_i) * src;
     }
+  }
+  /* SoilSublimation source! (energy_hydrology.jl:931-947), appended after
+   * the user sources by the EnergyHydrology constructor (:260-268) */
+  if (C->eh && p->atmos_on) {
+    const clm_earth_params* e = &C->cfg->earth;
+    const double vice = p->atmos[CLM_AF_VAPOR_ICE];
+    for (int k = 0; k < n; ++k)
+      dY->ti[k] += -vice * e->rho_l / e->rho_i *
+                   clmo_heaviside(C->z[k] + 2.0 * C->dz_top, 0.0) / (2.0 * C->dz_top);
+    dY->Fw += -vice;
   }
   /* RootExtraction source! (soil_canopy_root_interactions.jl:139-159), after
    * PhaseChange in the sources tuple */
@@ -1056,6 +1276,12 @@ static int check_problem(const clmo_problem* P) {
   if (P->cfg.hydrology_cm != CLM_CM_VAN_GENUCHTEN &&
       P->cfg.hydrology_cm != CLM_CM_BROOKS_COREY)
     return CLM_ERR_ARG;
+  if (P->cfg.bc_top_water == CLM_BC_ATMOS || P->cfg.bc_top_heat == CLM_BC_ATMOS) {
+    if (P->cfg.model != CLM_MODEL_ENERGY_HYDROLOGY || P->cfg.bc_top_water != CLM_BC_ATMOS ||
+        P->cfg.bc_top_heat != CLM_BC_ATMOS || P->cfg.runoff != CLM_RUNOFF_NONE || !P->atmos ||
+        P->root || P->atm.iterations < 1)
+      return CLM_ERR_ARG;
+  }
   if (P->cfg.bc_top_water == CLM_BC_PRECIP_RUNOFF) {
     if (P->cfg.model != CLM_MODEL_RICHARDS) return CLM_ERR_ARG;
     if (P->cfg.runoff < CLM_RUNOFF_NONE || P->cfg.runoff > CLM_RUNOFF_TOPMODEL) return CLM_ERR_ARG;
@@ -1074,6 +1300,26 @@ static void set_threads(const clmo_problem* P) {
 #else
   (void)P;
 #endif
+}
+
+int clmo_atmos_fluxes(const clmo_problem* P, const double* v, const double* ti,
+                      const double* e, double* out) {
+  int rc = check_problem(P);
+  if (rc) return rc;
+  if (P->cfg.bc_top_water != CLM_BC_ATMOS || !out) return CLM_ERR_ARG;
+  set_threads(P);
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < P->ncol; ++c) {
+    col_t C;
+    col_init(&C, P, c);
+    state_t Y;
+    cache_t p;
+    memset(&p, 0, sizeof(p));
+    state_load(&C, &Y, v, ti, e, NULL, NULL);
+    update_cache(&C, &Y, &p, 0.0);
+    for (int f = 0; f < CLM_AF_NFIELDS; ++f) out[(size_t)f * P->ncol + c] = p.atmos[f];
+  }
+  return CLM_OK;
 }
 
 int clmo_update_cache(const clmo_problem* P, const double* v, const double* ti,

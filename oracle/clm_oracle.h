@@ -32,6 +32,9 @@ typedef struct clmo_problem {
   int32_t nthreads;        /* OpenMP threads (<= 0: library default)      */
   const double* root;      /* CLM_RX_NFIELDS x ncol root-extraction canopy
                               values (EnergyHydrology), or NULL            */
+  const double* atmos;     /* CLM_AT_NFIELDS x ncol drivers of CLM_BC_ATMOS,
+                              or NULL                                      */
+  clm_atmos_params atm;    /* constants of CLM_BC_ATMOS                    */
 } clmo_problem;
 
 /* ---- pointwise physics (names follow the reference functions) -------- */
@@ -64,6 +67,21 @@ double clmo_plant_water_flux(double z1, double z2, double psi1, double psi2,
 double clmo_weibull_conductivity(double K_sat, double psi63, double c,
                                  double psi);
 double clmo_root_distribution(double z, double rooting_depth);
+/* atmosphere-driven top boundary (CLM_BC_ATMOS) */
+void clmo_atmos_params_default(clm_atmos_params* a);
+double clmo_q_vap_saturation(double T, double rho, int ice,
+                             const clm_atmos_params* a,
+                             const clm_earth_params* e);
+double clmo_dry_soil_layer_thickness(double S_l, double aS_c, double d_ds,
+                                     double p);
+double clmo_soil_conductance(double S_l, double S_c, double d_ds, double p,
+                             double alpha, double D_vapor);
+double clmo_businger_psi_m(double zeta, const clm_atmos_params* a);
+double clmo_businger_psi_h(double zeta, const clm_atmos_params* a);
+/* the boundary's diagnostics (CLM_AF_NFIELDS x ncol) at a state */
+int clmo_atmos_fluxes(const clmo_problem* P, const double* vartheta_l,
+                      const double* theta_i, const double* rho_e_int,
+                      double* out);
 double clmo_viscosity_factor(double T, double gamma, double gamma_T_ref);
 double clmo_heaviside(double x, double a);
 double clmo_soil_Tf_depressed(double theta_l, double theta_i, double nu,

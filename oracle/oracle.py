@@ -46,6 +46,8 @@ class _Problem(ctypes.Structure):
         ("forcing", ctypes.POINTER(ctypes.c_double) * 4),
         ("nthreads", ctypes.c_int32),
         ("root", ctypes.POINTER(ctypes.c_double)),
+        ("atmos", ctypes.POINTER(ctypes.c_double)),
+        ("atm", A.ClmAtmosParams),
     ]
 
 
@@ -98,6 +100,8 @@ def lib():
             "clmo_kappa_sat_frozen": [_D] * 3,
             "clmo_kappa_sat_unfrozen": [_D] * 3,
             "clmo_kappa_dry": [_D] * 4,
+            "clmo_dry_soil_layer_thickness": [_D] * 4,
+            "clmo_soil_conductance": [_D] * 6,
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -123,6 +127,17 @@ def lib():
                                 ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_int32)]
         L.clmo_budgets.restype = ctypes.c_int
         L.clmo_budgets.argtypes = [_PP, _DP, _DP, _DP, _DP, _DP]
+        apar = ctypes.POINTER(A.ClmAtmosParams)
+        L.clmo_q_vap_saturation.restype = _D
+        L.clmo_q_vap_saturation.argtypes = [_D, _D, ctypes.c_int, apar, ep]
+        for nm in ("clmo_businger_psi_m", "clmo_businger_psi_h"):
+            f = getattr(L, nm)
+            f.restype = _D
+            f.argtypes = [_D, apar]
+        L.clmo_atmos_params_default.restype = None
+        L.clmo_atmos_params_default.argtypes = [apar]
+        L.clmo_atmos_fluxes.restype = ctypes.c_int
+        L.clmo_atmos_fluxes.argtypes = [_PP, _DP, _DP, _DP, _DP]
         L.clmo_runoff.restype = ctypes.c_int
         L.clmo_runoff.argtypes = [_PP, _DP, _D] + [_DP] * 4
         _lib = L
@@ -164,6 +179,10 @@ class Oracle:
         P.nthreads = int(nthreads if nthreads else (os.cpu_count() or 1))
         root = getattr(w, "root", None)
         P.root = A.dptr(keep(root)) if root is not None else None
+        atmos = getattr(w, "atmos", None)
+        P.atmos = A.dptr(keep(atmos)) if atmos is not None else None
+        atm = getattr(w, "atmos_params", None) or A.default_atmos_params()
+        ctypes.memmove(ctypes.byref(P.atm), ctypes.byref(atm), ctypes.sizeof(A.ClmAtmosParams))
         self.P = P
         self.eh = w.cfg.model == A.CLM_MODEL_ENERGY_HYDROLOGY
 
@@ -185,6 +204,13 @@ class Oracle:
                              A.dptr(fe if self.eh else None), float(t), float(dt), int(nsteps),
                              A.uptr(flags), A.iptr(iters))
         return rc, flags, iters
+
+    def atmos_fluxes(self, state):
+        """CLM_AF_NFIELDS x ncol diagnostics of the atmosphere-driven boundary."""
+        out = np.zeros(A.CLM_AF_NFIELDS * self.w.ncol)
+        rc = lib().clmo_atmos_fluxes(ctypes.byref(self.P), *self._st(state), A.dptr(out))
+        assert rc == 0, rc
+        return out.reshape(A.CLM_AF_NFIELDS, self.w.ncol)
 
     def update_cache(self, state, t):
         nc = self.w.ncells

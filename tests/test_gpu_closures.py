@@ -35,6 +35,8 @@ WORKLOADS = {
     "richards_bc": lambda: WL.brooks_corey(WL.richards_c0(ncol=256)),
     "c4_bc": lambda: WL.brooks_corey(WL.full_scale_c4(ncol=256)),
     "c4_roots": lambda: WL.with_root_extraction(WL.full_scale_c4(ncol=256)),
+    "c4_atmos": lambda: WL.with_atmos(WL.full_scale_c4(ncol=256)),
+    "uneven_atmos_bc": lambda: WL.with_atmos(WL.brooks_corey(WL.uneven_c2(ncol=256))),
 }
 
 

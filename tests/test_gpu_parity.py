@@ -6,6 +6,7 @@ import json
 import numpy as np
 import pytest
 
+import oracle as O
 from climaland_gb300 import _abi as A
 from climaland_gb300 import device as D
 from climaland_gb300 import workloads as WL
@@ -152,6 +153,88 @@ def test_root_extraction_refused_for_richards_and_removable():
         g0.step(w.t0, w.dt, 4)
         for a, b in zip(g.get_state(), g0.get_state()):
             assert np.array_equal(a, b)
+
+
+# Atmosphere-driven top boundary (AtmosDrivenFluxBC + SoilSublimation): the
+# explicit-stage turbulent, radiative and precipitation fluxes at the top.
+ATMOS = {
+    "full_scale": (lambda: WL.with_atmos(WL.full_scale_c4(ncol=1024)), 48, {}),
+    "energy_hydrology": (lambda: WL.with_atmos(WL.energy_hydrology_c1().subset(1024)), 96, {}),
+    "uneven": (lambda: WL.with_atmos(WL.uneven_c2().subset(1024)), 48, {}),
+    "brooks_corey": (lambda: WL.with_atmos(WL.brooks_corey(WL.full_scale_c4(ncol=512))), 48, {}),
+    "full_scale_tol": (lambda: WL.with_atmos(WL.full_scale_c4(ncol=512)), 48,
+                       dict(oracle_cfg=TOL_MODE, **TOL_MODE)),
+    "mixed_full_scale": (lambda: WL.with_atmos(WL.full_scale_c4(ncol=1024)), 48, MIXED),
+    "mixed_brooks_corey": (lambda: WL.with_atmos(WL.brooks_corey(WL.full_scale_c4(ncol=512))), 48, MIXED),
+}
+
+
+@pytest.mark.parametrize("name", list(ATMOS))
+def test_atmos_driven_boundary(name):
+    make, nsteps, kw = ATMOS[name]
+    report(f"atmos_{name}", check_parity(make(), nsteps, **kw))
+
+
+@pytest.mark.parametrize("bc", [False, True])
+def test_atmos_fluxes_match_oracle(bc):
+    """clm_atmos_fluxes (turbulent fluxes, net radiation, surface humidity,
+    top fluxes) against the oracle at the same state: FP64 arithmetic in a
+    different order (table exp/log, reciprocals), 1e-11 of each field's
+    scale."""
+    base = WL.full_scale_c4(ncol=2048)
+    w = WL.with_atmos(WL.brooks_corey(base) if bc else base)
+    st = w.copy_state()
+    fo = O.Oracle(w).atmos_fluxes(st)
+    with D.SoilColumns(w) as g:
+        fg = g.atmos_fluxes()
+        for f in range(A.CLM_AF_NFIELDS):
+            sc = np.max(np.abs(fo[f])) + 1e-300
+            err = np.max(np.abs(fg[f] - fo[f]))
+            assert err <= 1e-11 * sc, (A.ATMOS_FLUXES[f], err, sc)
+        # after a few steps, at a state with sublimating and evaporating columns
+        g.step(w.t0, w.dt, 6)
+        st = g.get_state()
+        fo = O.Oracle(w).atmos_fluxes(st)
+        fg = g.atmos_fluxes()
+        assert (fo[A.CLM_AF_VAPOR_ICE] != 0).any() and (fo[A.CLM_AF_VAPOR_LIQ] != 0).any()
+        for f in range(A.CLM_AF_NFIELDS):
+            sc = np.max(np.abs(fo[f])) + 1e-300
+            assert np.max(np.abs(fg[f] - fo[f])) <= 1e-11 * sc, A.ATMOS_FLUXES[f]
+
+
+def test_atmos_boundary_refusals():
+    """EnergyHydrology only, both top kinds, NoRunoff; drivers required and
+    validated; no root extraction beside it; removing the drivers stops the
+    step until they are set again."""
+    w = WL.with_atmos(WL.full_scale_c4(ncol=64))
+    for mut in (dict(bc_top_heat=A.CLM_BC_FLUX), dict(runoff=A.CLM_RUNOFF_SURFACE)):
+        cfg = A.ClmConfig.from_buffer_copy(w.cfg)
+        for k, v in mut.items():
+            setattr(cfg, k, v)
+        bad = w.columns(0, w.ncol)
+        bad.cfg = cfg
+        with pytest.raises(D.ClmError) as e:
+            D.SoilColumns(bad)
+        assert e.value.code == A.CLM_ERR_ARG
+    r = WL.richards_c0(ncol=32, nlayers=5)
+    r.cfg.bc_top_water = r.cfg.bc_top_heat = A.CLM_BC_ATMOS
+    with pytest.raises(D.ClmError):
+        D.SoilColumns(r)
+    with D.SoilColumns(w) as g:
+        d = w.atmos.copy()
+        d[A.CLM_AT_Z_0M, 3] = 0.0
+        with pytest.raises(D.ClmError) as e:
+            g.set_atmos(d)
+        assert e.value.code == A.CLM_ERR_ARG
+        with pytest.raises(D.ClmError) as e:
+            g.set_root_extraction(np.ones((A.CLM_RX_NFIELDS, w.ncol)))
+        assert e.value.code == A.CLM_ERR_UNSUPPORTED
+        g.set_atmos(None)
+        with pytest.raises(D.ClmError) as e:
+            g.step(w.t0, w.dt, 1)
+        assert e.value.code == A.CLM_ERR_STATE
+        g.set_atmos(w.atmos)
+        g.step(w.t0, w.dt, 1)
 
 
 @pytest.mark.parametrize("kind", [A.CLM_RUNOFF_NONE, A.CLM_RUNOFF_SURFACE, A.CLM_RUNOFF_TOPMODEL])

@@ -694,3 +694,152 @@ def test_topmodel_sink_in_implicit_tendency():
     bound = 1e-14 * np.abs(dv).max(axis=1) * dz * dv.shape[1]
     assert np.all(np.abs(np.sum(dv, axis=1) * dz - d[3]) <= bound)
     assert np.array_equal(r0["R_ss"], np.zeros(w.ncol))
+
+
+# ---- atmosphere-driven top boundary (CLM_BC_ATMOS) ------------------------
+
+def _atm(L):
+    a = A.ClmAtmosParams()
+    L.clmo_atmos_params_default(ctypes.byref(a))
+    return a
+
+
+def test_dry_soil_layer_and_conductance(L):
+    """test/standalone/Soil/climate_drivers.jl:262-290: over surface contents
+    range(theta_r + eps, nu, 5) of the vanGenuchten(alpha = 2.6, n = 2) soil
+    (nu = 0.495, theta_r = 0.1), the dry-layer thickness relative to d_ds
+    runs from ((S_c - S_1) / S_1)^p down to 0 (S_c = hcm.S_c evap_alpha),
+    and the vapour conductance grows with wetness (gsoil[1] < gsoil[2])."""
+    nu, theta_r, n_vg = 0.495, 0.1, 2.0
+    m = 1.0 - 1.0 / n_vg
+    S_c_hcm = (1.0 + ((n_vg - 1.0) / n_vg) ** (1.0 - 2.0 * n_vg)) ** (-m)  # retention_models.jl:42
+    d_ds, p, alpha, D_v = 0.015, 3.0, 1.2, 2.5e-5
+    th = np.linspace(theta_r + EPS, nu, 5)
+    S = np.array([L.clmo_effective_saturation(nu, x, theta_r) for x in th])
+    S_c = S_c_hcm * alpha
+    dsl = np.array([L.clmo_dry_soil_layer_thickness(x, S_c, d_ds, p) for x in S])
+    assert (dsl / d_ds).min() == 0.0
+    assert approx((dsl / d_ds).max(), ((S_c - S[0]) / S[0]) ** p, rtol=1e-14)
+    g = np.array([L.clmo_soil_conductance(x, S_c_hcm, d_ds, p, alpha, D_v) for x in S])
+    assert g[0] < g[1]
+    assert approx(g[-1], D_v / EPS)  # no dry layer: D_vapor / max(0, eps)
+    # alpha S_c is clamped to [0, 1]
+    assert L.clmo_dry_soil_layer_thickness(0.5, 3.0, d_ds, p) == d_ds * ((1.0 - 0.5) / 0.5) ** p
+
+
+def test_saturation_humidity_and_stability_functions(L):
+    """The restated Clausius-Clapeyron saturation (latent heat linear in T):
+    at the triple point p_v,sat = p_tr over both phases; at 373.15 K over
+    liquid within 2 % of one atmosphere (the linear latent heat's error there);
+    q = p_v / (rho R_v T). Businger-Dyer:
+    psi(0) = 0, linear for zeta >= 0, closed form at zeta = -1 (x = 2)."""
+    a = _atm(L)
+    e = O.earth()
+    R_v = a.gas_constant / a.molmass_water
+    for ice in (0, 1):
+        q = L.clmo_q_vap_saturation(a.T_triple, 1.0, ice, ctypes.byref(a), ctypes.byref(e))
+        assert approx(q, a.press_triple / (R_v * a.T_triple), rtol=1e-14)
+    q100 = L.clmo_q_vap_saturation(373.15, 1.0, 0, ctypes.byref(a), ctypes.byref(e))
+    assert abs(q100 * R_v * 373.15 / 101325.0 - 1.0) < 0.02
+    # ice saturation below liquid saturation under the triple point
+    ql = L.clmo_q_vap_saturation(263.15, 1.3, 0, ctypes.byref(a), ctypes.byref(e))
+    qi = L.clmo_q_vap_saturation(263.15, 1.3, 1, ctypes.byref(a), ctypes.byref(e))
+    assert qi < ql
+    assert L.clmo_businger_psi_m(0.0, ctypes.byref(a)) == 0.0
+    assert L.clmo_businger_psi_h(0.0, ctypes.byref(a)) == 0.0
+    assert approx(L.clmo_businger_psi_m(0.5, ctypes.byref(a)), -a.a_m * 0.5, rtol=1e-15)
+    assert approx(L.clmo_businger_psi_h(0.5, ctypes.byref(a)), -a.a_h * 0.5 / a.Pr_0, rtol=1e-15)
+    x = 2.0  # (1 + 15)^(1/4)
+    ref = 2 * math.log(1.5) + math.log(2.5) - 2 * math.atan(x) + math.pi / 2
+    assert approx(L.clmo_businger_psi_m(-1.0, ctypes.byref(a)), ref, rtol=1e-14)
+    assert approx(L.clmo_businger_psi_h(-(3.0 ** 2 - 1) / 9.0, ctypes.byref(a)), 2 * math.log(2.0), rtol=1e-14)
+
+
+def test_atmos_boundary_fluxes(L):
+    """test/standalone/Soil/climate_drivers.jl:220-260: the top water flux is
+    the liquid influx plus the liquid vapour flux, the top energy flux
+    R_n + LHF + SHF + P_liq rho e_liq(T_air) (NoRunoff); net radiation
+    -(1 - alpha) SW_d - eps (LW_d - sigma T_sfc^4) with the two-band albedo
+    of the surface effective saturation (drivers.jl:699-716, soil_albedo.jl);
+    the vapour flux is liquid where T_sfc > Tf_depressed, ice elsewhere."""
+    w = WL.with_atmos(WL.energy_hydrology_c1(ncol=64, nlayers=6))
+    o = O.Oracle(w)
+    st = w.copy_state()
+    f = o.atmos_fluxes(st)
+    aux = o.update_cache(st, 0.0)
+    d = w.atmos
+    E_ = A.DEFAULT_EARTH
+    rho_e_air = E_["cp_l"] * E_["rho_l"] * (d[A.CLM_AT_T_AIR] - E_["T_0"])
+    assert np.array_equal(f[A.CLM_AF_TOP_WATER], d[A.CLM_AT_P_LIQ] + f[A.CLM_AF_VAPOR_LIQ])
+    assert np.array_equal(f[A.CLM_AF_TOP_HEAT],
+                          f[A.CLM_AF_R_N] + f[A.CLM_AF_LHF] + f[A.CLM_AF_SHF] + d[A.CLM_AT_P_LIQ] * rho_e_air)
+    # the cache's top boundary fluxes are the same numbers
+    assert np.array_equal(aux["bc"][0], f[A.CLM_AF_TOP_WATER])
+    assert np.array_equal(aux["bc"][1], f[A.CLM_AF_TOP_HEAT])
+    n = 6
+    top = np.arange(w.ncol) * n + n - 1
+    T_sfc, Tf = aux["T"][top], aux["Tf"][top]
+    liq = T_sfc - Tf > EPS
+    assert np.all(f[A.CLM_AF_VAPOR_ICE][liq] == 0.0) and np.all(f[A.CLM_AF_VAPOR_LIQ][~liq] == 0.0)
+    assert liq.any() and (~liq).any()
+    # LHF = LH_v0 E, vapour flux = E / rho_l
+    E_evap = f[A.CLM_AF_VAPOR_LIQ] + f[A.CLM_AF_VAPOR_ICE]
+    assert approx(f[A.CLM_AF_LHF], 2500800.0 * E_evap * E_["rho_l"], rtol=1e-13, atol=1e-12)
+    # net radiation on the columns whose albedo uses the top layer alone
+    nu, tr = w.params[A.CLM_P_NU], w.params[A.CLM_P_THETA_R]
+    dz = (w.z_hi - w.z_lo) / n
+    one = dz >= d[A.CLM_AT_ALBEDO_TOP_THICKNESS]
+    S = (np.maximum(aux["theta_l"][top], tr + 1.4901161193847656e-08) - tr) / (nu - tr)
+    alb = 0.5 * ((1 - S) * d[A.CLM_AT_PAR_ALBEDO_DRY] + S * d[A.CLM_AT_PAR_ALBEDO_WET]) + \
+        0.5 * ((1 - S) * d[A.CLM_AT_NIR_ALBEDO_DRY] + S * d[A.CLM_AT_NIR_ALBEDO_WET])
+    Rn = -(1 - alb) * d[A.CLM_AT_SW_D] - d[A.CLM_AT_EMISSIVITY] * (d[A.CLM_AT_LW_D] - 5.670374419e-8 * T_sfc ** 4)
+    assert one.any()
+    assert approx(f[A.CLM_AF_R_N][one], Rn[one], rtol=1e-12, atol=1e-9)
+
+
+def test_sublimation_source(L):
+    """SoilSublimation (energy_hydrology.jl:931-947): the explicit tendency
+    of theta_i gains -vapor_flux_ice rho_l / rho_i / (2 dz_top) in the top
+    layer only (surface at z = 0) and intF_w gains -vapor_flux_ice; the step
+    then keeps the water budget closed (the source is in both)."""
+    w = WL.with_atmos(WL.energy_hydrology_c1(ncol=64, nlayers=6))
+    o = O.Oracle(w)
+    st = w.copy_state()
+    f = o.atmos_fluxes(st)
+    d = o.exp_tendency(st, 0.0)
+    w0 = WL.energy_hydrology_c1(ncol=64, nlayers=6)
+    d0 = O.Oracle(w0).exp_tendency(w0.copy_state(), 0.0)
+    n = 6
+    E_ = A.DEFAULT_EARTH
+    vice = f[A.CLM_AF_VAPOR_ICE]
+    assert (vice != 0).any()
+    dz_top = 0.5 * (w.z_hi - w.z_lo) / n
+    for c in range(w.ncol):
+        sl = slice(c * n, (c + 1) * n)
+        want = np.zeros(n)
+        want[-1] = -vice[c] * E_["rho_l"] / E_["rho_i"] / (2 * dz_top[c])
+        assert approx(d[1][sl] - d0[1][sl], want, rtol=1e-12, atol=1e-25)
+    assert np.array_equal(d[3], -vice)
+    # budgets over a few steps: water (incl. the sublimated ice) and energy close
+    W0, E0 = o.budgets(st)
+    Fw0, Fe0 = st[3].copy(), st[4].copy()
+    rc, flags, _ = o.step(st, 0.0, w.dt, 4)
+    assert rc == 0
+    W1, E1 = o.budgets(st)
+    assert np.allclose(W1 - W0, st[3] - Fw0, rtol=0, atol=1e-12 * np.abs(W0).max())
+    assert np.allclose(E1 - E0, st[4] - Fe0, rtol=0, atol=1e-12 * np.abs(E0).max())
+
+
+def test_atmos_boundary_refusals(L):
+    """The boundary is EnergyHydrology-only, sets both top fluxes, needs its
+    drivers, and runs without a runoff model or root extraction."""
+    w = WL.with_atmos(WL.energy_hydrology_c1(ncol=8, nlayers=6))
+    st = w.copy_state()
+    for mut in (dict(bc_top_heat=A.CLM_BC_FLUX), dict(runoff=A.CLM_RUNOFF_SURFACE),
+                dict(model=A.CLM_MODEL_RICHARDS)):
+        o = O.Oracle(w)
+        o.set_cfg(**mut)
+        assert o.step(w.copy_state(), 0.0, 1.0, 1)[0] == A.CLM_ERR_ARG
+    o = O.Oracle(w)
+    o.P.atmos = None
+    assert o.step(st, 0.0, 1.0, 1)[0] == A.CLM_ERR_ARG
