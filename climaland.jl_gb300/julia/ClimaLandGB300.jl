@@ -27,10 +27,13 @@ const CLM_BC_FREE_DRAINAGE = Int32(1)
 const CLM_BC_STATE = Int32(2)
 const CLM_BC_FLUX_ADVECTIVE = Int32(3)
 const CLM_BC_PRECIP_RUNOFF = Int32(4)
+const CLM_BC_ATMOS = Int32(5)
 const CLM_CM_VAN_GENUCHTEN = Int32(0)
 const CLM_CM_BROOKS_COREY = Int32(1)
 const CLM_F_NFIELDS = 8
 const CLM_RX_NFIELDS = 8
+const CLM_AT_NFIELDS = 20
+const CLM_AF_NFIELDS = 8
 
 struct ClmEarthParams
     rho_l::Float64
@@ -156,6 +159,62 @@ canopy ψ, LAI, RAI, height, rooting depth, Weibull K_sat, ψ63, c), or
 set_root_extraction!(h::Handle, r::Union{Nothing, Matrix{Float64}}) =
     check(h, ccall((:clm_set_root_extraction, libclm), Cint, (Ptr{Cvoid}, Ptr{Float64}, Int32),
         h.ptr, r === nothing ? C_NULL : permutedims(r), r === nothing ? 0 : size(r, 1)))
+
+"Constants of the atmosphere-driven top boundary (`clm_atmos_params`)."
+mutable struct ClmAtmosParams
+    stefan::Float64
+    gas_constant::Float64
+    molmass_dryair::Float64
+    molmass_water::Float64
+    D_vapor::Float64
+    LH_v0::Float64
+    LH_s0::Float64
+    cp_d::Float64
+    cp_v::Float64
+    T_triple::Float64
+    press_triple::Float64
+    von_karman::Float64
+    Pr_0::Float64
+    a_m::Float64
+    a_h::Float64
+    b_m::Float64
+    b_h::Float64
+    zeta_max::Float64
+    iterations::Int32
+    pad::Int32
+end
+
+function atmos_params_default()
+    a = ClmAtmosParams(zeros(18)..., Int32(0), Int32(0))
+    ccall((:clm_atmos_params_default, libclm), Cvoid, (Ref{ClmAtmosParams},), a)
+    return a
+end
+
+"""
+    set_atmos!(h, drivers; params = atmos_params_default())
+
+Drivers of the atmosphere-driven top boundary (`cfg.bc_top_water =
+cfg.bc_top_heat = CLM_BC_ATMOS`) as a (CLM_AT_NFIELDS × ncol) matrix, rows in
+`enum clm_atmos_field` order: from a `PrescribedAtmosphere` /
+`PrescribedRadiativeFluxes`, `p.drivers.P_liq, T, u, q, P, SW_d, LW_d`,
+`atmos.h`, `atmos.gustiness`, then the soil's albedo parameters,
+emissivity, z_0m, z_0b, d_ds, evap_p, evap_α. Call after each
+`update_drivers!`; `nothing` removes them.
+"""
+function set_atmos!(h::Handle, d::Union{Nothing, Matrix{Float64}}; params = atmos_params_default())
+    d === nothing && return check(h, ccall((:clm_set_atmos, libclm), Cint,
+        (Ptr{Cvoid}, Ptr{ClmAtmosParams}, Ptr{Float64}, Int32), h.ptr, C_NULL, C_NULL, 0))
+    check(h, ccall((:clm_set_atmos, libclm), Cint,
+        (Ptr{Cvoid}, Ref{ClmAtmosParams}, Ptr{Float64}, Int32), h.ptr, params, permutedims(d), size(d, 1)))
+end
+
+"The boundary's diagnostics (lhf, shf, vapor_flux_liq, vapor_flux_ice, R_n, q_sfc, top water, top heat) as a (CLM_AF_NFIELDS × ncol) matrix."
+function atmos_fluxes(h::Handle, ncol::Integer)
+    out = Matrix{Float64}(undef, ncol, CLM_AF_NFIELDS)
+    check(h, ccall((:clm_atmos_fluxes, libclm), Cint, (Ptr{Cvoid}, Ptr{Float64}, Int32),
+        h.ptr, out, CLM_AF_NFIELDS))
+    return permutedims(out)
+end
 
 "Forcing descriptor for one boundary slot as a (CLM_F_NFIELDS × ncol) matrix."
 set_bc!(h::Handle, slot::Integer, f::Matrix{Float64}) =

@@ -78,9 +78,9 @@ def test_create_rejects_bad_config_before_touching_the_device(lib):
 
 def test_create_rejects_runoff_outside_richards(lib):
     # the precipitation/runoff top boundary is RichardsAtmosDrivenFluxBC: an
-    # EnergyHydrology handle (whose atmosphere-driven BC is not built), the
-    # heat or bottom slots and unknown runoff kinds are refused before any
-    # device work
+    # EnergyHydrology handle (whose atmosphere-driven boundary is
+    # CLM_BC_ATMOS), the heat or bottom slots and unknown runoff kinds are
+    # refused before any device work
     h = ctypes.c_void_p()
     cfg = A.default_config()
     cfg.ncol = 10
@@ -118,3 +118,33 @@ def test_julia_binding_config_matches_the_header_layout():
     assert [n for n, _ in fields] == [n for n, _ in A.ClmConfig._fields_]
     for (n, t), (_, ct) in zip(fields, A.ClmConfig._fields_):
         assert ctypes.sizeof(jl[t]) == ctypes.sizeof(ct), n
+
+
+def test_atmos_params_default_matches_the_mirror(lib):
+    # clm_atmos_params_default writes exactly sizeof(ClmAtmosParams) bytes
+    # and the Python twin holds the same values
+    buf = (ctypes.c_ubyte * (ctypes.sizeof(A.ClmAtmosParams) + 64))()
+    for i in range(len(buf)):
+        buf[i] = 0xAB
+    lib.clm_atmos_params_default(ctypes.cast(buf, ctypes.POINTER(A.ClmAtmosParams)))
+    assert all(b == 0xAB for b in bytes(buf[ctypes.sizeof(A.ClmAtmosParams):]))
+    a = A.ClmAtmosParams.from_buffer_copy(bytes(buf[: ctypes.sizeof(A.ClmAtmosParams)]))
+    for k, v in A.DEFAULT_ATMOS.items():
+        assert getattr(a, k) == v, k
+
+
+def test_create_rejects_misplaced_atmos_boundary(lib):
+    h = ctypes.c_void_p()
+    for model, tw, th, runoff in ((A.CLM_MODEL_RICHARDS, A.CLM_BC_ATMOS, A.CLM_BC_ATMOS, 0),
+                                  (A.CLM_MODEL_ENERGY_HYDROLOGY, A.CLM_BC_ATMOS, A.CLM_BC_FLUX, 0),
+                                  (A.CLM_MODEL_ENERGY_HYDROLOGY, A.CLM_BC_FLUX, A.CLM_BC_ATMOS, 0),
+                                  (A.CLM_MODEL_ENERGY_HYDROLOGY, A.CLM_BC_ATMOS, A.CLM_BC_ATMOS,
+                                   A.CLM_RUNOFF_SURFACE)):
+        cfg = A.default_config()
+        cfg.model, cfg.ncol, cfg.nlayers = model, 4, 5
+        cfg.bc_top_water, cfg.bc_top_heat, cfg.runoff = tw, th, runoff
+        assert lib.clm_create(ctypes.byref(cfg), ctypes.byref(h)) == A.CLM_ERR_ARG
+    cfg = A.default_config()
+    cfg.ncol, cfg.nlayers = 4, 5
+    cfg.bc_bottom_water = A.CLM_BC_ATMOS  # a top-only kind
+    assert lib.clm_create(ctypes.byref(cfg), ctypes.byref(h)) == A.CLM_ERR_ARG
