@@ -125,7 +125,7 @@ def profile_traffic(kernel_key: str) -> dict | None:
     return None
 
 
-def make_workload(name: str, ncol: int | None, rank: int):
+def make_workload(name: str, ncol: int | None, rank: int, top: str = "flux"):
     from climaland_gb300 import workloads as WL
 
     gen = WL.CONFIGS[name]
@@ -133,6 +133,8 @@ def make_workload(name: str, ncol: int | None, rank: int):
     if ncol:
         kw["ncol"] = ncol
     w = gen(**kw)
+    if top == "atmos":  # the atmosphere-driven top boundary on the same columns
+        w = WL.with_atmos(w, seed=rank)
     # rank r holds columns [r ncol, (r + 1) ncol) of one domain: the
     # rain-pulse hash sees global column indices
     w.cfg.column_offset = rank * w.ncol
@@ -165,7 +167,7 @@ def run_reference(args, rank, world):
     absent) on the host cores, same config and metric."""
     if rank != 0:
         return
-    w = make_workload(args.config, args.ncol, 0)
+    w = make_workload(args.config, args.ncol, 0, args.top)
     sys.path.insert(0, str(REPO / "oracle"))
     import oracle as O
 
@@ -212,7 +214,8 @@ def _error_stats(a, b, ncol_cells):
 def forms_block(args, torch, stream):
     """The three forms beside the plain path, on subsets that finish in
     seconds: mixed precision (EnergyHydrology and RichardsModel), uneven columns (autotuned, graph-replayed) and
-    learned guess + mixed precision in tolerance mode. Errors are per-column
+    learned guess + mixed precision in tolerance mode; and the atmosphere-driven
+    top boundary's cost on the full-scale columns. Errors are per-column
     max |vartheta_l| differences from the plain FP64 path on the same
     columns and steps (the plain path itself is held to the FP64 oracle by
     the parity tests)."""
@@ -299,6 +302,15 @@ def forms_block(args, torch, stream):
     rmx = run(w0, precision=A.CLM_PREC_MIXED)
     out["richards_subset"] = {"workload": w0.name, "plain_fp64": pub(r64, None, w0),
                               "mixed": pub(rmx, r64, w0)}
+    # the atmosphere-driven top boundary (turbulent fluxes, radiation,
+    # sublimation) on the full-scale columns: its cost over the flux boundary
+    wa = WL.with_atmos(w4)
+    a64 = run(wa)
+    amx = run(wa, precision=A.CLM_PREC_MIXED)
+    out["atmos_boundary"] = {"workload": wa.name, "plain_fp64": pub(a64, None, wa),
+                             "mixed": pub(amx, a64, wa),
+                             "cost_vs_flux_boundary_fp64": a64["ms_per_step"] / plain["ms_per_step"],
+                             "cost_vs_flux_boundary_mixed": amx["ms_per_step"] / mixed["ms_per_step"]}
     return out
 
 
@@ -311,6 +323,9 @@ def main():
     ap.add_argument("--config", default="c4")
     ap.add_argument("--ncol", type=int, default=None)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--top", default="flux", choices=["flux", "atmos"],
+                    help="top boundary: the workload's flux forcing, or the atmosphere-driven "
+                         "boundary (EnergyHydrology)")
     ap.add_argument("--cpu-sample-cols", type=int, default=65536)
     ap.add_argument("--cpu-sample-steps", type=int, default=128)
     ap.add_argument("--ref-sample-cols", type=int, default=32768)
@@ -345,7 +360,7 @@ def main():
     from climaland_gb300 import _abi as A
     from climaland_gb300 import device as D
 
-    w = make_workload(args.config, args.ncol, rank)
+    w = make_workload(args.config, args.ncol, rank, args.top)
     prec = A.CLM_PREC_MIXED if args.precision == "mixed" else A.CLM_PREC_FP64
     nl = float(w.nlayers.mean())
     g = D.SoilColumns(w, precision=prec)
@@ -431,9 +446,13 @@ def main():
 
     peaks = measured_peaks()
     bytes_per_launch = algorithmic_bytes_per_column_step(w.cfg.model, nl) * w.ncol
+    if args.top == "atmos":  # the per-column drivers, read once per step
+        bytes_per_launch += 8 * A.CLM_AT_NFIELDS * w.ncol
     avg_launch_s = statistics.mean(per_launch_ms) / 1e3
     achieved = bytes_per_launch / avg_launch_s / 1e9
     key = f"{'eh' if w.cfg.model == 1 else 'richards'}_step_{args.precision}"
+    if args.top == "atmos":
+        key += "_atmos"
     prof = profile_traffic(key)
     traffic = None
     if prof and prof.get("dram_bytes_per_column_step"):

@@ -142,7 +142,7 @@ DEFAULT_ATMOS = dict(
     stefan=5.670374419e-8, gas_constant=8.3144598, molmass_dryair=0.02897,
     molmass_water=0.01801528, D_vapor=2.5e-5, LH_v0=2500800.0, LH_s0=2834400.0, cp_d=1004.5,
     cp_v=1859.0, T_triple=273.16, press_triple=611.657, von_karman=0.4, Pr_0=0.74, a_m=4.7,
-    a_h=4.7, b_m=15.0, b_h=9.0, zeta_max=100.0, iterations=10,
+    a_h=4.7, b_m=15.0, b_h=9.0, zeta_max=100.0, iterations=8,
 )
 
 

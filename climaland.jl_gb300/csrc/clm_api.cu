@@ -794,7 +794,7 @@ void clm_atmos_params_default(clm_atmos_params* a) {
   a->b_m = 15.0;
   a->b_h = 9.0;
   a->zeta_max = 100.0;
-  a->iterations = 10;
+  a->iterations = 8;
 }
 
 int clm_set_atmos(clm_handle* h, const clm_atmos_params* prm, const double* d, int32_t nfields) {

@@ -16,10 +16,11 @@
 //   soil conductance   D_vapor / max(dsl, eps), dsl the dry-layer thickness
 //                      of Swenson et al. 2012 (:1338-1368);
 //   turbulent fluxes   Monin-Obukhov similarity at point values with the
-//                      Businger-Dyer functions, a fixed number of
-//                      fixed-point steps on zeta = dz / L_MO with the
-//                      surface humidity re-evaluated from the heat
-//                      conductance in each (update_q_vap_sfc_at_a_point,
+//                      Businger-Dyer functions: zeta = dz / L_MO from
+//                      zeta F_h = Ri_b F_m^2 (stable: the quadratic's root;
+//                      unstable: Newton steps), a fixed number of
+//                      iterations, the surface humidity re-evaluated from the
+//                      heat conductance in each (update_q_vap_sfc_at_a_point,
 //                      :1066-1099);
 //   radiation          R_n = -(1 - alpha) SW_d - eps (LW_d - sigma T^4), the
 //                      CLM two-band albedo over the top layers
@@ -45,7 +46,7 @@ struct AtmosK {
   double stefan, D_vapor, LH_v0, cp_d, cp_v, von_karman;
   double R_d, R_v, delta;    // delta = R_v / R_d - 1
   double Mw_over_R;          // M_w / R (Kelvin factor)
-  double Pr_0, a_m, a_h_over_Pr, b_m, b_h, zeta_max;
+  double Pr_0, a_m, a_h, a_h_over_Pr, b_m, b_h, zeta_max;
   int iterations;
   // saturation vapour pressure, liquid [0] / ice [1]:
   // p_v = p_tr exp(ex ln(T / T_tr) + cc (1 / T_tr - 1 / T))
@@ -67,6 +68,7 @@ inline AtmosK make_atmos_k(const clm_atmos_params& a, const clm_earth_params& e)
   K.Mw_over_R = a.molmass_water / a.gas_constant;
   K.Pr_0 = a.Pr_0;
   K.a_m = a.a_m;
+  K.a_h = a.a_h;
   K.a_h_over_Pr = a.a_h / a.Pr_0;
   K.b_m = a.b_m;
   K.b_h = a.b_h;
@@ -104,6 +106,25 @@ CLM_HD double psi_m(const Tables& Tb, const AtmosK& K, double zeta) {
 CLM_HD double psi_h(const Tables& Tb, const AtmosK& K, double zeta) {
   if (zeta >= 0.0) return -K.a_h_over_Pr * zeta;
   return 2.0 * fm::log(Tb, (1.0 + sqrt(1.0 - K.b_h * zeta)) * 0.5);
+}
+
+// The stable root of zeta F_h(zeta) = Ri F_m(zeta)^2 (Ri >= 0): with the linear
+// Businger-Dyer functions a quadratic A zeta^2 + B zeta + C = 0,
+// A = a_h (1 - r_b) - Ri a_m^2 (1 - r_m)^2, B = Pr_0 lh - 2 Ri a_m (1 - r_m) lm,
+// C = -Ri lm^2; the root continuous from zeta(0) = 0, or zeta_max above the
+// critical Richardson number (no root).
+CLM_HD double stable_zeta(const AtmosK& K, double Ri, double lm, double lh, double rm, double rb) {
+  const double am = K.a_m * (1.0 - rm), ah = K.a_h * (1.0 - rb);
+  const double A = ah - Ri * am * am, B = K.Pr_0 * lh - 2.0 * Ri * am * lm, C = -Ri * lm * lm;
+  const double D = B * B - 4.0 * A * C;
+  double z;
+  if (B > 0.0 && D >= 0.0)
+    z = -2.0 * C / (B + sqrt(D));
+  else if (A > 0.0)
+    z = (-B + sqrt(fmax(D, 0.0))) / (2.0 * A);
+  else
+    z = K.zeta_max;
+  return fmin(fmax(z, 0.0), K.zeta_max);
 }
 
 // S_c of the closure (retention_models.jl:42, :64)
@@ -172,20 +193,52 @@ CLM_HD AtmosOut atmos_bc(const Tables& Tb, const AtmosK& K, const Earth& E, cons
   const double lm = fm::log(Tb, dz / z0m), lh = fm::log(Tb, dz / z0b);
   const double thv_air = (T_air + grav * dz / K.cp_d) * (1.0 + K.delta * q_air);
   const double gU = grav * dz / (U * U);
+  const double rm = z0m / dz, rb = z0b / dz;
+  const double kk_U = K.von_karman * K.von_karman * U;
   double zeta = 0.0, g_h = 0.0, q_sfc = qsat;
   for (int it = 0;; ++it) {
-    const double F_m = lm - psi_m(Tb, K, zeta) + psi_m(Tb, K, zeta * z0m / dz);
-    const double F_h = K.Pr_0 * (lh - psi_h(Tb, K, zeta) + psi_h(Tb, K, zeta * z0b / dz));
-    const double ustar = K.von_karman * U / F_m;
-    g_h = K.von_karman * ustar / F_h;
+    // F_m = lm - psi_m(zeta) + psi_m(zeta z0m/dz), F_h = Pr_0 (lh - psi_h(zeta) +
+    // psi_h(zeta z0b/dz)) and, on the unstable side, their zeta-derivatives
+    // (psi'(zeta) = (1 - phi(zeta)) / zeta, phi_m = 1/x, phi_h = Pr_0 / y); the
+    // two logarithms and arctangents of each pair combine into one
+    // (atan x' - atan x = atan((x' - x) / (1 + x x')) for x, x' >= 1)
+    double F_m, F_h, dF_m = 0.0, dF_h = 0.0;
+    if (zeta >= 0.0) {
+      F_m = lm - psi_m(Tb, K, zeta) + psi_m(Tb, K, zeta * rm);
+      F_h = K.Pr_0 * (lh - psi_h(Tb, K, zeta) + psi_h(Tb, K, zeta * rb));
+    } else {
+      // x = v^(1/4) and 1/x from s = sqrt(v) = x^2 and rsqrt(s); y and 1/y alike
+      const double s = sqrt(1.0 - K.b_m * zeta), sp = sqrt(1.0 - K.b_m * (zeta * rm));
+      const double ix = rsqrt(s), ixp = rsqrt(sp);
+      const double x = s * ix, xp = sp * ixp;
+      const double num = (1.0 + xp) * (1.0 + xp) * (1.0 + sp), den = (1.0 + x) * (1.0 + x) * (1.0 + s);
+      F_m = lm + fm::log(Tb, num * fm::rcp(den)) - 2.0 * atan((xp - x) * fm::rcp(1.0 + x * xp));
+      const double w = 1.0 - K.b_h * zeta, wp = 1.0 - K.b_h * (zeta * rb);
+      const double iy = rsqrt(w), iyp = rsqrt(wp);
+      const double y = w * iy, yp = wp * iyp;
+      F_h = K.Pr_0 * (lh + 2.0 * fm::log(Tb, (1.0 + yp) * fm::rcp(1.0 + y)));
+      const double iz = fm::rcp(zeta);
+      dF_m = (ix - ixp) * iz;
+      dF_h = K.Pr_0 * (iy - iyp) * iz;
+    }
+    g_h = kk_U * fm::rcp(F_m * F_h);
     if (subl)
       q_sfc = q_air < qsat ? beta_ice * qsat + (1.0 - beta_ice) * q_air : qsat;
-    else
-      q_sfc = (g_soil / g_h * qsat + q_air) / (1.0 + g_soil / g_h);
+    else  // (g_soil / g_h qsat + q_air) / (1 + g_soil / g_h)
+      q_sfc = (g_soil * qsat + g_h * q_air) * fm::rcp(g_h + g_soil);
     if (it >= K.iterations) break;
     const double thv_sfc = sf.T * (1.0 + K.delta * q_sfc);
-    const double Ri = gU * (thv_air - thv_sfc) / thv_sfc;
-    zeta = fmin(fmax(Ri * F_m * F_m / F_h, -K.zeta_max), K.zeta_max);
+    const double Ri = gU * (thv_air - thv_sfc) * fm::rcp(thv_sfc);
+    if (Ri >= 0.0) {
+      zeta = stable_zeta(K, Ri, lm, lh, rm, rb);
+    } else if (zeta >= 0.0) {
+      zeta = Ri * lm * lm * fm::rcp(K.Pr_0 * lh);  // one fixed-point step from 0
+    } else {
+      // Newton on r = zeta F_h - Ri F_m^2 at fixed Ri
+      const double r = zeta * F_h - Ri * F_m * F_m;
+      const double dr = F_h + zeta * dF_h - 2.0 * Ri * F_m * dF_m;
+      zeta = fmin(fmax(zeta - r * fm::rcp(dr), -K.zeta_max), 0.0);
+    }
   }
   AtmosOut o;
   const double Ev = -rho_sfc * g_h * (q_air - q_sfc);

@@ -282,6 +282,8 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
     // layers), frozen through the Newton solve
     AtmosOut ab{};
     double dz_top = 0.0;
+    double sub_top = 0.0;  // SoilSublimation's theta_i tendency in the layers k >= k_sub
+    int k_sub = n;
     if constexpr (kAtmos) {
       auto theta_l_of = [&](int k) {
         const double Yv = B.gv[k], nu_eff = c.nu - B.gti[k];
@@ -306,6 +308,10 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       const AtmosRow D{A.atm, st, s};
       sf.th_alb = albedo_theta(G, D(CLM_AT_ALBEDO_TOP_THICKNESS), theta_l_of);
       ab = atmos_bc(Tb, A.ak, E, D, c.g, c.nu, c.theta_r, sf);
+      // H(z_k + 2 dz_top) rises with k: the source reaches the layers from
+      // k_sub up (the top layer alone for a surface at z = 0)
+      while (k_sub > 0 && sublimation_weight(G, k_sub - 1, dz_top) != 0.0) --k_sub;
+      sub_top = -ab.vice * E.rho_l / E.rho_i / (2.0 * dz_top);
     }
     for (int k = 0; k < n; ++k) {
       const double Yv = B.gv[k], Yti = B.gti[k], Ye = B.ge[k];
@@ -353,7 +359,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       }
       if constexpr (kAtmos) {
         // SoilSublimation after PhaseChange in the sources tuple
-        const double sub = -ab.vice * E.rho_l / E.rho_i * sublimation_weight(G, k, dz_top);
+        const double sub = k >= k_sub ? sub_top : 0.0;
         Uti = Yti + dt * ((A.phase_change ? E.rho_l_over_rho_i * pc : 0.0) + sub);
       }
       if constexpr (kRoots) {

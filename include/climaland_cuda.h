@@ -261,12 +261,16 @@ enum clm_atmos_field {
  *   psi_m = -a_m zeta, psi_h = -a_h zeta / Pr_0 (zeta >= 0);
  *   psi_m = 2 ln((1+x)/2) + ln((1+x^2)/2) - 2 atan x + pi/2, x = (1 - b_m zeta)^(1/4),
  *   psi_h = 2 ln((1+y)/2), y = (1 - b_h zeta)^(1/2) (zeta < 0);
- *   u* = kappa U / F_m, g_h = kappa u* / F_h, and zeta <- Ri_b F_m^2 / F_h
- *   (clamped to +-zeta_max) for `iterations` fixed-point steps from 0, with
- *   Ri_b = g dz (theta_v,air - theta_v,sfc) / (theta_v,sfc U^2),
+ *   u* = kappa U / F_m, g_h = kappa u* / F_h; `iterations` steps from zeta = 0,
+ *   each re-evaluating F_m, F_h, g_h, q_sfc and
+ *   Ri_b = g dz (theta_v,air - theta_v,sfc) / (theta_v,sfc U^2), then solving
+ *   zeta F_h(zeta) = Ri_b F_m(zeta)^2 for the next zeta: for Ri_b >= 0 exactly
+ *   (a quadratic with the linear stable functions; zeta_max above the
+ *   critical Richardson number), for Ri_b < 0 by a Newton step (the first
+ *   from Ri_b ln(dz/z_0m)^2 / (Pr_0 ln(dz/z_0b))), clamped to [-zeta_max, 0];
  *   theta_v,air = (T_air + g dz / cp_d)(1 + (R_v/R_d - 1) q_air),
- *   theta_v,sfc = T_sfc (1 + (R_v/R_d - 1) q_sfc), and q_sfc updated from g_h
- *   in every step by the reference's update_q_vap_sfc_at_a_point
+ *   theta_v,sfc = T_sfc (1 + (R_v/R_d - 1) q_sfc), and q_sfc from g_h by the
+ *   reference's update_q_vap_sfc_at_a_point
  *   (energy_hydrology.jl:1066-1099). Then
  *   E = -rho_sfc g_h (q_air - q_sfc), LHF = LH_v0 E,
  *   SHF = -rho_sfc cp_m g_h (T_air + g dz / cp_m - T_sfc),
@@ -284,7 +288,7 @@ typedef struct clm_atmos_params {
   double von_karman;
   double Pr_0, a_m, a_h, b_m, b_h; /* Businger-Dyer                        */
   double zeta_max;        /* |zeta| bound of the iteration                 */
-  int32_t iterations;     /* fixed-point steps (>= 1)                      */
+  int32_t iterations;     /* similarity iterations (>= 1; default 8)       */
   int32_t pad;
 } clm_atmos_params;
 

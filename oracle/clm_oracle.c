@@ -679,7 +679,7 @@ void clmo_atmos_params_default(clm_atmos_params* a) {
   a->b_m = 15.0;
   a->b_h = 9.0;
   a->zeta_max = 100.0;
-  a->iterations = 10;
+  a->iterations = 8;
 }
 
 /* q_vap_saturation(T, rho, Liquid() / Ice()): p_v,sat / (rho R_v T) with
@@ -722,6 +722,34 @@ double clmo_businger_psi_h(double zeta, const clm_atmos_params* a) {
   if (zeta >= 0.0) return -a->a_h * zeta / a->Pr_0;
   double y = sqrt(1.0 - a->b_h * zeta);
   return 2.0 * log((1.0 + y) / 2.0);
+}
+
+/* d psi / d zeta = (1 - phi(zeta)) / zeta on the unstable side:
+ * phi_m = (1 - b_m zeta)^(-1/4), phi_h / Pr_0 = (1 - b_h zeta)^(-1/2) */
+static double dpsi_m(double zeta, const clm_atmos_params* a) {
+  return (1.0 - pow(1.0 - a->b_m * zeta, -0.25)) / zeta;
+}
+static double dpsi_h(double zeta, const clm_atmos_params* a) {
+  return (1.0 - 1.0 / sqrt(1.0 - a->b_h * zeta)) / zeta;
+}
+
+/* The stable root of zeta F_h = Ri F_m^2 (Ri >= 0): with the linear
+ * Businger-Dyer functions the quadratic A zeta^2 + B zeta + C = 0,
+ * A = a_h (1 - r_b) - Ri a_m^2 (1 - r_m)^2, B = Pr_0 lh - 2 Ri a_m (1 - r_m) lm,
+ * C = -Ri lm^2; its root continuous from zeta(0) = 0, or zeta_max above the
+ * critical Richardson number. */
+static double stable_zeta(const clm_atmos_params* a, double Ri, double lm,
+                          double lh, double rm, double rb) {
+  double am = a->a_m * (1.0 - rm), ah = a->a_h * (1.0 - rb);
+  double A = ah - Ri * am * am, B = a->Pr_0 * lh - 2.0 * Ri * am * lm;
+  double C = -Ri * lm * lm, D = B * B - 4.0 * A * C, z;
+  if (B > 0.0 && D >= 0.0)
+    z = -2.0 * C / (B + sqrt(D));
+  else if (A > 0.0)
+    z = (-B + sqrt(fmax(D, 0.0))) / (2.0 * A);
+  else
+    z = a->zeta_max;
+  return fmin(fmax(z, 0.0), a->zeta_max);
 }
 
 /* S_c of the closure (retention_models.jl:42, :64) */
@@ -790,17 +818,28 @@ static void atmos_top_bc(const col_t* C, const state_t* Y, cache_t* p) {
   const double lm = log(dz / z0m), lh = log(dz / z0b);
   const double delta = R_v / R_d - 1.0;
   const double thv_air = (T_air + grav * dz / a->cp_d) * (1.0 + delta * q_air);
+  const double rm = z0m / dz, rb = z0b / dz;
   double zeta = 0.0, F_m = 0.0, F_h = 0.0, g_h = 0.0, q_sfc = qsat;
   for (int it = 0;; ++it) {
-    F_m = lm - clmo_businger_psi_m(zeta, a) + clmo_businger_psi_m(zeta * z0m / dz, a);
-    F_h = a->Pr_0 * (lh - clmo_businger_psi_h(zeta, a) + clmo_businger_psi_h(zeta * z0b / dz, a));
+    F_m = lm - clmo_businger_psi_m(zeta, a) + clmo_businger_psi_m(zeta * rm, a);
+    F_h = a->Pr_0 * (lh - clmo_businger_psi_h(zeta, a) + clmo_businger_psi_h(zeta * rb, a));
     const double ustar = a->von_karman * U / F_m;
     g_h = a->von_karman * ustar / F_h;
     q_sfc = q_sfc_update(g_h, q_air, T_sfc, Tf_sfc, g_soil, beta_ice, qsat);
     if (it >= a->iterations) break;
     const double thv_sfc = T_sfc * (1.0 + delta * q_sfc);
     const double Ri = grav * dz * (thv_air - thv_sfc) / (thv_sfc * U * U);
-    zeta = fmin(fmax(Ri * F_m * F_m / F_h, -a->zeta_max), a->zeta_max);
+    if (Ri >= 0.0) {
+      zeta = stable_zeta(a, Ri, lm, lh, rm, rb);
+    } else if (zeta >= 0.0) {
+      zeta = Ri * lm * lm / (a->Pr_0 * lh); /* one fixed-point step from 0 */
+    } else { /* Newton on r = zeta F_h - Ri F_m^2 at fixed Ri */
+      const double dF_m = -dpsi_m(zeta, a) + rm * dpsi_m(zeta * rm, a);
+      const double dF_h = a->Pr_0 * (-dpsi_h(zeta, a) + rb * dpsi_h(zeta * rb, a));
+      const double r = zeta * F_h - Ri * F_m * F_m;
+      const double dr = F_h + zeta * dF_h - 2.0 * Ri * F_m * dF_m;
+      zeta = fmin(fmax(zeta - r / dr, -a->zeta_max), 0.0);
+    }
   }
   const double E = -rho_sfc * g_h * (q_air - q_sfc);
   const double lhf = a->LH_v0 * E;
