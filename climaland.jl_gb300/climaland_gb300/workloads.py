@@ -456,7 +456,7 @@ def with_root_extraction(w: Workload, seed: int = 0) -> Workload:
     return out
 
 
-def with_atmos(w: Workload, seed: int = 0) -> Workload:
+def with_atmos(w: Workload, seed: int = 0, runoff: int = A.CLM_RUNOFF_NONE) -> Workload:
     """The EnergyHydrology workload under the atmosphere-driven top boundary
     (AtmosDrivenFluxBC, prescribed atmosphere and radiation, NoRunoff) with
     per-column drivers: air temperature within U[-8, 8] K of the top
@@ -470,7 +470,10 @@ def with_atmos(w: Workload, seed: int = 0) -> Workload:
     albedo thickness U[0.01, 0.4] m (from the top layer alone to a mean over
     several), emissivity U[0.9, 1], z_0m U[1e-3, 5e-2] m, z_0b U[0.05, 1]
     z_0m, dry-layer depth U[0.01, 0.02] m, evaporation exponent U[1, 3] and
-    scalar U[0.5, 2]."""
+    scalar U[0.5, 2]. `runoff` selects the runoff model; TOPMODEL adds the
+    parameter rows f_max U[0.2, 0.6], f_over U[2, 4] 1/m and R_sb U[0.5, 2]
+    x 1.484e-7 m/s around the reference's defaults (Soil.jl:343-345: 3.28 and
+    1.484e-4 / 1000)."""
     assert w.cfg.model == A.CLM_MODEL_ENERGY_HYDROLOGY
     rng = np.random.Generator(np.random.PCG64(12000 + seed))
     n = w.ncol
@@ -513,7 +516,36 @@ def with_atmos(w: Workload, seed: int = 0) -> Workload:
     out = w.columns(0, w.ncol, name=f"{w.name}_atmos")
     out.cfg.bc_top_water = A.CLM_BC_ATMOS
     out.cfg.bc_top_heat = A.CLM_BC_ATMOS
-    out.cfg.runoff = A.CLM_RUNOFF_NONE
+    out.cfg.runoff = runoff
+    if runoff == A.CLM_RUNOFF_TOPMODEL and out.params.shape[0] < A.CLM_NPARAM_MAX:
+        prm = np.zeros((A.CLM_NPARAM_MAX, n))
+        prm[: out.params.shape[0]] = out.params
+        prm[A.CLM_P_F_MAX] = rng.uniform(0.2, 0.6, n)
+        prm[A.CLM_P_F_OVER] = rng.uniform(2.0, 4.0, n)
+        prm[A.CLM_P_R_SB] = 1.484e-7 * rng.uniform(0.5, 2.0, n)
+        out.params = prm
+    if runoff == A.CLM_RUNOFF_TOPMODEL:
+        # a water table: in half the columns with K_sat < 2e-6 m/s (a table
+        # under fast-draining soil empties within a step) the unfrozen layers
+        # of the bottom third hold vartheta_l = nu + U[0, 0.002] without ice,
+        # rho e_int re-derived at each layer's temperature
+        nl = np.diff(out.offsets)
+        col = np.repeat(np.arange(n), nl)
+        k = np.arange(out.ncells) - np.repeat(out.offsets[:-1], nl)
+        v, ti, re = out.vartheta_l.copy(), out.theta_i.copy(), out.rho_e_int.copy()
+        nu_c = out.params[A.CLM_P_NU][col]
+        rcds = out.params[A.CLM_P_RHOC_DS][col]
+        tl0 = np.minimum(v, nu_c - ti)
+        T = e.T_0 + (re + ti * e.rho_i * e.LH_f0) / (rcds + tl0 * e.rho_l * e.cp_l + ti * e.rho_i * e.cp_i)
+        slow = (rng.random(n) < 0.5) & (out.params[A.CLM_P_K_SAT] < 2e-6)
+        wet = slow[col] & (k < nl[col] // 3) & (T > e.T_freeze + 1.0)
+        v[wet] = nu_c[wet] + rng.uniform(0.0, 0.002, int(wet.sum()))
+        ti[wet] = 0.0
+        tl = np.minimum(v, nu_c - ti)
+        re[wet] = ((rcds + tl * e.rho_l * e.cp_l) * (T - e.T_0))[wet]
+        out.vartheta_l, out.theta_i, out.rho_e_int = v, ti, re
+    if runoff != A.CLM_RUNOFF_NONE:
+        out.name = f"{out.name}_runoff{runoff}"
     out.forcing = {k: v for k, v in out.forcing.items()
                    if k not in (A.CLM_BC_TOP_WATER, A.CLM_BC_TOP_HEAT)}
     out.atmos = d

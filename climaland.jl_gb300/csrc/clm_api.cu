@@ -544,10 +544,11 @@ int clm_create(const clm_config* cfg, clm_handle** out) {
   if (cfg->bc_top_water == CLM_BC_PRECIP_RUNOFF &&
       (cfg->model != CLM_MODEL_RICHARDS || cfg->runoff < CLM_RUNOFF_NONE || cfg->runoff > CLM_RUNOFF_TOPMODEL))
     return CLM_ERR_ARG;
-  // AtmosDrivenFluxBC sets both top fluxes of EnergyHydrology (NoRunoff)
+  // AtmosDrivenFluxBC sets both top fluxes of EnergyHydrology
   if ((cfg->bc_top_water == CLM_BC_ATMOS) != (cfg->bc_top_heat == CLM_BC_ATMOS)) return CLM_ERR_ARG;
   if (cfg->bc_top_water == CLM_BC_ATMOS &&
-      (cfg->model != CLM_MODEL_ENERGY_HYDROLOGY || cfg->runoff != CLM_RUNOFF_NONE))
+      (cfg->model != CLM_MODEL_ENERGY_HYDROLOGY || cfg->runoff < CLM_RUNOFF_NONE ||
+       cfg->runoff > CLM_RUNOFF_TOPMODEL))
     return CLM_ERR_ARG;
   if (cfg->bc_top_water == CLM_BC_FREE_DRAINAGE || cfg->bc_top_water == CLM_BC_FLUX_ADVECTIVE ||
       cfg->bc_bottom_water == CLM_BC_FLUX_ADVECTIVE || cfg->bc_top_heat == CLM_BC_FREE_DRAINAGE ||
@@ -672,7 +673,8 @@ int clm_set_geometry(clm_handle* h, const double* z_lo, const double* z_hi, cons
 int clm_set_params(clm_handle* h, const double* p, int32_t nparams) {
   if (!h) return CLM_ERR_ARG;
   if (!h->have_geometry) return fail(h, CLM_ERR_STATE, "clm_set_geometry has not been called");
-  const bool topmodel = h->cfg.bc_top_water == CLM_BC_PRECIP_RUNOFF && h->cfg.runoff == CLM_RUNOFF_TOPMODEL;
+  const bool topmodel = (h->cfg.bc_top_water == CLM_BC_PRECIP_RUNOFF || h->cfg.bc_top_water == CLM_BC_ATMOS) &&
+                        h->cfg.runoff == CLM_RUNOFF_TOPMODEL;
   const int need = topmodel ? CLM_NPARAM_MAX : (is_eh(h) ? CLM_NPARAM_EH : CLM_NPARAM_RICHARDS);
   if (!p || nparams < need || nparams > CLM_NPARAM_MAX)
     return fail(h, CLM_ERR_ARG, "expected " + std::to_string(need) + " parameter rows");

@@ -141,6 +141,7 @@ struct AtmosSfc {
   double dz_top;        // top centre to the surface
   double th_alb;        // theta_l for the albedo (top-thickness mean or top centre)
   double ti;            // theta_i of the top centre
+  double infil;         // infiltration of P_liq after the runoff model (EHRunoff)
 };
 
 struct AtmosOut {
@@ -256,19 +257,9 @@ CLM_HD AtmosOut atmos_bc(const Tables& Tb, const AtmosK& K, const Earth& E, cons
   const double T2 = sf.T * sf.T;
   o.R_n = -(1.0 - alpha) * D(CLM_AT_SW_D) - D(CLM_AT_EMISSIVITY) * (D(CLM_AT_LW_D) - K.stefan * (T2 * T2));
   o.q_sfc = q_sfc;
-  o.top_w = P_liq + o.vliq;
-  o.top_h = ((o.R_n + o.lhf) + o.shf) + P_liq * rho_e_liq(E, T_air);
+  o.top_w = sf.infil + o.vliq;
+  o.top_h = ((o.R_n + o.lhf) + o.shf) + sf.infil * rho_e_liq(E, T_air);
   return o;
-}
-
-// Tf_depressed as update_aux computes it (energy_hydrology.jl:797-808 passes
-// (rho_l, rho_i) into the (rho_ice, rho_liq) slots of soil_Tf_depressed).
-template <class CM>
-CLM_HD double tf_depressed_aux(const Tables& Tb, const Earth& E, const CM& g, double nu,
-                               double theta_r, double theta_l, double theta_i) {
-  const double tt = fmin(E.rho_l / E.rho_i * theta_i + theta_l, nu);
-  const double pw = matric_of(Tb, g, nu, tt, theta_r);
-  return fmax(E.T_freeze * fm::exp(Tb, E.grav_over_LH_f0 * pw), 1.0);
 }
 
 // Layer geometry of a uniform column [z_lo, z_hi] with n layers, as the
@@ -281,6 +272,69 @@ struct ColGeom {
   CLM_HD double centre(int k) const { return 0.5 * (face(k) + face(k + 1)); }
   CLM_HD double width(int k) const { return face(k + 1) - face(k); }
 };
+
+// Runoff of the atmosphere-driven boundary on an EnergyHydrology column
+// (src/standalone/Soil/Runoff/Runoff.jl): NoRunoff (:69-71), SurfaceRunoff
+// (:129-148) and TOPMODELRunoff (:234-283) with the infiltration capacity
+// -K_sat impedance viscosity of the top centre (:401-413), and TOPMODEL's
+// implicit subsurface sink (:347-371): R_ss / max(h, eps) w_k on vartheta_l
+// and R_ess / max(h, eps) w_k on rho e_int, w_k the liquid saturation weights.
+struct EHRunoff {
+  double infil;       // infiltration (m/s)
+  double R_ss, R_ess; // subsurface water and energy runoff (TOPMODEL), else 0
+  double cw, ce;      // R_ss / max(h, eps), R_ess / max(h, eps)
+};
+
+// H(vartheta - nu) (vartheta - theta_r) / (nu - theta_r) with the runoff
+// heaviside (x > eps)
+CLM_HD double sat_weight(double twc, double nr) { return ((twc - nr) - 0.0 > kEps ? 1.0 : 0.0) * twc / nr; }
+
+// layer(k, v, ti, T) fills the layer's vartheta_l, theta_i and T
+template <class Layer>
+CLM_HD EHRunoff eh_runoff(const Tables& Tb, const Earth& E, const EHScalars& sc, int runoff,
+                          const ColGeom& G, double nu, double theta_r, double K_sat, double f_max,
+                          double f_over, double R_sb, double tl_top, double input, Layer layer) {
+  EHRunoff r{input, 0.0, 0.0, 0.0, 0.0};
+  if (runoff == CLM_RUNOFF_NONE) return r;
+  const int n = G.n;
+  double v, ti, T;
+  layer(n - 1, v, ti, T);
+  const double ic = -K_sat * fm::exp(Tb, -sc.omega_ln10 * (ti / (tl_top + ti - theta_r))) *
+                    fm::exp(Tb, sc.visc_gamma * (T - sc.visc_gamma_T_ref));
+  if (runoff == CLM_RUNOFF_SURFACE) {
+    const double is_sat = ((v + ti) - nu) - 0.0 > kEps ? 1.0 : 0.0;
+    r.infil = (1.0 - is_sat) * fmax(ic, input);
+    return r;
+  }
+  const double nr = nu - theta_r;
+  double h_ice = 0.0, h = 0.0, Ew = 0.0;
+  for (int k = 0; k < n; ++k) {
+    layer(k, v, ti, T);
+    const double dzk = G.width(k);
+    h_ice += dzk * sat_weight(v + ti - theta_r, nr);
+    const double w = sat_weight(v - theta_r, nr);
+    h += dzk * w;
+    Ew += dzk * (w * rho_e_liq(E, T));
+  }
+  const double depth = G.zhi - G.zlo;
+  const double f_sat = fmin(f_max * fm::exp(Tb, -f_over / 2.0 * (depth - h_ice)), 1.0);
+  r.infil = (1.0 - f_sat) * fmax(ic, input);
+  r.R_ss = R_sb * fm::exp(Tb, -f_over * (depth - h));
+  r.R_ess = Ew * (r.R_ss / fmax(h, kEps));
+  r.cw = r.R_ss / fmax(h, kEps);
+  r.ce = r.R_ess / fmax(h, kEps);
+  return r;
+}
+
+// Tf_depressed as update_aux computes it (energy_hydrology.jl:797-808 passes
+// (rho_l, rho_i) into the (rho_ice, rho_liq) slots of soil_Tf_depressed).
+template <class CM>
+CLM_HD double tf_depressed_aux(const Tables& Tb, const Earth& E, const CM& g, double nu,
+                               double theta_r, double theta_l, double theta_i) {
+  const double tt = fmin(E.rho_l / E.rho_i * theta_i + theta_l, nu);
+  const double pw = matric_of(Tb, g, nu, tt, theta_r);
+  return fmax(E.T_freeze * fm::exp(Tb, E.grav_over_LH_f0 * pw), 1.0);
+}
 
 // theta_l for the albedo: the mean over the layers centred within
 // `thick` of the surface when the thinnest layer is thinner than it

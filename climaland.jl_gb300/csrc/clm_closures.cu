@@ -110,6 +110,7 @@ __device__ void closure_column(const ClosureArgs& C, const Tables& Tb) {
   // atmosphere-driven top boundary (CLM_BC_ATMOS) from the aux values above
   const ColGeom G{A.z_lo[s], A.z_hi[s], n};
   AtmosOut ab{};
+  EHRunoff ro{0.0, 0.0, 0.0, 0.0, 0.0};
   double dz_top = 0.0;
   const bool atmos = eh && A.atm && A.bc_tw == CLM_BC_ATMOS;
   if (atmos) {
@@ -126,6 +127,14 @@ __device__ void closure_column(const ClosureArgs& C, const Tables& Tb) {
     sf.dz_top = dz_top;
     const AtmosRow D{A.atm, st, s};
     sf.th_alb = albedo_theta(G, D(CLM_AT_ALBEDO_TOP_THICKNESS), [&](int k) { return tlc[k]; });
+    ro = eh_runoff(Tb, E, sc, A.runoff, G, nu, theta_r, K_sat, P[CLM_P_F_MAX * st + s],
+                   P[CLM_P_F_OVER * st + s], P[CLM_P_R_SB * st + s], tlc[n - 1], D(CLM_AT_P_LIQ),
+                   [&](int k, double& v, double& ti, double& T) {
+                     v = C.v[o + k];
+                     ti = C.ti[o + k];
+                     T = Tc[k];
+                   });
+    sf.infil = ro.infil;
     ab = atmos_bc(Tb, A.ak, E, D, g, nu, theta_r, sf);
     Ftw = ab.top_w;
     Fth = ab.top_h;
@@ -216,16 +225,18 @@ __device__ void closure_column(const ClosureArgs& C, const Tables& Tb) {
         Fw_up = Ftw;
         Fe_up = Fth;
       }
-      if (C.dv) C.dv[o + k] = -((Fw_up - Fw_dn) * inv_dz);
+      // TOPMODEL's subsurface sink under the atmosphere-driven boundary
+      const double w = (ro.cw != 0.0 || ro.ce != 0.0) ? sat_weight(C.v[o + k] - theta_r, nu - theta_r) : 0.0;
+      if (C.dv) C.dv[o + k] = -((Fw_up - Fw_dn) * inv_dz) - ro.cw * w;
       if (eh) {
-        if (C.de) C.de[o + k] = -((Fe_up - Fe_dn) * inv_dz);
+        if (C.de) C.de[o + k] = -((Fe_up - Fe_dn) * inv_dz) - ro.ce * w;
         if (C.dti) C.dti[o + k] = 0.0;
       }
       Fw_dn = Fw_up;
       Fe_dn = Fe_up;
     }
-    if (C.dFw) C.dFw[orig] = -(Ftw - Fbw);
-    if (eh && C.dFe) C.dFe[orig] = -(Fth - Fbh);
+    if (C.dFw) C.dFw[orig] = -(Ftw - Fbw) - ro.R_ss;
+    if (eh && C.dFe) C.dFe[orig] = -(Fth - Fbh) - ro.R_ess;
     return;
   }
   if (KIND == CL_JAC) {

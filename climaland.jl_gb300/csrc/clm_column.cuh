@@ -284,6 +284,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
     double dz_top = 0.0;
     double sub_top = 0.0;  // SoilSublimation's theta_i tendency in the layers k >= k_sub
     int k_sub = n;
+    EHRunoff ro{0.0, 0.0, 0.0, 0.0, 0.0};
     if constexpr (kAtmos) {
       auto theta_l_of = [&](int k) {
         const double Yv = B.gv[k], nu_eff = c.nu - B.gti[k];
@@ -307,6 +308,18 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       sf.ti = Yti;
       const AtmosRow D{A.atm, st, s};
       sf.th_alb = albedo_theta(G, D(CLM_AT_ALBEDO_TOP_THICKNESS), theta_l_of);
+      // the runoff model's infiltration (and TOPMODEL's subsurface sink) from
+      // the update_aux values at Y_n
+      const double* P = A.prm;
+      ro = eh_runoff(Tb, E, sc, A.runoff, G, c.nu, c.theta_r, c.K_sat, P[CLM_P_F_MAX * st + s],
+                     P[CLM_P_F_OVER * st + s], P[CLM_P_R_SB * st + s], sf.th1, D(CLM_AT_P_LIQ),
+                     [&](int k, double& v, double& ti, double& T) {
+                       v = B.gv[k];
+                       ti = B.gti[k];
+                       T = E.T_0 + (B.ge[k] + ti * E.rho_i_LH_f0) *
+                                       fm::rcp(heat_capacity(E, theta_l_of(k), ti, c.rcds));
+                     });
+      sf.infil = ro.infil;
       ab = atmos_bc(Tb, A.ak, E, D, c.g, c.nu, c.theta_r, sf);
       // H(z_k + 2 dz_top) rises with k: the source reaches the layers from
       // k_sub up (the top layer alone for a surface at z = 0)
@@ -379,6 +392,15 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       }
       B.gv[k] = Uv;
       B.gti[k] = Uti;
+      if constexpr (kAtmos) {
+        // TOPMODEL's implicit subsurface sink, constant through the Newton
+        // solve: part of the residual's U + dt T_imp, not of the start x = U
+        if (ro.cw != 0.0 || ro.ce != 0.0) {
+          const double w = sat_weight(Yv - c.theta_r, c.nu - c.theta_r);
+          B.gv[k] = Uv - dt * (ro.cw * w);
+          B.ge[k] = Ue - dt * (ro.ce * w);
+        }
+      }
       if constexpr (!mixed)
         if (B.iden.p) B.iden[k] = sat_inv(c.nu - Uti, c.theta_r);
       if (use_guess) {
@@ -568,8 +590,8 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         Tc = Tn; psic = psin; Dc = Dn; Kc = Kn; relKc = relKn;
       }
       // integrated fluxes (their Jacobian block is -I): x += f
-      const double fFw = UFw + dt * (-(Ftw - Fbw)) - xFw;
-      const double fFe = UFe + dt * (-(Fth - Fbh)) - xFe;
+      const double fFw = UFw + dt * ((-(Ftw - Fbw)) - ro.R_ss) - xFw;
+      const double fFe = UFe + dt * ((-(Fth - Fbh)) - ro.R_ess) - xFe;
       xFw += fFw;
       xFe += fFe;
       // sweep 2 (top -> bottom): delta vartheta into dp

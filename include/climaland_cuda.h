@@ -93,15 +93,20 @@ enum clm_bc_kind {
                                  atmosphere and radiation, standalone soil
                                  (boundary_conditions.jl:610-677, 870-936):
                                  the drivers of clm_set_atmos; both top
-                                 kinds must be CLM_BC_ATMOS, cfg->runoff
-                                 CLM_RUNOFF_NONE                          */
+                                 kinds must be CLM_BC_ATMOS; cfg->runoff
+                                 splits P_liq (EnergyHydrology forms of
+                                 Runoff.jl: infiltration capacity
+                                 -K_sat impedance viscosity at the top,
+                                 saturation with ice, and TOPMODEL's
+                                 subsurface water and energy sink)        */
 };
 
 /* Per-column parameter rows for clm_set_params (SoA, row p of ncol). The
  * first CLM_NPARAM_RICHARDS rows are RichardsParameters (rre.jl:7-21); all
  * CLM_NPARAM_EH rows are the per-point EnergyHydrologyParameters
  * (energy_hydrology.jl:21-78). */
-/* Runoff model of CLM_BC_PRECIP_RUNOFF (src/standalone/Soil/Runoff/Runoff.jl). */
+/* Runoff model of CLM_BC_PRECIP_RUNOFF and CLM_BC_ATMOS
+ * (src/standalone/Soil/Runoff/Runoff.jl). */
 enum clm_runoff {
   CLM_RUNOFF_NONE = 0,     /* NoRunoff: infiltration = P (:56-80)            */
   CLM_RUNOFF_SURFACE = 1,  /* SurfaceRunoff: (1 - H(theta_top - nu)) max(-K_sat, P)
@@ -221,8 +226,9 @@ enum clm_root_field {
  *   ALBEDO_TOP_THICKNESS (soil_albedo.jl:146-198); net radiation
  *   -(1 - alpha) SW_d - eps (LW_d - sigma T_sfc^4) (drivers.jl:699-716);
  *   turbulent fluxes by Monin-Obukhov similarity (see clm_atmos_params);
- *   top water flux = P_liq + E / rho_l (liquid part), top energy flux =
- *   R_n + LHF + SHF + P_liq rho e_liq(T_air) (boundary_conditions.jl:
+ *   top water flux = infiltration + E / rho_l (liquid part), top energy flux =
+ *   R_n + LHF + SHF + infiltration rho e_liq(T_air), the infiltration P_liq
+ *   or, with cfg->runoff, its infiltrating part (boundary_conditions.jl:
  *   908-936, 988-1003); the sublimation part of E leaves theta_i of the
  *   layers with z + 2 dz_top > eps (the top layer for a surface at z = 0) and
  *   enters intF_w (SoilSublimation, energy_hydrology.jl:910-947). */

@@ -432,7 +432,7 @@ typedef struct { /* p.soil */
   int has_dflux;
   /* runoff (Runoff.jl): infiltration, surface runoff R_s, subsurface runoff
    * R_ss, saturated height h_sat, per-layer saturation weights */
-  double infiltration, R_s, R_ss, h_sat;
+  double infiltration, R_s, R_ss, h_sat, R_ess;
   double sat_w[MAXL];
   int runoff_sink;
   double dfluxBCdY;
@@ -768,6 +768,57 @@ static double q_sfc_update(double g_h, double q_air, double T_sfc, double Tf,
   return (g_soil / g_h * qsat + q_air) / (1.0 + g_soil / g_h);
 }
 
+/* Runoff of AtmosDrivenFluxBC on an EnergyHydrology column
+ * (src/standalone/Soil/Runoff/Runoff.jl): update_infiltration_water_flux! for
+ * NoRunoff (:69-71), SurfaceRunoff (:129-148) and TOPMODELRunoff (:234-283,
+ * with update_subsurface_energy_runoff!), the infiltration capacity
+ * -K_sat impedance(theta_i / (theta_l + theta_i - theta_r)) viscosity(T) of
+ * the top centre (:401-413); input is P_liq. */
+static void eh_runoff(const col_t* C, const state_t* Y, cache_t* p, double input) {
+  const int n = C->n;
+  const clm_config* cfg = C->cfg;
+  const clm_earth_params* e = &cfg->earth;
+  const double tl = p->theta_l[n - 1], ti = Y->ti[n - 1];
+  const double ic = -C->K_sat * clmo_impedance_factor(ti / (tl + ti - C->theta_r), cfg->ice_impedance_omega) *
+                    clmo_viscosity_factor(p->T[n - 1], cfg->visc_gamma, cfg->visc_gamma_T_ref);
+  switch (cfg->runoff) {
+    case CLM_RUNOFF_SURFACE: {
+      const double is_sat = runoff_heaviside((Y->v[n - 1] + Y->ti[n - 1]) - C->nu);
+      p->infiltration = (1.0 - is_sat) * fmax(ic, input);
+      p->R_s = fabs(input - p->infiltration);
+      break;
+    }
+    case CLM_RUNOFF_TOPMODEL: {
+      const double nr = C->nu - C->theta_r;
+      double h = 0.0;
+      for (int k = 0; k < n; ++k) { /* weights with ice */
+        const double twc = Y->v[k] + Y->ti[k] - C->theta_r;
+        h += C->dzc[k] * (runoff_heaviside(twc - nr) * twc / nr);
+      }
+      const double f_sat = fmin(C->f_max * exp(-C->f_over / 2.0 * (C->depth - h)), 1.0);
+      p->infiltration = (1.0 - f_sat) * fmax(ic, input);
+      p->R_s = fabs(input - p->infiltration);
+      h = 0.0; /* again with liquid water only, for the subsurface runoff */
+      double E = 0.0;
+      for (int k = 0; k < n; ++k) {
+        const double twc = Y->v[k] - C->theta_r;
+        p->sat_w[k] = runoff_heaviside(twc - nr) * twc / nr;
+        h += C->dzc[k] * p->sat_w[k];
+      }
+      for (int k = 0; k < n; ++k)
+        E += C->dzc[k] * (p->sat_w[k] * clmo_volumetric_internal_energy_liq(p->T[k], e));
+      p->h_sat = h;
+      p->R_ss = C->R_sb * exp(-C->f_over * (C->depth - h));
+      p->R_ess = E * (p->R_ss / fmax(h, EPS64));
+      p->runoff_sink = 1;
+      break;
+    }
+    default:
+      p->infiltration = input;
+      p->R_s = 0.0;
+  }
+}
+
 /* soil_boundary_fluxes!(::AtmosDrivenFluxBC, ::Val{(:soil,)}, ...) at the
  * update_aux values of Y: turbulent_fluxes!, net_radiation!, NoRunoff
  * infiltration and its energy, top_bc (boundary_conditions.jl:908-936). */
@@ -870,10 +921,11 @@ static void atmos_top_bc(const col_t* C, const state_t* Y, cache_t* p) {
   const double T2 = T_sfc * T_sfc;
   const double R_n = -(1.0 - alpha) * AT(CLM_AT_SW_D) -
                      AT(CLM_AT_EMISSIVITY) * (AT(CLM_AT_LW_D) - a->stefan * (T2 * T2));
-  /* NoRunoff: infiltration = P_liq; its energy at the air temperature */
-  p->infiltration = P_liq;
-  p->top_w = P_liq + vliq;
-  p->top_h = R_n + lhf + shf + P_liq * clmo_volumetric_internal_energy_liq(T_air, e);
+  /* the runoff model splits P_liq; the infiltration carries the energy of
+   * liquid water at the air temperature (boundary_conditions.jl:988-1003) */
+  eh_runoff(C, Y, p, P_liq);
+  p->top_w = p->infiltration + vliq;
+  p->top_h = R_n + lhf + shf + p->infiltration * clmo_volumetric_internal_energy_liq(T_air, e);
   p->atmos[CLM_AF_LHF] = lhf;
   p->atmos[CLM_AF_SHF] = shf;
   p->atmos[CLM_AF_VAPOR_LIQ] = vliq;
@@ -1120,6 +1172,12 @@ static void imp_tendency(const col_t* C, const state_t* Y, const cache_t* p,
       dY->e[k] = -((Fe[k + 1] - Fe[k]) / C->dzc[k]);
       dY->ti[k] = 0.0;
     }
+    if (p->runoff_sink) {
+      /* TOPMODELSubsurfaceRunoff on EnergyHydrology (Runoff.jl:347-371): the
+       * energy of the drained liquid water */
+      for (int k = 0; k < n; ++k) dY->e[k] -= (p->R_ess / fmax(p->h_sat, EPS64)) * p->sat_w[k];
+      dY->Fe -= p->R_ess;
+    }
   } else {
     dY->Fe = 0.0;
   }
@@ -1317,9 +1375,10 @@ static int check_problem(const clmo_problem* P) {
     return CLM_ERR_ARG;
   if (P->cfg.bc_top_water == CLM_BC_ATMOS || P->cfg.bc_top_heat == CLM_BC_ATMOS) {
     if (P->cfg.model != CLM_MODEL_ENERGY_HYDROLOGY || P->cfg.bc_top_water != CLM_BC_ATMOS ||
-        P->cfg.bc_top_heat != CLM_BC_ATMOS || P->cfg.runoff != CLM_RUNOFF_NONE || !P->atmos ||
-        P->root || P->atm.iterations < 1)
+        P->cfg.bc_top_heat != CLM_BC_ATMOS || P->cfg.runoff < CLM_RUNOFF_NONE ||
+        P->cfg.runoff > CLM_RUNOFF_TOPMODEL || !P->atmos || P->root || P->atm.iterations < 1)
       return CLM_ERR_ARG;
+    if (P->cfg.runoff == CLM_RUNOFF_TOPMODEL && P->nparams < CLM_NPARAM_MAX) return CLM_ERR_ARG;
   }
   if (P->cfg.bc_top_water == CLM_BC_PRECIP_RUNOFF) {
     if (P->cfg.model != CLM_MODEL_RICHARDS) return CLM_ERR_ARG;

@@ -138,8 +138,7 @@ def test_create_rejects_misplaced_atmos_boundary(lib):
     for model, tw, th, runoff in ((A.CLM_MODEL_RICHARDS, A.CLM_BC_ATMOS, A.CLM_BC_ATMOS, 0),
                                   (A.CLM_MODEL_ENERGY_HYDROLOGY, A.CLM_BC_ATMOS, A.CLM_BC_FLUX, 0),
                                   (A.CLM_MODEL_ENERGY_HYDROLOGY, A.CLM_BC_FLUX, A.CLM_BC_ATMOS, 0),
-                                  (A.CLM_MODEL_ENERGY_HYDROLOGY, A.CLM_BC_ATMOS, A.CLM_BC_ATMOS,
-                                   A.CLM_RUNOFF_SURFACE)):
+                                  (A.CLM_MODEL_ENERGY_HYDROLOGY, A.CLM_BC_ATMOS, A.CLM_BC_ATMOS, 7)):
         cfg = A.default_config()
         cfg.model, cfg.ncol, cfg.nlayers = model, 4, 5
         cfg.bc_top_water, cfg.bc_top_heat, cfg.runoff = tw, th, runoff

@@ -166,6 +166,14 @@ ATMOS = {
                        dict(oracle_cfg=TOL_MODE, **TOL_MODE)),
     "mixed_full_scale": (lambda: WL.with_atmos(WL.full_scale_c4(ncol=1024)), 48, MIXED),
     "mixed_brooks_corey": (lambda: WL.with_atmos(WL.brooks_corey(WL.full_scale_c4(ncol=512))), 48, MIXED),
+    "surface_runoff": (lambda: WL.with_atmos(WL.full_scale_c4(ncol=1024), runoff=A.CLM_RUNOFF_SURFACE), 48, {}),
+    "topmodel": (lambda: WL.with_atmos(WL.full_scale_c4(ncol=1024), runoff=A.CLM_RUNOFF_TOPMODEL), 48, {}),
+    "topmodel_uneven": (lambda: WL.with_atmos(WL.uneven_c2().subset(1024), runoff=A.CLM_RUNOFF_TOPMODEL), 48, {}),
+    # supersaturated water-table layers (dpsi/dvartheta = 1/S_s) make the
+    # mixed path's float Jacobian rows its least accurate part: with three
+    # fixed Newton iterations one column of 1024 reaches 1.8e-8 in rho e_int
+    "mixed_topmodel": (lambda: WL.with_atmos(WL.full_scale_c4(ncol=1024), runoff=A.CLM_RUNOFF_TOPMODEL), 48,
+                       dict(MIXED, tol_state=2e-8)),
 }
 
 
@@ -203,11 +211,11 @@ def test_atmos_fluxes_match_oracle(bc):
 
 
 def test_atmos_boundary_refusals():
-    """EnergyHydrology only, both top kinds, NoRunoff; drivers required and
+    """EnergyHydrology only, both top kinds, a known runoff model; drivers required and
     validated; no root extraction beside it; removing the drivers stops the
     step until they are set again."""
     w = WL.with_atmos(WL.full_scale_c4(ncol=64))
-    for mut in (dict(bc_top_heat=A.CLM_BC_FLUX), dict(runoff=A.CLM_RUNOFF_SURFACE)):
+    for mut in (dict(bc_top_heat=A.CLM_BC_FLUX), dict(runoff=7)):
         cfg = A.ClmConfig.from_buffer_copy(w.cfg)
         for k, v in mut.items():
             setattr(cfg, k, v)

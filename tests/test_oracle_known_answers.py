@@ -832,14 +832,68 @@ def test_sublimation_source(L):
 
 def test_atmos_boundary_refusals(L):
     """The boundary is EnergyHydrology-only, sets both top fluxes, needs its
-    drivers, and runs without a runoff model or root extraction."""
+    drivers, runs without root extraction, and TOPMODEL needs its parameter
+    rows."""
     w = WL.with_atmos(WL.energy_hydrology_c1(ncol=8, nlayers=6))
     st = w.copy_state()
-    for mut in (dict(bc_top_heat=A.CLM_BC_FLUX), dict(runoff=A.CLM_RUNOFF_SURFACE),
-                dict(model=A.CLM_MODEL_RICHARDS)):
+    for mut in (dict(bc_top_heat=A.CLM_BC_FLUX), dict(runoff=A.CLM_RUNOFF_TOPMODEL),
+                dict(runoff=7), dict(model=A.CLM_MODEL_RICHARDS)):
         o = O.Oracle(w)
         o.set_cfg(**mut)
         assert o.step(w.copy_state(), 0.0, 1.0, 1)[0] == A.CLM_ERR_ARG
     o = O.Oracle(w)
     o.P.atmos = None
     assert o.step(st, 0.0, 1.0, 1)[0] == A.CLM_ERR_ARG
+
+
+def test_energy_hydrology_runoff_under_the_atmos_boundary(L):
+    """test/standalone/Soil/runoff.jl:216-295 (EnergyHydrology, TOPMODEL):
+    h = sum dz H(vartheta - nu) (vartheta - theta_r) / (nu - theta_r),
+    R_ss = R_sb exp(-f_over (depth - h)), the infiltration
+    (1 - min(f_max exp(-f_over (depth - h_ice) / 2), 1)) max(i_c, P_liq) with
+    i_c = -K_sat impedance(theta_i / (theta_l + theta_i - theta_r)) viscosity(T)
+    (Runoff.jl:401-413), R_ess = sum dz w rho e_liq(T) R_ss / max(h, eps); the
+    implicit tendency loses R_ss from intF_w and R_ess from intF_e, and the
+    layers lose R_ss / h w and R_ess / h w. SurfaceRunoff: (1 - H(vartheta +
+    theta_i - nu)) max(i_c, P_liq) at the top."""
+    E_ = A.DEFAULT_EARTH
+    cfg = A.default_config()
+    for runoff in (A.CLM_RUNOFF_SURFACE, A.CLM_RUNOFF_TOPMODEL):
+        w = WL.with_atmos(WL.full_scale_c4(ncol=64, nlayers=8), runoff=runoff)
+        o = O.Oracle(w)
+        st = w.copy_state()
+        aux = o.update_cache(st, 0.0)
+        f = o.atmos_fluxes(st)
+        infil = f[A.CLM_AF_TOP_WATER] - f[A.CLM_AF_VAPOR_LIQ]
+        imp = o.imp_tendency(st, 0.0)
+        n = 8
+        for c in range(w.ncol):
+            sl = slice(c * n, (c + 1) * n)
+            v, ti = st[0][sl], st[1][sl]
+            T, tl = aux["T"][sl], aux["theta_l"][sl]
+            pr = w.params[:, c]
+            nu, tr = pr[A.CLM_P_NU], pr[A.CLM_P_THETA_R]
+            dz = np.diff(w.z_lo[c] + (w.z_hi[c] - w.z_lo[c]) * np.arange(n + 1) / n)
+            ic = (-pr[A.CLM_P_K_SAT] * 10.0 ** (-cfg.ice_impedance_omega * ti[-1] / (tl[-1] + ti[-1] - tr))
+                  * math.exp(cfg.visc_gamma * (T[-1] - cfg.visc_gamma_T_ref)))
+            P = w.atmos[A.CLM_AT_P_LIQ, c]
+            if runoff == A.CLM_RUNOFF_SURFACE:
+                sat = 1.0 if (v[-1] + ti[-1]) - nu > EPS else 0.0
+                assert approx(infil[c], (1 - sat) * max(ic, P), rtol=1e-12, atol=1e-22)
+                continue
+            H = lambda x: (x > EPS).astype(float)
+            nr = nu - tr
+            h_ice = np.sum(dz * (H((v + ti - tr) - nr) * (v + ti - tr) / nr))
+            wgt = H((v - tr) - nr) * (v - tr) / nr
+            h = np.sum(dz * wgt)
+            depth = w.z_hi[c] - w.z_lo[c]
+            fsat = min(pr[A.CLM_P_F_MAX] * math.exp(-pr[A.CLM_P_F_OVER] / 2 * (depth - h_ice)), 1.0)
+            assert approx(infil[c], (1 - fsat) * max(ic, P), rtol=1e-12, atol=1e-22)
+            R_ss = pr[A.CLM_P_R_SB] * math.exp(-pr[A.CLM_P_F_OVER] * (depth - h))
+            R_ess = np.sum(dz * wgt * E_["cp_l"] * E_["rho_l"] * (T - E_["T_0"])) * R_ss / max(h, EPS)
+            top_w, top_h = f[A.CLM_AF_TOP_WATER, c], f[A.CLM_AF_TOP_HEAT, c]
+            bot_w, bot_h = aux["bc"][2][c], aux["bc"][3][c]
+            assert approx(imp[3][c], -(top_w - bot_w) - R_ss, rtol=1e-12, atol=1e-20)
+            assert approx(imp[4][c], -(top_h - bot_h) - R_ess, rtol=1e-12, atol=1e-9)
+        if runoff == A.CLM_RUNOFF_TOPMODEL:
+            assert (w.vartheta_l > w.params[A.CLM_P_NU][np.repeat(np.arange(w.ncol), n)]).any()
