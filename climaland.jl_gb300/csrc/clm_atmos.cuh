@@ -18,8 +18,9 @@
 //   turbulent fluxes   Monin-Obukhov similarity at point values with the
 //                      Businger-Dyer functions: zeta = dz / L_MO from
 //                      zeta F_h = Ri_b F_m^2 (stable: the quadratic's root;
-//                      unstable: Newton steps), a fixed number of
-//                      iterations, the surface humidity re-evaluated from the
+//                      unstable: Newton steps), at most `iterations` steps
+//                      (fewer once zeta moves by <= 1e-12 (1 + |zeta|)),
+//                      the surface humidity re-evaluated from the
 //                      heat conductance in each (update_q_vap_sfc_at_a_point,
 //                      :1066-1099);
 //   radiation          R_n = -(1 - alpha) SW_d - eps (LW_d - sigma T^4), the
@@ -197,6 +198,7 @@ CLM_HD AtmosOut atmos_bc(const Tables& Tb, const AtmosK& K, const Earth& E, cons
   const double rm = z0m / dz, rb = z0b / dz;
   const double kk_U = K.von_karman * K.von_karman * U;
   double zeta = 0.0, g_h = 0.0, q_sfc = qsat;
+  bool done = false;  // the last step moved zeta by at most 1e-12 (1 + |zeta|)
   for (int it = 0;; ++it) {
     // F_m = lm - psi_m(zeta) + psi_m(zeta z0m/dz), F_h = Pr_0 (lh - psi_h(zeta) +
     // psi_h(zeta z0b/dz)) and, on the unstable side, their zeta-derivatives
@@ -227,19 +229,22 @@ CLM_HD AtmosOut atmos_bc(const Tables& Tb, const AtmosK& K, const Earth& E, cons
       q_sfc = q_air < qsat ? beta_ice * qsat + (1.0 - beta_ice) * q_air : qsat;
     else  // (g_soil / g_h qsat + q_air) / (1 + g_soil / g_h)
       q_sfc = (g_soil * qsat + g_h * q_air) * fm::rcp(g_h + g_soil);
-    if (it >= K.iterations) break;
+    if (it >= K.iterations || done) break;
     const double thv_sfc = sf.T * (1.0 + K.delta * q_sfc);
     const double Ri = gU * (thv_air - thv_sfc) * fm::rcp(thv_sfc);
+    double zn;
     if (Ri >= 0.0) {
-      zeta = stable_zeta(K, Ri, lm, lh, rm, rb);
+      zn = stable_zeta(K, Ri, lm, lh, rm, rb);
     } else if (zeta >= 0.0) {
-      zeta = Ri * lm * lm * fm::rcp(K.Pr_0 * lh);  // one fixed-point step from 0
+      zn = Ri * lm * lm * fm::rcp(K.Pr_0 * lh);  // one fixed-point step from 0
     } else {
       // Newton on r = zeta F_h - Ri F_m^2 at fixed Ri
       const double r = zeta * F_h - Ri * F_m * F_m;
       const double dr = F_h + zeta * dF_h - 2.0 * Ri * F_m * dF_m;
-      zeta = fmin(fmax(zeta - r * fm::rcp(dr), -K.zeta_max), 0.0);
+      zn = fmin(fmax(zeta - r * fm::rcp(dr), -K.zeta_max), 0.0);
     }
+    done = fabs(zn - zeta) <= 1e-12 * (1.0 + fabs(zeta));
+    zeta = zn;
   }
   AtmosOut o;
   const double Ev = -rho_sfc * g_h * (q_air - q_sfc);
@@ -262,15 +267,17 @@ CLM_HD AtmosOut atmos_bc(const Tables& Tb, const AtmosK& K, const Earth& E, cons
   return o;
 }
 
-// Layer geometry of a uniform column [z_lo, z_hi] with n layers, as the
-// reference's domain builds it: faces z_lo + (z_hi - z_lo) k / n (the top
-// face z_hi), centres the face midpoints.
+// Layer geometry of a uniform column [z_lo, z_hi] with n layers: widths
+// dz = (z_hi - z_lo) / n, centres z_lo + (k + 1/2) dz, the top face z_hi
+// (the reference's column builds the faces as z_lo + (z_hi - z_lo) k / n;
+// the two agree to rounding).
 struct ColGeom {
   double zlo, zhi;
   int n;
-  CLM_HD double face(int k) const { return k == n ? zhi : zlo + (zhi - zlo) * ((double)k / n); }
-  CLM_HD double centre(int k) const { return 0.5 * (face(k) + face(k + 1)); }
-  CLM_HD double width(int k) const { return face(k + 1) - face(k); }
+  double dz;
+  CLM_HD ColGeom(double lo, double hi, int nl) : zlo(lo), zhi(hi), n(nl), dz((hi - lo) / nl) {}
+  CLM_HD double centre(int k) const { return zlo + (k + 0.5) * dz; }
+  CLM_HD double width(int) const { return dz; }
 };
 
 // Runoff of the atmosphere-driven boundary on an EnergyHydrology column
@@ -341,18 +348,15 @@ CLM_HD double tf_depressed_aux(const Tables& Tb, const Earth& E, const CM& g, do
 // (column_integral_definite of H theta_l / N), else the top centre's.
 template <class ThetaL>
 CLM_HD double albedo_theta(const ColGeom& G, double thick, ThetaL theta_l) {
-  double dz_min = G.width(0);
-  for (int k = 1; k < G.n; ++k) dz_min = fmin(dz_min, G.width(k));
-  if (!(dz_min < thick)) return theta_l(G.n - 1);
-  const double z_sfc = G.zhi;
+  if (!(G.dz < thick)) return theta_l(G.n - 1);
+  // H(thick + sqrt(eps) - (z_sfc - z_k)) rises with k: the layers k0..n-1
+  auto H = [&](int k) { return (thick + kSqrtEps) - (G.zhi - G.centre(k)) > kEps; };
+  int k0 = G.n;
+  while (k0 > 0 && H(k0 - 1)) --k0;
   double N = 0.0;
-  for (int k = 0; k < G.n; ++k)
-    N += G.width(k) * (((thick + kSqrtEps) - (z_sfc - G.centre(k)) > kEps) ? 1.0 : 0.0);
+  for (int k = k0; k < G.n; ++k) N += G.dz;
   double I = 0.0;
-  for (int k = 0; k < G.n; ++k) {
-    const double H = ((thick + kSqrtEps) - (z_sfc - G.centre(k)) > kEps) ? 1.0 : 0.0;
-    if (H != 0.0) I += G.width(k) * (H * theta_l(k) / N);
-  }
+  for (int k = k0; k < G.n; ++k) I += G.dz * (theta_l(k) / N);
   return I;
 }
 

@@ -267,7 +267,8 @@ enum clm_atmos_field {
  *   psi_m = -a_m zeta, psi_h = -a_h zeta / Pr_0 (zeta >= 0);
  *   psi_m = 2 ln((1+x)/2) + ln((1+x^2)/2) - 2 atan x + pi/2, x = (1 - b_m zeta)^(1/4),
  *   psi_h = 2 ln((1+y)/2), y = (1 - b_h zeta)^(1/2) (zeta < 0);
- *   u* = kappa U / F_m, g_h = kappa u* / F_h; `iterations` steps from zeta = 0,
+ *   u* = kappa U / F_m, g_h = kappa u* / F_h; at most `iterations` steps from
+ *   zeta = 0 (a column stops once a step moves zeta by <= 1e-12 (1 + |zeta|)),
  *   each re-evaluating F_m, F_h, g_h, q_sfc and
  *   Ri_b = g dz (theta_v,air - theta_v,sfc) / (theta_v,sfc U^2), then solving
  *   zeta F_h(zeta) = Ri_b F_m(zeta)^2 for the next zeta: for Ri_b >= 0 exactly

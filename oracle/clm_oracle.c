@@ -871,26 +871,30 @@ static void atmos_top_bc(const col_t* C, const state_t* Y, cache_t* p) {
   const double thv_air = (T_air + grav * dz / a->cp_d) * (1.0 + delta * q_air);
   const double rm = z0m / dz, rb = z0b / dz;
   double zeta = 0.0, F_m = 0.0, F_h = 0.0, g_h = 0.0, q_sfc = qsat;
+  int done = 0; /* the last step moved zeta by at most 1e-12 (1 + |zeta|) */
   for (int it = 0;; ++it) {
     F_m = lm - clmo_businger_psi_m(zeta, a) + clmo_businger_psi_m(zeta * rm, a);
     F_h = a->Pr_0 * (lh - clmo_businger_psi_h(zeta, a) + clmo_businger_psi_h(zeta * rb, a));
     const double ustar = a->von_karman * U / F_m;
     g_h = a->von_karman * ustar / F_h;
     q_sfc = q_sfc_update(g_h, q_air, T_sfc, Tf_sfc, g_soil, beta_ice, qsat);
-    if (it >= a->iterations) break;
+    if (it >= a->iterations || done) break;
     const double thv_sfc = T_sfc * (1.0 + delta * q_sfc);
     const double Ri = grav * dz * (thv_air - thv_sfc) / (thv_sfc * U * U);
+    double zn;
     if (Ri >= 0.0) {
-      zeta = stable_zeta(a, Ri, lm, lh, rm, rb);
+      zn = stable_zeta(a, Ri, lm, lh, rm, rb);
     } else if (zeta >= 0.0) {
-      zeta = Ri * lm * lm / (a->Pr_0 * lh); /* one fixed-point step from 0 */
+      zn = Ri * lm * lm / (a->Pr_0 * lh); /* one fixed-point step from 0 */
     } else { /* Newton on r = zeta F_h - Ri F_m^2 at fixed Ri */
       const double dF_m = -dpsi_m(zeta, a) + rm * dpsi_m(zeta * rm, a);
       const double dF_h = a->Pr_0 * (-dpsi_h(zeta, a) + rb * dpsi_h(zeta * rb, a));
       const double r = zeta * F_h - Ri * F_m * F_m;
       const double dr = F_h + zeta * dF_h - 2.0 * Ri * F_m * dF_m;
-      zeta = fmin(fmax(zeta - r / dr, -a->zeta_max), 0.0);
+      zn = fmin(fmax(zeta - r / dr, -a->zeta_max), 0.0);
     }
+    done = fabs(zn - zeta) <= 1e-12 * (1.0 + fabs(zeta));
+    zeta = zn;
   }
   const double E = -rho_sfc * g_h * (q_air - q_sfc);
   const double lhf = a->LH_v0 * E;
