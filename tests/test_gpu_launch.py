@@ -148,3 +148,31 @@ def test_host_step_equals_set_step_get(torch, name, make, chunks, nsteps):
         dev = g.get_state()
     _same(ref, (st, f, it))
     _same(ref, (dev, f, it))
+
+
+def test_atmos_boundary_graph_host_and_dynamic_paths_agree(torch):
+    """The atmosphere-driven step (with TOPMODEL runoff) gives the same bits
+    through direct launches, CUDA graph replay, the dynamic tile order and the
+    host-buffer path (clm_step_host, pipelined chunks); drivers refreshed
+    between graph-launched steps are used by the next step."""
+    w = WL.with_atmos(WL.full_scale_c4(ncol=40000), runoff=A.CLM_RUNOFF_TOPMODEL)
+    calls = [(w.t0, 2), (w.t0 + 2 * w.dt, 3)]
+    ref = _run(w, calls, graph=0)
+    _same(ref, _run(w, calls, graph=1))
+    _same(ref, _run(w, calls, schedule=A.CLM_SCHED_DYNAMIC))
+    st = [None if a is None else a.copy() for a in w.copy_state()]
+    with SoilColumns(w, host_chunks=0) as g:
+        for t, n in calls:
+            g.step_host(st, t, w.dt, n)
+    for x, y in zip(ref[0], st):
+        assert (x is None and y is None) or np.array_equal(x, y)
+    # new drivers between replays of one captured graph
+    d2 = w.atmos.copy()
+    d2[A.CLM_AT_T_AIR] += 3.0
+    with SoilColumns(w, graph=1) as g, SoilColumns(w, graph=0) as g0:
+        for h in (g, g0):
+            h.step(w.t0, w.dt, 2)
+            h.set_atmos(d2)
+            h.step(w.t0 + 2 * w.dt, w.dt, 2)
+        for x, y in zip(g.get_state(), g0.get_state()):
+            assert (x is None and y is None) or np.array_equal(x, y)
