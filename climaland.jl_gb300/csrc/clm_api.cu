@@ -26,10 +26,10 @@ size_t step_smem_bytes(int model, int precision, int nmax, int wpc);
 cudaError_t step_grid(int model, int precision, int cm, int nmax, int wpc, int ntiles, int* grid);
 size_t step_scratch_doubles(int model, int precision, int nmax, int wpc, int grid);
 // clm_layout.cu
-cudaError_t ref_to_internal(const Layout& L, const double* src, double* dst, cudaStream_t st,
-                            int tile0 = 0, int ntl = -1);
-cudaError_t internal_to_ref(const Layout& L, const double* src, double* dst, cudaStream_t st,
-                            int tile0 = 0, int ntl = -1);
+cudaError_t ref_to_internal(const Layout& L, const XFields& F, cudaStream_t st, int tile0 = 0,
+                            int ntl = -1);
+cudaError_t internal_to_ref(const Layout& L, const XFields& F, cudaStream_t st, int tile0 = 0,
+                            int ntl = -1);
 cudaError_t cols_to_sorted(const Layout& L, const double* src, double* dst, cudaStream_t st);
 cudaError_t cols_to_orig(const Layout& L, const double* src, double* dst, cudaStream_t st);
 // clm_budget.cu
@@ -435,11 +435,15 @@ int set_state_impl(clm_handle* h, const double* v, const double* ti, const doubl
   const size_t nb = sizeof(double) * h->ncells_ref;
   const double* src[3] = {v, ti, e};
   double* dst[3] = {h->d_v, h->d_ti, h->d_e};
-  for (int i = 0; i < (eh ? 3 : 1); ++i) {
+  XFields F{};
+  F.nf = eh ? 3 : 1;
+  for (int i = 0; i < F.nf; ++i) {
     double* stg = h->d_stage + (size_t)i * h->ncells_ref;
     CLM_CUDA(h, cudaMemcpyAsync(stg, src[i], nb, kind, st));
-    CLM_CUDA(h, ref_to_internal(L, stg, dst[i], st));
+    F.src[i] = stg;
+    F.dst[i] = dst[i];
   }
+  CLM_CUDA(h, ref_to_internal(L, F, st));
   const double* cs[2] = {Fw, Fe};
   double* cd[2] = {h->d_Fw, h->d_Fe};
   for (int i = 0; i < (eh ? 2 : 1); ++i) {
@@ -461,12 +465,16 @@ int get_state_impl(clm_handle* h, double* v, double* ti, double* e, double* Fw, 
   const size_t nb = sizeof(double) * h->ncells_ref;
   double* outs[3] = {v, ti, e};
   const double* srcs[3] = {h->d_v, h->d_ti, h->d_e};
+  XFields F{};
   for (int i = 0; i < (eh ? 3 : 1); ++i) {
     if (!outs[i]) continue;
-    double* stg = h->d_stage + (size_t)i * h->ncells_ref;
-    CLM_CUDA(h, internal_to_ref(L, srcs[i], stg, st));
-    CLM_CUDA(h, cudaMemcpyAsync(outs[i], stg, nb, kind, st));
+    F.src[F.nf] = srcs[i];
+    F.dst[F.nf++] = h->d_stage + (size_t)i * h->ncells_ref;
   }
+  if (F.nf > 0) CLM_CUDA(h, internal_to_ref(L, F, st));
+  for (int i = 0; i < (eh ? 3 : 1); ++i)
+    if (outs[i])
+      CLM_CUDA(h, cudaMemcpyAsync(outs[i], h->d_stage + (size_t)i * h->ncells_ref, nb, kind, st));
   double* co[2] = {Fw, Fe};
   const double* cs[2] = {h->d_Fw, h->d_Fe};
   for (int i = 0; i < (eh ? 2 : 1); ++i) {
@@ -973,8 +981,14 @@ int clm_step_host(clm_handle* h, double* v, double* ti, double* e, double* Fw, d
     // transpose, step, transpose back on the handle's stream (step kernels
     // share the per-warp scratch, so they stay in one stream)
     CLM_CUDA(h, cudaStreamWaitEvent(h->stream, ev_in, 0));
-    for (int f = 0; f < nf; ++f)
-      CLM_CUDA(h, ref_to_internal(L, h->d_stage + f * h->ncells_ref, df[f], h->stream, T0, T1 - T0));
+    XFields Fi{}, Fo{};
+    Fi.nf = Fo.nf = nf;
+    for (int f = 0; f < nf; ++f) {
+      Fi.src[f] = Fo.dst[f] = h->d_stage + f * h->ncells_ref;
+      Fi.dst[f] = df[f];
+      Fo.src[f] = df[f];
+    }
+    CLM_CUDA(h, ref_to_internal(L, Fi, h->stream, T0, T1 - T0));
     A.tile_begin = T0;
     A.tile_end = T1;
     for (int s0 = 0; s0 < nsteps; s0 += 64) {
@@ -984,8 +998,7 @@ int clm_step_host(clm_handle* h, double* v, double* ti, double* e, double* Fw, d
       CLM_CUDA(h, launch_step(A, h->cfg.model, h->cfg.precision, h->wpc, h->grid, h->d_scratch, clk,
                               std::min(64, nsteps - s0), h->stream));
     }
-    for (int f = 0; f < nf; ++f)
-      CLM_CUDA(h, internal_to_ref(L, df[f], h->d_stage + f * h->ncells_ref, h->stream, T0, T1 - T0));
+    CLM_CUDA(h, internal_to_ref(L, Fo, h->stream, T0, T1 - T0));
     CLM_CUDA(h, cudaEventRecord(ev_done, h->stream));
     // out
     CLM_CUDA(h, cudaStreamWaitEvent(h->copy_out, ev_done, 0));

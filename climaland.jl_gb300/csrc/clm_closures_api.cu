@@ -17,8 +17,8 @@
 struct clm_handle;
 
 namespace clm {
-cudaError_t internal_to_ref(const Layout& L, const double* src, double* dst, cudaStream_t st,
-                            int tile0 = 0, int ntl = -1);
+cudaError_t internal_to_ref(const Layout& L, const XFields& F, cudaStream_t st, int tile0 = 0,
+                            int ntl = -1);
 StepArgs handle_step_args(clm_handle* h);
 Layout handle_layout(clm_handle* h);
 int handle_ready(clm_handle* h);
@@ -67,11 +67,14 @@ int state_ref(clm_handle* h, Scratch& S, const double** v, const double** ti, co
   if (err != cudaSuccess) return handle_cuda_fail(h, err, "cudaMalloc");
   Layout L = handle_layout(h);
   cudaStream_t st = handle_stream(h);
-  CLM_CUDA(h, internal_to_ref(L, handle_state_ptr(h, 0), bv, st));
-  if (eh) {
-    CLM_CUDA(h, internal_to_ref(L, handle_state_ptr(h, 1), bt, st));
-    CLM_CUDA(h, internal_to_ref(L, handle_state_ptr(h, 2), be, st));
+  XFields F{};
+  F.nf = eh ? 3 : 1;
+  double* outs[3] = {bv, bt, be};
+  for (int i = 0; i < F.nf; ++i) {
+    F.src[i] = handle_state_ptr(h, i);
+    F.dst[i] = outs[i];
   }
+  CLM_CUDA(h, internal_to_ref(L, F, st));
   *v = bv;
   *ti = bt;
   *e = be;

@@ -33,6 +33,14 @@ struct Layout {
   const int64_t* slot_ref;  // [stride]  first cell of the slot's column in the reference layout (0: padding)
 };
 
+// Up to three state fields converted by one layout-transpose launch.
+constexpr int kXposeMaxFields = 3;
+struct XFields {
+  const double* src[kXposeMaxFields];
+  double* dst[kXposeMaxFields];
+  int nf;
+};
+
 struct StepArgs {
   Layout L;
   const double* z_lo;   // [stride]
