@@ -30,6 +30,9 @@ def _workload(name):
         return WL.full_scale_c4(ncol=96, seed=5)
     if name == "uneven":
         return WL.uneven_c2(ncol=262144, seed=2).subset(120)
+    if name == "atmos_topmodel":  # per-column drivers and TOPMODEL rows travel with the shard
+        from climaland_gb300 import _abi as A
+        return WL.with_atmos(WL.full_scale_c4(ncol=96, seed=5), runoff=A.CLM_RUNOFF_TOPMODEL)
     return WL.richards_c0(ncol=64, seed=1)
 
 
@@ -95,7 +98,8 @@ def test_partition_is_contiguous_and_balanced():
         S.partition(np.ones(3), 4)
 
 
-@pytest.mark.parametrize("name,world", [("full_scale", 2), ("uneven", 3), ("richards", 2)])
+@pytest.mark.parametrize("name,world", [("full_scale", 2), ("uneven", 3), ("richards", 2),
+                                        ("atmos_topmodel", 2)])
 def test_sharded_run_equals_unsharded(name, world):
     _paths()
     import oracle as O
