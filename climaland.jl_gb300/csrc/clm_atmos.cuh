@@ -26,9 +26,11 @@
 //   radiation          R_n = -(1 - alpha) SW_d - eps (LW_d - sigma T^4), the
 //                      CLM two-band albedo over the top layers
 //                      (soil_albedo.jl:146-198);
-//   top fluxes         water P_liq + E_liq, energy R_n + LHF + SHF +
-//                      P_liq rho e_liq(T_air) (NoRunoff); the sublimation
-//                      part of E leaves theta_i (SoilSublimation, :931-947).
+//   top fluxes         water I + E_liq, energy R_n + LHF + SHF +
+//                      I rho e_liq(T_air), I the infiltrating part of P_liq
+//                      after the runoff model (eh_runoff below); the
+//                      sublimation part of E leaves theta_i (SoilSublimation,
+//                      :931-947).
 //
 // SurfaceFluxes.jl and Thermodynamics.jl are not among the reference
 // sources; the saturation humidity and the similarity solve restate the

@@ -199,7 +199,8 @@ cfg.bc_top_heat = CLM_BC_ATMOS`) as a (CLM_AT_NFIELDS × ncol) matrix, rows in
 `PrescribedRadiativeFluxes`, `p.drivers.P_liq, T, u, q, P, SW_d, LW_d`,
 `atmos.h`, `atmos.gustiness`, then the soil's albedo parameters,
 emissivity, z_0m, z_0b, d_ds, evap_p, evap_α. Call after each
-`update_drivers!`; `nothing` removes them.
+`update_drivers!`; `nothing` removes them. The BC's runoff model is `cfg.runoff` (CLM_RUNOFF_*; TOPMODEL
+also needs the f_max, f_over, R_sb parameter rows).
 """
 function set_atmos!(h::Handle, d::Union{Nothing, Matrix{Float64}}; params = atmos_params_default())
     d === nothing && return check(h, ccall((:clm_set_atmos, libclm), Cint,
