@@ -28,6 +28,9 @@ const CLM_BC_STATE = Int32(2)
 const CLM_BC_FLUX_ADVECTIVE = Int32(3)
 const CLM_BC_PRECIP_RUNOFF = Int32(4)
 const CLM_BC_ATMOS = Int32(5)
+const CLM_RUNOFF_NONE = Int32(0)
+const CLM_RUNOFF_SURFACE = Int32(1)
+const CLM_RUNOFF_TOPMODEL = Int32(2)
 const CLM_CM_VAN_GENUCHTEN = Int32(0)
 const CLM_CM_BROOKS_COREY = Int32(1)
 const CLM_F_NFIELDS = 8
