@@ -139,6 +139,25 @@ __device__ void closure_column(const ClosureArgs& C, const Tables& Tb) {
     Ftw = ab.top_w;
     Fth = ab.top_h;
   }
+  // RichardsAtmosDrivenFluxBC: the runoff model turns the precipitation into
+  // the infiltration; TOPMODEL's implicit subsurface sink (Runoff.jl:129-148,
+  // 234-270, 321-345, infiltration capacity -K_sat :386-389)
+  if (!eh && A.bc_tw == CLM_BC_PRECIP_RUNOFF && A.runoff != CLM_RUNOFF_NONE) {
+    const double ic = -1.0 * K_sat;
+    if (A.runoff == CLM_RUNOFF_SURFACE) {
+      const double is_sat = ((C.v[o + n - 1] + 0.0) - nu) > kEps ? 1.0 : 0.0;
+      Ftw = (1.0 - is_sat) * fmax(ic, ftw);
+    } else {
+      const double nr = nu - theta_r;
+      double h = 0.0;
+      for (int k = 0; k < n; ++k) h += G.width(k) * sat_weight(C.v[o + k] + 0.0 - theta_r, nr);
+      const double zwt = (G.zhi - G.zlo) - h;
+      const double f_sat = fmin(P[CLM_P_F_MAX * st + s] * fm::exp(Tb, -P[CLM_P_F_OVER * st + s] / 2.0 * zwt), 1.0);
+      Ftw = (1.0 - f_sat) * fmax(ic, ftw);
+      ro.R_ss = P[CLM_P_R_SB * st + s] * fm::exp(Tb, -P[CLM_P_F_OVER * st + s] * zwt);
+      ro.cw = ro.R_ss / fmax(h, kEps);
+    }
+  }
   if (KIND == CL_ATM) {
     if (atmos && C.atm_out) {
       const double vals[CLM_AF_NFIELDS] = {ab.lhf, ab.shf, ab.vliq, ab.vice, ab.R_n, ab.q_sfc, ab.top_w, ab.top_h};

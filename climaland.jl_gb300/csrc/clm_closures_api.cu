@@ -89,16 +89,7 @@ ClosureArgs base_args(clm_handle* h) {
   return C;
 }
 
-// The closures evaluate the boundary fluxes without a runoff model: the
-// precipitation-driven top boundary is available through clm_step only.
-int closure_ready(clm_handle* h) {
-  const int rc = handle_ready(h);
-  if (rc != CLM_OK) return rc;
-  if (handle_step_args(h).bc_tw == CLM_BC_PRECIP_RUNOFF)
-    return handle_fail(h, CLM_ERR_UNSUPPORTED,
-                       "closure entry points do not evaluate the runoff boundary condition");
-  return CLM_OK;
-}
+int closure_ready(clm_handle* h) { return handle_ready(h); }
 
 int copy_out(clm_handle* h, double* host, const double* dev, size_t n) {
   if (!host) return CLM_OK;

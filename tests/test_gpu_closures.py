@@ -38,6 +38,8 @@ WORKLOADS = {
     "c4_atmos": lambda: WL.with_atmos(WL.full_scale_c4(ncol=256)),
     "uneven_atmos_bc": lambda: WL.with_atmos(WL.brooks_corey(WL.uneven_c2(ncol=256))),
     "c4_atmos_topmodel": lambda: WL.with_atmos(WL.full_scale_c4(ncol=256), runoff=A.CLM_RUNOFF_TOPMODEL),
+    "richards_topmodel": lambda: WL.richards_runoff(ncol=256),
+    "richards_surface_runoff": lambda: WL.richards_runoff(ncol=256, runoff=A.CLM_RUNOFF_SURFACE),
     "c4_atmos_surface_runoff": lambda: WL.with_atmos(WL.full_scale_c4(ncol=256), runoff=A.CLM_RUNOFF_SURFACE),
 }
 

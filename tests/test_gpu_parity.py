@@ -257,14 +257,6 @@ def test_richards_precipitation_runoff(kind):
     report(f"richards_runoff_{kind}", check_parity(w, 48))
 
 
-def test_runoff_handles_refuse_closures():
-    w = WL.richards_runoff(ncol=64)
-    with D.SoilColumns(w) as g:
-        with pytest.raises(D.ClmError) as e:
-            g.update_aux(w.t0)
-        assert e.value.code == A.CLM_ERR_UNSUPPORTED
-
-
 def test_richards_tolerance_mode():
     w = WL.richards_c0(ncol=512)
     st = check_parity(w, 48, oracle_cfg=TOL_MODE, **TOL_MODE)
