@@ -848,9 +848,11 @@ int clm_set_atmos(clm_handle* h, const clm_atmos_params* prm, const double* d, i
     CLM_CUDA(h, cudaMalloc(&h->d_atm, sizeof(double) * h->stride * CLM_AT_NFIELDS));
     CLM_CUDA(h, cudaMemsetAsync(h->d_atm, 0, sizeof(double) * h->stride * CLM_AT_NFIELDS, h->stream));
   }
-  // graphs hold StepArgs (with the constants) by value
-  drop_graphs(h);
-  h->ak = make_atmos_k(a, h->cfg.earth);
+  // graphs hold StepArgs (with the constants) by value: new constants need
+  // new graphs, new drivers in the same buffer do not
+  const AtmosK ak = make_atmos_k(a, h->cfg.earth);
+  if (std::memcmp(&ak, &h->ak, sizeof ak) != 0) drop_graphs(h);
+  h->ak = ak;
   int rc = upload_cols_sorted(h, d, h->d_atm, nfields);
   if (rc != CLM_OK) return rc;
   CLM_CUDA(h, cudaStreamSynchronize(h->stream));

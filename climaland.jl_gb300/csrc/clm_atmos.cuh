@@ -58,7 +58,7 @@ struct AtmosK {
 };
 
 inline AtmosK make_atmos_k(const clm_atmos_params& a, const clm_earth_params& e) {
-  AtmosK K;
+  AtmosK K{};  // zeroed padding: handles compare the bytes
   K.stefan = a.stefan;
   K.D_vapor = a.D_vapor;
   K.LH_v0 = a.LH_v0;
