@@ -1,7 +1,10 @@
 """Benchmark of the fused soil column step on GB300.
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                [--config c4] [--precision fp64|mixed] [--ncol NCOL]
+                [--config c4] [--precision fp64|mixed] [--ncol NCOL] [--top flux|atmos]
+
+--top atmos runs the same columns under the atmosphere-driven top boundary
+(turbulent fluxes, radiation, sublimation) with seeded per-column drivers.
 
 Workload (default): the full-scale EnergyHydrology configuration,
 1,048,576 columns x 20 layers (depth 1-5 m, diurnal heat flux, rain pulses,
@@ -19,6 +22,8 @@ Prints one JSON line (rank 0). Metric: column-steps/s.
   roofline  dominant kernel (the step kernel) against the measured HBM peak
   compute_bound  the FP64 pipe's busy fraction for that kernel (committed ncu capture)
   cpu_baseline  the FP64 CPU oracle on a bounded sample, all host threads
+  forms     mixed precision, uneven columns, learned guess and the
+            atmosphere-driven boundary on 262,144-column subsets
 """
 from __future__ import annotations
 
