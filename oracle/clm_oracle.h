@@ -9,6 +9,14 @@
  *
  * Layout: same as include/climaland_cuda.h (cell = offsets[c] + k, k = 0 the
  * bottom layer; per-column parameters and forcing as SoA rows of ncol).
+ *
+ * Pinning: the closures, tendencies, Jacobians and boundary conditions are
+ * pinned by the reference's own known-answer tests (tests/
+ * test_oracle_known_answers.py). The atmosphere-driven boundary's turbulent
+ * fluxes and saturation humidity come from SurfaceFluxes.jl and
+ * Thermodynamics.jl, which are not among the reference sources: they are
+ * restated from the published formulations, and their parity is unpinned
+ * (only the reference's identities around them are checked).
  */
 #ifndef CLM_ORACLE_H
 #define CLM_ORACLE_H
