@@ -897,3 +897,10 @@ def test_energy_hydrology_runoff_under_the_atmos_boundary(L):
             assert approx(imp[4][c], -(top_h - bot_h) - R_ess, rtol=1e-12, atol=1e-9)
         if runoff == A.CLM_RUNOFF_TOPMODEL:
             assert (w.vartheta_l > w.params[A.CLM_P_NU][np.repeat(np.arange(w.ncol), n)]).any()
+
+
+def test_atmos_defaults_agree(L):
+    """The oracle's clm_atmos_params defaults are the library's (Python twin)."""
+    a = _atm(L)
+    for k, v in A.DEFAULT_ATMOS.items():
+        assert getattr(a, k) == v, k
