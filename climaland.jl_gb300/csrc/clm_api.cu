@@ -489,6 +489,49 @@ int get_state_impl(clm_handle* h, double* v, double* ti, double* e, double* Fw, 
 
 }  // namespace
 
+namespace clm {
+
+// The configuration checks shared by clm_create and clm_step_eh_noalloc
+// (sizes are checked by each): enums in range, the Newton settings, and the
+// boundary kinds each slot and model admit.
+int check_config(const clm_config* cfg) {
+  if (!cfg) return CLM_ERR_ARG;
+  if (cfg->model != CLM_MODEL_RICHARDS && cfg->model != CLM_MODEL_ENERGY_HYDROLOGY) return CLM_ERR_ARG;
+  if (cfg->max_iters < 1 || cfg->max_iters > 1000) return CLM_ERR_ARG;
+  if (cfg->precision != CLM_PREC_FP64 && cfg->precision != CLM_PREC_MIXED) return CLM_ERR_ARG;
+  if (cfg->learned_guess && (cfg->model != CLM_MODEL_ENERGY_HYDROLOGY || cfg->newton_mode != CLM_NEWTON_TOL))
+    return CLM_ERR_ARG;  // the guess only changes where tolerance-mode Newton starts
+  if (cfg->newton_mode != CLM_NEWTON_FIXED && cfg->newton_mode != CLM_NEWTON_TOL) return CLM_ERR_ARG;
+  if (cfg->schedule != CLM_SCHED_STATIC && cfg->schedule != CLM_SCHED_DYNAMIC) return CLM_ERR_ARG;
+  if (cfg->graph != 0 && cfg->graph != 1) return CLM_ERR_ARG;
+  if (cfg->cols_per_cta < 0) return CLM_ERR_ARG;
+  if (cfg->hydrology_cm != CLM_CM_VAN_GENUCHTEN && cfg->hydrology_cm != CLM_CM_BROOKS_COREY)
+    return CLM_ERR_ARG;
+  const int kinds[4] = {cfg->bc_top_water, cfg->bc_top_heat, cfg->bc_bottom_water, cfg->bc_bottom_heat};
+  for (int i = 0; i < 4; ++i) {
+    const int k = kinds[i];
+    const bool runoff_top = (i == 0 && k == CLM_BC_PRECIP_RUNOFF);
+    const bool atmos_top = (i < 2 && k == CLM_BC_ATMOS);
+    if (!runoff_top && !atmos_top && (k < CLM_BC_FLUX || k > CLM_BC_FLUX_ADVECTIVE)) return CLM_ERR_ARG;
+  }
+  if (cfg->bc_top_water == CLM_BC_PRECIP_RUNOFF &&
+      (cfg->model != CLM_MODEL_RICHARDS || cfg->runoff < CLM_RUNOFF_NONE || cfg->runoff > CLM_RUNOFF_TOPMODEL))
+    return CLM_ERR_ARG;
+  // AtmosDrivenFluxBC sets both top fluxes of EnergyHydrology
+  if ((cfg->bc_top_water == CLM_BC_ATMOS) != (cfg->bc_top_heat == CLM_BC_ATMOS)) return CLM_ERR_ARG;
+  if (cfg->bc_top_water == CLM_BC_ATMOS &&
+      (cfg->model != CLM_MODEL_ENERGY_HYDROLOGY || cfg->runoff < CLM_RUNOFF_NONE ||
+       cfg->runoff > CLM_RUNOFF_TOPMODEL))
+    return CLM_ERR_ARG;
+  if (cfg->bc_top_water == CLM_BC_FREE_DRAINAGE || cfg->bc_top_water == CLM_BC_FLUX_ADVECTIVE ||
+      cfg->bc_bottom_water == CLM_BC_FLUX_ADVECTIVE || cfg->bc_top_heat == CLM_BC_FREE_DRAINAGE ||
+      cfg->bc_bottom_heat == CLM_BC_FLUX_ADVECTIVE)
+    return CLM_ERR_ARG;
+  return CLM_OK;
+}
+
+}  // namespace clm
+
 extern "C" {
 
 const char* clm_version(void) { return "libclimaland_cuda 0.1 (sm_103a)"; }
@@ -529,39 +572,8 @@ void clm_config_default(clm_config* c) {
 int clm_create(const clm_config* cfg, clm_handle** out) {
   if (!cfg || !out) return CLM_ERR_ARG;
   *out = nullptr;
-  if (cfg->model != CLM_MODEL_RICHARDS && cfg->model != CLM_MODEL_ENERGY_HYDROLOGY) return CLM_ERR_ARG;
-  if (cfg->ncol <= 0 || cfg->nlayers < 0 || cfg->nlayers > kMaxLayers || cfg->max_iters < 1 ||
-      cfg->max_iters > 1000)
-    return CLM_ERR_ARG;
-  if (cfg->precision != CLM_PREC_FP64 && cfg->precision != CLM_PREC_MIXED) return CLM_ERR_ARG;
-  if (cfg->learned_guess && (cfg->model != CLM_MODEL_ENERGY_HYDROLOGY || cfg->newton_mode != CLM_NEWTON_TOL))
-    return CLM_ERR_ARG;  // the guess only changes where tolerance-mode Newton starts
-  if (cfg->newton_mode != CLM_NEWTON_FIXED && cfg->newton_mode != CLM_NEWTON_TOL) return CLM_ERR_ARG;
-  if (cfg->schedule != CLM_SCHED_STATIC && cfg->schedule != CLM_SCHED_DYNAMIC) return CLM_ERR_ARG;
-  if (cfg->graph != 0 && cfg->graph != 1) return CLM_ERR_ARG;
-  if (cfg->cols_per_cta < 0) return CLM_ERR_ARG;
-  if (cfg->hydrology_cm != CLM_CM_VAN_GENUCHTEN && cfg->hydrology_cm != CLM_CM_BROOKS_COREY)
-    return CLM_ERR_ARG;
-  const int kinds[4] = {cfg->bc_top_water, cfg->bc_top_heat, cfg->bc_bottom_water, cfg->bc_bottom_heat};
-  for (int i = 0; i < 4; ++i) {
-    const int k = kinds[i];
-    const bool runoff_top = (i == 0 && k == CLM_BC_PRECIP_RUNOFF);
-    const bool atmos_top = (i < 2 && k == CLM_BC_ATMOS);
-    if (!runoff_top && !atmos_top && (k < CLM_BC_FLUX || k > CLM_BC_FLUX_ADVECTIVE)) return CLM_ERR_ARG;
-  }
-  if (cfg->bc_top_water == CLM_BC_PRECIP_RUNOFF &&
-      (cfg->model != CLM_MODEL_RICHARDS || cfg->runoff < CLM_RUNOFF_NONE || cfg->runoff > CLM_RUNOFF_TOPMODEL))
-    return CLM_ERR_ARG;
-  // AtmosDrivenFluxBC sets both top fluxes of EnergyHydrology
-  if ((cfg->bc_top_water == CLM_BC_ATMOS) != (cfg->bc_top_heat == CLM_BC_ATMOS)) return CLM_ERR_ARG;
-  if (cfg->bc_top_water == CLM_BC_ATMOS &&
-      (cfg->model != CLM_MODEL_ENERGY_HYDROLOGY || cfg->runoff < CLM_RUNOFF_NONE ||
-       cfg->runoff > CLM_RUNOFF_TOPMODEL))
-    return CLM_ERR_ARG;
-  if (cfg->bc_top_water == CLM_BC_FREE_DRAINAGE || cfg->bc_top_water == CLM_BC_FLUX_ADVECTIVE ||
-      cfg->bc_bottom_water == CLM_BC_FLUX_ADVECTIVE || cfg->bc_top_heat == CLM_BC_FREE_DRAINAGE ||
-      cfg->bc_bottom_heat == CLM_BC_FLUX_ADVECTIVE)
-    return CLM_ERR_ARG;
+  if (check_config(cfg) != CLM_OK) return CLM_ERR_ARG;
+  if (cfg->ncol <= 0 || cfg->nlayers < 0 || cfg->nlayers > kMaxLayers) return CLM_ERR_ARG;
   clm_handle* h = new (std::nothrow) clm_handle();
   if (!h) return CLM_ERR_ARG;
   h->cfg = *cfg;

@@ -110,6 +110,10 @@ __device__ __forceinline__ void release_tiles(int* ctr, int nwarps) {
 }
 #endif
 
+// clm_api.cu: the configuration checks of clm_create (CLM_OK or CLM_ERR_ARG),
+// shared with the allocation-free entry point.
+int check_config(const clm_config* cfg);
+
 // Shared-memory view of one warp's column tile: array a, layer k.
 template <typename T>
 struct Tile {

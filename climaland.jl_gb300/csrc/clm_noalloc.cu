@@ -22,10 +22,16 @@
 //    cleared between calls;
 //  * the first call on each device looks up the array's device address
 //    (cudaGetSymbolAddress) and configures the kernel; make that first call
-//    before capturing the stream into a CUDA graph.
+//    before capturing the stream into a CUDA graph. Later calls repeat the
+//    lookup and redo the configuration when the address has changed (a new
+//    primary context after cudaDeviceReset);
+//  * the parameter rows are device memory and are not validated: they must
+//    satisfy clm_set_params' constraints (nu > theta_r >= 0, K_sat > 0, ...);
+//    a column whose state becomes non-finite is flagged CLM_COL_NONFINITE.
 
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <mutex>
 
 #include "../../include/climaland_cuda.h"
@@ -102,12 +108,15 @@ __global__ void __launch_bounds__(32, 1)
 int setup_device(int dev, DeviceSetup* out) {
   std::lock_guard<std::mutex> lock(g_setup_mu);
   DeviceSetup& s = g_setup[dev];
-  if (s.scratch == nullptr) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess) {
-      cudaGetLastError();
-      return CLM_ERR_CUDA;
-    }
+  // the array's address in the current context: a context created after a
+  // cudaDeviceReset places it anew and has lost the kernel attributes, so a
+  // changed address repeats the set-up (the lookup allocates nothing)
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess) {
+    cudaGetLastError();
+    return CLM_ERR_CUDA;
+  }
+  if (s.scratch != static_cast<double*>(p)) {
     const size_t smem = noalloc_smem(kNoAllocMaxLayers);
     int nsm = 0, per_vg = 0, per_bc = 0;
     if (cudaFuncSetAttribute(eh_step_noalloc_kernel<VG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -142,17 +151,18 @@ extern "C" int clm_step_eh_noalloc(const clm_config* cfg, int32_t ncol, int32_t 
                                    double* theta_i, double* rho_e_int, double* intF_w,
                                    double* intF_e, uint32_t* flags, double t, double dt,
                                    int32_t nsteps, void* cuda_stream) {
-  if (!cfg || cfg->model != CLM_MODEL_ENERGY_HYDROLOGY || cfg->precision != CLM_PREC_FP64)
+  // the checks of clm_create (enums, Newton settings, which boundary kind
+  // each slot admits), then what this entry point does not carry: the mixed
+  // path, the learned guess and the boundaries and sources that need
+  // handle-owned driver arrays
+  if (!cfg || check_config(cfg) != CLM_OK) return CLM_ERR_ARG;
+  if (cfg->model != CLM_MODEL_ENERGY_HYDROLOGY || cfg->precision != CLM_PREC_FP64 || cfg->learned_guess)
     return CLM_ERR_ARG;
+  if (cfg->bc_top_water == CLM_BC_ATMOS || cfg->bc_top_water == CLM_BC_PRECIP_RUNOFF) return CLM_ERR_ARG;
   if (ncol <= 0 || nlayers < 2 || nlayers > kNoAllocMaxLayers) return CLM_ERR_ARG;
   if (!z_lo || !z_hi || !params || !vartheta_l || !theta_i || !rho_e_int || !intF_w || !intF_e)
     return CLM_ERR_ARG;
-  if (!(dt > 0) || nsteps < 0 || cfg->max_iters < 1) return CLM_ERR_ARG;
-  if (cfg->hydrology_cm != CLM_CM_VAN_GENUCHTEN && cfg->hydrology_cm != CLM_CM_BROOKS_COREY)
-    return CLM_ERR_ARG;
-  const int kinds[4] = {cfg->bc_top_water, cfg->bc_top_heat, cfg->bc_bottom_water, cfg->bc_bottom_heat};
-  for (int k : kinds)
-    if (k < CLM_BC_FLUX || k > CLM_BC_FLUX_ADVECTIVE) return CLM_ERR_ARG;
+  if (!(dt > 0) || !std::isfinite(t) || nsteps < 0) return CLM_ERR_ARG;
   if (nsteps == 0) return CLM_OK;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) {

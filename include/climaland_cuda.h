@@ -574,12 +574,17 @@ int clm_mlp_set(clm_mlp* m, const void* blob, int64_t nbytes);
  * updated in place; flags (ncol, CLM_COL_*) may be NULL. forcing is a
  * host array of 4 device pointers, one per clm_bc_slot (CLM_F_NFIELDS rows
  * of ncol each, or NULL); forcing itself may be NULL. cfg (host memory)
- * supplies the model constants and must ask for EnergyHydrology in FP64.
- * Limits: 2 <= nlayers <= 32, the same for every column; otherwise
- * CLM_ERR_ARG. The kernel's working scratch is a fixed 24 MiB device array
- * inside the library, held by every GPU that loads it until the process
- * exits. All calls share it: calls that overlap on the GPU (other streams
- * or host threads) race. The first call on each device looks up that
+ * supplies the model constants and must ask for EnergyHydrology in FP64;
+ * it passes clm_create's configuration checks, and neither the learned
+ * guess nor the atmosphere-driven or precipitation/runoff top boundary is
+ * available here. Limits: 2 <= nlayers <= 32, the same for every column;
+ * otherwise CLM_ERR_ARG. The parameter rows are device memory and are not
+ * validated: they must satisfy clm_set_params' constraints (a column whose
+ * state turns non-finite gets CLM_COL_NONFINITE). The kernel's working
+ * scratch is a fixed 24 MiB device array inside the library, held by every
+ * GPU that loads it until the process exits. All calls share it: calls that
+ * overlap on the GPU (other streams or host threads) race. The first call
+ * on each device (and the first after a cudaDeviceReset) looks up that
  * array and configures the kernel, so make it before any stream capture.
  * Runs asynchronously on cuda_stream (a cudaStream_t, NULL for the legacy
  * default stream). */

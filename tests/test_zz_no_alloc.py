@@ -37,12 +37,20 @@ def _workload(brooks_corey=False):
     return WL.brooks_corey(w) if brooks_corey else w
 
 
-@pytest.mark.parametrize("brooks_corey", [False, True])
-def test_noalloc_matches_handle_path_two_calls(torch_cuda, brooks_corey):
+@pytest.mark.parametrize("case", ["van_genuchten", "brooks_corey", "deepest_widest"])
+def test_noalloc_matches_handle_path_two_calls(torch_cuda, case):
     torch = torch_cuda
     lib = D.load_library()
-    w = _workload(brooks_corey)
     nsteps = 6
+    if case == "deepest_widest":
+        # the documented maximum depth (32 layers: the largest shared-memory
+        # request) on enough columns that the grid reaches the 1024-slot cap
+        # of the fixed scratch array, so the last slot's scratch is used
+        w = WL.energy_hydrology_c1(ncol=40000, nlayers=32, seed=11)
+        w.params[A.CLM_P_K_SAT] = np.minimum(w.params[A.CLM_P_K_SAT], 1e-5)
+        nsteps = 2
+    else:
+        w = _workload(case == "brooks_corey")
     # reference: the handle API, two calls
     with D.SoilColumns(w) as g:
         g.step(w.t0, w.dt, nsteps)
@@ -100,8 +108,39 @@ def test_noalloc_rejects_sizes_beyond_its_maximum(torch_cuda):
         rc = lib.clm_step_eh_noalloc(ctypes.byref(w.cfg), w.ncol, nl, null, null, null, null,
                                      null, null, null, null, null, null, 0.0, w.dt, 1, null)
         assert rc == A.CLM_ERR_ARG
+
+
+# configurations clm_create refuses (a boundary kind in a slot that does not
+# admit it, Newton settings out of range; create=True) and the options this
+# entry point does not carry (mixed path, learned guess, RichardsModel)
+REFUSED = [
+    ("bc_top_water", A.CLM_BC_FREE_DRAINAGE, True),
+    ("bc_top_heat", A.CLM_BC_FREE_DRAINAGE, True),
+    ("bc_top_water", A.CLM_BC_FLUX_ADVECTIVE, True),
+    ("bc_bottom_water", A.CLM_BC_FLUX_ADVECTIVE, True),
+    ("bc_bottom_heat", A.CLM_BC_FLUX_ADVECTIVE, True),
+    ("bc_top_water", A.CLM_BC_PRECIP_RUNOFF, True),
+    ("newton_mode", 7, True),
+    ("max_iters", 0, True),
+    ("max_iters", 1001, True),
+    ("hydrology_cm", 5, True),
+    ("precision", A.CLM_PREC_MIXED, False),
+    ("learned_guess", 1, False),
+    ("model", A.CLM_MODEL_RICHARDS, False),
+]
+
+
+@pytest.mark.parametrize("field,value,create", REFUSED)
+def test_noalloc_rejects_configurations_clm_create_rejects(torch_cuda, field, value, create):
+    lib = D.load_library()
+    w = _workload()
+    null = None
     cfg = A.ClmConfig.from_buffer_copy(w.cfg)
-    cfg.precision = A.CLM_PREC_MIXED
+    setattr(cfg, field, value)
     rc = lib.clm_step_eh_noalloc(ctypes.byref(cfg), w.ncol, 15, null, null, null, null,
                                  null, null, null, null, null, null, 0.0, w.dt, 1, null)
     assert rc == A.CLM_ERR_ARG
+    if create:  # the handle API refuses the same configuration
+        h = A._H()
+        assert lib.clm_create(ctypes.byref(cfg), ctypes.byref(h)) == A.CLM_ERR_ARG
+        assert not h.value
