@@ -280,6 +280,7 @@ SIGNATURES = [
     ("clm_destroy", None, [_H]),
     ("clm_last_error", ctypes.c_char_p, [_H]),
     ("clm_set_geometry", ctypes.c_int, [_H, _DP, _DP, _IP]),
+    ("clm_set_faces", ctypes.c_int, [_H, _DP]),
     ("clm_set_params", ctypes.c_int, [_H, _DP, ctypes.c_int32]),
     ("clm_set_root_extraction", ctypes.c_int, [_H, _DP, ctypes.c_int32]),
     ("clm_atmos_params_default", None, [ctypes.POINTER(ClmAtmosParams)]),

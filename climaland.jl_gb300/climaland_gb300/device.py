@@ -84,6 +84,8 @@ class SoilColumns:
         self.h = h
         self._check(self.lib.clm_set_geometry(self.h, A.dptr(_c(w.z_lo)), A.dptr(_c(w.z_hi)),
                                               A.iptr(_c(w.offsets, np.int32))))
+        if getattr(w, "z_faces", None) is not None:  # stretched columns
+            self._check(self.lib.clm_set_faces(self.h, A.dptr(_c(w.z_faces))))
         prm = _c(w.params)
         self._check(self.lib.clm_set_params(self.h, A.dptr(prm), prm.shape[0]))
         for slot, f in w.forcing.items():

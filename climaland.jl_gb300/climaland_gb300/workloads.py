@@ -55,6 +55,9 @@ class Workload:
     # and its constants (ClmAtmosParams; None: the defaults), or None
     atmos: np.ndarray | None = None
     atmos_params: object = None
+    # face coordinates of stretched columns (ncells + ncol: column c's
+    # n + 1 faces at offsets[c] + c ...), or None for uniform layers
+    z_faces: np.ndarray | None = None
 
     @property
     def ncells(self) -> int:
@@ -102,7 +105,8 @@ class Workload:
             nsteps=self.nsteps, meta=dict(self.meta),
             root=None if self.root is None else np.ascontiguousarray(self.root[:, c0:c1]),
             atmos=None if self.atmos is None else np.ascontiguousarray(self.atmos[:, c0:c1]),
-            atmos_params=self.atmos_params)
+            atmos_params=self.atmos_params,
+            z_faces=None if self.z_faces is None else self.z_faces[a + c0: b + c1].copy())
 
 
 def _forcing(ncol: int) -> np.ndarray:
@@ -429,7 +433,8 @@ def brooks_corey(w: Workload, seed: int = 0) -> Workload:
         rho_e_int=e, intF_w=w.intF_w.copy(),
         intF_e=None if w.intF_e is None else w.intF_e.copy(), t0=w.t0, dt=w.dt,
         nsteps=w.nsteps, meta=dict(w.meta), root=None if w.root is None else w.root.copy(),
-        atmos=None if w.atmos is None else w.atmos.copy(), atmos_params=w.atmos_params)
+        atmos=None if w.atmos is None else w.atmos.copy(), atmos_params=w.atmos_params,
+        z_faces=None if w.z_faces is None else w.z_faces.copy())
 
 
 def with_root_extraction(w: Workload, seed: int = 0) -> Workload:
@@ -549,6 +554,170 @@ def with_atmos(w: Workload, seed: int = 0, runoff: int = A.CLM_RUNOFF_NONE) -> W
     out.forcing = {k: v for k, v in out.forcing.items()
                    if k not in (A.CLM_BC_TOP_WATER, A.CLM_BC_TOP_HEAT)}
     out.atmos = d
+    return out
+
+
+def generalized_exponential_faces(z_lo: float, z_hi: float, n: int, dz_bottom: float,
+                                  dz_top: float) -> np.ndarray:
+    """n + 1 face coordinates from z_lo to z_hi with a bottom layer of
+    dz_bottom and a top layer of dz_top: a restatement of ClimaCore's
+    GeneralizedExponentialStretching in the reverse mode that ClimaLand's
+    Column and global domains use (src/shared_utilities/Domains.jl:198-207),
+    i.e. measured from the surface down. With eta = j / n and the
+    exponential map sigma(eta; h) = -h log(1 - (1 - exp(-1/h)) eta), the
+    scale height h varies linearly in eta from h_s (fitted so that the first
+    layer below the surface is dz_top) at eta = 1/n to h_d (fitted so that
+    the deepest layer is dz_bottom) at eta = (n - 1)/n; face j lies at depth
+    (z_hi - z_lo) sigma(eta_j; h(eta_j)). The library takes whatever faces
+    the caller's mesh has, so this generator only shapes synthetic inputs."""
+    depth = z_hi - z_lo
+    a, b = dz_top / depth, dz_bottom / depth
+    if not (n >= 3 and a < 1.0 / n < b < 1.0):
+        raise ValueError("need dz_top < depth / n < dz_bottom < depth and n >= 3")
+
+    def sigma(eta, h):
+        return -h * np.log1p(-(-np.expm1(-1.0 / h)) * eta)
+
+    def fit(fn, target):  # fn increasing in log h; bisection over log h
+        lo, hi = -12.0, 12.0
+        for _ in range(200):
+            mid = 0.5 * (lo + hi)
+            if fn(np.exp(mid)) < target:
+                lo = mid
+            else:
+                hi = mid
+        return np.exp(0.5 * (lo + hi))
+
+    e1, en = 1.0 / n, (n - 1.0) / n
+    h_s = fit(lambda h: sigma(e1, h), a)
+    h_d = fit(lambda h: -(1.0 - sigma(en, h)), -b)
+    eta = np.arange(n + 1) / n
+    h = h_s + (h_d - h_s) * (eta - e1) / (en - e1)
+    zeta = np.empty(n + 1)
+    zeta[0] = 0.0
+    zeta[n] = 1.0
+    zeta[1:n] = sigma(eta[1:n], h[1:n])
+    faces = z_hi - depth * zeta[::-1]
+    faces[0], faces[n] = z_lo, z_hi
+    if not np.all(np.diff(faces) > 0):
+        raise ValueError("stretching does not give increasing faces")
+    return faces
+
+
+def stretched(w: Workload, dz_bottom_frac=(0.15, 0.3), dz_top_frac=(0.01, 0.04),
+              dz_top_min: float = 0.05, seed: int = 0) -> Workload:
+    """The workload on stretched columns: each column keeps its depth and
+    layer count, with generalized exponential faces whose top layer is
+    U[dz_top_frac] of the depth, at least dz_top_min metres (the reference's
+    global domain has 0.05 m at the top and 10 m at the bottom of 50 m), and
+    whose bottom layer is U[dz_bottom_frac] of it; a column too shallow for
+    such a top layer keeps uniform faces. Thinner layers make the reference
+    algorithm itself unstable at dt = 450 s: its explicit phase-change source
+    overshoots when dt exceeds twice the thermal time 3 rho c dz^2 / kappa
+    (about 6 minutes for a 1 cm layer), and three Newton iterations diverge on
+    millimetre layers. The state arrays are kept cell by cell."""
+    rng = np.random.Generator(np.random.PCG64(13000 + seed))
+    nl = w.nlayers
+    faces = np.empty(w.ncells + w.ncol)
+    for c in range(w.ncol):
+        n = int(nl[c])
+        depth = w.z_hi[c] - w.z_lo[c]
+        fb = rng.uniform(*dz_bottom_frac)
+        ft = rng.uniform(*dz_top_frac)
+        fb = max(fb, 1.5 / n)
+        ft = max(ft, dz_top_min / depth)
+        o = int(w.offsets[c]) + c
+        if ft < 0.5 / n:
+            faces[o: o + n + 1] = generalized_exponential_faces(w.z_lo[c], w.z_hi[c], n, fb * depth,
+                                                                ft * depth)
+        else:
+            faces[o: o + n + 1] = w.z_lo[c] + (w.z_hi[c] - w.z_lo[c]) * (np.arange(n + 1) / n)
+            faces[o + n] = w.z_hi[c]
+    out = w.columns(0, w.ncol, name=f"{w.name}_stretched")
+    out.z_faces = faces
+    return out
+
+
+def richards_benchmark(ncol: int = 65536, seed: int = 0) -> Workload:
+    """The geometry and solver settings of the reference's RichardsModel GPU
+    benchmark (experiments/benchmarks/richards.jl:64-137) on synthetic
+    columns: 15 layers over 50 m stretched with dz_tuple = (10.0, 0.1)
+    (global_domain, Domains.jl:1292-1298), RichardsModel{FT}(domain, forcing)
+    defaults (Soil.jl:339-365): RichardsAtmosDrivenFluxBC with
+    TOPMODELRunoff (f_over 3.28 1/m, R_sb 1.484e-7 m/s, f_max U[0.3, 0.7] in
+    place of the topmodel_fmax map), no-flux bottom, S_s = 1e-3; dt = 1800 s,
+    ARS111 with 2 Newton iterations, one week = 336 steps; the benchmark's
+    hydrostatic initial profile (vartheta_l = nu + S_s (z_grad - z) below
+    z_grad, van Genuchten saturation above) with the water table at
+    z_grad = zmin / 5 = -10 m (the benchmark's z_grad = zmin / 5 + (zmax - zmin)
+    / 2.5 = +10 m lies above the surface: every layer starts supersaturated,
+    z_wt = depth - h_sat is about -4 m and TOPMODEL's R_sb exp(-f_over z_wt)
+    drains ~0.3 m/s, after which the reference algorithm's states leave the
+    physical range within tens of steps);
+    precipitation -1e-6 + 5e-7 sin(2 pi t / day) m/s with hourly storms of
+    -2e-5 m/s on 10 % of hours in place of the ERA5 rates; the hydraulics of
+    the 1024 x 20 configuration."""
+    rng = np.random.Generator(np.random.PCG64(14000 + seed))
+    nlayers = 15
+    cfg = A.default_config()
+    cfg.model = A.CLM_MODEL_RICHARDS
+    cfg.ncol = ncol
+    cfg.nlayers = nlayers
+    cfg.bc_top_water = A.CLM_BC_PRECIP_RUNOFF
+    cfg.bc_bottom_water = A.CLM_BC_FLUX
+    cfg.runoff = A.CLM_RUNOFF_TOPMODEL
+    cfg.max_iters = 2
+    cfg.phase_change = 0
+    cfg.forcing_seed = 14000 + seed
+    hyd = _hydraulics(rng, ncol)
+    offsets = (np.arange(ncol + 1) * nlayers).astype(np.int32)
+    zmin, zmax = -50.0, 0.0
+    f1 = generalized_exponential_faces(zmin, zmax, nlayers, 10.0, 0.1)
+    faces = np.tile(f1, ncol)
+    zc = 0.5 * (f1[:-1] + f1[1:])
+    z_grad = zmin / 5.0
+    nu, tr = hyd["nu"][:, None], hyd["theta_r"][:, None]
+    al, vn = hyd["alpha"][:, None], hyd["n"][:, None]
+    m = 1.0 - 1.0 / vn
+    z = zc[None, :]
+    above = z > z_grad
+    S = (1.0 + (al * np.abs(z - z_grad)) ** vn) ** (-m)
+    v = np.where(above, S * (nu - tr) + tr, -hyd["S_s"][:, None] * (z - z_grad) + nu).ravel()
+    params = np.zeros((A.CLM_NPARAM_MAX, ncol))
+    params[A.CLM_P_NU] = hyd["nu"]
+    params[A.CLM_P_K_SAT] = hyd["K_sat"]
+    params[A.CLM_P_S_S] = hyd["S_s"]
+    params[A.CLM_P_THETA_R] = hyd["theta_r"]
+    params[A.CLM_P_VG_ALPHA] = hyd["alpha"]
+    params[A.CLM_P_VG_N] = hyd["n"]
+    params[A.CLM_P_F_MAX] = rng.uniform(0.3, 0.7, ncol)
+    params[A.CLM_P_F_OVER] = 3.28
+    params[A.CLM_P_R_SB] = 1.484e-4 / 1000.0
+    ftw = _forcing(ncol)
+    ftw[A.CLM_F_BASE] = -1e-6
+    ftw[A.CLM_F_AMP] = 5e-7
+    ftw[A.CLM_F_OMEGA] = 2.0 * np.pi / DAY
+    ftw[A.CLM_F_PULSE_AMP] = -2e-5
+    ftw[A.CLM_F_PULSE_PERIOD] = 3600.0
+    ftw[A.CLM_F_PULSE_DUTY] = 0.1
+    return Workload(
+        name=f"richards_benchmark_{ncol}x{nlayers}_stretched", cfg=cfg, ncol=ncol,
+        offsets=offsets, z_lo=np.full(ncol, zmin), z_hi=np.full(ncol, zmax), params=params,
+        forcing={A.CLM_BC_TOP_WATER: ftw}, vartheta_l=v, theta_i=None, rho_e_int=None,
+        intF_w=np.zeros(ncol), intF_e=None, t0=0.0, dt=1800.0, nsteps=336, z_faces=faces)
+
+
+def global_eh_stretched(ncol: int = 65536, seed: int = 0) -> Workload:
+    """EnergyHydrology on the reference's global soil column: 15 layers over
+    50 m with global_domain's default dz_tuple = (10.0, 0.05)
+    (Domains.jl:1292-1298), the 65,536 x 15 configuration's hydraulics,
+    thermal parameters, initial temperatures and forcing."""
+    w = energy_hydrology_c1(ncol=ncol, nlayers=15, seed=seed)
+    f1 = generalized_exponential_faces(-50.0, 0.0, 15, 10.0, 0.05)
+    out = w.columns(0, w.ncol, name=f"global_eh_{ncol}x15_stretched")
+    out.z_lo = np.full(ncol, -50.0)
+    out.z_hi = np.zeros(ncol)
+    out.z_faces = np.tile(f1, ncol)
     return out
 
 

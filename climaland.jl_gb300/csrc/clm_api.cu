@@ -23,7 +23,8 @@ namespace clm {
 cudaError_t launch_step(const StepArgs& A, int model, int precision, int wpc, int grid,
                         double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream);
 size_t step_smem_bytes(int model, int precision, int nmax, int wpc);
-cudaError_t step_grid(int model, int precision, int cm, int nmax, int wpc, int ntiles, int* grid);
+cudaError_t step_grid(int model, int precision, int cm, bool str, int nmax, int wpc, int ntiles,
+                      int* grid);
 size_t step_scratch_doubles(int model, int precision, int nmax, int wpc, int grid);
 // clm_layout.cu
 cudaError_t ref_to_internal(const Layout& L, const XFields& F, cudaStream_t st, int tile0 = 0,
@@ -65,6 +66,11 @@ struct clm_handle {
   int32_t* d_ref_off = nullptr;
   int64_t* d_slot_ref = nullptr;
   double *d_zlo = nullptr, *d_zhi = nullptr, *d_prm = nullptr, *d_lkap = nullptr;
+  // per-layer geometry of clm_set_faces (null: uniform layers): 5 cell arrays
+  // in the internal layout (centre, width, 1 / width, gap, 0.5 / gap) and 3
+  // sorted per-column rows (Δz_bottom, thinnest width, sum of widths)
+  double* d_geo = nullptr;
+  double* d_geocol = nullptr;
   double* d_forc[4] = {nullptr, nullptr, nullptr, nullptr};
   double* d_rx = nullptr;  // root-extraction canopy rows (sorted), or null
   double* d_atm = nullptr; // atmosphere drivers of CLM_BC_ATMOS (sorted), or null
@@ -163,6 +169,11 @@ StepArgs step_args(const clm_handle* h) {
   A.L = layout_of(h);
   A.z_lo = h->d_zlo;
   A.z_hi = h->d_zhi;
+  if (h->d_geo) {
+    const int64_t ni = h->ncells_int;
+    A.geo = GeoArrays{h->d_geo, h->d_geo + ni, h->d_geo + 2 * ni, h->d_geo + 3 * ni,
+                      h->d_geo + 4 * ni, h->d_geocol};
+  }
   A.prm = h->d_prm;
   A.lkap = h->d_lkap;
   for (int i = 0; i < 4; ++i) A.forc[i] = h->d_forc[i];
@@ -196,10 +207,28 @@ StepArgs step_args(const clm_handle* h) {
   return A;
 }
 
+// The persistent grid of the step kernel in use (uniform or per-layer
+// geometry) for the current warps per CTA, and its scratch.
+int configure_grid(clm_handle* h) {
+  CLM_CUDA(h, step_grid(h->cfg.model, h->cfg.precision, h->cfg.hydrology_cm, h->d_geo != nullptr,
+                        h->nmax, h->wpc, h->ntiles, &h->grid));
+  const size_t nsc = step_scratch_doubles(h->cfg.model, h->cfg.precision, h->nmax, h->wpc, h->grid);
+  if (nsc != h->scratch_doubles || (nsc && !h->d_scratch)) {
+    dfree(h->d_scratch);
+    if (nsc) CLM_CUDA(h, cudaMalloc(&h->d_scratch, sizeof(double) * nsc));
+    h->scratch_doubles = nsc;
+  }
+  h->guess_grid = 0;
+  return CLM_OK;
+}
+
 // Build the sorted, tiled layout from per-column layer counts.
 int build_layout(clm_handle* h, const std::vector<int>& nl) {
   const int ncol = h->ncol;
   drop_graphs(h);
+  // a new layout invalidates the per-layer geometry (clm_set_faces again)
+  dfree(h->d_geo);
+  dfree(h->d_geocol);
   h->ref_off.assign(ncol + 1, 0);
   for (int c = 0; c < ncol; ++c) {
     if (nl[c] < 2 || nl[c] > kMaxLayers)
@@ -283,13 +312,7 @@ int build_layout(clm_handle* h, const std::vector<int>& nl) {
     return fail(h, CLM_ERR_ARG, "column depth " + std::to_string(h->nmax) +
                                     " needs more shared memory than the device offers");
   h->wpc = want;
-  CLM_CUDA(h, step_grid(h->cfg.model, h->cfg.precision, h->cfg.hydrology_cm, h->nmax, h->wpc, h->ntiles, &h->grid));
-  dfree(h->d_scratch);
-  const size_t nsc = step_scratch_doubles(h->cfg.model, h->cfg.precision, h->nmax, h->wpc, h->grid);
-  if (nsc) CLM_CUDA(h, cudaMalloc(&h->d_scratch, sizeof(double) * nsc));
-  h->scratch_doubles = nsc;
-  h->guess_grid = 0;
-  return CLM_OK;
+  return configure_grid(h);
 }
 
 // Start time of step s of a call that starts at t: the one expression both
@@ -636,6 +659,7 @@ void clm_destroy(clm_handle* h) {
   dfree(h->d_tile_off); dfree(h->d_tile_n); dfree(h->d_col_n); dfree(h->d_perm); dfree(h->d_ref_off);
   dfree(h->d_slot_ref);
   dfree(h->d_zlo); dfree(h->d_zhi); dfree(h->d_prm); dfree(h->d_lkap);
+  dfree(h->d_geo); dfree(h->d_geocol);
   for (auto& p : h->d_forc) dfree(p);
   dfree(h->d_rx);
   dfree(h->d_atm);
@@ -687,7 +711,70 @@ int clm_set_geometry(clm_handle* h, const double* z_lo, const double* z_hi, cons
   if (rc != CLM_OK) return rc;
   CLM_CUDA(h, cudaStreamSynchronize(h->stream));
   h->have_geometry = true;
+  if (h->d_geo) {  // uniform layers from here on: faces set earlier no longer apply
+    drop_graphs(h);
+    dfree(h->d_geo);
+    dfree(h->d_geocol);
+    return configure_grid(h);
+  }
   return CLM_OK;
+}
+
+int clm_set_faces(clm_handle* h, const double* zf) {
+  if (!h) return CLM_ERR_ARG;
+  if (!h->have_geometry) return fail(h, CLM_ERR_STATE, "clm_set_geometry has not been called");
+  drop_graphs(h);
+  if (!zf) {  // back to uniform layers between the current z_lo and z_hi
+    dfree(h->d_geo);
+    dfree(h->d_geocol);
+    return configure_grid(h);
+  }
+  const int ncol = h->ncol;
+  const int64_t nc = h->ncells_ref;
+  // the column geometry ClimaCore derives from the faces (midpoint centres,
+  // widths, centre spacings, the boundary half-spacings), computed here once
+  std::vector<double> g(5 * (size_t)nc, 0.0), rows(3 * (size_t)ncol), zlo(ncol), zhi(ncol);
+  for (int c = 0; c < ncol; ++c) {
+    const int64_t o = h->ref_off[c];
+    const int n = h->ref_off[c + 1] - h->ref_off[c];
+    const double* f = zf + o + c;
+    for (int k = 0; k <= n; ++k)
+      if (!std::isfinite(f[k]) || (k > 0 && !(f[k] > f[k - 1])))
+        return fail(h, CLM_ERR_ARG, "column " + std::to_string(c) + " needs finite, increasing faces");
+    const GeoColumn gc = column_geometry(f, n, 1, &g[0 * nc + o], &g[1 * nc + o], &g[2 * nc + o],
+                                         &g[3 * nc + o], &g[4 * nc + o]);
+    rows[c] = gc.bot;
+    rows[ncol + c] = gc.wmin;
+    rows[2 * (size_t)ncol + c] = gc.wsum;
+    zlo[c] = f[0];
+    zhi[c] = f[n];
+  }
+  cudaStream_t st = h->stream;
+  Layout L = layout_of(h);
+  const int64_t ni = std::max<int64_t>(h->ncells_int, 1);
+  if (!h->d_geo) CLM_CUDA(h, cudaMalloc(&h->d_geo, sizeof(double) * 5 * ni));
+  if (!h->d_geocol) CLM_CUDA(h, cudaMalloc(&h->d_geocol, sizeof(double) * 3 * h->stride));
+  CLM_CUDA(h, cudaMemsetAsync(h->d_geo, 0, sizeof(double) * 5 * ni, st));
+  CLM_CUDA(h, cudaMemsetAsync(h->d_geocol, 0, sizeof(double) * 3 * h->stride, st));
+  for (int f0 = 0; f0 < 5; f0 += 3) {
+    XFields F{};
+    F.nf = std::min(3, 5 - f0);
+    for (int i = 0; i < F.nf; ++i) {
+      double* stg = h->d_stage + (size_t)i * nc;
+      CLM_CUDA(h, cudaMemcpyAsync(stg, g.data() + (size_t)(f0 + i) * nc, sizeof(double) * nc,
+                                  cudaMemcpyHostToDevice, st));
+      F.src[i] = stg;
+      F.dst[i] = h->d_geo + (f0 + i) * ni;
+    }
+    CLM_CUDA(h, ref_to_internal(L, F, st));
+    CLM_CUDA(h, cudaStreamSynchronize(st));  // the staging is reused
+  }
+  int rc = upload_cols_sorted(h, rows.data(), h->d_geocol, 3);
+  if (rc == CLM_OK) rc = upload_cols_sorted(h, zlo.data(), h->d_zlo, 1);
+  if (rc == CLM_OK) rc = upload_cols_sorted(h, zhi.data(), h->d_zhi, 1);
+  if (rc != CLM_OK) return rc;
+  CLM_CUDA(h, cudaStreamSynchronize(st));
+  return configure_grid(h);
 }
 
 int clm_set_params(clm_handle* h, const double* p, int32_t nparams) {
@@ -1044,7 +1131,8 @@ int clm_autotune(clm_handle* h, double t, double dt, int32_t probe_steps, clm_tu
   for (int w = 1; w <= 4; ++w) {
     if (step_smem_bytes(h->cfg.model, h->cfg.precision, h->nmax, w) > (size_t)dev_smem) break;
     int grid = 0;
-    CLM_CUDA(h, step_grid(h->cfg.model, h->cfg.precision, h->cfg.hydrology_cm, h->nmax, w, h->ntiles, &grid));
+    CLM_CUDA(h, step_grid(h->cfg.model, h->cfg.precision, h->cfg.hydrology_cm, h->d_geo != nullptr, h->nmax,
+                          w, h->ntiles, &grid));
     need = std::max(need, step_scratch_doubles(h->cfg.model, h->cfg.precision, h->nmax, w, grid));
     for (int sch : {CLM_SCHED_STATIC, CLM_SCHED_DYNAMIC}) {
       clm_tune_entry e{};

@@ -38,6 +38,7 @@
 
 #pragma once
 
+#include "clm_geometry.cuh"
 #include "clm_physics.cuh"
 
 namespace clm {
@@ -269,19 +270,6 @@ CLM_HD AtmosOut atmos_bc(const Tables& Tb, const AtmosK& K, const Earth& E, cons
   return o;
 }
 
-// Layer geometry of a uniform column [z_lo, z_hi] with n layers: widths
-// dz = (z_hi - z_lo) / n, centres z_lo + (k + 1/2) dz, the top face z_hi
-// (the reference's column builds the faces as z_lo + (z_hi - z_lo) k / n;
-// the two agree to rounding).
-struct ColGeom {
-  double zlo, zhi;
-  int n;
-  double dz;
-  CLM_HD ColGeom(double lo, double hi, int nl) : zlo(lo), zhi(hi), n(nl), dz((hi - lo) / nl) {}
-  CLM_HD double centre(int k) const { return zlo + (k + 0.5) * dz; }
-  CLM_HD double width(int) const { return dz; }
-};
-
 // Runoff of the atmosphere-driven boundary on an EnergyHydrology column
 // (src/standalone/Soil/Runoff/Runoff.jl): NoRunoff (:69-71), SurfaceRunoff
 // (:129-148) and TOPMODELRunoff (:234-283) with the infiltration capacity
@@ -299,9 +287,9 @@ struct EHRunoff {
 CLM_HD double sat_weight(double twc, double nr) { return ((twc - nr) - 0.0 > kEps ? 1.0 : 0.0) * twc / nr; }
 
 // layer(k, v, ti, T) fills the layer's vartheta_l, theta_i and T
-template <class Layer>
+template <class Layer, class G_>
 CLM_HD EHRunoff eh_runoff(const Tables& Tb, const Earth& E, const EHScalars& sc, int runoff,
-                          const ColGeom& G, double nu, double theta_r, double K_sat, double f_max,
+                          const G_& G, double nu, double theta_r, double K_sat, double f_max,
                           double f_over, double R_sb, double tl_top, double input, Layer layer) {
   EHRunoff r{input, 0.0, 0.0, 0.0, 0.0};
   if (runoff == CLM_RUNOFF_NONE) return r;
@@ -348,23 +336,24 @@ CLM_HD double tf_depressed_aux(const Tables& Tb, const Earth& E, const CM& g, do
 // theta_l for the albedo: the mean over the layers centred within
 // `thick` of the surface when the thinnest layer is thinner than it
 // (column_integral_definite of H theta_l / N), else the top centre's.
-template <class ThetaL>
-CLM_HD double albedo_theta(const ColGeom& G, double thick, ThetaL theta_l) {
-  if (!(G.dz < thick)) return theta_l(G.n - 1);
+template <class ThetaL, class G_>
+CLM_HD double albedo_theta(const G_& G, double thick, ThetaL theta_l) {
+  if (!(G.min_width() < thick)) return theta_l(G.n - 1);
   // H(thick + sqrt(eps) - (z_sfc - z_k)) rises with k: the layers k0..n-1
   auto H = [&](int k) { return (thick + kSqrtEps) - (G.zhi - G.centre(k)) > kEps; };
   int k0 = G.n;
   while (k0 > 0 && H(k0 - 1)) --k0;
   double N = 0.0;
-  for (int k = k0; k < G.n; ++k) N += G.dz;
+  for (int k = k0; k < G.n; ++k) N += G.width(k);
   double I = 0.0;
-  for (int k = k0; k < G.n; ++k) I += G.dz * (theta_l(k) / N);
+  for (int k = k0; k < G.n; ++k) I += G.width(k) * (theta_l(k) / N);
   return I;
 }
 
 // SoilSublimation's factor for layer k: H(z_k + 2 dz_top) / (2 dz_top), with
 // the reference's absolute coordinates.
-CLM_HD double sublimation_weight(const ColGeom& G, int k, double dz_top) {
+template <class G_>
+CLM_HD double sublimation_weight(const G_& G, int k, double dz_top) {
   return (((G.centre(k) + 2.0 * dz_top) - 0.0 > kEps) ? 1.0 : 0.0) / (2.0 * dz_top);
 }
 

@@ -21,11 +21,12 @@ __global__ void budgets_kernel(StepArgs A, int eh, double* __restrict__ W, doubl
   }
   const int tile = s / kTile, lane = s % kTile;
   const int64_t base = A.L.tile_off[tile] + lane;
-  const double dz = (A.z_hi[s] - A.z_lo[s]) / n;
+  const double dzu = (A.z_hi[s] - A.z_lo[s]) / n;
   const double r = A.E.rho_i_over_rho_l;
   double w = 0.0, e = 0.0;
   for (int k = 0; k < n; ++k) {
     const int64_t i = base + (int64_t)k * kTile;
+    const double dz = A.geo.w ? A.geo.w[i] : dzu;  // layer width (stretched: per layer)
     double v = A.v[i];
     if (eh) {
       v += A.ti[i] * r;

@@ -21,13 +21,14 @@
 
 namespace clm {
 
-template <int KIND, class CM>
+template <int KIND, class CM, class Geom>
 __device__ void closure_column(const ClosureArgs& C, const Tables& Tb) {
   const StepArgs& A = C.A;
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= A.L.stride) return;
   const int n = A.L.col_n[s];
   if (n <= 0) return;
+  const auto G = GeomOf<Geom::kStretched>::make(A, A.L.tile_off[s / kTile] + s % kTile, s, n);
   const int orig = A.L.perm[s];
   const int64_t o = C.ref_off[orig];
   const int st = A.L.stride;
@@ -39,8 +40,6 @@ __device__ void closure_column(const ClosureArgs& C, const Tables& Tb) {
   const double nu = P[CLM_P_NU * st + s], K_sat = P[CLM_P_K_SAT * st + s];
   const double S_s = P[CLM_P_S_S * st + s], theta_r = P[CLM_P_THETA_R * st + s];
   const CM g = make_cm<CM>(P[CLM_P_VG_ALPHA * st + s], P[CLM_P_VG_N * st + s]);
-  const double dz = (A.z_hi[s] - A.z_lo[s]) / n;
-  const double inv_dz = 1.0 / dz, half = 0.5 * dz;
   double kdry = 0, ksf = 0, ksu = 0, rcds = 0, nuom = 0, nuq = 0, nug = 0, lku = 0, lkf = 0;
   if (eh) {
     kdry = P[CLM_P_KAPPA_DRY * st + s];
@@ -86,29 +85,28 @@ __device__ void closure_column(const ClosureArgs& C, const Tables& Tb) {
   if (A.bc_tw == CLM_BC_STATE) {
     double pb, d;
     psi_dpsi<false>(Tb, g, nu, ftw, theta_r, S_s, pb, d);
-    Ftw = -Kc[n - 1] * ((pb + half) - psic[n - 1]) / half;
+    Ftw = -Kc[n - 1] * ((pb + G.half_top()) - psic[n - 1]) / G.half_top();
   }
   if (A.bc_bw == CLM_BC_FREE_DRAINAGE) {
     Fbw = -1.0 * Kc[0];
   } else if (A.bc_bw == CLM_BC_STATE) {
     double pb, d;
     psi_dpsi<false>(Tb, g, nu, fbw, theta_r, S_s, pb, d);
-    Fbw = -Kc[0] * ((psic[0] + half) - pb) / half;
+    Fbw = -Kc[0] * ((psic[0] + G.half_bot()) - pb) / G.half_bot();
   }
   if (eh) {
     Fth = fth;
-    if (A.bc_th == CLM_BC_STATE) Fth = -kapc[n - 1] * (fth - Tc[n - 1]) / half;
+    if (A.bc_th == CLM_BC_STATE) Fth = -kapc[n - 1] * (fth - Tc[n - 1]) / G.half_top();
     else if (A.bc_th == CLM_BC_FLUX_ADVECTIVE) {
       const double* F = A.forc[CLM_BC_TOP_HEAT];
       Fth = fth + Ftw * rho_e_liq(E, F ? F[CLM_F_T_ADV * st + s] : E.T_0);
     }
     Fbh = fbh;
     if (A.bc_bh == CLM_BC_FREE_DRAINAGE) Fbh = -1.0 * Kc[0] * rho_e_liq(E, Tc[0]);
-    else if (A.bc_bh == CLM_BC_STATE) Fbh = -kapc[0] * (Tc[0] - fbh) / half;
+    else if (A.bc_bh == CLM_BC_STATE) Fbh = -kapc[0] * (Tc[0] - fbh) / G.half_bot();
   }
   const bool dflux = !eh && A.bc_tw == CLM_BC_STATE;
   // atmosphere-driven top boundary (CLM_BC_ATMOS) from the aux values above
-  const ColGeom G{A.z_lo[s], A.z_hi[s], n};
   AtmosOut ab{};
   EHRunoff ro{0.0, 0.0, 0.0, 0.0, 0.0};
   double dz_top = 0.0;
@@ -123,7 +121,7 @@ __device__ void closure_column(const ClosureArgs& C, const Tables& Tb) {
     sf.Tf = tf_depressed_aux(Tb, E, g, nu, theta_r, sf.th1, sf.ti);
     sf.z1 = G.centre(n - 1);
     sf.z2 = G.centre(n - 2);
-    dz_top = G.zhi - sf.z1;
+    dz_top = G.top_gap();
     sf.dz_top = dz_top;
     const AtmosRow D{A.atm, st, s};
     sf.th_alb = albedo_theta(G, D(CLM_AT_ALBEDO_TOP_THICKNESS), [&](int k) { return tlc[k]; });
@@ -204,21 +202,18 @@ __device__ void closure_column(const ClosureArgs& C, const Tables& Tb) {
         const double Yti = C.ti[o + k];
         const double rc = heat_capacity(E, tlc[k], Yti, rcds);
         uint32_t fl = 0;
-        const double pc = phase_change(Tb, E, g, nu, theta_r, tlc[k], Yti, Tc[k], rc, kapc[k], dz, fl);
+        const double pc = phase_change(Tb, E, g, nu, theta_r, tlc[k], Yti, Tc[k], rc, kapc[k], G.width(k), fl);
         dv = -pc;
         dti = E.rho_l_over_rho_i * pc;
       }
       if (atmos) dti += -ab.vice * E.rho_l / E.rho_i * sublimation_weight(G, k, dz_top);
       if (roots) {
-        const double zlo = A.z_lo[s], zhi = A.z_hi[s];
-        const double zc = 0.5 * ((zlo + (zhi - zlo) * ((double)k / n)) +
-                                 (k + 1 == n ? zhi : zlo + (zhi - zlo) * ((double)(k + 1) / n)));
-        const double re = root_rate(Tb, rcol, zc, psic[k], Kc[k]);
+        const double re = root_rate(Tb, rcol, G.face_centre(k), psic[k], Kc[k]);
         const double ree = re * rho_e_liq(E, Tc[k]);
         dv += -1.0 * re;
         de += -1.0 * ree;
-        root_e += dz * ree;
-        root_w += dz * re;
+        root_e += G.width(k) * ree;
+        root_w += G.width(k) * re;
       }
       if (C.dv) C.dv[o + k] = dv;
       if (eh && C.dti) C.dti[o + k] = dti;
@@ -233,11 +228,12 @@ __device__ void closure_column(const ClosureArgs& C, const Tables& Tb) {
     for (int k = 0; k < n; ++k) {
       double Fw_up, Fe_up = 0.0;
       if (k < n - 1) {
-        const double dh = (psic[k + 1] - psic[k]) + dz;
-        Fw_up = -0.5 * (Kc[k] + Kc[k + 1]) * inv_dz * dh;
+        const double rg = 2.0 * G.hinv_gap(k);  // 1 / gap
+        const double dh = (psic[k + 1] - psic[k]) + G.gap(k);
+        Fw_up = -0.5 * (Kc[k] + Kc[k + 1]) * rg * dh;
         if (eh) {
-          const double ak = 0.5 * (kapc[k] + kapc[k + 1]) * inv_dz;
-          const double ae = 0.5 * (rho_e_liq(E, Tc[k]) * Kc[k] + rho_e_liq(E, Tc[k + 1]) * Kc[k + 1]) * inv_dz;
+          const double ak = 0.5 * (kapc[k] + kapc[k + 1]) * rg;
+          const double ae = 0.5 * (rho_e_liq(E, Tc[k]) * Kc[k] + rho_e_liq(E, Tc[k + 1]) * Kc[k + 1]) * rg;
           Fe_up = -ak * (Tc[k + 1] - Tc[k]) - ae * dh;
         }
       } else {
@@ -246,9 +242,9 @@ __device__ void closure_column(const ClosureArgs& C, const Tables& Tb) {
       }
       // TOPMODEL's subsurface sink under the atmosphere-driven boundary
       const double w = (ro.cw != 0.0 || ro.ce != 0.0) ? sat_weight(C.v[o + k] - theta_r, nu - theta_r) : 0.0;
-      if (C.dv) C.dv[o + k] = -((Fw_up - Fw_dn) * inv_dz) - ro.cw * w;
+      if (C.dv) C.dv[o + k] = -((Fw_up - Fw_dn) * G.inv_width(k)) - ro.cw * w;
       if (eh) {
-        if (C.de) C.de[o + k] = -((Fe_up - Fe_dn) * inv_dz) - ro.ce * w;
+        if (C.de) C.de[o + k] = -((Fe_up - Fe_dn) * G.inv_width(k)) - ro.ce * w;
         if (C.dti) C.dti[o + k] = 0.0;
       }
       Fw_dn = Fw_up;
@@ -259,7 +255,6 @@ __device__ void closure_column(const ClosureArgs& C, const Tables& Tb) {
     return;
   }
   if (KIND == CL_JAC) {
-    const double rdz = C.dtgamma * inv_dz;
     double D[kMaxLayers];
     for (int k = 0; k < n; ++k) {
       double p;
@@ -281,12 +276,14 @@ __device__ void closure_column(const ClosureArgs& C, const Tables& Tb) {
           return 1.0 / heat_capacity(E, tlc[a], C.ti[o + a], rcds);
         };
         d0 = dd(k);
-        if (k < n - 1) { cup = coef(k) * inv_dz; dp = dd(k + 1); }
-        if (k > 0) { cdn = coef(k - 1) * inv_dz; dm = dd(k - 1); }
+        const double rdz = C.dtgamma * G.inv_width(k);
+        if (k < n - 1) { cup = coef(k) * (2.0 * G.hinv_gap(k)); dp = dd(k + 1); }
+        if (k > 0) { cdn = coef(k - 1) * (2.0 * G.hinv_gap(k - 1)); dm = dd(k - 1); }
         double L = (k > 0) ? rdz * cdn * dm : 0.0;
         double U = (k < n - 1) ? rdz * cup * dp : 0.0;
         double M = -rdz * (cup + cdn) * d0 - 1.0;
-        if (blk == 0 && dflux && k == n - 1) M += -C.dtgamma * ((Kc[n - 1] * D[n - 1] / half) * inv_dz);
+        if (blk == 0 && dflux && k == n - 1)
+          M += -C.dtgamma * ((Kc[n - 1] * D[n - 1] / G.half_top()) * G.inv_width(k));
         W[3 * (o + k) + 0] = L;
         W[3 * (o + k) + 1] = M;
         W[3 * (o + k) + 2] = U;
@@ -300,10 +297,14 @@ __global__ void closure_kernel(ClosureArgs C) {
   __shared__ double tab[fm::TABLE_SIZE];
   const Tables Tb = fm::stage_tables(tab);
   __syncthreads();
-  if (C.A.cm == CLM_CM_BROOKS_COREY)
-    closure_column<KIND, BC>(C, Tb);
-  else
-    closure_column<KIND, VG>(C, Tb);
+  const bool str = C.A.geo.z != nullptr;
+  if (C.A.cm == CLM_CM_BROOKS_COREY) {
+    if (str) closure_column<KIND, BC, ColGeomS>(C, Tb);
+    else closure_column<KIND, BC, ColGeom>(C, Tb);
+  } else {
+    if (str) closure_column<KIND, VG, ColGeomS>(C, Tb);
+    else closure_column<KIND, VG, ColGeom>(C, Tb);
+  }
 }
 
 __device__ void thomas_ref(int n, const double* W, const double* f, double* x) {

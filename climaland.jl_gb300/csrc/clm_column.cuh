@@ -54,27 +54,11 @@
 
 namespace clm {
 
-template <typename T>
-struct Col {
-  T* p;
-  int s;
-  CLM_HD T& operator[](int k) const { return p[(int64_t)k * s]; }
-  // a store this launch does not read back: cache-streaming (evict-first)
-  CLM_HD void store_last(int k, T v) const {
-#ifdef __CUDA_ARCH__
-    __stcs(p + (int64_t)k * s, v);
-#else
-    p[(int64_t)k * s] = v;
-#endif
-  }
-};
-
 template <class CM>
 struct EHCol {
   double nu, K_sat, S_s, theta_r;
   CM g;  // hydrology closure (VG or BC)
   double kdry, ksf, ksu, rcds, nuom, nuq, nug, lku, lkf;
-  double dz, inv_dz;
   double inv_S_s;  // 1 / S_s
 };
 
@@ -104,8 +88,6 @@ CLM_HD EHCol<CM> load_eh_col(const StepArgs& A, const Tables& Tb, int s, int n) 
     c.lku = A.lkap[s];
     c.lkf = A.lkap[st + s];
   }
-  c.dz = (A.z_hi[s] - A.z_lo[s]) / n;
-  c.inv_dz = 1.0 / c.dz;
   c.inv_S_s = 1.0 / c.S_s;
   return c;
 }
@@ -237,28 +219,32 @@ constexpr int kSrcNone = 0;
 constexpr int kSrcRoots = 1;  // RootExtraction (A.rx)
 constexpr int kSrcAtmos = 2;  // atmosphere-driven top boundary + SoilSublimation (A.atm)
 
-template <typename JT, class CM, bool kLogKappaHere = false, int kSrc = kSrcNone>
+// Geom: ColGeom (uniform layers) or ColGeomS (per-layer geometry); G holds
+// the column's. On a uniform column rdz(k) = dt / dz and the face means
+// 0.5 (a + b) / dz are exactly (a + b) hinv_gap(k).
+template <typename JT, class CM, bool kLogKappaHere = false, int kSrc = kSrcNone,
+          class Geom = ColGeom>
 CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int orig,
-                      const EHBuffers& B, const EHJac<JT>& J, double t0, double dt, int nsteps,
-                      double& Fw, double& Fe, uint32_t& flags, int& iters_done) {
+                      const EHBuffers& B, const EHJac<JT>& J, const Geom& G, double t0,
+                      double dt, int nsteps, double& Fw, double& Fe, uint32_t& flags,
+                      int& iters_done) {
   const Earth& E = A.E;
   const EHScalars& sc = A.sc;
   const EHCol<CM> c = load_eh_col<CM, kLogKappaHere>(A, Tb, s, n);
   const int st = A.L.stride;
-  const double rdz = dt * c.inv_dz;
-  const double half = 0.5 * c.dz;
-  const double hinv_dz = 0.5 * c.inv_dz;  // face means: 0.5 (a + b) / dz, exactly (a + b) hinv_dz
+  constexpr bool kStr = Geom::kStretched;
+  auto rdz = [&](int k) { return dt * G.inv_width(k); };
   // mixed: the energy advection coefficient at a face, 0.5 (rho e_l(T_k) K_k
   // + rho e_l(T_k+1) K_k+1) / dz, as the sum of the layers' q K (rho c_l 0.5 / dz)
-  const double c_adv = E.rhocp_l * hinv_dz;
+  // (on a stretched column q K rho c_l, times 0.5 / gap at the face)
+  const double c_adv = kStr ? E.rhocp_l : E.rhocp_l * G.hinv_gap(0);
   constexpr bool mixed = sizeof(JT) < sizeof(double);
   EHMixed<CM> MX;
-  const PCCol pcc = make_pc_col(c.nu, c.theta_r, c.dz);
+  PCCol pcc = make_pc_col(c.nu, c.theta_r, G.width(0));
   if constexpr (mixed) MX = make_eh_mixed(Tb, E, sc, c);
   const bool tol = A.newton_mode == CLM_NEWTON_TOL;  // the increment norms are needed only then
   constexpr bool kRoots = kSrc == kSrcRoots;
   constexpr bool kAtmos = kSrc == kSrcAtmos;
-  const ColGeom G{A.z_lo[s], A.z_hi[s], n};
 
   bool finite = true;  // the last step's state, checked as it is stored
   for (int step = 0; step < nsteps; ++step) {
@@ -303,7 +289,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       sf.Tf = tf_depressed_aux(Tb, E, c.g, c.nu, c.theta_r, sf.th1, Yti);
       sf.z1 = G.centre(k1);
       sf.z2 = G.centre(k1 - 1);
-      dz_top = G.zhi - sf.z1;
+      dz_top = G.top_gap();
       sf.dz_top = dz_top;
       sf.ti = Yti;
       const AtmosRow D{A.atm, st, s};
@@ -334,6 +320,8 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       const double nu_safe = fmax(nu_eff, c.theta_r + kSqrtEps);
       const double tl = (v_safe < nu_safe) ? v_safe : nu_safe;
       const double rc = heat_capacity(E, tl, Yti, c.rcds);
+      // thermal_time's 1 / (3 dz^2) of this layer
+      if constexpr (kStr) pcc.inv_3dz2 = fm::rcp(3.0 * (G.width(k) * G.width(k)));
       // one reciprocal of rho c for T and the phase change
       const double inv_rc = fm::rcp(rc);
       const double T = E.T_0 + (Ye + Yti * E.rho_i_LH_f0) * inv_rc;
@@ -345,7 +333,9 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         const F2 guard = ff::add_f(MX.cf.theta_r, 1.4901161193847656e-08f);
         const F2 S = ff::div(ff::sub(ff_max(ff::from_double(Yv), guard), MX.cf.theta_r),
                              ff::sub(ff_max(MX.cf.nu, guard), MX.cf.theta_r));
-        const F2 fi = Yti > 0.0 ? ff::div(ti_f, ff::sub(ff::add(tl_f, ti_f), MX.cf.theta_r))
+        // f_i = 0 without the division only where theta_i is exactly 0 (a
+        // negative theta_i gives the reference's f_i < 0)
+        const F2 fi = Yti != 0.0 ? ff::div(ti_f, ff::sub(ff::add(tl_f, ti_f), MX.cf.theta_r))
                                 : ff::make(0.0f);
         const F2 lnf = ff::add(ff::neg(ff::mul(MX.omega_ln10, fi)),
                                ff::mul(MX.visc_gamma, ff::sub(ff::from_double(T), MX.visc_T_ref)));
@@ -356,7 +346,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         kap = conductivity_heat(Tb, sc, tl, Yti, c.nu, c.kdry, c.ksu, c.ksf, c.lku, c.lkf, c.nuom,
                                 c.nuq, c.nug);
         const double SK = saturation_r(pcc.inv_den, Yv, c.theta_r);
-        const double fi = Yti > 0.0 ? Yti / (tl + Yti - c.theta_r) : 0.0;
+        const double fi = Yti != 0.0 ? Yti / (tl + Yti - c.theta_r) : 0.0;
         // impedance_factor * viscosity_factor * hydraulic_conductivity, with
         // the sqrt(S) of the van Genuchten K inside the same exponential
         const double lnf = -sc.omega_ln10 * fi + sc.visc_gamma * (T - sc.visc_gamma_T_ref);
@@ -379,15 +369,12 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         // psi at Y_n (update_aux!), the layer centre z, K and T of this stage
         double psi_n, d;
         psi_dpsi<false>(Tb, c.g, nu_eff, Yv, c.theta_r, c.S_s, psi_n, d);
-        const double zc = 0.5 * ((A.z_lo[s] + (A.z_hi[s] - A.z_lo[s]) * ((double)k / n)) +
-                                 (k + 1 == n ? A.z_hi[s]
-                                             : A.z_lo[s] + (A.z_hi[s] - A.z_lo[s]) * ((double)(k + 1) / n)));
-        const double re = root_rate(Tb, rcol, zc, psi_n, K);
+        const double re = root_rate(Tb, rcol, G.face_centre(k), psi_n, K);
         const double ree = re * rho_e_liq(E, T);
         Uv = Yv + dt * ((-pc) + (-1.0 * re));  // sources in the reference's order
         Ue = Ye + dt * (-1.0 * ree);
-        root_e += c.dz * ree;
-        root_w += c.dz * re;
+        root_e += G.width(k) * ree;
+        root_w += G.width(k) * re;
         B.ge[k] = Ue;
       }
       B.gv[k] = Uv;
@@ -421,13 +408,17 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       // face conductances k-1|k, frozen through the Newton solve: kappa on
       // the face into kappa's slot (the cell value is not used after stage 1)
       if (k > 0) {
-        const double ak = (kap_prev + kap) * hinv_dz;
-        const double aw = (K_prev + K) * hinv_dz;
+        const double ak = (kap_prev + kap) * G.hinv_gap(k - 1);
+        const double aw = (K_prev + K) * G.hinv_gap(k - 1);
         B.kap[k - 1] = ak;
         if (B.aw.p) B.aw[k - 1] = aw;
         if constexpr (mixed) {
-          B.awr[k - 1] = ff::narrow_trunc(rdz * aw);
-          B.akr[k - 1] = ff::narrow_trunc(rdz * ak);
+          // the float rows' face products: dt K_face / (dz gap) (uniform:
+          // W's own rows), or dt K_face / gap (stretched: W's rows times the
+          // layer width)
+          const double fac = kStr ? dt : rdz(k - 1);
+          B.awr[k - 1] = ff::narrow_trunc(fac * aw);
+          B.akr[k - 1] = ff::narrow_trunc(fac * ak);
         }
       }
       kap_prev = kap;
@@ -463,7 +454,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       } else if (A.bc_tw == CLM_BC_STATE) {
         double pb, d;
         psi_dpsi<false>(Tb, c.g, c.nu, ftw, c.theta_r, c.S_s, pb, d);
-        Ftw = -Kt * ((pb + half) - psit) / half;  // diffusive_flux
+        Ftw = -Kt * ((pb + G.half_top()) - psit) / G.half_top();  // diffusive_flux
       } else {
         Ftw = ftw;
       }
@@ -472,14 +463,14 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       } else if (A.bc_bw == CLM_BC_STATE) {
         double pb, d;
         psi_dpsi<false>(Tb, c.g, c.nu, fbw, c.theta_r, c.S_s, pb, d);
-        Fbw = -K0 * ((psi0 + half) - pb) / half;
+        Fbw = -K0 * ((psi0 + G.half_bot()) - pb) / G.half_bot();
       } else {
         Fbw = fbw;
       }
       if (kAtmos) {
         Fth = ab.top_h;
       } else if (A.bc_th == CLM_BC_STATE) {
-        Fth = -kapt * (fth - Tt) / half;
+        Fth = -kapt * (fth - Tt) / G.half_top();
       } else if (A.bc_th == CLM_BC_FLUX_ADVECTIVE) {
         const double* F = A.forc[CLM_BC_TOP_HEAT];
         const double Tadv = F ? F[CLM_F_T_ADV * st + s] : E.T_0;
@@ -490,7 +481,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       if (A.bc_bh == CLM_BC_FREE_DRAINAGE) {
         Fbh = -1.0 * K0 * rho_e_liq(E, T0);
       } else if (A.bc_bh == CLM_BC_STATE) {
-        Fbh = -kap0 * (T0 - fbh) / half;
+        Fbh = -kap0 * (T0 - fbh) / G.half_bot();
       } else {
         Fbh = fbh;
       }
@@ -528,10 +519,10 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
                            psin, Dn);
           Kn = B.K[k + 1];
           relKn = mixed ? Tn * (Kn * c_adv) : rho_e_liq(E, Tn) * Kn;
-          aw_up = B.aw.p ? B.aw[k] : (Kc + Kn) * hinv_dz;
+          aw_up = B.aw.p ? B.aw[k] : (Kc + Kn) * G.hinv_gap(k);
           const double ak_up = B.kap[k];  // face k|k+1 (stage 1)
-          ae_up = mixed ? relKc + relKn : (relKc + relKn) * hinv_dz;
-          const double dh = (psin - psic) + c.dz;
+          ae_up = (mixed && !kStr) ? relKc + relKn : (relKc + relKn) * G.hinv_gap(k);
+          const double dh = (psin - psic) + G.gap(k);
           Fw_up = -aw_up * dh;
           Fe_up = -ak_up * (Tn - Tc) - ae_up * dh;
           if constexpr (mixed) awr_up = B.awr[k];
@@ -542,29 +533,32 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         double fv, fe;
         if constexpr (mixed) {
           // U + dt T - x with dt T = rdz (F_dn - F_up): one rounding fewer
-          fv = (B.gv[k] - B.xv[k]) + rdz * (Fw_dn - Fw_up);
-          fe = (B.ge[k] - B.xe[k]) + rdz * (Fe_dn - Fe_up);
+          fv = (B.gv[k] - B.xv[k]) + rdz(k) * (Fw_dn - Fw_up);
+          fe = (B.ge[k] - B.xe[k]) + rdz(k) * (Fe_dn - Fe_up);
         } else {
-          const double Tv = -((Fw_up - Fw_dn) * c.inv_dz);
-          const double Tee = -((Fe_up - Fe_dn) * c.inv_dz);
+          const double Tv = -((Fw_up - Fw_dn) * G.inv_width(k));
+          const double Tee = -((Fe_up - Fe_dn) * G.inv_width(k));
           fv = B.gv[k] + dt * Tv - B.xv[k];
           fe = B.ge[k] + dt * Tee - B.xe[k];
         }
-        sum_fv += fv;
-        sum_fe += fe;
+        // the mixed path's weighted sums (row weight 1 on a uniform column)
+        sum_fv += G.row_w(k) * fv;
+        sum_fe += G.row_w(k) * fe;
         JT L, U, Md;
         if constexpr (mixed) {  // rows from the float face products
           L = awr_dn * D_prev;
           U = awr_up * Dn;
           Md = -(awr_up + awr_dn) * Dc - 1.0f;
         } else {
-          L = (JT)(rdz * aw_dn) * D_prev;
-          U = (k < n - 1) ? (JT)(rdz * aw_up * Dn) : (JT)0;
-          Md = (JT)(-rdz * (aw_up + aw_dn) * Dc - 1.0);
+          L = (JT)(rdz(k) * aw_dn) * D_prev;
+          U = (k < n - 1) ? (JT)(rdz(k) * aw_up * Dn) : (JT)0;
+          Md = (JT)(-rdz(k) * (aw_up + aw_dn) * Dc - 1.0);
         }
         JT piv;
         if constexpr (mixed) {
-          const JT sp = (k == 0) ? (JT)-1 : (JT)-1 - U_prev * (sp_prev / piv_prev);
+          // the column sum of row k's block column: -(row weight)
+          const JT wk = kStr ? (JT)G.row_w(k) : (JT)1;
+          const JT sp = (k == 0) ? -wk : -wk - U_prev * (sp_prev / piv_prev);
           piv = sp - awr_up * Dc;  // L_{k+1} = dt K_face(k|k+1) / dz^2 dpsi_k
           U_prev = U;
           sp_prev = sp;
@@ -574,7 +568,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         }
         const JT inv = rcp_jt(piv);
         const JT cpk = U * inv;
-        const JT dpk = (to_jt<JT>(fv) - L * dp_prev) * inv;
+        const JT dpk = (to_jt<JT>(kStr && mixed ? G.row_w(k) * fv : fv) - L * dp_prev) * inv;
         J.cp[k] = cpk;
         J.dp[k] = dpk;
         J.d[k] = Dc;
@@ -602,11 +596,11 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
           const JT d = J.dp[k] - J.cp[k] * nxt;
           J.dp[k] = d;
           nxt = d;
-          if (mixed) sdv += from_jt<JT>(d);
+          if (mixed) sdv += G.row_w(k) * from_jt<JT>(d);
         }
       }
-      // FP64 column-sum projection (mixed path): sum(delta_v) = -sum(f_v)
-      const double corr_v = mixed ? (sdv + sum_fv) / n : 0.0;
+      // FP64 column-sum projection (mixed path): sum(w delta_v) = -sum(w f_v)
+      const double corr_v = mixed ? (sdv + sum_fv) / G.wsum() : 0.0;
       const double flux2 = fFw * fFw + fFe * fFe;  // integrated fluxes
       double state2 = 0.0;                           // state increments
       // sweep 3 (bottom -> top): energy right-hand side, rho e forward
@@ -648,7 +642,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
           }
           const JT Gup = (k < n - 1) ? (Dp * dvp - D0 * dv0) : (JT)0;
           const JT Gdn = (k > 0) ? (D0 * dv0 - Dm * dvm) : (JT)0;
-          const JT wev = (JT)rdz * (ae_up * Gup - ae_dn * Gdn) - dv0;
+          const JT wev = (JT)rdz(k) * (ae_up * Gup - ae_dn * Gdn) - dv0;
           const double g = B.fe[k] - from_jt<JT>(wev);
           JT L, U, Md;
           if constexpr (mixed) {
@@ -656,13 +650,14 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
             U = akr_up * ircf_n;
             Md = -(akr_up + akr_dn) * ircf_c - 1.0f;
           } else {
-            L = (JT)(rdz * ak_dn * irc_m);
-            U = (JT)(rdz * ak_up * irc_n);
-            Md = (JT)(-rdz * (ak_up + ak_dn) * irc_c - 1.0);
+            L = (JT)(rdz(k) * ak_dn * irc_m);
+            U = (JT)(rdz(k) * ak_up * irc_n);
+            Md = (JT)(-rdz(k) * (ak_up + ak_dn) * irc_c - 1.0);
           }
           JT piv;
           if constexpr (mixed) {
-            const JT sp = (k == 0) ? (JT)-1 : (JT)-1 - U_prev * (sp_prev / piv_prev);
+            const JT wk = kStr ? (JT)G.row_w(k) : (JT)1;
+            const JT sp = (k == 0) ? -wk : -wk - U_prev * (sp_prev / piv_prev);
             piv = sp - akr_up * ircf_c;  // L_{k+1} = dt kappa_face(k|k+1) / dz^2 / rho c_k
             U_prev = U;
             sp_prev = sp;
@@ -672,7 +667,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
           }
           const JT inv = rcp_jt(piv);
           const JT ck = U * inv;
-          const JT dk = (to_jt<JT>(g) - L * d_prev) * inv;
+          const JT dk = (to_jt<JT>(kStr && mixed ? G.row_w(k) * g : g) - L * d_prev) * inv;
           J.cp[k] = ck;
           J.dp[k] = dk;
           c_prev = ck;
@@ -698,12 +693,12 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
           for (int k = n - 1; k >= 0; --k) {
             const JT d = J.dp[k] - J.cp[k] * nxt;
             J.dp[k] = d;
-            sde += from_jt<JT>(d);
+            sde += G.row_w(k) * from_jt<JT>(d);
             nxt = d;
           }
-          // W_ee and W_ev + I have zero column sums:
-          // sum(delta_e) = -sum(f_e) - sum(delta_v) = -sum(f_e) + sum(f_v)
-          const double corr_e = (sde + sum_fe - sum_fv) / n;
+          // W_ee and W_ev + I have zero (width-weighted) column sums:
+          // sum(w delta_e) = -sum(w f_e) - sum(w delta_v) = -sum(w f_e) + sum(w f_v)
+          const double corr_e = (sde + sum_fe - sum_fv) / G.wsum();
           for (int k = 0; k < n; ++k) {
             const double d = from_jt<JT>(J.dp[k]) - corr_e;
             B.xe[k] -= d;
@@ -785,10 +780,11 @@ struct RJac {
   Col<JT> dpl{nullptr, 0};
 };
 
-template <typename JT, class CM>
+template <typename JT, class CM, class Geom = ColGeom>
 CLM_HD void richards_column(const StepArgs& A, const Tables& Tb, int s, int n, int orig,
-                            const RBuffers& B, const RJac<JT>& J, double t0, double dt,
-                            int nsteps, double& Fw, uint32_t& flags, int& iters_done) {
+                            const RBuffers& B, const RJac<JT>& J, const Geom& G, double t0,
+                            double dt, int nsteps, double& Fw, uint32_t& flags,
+                            int& iters_done) {
   const int st = A.L.stride;
   const double* P = A.prm;
   const double nu = P[CLM_P_NU * st + s];
@@ -797,10 +793,8 @@ CLM_HD void richards_column(const StepArgs& A, const Tables& Tb, int s, int n, i
   const double theta_r = P[CLM_P_THETA_R * st + s];
   const CM g = make_cm<CM>(P[CLM_P_VG_ALPHA * st + s], P[CLM_P_VG_N * st + s]);
   const double inv = sat_inv(nu, theta_r), inv_S_s = 1.0 / S_s;
-  const double dz = (A.z_hi[s] - A.z_lo[s]) / n;
-  const double inv_dz = 1.0 / dz;
-  const double half = 0.5 * dz;
-  const double rdz = dt * inv_dz;
+  auto rdz = [&](int k) { return dt * G.inv_width(k); };
+  constexpr bool kStr = Geom::kStretched;
   constexpr bool mixed = sizeof(JT) < sizeof(double);
   // mixed path: K, psi and dpsi in double-float (FP64 closure where it declines)
   typename ColFFOf<CM>::type cf;
@@ -855,9 +849,9 @@ CLM_HD void richards_column(const StepArgs& A, const Tables& Tb, int s, int n, i
         double h = 0.0;  // column_integral_definite of the saturation weights
         for (int k = 0; k < n; ++k) {
           const double twc = B.gv[k] + 0.0 - theta_r;
-          h += dz * ((twc - nr > kEps ? 1.0 : 0.0) * twc / nr);
+          h += G.width(k) * ((twc - nr > kEps ? 1.0 : 0.0) * twc / nr);
         }
-        const double zwt = (A.z_hi[s] - A.z_lo[s]) - h;
+        const double zwt = (G.zhi - G.zlo) - h;
         const double f_sat = fmin(P[CLM_P_F_MAX * st + s] *
                                       fm::exp(Tb, -P[CLM_P_F_OVER * st + s] / 2.0 * zwt), 1.0);
         Ftw = (1.0 - f_sat) * fmax(ic, ftw);
@@ -878,7 +872,7 @@ CLM_HD void richards_column(const StepArgs& A, const Tables& Tb, int s, int n, i
       point(B.xv[0], Kc, psic, Dc);
       if (refresh_bc) {
         if (A.bc_bw == CLM_BC_FREE_DRAINAGE) Fbw = -1.0 * Kc;
-        else if (A.bc_bw == CLM_BC_STATE) Fbw = -Kc * ((psic + half) - psi_bb) / half;
+        else if (A.bc_bw == CLM_BC_STATE) Fbw = -Kc * ((psic + G.half_bot()) - psi_bb) / G.half_bot();
       }
       double Fw_dn = Fbw;
       for (int k = 0; k < n; ++k) {
@@ -887,30 +881,37 @@ CLM_HD void richards_column(const StepArgs& A, const Tables& Tb, int s, int n, i
         double Md_extra = 0.0;
         if (k < n - 1) {
           point(B.xv[k + 1], Kn, psin, Dn);
-          aw_up = 0.5 * (Kc + Kn) * inv_dz;
-          Fw_up = -aw_up * ((psin - psic) + dz);
+          aw_up = 0.5 * (Kc + Kn) * (2.0 * G.hinv_gap(k));
+          Fw_up = -aw_up * ((psin - psic) + G.gap(k));
         } else {
+          const double half = G.half_top();
           if (refresh_bc && A.bc_tw == CLM_BC_STATE) Ftw = -Kc * ((psi_tb + half) - psic) / half;
-          // set_dfluxBCdY! (boundary_conditions.jl:375-426): K_N dpsi_N / dz_top
-          if (dflux) Md_extra = -dt * ((Kc * Dc / half) * inv_dz);
+          // set_dfluxBCdY! (boundary_conditions.jl:375-426): K_N dpsi_N / dz_top;
+          // the mixed path's weighted row (stretched) takes it without the 1 / dz
+          if (dflux) Md_extra = (kStr && mixed) ? -dt * (Kc * Dc / half)
+                                                : -dt * ((Kc * Dc / half) * G.inv_width(k));
           Fw_up = Ftw;
         }
-        double Tv = -((Fw_up - Fw_dn) * inv_dz);
+        double Tv = -((Fw_up - Fw_dn) * G.inv_width(k));
         if (q_sink != 0.0) {
           const double twc = B.gv[k] + 0.0 - theta_r;  // U = u for Richards
           Tv -= q_sink * ((twc - nr > kEps ? 1.0 : 0.0) * twc / nr);
         }
         const double f = B.gv[k] + dt * Tv - B.xv[k];
-        sum_f += f;
-        const JT L = (JT)(rdz * aw_dn) * D_prev;
-        const JT U = (k < n - 1) ? (JT)(rdz * aw_up * Dn) : (JT)0;
-        const JT M = (JT)(-rdz * (aw_up + aw_dn) * Dc - 1.0 + Md_extra);
+        sum_f += G.row_w(k) * f;
+        // rows of W; the mixed path on a stretched column uses W's rows times
+        // the layer width (face products dt K_face / gap), whose block
+        // columns sum to -width
+        const double rk = (kStr && mixed) ? dt : rdz(k);
+        const JT L = (JT)(rk * aw_dn) * D_prev;
+        const JT U = (k < n - 1) ? (JT)(rk * aw_up * Dn) : (JT)0;
+        const JT M = (JT)(-rdz(k) * (aw_up + aw_dn) * Dc - 1.0 + Md_extra);
         JT piv;
         if constexpr (mixed) {
           // column sum -1 (+ the MoistureStateBC term of the top column)
-          const JT s_k = (JT)(-1.0 + Md_extra);
+          const JT s_k = (JT)(-G.row_w(k) + Md_extra);
           const JT sp = (k == 0) ? s_k : s_k - U_prev * (sp_prev / piv_prev);
-          piv = sp - ((k < n - 1) ? (JT)(rdz * aw_up) * (JT)Dc : (JT)0);  // L_{k+1}
+          piv = sp - ((k < n - 1) ? (JT)(rk * aw_up) * (JT)Dc : (JT)0);  // L_{k+1}
           U_prev = U;
           sp_prev = sp;
           piv_prev = piv;
@@ -921,7 +922,7 @@ CLM_HD void richards_column(const StepArgs& A, const Tables& Tb, int s, int n, i
         const JT cpk = U * inv;
         J.cp[k] = cpk;
         if constexpr (mixed) {
-          const F2 dpf = ff::mul_f(ff::sub(ff::from_double(f), ff::mul_f(dpf_prev, L)), inv);
+          const F2 dpf = ff::mul_f(ff::sub(ff::from_double(kStr ? G.row_w(k) * f : f), ff::mul_f(dpf_prev, L)), inv);
           J.dp[k] = dpf.hi;
           J.dpl[k] = dpf.lo;
           dpf_prev = dpf;
@@ -946,10 +947,10 @@ CLM_HD void richards_column(const StepArgs& A, const Tables& Tb, int s, int n, i
           const F2 d = ff::sub(F2{J.dp[k], J.dpl[k]}, ff::mul_f(nxt, J.cp[k]));
           J.dp[k] = d.hi;
           J.dpl[k] = d.lo;
-          sd += ff::to_double(d);
+          sd += G.row_w(k) * ff::to_double(d);
           nxt = d;
         }
-        const double corr = dflux ? 0.0 : (sd + sum_f) / n;
+        const double corr = dflux ? 0.0 : (sd + sum_f) / G.wsum();
         for (int k = 0; k < n; ++k) {
           const double d = ff::to_double(F2{J.dp[k], J.dpl[k]}) - corr;
           B.xv[k] -= d;

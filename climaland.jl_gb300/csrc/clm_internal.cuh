@@ -45,6 +45,9 @@ struct StepArgs {
   Layout L;
   const double* z_lo;   // [stride]
   const double* z_hi;   // [stride]
+  // per-layer geometry of stretched columns (clm_set_faces; internal layout),
+  // all null for uniform layers
+  GeoArrays geo{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   const double* prm;    // [CLM_NPARAM_MAX][stride]
   const double* lkap;   // [2][stride] log kappa_sat_unfrozen, log kappa_sat_frozen
   const double* forc[4];  // [CLM_F_NFIELDS][stride] per slot, or null
@@ -74,6 +77,23 @@ struct StepArgs {
   int64_t col0 = 0;     // global index of column 0 (rain-pulse hash)
   int tile_begin = 0;   // the launch's tiles: [tile_begin, tile_end)
   int tile_end = -1;    // -1: through the last tile
+};
+
+// The column's geometry: uniform layers from z_lo, z_hi, or the per-layer
+// arrays of a stretched mesh (A.geo, kStr).
+template <bool kStr>
+struct GeomOf {
+  using type = ColGeom;
+  static CLM_HD ColGeom make(const StepArgs& A, int64_t, int s, int n) {
+    return ColGeom(A.z_lo[s], A.z_hi[s], n);
+  }
+};
+template <>
+struct GeomOf<true> {
+  using type = ColGeomS;
+  static CLM_HD ColGeomS make(const StepArgs& A, int64_t base, int s, int n) {
+    return ColGeomS(A.geo, base, 32, s, A.L.stride, A.z_lo[s], A.z_hi[s], n);
+  }
 };
 
 // Start time and step of a launch: by value, or (CUDA graph replay) read

@@ -97,7 +97,8 @@ __global__ void __launch_bounds__(32, 1)
     double Fw = A.Fw[c], Fe = A.Fe[c];
     uint32_t fl = 0;
     int it = 0;
-    eh_column<double, CM, true>(A, Tb, c, n, c, B, J, t0, dt, nsteps, Fw, Fe, fl, it);
+    const ColGeom G(A.z_lo[c], A.z_hi[c], n);
+    eh_column<double, CM, true>(A, Tb, c, n, c, B, J, G, t0, dt, nsteps, Fw, Fe, fl, it);
     A.Fw[c] = Fw;
     A.Fe[c] = Fe;
     if (flags_out) flags_out[c] = fl;

@@ -1,14 +1,18 @@
 // Launch configuration of the step kernels (clm_step_kernels.cuh) and their
-// van Genuchten instantiations; the Brooks-Corey ones compile in parallel in
-// clm_step_bc.cu.
+// van Genuchten instantiations on uniform columns; the Brooks-Corey ones and
+// those with per-layer geometry compile in parallel in clm_step_bc.cu,
+// clm_step_s.cu and clm_step_bc_s.cu.
 
 #include "clm_step_kernels.cuh"
 
 namespace clm {
 
-void* step_fn_bc(int model, int precision, int src);
-void launch_step_bc(const StepArgs& A, int model, int precision, int grid, dim3 block, size_t smem,
-                    double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream);
+void* step_fn_vg(int model, int precision, int src) { return step_fn_t<VG, false>(model, precision, src); }
+
+void launch_step_vg(const StepArgs& A, int model, int precision, int grid, dim3 block, size_t smem,
+                    double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream) {
+  launch_step_t<VG, false>(A, model, precision, grid, block, smem, scratch, clk, nsteps, stream);
+}
 
 // ---------------------------------------------------------------------------
 // launch configuration
@@ -25,19 +29,23 @@ size_t step_smem_bytes(int model, int precision, int nmax, int wpc) {
   return tab * sizeof(double) + per_layer * (size_t)nmax * kTile * wpc;
 }
 
-static void* step_fn(int model, int precision, int cm, int src = kSrcNone) {
-  return cm == CLM_CM_BROOKS_COREY ? step_fn_bc(model, precision, src) : step_fn_t<VG>(model, precision, src);
+static void* step_fn(int model, int precision, int cm, bool str, int src = kSrcNone) {
+  if (cm == CLM_CM_BROOKS_COREY)
+    return str ? step_fn_bc_s(model, precision, src) : step_fn_bc(model, precision, src);
+  return str ? step_fn_vg_s(model, precision, src) : step_fn_vg(model, precision, src);
 }
 
-// CTAs of `wpc` warps that can be resident on the whole device.
-cudaError_t step_grid(int model, int precision, int cm, int nmax, int wpc, int ntiles, int* grid) {
+// CTAs of `wpc` warps that can be resident on the whole device (the
+// kernels of uniform columns, or with per-layer geometry when `str`).
+cudaError_t step_grid(int model, int precision, int cm, bool str, int nmax, int wpc, int ntiles,
+                      int* grid) {
   const size_t smem = step_smem_bytes(model, precision, nmax, wpc);
-  void* fn = step_fn(model, precision, cm);
+  void* fn = step_fn(model, precision, cm, str);
   cudaError_t err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
   if (model == CLM_MODEL_ENERGY_HYDROLOGY) {  // the same launch shape with a source variant
     for (int src : {kSrcRoots, kSrcAtmos})
-      if ((err = cudaFuncSetAttribute(step_fn(model, precision, cm, src),
+      if ((err = cudaFuncSetAttribute(step_fn(model, precision, cm, str, src),
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
         return err;
   }
@@ -61,10 +69,14 @@ cudaError_t launch_step(const StepArgs& A, int model, int precision, int wpc, in
                         double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream) {
   const size_t smem = step_smem_bytes(model, precision, A.L.nmax, wpc);
   const dim3 block(32 * wpc);
-  if (A.cm == CLM_CM_BROOKS_COREY)
-    launch_step_bc(A, model, precision, grid, block, smem, scratch, clk, nsteps, stream);
-  else
-    launch_step_t<VG>(A, model, precision, grid, block, smem, scratch, clk, nsteps, stream);
+  const bool str = A.geo.z != nullptr;
+  if (A.cm == CLM_CM_BROOKS_COREY) {
+    if (str) launch_step_bc_s(A, model, precision, grid, block, smem, scratch, clk, nsteps, stream);
+    else launch_step_bc(A, model, precision, grid, block, smem, scratch, clk, nsteps, stream);
+  } else {
+    if (str) launch_step_vg_s(A, model, precision, grid, block, smem, scratch, clk, nsteps, stream);
+    else launch_step_vg(A, model, precision, grid, block, smem, scratch, clk, nsteps, stream);
+  }
   return cudaGetLastError();
 }
 

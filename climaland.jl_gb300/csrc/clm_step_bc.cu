@@ -6,11 +6,11 @@
 
 namespace clm {
 
-void* step_fn_bc(int model, int precision, int src) { return step_fn_t<BC>(model, precision, src); }
+void* step_fn_bc(int model, int precision, int src) { return step_fn_t<BC, false>(model, precision, src); }
 
 void launch_step_bc(const StepArgs& A, int model, int precision, int grid, dim3 block, size_t smem,
                     double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream) {
-  launch_step_t<BC>(A, model, precision, grid, block, smem, scratch, clk, nsteps, stream);
+  launch_step_t<BC, false>(A, model, precision, grid, block, smem, scratch, clk, nsteps, stream);
 }
 
 }  // namespace clm

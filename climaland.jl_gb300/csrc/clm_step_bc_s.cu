@@ -1,0 +1,15 @@
+// Step kernels of Brooks-Corey columns with per-layer geometry (stretched
+// meshes, clm_set_faces), in their own translation unit.
+
+#include "clm_step_kernels.cuh"
+
+namespace clm {
+
+void* step_fn_bc_s(int model, int precision, int src) { return step_fn_t<BC, true>(model, precision, src); }
+
+void launch_step_bc_s(const StepArgs& A, int model, int precision, int grid, dim3 block, size_t smem,
+                      double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream) {
+  launch_step_t<BC, true>(A, model, precision, grid, block, smem, scratch, clk, nsteps, stream);
+}
+
+}  // namespace clm

@@ -49,8 +49,8 @@ __host__ __device__ constexpr int eh_scratch_slots(bool mixed) { return mixed ? 
 
 // kSrc: the RootExtraction source (A.rx) or the atmosphere-driven top
 // boundary (A.atm) compiled in; separate kernels so that their registers do
-// not weigh on the step without them.
-template <typename JT, class CM, int kSrc>
+// not weigh on the step without them. kStr: per-layer geometry.
+template <typename JT, class CM, int kSrc, bool kStr>
 __global__ void __launch_bounds__(128, 1)
     eh_step_kernel(StepArgs A, double* __restrict__ scratch, StepClock clk, int nsteps) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -112,7 +112,9 @@ __global__ void __launch_bounds__(128, 1)
       double Fw = A.Fw[s], Fe = A.Fe[s];
       uint32_t flags = 0;
       int iters = 0;
-      eh_column<JT, CM, false, kSrc>(A, Tb, s, n, A.L.perm[s], B, J, t0, dt, nsteps, Fw, Fe, flags, iters);
+      const auto G = GeomOf<kStr>::make(A, base, s, n);
+      eh_column<JT, CM, false, kSrc>(A, Tb, s, n, A.L.perm[s], B, J, G, t0, dt, nsteps, Fw, Fe, flags,
+                                     iters);
       A.Fw[s] = Fw;
       A.Fe[s] = Fe;
       A.flags[s] = flags;
@@ -123,7 +125,7 @@ __global__ void __launch_bounds__(128, 1)
   if (dyn) release_tiles(A.tile_ctr, nwarps);
 }
 
-template <typename JT, class CM>
+template <typename JT, class CM, bool kStr>
 __global__ void __launch_bounds__(128, 1)
     richards_step_kernel(StepArgs A, StepClock clk, int nsteps) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -155,11 +157,13 @@ __global__ void __launch_bounds__(128, 1)
     const int s = tile * kTile + lane;
     const int n = A.L.col_n[s];
     if (n > 0) {
-      B.gv = Col<double>{A.v + A.L.tile_off[tile] + lane, kTile};
+      const int64_t base = A.L.tile_off[tile] + lane;
+      B.gv = Col<double>{A.v + base, kTile};
       double Fw = A.Fw[s];
       uint32_t flags = 0;
       int iters = 0;
-      richards_column<JT, CM>(A, Tb, s, n, A.L.perm[s], B, J, t0, dt, nsteps, Fw, flags, iters);
+      const auto G = GeomOf<kStr>::make(A, base, s, n);
+      richards_column<JT, CM>(A, Tb, s, n, A.L.perm[s], B, J, G, t0, dt, nsteps, Fw, flags, iters);
       A.Fw[s] = Fw;
       A.flags[s] = flags;
       A.iters[s] = iters;
@@ -174,50 +178,70 @@ inline int step_src(const StepArgs& A) {
   return A.atm ? kSrcAtmos : A.rx ? kSrcRoots : kSrcNone;
 }
 
-// The kernel of (model, precision, source variant) for closure CM, and its launch.
-template <class CM>
+// The kernel of (model, precision, source variant) for closure CM and
+// geometry kStr, and its launch.
+template <class CM, bool kStr>
 void* step_fn_t(int model, int precision, int src = kSrcNone) {
   if (model == CLM_MODEL_ENERGY_HYDROLOGY) {
     const bool mx = precision == CLM_PREC_MIXED;
     if (src == kSrcRoots)
-      return mx ? (void*)eh_step_kernel<float, CM, kSrcRoots> : (void*)eh_step_kernel<double, CM, kSrcRoots>;
+      return mx ? (void*)eh_step_kernel<float, CM, kSrcRoots, kStr>
+                : (void*)eh_step_kernel<double, CM, kSrcRoots, kStr>;
     if (src == kSrcAtmos)
-      return mx ? (void*)eh_step_kernel<float, CM, kSrcAtmos> : (void*)eh_step_kernel<double, CM, kSrcAtmos>;
-    return mx ? (void*)eh_step_kernel<float, CM, kSrcNone> : (void*)eh_step_kernel<double, CM, kSrcNone>;
+      return mx ? (void*)eh_step_kernel<float, CM, kSrcAtmos, kStr>
+                : (void*)eh_step_kernel<double, CM, kSrcAtmos, kStr>;
+    return mx ? (void*)eh_step_kernel<float, CM, kSrcNone, kStr>
+              : (void*)eh_step_kernel<double, CM, kSrcNone, kStr>;
   }
-  return precision == CLM_PREC_MIXED ? (void*)richards_step_kernel<float, CM>
-                                     : (void*)richards_step_kernel<double, CM>;
+  return precision == CLM_PREC_MIXED ? (void*)richards_step_kernel<float, CM, kStr>
+                                     : (void*)richards_step_kernel<double, CM, kStr>;
 }
 
-template <typename JT, class CM>
+template <typename JT, class CM, bool kStr>
 void launch_eh_t(const StepArgs& A, int grid, dim3 block, size_t smem, double* scratch,
                  const StepClock& clk, int nsteps, cudaStream_t stream) {
   switch (step_src(A)) {
     case kSrcRoots:
-      eh_step_kernel<JT, CM, kSrcRoots><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
+      eh_step_kernel<JT, CM, kSrcRoots, kStr><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
       break;
     case kSrcAtmos:
-      eh_step_kernel<JT, CM, kSrcAtmos><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
+      eh_step_kernel<JT, CM, kSrcAtmos, kStr><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
       break;
     default:
-      eh_step_kernel<JT, CM, kSrcNone><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
+      eh_step_kernel<JT, CM, kSrcNone, kStr><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
   }
 }
 
-template <class CM>
+template <class CM, bool kStr>
 void launch_step_t(const StepArgs& A, int model, int precision, int grid, dim3 block, size_t smem,
                    double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream) {
   if (model == CLM_MODEL_ENERGY_HYDROLOGY) {
     if (precision == CLM_PREC_MIXED)
-      launch_eh_t<float, CM>(A, grid, block, smem, scratch, clk, nsteps, stream);
+      launch_eh_t<float, CM, kStr>(A, grid, block, smem, scratch, clk, nsteps, stream);
     else
-      launch_eh_t<double, CM>(A, grid, block, smem, scratch, clk, nsteps, stream);
+      launch_eh_t<double, CM, kStr>(A, grid, block, smem, scratch, clk, nsteps, stream);
   } else {
     if (precision == CLM_PREC_MIXED)
-      richards_step_kernel<float, CM><<<grid, block, smem, stream>>>(A, clk, nsteps);
+      richards_step_kernel<float, CM, kStr><<<grid, block, smem, stream>>>(A, clk, nsteps);
     else
-      richards_step_kernel<double, CM><<<grid, block, smem, stream>>>(A, clk, nsteps);
+      richards_step_kernel<double, CM, kStr><<<grid, block, smem, stream>>>(A, clk, nsteps);
   }
 }
+
+// One translation unit per (closure, geometry) instantiates these: the entry
+// points each defines (clm_step.cu, clm_step_bc.cu, clm_step_s.cu,
+// clm_step_bc_s.cu).
+void* step_fn_vg(int model, int precision, int src);
+void* step_fn_bc(int model, int precision, int src);
+void* step_fn_vg_s(int model, int precision, int src);
+void* step_fn_bc_s(int model, int precision, int src);
+void launch_step_vg(const StepArgs& A, int model, int precision, int grid, dim3 block, size_t smem,
+                    double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream);
+void launch_step_bc(const StepArgs& A, int model, int precision, int grid, dim3 block, size_t smem,
+                    double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream);
+void launch_step_vg_s(const StepArgs& A, int model, int precision, int grid, dim3 block, size_t smem,
+                      double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream);
+void launch_step_bc_s(const StepArgs& A, int model, int precision, int grid, dim3 block, size_t smem,
+                      double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream);
 
 }  // namespace clm

@@ -1,0 +1,16 @@
+// Step kernels of van Genuchten columns with per-layer geometry (stretched
+// meshes, clm_set_faces), in their own translation unit so that they compile
+// in parallel with the uniform ones.
+
+#include "clm_step_kernels.cuh"
+
+namespace clm {
+
+void* step_fn_vg_s(int model, int precision, int src) { return step_fn_t<VG, true>(model, precision, src); }
+
+void launch_step_vg_s(const StepArgs& A, int model, int precision, int grid, dim3 block, size_t smem,
+                      double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream) {
+  launch_step_t<VG, true>(A, model, precision, grid, block, smem, scratch, clk, nsteps, stream);
+}
+
+}  // namespace clm

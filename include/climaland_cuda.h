@@ -376,6 +376,22 @@ const char* clm_last_error(const clm_handle* h);
 int clm_set_geometry(clm_handle* h, const double* z_lo, const double* z_hi,
                      const int32_t* offsets);
 
+/* Per-layer geometry of stretched columns. Replaces the mesh of
+ * Column(; zlim, nelements, dz_tuple) (Domains.jl:188-215: ClimaCore's
+ * GeneralizedExponentialStretching, reverse_mode) and of the 3-D domains
+ * built on it (global_domain's default dz_tuple = (10.0, 0.05), Domains.jl:
+ * 1292-1298): z_faces holds each column's n + 1 face coordinates, bottom to
+ * top, column c's at offsets[c] + c + j (the layout of a ClimaCore face
+ * field: parent(coordinate_field(face_space).z) for a column space). The
+ * library derives what ClimaCore's grid and get_Δz (:935-949) derive from
+ * them: centres at the faces' midpoints, layer widths (divergence, column
+ * integrals, thermal_time), centre spacings (gradients), Δz_top and
+ * Δz_bottom (state boundary conditions, the atmosphere-driven boundary),
+ * and sets z_lo / z_hi to the first and last face. Call after
+ * clm_set_geometry (which returns the handle to uniform layers); NULL
+ * returns to uniform layers. Faces must be finite and increasing. */
+int clm_set_faces(clm_handle* h, const double* z_faces);
+
 /* Per-column parameters, nparams rows of ncol (enum clm_param). Replaces
  * RichardsParameters / EnergyHydrologyParameters fields. */
 int clm_set_params(clm_handle* h, const double* soa_params, int32_t nparams);

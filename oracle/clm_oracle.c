@@ -421,6 +421,7 @@ typedef struct {
   double nu_om, nu_quartz, nu_gravel;
   double f_max, f_over, R_sb; /* TOPMODEL (Runoff.jl:198-232)          */
   double depth;               /* model.domain.depth: z_hi - z_lo       */
+  double z_sfc;               /* the top face (Domains.jl:1054)        */
   const clm_config* cfg;
   const clmo_problem* P;
   int c;
@@ -464,9 +465,20 @@ static void col_init(col_t* C, const clmo_problem* P, int c) {
   C->eh = (cfg->model == CLM_MODEL_ENERGY_HYDROLOGY);
   int n = C->n;
   double zlo = P->z_lo[c], zhi = P->z_hi[c];
-  double zf[MAXL + 1];
-  for (int k = 0; k <= n; ++k) zf[k] = zlo + (zhi - zlo) * ((double)k / n);
-  zf[n] = zhi;
+  double zf[MAXL + 1] = {0.0};
+  if (P->z_faces) {
+    /* the caller's mesh (ClimaCore IntervalMesh faces, e.g. from
+     * GeneralizedExponentialStretching): centres are the faces' midpoints,
+     * the layer widths their differences (ClimaCore's FiniteDifferenceGrid) */
+    const double* f = P->z_faces + P->offsets[c] + c;
+    for (int k = 0; k <= n; ++k) zf[k] = f[k];
+    zlo = zf[0];
+    zhi = zf[n];
+  } else {
+    /* Column(; zlim, nelements): IntervalMesh with uniform faces */
+    for (int k = 0; k <= n; ++k) zf[k] = zlo + (zhi - zlo) * ((double)k / n);
+    zf[n] = zhi;
+  }
   for (int k = 0; k < n; ++k) {
     C->z[k] = 0.5 * (zf[k] + zf[k + 1]);
     C->dzc[k] = zf[k + 1] - zf[k];
@@ -491,6 +503,7 @@ static void col_init(col_t* C, const clmo_problem* P, int c) {
     C->hcm = hcm_vg(p[CLM_P_VG_ALPHA * ncol + c], vgn, 1.0 - 1.0 / vgn);
   }
   C->depth = zhi - zlo;
+  C->z_sfc = zhi;
   C->f_max = C->f_over = C->R_sb = 0.0;
   if (P->nparams >= CLM_NPARAM_MAX) {
     C->f_max = p[CLM_P_F_MAX * ncol + c];
@@ -908,7 +921,7 @@ static void atmos_top_bc(const col_t* C, const state_t* Y, cache_t* p) {
   for (int k = 1; k < n; ++k) dz_min = fmin(dz_min, C->dzc[k]);
   double th_alb;
   if (dz_min < thick) {
-    const double z_sfc = P->z_hi[c]; /* the top face (Domains.jl:1054) */
+    const double z_sfc = C->z_sfc;
     double N = 0.0, I = 0.0;
     for (int k = 0; k < n; ++k)
       N += C->dzc[k] * clmo_heaviside(thick + SQRT_EPS, z_sfc - C->z[k]);

@@ -43,6 +43,11 @@ typedef struct clmo_problem {
   const double* atmos;     /* CLM_AT_NFIELDS x ncol drivers of CLM_BC_ATMOS,
                               or NULL                                      */
   clm_atmos_params atm;    /* constants of CLM_BC_ATMOS                    */
+  const double* z_faces;   /* face coordinates, column c's faces at
+                              offsets[c] + c + j, j = 0..n (bottom to top):
+                              a stretched column (Domains.jl:188-215 with
+                              dz_tuple); NULL: n equal layers from z_lo to
+                              z_hi                                         */
 } clmo_problem;
 
 /* ---- pointwise physics (names follow the reference functions) -------- */

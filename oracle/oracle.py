@@ -48,6 +48,7 @@ class _Problem(ctypes.Structure):
         ("root", ctypes.POINTER(ctypes.c_double)),
         ("atmos", ctypes.POINTER(ctypes.c_double)),
         ("atm", A.ClmAtmosParams),
+        ("z_faces", ctypes.POINTER(ctypes.c_double)),
     ]
 
 
@@ -183,6 +184,8 @@ class Oracle:
         P.atmos = A.dptr(keep(atmos)) if atmos is not None else None
         atm = getattr(w, "atmos_params", None) or A.default_atmos_params()
         ctypes.memmove(ctypes.byref(P.atm), ctypes.byref(atm), ctypes.sizeof(A.ClmAtmosParams))
+        zf = getattr(w, "z_faces", None)
+        P.z_faces = A.dptr(keep(zf)) if zf is not None else None
         self.P = P
         self.eh = w.cfg.model == A.CLM_MODEL_ENERGY_HYDROLOGY
 

@@ -10,17 +10,29 @@ perturbation of the input to 1e-8 .. 1e-5 within a few dozen steps. On
 those columns no implementation can agree with the oracle more closely than
 the oracle agrees with itself under rounding. The test therefore measures,
 per column, the oracle's own spread under random 1-ulp noise added to all
-state arrays at every step (several seeds), and requires on every column
-  error <= max(1e-10, 1000 x spread),
+state arrays at every step (8 seeds), and requires on every column
+  error <= max(1e-10, 10 x spread),
 i.e. the bar wherever the oracle reproduces itself; at most 5 % of the
-columns may need the widened bound (error above 1e-10).
+columns may need the widened bound (error above 1e-10). Measured on the
+GB300, the FP64 path's error on such columns is at most 2 x the spread.
+Each test records the excused fraction (columns above 1e-10), printed in
+the session summary.
+
+Mixed path: 1e-8, with the spread measured under per-step noise as large as
+each column's own one-step difference from the oracle (the mixed path
+stepping from the oracle's state, sampled along the oracle's trajectory;
+at least 2^-44, the double-float closures' precision, at most 1e-9). Its
+float Jacobian converges more slowly than the FP64 one on stiff columns, so
+three fixed Newton iterations leave differences up to ~1e-9 per step there;
+the converged root itself is the oracle's (test_gpu_parity.py checks it
+with eight iterations).
 
 Budgets, per column: water and energy close to 1e-12 relative on the GPU
 state, except where the reference itself does not close them
 (MoistureStateBC with a fixed number of Newton iterations: the integrated
 flux uses the boundary flux of the iterate before the last update; columns
 whose three Newton iterations do not converge); there the GPU's defect must
-equal the oracle's to 1e-8 of it, or to 1000 x the spread of the oracle's
+equal the oracle's to 1e-8 of it, or to 10 x the spread of the oracle's
 own defect under the same perturbations.
 """
 import numpy as np
@@ -33,9 +45,14 @@ from climaland_gb300 import device as D
 TOL_STATE = 1e-10
 TOL_BUDGET = 1e-12
 SENSITIVE = 1e-13      # oracle self-spread above which a column is sensitive
-SPREAD_FACTOR = 1000.0  # allowed multiple of the oracle's own spread
+SPREAD_FACTOR = 10.0   # allowed multiple of the oracle's own spread
 MAX_SENSITIVE = 0.05    # at most this fraction of columns may be sensitive
-NSEEDS = 4
+NSEEDS = 8
+NOISE_FLOOR_MIXED = 2.0 ** -44  # the double-float closures' precision
+NOISE_CAP = 1e-9                # calibrated noise never exceeds this
+
+# per-test parity statistics, printed in the session summary (conftest.py)
+SUMMARY = []
 
 
 def require_gpu():
@@ -60,8 +77,8 @@ def _colmax(w, a, b):
 def oracle_run(w, nsteps, oracle_cfg=None, perturb_seed=None, noise=None):
     """The oracle; with perturb_seed, random relative noise of size `noise`
     (default 1 ulp: the rounding differences an independent FP64
-    implementation makes every step) is added to every state array before
-    each step."""
+    implementation makes every step; a scalar or one value per column) is
+    added to every state array before each step."""
     o = O.Oracle(w)
     if oracle_cfg:
         o.set_cfg(**oracle_cfg)
@@ -72,6 +89,8 @@ def oracle_run(w, nsteps, oracle_cfg=None, perturb_seed=None, noise=None):
         return st, fl, it
     rng = np.random.default_rng(perturb_seed)
     eps = np.finfo(np.float64).eps if noise is None else noise
+    if np.ndim(eps):
+        eps = np.repeat(np.asarray(eps, np.float64), w.nlayers)
     for k in range(nsteps):
         for i in (0, 1, 2):
             if st[i] is not None:
@@ -97,6 +116,31 @@ def oracle_spread(w, nsteps, ref_state, oracle_cfg=None, nseeds=NSEEDS, noise=No
     return spread, bspread
 
 
+def step_deviation(w, nsteps, oracle_cfg=None, every=4, **dev_kw):
+    """Per column, the largest one-step difference (the parity fields) between
+    the GPU and the oracle, each stepping from the oracle's state, at every
+    `every`-th step of the oracle's trajectory."""
+    o = O.Oracle(w)
+    if oracle_cfg:
+        o.set_cfg(**oracle_cfg)
+    st = w.copy_state()
+    dev = np.zeros(w.ncol)
+    with D.SoilColumns(w, **dev_kw) as g:
+        for k in range(nsteps):
+            t = w.t0 + k * w.dt
+            sg = None
+            if k % every == 0:
+                g.set_state(*[None if a is None else a.copy() for a in st])
+                g.step(t, w.dt, 1)
+                sg = g.get_state()
+            rc, _, _ = o.step(st, t, w.dt, 1)
+            assert rc == 0, rc
+            if sg is not None:
+                for a, b in zip(_fields(w, st), _fields(w, sg)):
+                    dev = np.maximum(dev, _colmax(w, a, b))
+    return dev
+
+
 def gpu_run(w, nsteps, **dev_kw):
     with D.SoilColumns(w, **dev_kw) as g:
         g.step(w.t0, w.dt, nsteps)
@@ -107,14 +151,20 @@ def gpu_run(w, nsteps, **dev_kw):
 
 
 def check_parity(w, nsteps, oracle_cfg=None, spread=True, tol_state=TOL_STATE, noise=None,
-                 nseeds=NSEEDS, **dev_kw):
+                 nseeds=NSEEDS, name=None, **dev_kw):
     """Run the oracle and the GPU on the same workload and apply the
-    criterion above. Returns a stats dict."""
+    criterion above. noise: None (1 ulp), a relative size, or "calibrated"
+    (each column's own one-step difference, the mixed path). Returns a
+    stats dict, also kept in SUMMARY."""
     so, fo, io = oracle_run(w, nsteps, oracle_cfg)
     sg, fg, ig, Wg, Eg = gpu_run(w, nsteps, **dev_kw)
     ref, got = _fields(w, so), _fields(w, sg)
     errs = [_colmax(w, r, g) for r, g in zip(ref, got)]
     names = ["vartheta_l", "theta_i", "rho_e_int_rel"][: len(errs)]
+    noise_desc = "1 ulp" if noise is None else (noise if isinstance(noise, str) else f"{noise:.3g}")
+    if isinstance(noise, str) and noise == "calibrated":
+        dev = step_deviation(w, nsteps, oracle_cfg, **dev_kw)
+        noise = np.clip(dev, NOISE_FLOOR_MIXED, NOISE_CAP)
     if spread:
         spr, bspr = oracle_spread(w, nsteps, so, oracle_cfg, nseeds=nseeds, noise=noise)
     else:
@@ -122,7 +172,8 @@ def check_parity(w, nsteps, oracle_cfg=None, spread=True, tol_state=TOL_STATE, n
         bspr = [np.zeros(w.ncol), np.zeros(w.ncol)]
     total_spread = np.max(np.stack(spr), axis=0)
     sensitive = total_spread > SENSITIVE
-    stats = {"columns": w.ncol, "sensitive": int(sensitive.sum())}
+    stats = {"columns": w.ncol, "steps": nsteps, "noise": noise_desc, "seeds": nseeds,
+             "sensitive": int(sensitive.sum())}
     excused = np.zeros(w.ncol, bool)
     for nm, e, sp in zip(names, errs, spr):
         excused |= e > tol_state
@@ -135,6 +186,11 @@ def check_parity(w, nsteps, oracle_cfg=None, spread=True, tol_state=TOL_STATE, n
             f"oracle spread) on columns {np.nonzero(bad)[0][:8]} "
             f"(spread {sp[bad][:4]}, error {e[bad][:4]})")
     stats["excused"] = int(excused.sum())
+    stats["excused_frac"] = float(excused.mean())
+    total_err = np.max(np.stack(errs), axis=0)
+    ratio = total_err[excused] / np.maximum(total_spread[excused], 1e-300)
+    stats["excused_err_over_spread_max"] = float(ratio.max()) if excused.any() else 0.0
+    SUMMARY.append((name or w.name, stats))
     assert excused.mean() <= MAX_SENSITIVE, stats
     err_fw = float(np.max(np.abs(so[3] - sg[3])) / max(np.max(np.abs(so[3])), 1e-30))
     stats["intF_w_rel"] = err_fw
