@@ -275,4 +275,195 @@ function step!(h::Handle, Y, t::Real, dt::Real)
     return Y
 end
 
+"""
+    set_faces!(h, z_faces)
+
+Per-layer geometry of stretched columns (`Column(; dz_tuple)`,
+`global_domain`): each column's n + 1 face coordinates, bottom to top, in the
+layout of a face field (`parent(coordinate_field(face_space(space)).z)`),
+or `nothing` for uniform layers.
+"""
+set_faces!(h::Handle, z_faces::Union{Nothing, Vector{Float64}}) =
+    check(h, ccall((:clm_set_faces, libclm), Cint, (Ptr{Cvoid}, Ptr{Float64}),
+        h.ptr, z_faces === nothing ? C_NULL : z_faces))
+
+"The handle's work on a caller's CUDA stream (e.g. `CUDA.stream().handle`), or `nothing` for its own."
+set_stream!(h::Handle, stream) =
+    check(h, ccall((:clm_set_stream, libclm), Cint, (Ptr{Cvoid}, Ptr{Cvoid}),
+        h.ptr, stream === nothing ? C_NULL : stream))
+
+"""
+    set_state_device!(h, ϑ_l, θ_i, ρe_int, ∫F_w, ∫F_e)
+
+The state from device memory: `pointer(parent(field))` of CuArray-backed
+fields (reference layout); copied on the handle's stream.
+"""
+set_state_device!(h::Handle, ϑ_l, θ_i, ρe_int, ∫F_w, ∫F_e) =
+    check(h, ccall((:clm_set_state_device, libclm), Cint,
+        (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}),
+        h.ptr, ϑ_l, θ_i === nothing ? C_NULL : θ_i, ρe_int === nothing ? C_NULL : ρe_int,
+        ∫F_w, ∫F_e === nothing ? C_NULL : ∫F_e))
+
+get_state_device!(h::Handle, ϑ_l, θ_i, ρe_int, ∫F_w, ∫F_e) =
+    check(h, ccall((:clm_get_state_device, libclm), Cint,
+        (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}),
+        h.ptr, ϑ_l, θ_i === nothing ? C_NULL : θ_i, ρe_int === nothing ? C_NULL : ρe_int,
+        ∫F_w, ∫F_e === nothing ? C_NULL : ∫F_e))
+
+"Column budgets `total_water`, `total_energy` of the current state (rre.jl:502-511, energy_hydrology.jl:1282-1320)."
+function budgets(h::Handle)
+    W = Vector{Float64}(undef, h.ncol)
+    E = Vector{Float64}(undef, h.ncol)
+    check(h, ccall((:clm_get_budgets, libclm), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}),
+        h.ptr, W, E))
+    return W, E
+end
+
+"Per-column status flags (CLM_COL_*) and Newton iterations of the last step call."
+function status(h::Handle)
+    flags = Vector{UInt32}(undef, h.ncol)
+    iters = Vector{Int32}(undef, h.ncol)
+    check(h, ccall((:clm_get_status, libclm), Cint, (Ptr{Cvoid}, Ptr{UInt32}, Ptr{Int32}),
+        h.ptr, flags, iters))
+    return flags, iters
+end
+
+# ---- closure level: the functions ClimaLand hands to ClimaTimeSteppers ----
+# Each takes the handle's current state (set_state! / set_state_device!) at
+# time t and writes host arrays in the reference layout.
+
+"""
+    update_aux!(h, t; K, ψ, θ_l, T, κ, Tf, bc)
+
+`make_update_aux` + boundary fluxes (rre.jl:368-380, 111-149;
+energy_hydrology.jl:722-814, 273-298): per-cell aux fields (any may be
+`nothing`) and the boundary fluxes `bc` (4 × ncol: top water, top heat,
+bottom water, bottom heat).
+"""
+function update_aux!(h::Handle, t::Real; K = nothing, ψ = nothing, θ_l = nothing, T = nothing,
+                     κ = nothing, Tf = nothing, bc = nothing)
+    p(x) = x === nothing ? C_NULL : x
+    check(h, ccall((:clm_update_aux, libclm), Cint,
+        (Ptr{Cvoid}, Float64, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+         Ptr{Float64}, Ptr{Float64}),
+        h.ptr, t, p(K), p(ψ), p(θ_l), p(T), p(κ), p(Tf), p(bc)))
+end
+
+"`make_exp_tendency` (models.jl:279-287) into host arrays dY (per cell) and d∫F (per column)."
+exp_tendency!(h::Handle, t::Real, dϑ, dθ_i, dρe, d∫F_w, d∫F_e) =
+    check(h, ccall((:clm_exp_tendency, libclm), Cint,
+        (Ptr{Cvoid}, Float64, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+        h.ptr, t, dϑ, dθ_i === nothing ? C_NULL : dθ_i, dρe === nothing ? C_NULL : dρe,
+        d∫F_w, d∫F_e === nothing ? C_NULL : d∫F_e))
+
+"`make_compute_imp_tendency` (implicit_timestepping.jl:25-28; rre.jl:161-203, energy_hydrology.jl:363-425) after the cache update."
+imp_tendency!(h::Handle, t::Real, dϑ, dθ_i, dρe, d∫F_w, d∫F_e) =
+    check(h, ccall((:clm_imp_tendency, libclm), Cint,
+        (Ptr{Cvoid}, Float64, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+        h.ptr, t, dϑ, dθ_i === nothing ? C_NULL : dθ_i, dρe === nothing ? C_NULL : dρe,
+        d∫F_w, d∫F_e === nothing ? C_NULL : d∫F_e))
+
+"""
+    jacobian!(h, t, dtγ, W_vv, W_ev, W_ee)
+
+`make_compute_jacobian` (rre.jl:391-458; energy_hydrology.jl:466-576):
+W = dtγ ∂T/∂Y - I as tridiagonal blocks, 3 values per cell (lower, diagonal,
+upper): the rows of the `BidiagonalMatrixRow`/`TridiagonalMatrixRow`
+entries of ClimaCore's FieldMatrix at (@name(soil.ϑ_l), @name(soil.ϑ_l)),
+(@name(soil.ρe_int), @name(soil.ϑ_l)) and (@name(soil.ρe_int), @name(soil.ρe_int)).
+"""
+jacobian!(h::Handle, t::Real, dtγ::Real, W_vv, W_ev, W_ee) =
+    check(h, ccall((:clm_jacobian, libclm), Cint,
+        (Ptr{Cvoid}, Float64, Float64, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+        h.ptr, t, dtγ, W_vv, W_ev === nothing ? C_NULL : W_ev, W_ee === nothing ? C_NULL : W_ee))
+
+"The block solve of initialize_jacobian's FieldMatrixSolver (implicit_timestepping.jl:160-171): W δ = f per column."
+solve!(h::Handle, W_vv, W_ev, W_ee, f_v, f_e, δ_v, δ_e) =
+    check(h, ccall((:clm_solve, libclm), Cint,
+        (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+         Ptr{Float64}),
+        h.ptr, W_vv, W_ev === nothing ? C_NULL : W_ev, W_ee === nothing ? C_NULL : W_ee, f_v,
+        f_e === nothing ? C_NULL : f_e, δ_v, δ_e === nothing ? C_NULL : δ_e))
+
+"""
+    closures(h)
+
+The model closures `Simulations.jl:171-199` assembles into
+`CTS.ClimaODEFunction(; T_exp!, T_imp! = ODEFunction(T_imp!; jac_prototype, Wfact), cache_imp!)`,
+evaluated by the library on the soil state. Each takes ClimaLand's
+arguments and moves `Y.soil` through host memory:
+  T_imp!(dY, Y, p, t)          make_compute_imp_tendency
+  T_exp!(dY, Y, p, t)          make_exp_tendency
+  cache_imp!(Y, p, t)          make_update_implicit_cache (aux into p.soil)
+  Wfact!(W, Y, p, dtγ, t)      make_compute_jacobian (W: a NamedTuple of
+                               three 3 × ncells matrices vv, ev, ee)
+"""
+function closures(h::Handle)
+    eh(Y) = hasproperty(Y.soil, :ρe_int)
+    host(f) = vec(Array(parent(f)))
+    function load!(Y)
+        s = Y.soil
+        set_state!(h, host(s.ϑ_l), eh(Y) ? host(s.θ_i) : nothing, eh(Y) ? host(s.ρe_int) : nothing,
+                   host(s.∫F_vol_liq_water_dt), eh(Y) ? host(s.∫F_e_dt) : nothing)
+    end
+    function store!(dY, dv, dti, de, dfw, dfe)
+        s = dY.soil
+        copyto!(parent(s.ϑ_l), dv)
+        copyto!(parent(s.∫F_vol_liq_water_dt), dfw)
+        if dti !== nothing
+            copyto!(parent(s.θ_i), dti)
+            copyto!(parent(s.ρe_int), de)
+            copyto!(parent(s.∫F_e_dt), dfe)
+        end
+        return nothing
+    end
+    function tendency(f)
+        return function (dY, Y, p, t)
+            load!(Y)
+            nc, e = h.ncells, eh(Y)
+            dv, dfw = zeros(nc), zeros(h.ncol)
+            dti, de, dfe = e ? zeros(nc) : nothing, e ? zeros(nc) : nothing, e ? zeros(h.ncol) : nothing
+            f(h, t, dv, dti, de, dfw, dfe)
+            store!(dY, dv, dti, de, dfw, dfe)
+        end
+    end
+    function cache_imp!(Y, p, t)
+        load!(Y)
+        nc = h.ncells
+        K, ψ = zeros(nc), zeros(nc)
+        T = eh(Y) ? zeros(nc) : nothing
+        update_aux!(h, t; K, ψ, T)
+        copyto!(parent(p.soil.ψ), ψ)
+        eh(Y) && copyto!(parent(p.soil.T), T)
+        return nothing
+    end
+    function Wfact!(W, Y, p, dtγ, t)
+        load!(Y)
+        jacobian!(h, t, dtγ, W.vv, eh(Y) ? W.ev : nothing, eh(Y) ? W.ee : nothing)
+        return nothing
+    end
+    return (; T_imp! = tendency(imp_tendency!), T_exp! = tendency(exp_tendency!), cache_imp!, Wfact!)
+end
+
+"""
+    GB300Simulation(landsim, h)
+
+A `LandSimulation` whose soil step runs on the GPU: `step!(sim)` advances
+`landsim._integrator`'s state `u` by one step of size `dt` from `t` through
+the handle (the body of `step!(landsim)`, Simulations.jl:312-314, for a
+soil-only model), then advances the integrator's time, so that the
+simulation's callbacks and diagnostics see the same `u` and `t`.
+"""
+struct GB300Simulation{S}
+    landsim::S
+    h::Handle
+end
+
+function step!(sim::GB300Simulation)
+    integ = sim.landsim._integrator
+    step!(sim.h, integ.u, integ.t, integ.dt)
+    integ.t += integ.dt
+    return sim
+end
+
 end # module

@@ -147,3 +147,119 @@ def test_create_rejects_misplaced_atmos_boundary(lib):
     cfg.ncol, cfg.nlayers = 4, 5
     cfg.bc_bottom_water = A.CLM_BC_ATMOS  # a top-only kind
     assert lib.clm_create(ctypes.byref(cfg), ctypes.byref(h)) == A.CLM_ERR_ARG
+
+
+# ---- the Julia binding's ccall signatures against the header ------------------
+
+def _header_prototypes():
+    """{name: (return type, [argument types])} of every function the header
+    declares (argument names dropped, whitespace normalised)."""
+    text = (REPO / "include" / "climaland_cuda.h").read_text()
+    text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
+    out = {}
+    for m in re.finditer(r"\n\s*([A-Za-z_][A-Za-z0-9_ \*]*?)\b(clm_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", text):
+        ret = " ".join(m.group(1).split())
+        args = [] if m.group(3).strip() in ("", "void") else [" ".join(a.split()) for a in m.group(3).split(",")]
+        types = []
+        for a in args:
+            a = re.sub(r"\s*\*\s*", "* ", a).strip()
+            parts = a.split()
+            # drop the parameter name: the last token unless it is a type word
+            if len(parts) > 1 and not parts[-1].endswith("*") and parts[-1] not in ("int", "double"):
+                parts = parts[:-1]
+            types.append(" ".join(parts).replace("* *", "**").replace(" *", "*"))
+        out[m.group(2)] = (ret, types)
+    return out
+
+
+def _julia_ccalls():
+    """[(name, return type, [argument types])] of every ccall in the binding."""
+    text = (REPO / "climaland.jl_gb300" / "julia" / "ClimaLandGB300.jl").read_text()
+    calls = []
+    for m in re.finditer(r"ccall\(\(:(clm_[a-z0-9_]+),\s*libclm\),\s*([A-Za-z0-9_{}]+),\s*\(", text):
+        i, depth, j = m.end(), 1, m.end()
+        while depth:
+            depth += {"(": 1, ")": -1}.get(text[j], 0)
+            j += 1
+        tup = text[i:j - 1]
+        types, buf, d = [], "", 0
+        for ch in tup:
+            if ch == "," and d == 0:
+                types.append(buf.strip())
+                buf = ""
+                continue
+            d += {"{": 1, "}": -1}.get(ch, 0)
+            buf += ch
+        if buf.strip():
+            types.append(buf.strip())
+        calls.append((m.group(1), m.group(2), types))
+    return calls
+
+
+_C_TO_JULIA = {
+    "int": {"Cint", "Int32"}, "void": {"Cvoid"}, "const char*": {"Cstring"}, "double": {"Float64"},
+    "int32_t": {"Int32"}, "int64_t": {"Int64"}, "uint64_t": {"UInt64"},
+    "clm_handle*": {"Ptr{Cvoid}"}, "const clm_handle*": {"Ptr{Cvoid}"}, "clm_handle**": {"Ref{Ptr{Cvoid}}"},
+    "const clm_config*": {"Ref{ClmConfig}", "Ptr{ClmConfig}"}, "clm_config*": {"Ref{ClmConfig}"},
+    "clm_atmos_params*": {"Ref{ClmAtmosParams}"},
+    "const clm_atmos_params*": {"Ref{ClmAtmosParams}", "Ptr{ClmAtmosParams}"},
+    "double*": {"Ptr{Float64}", "Ref{Float64}", "Ptr{Cvoid}"},
+    "const double*": {"Ptr{Float64}", "Ref{Float64}", "Ptr{Cvoid}"},
+    "int32_t*": {"Ptr{Int32}"}, "const int32_t*": {"Ptr{Int32}"}, "uint32_t*": {"Ptr{UInt32}"},
+    "void*": {"Ptr{Cvoid}"}, "const void*": {"Ptr{Cvoid}"},
+}
+
+
+def test_julia_ccalls_match_the_header():
+    """Every ccall of the Julia binding names a header function with the same
+    number of arguments, and each Julia argument type is one that ccall
+    converts to the header's C type (pointers of the right element type, or
+    Ptr{Cvoid} for device memory; integer widths exact)."""
+    protos = _header_prototypes()
+    calls = _julia_ccalls()
+    assert len(calls) >= 25
+    wrapped = set()
+    for name, ret, types in calls:
+        assert name in protos, name
+        cret, cargs = protos[name]
+        assert ret in _C_TO_JULIA[cret], (name, ret, cret)
+        assert len(types) == len(cargs), (name, types, cargs)
+        for jt, ct in zip(types, cargs):
+            assert jt in _C_TO_JULIA[ct], (name, jt, ct)
+        wrapped.add(name)
+    # the closure-level entry points a ClimaTimeSteppers host binds
+    for name in ("clm_update_aux", "clm_exp_tendency", "clm_imp_tendency", "clm_jacobian", "clm_solve",
+                 "clm_get_budgets", "clm_get_status", "clm_set_faces", "clm_step", "clm_set_state",
+                 "clm_get_state", "clm_set_state_device"):
+        assert name in wrapped, name
+
+
+def test_julia_structs_match_the_header_offsets():
+    """ClmConfig, ClmEarthParams and ClmAtmosParams: each Julia field at the C
+    offset (natural alignment, as Julia lays out isbits fields)."""
+    text = (REPO / "climaland.jl_gb300" / "julia" / "ClimaLandGB300.jl").read_text()
+    size = {"Int32": 4, "Int64": 8, "UInt64": 8, "Float64": 8}
+    layouts = {}
+
+    def layout(name):
+        if name in layouts:
+            return layouts[name]
+        body = re.search(r"(?:mutable )?struct %s\n(.*?)\n(?:\s*%s\(\) = new\(\)\n)?end" % (name, name), text, re.S).group(1)
+        off, fields, align = 0, [], 1
+        for fn, ft in re.findall(r"^\s*([A-Za-z_0-9]+)::([A-Za-z0-9]+)", body, re.M):
+            sz, al = (size[ft], size[ft]) if ft in size else layout(ft)[1:3]
+            off = (off + al - 1) // al * al
+            fields.append((fn, off))
+            off += sz
+            align = max(align, al)
+        total = (off + align - 1) // align * align
+        layouts[name] = (fields, total, align)
+        return layouts[name]
+
+    for jname, cstruct in (("ClmConfig", A.ClmConfig), ("ClmEarthParams", A.ClmEarthParams),
+                           ("ClmAtmosParams", A.ClmAtmosParams)):
+        fields, total, _ = layout(jname)
+        assert [f for f, _ in fields] == [f for f, _ in cstruct._fields_], jname
+        for fn, off in fields:
+            assert getattr(cstruct, fn).offset == off, (jname, fn)
+        assert total == ctypes.sizeof(cstruct), jname

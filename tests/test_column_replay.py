@@ -45,8 +45,10 @@ def _lib():
     return ctypes.CDLL(str(OUT))
 
 
-def replay(w, nsteps, t0=None, **cfgkw):
-    """The column code on the host: (state, flags, iterations) after nsteps."""
+def replay(w, nsteps, t0=None, guess=None, **cfgkw):
+    """The column code on the host: (state, flags, iterations) after nsteps.
+    guess: (vartheta_l, rho_e_int) per-cell float32 Newton starting
+    increments, or None."""
     L = _lib()
     cfg = A.ClmConfig.from_buffer_copy(w.cfg)
     for k, v in cfgkw.items():
@@ -72,13 +74,18 @@ def replay(w, nsteps, t0=None, **cfgkw):
     fl = np.zeros(w.ncol, np.uint32)
     it = np.zeros(w.ncol, np.int32)
     t = w.t0 if t0 is None else t0
+    gp = [None, None]
+    if guess is not None:
+        g32 = [np.ascontiguousarray(g, np.float32) for g in guess]
+        keep += g32
+        gp = [g.ctypes.data_as(ctypes.POINTER(ctypes.c_float)) for g in g32]
     rc = L.clmr_step(ctypes.byref(cfg), ctypes.c_int(w.ncol), off.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
                      d(w.z_lo), d(w.z_hi), d(w.z_faces), prm.ctypes.data_as(_DP), ctypes.c_int(prm.shape[0]), fp,
                      d(w.root), d(w.atmos), ctypes.byref(ap),
                      *[None if a is None else a.ctypes.data_as(_DP) for a in st],
                      ctypes.c_double(t), ctypes.c_double(w.dt), ctypes.c_int(nsteps),
                      fl.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
-                     it.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+                     it.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), *gp)
     assert rc == 0
     return st, fl, it
 
