@@ -134,16 +134,27 @@ class ClmAtmosParams(ctypes.Structure):
     _fields_ = [(n, ctypes.c_double) for n in (
         "stefan", "gas_constant", "molmass_dryair", "molmass_water", "D_vapor", "LH_v0", "LH_s0",
         "cp_d", "cp_v", "T_triple", "press_triple", "von_karman", "Pr_0", "a_m", "a_h", "b_m", "b_h",
-        "zeta_max")] + [("iterations", ctypes.c_int32), ("pad", ctypes.c_int32)]
+        "zeta_max")] + [("iterations", ctypes.c_int32), ("universal_functions", ctypes.c_int32),
+                        ("gryanik_b_m", ctypes.c_double), ("gryanik_b_h", ctypes.c_double)]
 
 
-# Python twin of clm_atmos_params_default (ClimaParams values; Businger-Dyer).
+# Python twin of clm_atmos_params_default (ClimaParams values; Gryanik et al.
+# 2020 on the stable side, Businger-Dyer on the unstable side).
 DEFAULT_ATMOS = dict(
     stefan=5.670374419e-8, gas_constant=8.3144598, molmass_dryair=0.02897,
     molmass_water=0.01801528, D_vapor=2.5e-5, LH_v0=2500800.0, LH_s0=2834400.0, cp_d=1004.5,
-    cp_v=1859.0, T_triple=273.16, press_triple=611.657, von_karman=0.4, Pr_0=0.74, a_m=4.7,
-    a_h=4.7, b_m=15.0, b_h=9.0, zeta_max=100.0, iterations=8,
+    cp_v=1859.0, T_triple=273.16, press_triple=611.657, von_karman=0.4, Pr_0=0.98, a_m=5.0,
+    a_h=5.0, b_m=15.0, b_h=9.0, zeta_max=100.0, iterations=8, universal_functions=1,
+    gryanik_b_m=0.3, gryanik_b_h=0.4,
 )
+# Businger-Dyer on both sides (CLM_UF_BUSINGER): Businger et al. (1971)
+BUSINGER_ATMOS = dict(DEFAULT_ATMOS, Pr_0=0.74, a_m=4.7, a_h=4.7, universal_functions=0,
+                      gryanik_b_m=0.0, gryanik_b_h=0.0)
+
+
+# enum clm_universal_functions
+CLM_UF_BUSINGER = 0
+CLM_UF_GRYANIK = 1
 
 
 def default_atmos_params() -> "ClmAtmosParams":

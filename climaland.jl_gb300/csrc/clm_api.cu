@@ -897,9 +897,15 @@ void clm_atmos_params_default(clm_atmos_params* a) {
   a->T_triple = 273.16;
   a->press_triple = 611.657;
   a->von_karman = 0.4;
-  a->Pr_0 = 0.74;
-  a->a_m = 4.7;
-  a->a_h = 4.7;
+  // ClimaParams' Gryanik coefficients (Gryanik et al. 2020), the
+  // reference's universal functions; Businger-Dyer's b_m, b_h on the
+  // unstable side
+  a->universal_functions = CLM_UF_GRYANIK;
+  a->Pr_0 = 0.98;
+  a->a_m = 5.0;
+  a->a_h = 5.0;
+  a->gryanik_b_m = 0.3;
+  a->gryanik_b_h = 0.4;
   a->b_m = 15.0;
   a->b_h = 9.0;
   a->zeta_max = 100.0;
@@ -927,6 +933,11 @@ int clm_set_atmos(clm_handle* h, const clm_atmos_params* prm, const double* d, i
   const double fin[] = {a.LH_v0, a.LH_s0, a.a_m, a.a_h, a.b_m, a.b_h};
   for (double x : fin)
     if (!std::isfinite(x) || x < 0) return fail(h, CLM_ERR_ARG, "invalid clm_atmos_params constant");
+  if (a.universal_functions != CLM_UF_BUSINGER && a.universal_functions != CLM_UF_GRYANIK)
+    return fail(h, CLM_ERR_ARG, "universal_functions must be CLM_UF_BUSINGER or CLM_UF_GRYANIK");
+  if (a.universal_functions == CLM_UF_GRYANIK && (!(a.gryanik_b_m > 0) || !(a.gryanik_b_h > 0) ||
+                                                  !std::isfinite(a.gryanik_b_m) || !std::isfinite(a.gryanik_b_h)))
+    return fail(h, CLM_ERR_ARG, "invalid Gryanik coefficients");
   if (a.iterations < 1 || a.iterations > 1000) return fail(h, CLM_ERR_ARG, "iterations must be in [1, 1000]");
   const int ncol = h->ncol;
   for (int64_t i = 0; i < (int64_t)nfields * ncol; ++i)

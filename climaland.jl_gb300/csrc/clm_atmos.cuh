@@ -16,9 +16,12 @@
 //   soil conductance   D_vapor / max(dsl, eps), dsl the dry-layer thickness
 //                      of Swenson et al. 2012 (:1338-1368);
 //   turbulent fluxes   Monin-Obukhov similarity at point values with the
-//                      Businger-Dyer functions: zeta = dz / L_MO from
-//                      zeta F_h = Ri_b F_m^2 (stable: the quadratic's root;
-//                      unstable: Newton steps), at most `iterations` steps
+//                      reference's universal functions (Gryanik et al. 2020
+//                      on the stable side, Businger-Dyer on the unstable
+//                      side; Businger-Dyer on both with CLM_UF_BUSINGER):
+//                      zeta = dz / L_MO from zeta F_h = Ri_b F_m^2 (stable
+//                      Businger-Dyer: the quadratic's root; otherwise Newton
+//                      steps), at most `iterations` steps
 //                      (fewer once zeta moves by <= 1e-12 (1 + |zeta|)),
 //                      the surface humidity re-evaluated from the
 //                      heat conductance in each (update_q_vap_sfc_at_a_point,
@@ -52,6 +55,9 @@ struct AtmosK {
   double Mw_over_R;          // M_w / R (Kelvin factor)
   double Pr_0, a_m, a_h, a_h_over_Pr, b_m, b_h, zeta_max;
   int iterations;
+  int gryanik;               // stable side: Gryanik et al. (2020) instead of Businger-Dyer
+  double gb_m, gb_h;         // Gryanik's b_m, b_h
+  double g3am, gah;          // 3 a_m / gb_m, a_h / gb_h
   // saturation vapour pressure, liquid [0] / ice [1]:
   // p_v = p_tr exp(ex ln(T / T_tr) + cc (1 / T_tr - 1 / T))
   double ex[2], cc[2];
@@ -78,6 +84,13 @@ inline AtmosK make_atmos_k(const clm_atmos_params& a, const clm_earth_params& e)
   K.b_h = a.b_h;
   K.zeta_max = a.zeta_max;
   K.iterations = a.iterations;
+  K.gryanik = a.universal_functions == CLM_UF_GRYANIK;
+  if (K.gryanik) {
+    K.gb_m = a.gryanik_b_m;
+    K.gb_h = a.gryanik_b_h;
+    K.g3am = 3.0 * a.a_m / a.gryanik_b_m;
+    K.gah = a.a_h / a.gryanik_b_h;
+  }
   const double LH0[2] = {a.LH_v0, a.LH_s0};
   const double cpc[2] = {e.cp_l, e.cp_i};
   for (int i = 0; i < 2; ++i) {
@@ -100,7 +113,8 @@ CLM_HD double q_sat(const Tables& Tb, const AtmosK& K, double T, double rho, int
   return pv_over_Rv / (rho * T);
 }
 
-// Businger-Dyer integrated stability functions
+// Businger-Dyer integrated stability functions (the stable side of
+// CLM_UF_BUSINGER; the unstable side of both families)
 CLM_HD double psi_m(const Tables& Tb, const AtmosK& K, double zeta) {
   if (zeta >= 0.0) return -K.a_m * zeta;
   const double x = sqrt(sqrt(1.0 - K.b_m * zeta));
@@ -209,7 +223,17 @@ CLM_HD AtmosOut atmos_bc(const Tables& Tb, const AtmosK& K, const Earth& E, cons
     // two logarithms and arctangents of each pair combine into one
     // (atan x' - atan x = atan((x' - x) / (1 + x x')) for x, x' >= 1)
     double F_m, F_h, dF_m = 0.0, dF_h = 0.0;
-    if (zeta >= 0.0) {
+    if (zeta >= 0.0 && K.gryanik) {
+      // Gryanik et al. (2020): psi_m = -3 a_m / b_m ((1 + b_m zeta)^(1/3) - 1),
+      // psi_h = -a_h / b_h ln(1 + b_h zeta); psi' = -a_m (1 + b_m zeta)^(-2/3),
+      // -a_h / (1 + b_h zeta)
+      const double c = cbrt(1.0 + K.gb_m * zeta), cp = cbrt(1.0 + K.gb_m * (zeta * rm));
+      const double u = 1.0 + K.gb_h * zeta, up = 1.0 + K.gb_h * (zeta * rb);
+      F_m = lm + K.g3am * (c - cp);
+      F_h = K.Pr_0 * (lh + K.gah * fm::log(Tb, u * fm::rcp(up)));
+      dF_m = K.a_m * (fm::rcp(c * c) - rm * fm::rcp(cp * cp));
+      dF_h = K.Pr_0 * K.a_h * (fm::rcp(u) - rb * fm::rcp(up));
+    } else if (zeta >= 0.0) {
       F_m = lm - psi_m(Tb, K, zeta) + psi_m(Tb, K, zeta * rm);
       F_h = K.Pr_0 * (lh - psi_h(Tb, K, zeta) + psi_h(Tb, K, zeta * rb));
     } else {
@@ -236,15 +260,20 @@ CLM_HD AtmosOut atmos_bc(const Tables& Tb, const AtmosK& K, const Earth& E, cons
     const double thv_sfc = sf.T * (1.0 + K.delta * q_sfc);
     const double Ri = gU * (thv_air - thv_sfc) * fm::rcp(thv_sfc);
     double zn;
-    if (Ri >= 0.0) {
+    if (Ri >= 0.0 && (!K.gryanik || zeta <= 0.0)) {
+      // Businger-Dyer: the exact root; Gryanik: its small-zeta form as the
+      // start of the Newton steps
       zn = stable_zeta(K, Ri, lm, lh, rm, rb);
-    } else if (zeta >= 0.0) {
+    } else if (Ri < 0.0 && zeta >= 0.0) {
       zn = Ri * lm * lm * fm::rcp(K.Pr_0 * lh);  // one fixed-point step from 0
     } else {
       // Newton on r = zeta F_h - Ri F_m^2 at fixed Ri
       const double r = zeta * F_h - Ri * F_m * F_m;
       const double dr = F_h + zeta * dF_h - 2.0 * Ri * F_m * dF_m;
-      zn = fmin(fmax(zeta - r * fm::rcp(dr), -K.zeta_max), 0.0);
+      if (Ri < 0.0)
+        zn = fmin(fmax(zeta - r * fm::rcp(dr), -K.zeta_max), 0.0);
+      else
+        zn = dr > 0.0 ? fmin(fmax(zeta - r * fm::rcp(dr), 0.0), K.zeta_max) : K.zeta_max;
     }
     done = fabs(zn - zeta) <= 1e-12 * (1.0 + fabs(zeta));
     zeta = zn;

@@ -184,11 +184,16 @@ mutable struct ClmAtmosParams
     b_h::Float64
     zeta_max::Float64
     iterations::Int32
-    pad::Int32
+    universal_functions::Int32   # CLM_UF_BUSINGER or CLM_UF_GRYANIK
+    gryanik_b_m::Float64
+    gryanik_b_h::Float64
 end
 
+const CLM_UF_BUSINGER = Int32(0)
+const CLM_UF_GRYANIK = Int32(1)
+
 function atmos_params_default()
-    a = ClmAtmosParams(zeros(18)..., Int32(0), Int32(0))
+    a = ClmAtmosParams(zeros(18)..., Int32(0), Int32(0), 0.0, 0.0)
     ccall((:clm_atmos_params_default, libclm), Cvoid, (Ref{ClmAtmosParams},), a)
     return a
 end

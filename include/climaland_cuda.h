@@ -256,25 +256,40 @@ enum clm_atmos_field {
   CLM_AT_NFIELDS = 20
 };
 
+/* Universal functions of the similarity solve (clm_atmos_params). */
+enum clm_universal_functions {
+  CLM_UF_BUSINGER = 0, /* Businger-Dyer on both sides of neutral (Businger et
+                          al. 1971; Paulson 1970 integral forms)            */
+  CLM_UF_GRYANIK = 1   /* the reference's UF.GryanikParams
+                          (src/shared_utilities/Parameters.jl:83): Gryanik
+                          et al. (2020) on the stable side, Businger-Dyer on
+                          the unstable side; the default                   */
+};
+
 /* Constants of the atmosphere-driven boundary (ClimaParams names). The
  * turbulent fluxes follow Monin-Obukhov similarity theory at point values
- * with the Businger-Dyer stability functions (Businger et al. 1971; as
- * restated here, since SurfaceFluxes.jl is not part of the reference
- * sources):
+ * (as restated here from the published formulations, since SurfaceFluxes.jl
+ * is not part of the reference sources):
  *   U = max(|u|, gustiness), dz = h_air, zeta = dz / L_MO,
  *   F_m = ln(dz/z_0m) - psi_m(zeta) + psi_m(zeta z_0m/dz),
  *   F_h = Pr_0 (ln(dz/z_0b) - psi_h(zeta) + psi_h(zeta z_0b/dz)),
- *   psi_m = -a_m zeta, psi_h = -a_h zeta / Pr_0 (zeta >= 0);
+ *   unstable (zeta < 0), Businger-Dyer:
  *   psi_m = 2 ln((1+x)/2) + ln((1+x^2)/2) - 2 atan x + pi/2, x = (1 - b_m zeta)^(1/4),
- *   psi_h = 2 ln((1+y)/2), y = (1 - b_h zeta)^(1/2) (zeta < 0);
+ *   psi_h = 2 ln((1+y)/2), y = (1 - b_h zeta)^(1/2);
+ *   stable (zeta >= 0), Businger-Dyer: psi_m = -a_m zeta, psi_h = -a_h zeta / Pr_0;
+ *   stable, Gryanik et al. (2020), phi_m = 1 + a_m zeta / (1 + gb_m zeta)^(2/3),
+ *   phi_h = Pr_0 (1 + a_h zeta / (1 + gb_h zeta)):
+ *   psi_m = -3 a_m / gb_m ((1 + gb_m zeta)^(1/3) - 1),
+ *   psi_h = -a_h / gb_h ln(1 + gb_h zeta) (gb_m, gb_h: gryanik_b_m, gryanik_b_h);
  *   u* = kappa U / F_m, g_h = kappa u* / F_h; at most `iterations` steps from
  *   zeta = 0 (a column stops once a step moves zeta by <= 1e-12 (1 + |zeta|)),
  *   each re-evaluating F_m, F_h, g_h, q_sfc and
  *   Ri_b = g dz (theta_v,air - theta_v,sfc) / (theta_v,sfc U^2), then solving
- *   zeta F_h(zeta) = Ri_b F_m(zeta)^2 for the next zeta: for Ri_b >= 0 exactly
- *   (a quadratic with the linear stable functions; zeta_max above the
- *   critical Richardson number), for Ri_b < 0 by a Newton step (the first
- *   from Ri_b ln(dz/z_0m)^2 / (Pr_0 ln(dz/z_0b))), clamped to [-zeta_max, 0];
+ *   zeta F_h(zeta) = Ri_b F_m(zeta)^2 for the next zeta: for Ri_b >= 0 with
+ *   Businger-Dyer exactly (a quadratic with the linear stable functions;
+ *   zeta_max above the critical Richardson number), otherwise by a Newton
+ *   step at fixed Ri_b (the first unstable one from Ri_b ln(dz/z_0m)^2 /
+ *   (Pr_0 ln(dz/z_0b))), clamped to [-zeta_max, 0] or [0, zeta_max];
  *   theta_v,air = (T_air + g dz / cp_d)(1 + (R_v/R_d - 1) q_air),
  *   theta_v,sfc = T_sfc (1 + (R_v/R_d - 1) q_sfc), and q_sfc from g_h by the
  *   reference's update_q_vap_sfc_at_a_point
@@ -293,10 +308,12 @@ typedef struct clm_atmos_params {
   double T_triple;        /* K                                             */
   double press_triple;    /* Pa                                            */
   double von_karman;
-  double Pr_0, a_m, a_h, b_m, b_h; /* Businger-Dyer                        */
+  double Pr_0, a_m, a_h;  /* Pr_0 and the stable-side a_m, a_h            */
+  double b_m, b_h;        /* unstable-side Businger-Dyer b_m, b_h          */
   double zeta_max;        /* |zeta| bound of the iteration                 */
   int32_t iterations;     /* similarity iterations (>= 1; default 8)       */
-  int32_t pad;
+  int32_t universal_functions; /* enum clm_universal_functions             */
+  double gryanik_b_m, gryanik_b_h; /* stable-side b_m, b_h of CLM_UF_GRYANIK */
 } clm_atmos_params;
 
 /* Diagnostics of clm_atmos_fluxes (row f of ncol): the reference's

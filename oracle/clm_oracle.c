@@ -686,9 +686,12 @@ void clmo_atmos_params_default(clm_atmos_params* a) {
   a->T_triple = 273.16;
   a->press_triple = 611.657;
   a->von_karman = 0.4;
-  a->Pr_0 = 0.74;
-  a->a_m = 4.7;
-  a->a_h = 4.7;
+  a->universal_functions = CLM_UF_GRYANIK;
+  a->Pr_0 = 0.98;
+  a->a_m = 5.0;
+  a->a_h = 5.0;
+  a->gryanik_b_m = 0.3;
+  a->gryanik_b_h = 0.4;
   a->b_m = 15.0;
   a->b_h = 9.0;
   a->zeta_max = 100.0;
@@ -721,6 +724,20 @@ double clmo_soil_conductance(double S_l, double S_c, double d_ds, double p,
                              double alpha, double D_vapor) {
   double dsl = clmo_dry_soil_layer_thickness(S_l, alpha * S_c, d_ds, p);
   return D_vapor / fmax(dsl, EPS64);
+}
+
+/* Gryanik et al. (2020) stable-side integrated stability functions, in the
+ * convention F_h = Pr_0 (ln(dz/z_0b) - psi_h(zeta) + psi_h(zeta z_0b/dz)):
+ * phi_m = 1 + a_m zeta / (1 + b_m zeta)^(2/3) gives
+ * psi_m = -3 a_m / b_m ((1 + b_m zeta)^(1/3) - 1); phi_h = Pr_0 (1 + a_h
+ * zeta / (1 + b_h zeta)) gives psi_h = -a_h / b_h ln(1 + b_h zeta), with
+ * b_m, b_h = gryanik_b_m, gryanik_b_h. Gryanik, V. M., C. Lupkes, A. Grachev
+ * and D. Sidorenko (2020), J. Atmos. Sci. 77, 2687-2716. */
+double clmo_gryanik_psi_m(double zeta, const clm_atmos_params* a) {
+  return -3.0 * a->a_m / a->gryanik_b_m * (cbrt(1.0 + a->gryanik_b_m * zeta) - 1.0);
+}
+double clmo_gryanik_psi_h(double zeta, const clm_atmos_params* a) {
+  return -a->a_h / a->gryanik_b_h * log(1.0 + a->gryanik_b_h * zeta);
 }
 
 /* Businger-Dyer integrated stability functions */
@@ -765,6 +782,96 @@ static double stable_zeta(const clm_atmos_params* a, double Ri, double lm,
   return fmin(fmax(z, 0.0), a->zeta_max);
 }
 
+/* The stability functions of the configured family (zeta >= 0: Businger-
+ * Dyer or Gryanik; zeta < 0: Businger-Dyer) and d psi / d zeta. */
+static double uf_psi_m(double zeta, const clm_atmos_params* a) {
+  if (zeta >= 0.0 && a->universal_functions == CLM_UF_GRYANIK) return clmo_gryanik_psi_m(zeta, a);
+  return clmo_businger_psi_m(zeta, a);
+}
+static double uf_psi_h(double zeta, const clm_atmos_params* a) {
+  if (zeta >= 0.0 && a->universal_functions == CLM_UF_GRYANIK) return clmo_gryanik_psi_h(zeta, a);
+  return clmo_businger_psi_h(zeta, a);
+}
+static double uf_dpsi_m(double zeta, const clm_atmos_params* a) {
+  if (zeta >= 0.0) /* Gryanik: -a_m (1 + b_m zeta)^(-2/3); Businger: -a_m */
+    return a->universal_functions == CLM_UF_GRYANIK
+               ? -a->a_m / pow(1.0 + a->gryanik_b_m * zeta, 2.0 / 3.0) : -a->a_m;
+  return dpsi_m(zeta, a);
+}
+static double uf_dpsi_h(double zeta, const clm_atmos_params* a) {
+  if (zeta >= 0.0)
+    return a->universal_functions == CLM_UF_GRYANIK ? -a->a_h / (1.0 + a->gryanik_b_h * zeta)
+                                                    : -a->a_h / a->Pr_0;
+  return dpsi_h(zeta, a);
+}
+
+/* Monin-Obukhov similarity at point values (the header's clm_atmos_params
+ * comment): `iterations` steps from zeta = 0, each evaluating F_m, F_h, g_h,
+ * the surface humidity (q_update, or thv_sfc fixed when q_update is NULL)
+ * and Ri_b, then the next zeta from zeta F_h = Ri_b F_m^2 at fixed Ri_b
+ * (exact for the linear Businger-Dyer stable functions, else one Newton
+ * step). out: zeta, F_m, F_h, g_h, q_sfc, u*. */
+typedef double (*mo_q_fn)(double g_h, const void* ctx);
+static void mo_solve(const clm_atmos_params* a, double grav, double dz, double U, double z0m,
+                     double z0b, double thv_air, double T_sfc, double delta, double q0,
+                     mo_q_fn q_update, const void* ctx, double thv_sfc_fixed, double out[6]) {
+  const double lm = log(dz / z0m), lh = log(dz / z0b);
+  const double rm = z0m / dz, rb = z0b / dz;
+  const int gry = a->universal_functions == CLM_UF_GRYANIK;
+  double zeta = 0.0, F_m = 0.0, F_h = 0.0, g_h = 0.0, q_sfc = q0, ustar = 0.0;
+  int done = 0; /* the last step moved zeta by at most 1e-12 (1 + |zeta|) */
+  for (int it = 0;; ++it) {
+    F_m = lm - uf_psi_m(zeta, a) + uf_psi_m(zeta * rm, a);
+    F_h = a->Pr_0 * (lh - uf_psi_h(zeta, a) + uf_psi_h(zeta * rb, a));
+    ustar = a->von_karman * U / F_m;
+    g_h = a->von_karman * ustar / F_h;
+    if (q_update) q_sfc = q_update(g_h, ctx);
+    if (it >= a->iterations || done) break;
+    const double thv_sfc = q_update ? T_sfc * (1.0 + delta * q_sfc) : thv_sfc_fixed;
+    const double Ri = grav * dz * (thv_air - thv_sfc) / (thv_sfc * U * U);
+    double zn;
+    if (Ri >= 0.0 && (!gry || zeta <= 0.0)) {
+      /* Businger-Dyer: the exact root; Gryanik: its small-zeta form as the
+       * start of the Newton steps */
+      zn = stable_zeta(a, Ri, lm, lh, rm, rb);
+    } else if (Ri < 0.0 && zeta >= 0.0) {
+      zn = Ri * lm * lm / (a->Pr_0 * lh); /* one fixed-point step from 0 */
+    } else { /* Newton on r = zeta F_h - Ri F_m^2 at fixed Ri */
+      const double dF_m = -uf_dpsi_m(zeta, a) + rm * uf_dpsi_m(zeta * rm, a);
+      const double dF_h = a->Pr_0 * (-uf_dpsi_h(zeta, a) + rb * uf_dpsi_h(zeta * rb, a));
+      const double r = zeta * F_h - Ri * F_m * F_m;
+      const double dr = F_h + zeta * dF_h - 2.0 * Ri * F_m * dF_m;
+      if (Ri < 0.0)
+        zn = fmin(fmax(zeta - r / dr, -a->zeta_max), 0.0);
+      else
+        zn = dr > 0.0 ? fmin(fmax(zeta - r / dr, 0.0), a->zeta_max) : a->zeta_max;
+    }
+    done = fabs(zn - zeta) <= 1e-12 * (1.0 + fabs(zeta));
+    zeta = zn;
+  }
+  out[0] = zeta;
+  out[1] = F_m;
+  out[2] = F_h;
+  out[3] = g_h;
+  out[4] = q_sfc;
+  out[5] = ustar;
+}
+
+/* The similarity solve alone at a fixed surface virtual potential
+ * temperature (for the known-answer tests). out: zeta, F_m, F_h, g_h, u*. */
+int clmo_similarity(const clm_atmos_params* a, double grav, double dz, double U, double z0m,
+                    double z0b, double thv_air, double thv_sfc, double* out) {
+  if (!a || !out || !(dz > z0m) || !(dz > z0b) || !(U > 0)) return 1;
+  double o[6];
+  mo_solve(a, grav, dz, U, z0m, z0b, thv_air, 0.0, 0.0, 0.0, NULL, NULL, thv_sfc, o);
+  out[0] = o[0];
+  out[1] = o[1];
+  out[2] = o[2];
+  out[3] = o[3];
+  out[4] = o[5];
+  return 0;
+}
+
 /* S_c of the closure (retention_models.jl:42, :64) */
 static double hcm_S_c(const hcm_t* h) {
   if (h->bc) return pow(1.0 + 1.0 / h->c, -h->c);
@@ -779,6 +886,13 @@ static double q_sfc_update(double g_h, double q_air, double T_sfc, double Tf,
     return qsat;
   }
   return (g_soil / g_h * qsat + q_air) / (1.0 + g_soil / g_h);
+}
+typedef struct {
+  double q_air, T_sfc, Tf, g_soil, beta_ice, qsat;
+} q_ctx_t;
+static double q_sfc_of(double g_h, const void* ctx) {
+  const q_ctx_t* q = (const q_ctx_t*)ctx;
+  return q_sfc_update(g_h, q->q_air, q->T_sfc, q->Tf, q->g_soil, q->beta_ice, q->qsat);
 }
 
 /* Runoff of AtmosDrivenFluxBC on an EnergyHydrology column
@@ -879,36 +993,12 @@ static void atmos_top_bc(const col_t* C, const state_t* Y, cache_t* p) {
   const double dz = h_air;
   const double U = fmax(fabs(u_air), AT(CLM_AT_GUSTINESS));
   const double z0m = AT(CLM_AT_Z_0M), z0b = AT(CLM_AT_Z_0B);
-  const double lm = log(dz / z0m), lh = log(dz / z0b);
   const double delta = R_v / R_d - 1.0;
   const double thv_air = (T_air + grav * dz / a->cp_d) * (1.0 + delta * q_air);
-  const double rm = z0m / dz, rb = z0b / dz;
-  double zeta = 0.0, F_m = 0.0, F_h = 0.0, g_h = 0.0, q_sfc = qsat;
-  int done = 0; /* the last step moved zeta by at most 1e-12 (1 + |zeta|) */
-  for (int it = 0;; ++it) {
-    F_m = lm - clmo_businger_psi_m(zeta, a) + clmo_businger_psi_m(zeta * rm, a);
-    F_h = a->Pr_0 * (lh - clmo_businger_psi_h(zeta, a) + clmo_businger_psi_h(zeta * rb, a));
-    const double ustar = a->von_karman * U / F_m;
-    g_h = a->von_karman * ustar / F_h;
-    q_sfc = q_sfc_update(g_h, q_air, T_sfc, Tf_sfc, g_soil, beta_ice, qsat);
-    if (it >= a->iterations || done) break;
-    const double thv_sfc = T_sfc * (1.0 + delta * q_sfc);
-    const double Ri = grav * dz * (thv_air - thv_sfc) / (thv_sfc * U * U);
-    double zn;
-    if (Ri >= 0.0) {
-      zn = stable_zeta(a, Ri, lm, lh, rm, rb);
-    } else if (zeta >= 0.0) {
-      zn = Ri * lm * lm / (a->Pr_0 * lh); /* one fixed-point step from 0 */
-    } else { /* Newton on r = zeta F_h - Ri F_m^2 at fixed Ri */
-      const double dF_m = -dpsi_m(zeta, a) + rm * dpsi_m(zeta * rm, a);
-      const double dF_h = a->Pr_0 * (-dpsi_h(zeta, a) + rb * dpsi_h(zeta * rb, a));
-      const double r = zeta * F_h - Ri * F_m * F_m;
-      const double dr = F_h + zeta * dF_h - 2.0 * Ri * F_m * dF_m;
-      zn = fmin(fmax(zeta - r / dr, -a->zeta_max), 0.0);
-    }
-    done = fabs(zn - zeta) <= 1e-12 * (1.0 + fabs(zeta));
-    zeta = zn;
-  }
+  const q_ctx_t qc = {q_air, T_sfc, Tf_sfc, g_soil, beta_ice, qsat};
+  double mo[6];
+  mo_solve(a, grav, dz, U, z0m, z0b, thv_air, T_sfc, delta, qsat, q_sfc_of, &qc, 0.0, mo);
+  const double g_h = mo[3], q_sfc = mo[4];
   const double E = -rho_sfc * g_h * (q_air - q_sfc);
   const double lhf = a->LH_v0 * E;
   const double shf = -rho_sfc * cp_m * g_h * (T_air + grav * dz / cp_m - T_sfc);

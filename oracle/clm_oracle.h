@@ -82,6 +82,13 @@ double clmo_weibull_conductivity(double K_sat, double psi63, double c,
 double clmo_root_distribution(double z, double rooting_depth);
 /* atmosphere-driven top boundary (CLM_BC_ATMOS) */
 void clmo_atmos_params_default(clm_atmos_params* a);
+/* The Monin-Obukhov solve at a fixed surface virtual potential temperature
+ * (known-answer tests): out = zeta, F_m, F_h, g_h, u*; returns 0. */
+int clmo_similarity(const clm_atmos_params* a, double grav, double dz, double U,
+                    double z0m, double z0b, double thv_air, double thv_sfc,
+                    double* out);
+double clmo_gryanik_psi_m(double zeta, const clm_atmos_params* a);
+double clmo_gryanik_psi_h(double zeta, const clm_atmos_params* a);
 double clmo_q_vap_saturation(double T, double rho, int ice,
                              const clm_atmos_params* a,
                              const clm_earth_params* e);

@@ -131,7 +131,9 @@ def lib():
         apar = ctypes.POINTER(A.ClmAtmosParams)
         L.clmo_q_vap_saturation.restype = _D
         L.clmo_q_vap_saturation.argtypes = [_D, _D, ctypes.c_int, apar, ep]
-        for nm in ("clmo_businger_psi_m", "clmo_businger_psi_h"):
+        L.clmo_similarity.restype = ctypes.c_int
+        L.clmo_similarity.argtypes = [apar] + [_D] * 7 + [_DP]
+        for nm in ("clmo_businger_psi_m", "clmo_businger_psi_h", "clmo_gryanik_psi_m", "clmo_gryanik_psi_h"):
             f = getattr(L, nm)
             f.restype = _D
             f.argtypes = [_D, apar]

@@ -755,6 +755,141 @@ def test_saturation_humidity_and_stability_functions(L):
     assert approx(L.clmo_businger_psi_h(-(3.0 ** 2 - 1) / 9.0, ctypes.byref(a)), 2 * math.log(2.0), rtol=1e-14)
 
 
+# The similarity solve of the atmosphere-driven boundary, pinned to the
+# published formulation: Monin-Obukhov similarity at point values,
+#   u* = kappa U / F_m,  g_h = kappa u* / F_h,
+#   F_m = ln(dz/z0m) - psi_m(zeta) + psi_m(zeta z0m/dz),
+#   F_h = Pr_0 (ln(dz/z0b) - psi_h(zeta) + psi_h(zeta z0b/dz)),
+#   zeta F_h(zeta) = Ri_b F_m(zeta)^2,  Ri_b = g dz (thv_air - thv_sfc) / (thv_sfc U^2),
+# with psi(zeta) = int_0^zeta (1 - phi(s)) / s ds for momentum and
+# int_0^zeta (1 - phi_h(s) / Pr_0) / s ds for heat, and the flux-profile
+# functions phi of Businger et al. (1971) / Dyer (unstable: phi_m =
+# (1 - 15 zeta)^(-1/4), phi_h = Pr_0 (1 - 9 zeta)^(-1/2); stable: phi_m = 1 +
+# 4.7 zeta, phi_h = Pr_0 + 4.7 zeta) and of Gryanik et al. (2020, J. Atmos.
+# Sci. 77, 2687-2716; stable: phi_m = 1 + a_m zeta / (1 + b_m zeta)^(2/3),
+# phi_h = Pr_0 (1 + a_h zeta / (1 + b_h zeta)), a_m = a_h = 5, b_m = 0.3,
+# b_h = 0.4, Pr_0 = 0.98), which the reference configures (UF.GryanikParams,
+# src/shared_utilities/Parameters.jl:83).
+
+def _phi(a, zeta, heat):
+    """The published flux-profile functions (heat: phi_h / Pr_0)."""
+    if zeta < 0.0:
+        return (1.0 - a.b_h * zeta) ** -0.5 if heat else (1.0 - a.b_m * zeta) ** -0.25
+    if a.universal_functions == A.CLM_UF_GRYANIK:
+        if heat:
+            return 1.0 + a.a_h * zeta / (1.0 + a.gryanik_b_h * zeta)
+        return 1.0 + a.a_m * zeta / (1.0 + a.gryanik_b_m * zeta) ** (2.0 / 3.0)
+    return 1.0 + (a.a_h / a.Pr_0 if heat else a.a_m) * zeta
+
+
+def _psi_quad(a, zeta, heat):
+    from scipy.integrate import quad
+    if zeta == 0.0:
+        return 0.0
+    val, _ = quad(lambda s: (1.0 - _phi(a, s, heat)) / s, 0.0, zeta, epsabs=1e-14, epsrel=1e-13, limit=200)
+    return val
+
+
+def _similarity_reference(a, g, dz, U, z0m, z0b, thv_air, thv_sfc):
+    """zeta, u*, g_h by a bracketing root solve on the quadrature psi."""
+    from scipy.optimize import brentq
+    lm, lh = math.log(dz / z0m), math.log(dz / z0b)
+    Ri = g * dz * (thv_air - thv_sfc) / (thv_sfc * U * U)
+
+    def F(z):
+        Fm = lm - _psi_quad(a, z, False) + _psi_quad(a, z * z0m / dz, False)
+        Fh = a.Pr_0 * (lh - _psi_quad(a, z, True) + _psi_quad(a, z * z0b / dz, True))
+        return Fm, Fh
+
+    if Ri == 0.0:
+        zeta = 0.0
+    else:
+        def r(z):
+            Fm, Fh = F(z)
+            return z * Fh - Ri * Fm * Fm
+        zeta = brentq(r, 0.0, 50.0, xtol=1e-15, rtol=1e-14) if Ri > 0 else \
+            brentq(r, -50.0, 0.0, xtol=1e-15, rtol=1e-14)
+    Fm, Fh = F(zeta)
+    ustar = a.von_karman * U / Fm
+    return zeta, ustar, a.von_karman * ustar / Fh
+
+
+def _businger(L):
+    a = _atm(L)
+    for k, v in A.BUSINGER_ATMOS.items():
+        setattr(a, k, v)
+    return a
+
+
+@pytest.mark.parametrize("family", ["gryanik", "businger"])
+def test_stability_functions_are_the_integrals_of_phi(L, family):
+    """The closed forms psi(zeta) against the quadrature of (1 - phi) / zeta."""
+    pytest.importorskip("scipy")
+    a = _atm(L) if family == "gryanik" else _businger(L)
+    for zeta in (-5.0, -0.7, -0.01, 0.01, 0.3, 2.0, 10.0):
+        if zeta >= 0.0 and family == "gryanik":
+            pm = L.clmo_gryanik_psi_m(zeta, ctypes.byref(a))
+            ph = L.clmo_gryanik_psi_h(zeta, ctypes.byref(a))
+        else:
+            pm = L.clmo_businger_psi_m(zeta, ctypes.byref(a))
+            ph = L.clmo_businger_psi_h(zeta, ctypes.byref(a))
+        assert approx(pm, _psi_quad(a, zeta, False), rtol=1e-9, atol=1e-12), (zeta, "m")
+        assert approx(ph, _psi_quad(a, zeta, True), rtol=1e-9, atol=1e-12), (zeta, "h")
+
+
+# (dz, U, z0m, z0b, thv_air, thv_sfc): a neutral, two stable (one strongly)
+# and two unstable cases
+SIMILARITY_CASES = {
+    "neutral": (10.0, 5.0, 0.1, 0.01, 290.0, 290.0),
+    "stable": (10.0, 5.0, 0.1, 0.01, 291.0, 288.0),
+    "strongly_stable": (20.0, 3.0, 0.05, 0.005, 287.0, 285.0),
+    "unstable": (10.0, 4.0, 0.1, 0.01, 288.0, 292.0),
+    "strongly_unstable": (30.0, 1.5, 0.02, 0.002, 285.0, 295.0),
+}
+
+
+@pytest.mark.parametrize("family", ["gryanik", "businger"])
+@pytest.mark.parametrize("case", list(SIMILARITY_CASES))
+def test_similarity_solve_known_answers(L, family, case):
+    """The oracle's solve (the same function its boundary uses) reaches the
+    published formulation's root: zeta, u* and the heat conductance g_h to
+    1e-10. Neutral: zeta = 0 and the log law, u* = kappa U / ln(dz/z0m),
+    g_h = kappa^2 U / (Pr_0 ln(dz/z0m) ln(dz/z0b))."""
+    pytest.importorskip("scipy")
+    a = _atm(L) if family == "gryanik" else _businger(L)
+    a.iterations = 60
+    dz, U, z0m, z0b, ta, ts = SIMILARITY_CASES[case]
+    out = (ctypes.c_double * 5)()
+    assert L.clmo_similarity(ctypes.byref(a), 9.81, dz, U, z0m, z0b, ta, ts, out) == 0
+    zeta, ustar, g_h = out[0], out[4], out[3]
+    if case == "neutral":
+        lm, lh = math.log(dz / z0m), math.log(dz / z0b)
+        assert zeta == 0.0
+        assert approx(ustar, a.von_karman * U / lm, rtol=1e-15)
+        assert approx(g_h, a.von_karman ** 2 * U / (a.Pr_0 * lm * lh), rtol=1e-15)
+        return
+    zr, ur, gr = _similarity_reference(a, 9.81, dz, U, z0m, z0b, ta, ts)
+    assert (zeta > 0) == (ta > ts)
+    assert approx(zeta, zr, rtol=1e-10, atol=1e-12), (zeta, zr)
+    assert approx(ustar, ur, rtol=1e-10)
+    assert approx(g_h, gr, rtol=1e-10)
+
+
+def test_default_iterations_converge_on_the_similarity_cases(L):
+    """The default 8 iterations reach the converged root to 1e-9 (zeta) on
+    every case (the step's own iteration count)."""
+    a = _atm(L)
+    for case, (dz, U, z0m, z0b, ta, ts) in SIMILARITY_CASES.items():
+        out8 = (ctypes.c_double * 5)()
+        out60 = (ctypes.c_double * 5)()
+        L.clmo_similarity(ctypes.byref(a), 9.81, dz, U, z0m, z0b, ta, ts, out8)
+        a60 = A.ClmAtmosParams.from_buffer_copy(a)
+        a60.iterations = 60
+        L.clmo_similarity(ctypes.byref(a60), 9.81, dz, U, z0m, z0b, ta, ts, out60)
+        assert approx(out8[0], out60[0], rtol=1e-9, atol=1e-12), case
+        assert approx(out8[3], out60[3], rtol=1e-9), case
+
+
 def test_atmos_boundary_fluxes(L):
     """test/standalone/Soil/climate_drivers.jl:220-260: the top water flux is
     the liquid influx plus the liquid vapour flux, the top energy flux
