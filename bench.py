@@ -205,6 +205,63 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def oracle_errors(w, state, nsteps, sample_cols, oracle_cfg=None, nseeds=8):
+    """The form's error against the FP64 oracle (the checker) on the first
+    `sample_cols` columns: max |vartheta_l|, |theta_i| and |rho_e_int| /
+    max |rho_e_int| differences after `nsteps` steps, the fraction of
+    columns within 1e-8 and 1e-10 in vartheta_l, and how many columns are
+    above 1e-10 in any field, of which how many lie within 10 x the oracle's
+    own spread under per-step 1-ulp noise (8 seeds) -- the parity tests'
+    criterion."""
+    sys.path.insert(0, str(REPO / "oracle"))
+    import oracle as O
+
+    sub = w.subset(sample_cols)
+    n = sub.ncells
+    got = [None if a is None else a[:n] for a in state[:3]]
+    o = O.Oracle(sub)
+    if oracle_cfg:
+        o.set_cfg(**oracle_cfg)
+    ref = sub.copy_state()
+    o.step(ref, sub.t0, sub.dt, nsteps)
+    off = sub.offsets[:-1].astype(np.int64)
+    eh = ref[2] is not None
+    scale = float(np.max(np.abs(sub.rho_e_int))) if eh else 1.0
+
+    def fields(st):
+        return [st[0]] + ([st[1], st[2] / scale] if eh else [])
+
+    colerr = [np.maximum.reduceat(np.abs(a - b), off) for a, b in zip(fields(ref), fields(got))]
+    tot = np.max(np.stack(colerr), axis=0)
+    above = tot > 1e-10
+    excused = 0
+    if above.any():
+        spread = np.zeros(sub.ncol)
+        rng_eps = np.finfo(np.float64).eps
+        for seed in range(nseeds):
+            rng = np.random.default_rng(seed)
+            st = sub.copy_state()
+            for k in range(nsteps):
+                for i in (0, 1, 2):
+                    if st[i] is not None:
+                        st[i][:] = st[i] * (1.0 + rng_eps * rng.choice([-1.0, 1.0], st[i].shape))
+                o.step(st, sub.t0 + k * sub.dt, sub.dt, 1)
+            sp = [np.maximum.reduceat(np.abs(a - b), off) for a, b in zip(fields(ref), fields(st))]
+            spread = np.maximum(spread, np.max(np.stack(sp), axis=0))
+        excused = int(np.sum(above & (tot <= 10.0 * spread)))
+    out = {"sample_cols": sub.ncol, "steps": nsteps,
+           "vartheta_l_max_abs": float(colerr[0].max()),
+           "frac_cols_le_1e-8": float(np.mean(colerr[0] <= 1e-8)),
+           "frac_cols_le_1e-10": float(np.mean(colerr[0] <= 1e-10)),
+           "cols_above_1e-10": int(above.sum()), "of_which_within_10x_oracle_spread": excused}
+    if eh:
+        out["theta_i_max_abs"] = float(colerr[1].max())
+        out["rho_e_int_max_rel"] = float(colerr[2].max())
+    if oracle_cfg:
+        out["oracle_newton"] = dict(oracle_cfg)
+    return out
+
+
 def _error_stats(a, b, ncol_cells):
     """Per-column max |vartheta_l| difference statistics of state a vs b."""
     d = np.abs(a[0] - b[0])
@@ -218,12 +275,15 @@ def _error_stats(a, b, ncol_cells):
 
 def forms_block(args, torch, stream):
     """The three forms beside the plain path, on subsets that finish in
-    seconds: mixed precision (EnergyHydrology and RichardsModel), uneven columns (autotuned, graph-replayed) and
-    learned guess + mixed precision in tolerance mode; and the atmosphere-driven
-    top boundary's cost on the full-scale columns. Errors are per-column
-    max |vartheta_l| differences from the plain FP64 path on the same
-    columns and steps (the plain path itself is held to the FP64 oracle by
-    the parity tests)."""
+    seconds: mixed precision (EnergyHydrology and RichardsModel), uneven
+    columns (autotuned, graph-replayed) and learned guess + mixed precision in
+    tolerance mode; stretched columns (the reference RichardsModel
+    benchmark's geometry and Newton settings, EnergyHydrology on the global
+    domain's column); and the atmosphere-driven top boundary's cost on the
+    full-scale columns. Each form reports err_vs_plain_fp64 (per-column max
+    |vartheta_l| differences from the plain FP64 path on the same columns and
+    steps) and err_vs_oracle (the FP64 oracle, as the checker, on the first
+    --oracle-cols columns)."""
     from climaland_gb300 import _abi as A
     from climaland_gb300 import device as D
     from climaland_gb300 import learned as LG
@@ -263,12 +323,14 @@ def forms_block(args, torch, stream):
                     "fallback_frac": float(np.mean((f & A.CLM_COL_GUESS_FALLBACK) > 0)),
                     "launch_config": g.launch_config()}
 
-    def pub(r, base, w):
+    def pub(r, base, w, oracle_cfg=None):
         out = {k: v for k, v in r.items() if k != "state"}
         out["unit"] = "column-steps/s"
         if base is not None:
             out["speedup_vs_plain_fp64"] = r["value"] / base["value"]
             out["err_vs_plain_fp64"] = _error_stats(r["state"], base["state"], w.offsets)
+        if args.oracle_cols > 0:
+            out["err_vs_oracle"] = oracle_errors(w, r["state"], nst, args.oracle_cols, oracle_cfg)
         return out
 
     out = {"steps": nst}
@@ -289,8 +351,8 @@ def forms_block(args, torch, stream):
     tol = dict(newton_mode=A.CLM_NEWTON_TOL, max_iters=20, newton_tol=1e-8, energy_norm_scale=1e-9)
     plain_tol = run(w4, **tol)
     learned = run(w4, blob=res.blob, learned_guess=1, precision=A.CLM_PREC_MIXED, **tol)
-    out["full_scale_subset"]["plain_fp64_tol1e-8"] = pub(plain_tol, plain, w4)
-    out["full_scale_subset"]["learned_mixed_tol1e-8"] = pub(learned, plain, w4)
+    out["full_scale_subset"]["plain_fp64_tol1e-8"] = pub(plain_tol, plain, w4, tol)
+    out["full_scale_subset"]["learned_mixed_tol1e-8"] = pub(learned, plain, w4, tol)
     out["full_scale_subset"]["learned_training"] = {
         "pairs": res.nrows, "train_steps": 20000, "loss_first": float(res.loss[:50].mean()),
         "loss_last": float(res.loss[-200:].mean()), "train_s": res.seconds, "gen_train_s": gen_train_s}
@@ -307,6 +369,18 @@ def forms_block(args, torch, stream):
     rmx = run(w0, precision=A.CLM_PREC_MIXED)
     out["richards_subset"] = {"workload": w0.name, "plain_fp64": pub(r64, None, w0),
                               "mixed": pub(rmx, r64, w0)}
+    # stretched columns: the reference RichardsModel benchmark
+    # (experiments/benchmarks/richards.jl: 15 layers over 50 m with
+    # dz_tuple = (10.0, 0.1), TOPMODEL, 2 Newton iterations, dt = 1800 s) and
+    # EnergyHydrology on global_domain's column (dz_tuple = (10.0, 0.05))
+    wrb = WL.richards_benchmark(ncol=args.forms_ncol, seed=0)
+    rb64 = run(wrb)
+    out["stretched_richards_benchmark"] = {"workload": wrb.name, "plain_fp64": pub(rb64, None, wrb)}
+    wge = WL.global_eh_stretched(ncol=args.forms_ncol, seed=0)
+    ge64 = run(wge)
+    gemx = run(wge, precision=A.CLM_PREC_MIXED)
+    out["stretched_global_domain"] = {"workload": wge.name, "plain_fp64": pub(ge64, None, wge),
+                                      "mixed": pub(gemx, ge64, wge)}
     # the atmosphere-driven top boundary (turbulent fluxes, radiation,
     # sublimation) on the full-scale columns: its cost over the flux boundary
     wa = WL.with_atmos(w4)
@@ -317,6 +391,64 @@ def forms_block(args, torch, stream):
                              "cost_vs_flux_boundary_fp64": a64["ms_per_step"] / plain["ms_per_step"],
                              "cost_vs_flux_boundary_mixed": amx["ms_per_step"] / mixed["ms_per_step"]}
     return out
+
+
+def full_run(args, torch):
+    """The full-scale configuration over its whole run: 1,048,576 x 20
+    columns, 1536 steps of dt = 450 s (8 simulated days), for the plain FP64
+    path (3 fixed Newton iterations), the mixed path, and learned guess +
+    mixed in tolerance mode (1e-8) with the step sequence replayed as CUDA
+    graphs; each timed end to end on the device, and its final state
+    compared with the FP64 oracle (the checker: fixed iterations, or the same
+    tolerance) on the first --full-oracle-cols columns."""
+    from climaland_gb300 import _abi as A
+    from climaland_gb300 import device as D
+    from climaland_gb300 import learned as LG
+    from climaland_gb300 import workloads as WL
+
+    w = WL.full_scale_c4(ncol=args.ncol or 1048576, seed=0)
+    nst = w.nsteps
+    stream = torch.cuda.Stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    tol = dict(newton_mode=A.CLM_NEWTON_TOL, max_iters=20, newton_tol=1e-8, energy_norm_scale=1e-9)
+    t0 = time.perf_counter()
+    wtr = WL.full_scale_c4(ncol=65536, seed=7)
+    X, Y = LG.generate(wtr, 32)
+    res = LG.train(X, Y, steps=20000, batch=4096, lr=2e-3)
+    del X, Y
+    train_s = time.perf_counter() - t0
+    forms = [("plain_fp64", {}, None), ("mixed", dict(precision=A.CLM_PREC_MIXED), None),
+             ("learned_mixed_tol1e-8_graph", dict(precision=A.CLM_PREC_MIXED, learned_guess=1, graph=1, **tol),
+              res.blob)]
+    out = {"workload": w.name, "columns": w.ncol, "steps": nst, "simulated_days": nst * w.dt / 86400.0,
+           "learned_training_s": train_s}
+    for name, kw, blob in forms:
+        with D.SoilColumns(w, **kw) as g:
+            g.set_stream(stream.cuda_stream)
+            g.autotune(w.t0, w.dt, probe_steps=2)
+            if blob is not None:
+                g.load_mlp(blob)
+            g.step(w.t0, w.dt, 2)  # warm-up (graph capture); the state is set again below
+            g.set_state(*w.copy_state())
+            torch.cuda.synchronize()
+            e0.record(stream)
+            g.step_async(w.t0, w.dt, nst)
+            e1.record(stream)
+            stream.synchronize()
+            ms = e0.elapsed_time(e1)
+            state = g.get_state()
+            flags, iters = g.status()
+        cfg = tol if "tol" in name else None
+        r = {"seconds": ms / 1e3, "column_steps_per_s": w.ncol * nst / (ms / 1e3),
+             "flagged_columns": int(np.count_nonzero(flags & ~np.uint32(A.CLM_COL_GUESS_FALLBACK))),
+             "err_vs_oracle": oracle_errors(w, state, nst, args.full_oracle_cols, cfg)}
+        out[name] = r
+        print(json.dumps({name: r}), file=sys.stderr, flush=True)
+    base = out["plain_fp64"]["column_steps_per_s"]
+    for name, _, _ in forms[1:]:
+        out[name]["speedup_vs_plain_fp64"] = out[name]["column_steps_per_s"] / base
+    print(json.dumps({"full_run": out}), flush=True)
 
 
 def main():
@@ -340,6 +472,12 @@ def main():
     ap.add_argument("--no-forms", action="store_true")
     ap.add_argument("--forms-ncol", type=int, default=262144)
     ap.add_argument("--forms-steps", type=int, default=32)
+    ap.add_argument("--oracle-cols", type=int, default=4096,
+                    help="columns of each form checked against the FP64 oracle (0: none)")
+    ap.add_argument("--full-run", action="store_true",
+                    help="the full-scale configuration's whole 8-day run per form (minutes), "
+                         "instead of the bench line")
+    ap.add_argument("--full-oracle-cols", type=int, default=8192)
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -364,6 +502,10 @@ def main():
     G.build()
     from climaland_gb300 import _abi as A
     from climaland_gb300 import device as D
+
+    if args.full_run:
+        full_run(args, torch)
+        return
 
     w = make_workload(args.config, args.ncol, rank, args.top)
     prec = A.CLM_PREC_MIXED if args.precision == "mixed" else A.CLM_PREC_FP64

@@ -176,3 +176,33 @@ def test_atmos_boundary_graph_host_and_dynamic_paths_agree(torch):
             h.step(w.t0 + 2 * w.dt, w.dt, 2)
         for x, y in zip(g.get_state(), g0.get_state()):
             assert (x is None and y is None) or np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("make", [lambda: WL.full_scale_c4(ncol=2000, seed=5),
+                                  lambda: WL.stretched(WL.uneven_c2(ncol=2000, seed=5))])
+def test_restart_from_saved_state_bitwise_equals_continuing(torch, make):
+    """Checkpoint / restart as ClimaLand does it (save Y, read it back into a
+    new simulation): the state read out with clm_get_state after 7 steps,
+    loaded into a fresh handle with clm_set_state and stepped 5 more, gives
+    the bits of one handle stepping 12; the same through the device-pointer
+    entry points."""
+    w = make()
+
+    def same_state(a, b):
+        for x, y in zip(a, b):
+            assert (x is None and y is None) or np.array_equal(x, y)
+
+    for prec in (A.CLM_PREC_FP64, A.CLM_PREC_MIXED):
+        ref = _run(w, [(w.t0, 12)], precision=prec)[0]
+        with SoilColumns(w, precision=prec) as g:
+            g.step(w.t0, w.dt, 7)
+            saved = g.get_state()
+        wr = w.columns(0, w.ncol)
+        wr.vartheta_l, wr.theta_i, wr.rho_e_int, wr.intF_w, wr.intF_e = saved
+        same_state(ref, _run(wr, [(w.t0 + 7 * w.dt, 5)], precision=prec)[0])
+        # device buffers (CuArray-style caller memory)
+        dev = [None if a is None else torch.tensor(a, device="cuda") for a in saved]
+        with SoilColumns(w, precision=prec) as g:
+            g.set_state_device([None if d is None else d.data_ptr() for d in dev])
+            g.step(w.t0 + 7 * w.dt, w.dt, 5)
+            same_state(ref, g.get_state())
