@@ -8,7 +8,8 @@ mixed path's float Jacobian. The device's own results are held to the
 oracle by the GPU parity tests.
 
 Criterion (FP64): every column within max(1e-10, 10 x the oracle's own
-spread under per-step 1-ulp noise); mixed: the oracle's root to 1e-11 once
+spread under per-step noise of 1 ulp of each field's scale on nonzero
+values); mixed: the oracle's root to 1e-11 once
 Newton has converged (8 iterations: the float Jacobian changes only the rate
 of convergence; the closures are double-float), and over a trajectory at the
 configured 3 iterations within max(1e-8, 10 x the spread under per-step
@@ -106,8 +107,9 @@ def _errors(w, so, sr):
 
 
 def _oracle(w, nsteps, noise=None, seed=None):
-    """The oracle; with a seed, relative noise of size `noise` (a scalar, or
-    one value per column) on every state array before each step."""
+    """The oracle; with a seed, noise of size `noise` (relative to each
+    field's scale; a scalar, or one value per column) on every nonzero state
+    value before each step."""
     o = O.Oracle(w)
     st = w.copy_state()
     if seed is None:
@@ -116,10 +118,11 @@ def _oracle(w, nsteps, noise=None, seed=None):
         return st
     rng = np.random.default_rng(seed)
     eps = np.repeat(np.broadcast_to(noise, (w.ncol,)), w.nlayers)
+    scale = [None if a is None else float(np.max(np.abs(a))) for a in w.copy_state()[:3]]
     for k in range(nsteps):
         for i in (0, 1, 2):
             if st[i] is not None:
-                st[i][:] = st[i] * (1.0 + eps * rng.choice([-1.0, 1.0], st[i].shape))
+                st[i][:] = st[i] + (st[i] != 0.0) * (eps * scale[i]) * rng.choice([-1.0, 1.0], st[i].shape)
         o.step(st, w.t0 + k * w.dt, w.dt, 1)
     return st
 
