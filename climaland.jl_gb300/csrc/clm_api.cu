@@ -33,6 +33,9 @@ cudaError_t internal_to_ref(const Layout& L, const XFields& F, cudaStream_t st, 
                             int ntl = -1);
 cudaError_t cols_to_sorted(const Layout& L, const double* src, double* dst, cudaStream_t st);
 cudaError_t cols_to_orig(const Layout& L, const double* src, double* dst, cudaStream_t st);
+// clm_order.cu
+cudaError_t regroup_slots(const Layout& L, const int32_t* iters, int* order, int* bins, cudaStream_t st);
+size_t order_bins_count();
 // clm_budget.cu
 cudaError_t launch_budgets(const StepArgs& A, int model, double* W, double* E, cudaStream_t st);
 // clm_mlp.cu
@@ -87,6 +90,8 @@ struct clm_handle {
   int grid = 0;  // resident CTAs of the step kernel
   int sched = CLM_SCHED_STATIC;  // tile order of the step kernel
   int* d_ctr = nullptr;          // dynamic tile order: [next tile, warps done]
+  int* d_order = nullptr;        // iteration-class slot order (tolerance mode)
+  int* d_order_bins = nullptr;   // its counting-sort bins
   double* d_scratch = nullptr;  // per-warp-slot frozen aux arrays
   size_t scratch_doubles = 0;
   int guess_grid = 0;           // persistent grid of the guess kernel
@@ -140,6 +145,12 @@ void dfree(T*& p) {
 
 bool is_eh(const clm_handle* h) { return h->cfg.model == CLM_MODEL_ENERGY_HYDROLOGY; }
 
+// Tolerance mode groups columns into warps by their last Newton iteration
+// count, re-sorted after every step (clm_order.cu).
+bool regroups(const clm_handle* h) {
+  return h->cfg.newton_mode == CLM_NEWTON_TOL && h->cfg.tol_regroup && h->d_order;
+}
+
 // Captured graphs hold kernel arguments by value (buffer pointers, launch
 // shape): drop them whenever one of those changes.
 void drop_graphs(clm_handle* h) {
@@ -189,6 +200,7 @@ StepArgs step_args(const clm_handle* h) {
   A.iters = h->d_iters;
   A.guess = h->cfg.learned_guess ? h->d_guess : nullptr;
   A.tile_ctr = h->sched == CLM_SCHED_DYNAMIC ? h->d_ctr : nullptr;
+  A.order = regroups(h) ? h->d_order : nullptr;
   A.E = h->E;
   A.sc = h->sc;
   A.bc_tw = h->cfg.bc_top_water;
@@ -274,6 +286,7 @@ int build_layout(clm_handle* h, const std::vector<int>& nl) {
   for (int s = 0; s < ncol; ++s) slot_ref[s] = h->ref_off[h->perm[s]];
   dfree(h->d_tile_off); dfree(h->d_tile_n); dfree(h->d_col_n); dfree(h->d_perm); dfree(h->d_ref_off);
   dfree(h->d_slot_ref);
+  dfree(h->d_order);
   cudaStream_t st = h->stream;
   CLM_CUDA(h, cudaMalloc(&h->d_tile_off, sizeof(int64_t) * h->ntiles));
   CLM_CUDA(h, cudaMalloc(&h->d_tile_n, sizeof(int) * h->ntiles));
@@ -287,7 +300,13 @@ int build_layout(clm_handle* h, const std::vector<int>& nl) {
   CLM_CUDA(h, cudaMemcpyAsync(h->d_ref_off, h->ref_off.data(), sizeof(int32_t) * (ncol + 1), cudaMemcpyHostToDevice, st));
   CLM_CUDA(h, cudaMalloc(&h->d_slot_ref, sizeof(int64_t) * h->stride));
   CLM_CUDA(h, cudaMemcpyAsync(h->d_slot_ref, slot_ref.data(), sizeof(int64_t) * h->stride, cudaMemcpyHostToDevice, st));
-  // the host vector above goes out of scope: wait for its copy
+  // iteration-class order: the tiles' own slots until a step has run
+  std::vector<int> ident(h->stride);
+  std::iota(ident.begin(), ident.end(), 0);
+  CLM_CUDA(h, cudaMalloc(&h->d_order, sizeof(int) * h->stride));
+  CLM_CUDA(h, cudaMemcpyAsync(h->d_order, ident.data(), sizeof(int) * h->stride, cudaMemcpyHostToDevice, st));
+  if (!h->d_order_bins) CLM_CUDA(h, cudaMalloc(&h->d_order_bins, sizeof(int) * order_bins_count()));
+  // the host vectors above go out of scope: wait for their copies
   CLM_CUDA(h, cudaStreamSynchronize(st));
   // per-layout buffers
   dfree(h->d_v); dfree(h->d_ti); dfree(h->d_e); dfree(h->d_stage);
@@ -332,7 +351,7 @@ struct Launch {
 // start: one guess launch, then one step launch, per step.
 std::vector<Launch> launch_sequence(const clm_handle* h, int nsteps) {
   std::vector<Launch> seq;
-  if (h->cfg.learned_guess) {
+  if (h->cfg.learned_guess || regroups(h)) {  // per step: guess, or regroup, in between
     for (int i = 0; i < nsteps; ++i) seq.push_back({i, 1, true});
   } else {
     const int chunk = 64;
@@ -349,6 +368,7 @@ int issue(clm_handle* h, const Launch& l, const StepClock& clk, cudaStream_t st)
   }
   CLM_CUDA(h, launch_step(A, h->cfg.model, h->cfg.precision, h->wpc, h->grid, h->d_scratch, clk,
                           l.nsteps, st));
+  if (A.order) CLM_CUDA(h, regroup_slots(A.L, h->d_iters, h->d_order, h->d_order_bins, st));
   return CLM_OK;
 }
 
@@ -362,7 +382,7 @@ int step_graph(clm_handle* h, double t, double dt, int nsteps) {
     CLM_CUDA(h, cudaMallocHost(&h->h_clock, sizeof(double) * (kClockSlots + 1) * clm_handle::kRing));
     for (auto& ev : h->clock_ev) CLM_CUDA(h, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   }
-  const int per_launch = h->cfg.learned_guess ? 1 : 64;
+  const int per_launch = (h->cfg.learned_guess || regroups(h)) ? 1 : 64;
   const int piece_max = per_launch * kClockSlots;
   for (int s_begin = 0; s_begin < nsteps; s_begin += piece_max) {
     const int P = std::min(piece_max, nsteps - s_begin);
@@ -527,6 +547,7 @@ int check_config(const clm_config* cfg) {
   if (cfg->newton_mode != CLM_NEWTON_FIXED && cfg->newton_mode != CLM_NEWTON_TOL) return CLM_ERR_ARG;
   if (cfg->schedule != CLM_SCHED_STATIC && cfg->schedule != CLM_SCHED_DYNAMIC) return CLM_ERR_ARG;
   if (cfg->graph != 0 && cfg->graph != 1) return CLM_ERR_ARG;
+  if (cfg->tol_regroup != 0 && cfg->tol_regroup != 1) return CLM_ERR_ARG;
   if (cfg->cols_per_cta < 0) return CLM_ERR_ARG;
   if (cfg->hydrology_cm != CLM_CM_VAN_GENUCHTEN && cfg->hydrology_cm != CLM_CM_BROOKS_COREY)
     return CLM_ERR_ARG;
@@ -590,6 +611,7 @@ void clm_config_default(clm_config* c) {
   c->earth.LH_f0 = 2834400.0 - 2500800.0;
   c->earth.grav = 9.81;
   c->phase_change = 1;
+  c->tol_regroup = 1;
 }
 
 int clm_create(const clm_config* cfg, clm_handle** out) {
@@ -668,6 +690,8 @@ void clm_destroy(clm_handle* h) {
   dfree(h->d_scratch);
   dfree(h->d_mlp);
   dfree(h->d_ctr);
+  dfree(h->d_order);
+  dfree(h->d_order_bins);
   drop_graphs(h);
   dfree(h->d_clock);
   if (h->h_clock) cudaFreeHost(h->h_clock);
@@ -1103,6 +1127,7 @@ int clm_step_host(clm_handle* h, double* v, double* ti, double* e, double* Fw, d
     CLM_CUDA(h, ref_to_internal(L, Fi, h->stream, T0, T1 - T0));
     A.tile_begin = T0;
     A.tile_end = T1;
+    A.order = nullptr;  // a chunk's launch covers its own tiles' columns
     for (int s0 = 0; s0 < nsteps; s0 += 64) {
       StepClock clk;
       clk.t0 = step_time(t, s0, dt);

@@ -371,6 +371,12 @@ typedef struct clm_config {
                              rain-pulse hash uses the global column index  */
   int32_t host_chunks;    /* clm_step_host pipeline depth (0: by size)      */
   int32_t runoff;         /* enum clm_runoff (CLM_BC_PRECIP_RUNOFF)         */
+  int32_t tol_regroup;    /* tolerance mode: 1 (default) groups columns into
+                             warps by their last Newton iteration count each
+                             step (a warp runs as many iterations as its
+                             slowest column); 0 keeps the depth-sorted tiles.
+                             Results do not depend on it                    */
+  int32_t pad1;
 } clm_config;
 
 typedef struct clm_handle clm_handle;
