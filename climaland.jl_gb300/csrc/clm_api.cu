@@ -42,7 +42,7 @@ cudaError_t launch_budgets(const StepArgs& A, int model, double* W, double* E, c
 cudaError_t mlp_features(const StepArgs& A, double t, double dt, float* X, cudaStream_t st);
 cudaError_t mlp_guess_setup(int64_t rows, int* grid);
 cudaError_t mlp_guess(const StepArgs& A, const float* P, const float* norm, const StepClock& clk,
-                      float* guess, int grid, cudaStream_t st);
+                      float* guess, double* prev, int grid, cudaStream_t st);
 }  // namespace clm
 
 #include "clm_mlp.cuh"
@@ -84,6 +84,7 @@ struct clm_handle {
   double* d_stage = nullptr;  // ncells_ref * 3 staging (reference layout)
   double* d_colstage = nullptr;  // 4 * stride: upload staging, W, E, spare
   float* d_guess = nullptr;  // learned guess, 2 x ncells_int (NaN: none)
+  double* d_prev = nullptr;  // the state at the previous guess (vartheta_l, rho_e_int), 2 x ncells_int
   float* d_mlp = nullptr;    // network parameters then standardisation
   bool have_geometry = false, have_params = false, have_state = false;
   int wpc = 1;   // warps (32-column tiles) per CTA of the step kernel
@@ -364,7 +365,7 @@ int issue(clm_handle* h, const Launch& l, const StepClock& clk, cudaStream_t st)
   const StepArgs A = step_args(h);
   if (l.guess) {
     const float* P = h->d_mlp;
-    CLM_CUDA(h, mlp_guess(A, P, P + kMlpParams, clk, h->d_guess, h->guess_grid, st));
+    CLM_CUDA(h, mlp_guess(A, P, P + kMlpParams, clk, h->d_guess, h->d_prev, h->guess_grid, st));
   }
   CLM_CUDA(h, launch_step(A, h->cfg.model, h->cfg.precision, h->wpc, h->grid, h->d_scratch, clk,
                           l.nsteps, st));
@@ -464,6 +465,20 @@ int ready(clm_handle* h) {
   if (h->cfg.bc_top_water == CLM_BC_ATMOS && !h->d_atm)
     return fail(h, CLM_ERR_STATE, "clm_set_atmos has not been called");
   return CLM_OK;
+}
+
+// The learned guess's history restarts at the current state (clm_load_mlp):
+// the first guess after it has no previous increment. clm_set_state keeps
+// the history, so a caller that round-trips its state every step keeps it;
+// a state unrelated to the previous one gives one poor first guess, which
+// the step's fallback replaces by the plain start.
+cudaError_t restart_guess_history(clm_handle* h) {
+  if (!h->d_prev || !h->d_v || !h->d_e) return cudaSuccess;
+  const size_t nb = sizeof(double) * (size_t)h->ncells_int;
+  cudaError_t e = cudaMemcpyAsync(h->d_prev, h->d_v, nb, cudaMemcpyDeviceToDevice, h->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(h->d_prev + h->ncells_int, h->d_e, nb, cudaMemcpyDeviceToDevice, h->stream);
+  return e;
 }
 
 int set_state_impl(clm_handle* h, const double* v, const double* ti, const double* e,
@@ -687,6 +702,7 @@ void clm_destroy(clm_handle* h) {
   dfree(h->d_atm);
   dfree(h->d_v); dfree(h->d_ti); dfree(h->d_e); dfree(h->d_Fw); dfree(h->d_Fe);
   dfree(h->d_flags); dfree(h->d_iters); dfree(h->d_stage); dfree(h->d_colstage); dfree(h->d_guess);
+  dfree(h->d_prev);
   dfree(h->d_scratch);
   dfree(h->d_mlp);
   dfree(h->d_ctr);
@@ -1377,6 +1393,9 @@ int clm_load_mlp(clm_handle* h, const void* weights, int64_t nbytes) {
     CLM_CUDA(h, cudaMalloc(&h->d_guess, gb));
     CLM_CUDA(h, cudaMemsetAsync(h->d_guess, 0xFF, gb, h->stream));  // NaN: no guess
   }
+  if (!h->d_prev)
+    CLM_CUDA(h, cudaMalloc(&h->d_prev, sizeof(double) * 2 * (size_t)std::max<int64_t>(h->ncells_int, 1)));
+  CLM_CUDA(h, restart_guess_history(h));
   CLM_CUDA(h, cudaStreamSynchronize(h->stream));
   return CLM_OK;
 }
