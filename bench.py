@@ -354,9 +354,18 @@ def forms_block(args, torch, stream):
     gen_train_s = time.perf_counter() - t0
     del X, Y
     plain_tol = run(w4, **tol)
+    mixed_tol = run(w4, precision=A.CLM_PREC_MIXED, **tol)
     learned = run(w4, blob=res.blob, learned_guess=1, precision=A.CLM_PREC_MIXED, **tol)
+    # the previous increment alone (the network's output held at zero)
+    tr = LG.Trainer(seed=0)
+    tr.set_normalization(np.zeros(LG.N_IN), np.ones(LG.N_IN), np.zeros(LG.N_OUT), np.full(LG.N_OUT, 1e-30))
+    zero_blob = tr.blob()
+    tr.close()
+    persist = run(w4, blob=zero_blob, learned_guess=1, precision=A.CLM_PREC_MIXED, **tol)
     out["full_scale_subset"]["plain_fp64_tol1e-8"] = pub(plain_tol, plain, w4, tol)
+    out["full_scale_subset"]["mixed_tol1e-8"] = pub(mixed_tol, plain, w4, tol)
     out["full_scale_subset"]["learned_mixed_tol1e-8"] = pub(learned, plain, w4, tol)
+    out["full_scale_subset"]["previous_increment_mixed_tol1e-8"] = pub(persist, plain, w4, tol)
     out["full_scale_subset"]["learned_training"] = {
         "pairs": res.nrows, "train_steps": 20000, "loss_first": float(res.loss[:50].mean()),
         "loss_last": float(res.loss[-200:].mean()), "train_s": res.seconds, "gen_train_s": gen_train_s}
