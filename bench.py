@@ -310,8 +310,12 @@ def forms_block(args, torch, stream):
                 its.append(it)
             state = g.get_state()
             g.set_state(*w.copy_state())
+            if blob is not None:
+                g.load_mlp(blob)  # restarts the guess history at the initial state
             g.step(w.t0, w.dt, nst)  # same call as timed: captures its graph if any
             g.set_state(*w.copy_state())
+            if blob is not None:
+                g.load_mlp(blob)
             torch.cuda.synchronize()
             e0.record(stream)
             g.step_async(w.t0, w.dt, nst)
@@ -343,17 +347,26 @@ def forms_block(args, torch, stream):
                                 "mixed": pub(mixed, plain, w4)}
     # (1)+(4) learned guess + mixed precision, tolerance-stopped Newton:
     # network trained on the plain solver's trajectories (another seed)
+    tol = dict(newton_mode=A.CLM_NEWTON_TOL, max_iters=20, newton_tol=1e-8, energy_norm_scale=1e-9)
     wtr = WL.full_scale_c4(ncol=65536, seed=7)
     t0 = time.perf_counter()
-    X, Y = LG.generate(wtr, 32)
+    X, Y = LG.generate(wtr, 32, newton=tol)  # trajectories at the evaluated tolerance
     res = LG.train(X, Y, steps=20000, batch=4096, lr=2e-3)
     gen_train_s = time.perf_counter() - t0
     del X, Y
-    tol = dict(newton_mode=A.CLM_NEWTON_TOL, max_iters=20, newton_tol=1e-8, energy_norm_scale=1e-9)
     plain_tol = run(w4, **tol)
+    mixed_tol = run(w4, precision=A.CLM_PREC_MIXED, **tol)
     learned = run(w4, blob=res.blob, learned_guess=1, precision=A.CLM_PREC_MIXED, **tol)
+    # the previous increment alone (the network's output held at zero)
+    tr = LG.Trainer(seed=0)
+    tr.set_normalization(np.zeros(LG.N_IN), np.ones(LG.N_IN), np.zeros(LG.N_OUT), np.full(LG.N_OUT, 1e-30))
+    zero_blob = tr.blob()
+    tr.close()
+    persist = run(w4, blob=zero_blob, learned_guess=1, precision=A.CLM_PREC_MIXED, **tol)
     out["full_scale_subset"]["plain_fp64_tol1e-8"] = pub(plain_tol, plain, w4, tol)
+    out["full_scale_subset"]["mixed_tol1e-8"] = pub(mixed_tol, plain, w4, tol)
     out["full_scale_subset"]["learned_mixed_tol1e-8"] = pub(learned, plain, w4, tol)
+    out["full_scale_subset"]["previous_increment_mixed_tol1e-8"] = pub(persist, plain, w4, tol)
     out["full_scale_subset"]["learned_training"] = {
         "pairs": res.nrows, "train_steps": 20000, "loss_first": float(res.loss[:50].mean()),
         "loss_last": float(res.loss[-200:].mean()), "train_s": res.seconds, "gen_train_s": gen_train_s}
@@ -415,7 +428,7 @@ def full_run(args, torch):
     tol = dict(newton_mode=A.CLM_NEWTON_TOL, max_iters=20, newton_tol=1e-8, energy_norm_scale=1e-9)
     t0 = time.perf_counter()
     wtr = WL.full_scale_c4(ncol=65536, seed=7)
-    X, Y = LG.generate(wtr, 32)
+    X, Y = LG.generate(wtr, 32, newton=tol)
     res = LG.train(X, Y, steps=20000, batch=4096, lr=2e-3)
     del X, Y
     train_s = time.perf_counter() - t0

@@ -195,6 +195,8 @@ class ClmConfig(ctypes.Structure):
         ("column_offset", ctypes.c_int64),
         ("host_chunks", ctypes.c_int32),
         ("runoff", ctypes.c_int32),
+        ("tol_regroup", ctypes.c_int32),
+        ("pad1", ctypes.c_int32),
     ]
 
 
@@ -243,6 +245,7 @@ def default_config() -> ClmConfig:
     c.cols_per_cta = 0
     c.schedule = CLM_SCHED_STATIC
     c.graph = 0
+    c.tol_regroup = 1
     return c
 
 

@@ -49,7 +49,7 @@ class SoilColumns:
 
     def __init__(self, w, *, precision=None, newton_mode=None, max_iters=None,
                  newton_tol=None, energy_norm_scale=None, cols_per_cta=None, learned_guess=None,
-                 schedule=None, graph=None, host_chunks=None, lib=None):
+                 schedule=None, graph=None, host_chunks=None, tol_regroup=None, lib=None):
         self.lib = lib or load_library()
         self.w = w
         cfg = A.ClmConfig.from_buffer_copy(w.cfg)
@@ -67,6 +67,8 @@ class SoilColumns:
             cfg.cols_per_cta = cols_per_cta
         if learned_guess is not None:
             cfg.learned_guess = int(learned_guess)
+        if tol_regroup is not None:
+            cfg.tol_regroup = int(bool(tol_regroup))
         if schedule is not None:
             cfg.schedule = int(schedule)
         if graph is not None:

@@ -116,8 +116,11 @@ TOL = dict(newton_mode=A.CLM_NEWTON_TOL, max_iters=20, newton_tol=1e-12, energy_
 
 def generate(w, nsteps, newton=TOL):
     """(X, Y) pairs from the plain FP64 solver in tolerance mode: X the raw
-    inputs at the start of each step, Y = u_{n+1} - u_n of vartheta_l and
-    rho_e_int (20 layers each), for every column and step (device tensors)."""
+    inputs at the start of step n, Y the change of the step's increment of
+    vartheta_l and rho_e_int (20 layers each) from the previous step's,
+    (u_{n+1} - u_n) - (u_n - u_{n-1}), for every column and step n >= 1
+    (device tensors): the guess kernel adds the prediction to the column's
+    previous increment."""
     torch = _torch()
     assert np.all(w.nlayers == LAYERS), "the network is built for 20-layer columns"
     ncol = w.ncol
@@ -127,6 +130,7 @@ def generate(w, nsteps, newton=TOL):
     ptrs = [x.data_ptr() for x in st]
     with SoilColumns(w, **newton) as g:
         t = w.t0
+        inc_v = inc_e = None
         for i in range(nsteps):
             g.features(t, w.dt, X[i].data_ptr())
             prev_v = st[0].clone()
@@ -134,10 +138,14 @@ def generate(w, nsteps, newton=TOL):
             g.step(t, w.dt, 1)
             g.get_state_device(ptrs)
             torch.cuda.synchronize()
-            Y[i, :, :LAYERS] = (st[0] - prev_v).view(ncol, LAYERS).float()
-            Y[i, :, LAYERS:] = (st[2] - prev_e).view(ncol, LAYERS).float()
+            dv, de = st[0] - prev_v, st[2] - prev_e
+            if inc_v is not None:
+                Y[i, :, :LAYERS] = (dv - inc_v).view(ncol, LAYERS).float()
+                Y[i, :, LAYERS:] = (de - inc_e).view(ncol, LAYERS).float()
+            inc_v, inc_e = dv, de
             t += w.dt
-    return X.view(-1, N_IN), Y.view(-1, N_OUT)
+    # the first step has no previous increment: its pair is not used
+    return X[1:].reshape(-1, N_IN), Y[1:].reshape(-1, N_OUT)
 
 
 @dataclass

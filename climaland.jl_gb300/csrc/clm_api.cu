@@ -33,13 +33,16 @@ cudaError_t internal_to_ref(const Layout& L, const XFields& F, cudaStream_t st, 
                             int ntl = -1);
 cudaError_t cols_to_sorted(const Layout& L, const double* src, double* dst, cudaStream_t st);
 cudaError_t cols_to_orig(const Layout& L, const double* src, double* dst, cudaStream_t st);
+// clm_order.cu
+cudaError_t regroup_slots(const Layout& L, const int32_t* iters, int* order, int* bins, cudaStream_t st);
+size_t order_bins_count();
 // clm_budget.cu
 cudaError_t launch_budgets(const StepArgs& A, int model, double* W, double* E, cudaStream_t st);
 // clm_mlp.cu
 cudaError_t mlp_features(const StepArgs& A, double t, double dt, float* X, cudaStream_t st);
 cudaError_t mlp_guess_setup(int64_t rows, int* grid);
 cudaError_t mlp_guess(const StepArgs& A, const float* P, const float* norm, const StepClock& clk,
-                      float* guess, int grid, cudaStream_t st);
+                      float* guess, double* prev, int grid, cudaStream_t st);
 }  // namespace clm
 
 #include "clm_mlp.cuh"
@@ -81,12 +84,15 @@ struct clm_handle {
   double* d_stage = nullptr;  // ncells_ref * 3 staging (reference layout)
   double* d_colstage = nullptr;  // 4 * stride: upload staging, W, E, spare
   float* d_guess = nullptr;  // learned guess, 2 x ncells_int (NaN: none)
+  double* d_prev = nullptr;  // the state at the previous guess (vartheta_l, rho_e_int), 2 x ncells_int
   float* d_mlp = nullptr;    // network parameters then standardisation
   bool have_geometry = false, have_params = false, have_state = false;
   int wpc = 1;   // warps (32-column tiles) per CTA of the step kernel
   int grid = 0;  // resident CTAs of the step kernel
   int sched = CLM_SCHED_STATIC;  // tile order of the step kernel
   int* d_ctr = nullptr;          // dynamic tile order: [next tile, warps done]
+  int* d_order = nullptr;        // iteration-class slot order (tolerance mode)
+  int* d_order_bins = nullptr;   // its counting-sort bins
   double* d_scratch = nullptr;  // per-warp-slot frozen aux arrays
   size_t scratch_doubles = 0;
   int guess_grid = 0;           // persistent grid of the guess kernel
@@ -140,6 +146,12 @@ void dfree(T*& p) {
 
 bool is_eh(const clm_handle* h) { return h->cfg.model == CLM_MODEL_ENERGY_HYDROLOGY; }
 
+// Tolerance mode groups columns into warps by their last Newton iteration
+// count, re-sorted after every step (clm_order.cu).
+bool regroups(const clm_handle* h) {
+  return h->cfg.newton_mode == CLM_NEWTON_TOL && h->cfg.tol_regroup && h->d_order;
+}
+
 // Captured graphs hold kernel arguments by value (buffer pointers, launch
 // shape): drop them whenever one of those changes.
 void drop_graphs(clm_handle* h) {
@@ -189,6 +201,7 @@ StepArgs step_args(const clm_handle* h) {
   A.iters = h->d_iters;
   A.guess = h->cfg.learned_guess ? h->d_guess : nullptr;
   A.tile_ctr = h->sched == CLM_SCHED_DYNAMIC ? h->d_ctr : nullptr;
+  A.order = regroups(h) ? h->d_order : nullptr;
   A.E = h->E;
   A.sc = h->sc;
   A.bc_tw = h->cfg.bc_top_water;
@@ -274,6 +287,7 @@ int build_layout(clm_handle* h, const std::vector<int>& nl) {
   for (int s = 0; s < ncol; ++s) slot_ref[s] = h->ref_off[h->perm[s]];
   dfree(h->d_tile_off); dfree(h->d_tile_n); dfree(h->d_col_n); dfree(h->d_perm); dfree(h->d_ref_off);
   dfree(h->d_slot_ref);
+  dfree(h->d_order);
   cudaStream_t st = h->stream;
   CLM_CUDA(h, cudaMalloc(&h->d_tile_off, sizeof(int64_t) * h->ntiles));
   CLM_CUDA(h, cudaMalloc(&h->d_tile_n, sizeof(int) * h->ntiles));
@@ -287,7 +301,13 @@ int build_layout(clm_handle* h, const std::vector<int>& nl) {
   CLM_CUDA(h, cudaMemcpyAsync(h->d_ref_off, h->ref_off.data(), sizeof(int32_t) * (ncol + 1), cudaMemcpyHostToDevice, st));
   CLM_CUDA(h, cudaMalloc(&h->d_slot_ref, sizeof(int64_t) * h->stride));
   CLM_CUDA(h, cudaMemcpyAsync(h->d_slot_ref, slot_ref.data(), sizeof(int64_t) * h->stride, cudaMemcpyHostToDevice, st));
-  // the host vector above goes out of scope: wait for its copy
+  // iteration-class order: the tiles' own slots until a step has run
+  std::vector<int> ident(h->stride);
+  std::iota(ident.begin(), ident.end(), 0);
+  CLM_CUDA(h, cudaMalloc(&h->d_order, sizeof(int) * h->stride));
+  CLM_CUDA(h, cudaMemcpyAsync(h->d_order, ident.data(), sizeof(int) * h->stride, cudaMemcpyHostToDevice, st));
+  if (!h->d_order_bins) CLM_CUDA(h, cudaMalloc(&h->d_order_bins, sizeof(int) * order_bins_count()));
+  // the host vectors above go out of scope: wait for their copies
   CLM_CUDA(h, cudaStreamSynchronize(st));
   // per-layout buffers
   dfree(h->d_v); dfree(h->d_ti); dfree(h->d_e); dfree(h->d_stage);
@@ -332,7 +352,7 @@ struct Launch {
 // start: one guess launch, then one step launch, per step.
 std::vector<Launch> launch_sequence(const clm_handle* h, int nsteps) {
   std::vector<Launch> seq;
-  if (h->cfg.learned_guess) {
+  if (h->cfg.learned_guess || regroups(h)) {  // per step: guess, or regroup, in between
     for (int i = 0; i < nsteps; ++i) seq.push_back({i, 1, true});
   } else {
     const int chunk = 64;
@@ -345,10 +365,11 @@ int issue(clm_handle* h, const Launch& l, const StepClock& clk, cudaStream_t st)
   const StepArgs A = step_args(h);
   if (l.guess) {
     const float* P = h->d_mlp;
-    CLM_CUDA(h, mlp_guess(A, P, P + kMlpParams, clk, h->d_guess, h->guess_grid, st));
+    CLM_CUDA(h, mlp_guess(A, P, P + kMlpParams, clk, h->d_guess, h->d_prev, h->guess_grid, st));
   }
   CLM_CUDA(h, launch_step(A, h->cfg.model, h->cfg.precision, h->wpc, h->grid, h->d_scratch, clk,
                           l.nsteps, st));
+  if (A.order) CLM_CUDA(h, regroup_slots(A.L, h->d_iters, h->d_order, h->d_order_bins, st));
   return CLM_OK;
 }
 
@@ -362,7 +383,7 @@ int step_graph(clm_handle* h, double t, double dt, int nsteps) {
     CLM_CUDA(h, cudaMallocHost(&h->h_clock, sizeof(double) * (kClockSlots + 1) * clm_handle::kRing));
     for (auto& ev : h->clock_ev) CLM_CUDA(h, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   }
-  const int per_launch = h->cfg.learned_guess ? 1 : 64;
+  const int per_launch = (h->cfg.learned_guess || regroups(h)) ? 1 : 64;
   const int piece_max = per_launch * kClockSlots;
   for (int s_begin = 0; s_begin < nsteps; s_begin += piece_max) {
     const int P = std::min(piece_max, nsteps - s_begin);
@@ -446,6 +467,20 @@ int ready(clm_handle* h) {
   return CLM_OK;
 }
 
+// The learned guess's history restarts at the current state (clm_load_mlp):
+// the first guess after it has no previous increment. clm_set_state keeps
+// the history, so a caller that round-trips its state every step keeps it;
+// a state unrelated to the previous one gives one poor first guess, which
+// the step's fallback replaces by the plain start.
+cudaError_t restart_guess_history(clm_handle* h) {
+  if (!h->d_prev || !h->d_v || !h->d_e) return cudaSuccess;
+  const size_t nb = sizeof(double) * (size_t)h->ncells_int;
+  cudaError_t e = cudaMemcpyAsync(h->d_prev, h->d_v, nb, cudaMemcpyDeviceToDevice, h->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(h->d_prev + h->ncells_int, h->d_e, nb, cudaMemcpyDeviceToDevice, h->stream);
+  return e;
+}
+
 int set_state_impl(clm_handle* h, const double* v, const double* ti, const double* e,
                    const double* Fw, const double* Fe, cudaMemcpyKind kind) {
   if (!h) return CLM_ERR_ARG;
@@ -527,6 +562,7 @@ int check_config(const clm_config* cfg) {
   if (cfg->newton_mode != CLM_NEWTON_FIXED && cfg->newton_mode != CLM_NEWTON_TOL) return CLM_ERR_ARG;
   if (cfg->schedule != CLM_SCHED_STATIC && cfg->schedule != CLM_SCHED_DYNAMIC) return CLM_ERR_ARG;
   if (cfg->graph != 0 && cfg->graph != 1) return CLM_ERR_ARG;
+  if (cfg->tol_regroup != 0 && cfg->tol_regroup != 1) return CLM_ERR_ARG;
   if (cfg->cols_per_cta < 0) return CLM_ERR_ARG;
   if (cfg->hydrology_cm != CLM_CM_VAN_GENUCHTEN && cfg->hydrology_cm != CLM_CM_BROOKS_COREY)
     return CLM_ERR_ARG;
@@ -590,6 +626,7 @@ void clm_config_default(clm_config* c) {
   c->earth.LH_f0 = 2834400.0 - 2500800.0;
   c->earth.grav = 9.81;
   c->phase_change = 1;
+  c->tol_regroup = 1;
 }
 
 int clm_create(const clm_config* cfg, clm_handle** out) {
@@ -665,9 +702,12 @@ void clm_destroy(clm_handle* h) {
   dfree(h->d_atm);
   dfree(h->d_v); dfree(h->d_ti); dfree(h->d_e); dfree(h->d_Fw); dfree(h->d_Fe);
   dfree(h->d_flags); dfree(h->d_iters); dfree(h->d_stage); dfree(h->d_colstage); dfree(h->d_guess);
+  dfree(h->d_prev);
   dfree(h->d_scratch);
   dfree(h->d_mlp);
   dfree(h->d_ctr);
+  dfree(h->d_order);
+  dfree(h->d_order_bins);
   drop_graphs(h);
   dfree(h->d_clock);
   if (h->h_clock) cudaFreeHost(h->h_clock);
@@ -1103,6 +1143,7 @@ int clm_step_host(clm_handle* h, double* v, double* ti, double* e, double* Fw, d
     CLM_CUDA(h, ref_to_internal(L, Fi, h->stream, T0, T1 - T0));
     A.tile_begin = T0;
     A.tile_end = T1;
+    A.order = nullptr;  // a chunk's launch covers its own tiles' columns
     for (int s0 = 0; s0 < nsteps; s0 += 64) {
       StepClock clk;
       clk.t0 = step_time(t, s0, dt);
@@ -1352,6 +1393,9 @@ int clm_load_mlp(clm_handle* h, const void* weights, int64_t nbytes) {
     CLM_CUDA(h, cudaMalloc(&h->d_guess, gb));
     CLM_CUDA(h, cudaMemsetAsync(h->d_guess, 0xFF, gb, h->stream));  // NaN: no guess
   }
+  if (!h->d_prev)
+    CLM_CUDA(h, cudaMalloc(&h->d_prev, sizeof(double) * 2 * (size_t)std::max<int64_t>(h->ncells_int, 1)));
+  CLM_CUDA(h, restart_guess_history(h));
   CLM_CUDA(h, cudaStreamSynchronize(h->stream));
   return CLM_OK;
 }

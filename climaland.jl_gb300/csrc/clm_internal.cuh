@@ -60,6 +60,9 @@ struct StepArgs {
   int32_t* iters;       // [stride]
   const float* guess = nullptr;  // learned Newton guess (internal layout, 2 per cell) or null
   int* tile_ctr = nullptr;       // dynamic tile order: [next tile, warps done], or null (static)
+  // iteration-class order (tolerance mode): warp w of the launch takes the
+  // slots order[32 w + lane], or null for the tiles' own slots
+  const int* order = nullptr;
   Earth E;
   EHScalars sc;
   int bc_tw, bc_th, bc_bw, bc_bh;

@@ -439,11 +439,14 @@ __global__ void features_kernel(StepArgs A, double t, double dt, float* __restri
 }
 
 // guess[0][cell] = delta vartheta_l, guess[1][cell] = delta rho_e_int
-// (internal layout), for every 20-layer column. A warp takes 16 columns;
-// its two half-warps build the features of layers 0-9 and 10-19.
+// (internal layout), for every 20-layer column: the column's previous
+// increment (its state now minus `prev`, the state at the previous guess)
+// plus the network's predicted change of the increment; `prev` then takes
+// the current state. A warp takes 16 columns; its two half-warps build the
+// features of layers 0-9 and 10-19.
 __global__ void __launch_bounds__(kInferWarps * 32)
     guess_kernel(StepArgs A, const float* __restrict__ P, const float* __restrict__ norm,
-                 StepClock clk, float* __restrict__ guess) {
+                 StepClock clk, float* __restrict__ guess, double* __restrict__ prev) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   InferSmem& S = *reinterpret_cast<InferSmem*>(smem_raw);
   stage_forward(S, P, norm);
@@ -484,7 +487,11 @@ __global__ void __launch_bounds__(kInferWarps * 32)
         if (A.L.col_n[s] != kMlpLayers) continue;
         const int k = o % kMlpLayers;
         const int64_t cell = A.L.tile_off[s / kTile] + (int64_t)k * kTile + s % kTile;
-        guess[(o < kMlpLayers ? 0 : nci) + cell] = F.Y[j][q] * S.out_std[o] + S.out_mean[o];
+        const int64_t slot = (o < kMlpLayers ? 0 : nci) + cell;
+        const double cur = o < kMlpLayers ? A.v[cell] : A.e[cell];
+        const double inc = cur - prev[slot];
+        prev[slot] = cur;
+        guess[slot] = (float)(inc + (double)(F.Y[j][q] * S.out_std[o] + S.out_mean[o]));
       }
     __syncwarp();
   }
@@ -552,8 +559,8 @@ cudaError_t mlp_guess_setup(int64_t rows, int* grid) {
 }
 
 cudaError_t mlp_guess(const StepArgs& A, const float* P, const float* norm, const StepClock& clk,
-                      float* guess, int grid, cudaStream_t st) {
-  mlp::guess_kernel<<<grid, mlp::kInferWarps * 32, sizeof(mlp::InferSmem), st>>>(A, P, norm, clk, guess);
+                      float* guess, double* prev, int grid, cudaStream_t st) {
+  mlp::guess_kernel<<<grid, mlp::kInferWarps * 32, sizeof(mlp::InferSmem), st>>>(A, P, norm, clk, guess, prev);
   return cudaGetLastError();
 }
 

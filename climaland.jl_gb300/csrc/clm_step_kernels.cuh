@@ -98,10 +98,10 @@ __global__ void __launch_bounds__(128, 1)
   const int tend = A.tile_end < 0 ? A.L.ntiles : A.tile_end;
   int tile = A.tile_begin + (dyn ? claim_tile(A.tile_ctr) : gwarp);
   while (tile < tend) {
-    const int s = tile * kTile + lane;
+    const int s = A.order ? A.order[tile * kTile + lane] : tile * kTile + lane;
     const int n = A.L.col_n[s];
     if (n > 0) {
-      const int64_t base = A.L.tile_off[tile] + lane;
+      const int64_t base = A.L.tile_off[s / kTile] + s % kTile;
       B.gv = Col<double>{A.v + base, kTile};
       B.gti = Col<double>{A.ti + base, kTile};
       B.ge = Col<double>{A.e + base, kTile};
@@ -154,10 +154,10 @@ __global__ void __launch_bounds__(128, 1)
   const int tend = A.tile_end < 0 ? A.L.ntiles : A.tile_end;
   int tile = A.tile_begin + (dyn ? claim_tile(A.tile_ctr) : gwarp);
   while (tile < tend) {
-    const int s = tile * kTile + lane;
+    const int s = A.order ? A.order[tile * kTile + lane] : tile * kTile + lane;
     const int n = A.L.col_n[s];
     if (n > 0) {
-      const int64_t base = A.L.tile_off[tile] + lane;
+      const int64_t base = A.L.tile_off[s / kTile] + s % kTile;
       B.gv = Col<double>{A.v + base, kTile};
       double Fw = A.Fw[s];
       uint32_t flags = 0;

@@ -80,6 +80,8 @@ mutable struct ClmConfig
     column_offset::Int64
     host_chunks::Int32
     runoff::Int32
+    tol_regroup::Int32
+    pad1::Int32
     ClmConfig() = new()
 end
 

@@ -371,6 +371,12 @@ typedef struct clm_config {
                              rain-pulse hash uses the global column index  */
   int32_t host_chunks;    /* clm_step_host pipeline depth (0: by size)      */
   int32_t runoff;         /* enum clm_runoff (CLM_BC_PRECIP_RUNOFF)         */
+  int32_t tol_regroup;    /* tolerance mode: 1 (default) groups columns into
+                             warps by their last Newton iteration count each
+                             step (a warp runs as many iterations as its
+                             slowest column); 0 keeps the depth-sorted tiles.
+                             Results do not depend on it                    */
+  int32_t pad1;
 } clm_config;
 
 typedef struct clm_handle clm_handle;
@@ -558,13 +564,15 @@ int clm_solve(clm_handle* h, const double* W_vv, const double* W_ev,
 /* ---- learned Newton guess (no reference counterpart) ------------------
  * A small MLP (inputs: the 20-layer vartheta_l, theta_i, T profiles, top
  * water and heat fluxes, alpha, n, nu, log10 K_sat, dt; two hidden layers
- * of 64 with GELU; outputs: the step's increments of vartheta_l and
- * rho_e_int) predicts where each column's Newton solve will end. With
+ * of 64 with GELU; outputs: 20-layer vartheta_l and rho_e_int) predicts how
+ * each column's step increment changes from its previous step's. With
  * cfg->learned_guess = 1 (EnergyHydrology, tolerance mode, 20-layer
- * columns) Newton starts from u_n + prediction; a column whose first Newton
- * increment exceeds the predicted one restarts from the zero guess
- * (CLM_COL_GUESS_FALLBACK). Weights are a blob of clm_mlp_blob_bytes()
- * bytes written by clm_mlp_get. */
+ * columns) Newton starts from u_n + (u_n - u_{n-1}) + prediction, u_{n-1}
+ * the state at the previous guess; a column whose first Newton increment
+ * exceeds its guessed one restarts from the plain start
+ * (CLM_COL_GUESS_FALLBACK). clm_load_mlp restarts the history (the first
+ * guess after it is the prediction alone); clm_set_state keeps it. Weights
+ * are a blob of clm_mlp_blob_bytes() bytes written by clm_mlp_get. */
 int clm_load_mlp(clm_handle* h, const void* weights, int64_t nbytes);
 
 /* Raw network inputs of every 20-layer column at time t (device array of

@@ -206,3 +206,21 @@ def test_restart_from_saved_state_bitwise_equals_continuing(torch, make):
             g.set_state_device([None if d is None else d.data_ptr() for d in dev])
             g.step(w.t0 + 7 * w.dt, w.dt, 5)
             same_state(ref, g.get_state())
+
+
+@pytest.mark.parametrize("make", [lambda: WL.full_scale_c4(ncol=3000, seed=9),
+                                  lambda: WL.uneven_c2(ncol=3000, seed=9),
+                                  lambda: WL.richards_c0(ncol=3000, seed=9)])
+def test_tolerance_mode_regrouping_bitwise_equals_tile_order(torch, make):
+    """Tolerance mode re-sorts the columns into warps by their last Newton
+    iteration count after every step; the states, flags and iteration counts
+    are those of the depth-sorted tiles bit for bit (direct launches and
+    graph replay, FP64 and mixed)."""
+    w = make()
+    tol = dict(newton_mode=A.CLM_NEWTON_TOL, max_iters=20, newton_tol=1e-8, energy_norm_scale=1e-9)
+    calls = [(w.t0, 5), (w.t0 + 5 * w.dt, 3)]
+    for prec in (A.CLM_PREC_FP64, A.CLM_PREC_MIXED):
+        ref = _run(w, calls, precision=prec, tol_regroup=0, **tol)
+        _same(ref, _run(w, calls, precision=prec, tol_regroup=1, **tol))
+        _same(ref, _run(w, calls, precision=prec, tol_regroup=1, graph=1, **tol))
+        _same(ref, _run(w, calls, precision=prec, tol_regroup=1, schedule=A.CLM_SCHED_DYNAMIC, **tol))

@@ -109,19 +109,28 @@ def test_features_kernel_matches_host(torch):
 
 
 def test_learned_guess_saves_newton_iterations(torch):
-    """Train on the plain solver's trajectories, then solve unseen columns to
-    the same tolerance with and without the guess: fewer iterations, same
-    answer (the plain solve is the reference for its error)."""
+    """Train on the plain solver's trajectories, then solve unseen columns of
+    the learned-guess evaluation configuration (65,536 x 20) to the bench's
+    tolerance (1e-8) with and without the guess: fewer Newton iterations per
+    column, the same answer within 1e-8 (the plain solve is the reference
+    for its error). The guess is the previous increment plus the network's
+    predicted change; the previous increment alone (the network's output
+    held at zero) is measured beside it."""
+    tol = dict(LG.TOL, newton_tol=1e-8)
     wtr = LG.training_workload(ncol=16384, seed=0)
-    X, Y = LG.generate(wtr, 24)
+    X, Y = LG.generate(wtr, 24, newton=tol)
     res = LG.train(X, Y, steps=3000, batch=4096, lr=2e-3)
-    wev = LG.eval_workload(ncol=8192, seed=1)
+    tr = LG.Trainer(seed=0)
+    tr.set_normalization(np.zeros(LG.N_IN), np.ones(LG.N_IN), np.zeros(LG.N_OUT), np.full(LG.N_OUT, 1e-30))
+    zero_blob = tr.blob()
+    tr.close()
+    wev = LG.eval_workload(ncol=65536, seed=1)
     nsteps = 24
     out = {}
-    for name, guess in (("plain", False), ("learned", True)):
-        with SoilColumns(wev, learned_guess=1 if guess else None, **LG.TOL) as g:
-            if guess:
-                g.load_mlp(res.blob)
+    for name, blob in (("plain", None), ("learned", res.blob), ("previous_increment", zero_blob)):
+        with SoilColumns(wev, learned_guess=1 if blob else None, **tol) as g:
+            if blob:
+                g.load_mlp(blob)
             iters = []
             t = wev.t0
             for i in range(nsteps):
@@ -130,13 +139,16 @@ def test_learned_guess_saves_newton_iterations(torch):
                 f, it = g.status()
                 iters.append(it.astype(np.float64))
             out[name] = (g.get_state(), np.mean(iters), f)
-    (sp, ip, fp), (sl, il, fl) = out["plain"], out["learned"]
-    colerr = np.max(np.abs(sp[0] - sl[0]).reshape(wev.ncol, 20), axis=1)
-    frac_ok = float(np.mean(colerr <= 1e-8))
+    sp, ip, _ = out["plain"]
     stats = dict(train_rows=res.nrows, train_seconds=res.seconds, loss_first=float(res.loss[:50].mean()),
-                 loss_last=float(res.loss[-50:].mean()), iters_plain=ip, iters_learned=il,
-                 fallback_frac=float(np.mean((fl & A.CLM_COL_GUESS_FALLBACK) > 0)),
-                 frac_cols_within_1e8=frac_ok, max_err=float(colerr.max()))
+                 loss_last=float(res.loss[-50:].mean()), iters_plain=ip)
+    for name in ("learned", "previous_increment"):
+        sl, il, fl = out[name]
+        colerr = np.max(np.abs(sp[0] - sl[0]).reshape(wev.ncol, 20), axis=1)
+        stats[f"iters_{name}"] = il
+        stats[f"fallback_frac_{name}"] = float(np.mean((fl & A.CLM_COL_GUESS_FALLBACK) > 0))
+        stats[f"frac_cols_within_1e8_{name}"] = float(np.mean(colerr <= 1e-8))
+        stats[f"max_err_{name}"] = float(colerr.max())
     print("LEARNED " + json.dumps(stats))
-    assert il < ip
-    assert frac_ok >= 0.99
+    assert stats["iters_learned"] < ip
+    assert stats["frac_cols_within_1e8_learned"] >= 0.99
