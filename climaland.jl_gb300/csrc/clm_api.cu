@@ -349,11 +349,13 @@ struct Launch {
 // Steps are fused in one launch (a column stays in shared memory between
 // steps), 64 per launch so that one launch stays short; with the learned
 // guess, the network predicts each step's increment from the state at its
-// start: one guess launch, then one step launch, per step.
+// start: one guess launch, then one step launch, per step; with tolerance
+// regrouping, one step launch per step, each followed by the regrouping.
 std::vector<Launch> launch_sequence(const clm_handle* h, int nsteps) {
   std::vector<Launch> seq;
   if (h->cfg.learned_guess || regroups(h)) {  // per step: guess, or regroup, in between
-    for (int i = 0; i < nsteps; ++i) seq.push_back({i, 1, true});
+    const bool guess = h->cfg.learned_guess != 0;
+    for (int i = 0; i < nsteps; ++i) seq.push_back({i, 1, guess});
   } else {
     const int chunk = 64;
     for (int s0 = 0; s0 < nsteps; s0 += chunk) seq.push_back({s0, std::min(chunk, nsteps - s0), false});

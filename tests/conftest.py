@@ -27,5 +27,7 @@ def pytest_terminal_summary(terminalreporter):
     for name, st in gc.SUMMARY:
         errs = " ".join(f"{k[:-len('_max_err_all')]}={v:.2e}" for k, v in st.items() if k.endswith("_max_err_all"))
         tr.write_line(f"{name}: {st['columns']} cols x {st.get('steps', '?')} steps, noise {st.get('noise')}, "
-                      f"excused {st['excused']} ({100 * st['excused_frac']:.2f} %), "
-                      f"err/spread max {st['excused_err_over_spread_max']:.2g}, {errs}")
+                      f"excused {st['excused']} ({100 * st['excused_frac']:.2f} %; oracle itself "
+                      f"{100 * st.get('oracle_self_excused_frac', 0.0):.2f} %), "
+                      f"err/spread max {st['excused_err_over_spread_max']:.2g}, "
+                      f"re-measured {st.get('rechecked', 0)}, {errs}")

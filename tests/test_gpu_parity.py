@@ -415,19 +415,24 @@ def test_stretched_columns(name):
     report(f"stretched_{name}", check_parity(make(), nsteps, **kw))
 
 
-@pytest.mark.parametrize("name,make", [
-    ("full_scale", lambda: WL.full_scale_c4(ncol=1024)),
-    ("stretched_full_scale", lambda: WL.stretched(WL.full_scale_c4(ncol=1024))),
-    ("stretched_richards", lambda: WL.stretched(WL.richards_c0())),
+@pytest.mark.parametrize("name,make,bound", [
+    ("full_scale", lambda: WL.full_scale_c4(ncol=1024), 1e-11),
+    ("stretched_full_scale", lambda: WL.stretched(WL.full_scale_c4(ncol=1024)), 1e-11),
+    ("stretched_richards", lambda: WL.stretched(WL.richards_c0()), 1e-9),
 ])
-def test_mixed_path_converges_to_the_oracle_root(name, make):
+def test_mixed_path_converges_to_the_oracle_root(name, make, bound):
     """Eight fixed Newton iterations on both: one step of the mixed path from
     states along the oracle's trajectory lands on the oracle's step to 1e-11
     (the float Jacobian changes only how fast Newton converges; the
-    residual's closures are double-float, ~2^-44 relative)."""
+    residual's closures are double-float, ~2^-44 relative). On the stretched
+    RichardsModel columns Newton with the reference's approximate Jacobian
+    converges only linearly in saturated layers (after 8 iterations the
+    oracle itself is up to 2.5e-4 from its 40-iteration result), so there the
+    two iterations are compared at equal counts, to 1e-9 (1.3e-10 measured
+    on the 1024 columns)."""
     from gpu_common import step_deviation
 
     w = make()
     w.cfg.max_iters = 8
     dev = step_deviation(w, 24, every=4, precision=A.CLM_PREC_MIXED)
-    assert float(dev.max()) <= 1e-11, float(dev.max())
+    assert float(dev.max()) <= bound, float(dev.max())
