@@ -1037,6 +1037,9 @@ int clm_step_async(clm_handle* h, double t, double dt, int32_t nsteps) {
   if (nsteps == 0) return CLM_OK;
   if (h->cfg.learned_guess && (!h->d_mlp || !h->d_guess))
     return fail(h, CLM_ERR_STATE, "clm_load_mlp has not been called");
+  // the step kernels OR each column's flags into d_flags: one call's flags
+  // cover all of its steps, whatever its launches
+  CLM_CUDA(h, cudaMemsetAsync(h->d_flags, 0, sizeof(uint32_t) * h->stride, h->stream));
   if (h->cfg.graph) {
     // a caller that is capturing the stream itself records the plain launches
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -1113,6 +1116,7 @@ int clm_step_host(clm_handle* h, double* v, double* ti, double* e, double* Fw, d
   }
   const Layout L = layout_of(h);
   StepArgs A = step_args(h);
+  CLM_CUDA(h, cudaMemsetAsync(h->d_flags, 0, sizeof(uint32_t) * h->stride, h->stream));
   double* hf[3] = {v, ti, e};
   double* df[3] = {h->d_v, h->d_ti, h->d_e};
   double* hc[2] = {Fw, Fe};

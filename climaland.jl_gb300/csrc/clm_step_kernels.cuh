@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(128, 1)
                                      iters);
       A.Fw[s] = Fw;
       A.Fe[s] = Fe;
-      A.flags[s] = flags;
+      A.flags[s] |= flags;  // cleared at the start of each step call
       A.iters[s] = iters;
     }
     tile = dyn ? A.tile_begin + claim_tile(A.tile_ctr) : tile + nwarps;
@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(128, 1)
       const auto G = GeomOf<kStr>::make(A, base, s, n);
       richards_column<JT, CM>(A, Tb, s, n, A.L.perm[s], B, J, G, t0, dt, nsteps, Fw, flags, iters);
       A.Fw[s] = Fw;
-      A.flags[s] = flags;
+      A.flags[s] |= flags;  // cleared at the start of each step call
       A.iters[s] = iters;
     }
     tile = dyn ? A.tile_begin + claim_tile(A.tile_ctr) : tile + nwarps;

@@ -514,9 +514,9 @@ int clm_set_stream(clm_handle* h, void* cuda_stream);
  * energy_hydrology.jl:1282-1320) of the current state, per column. */
 int clm_get_budgets(clm_handle* h, double* total_water, double* total_energy);
 
-/* Per-column status flags (CLM_COL_*) and Newton iteration counts of the
- * last step call (either pointer may be NULL). Stands in for
- * NaNCheckCallback (utils.jl:684-694). */
+/* Per-column status flags (CLM_COL_*, OR-ed over every step of the last
+ * step call) and Newton iteration counts (of that call's last step); either
+ * pointer may be NULL. Stands in for NaNCheckCallback (utils.jl:684-694). */
 int clm_get_status(clm_handle* h, uint32_t* flags, int32_t* newton_iters);
 
 /* ---- closure-level entry points (for parity of each closure) ---------
