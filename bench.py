@@ -370,25 +370,24 @@ def forms_block(args, torch, stream):
     wtr = WL.full_scale_c4(ncol=65536, seed=7)
     t0 = time.perf_counter()
     X, Y = LG.generate(wtr, 32, newton=tol)  # trajectories at the evaluated tolerance
-    res = LG.train(X, Y, steps=20000, batch=4096, lr=2e-3)
+    # the network as trained (no validation gate), to show what it adds
+    res = LG.train(X, Y, steps=20000, batch=4096, lr=2e-3, gate=False)
     gen_train_s = time.perf_counter() - t0
     del X, Y
     plain_tol = run(w4, **tol)
     mixed_tol = run(w4, precision=A.CLM_PREC_MIXED, **tol)
     learned = run(w4, blob=res.blob, learned_guess=1, precision=A.CLM_PREC_MIXED, **tol)
     # the previous increment alone (the network's output held at zero)
-    tr = LG.Trainer(seed=0)
-    tr.set_normalization(np.zeros(LG.N_IN), np.ones(LG.N_IN), np.zeros(LG.N_OUT), np.full(LG.N_OUT, 1e-30))
-    zero_blob = tr.blob()
-    tr.close()
-    persist = run(w4, blob=zero_blob, learned_guess=1, precision=A.CLM_PREC_MIXED, **tol)
+    persist = run(w4, blob=LG.zero_change_blob(), learned_guess=1, precision=A.CLM_PREC_MIXED, **tol)
     out["full_scale_subset"]["plain_fp64_tol1e-8"] = pub(plain_tol, plain, w4, tol)
     out["full_scale_subset"]["mixed_tol1e-8"] = pub(mixed_tol, plain, w4, tol)
     out["full_scale_subset"]["learned_mixed_tol1e-8"] = pub(learned, plain, w4, tol)
     out["full_scale_subset"]["previous_increment_mixed_tol1e-8"] = pub(persist, plain, w4, tol)
     out["full_scale_subset"]["learned_training"] = {
         "pairs": res.nrows, "train_steps": 20000, "loss_first": float(res.loss[:50].mean()),
-        "loss_last": float(res.loss[-200:].mean()), "train_s": res.seconds, "gen_train_s": gen_train_s}
+        "loss_last": float(res.loss[-200:].mean()), "train_s": res.seconds, "gen_train_s": gen_train_s,
+        "heldout_mse": res.val_mse, "heldout_mse_zero_change": res.val_mse_zero,
+        "validation_gate_would_replace_it": bool(not res.val_mse < res.val_mse_zero)}
     # (2) uneven columns, 4-30 layers, CSR: autotuned launch, CUDA graph replay
     w2 = WL.uneven_c2(ncol=args.forms_ncol, seed=0)
     u64 = run(w2, graph=1)
@@ -452,7 +451,7 @@ def full_run(args, torch):
     t0 = time.perf_counter()
     wtr = WL.full_scale_c4(ncol=65536, seed=7)
     X, Y = LG.generate(wtr, 32, newton=tol)
-    res = LG.train(X, Y, steps=20000, batch=4096, lr=2e-3)
+    res = LG.train(X, Y, steps=20000, batch=4096, lr=2e-3)  # validation-gated
     del X, Y
     train_s = time.perf_counter() - t0
     mx = dict(precision=A.CLM_PREC_MIXED)
@@ -460,7 +459,10 @@ def full_run(args, torch):
              ("mixed_tol1e-8", dict(mx, **tol), None),
              ("learned_mixed_tol1e-8_graph", dict(mx, learned_guess=1, graph=1, **tol), res.blob)]
     out = {"workload": w.name, "columns": w.ncol, "steps": nst, "simulated_days": nst * w.dt / 86400.0,
-           "learned_training_s": train_s, "timing": f"device, calls of {chunk} steps"}
+           "learned_training_s": train_s, "learned_heldout_mse": res.val_mse,
+           "learned_heldout_mse_zero_change": res.val_mse_zero,
+           "learned_gated_to_previous_increment": res.gated,
+           "timing": f"device, calls of {chunk} steps"}
     for name, kw, blob in forms:
         with D.SoilColumns(w, **kw) as g:
             g.set_stream(stream.cuda_stream)
@@ -500,6 +502,13 @@ def full_run(args, torch):
     print(json.dumps({"full_run": out}), flush=True)
 
 
+def WL_full_scale(ncol, seed):
+    """Training columns for the learned guess: the full-scale distributions
+    with another seed than the timed columns."""
+    from climaland_gb300 import workloads as WL
+    return WL.full_scale_c4(ncol=ncol, seed=seed)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -509,6 +518,11 @@ def main():
     ap.add_argument("--config", default="c4")
     ap.add_argument("--ncol", type=int, default=None)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--newton", default="fixed", choices=["fixed", "tol"],
+                    help="fixed: the configuration's 3 iterations; tol: stop at 1e-8 (at most 20)")
+    ap.add_argument("--guess", default="none", choices=["none", "previous", "learned"],
+                    help="Newton start (tolerance mode): U, the previous increment, or the previous "
+                         "increment + the network's change (trained at start, validation-gated)")
     ap.add_argument("--top", default="flux", choices=["flux", "atmos"],
                     help="top boundary: the workload's flux forcing, or the atmosphere-driven "
                          "boundary (EnergyHydrology)")
@@ -559,7 +573,21 @@ def main():
     w = make_workload(args.config, args.ncol, rank, args.top)
     prec = A.CLM_PREC_MIXED if args.precision == "mixed" else A.CLM_PREC_FP64
     nl = float(w.nlayers.mean())
-    g = D.SoilColumns(w, precision=prec)
+    newton = {}
+    if args.newton == "tol" or args.guess != "none":
+        newton = dict(newton_mode=A.CLM_NEWTON_TOL, max_iters=20, newton_tol=1e-8, energy_norm_scale=1e-9)
+    blob = None
+    if args.guess != "none":
+        from climaland_gb300 import learned as LG
+        if args.guess == "learned":
+            X, Y = LG.generate(WL_full_scale(65536, 7), 32, newton=newton)
+            blob = LG.train(X, Y, steps=20000, batch=4096, lr=2e-3).blob
+            del X, Y
+        else:
+            blob = LG.zero_change_blob()
+    g = D.SoilColumns(w, precision=prec, learned_guess=1 if blob else None, **newton)
+    if blob:
+        g.load_mlp(blob)
     stream = torch.cuda.Stream()
     g.set_stream(stream.cuda_stream)
     tune = None
@@ -679,18 +707,25 @@ def main():
         "data": "synthetic",
         "config": {"workload": w.name, "columns_per_gpu": w.ncol, "layers": int(w.nlayers.max()),
                    "model": "EnergyHydrology" if w.cfg.model == 1 else "RichardsModel",
-                   "newton": f"fixed {w.cfg.max_iters} iterations", "precision": args.precision,
+                   "newton": (f"fixed {w.cfg.max_iters} iterations" if not newton else
+                              "tolerance 1e-8 (at most 20 iterations), warps regrouped by iteration count"),
+                   "newton_start": {"none": "U", "previous": "previous increment",
+                                    "learned": "previous increment + network"}[args.guess],
+                   "precision": args.precision,
                    "l2": "inputs larger than L2 (state 48 B x cells)", "dt_s": w.dt},
         "e2e": {"value": e2e, "unit": "column-steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": h2d, "steps": e2e_steps},
-        "gpu_launches": args.steps,
+        # per step: the step kernel; in tolerance mode the regrouping's
+        # three kernels; with a guess, the guess kernel
+        "gpu_launches": args.steps * (1 + (3 if newton else 0) + (1 if blob else 0)),
         "launch_config": dict(g.launch_config(), autotuned=tune is not None),
         "roofline": roofline,
         "compute_bound": compute,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "status": {"flagged_columns": int(np.count_nonzero(flags)),
-                   "newton_iters_max": int(iters.max())},
+                   "newton_iters_max": int(iters.max()),
+                   "newton_iters_mean_last_step": float(iters.mean())},
         "forms": forms,
     }
     print(json.dumps(line), flush=True)

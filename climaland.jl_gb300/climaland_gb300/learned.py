@@ -154,16 +154,36 @@ class TrainResult:
     loss: np.ndarray
     nrows: int
     seconds: float
+    val_mse: float = float("nan")       # held-out rows: the network's mean squared error
+    val_mse_zero: float = float("nan")  # the same for a predicted change of zero
+    gated: bool = False                 # blob is the zero-change network (see train)
 
 
-def train(X, Y, steps=4000, batch=4096, lr=2e-3, seed=0):
+def zero_change_blob() -> bytes:
+    """Weights whose prediction is a change of zero: the guess is then the
+    column's previous step increment alone."""
+    tr = Trainer(seed=0)
+    tr.set_normalization(np.zeros(N_IN), np.ones(N_IN), np.zeros(N_OUT), np.full(N_OUT, 1e-30))
+    blob = tr.blob()
+    tr.close()
+    return blob
+
+
+def train(X, Y, steps=4000, batch=4096, lr=2e-3, seed=0, val_frac=0.05, gate=True):
     """Standardise, shuffle and train with the library's kernels; returns the
-    weight blob for clm_load_mlp."""
+    weight blob for clm_load_mlp. A fraction val_frac of the shuffled rows is
+    held out; with gate, a network whose held-out error is not below that of
+    predicting no change is replaced by the zero-change weights (the guess
+    falls back to the previous increment)."""
     import time
     torch = _torch()
     gen = torch.Generator(device="cuda")
     gen.manual_seed(seed)
     perm = torch.randperm(X.shape[0], device="cuda", generator=gen)
+    nval = int(X.shape[0] * val_frac)
+    Xv = X[perm[:nval]].contiguous()
+    Yv = Y[perm[:nval]].contiguous()
+    perm = perm[nval:]
     Xs = X[perm].contiguous()
     Ys = Y[perm].contiguous()
     in_mean = Xs.mean(0).cpu().numpy()
@@ -184,9 +204,18 @@ def train(X, Y, steps=4000, batch=4096, lr=2e-3, seed=0):
         done += k
     el = time.perf_counter() - t0
     blob = tr.blob()
+    val = zero = float("nan")
+    if nval > 0:
+        P = tr.predict(Xv)
+        val = float(((P - Yv) ** 2).mean())
+        zero = float((Yv ** 2).mean())
     tr.close()
+    gated = bool(gate and nval > 0 and not val < zero)
+    if gated:
+        blob = zero_change_blob()
     loss = np.concatenate(losses) / (batch * N_OUT)
-    return TrainResult(blob=blob, loss=loss, nrows=int(X.shape[0]), seconds=el)
+    return TrainResult(blob=blob, loss=loss, nrows=int(Xs.shape[0]), seconds=el, val_mse=val,
+                       val_mse_zero=zero, gated=gated)
 
 
 def eval_workload(ncol=262144, seed=0):

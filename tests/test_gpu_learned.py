@@ -80,6 +80,19 @@ def test_training_fits_a_smooth_map(torch):
     res = LG.train(Xd, Yd, steps=3000, batch=2048, lr=2e-3)
     print(f"TRAIN loss {res.loss[:50].mean():.4f} -> {res.loss[-50:].mean():.4f} in {res.seconds:.2f}s")
     assert res.loss[-50:].mean() < 0.2 * res.loss[:50].mean()
+    # the held-out rows confirm the fit: the network is kept
+    assert res.val_mse < 0.2 * res.val_mse_zero and not res.gated
+
+
+def test_validation_gate_drops_a_network_that_predicts_nothing(torch):
+    """Targets independent of the inputs (zero-mean noise): the held-out error
+    is not below predicting zero, so train returns the zero-change weights."""
+    rng = np.random.default_rng(4)
+    n = 32768
+    X = rng.normal(size=(n, LG.N_IN)).astype(np.float32)
+    Y = rng.normal(size=(n, LG.N_OUT)).astype(np.float32)
+    res = LG.train(torch.tensor(X, device="cuda"), torch.tensor(Y, device="cuda"), steps=1000, batch=2048)
+    assert res.gated and res.blob == LG.zero_change_blob(), (res.val_mse, res.val_mse_zero)
 
 
 def test_features_kernel_matches_host(torch):
@@ -114,16 +127,15 @@ def test_learned_guess_saves_newton_iterations(torch):
     tolerance (1e-8) with and without the guess: fewer Newton iterations per
     column, the same answer within 1e-8 (the plain solve is the reference
     for its error). The guess is the previous increment plus the network's
-    predicted change; the previous increment alone (the network's output
-    held at zero) is measured beside it."""
+    predicted change (train's validation gate keeps the network only where
+    its held-out error is below that of predicting no change); the previous
+    increment alone (the network's output held at zero) is measured beside
+    it."""
     tol = dict(LG.TOL, newton_tol=1e-8)
     wtr = LG.training_workload(ncol=16384, seed=0)
     X, Y = LG.generate(wtr, 24, newton=tol)
     res = LG.train(X, Y, steps=3000, batch=4096, lr=2e-3)
-    tr = LG.Trainer(seed=0)
-    tr.set_normalization(np.zeros(LG.N_IN), np.ones(LG.N_IN), np.zeros(LG.N_OUT), np.full(LG.N_OUT, 1e-30))
-    zero_blob = tr.blob()
-    tr.close()
+    zero_blob = LG.zero_change_blob()
     wev = LG.eval_workload(ncol=65536, seed=1)
     nsteps = 24
     out = {}
@@ -141,7 +153,8 @@ def test_learned_guess_saves_newton_iterations(torch):
             out[name] = (g.get_state(), np.mean(iters), f)
     sp, ip, _ = out["plain"]
     stats = dict(train_rows=res.nrows, train_seconds=res.seconds, loss_first=float(res.loss[:50].mean()),
-                 loss_last=float(res.loss[-50:].mean()), iters_plain=ip)
+                 loss_last=float(res.loss[-50:].mean()), heldout_mse=res.val_mse,
+                 heldout_mse_zero_change=res.val_mse_zero, gated=res.gated, iters_plain=ip)
     for name in ("learned", "previous_increment"):
         sl, il, fl = out[name]
         colerr = np.max(np.abs(sp[0] - sl[0]).reshape(wev.ncol, 20), axis=1)
