@@ -520,6 +520,8 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--newton", default="fixed", choices=["fixed", "tol"],
                     help="fixed: the configuration's 3 iterations; tol: stop at 1e-8 (at most 20)")
+    ap.add_argument("--no-regroup", action="store_true",
+                    help="tolerance mode without regrouping the columns into warps by iteration count")
     ap.add_argument("--guess", default="none", choices=["none", "previous", "learned"],
                     help="Newton start (tolerance mode): U, the previous increment, or the previous "
                          "increment + the network's change (trained at start, validation-gated)")
@@ -585,6 +587,8 @@ def main():
             del X, Y
         else:
             blob = LG.zero_change_blob()
+    if newton and args.no_regroup:
+        newton["tol_regroup"] = 0
     g = D.SoilColumns(w, precision=prec, learned_guess=1 if blob else None, **newton)
     if blob:
         g.load_mlp(blob)
@@ -708,7 +712,8 @@ def main():
         "config": {"workload": w.name, "columns_per_gpu": w.ncol, "layers": int(w.nlayers.max()),
                    "model": "EnergyHydrology" if w.cfg.model == 1 else "RichardsModel",
                    "newton": (f"fixed {w.cfg.max_iters} iterations" if not newton else
-                              "tolerance 1e-8 (at most 20 iterations), warps regrouped by iteration count"),
+                              "tolerance 1e-8 (at most 20 iterations)" +
+                              ("" if args.no_regroup else ", warps regrouped by iteration count")),
                    "newton_start": {"none": "U", "previous": "previous increment",
                                     "learned": "previous increment + network"}[args.guess],
                    "precision": args.precision,
@@ -717,7 +722,7 @@ def main():
                 "d2h_bytes_per_step": h2d, "steps": e2e_steps},
         # per step: the step kernel; in tolerance mode the regrouping's
         # three kernels; with a guess, the guess kernel
-        "gpu_launches": args.steps * (1 + (3 if newton else 0) + (1 if blob else 0)),
+        "gpu_launches": args.steps * (1 + (3 if newton and not args.no_regroup else 0) + (1 if blob else 0)),
         "launch_config": dict(g.launch_config(), autotuned=tune is not None),
         "roofline": roofline,
         "compute_bound": compute,
