@@ -379,10 +379,13 @@ def forms_block(args, torch, stream):
     learned = run(w4, blob=res.blob, learned_guess=1, precision=A.CLM_PREC_MIXED, **tol)
     # the previous increment alone (the network's output held at zero)
     persist = run(w4, blob=LG.zero_change_blob(), learned_guess=1, precision=A.CLM_PREC_MIXED, **tol)
+    # the same start computed inside the step kernel (no network launch)
+    extrap = run(w4, learned_guess=A.CLM_GUESS_EXTRAPOLATE, precision=A.CLM_PREC_MIXED, **tol)
     out["full_scale_subset"]["plain_fp64_tol1e-8"] = pub(plain_tol, plain, w4, tol)
     out["full_scale_subset"]["mixed_tol1e-8"] = pub(mixed_tol, plain, w4, tol)
     out["full_scale_subset"]["learned_mixed_tol1e-8"] = pub(learned, plain, w4, tol)
     out["full_scale_subset"]["previous_increment_mixed_tol1e-8"] = pub(persist, plain, w4, tol)
+    out["full_scale_subset"]["extrapolated_mixed_tol1e-8"] = pub(extrap, plain, w4, tol)
     out["full_scale_subset"]["learned_training"] = {
         "pairs": res.nrows, "train_steps": 20000, "loss_first": float(res.loss[:50].mean()),
         "loss_last": float(res.loss[-200:].mean()), "train_s": res.seconds, "gen_train_s": gen_train_s,
@@ -451,17 +454,19 @@ def full_run(args, torch):
     t0 = time.perf_counter()
     wtr = WL.full_scale_c4(ncol=65536, seed=7)
     X, Y = LG.generate(wtr, 32, newton=tol)
-    res = LG.train(X, Y, steps=20000, batch=4096, lr=2e-3)  # validation-gated
+    res = LG.train(X, Y, steps=20000, batch=4096, lr=2e-3, gate=False)  # the network as trained
     del X, Y
     train_s = time.perf_counter() - t0
     mx = dict(precision=A.CLM_PREC_MIXED)
     forms = [("plain_fp64", {}, None), ("plain_fp64_tol1e-8", dict(tol), None), ("mixed", mx, None),
              ("mixed_tol1e-8", dict(mx, **tol), None),
-             ("learned_mixed_tol1e-8_graph", dict(mx, learned_guess=1, graph=1, **tol), res.blob)]
+             ("learned_mixed_tol1e-8_graph", dict(mx, learned_guess=1, graph=1, **tol), res.blob),
+             ("extrapolated_mixed_tol1e-8_graph",
+              dict(mx, learned_guess=A.CLM_GUESS_EXTRAPOLATE, graph=1, **tol), None)]
     out = {"workload": w.name, "columns": w.ncol, "steps": nst, "simulated_days": nst * w.dt / 86400.0,
            "learned_training_s": train_s, "learned_heldout_mse": res.val_mse,
            "learned_heldout_mse_zero_change": res.val_mse_zero,
-           "learned_gated_to_previous_increment": res.gated,
+           "learned_validation_gate_would_replace_it": bool(not res.val_mse < res.val_mse_zero),
            "timing": f"device, calls of {chunk} steps"}
     for name, kw, blob in forms:
         with D.SoilColumns(w, **kw) as g:
@@ -522,9 +527,11 @@ def main():
                     help="fixed: the configuration's 3 iterations; tol: stop at 1e-8 (at most 20)")
     ap.add_argument("--no-regroup", action="store_true",
                     help="tolerance mode without regrouping the columns into warps by iteration count")
-    ap.add_argument("--guess", default="none", choices=["none", "previous", "learned"],
-                    help="Newton start (tolerance mode): U, the previous increment, or the previous "
-                         "increment + the network's change (trained at start, validation-gated)")
+    ap.add_argument("--guess", default="none", choices=["none", "extrapolate", "previous", "learned"],
+                    help="Newton start (tolerance mode): U; the previous increment, inside the step "
+                         "kernel (extrapolate) or through the network's launch with the network's "
+                         "output held at zero (previous); or the previous increment + the network's "
+                         "change (learned: trained at start, validation-gated)")
     ap.add_argument("--top", default="flux", choices=["flux", "atmos"],
                     help="top boundary: the workload's flux forcing, or the atmosphere-driven "
                          "boundary (EnergyHydrology)")
@@ -579,7 +586,7 @@ def main():
     if args.newton == "tol" or args.guess != "none":
         newton = dict(newton_mode=A.CLM_NEWTON_TOL, max_iters=20, newton_tol=1e-8, energy_norm_scale=1e-9)
     blob = None
-    if args.guess != "none":
+    if args.guess in ("previous", "learned"):
         from climaland_gb300 import learned as LG
         if args.guess == "learned":
             X, Y = LG.generate(WL_full_scale(65536, 7), 32, newton=newton)
@@ -589,7 +596,8 @@ def main():
             blob = LG.zero_change_blob()
     if newton and args.no_regroup:
         newton["tol_regroup"] = 0
-    g = D.SoilColumns(w, precision=prec, learned_guess=1 if blob else None, **newton)
+    mode = A.CLM_GUESS_NETWORK if blob else (A.CLM_GUESS_EXTRAPOLATE if args.guess == "extrapolate" else None)
+    g = D.SoilColumns(w, precision=prec, learned_guess=mode, **newton)
     if blob:
         g.load_mlp(blob)
     stream = torch.cuda.Stream()
@@ -714,7 +722,8 @@ def main():
                    "newton": (f"fixed {w.cfg.max_iters} iterations" if not newton else
                               "tolerance 1e-8 (at most 20 iterations)" +
                               ("" if args.no_regroup else ", warps regrouped by iteration count")),
-                   "newton_start": {"none": "U", "previous": "previous increment",
+                   "newton_start": {"none": "U", "extrapolate": "previous increment (in the step kernel)",
+                                    "previous": "previous increment (network launch, zero output)",
                                     "learned": "previous increment + network"}[args.guess],
                    "precision": args.precision,
                    "l2": "inputs larger than L2 (state 48 B x cells)", "dt_s": w.dt},

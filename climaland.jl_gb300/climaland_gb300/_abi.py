@@ -42,6 +42,9 @@ CLM_PREC_FP64 = 0
 CLM_PREC_MIXED = 1
 CLM_NEWTON_FIXED = 0
 CLM_NEWTON_TOL = 1
+CLM_GUESS_NONE = 0
+CLM_GUESS_NETWORK = 1
+CLM_GUESS_EXTRAPOLATE = 2
 CLM_SCHED_STATIC = 0
 CLM_SCHED_DYNAMIC = 1
 CLM_BC_FLUX = 0

@@ -85,6 +85,7 @@ struct clm_handle {
   double* d_colstage = nullptr;  // 4 * stride: upload staging, W, E, spare
   float* d_guess = nullptr;  // learned guess, 2 x ncells_int (NaN: none)
   double* d_prev = nullptr;  // the state at the previous guess (vartheta_l, rho_e_int), 2 x ncells_int
+  bool prev_valid = false;   // d_prev holds a state of this layout (extrapolated guess)
   float* d_mlp = nullptr;    // network parameters then standardisation
   bool have_geometry = false, have_params = false, have_state = false;
   int wpc = 1;   // warps (32-column tiles) per CTA of the step kernel
@@ -199,7 +200,8 @@ StepArgs step_args(const clm_handle* h) {
   A.Fe = h->d_Fe;
   A.flags = h->d_flags;
   A.iters = h->d_iters;
-  A.guess = h->cfg.learned_guess ? h->d_guess : nullptr;
+  A.guess = h->cfg.learned_guess == CLM_GUESS_NETWORK ? h->d_guess : nullptr;
+  A.prev = h->cfg.learned_guess == CLM_GUESS_EXTRAPOLATE && h->prev_valid ? h->d_prev : nullptr;
   A.tile_ctr = h->sched == CLM_SCHED_DYNAMIC ? h->d_ctr : nullptr;
   A.order = regroups(h) ? h->d_order : nullptr;
   A.E = h->E;
@@ -288,6 +290,11 @@ int build_layout(clm_handle* h, const std::vector<int>& nl) {
   dfree(h->d_tile_off); dfree(h->d_tile_n); dfree(h->d_col_n); dfree(h->d_perm); dfree(h->d_ref_off);
   dfree(h->d_slot_ref);
   dfree(h->d_order);
+  // the guesses and their history are per layout (a new layout needs
+  // clm_load_mlp again for the network guess)
+  dfree(h->d_guess);
+  dfree(h->d_prev);
+  h->prev_valid = false;
   cudaStream_t st = h->stream;
   CLM_CUDA(h, cudaMalloc(&h->d_tile_off, sizeof(int64_t) * h->ntiles));
   CLM_CUDA(h, cudaMalloc(&h->d_tile_n, sizeof(int) * h->ntiles));
@@ -353,8 +360,8 @@ struct Launch {
 // regrouping, one step launch per step, each followed by the regrouping.
 std::vector<Launch> launch_sequence(const clm_handle* h, int nsteps) {
   std::vector<Launch> seq;
-  if (h->cfg.learned_guess || regroups(h)) {  // per step: guess, or regroup, in between
-    const bool guess = h->cfg.learned_guess != 0;
+  if (h->cfg.learned_guess == CLM_GUESS_NETWORK || regroups(h)) {  // per step: guess, or regroup, in between
+    const bool guess = h->cfg.learned_guess == CLM_GUESS_NETWORK;
     for (int i = 0; i < nsteps; ++i) seq.push_back({i, 1, guess});
   } else {
     const int chunk = 64;
@@ -385,7 +392,7 @@ int step_graph(clm_handle* h, double t, double dt, int nsteps) {
     CLM_CUDA(h, cudaMallocHost(&h->h_clock, sizeof(double) * (kClockSlots + 1) * clm_handle::kRing));
     for (auto& ev : h->clock_ev) CLM_CUDA(h, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   }
-  const int per_launch = (h->cfg.learned_guess || regroups(h)) ? 1 : 64;
+  const int per_launch = (h->cfg.learned_guess == CLM_GUESS_NETWORK || regroups(h)) ? 1 : 64;
   const int piece_max = per_launch * kClockSlots;
   for (int s_begin = 0; s_begin < nsteps; s_begin += piece_max) {
     const int P = std::min(piece_max, nsteps - s_begin);
@@ -559,6 +566,9 @@ int check_config(const clm_config* cfg) {
   if (cfg->model != CLM_MODEL_RICHARDS && cfg->model != CLM_MODEL_ENERGY_HYDROLOGY) return CLM_ERR_ARG;
   if (cfg->max_iters < 1 || cfg->max_iters > 1000) return CLM_ERR_ARG;
   if (cfg->precision != CLM_PREC_FP64 && cfg->precision != CLM_PREC_MIXED) return CLM_ERR_ARG;
+  if (cfg->learned_guess != CLM_GUESS_NONE && cfg->learned_guess != CLM_GUESS_NETWORK &&
+      cfg->learned_guess != CLM_GUESS_EXTRAPOLATE)
+    return CLM_ERR_ARG;
   if (cfg->learned_guess && (cfg->model != CLM_MODEL_ENERGY_HYDROLOGY || cfg->newton_mode != CLM_NEWTON_TOL))
     return CLM_ERR_ARG;  // the guess only changes where tolerance-mode Newton starts
   if (cfg->newton_mode != CLM_NEWTON_FIXED && cfg->newton_mode != CLM_NEWTON_TOL) return CLM_ERR_ARG;
@@ -1035,8 +1045,17 @@ int clm_step_async(clm_handle* h, double t, double dt, int32_t nsteps) {
   if (!(dt > 0) || !std::isfinite(dt) || !std::isfinite(t) || nsteps < 0)
     return fail(h, CLM_ERR_ARG, "need dt > 0, finite t, nsteps >= 0");
   if (nsteps == 0) return CLM_OK;
-  if (h->cfg.learned_guess && (!h->d_mlp || !h->d_guess))
+  if (h->cfg.learned_guess == CLM_GUESS_NETWORK && (!h->d_mlp || !h->d_guess))
     return fail(h, CLM_ERR_STATE, "clm_load_mlp has not been called");
+  if (h->cfg.learned_guess == CLM_GUESS_EXTRAPOLATE && !h->prev_valid) {
+    // the history starts at the current state: the first step's guessed
+    // increment is zero
+    if (!h->d_prev)
+      CLM_CUDA(h, cudaMalloc(&h->d_prev, sizeof(double) * 2 * (size_t)std::max<int64_t>(h->ncells_int, 1)));
+    CLM_CUDA(h, restart_guess_history(h));
+    h->prev_valid = true;
+    drop_graphs(h);  // captured launches hold A.prev by value
+  }
   // the step kernels OR each column's flags into d_flags: one call's flags
   // cover all of its steps, whatever its launches
   CLM_CUDA(h, cudaMemsetAsync(h->d_flags, 0, sizeof(uint32_t) * h->stride, h->stream));
@@ -1268,6 +1287,7 @@ int clm_autotune(clm_handle* h, double t, double dt, int32_t probe_steps, clm_tu
     h->sched = c.schedule;
     StepArgs A = step_args(h);
     A.guess = nullptr;  // the probe times the step kernel alone
+    A.prev = nullptr;   // and leaves the extrapolation history alone
     StepClock clk;
     clk.t0 = t;
     clk.dt = dt;
@@ -1402,6 +1422,7 @@ int clm_load_mlp(clm_handle* h, const void* weights, int64_t nbytes) {
   if (!h->d_prev)
     CLM_CUDA(h, cudaMalloc(&h->d_prev, sizeof(double) * 2 * (size_t)std::max<int64_t>(h->ncells_int, 1)));
   CLM_CUDA(h, restart_guess_history(h));
+  h->prev_valid = true;
   CLM_CUDA(h, cudaStreamSynchronize(h->stream));
   return CLM_OK;
 }

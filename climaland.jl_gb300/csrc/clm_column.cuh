@@ -179,6 +179,10 @@ struct EHBuffers {
   // learned Newton guess: predicted u_{n+1} - u_n of vartheta_l and rho_e_int
   // (p == nullptr: no guess)
   Col<const float> guess_v{nullptr, 0}, guess_e{nullptr, 0};
+  // extrapolated guess: vartheta_l and rho_e_int at the previous step's
+  // start, read for the guess u_n + (u_n - u_{n-1}) and replaced by u_n
+  // (p == nullptr: no extrapolation)
+  Col<double> prev_v{nullptr, 0}, prev_e{nullptr, 0};
 };
 
 // FP64 <-> Jacobian-type conversions: identities on the FP64 path; on the
@@ -249,11 +253,15 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
   bool finite = true;  // the last step's state, checked as it is stored
   for (int step = 0; step < nsteps; ++step) {
     const double t = t0 + step * dt;
-    // learned guess (tolerance mode only): Newton starts from u_n + predicted
-    // increment instead of U, and falls back to U when its first increment
-    // is larger than the predicted one (the guess was worse than none)
-    bool use_guess = B.guess_v.p != nullptr && A.newton_mode == CLM_NEWTON_TOL &&
-                     isfinite(B.guess_v[0]) && isfinite(B.guess_e[0]);
+    // Newton guess (tolerance mode only): Newton starts from u_n + a guessed
+    // increment instead of U -- the learned guess's (guess_v, guess_e) or the
+    // previous step's increment (prev_v, prev_e) -- and falls back to U when
+    // its first increment is more than ten times the guessed one (a grossly
+    // wrong guess; one a little worse than U still converges about as fast,
+    // while a restart costs the whole warp an iteration)
+    const bool extrap = B.prev_v.p != nullptr && tol;
+    bool use_guess = extrap || (B.guess_v.p != nullptr && tol && isfinite(B.guess_v[0]) &&
+                                isfinite(B.guess_e[0]));
     double pred2 = 0.0;
     // ---------------- stage 1: aux at Y_n, explicit tendency, U ----------
     double K0 = 0, T0 = 0, kap0 = 0, psi0 = 0;
@@ -391,7 +399,17 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       if constexpr (!mixed)
         if (B.iden.p) B.iden[k] = sat_inv(c.nu - Uti, c.theta_r);
       if (use_guess) {
-        double xv0 = Yv + (double)B.guess_v[k], xe0 = Ye + (double)B.guess_e[k];
+        double gv, ge;
+        if (extrap) {
+          gv = Yv - B.prev_v[k];
+          ge = Ye - B.prev_e[k];
+          B.prev_v[k] = Yv;
+          B.prev_e[k] = Ye;
+        } else {
+          gv = (double)B.guess_v[k];
+          ge = (double)B.guess_e[k];
+        }
+        double xv0 = Yv + gv, xe0 = Ye + ge;
         // a layer whose guess leaves the retention curve's domain
         // (vartheta_l <= theta_r) or is not finite starts from U
         if (!(xv0 > c.theta_r + kSqrtEps) || !isfinite(xv0)) xv0 = Uv;
@@ -718,7 +736,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         const double nrm = sqrt(flux2 + state2);
         // the guess test uses the state part only: the integrated-flux
         // increments do not depend on the starting point
-        if (use_guess && it == 1 && state2 > pred2) {
+        if (use_guess && it == 1 && state2 > 100.0 * pred2 && !(sqrt(state2) < A.tol)) {
           // restart from the zero guess x = U
           for (int k = 0; k < n; ++k) {
             B.xv[k] = B.gv[k];

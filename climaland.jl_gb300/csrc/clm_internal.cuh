@@ -59,6 +59,9 @@ struct StepArgs {
   uint32_t* flags;      // [stride]
   int32_t* iters;       // [stride]
   const float* guess = nullptr;  // learned Newton guess (internal layout, 2 per cell) or null
+  // extrapolated Newton guess: vartheta_l then rho_e_int at the previous
+  // step's start (internal layout, 2 x ncells_int), or null
+  double* prev = nullptr;
   int* tile_ctr = nullptr;       // dynamic tile order: [next tile, warps done], or null (static)
   // iteration-class order (tolerance mode): warp w of the launch takes the
   // slots order[32 w + lane], or null for the tiles' own slots

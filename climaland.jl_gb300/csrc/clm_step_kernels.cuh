@@ -109,6 +109,10 @@ __global__ void __launch_bounds__(128, 1)
         B.guess_v = Col<const float>{A.guess + base, kTile};
         B.guess_e = Col<const float>{A.guess + A.L.ncells_int + base, kTile};
       }
+      if (A.prev) {
+        B.prev_v = Col<double>{A.prev + base, kTile};
+        B.prev_e = Col<double>{A.prev + A.L.ncells_int + base, kTile};
+      }
       double Fw = A.Fw[s], Fe = A.Fe[s];
       uint32_t flags = 0;
       int iters = 0;

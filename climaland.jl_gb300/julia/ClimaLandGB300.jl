@@ -22,6 +22,9 @@ const CLM_PREC_FP64 = Int32(0)
 const CLM_PREC_MIXED = Int32(1)
 const CLM_NEWTON_FIXED = Int32(0)
 const CLM_NEWTON_TOL = Int32(1)
+const CLM_GUESS_NONE = Int32(0)
+const CLM_GUESS_NETWORK = Int32(1)
+const CLM_GUESS_EXTRAPOLATE = Int32(2)
 const CLM_BC_FLUX = Int32(0)
 const CLM_BC_FREE_DRAINAGE = Int32(1)
 const CLM_BC_STATE = Int32(2)

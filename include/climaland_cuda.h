@@ -64,6 +64,17 @@ enum clm_newton_mode {
                            newton_tol (CTS MaximumError on the norm)       */
 };
 
+/* Newton starting point in tolerance mode (clm_config.learned_guess).
+ * No reference counterpart: the reference starts every solve from U.
+ * NETWORK: u_n plus the column's previous step increment plus the change
+ *   the loaded network predicts (clm_load_mlp; one guess launch per step).
+ * EXTRAPOLATE: u_n plus the previous step increment, computed inside the
+ *   step kernel (no network, no extra launch); the handle keeps the state
+ *   at the previous step's start, initialised at the first step call.
+ * Both fall back to U where the first Newton increment exceeds ten times
+ * the guessed one (CLM_COL_GUESS_FALLBACK). */
+enum clm_guess { CLM_GUESS_NONE = 0, CLM_GUESS_NETWORK = 1, CLM_GUESS_EXTRAPOLATE = 2 };
+
 /* Tile order of the persistent step kernel (no reference counterpart: a
  * launch-configuration choice). Tiles of 32 columns are sorted deepest
  * first; results do not depend on the order. */
@@ -349,7 +360,8 @@ typedef struct clm_config {
   int32_t max_iters;      /* Newton iterations (fixed) or cap (tolerance)  */
   double newton_tol;      /* tolerance-mode threshold                      */
   double energy_norm_scale; /* weight of rho e_int in the tolerance norm   */
-  int32_t learned_guess;  /* 1: use the loaded MLP as the Newton guess     */
+  int32_t learned_guess;  /* enum clm_guess: where tolerance-mode Newton
+                             starts (EnergyHydrology)                      */
   int32_t bc_top_water, bc_top_heat, bc_bottom_water, bc_bottom_heat;
   /* scalar EnergyHydrologyParameters (energy_hydrology.jl:44-61) */
   double kersten_alpha, kersten_beta, ice_impedance_omega;
@@ -566,13 +578,13 @@ int clm_solve(clm_handle* h, const double* W_vv, const double* W_ev,
  * water and heat fluxes, alpha, n, nu, log10 K_sat, dt; two hidden layers
  * of 64 with GELU; outputs: 20-layer vartheta_l and rho_e_int) predicts how
  * each column's step increment changes from its previous step's. With
- * cfg->learned_guess = 1 (EnergyHydrology, tolerance mode, 20-layer
- * columns) Newton starts from u_n + (u_n - u_{n-1}) + prediction, u_{n-1}
- * the state at the previous guess; a column whose first Newton increment
- * exceeds its guessed one restarts from the plain start
- * (CLM_COL_GUESS_FALLBACK). clm_load_mlp restarts the history (the first
- * guess after it is the prediction alone); clm_set_state keeps it. Weights
- * are a blob of clm_mlp_blob_bytes() bytes written by clm_mlp_get. */
+ * cfg->learned_guess = CLM_GUESS_NETWORK (EnergyHydrology, tolerance mode,
+ * 20-layer columns) Newton starts from u_n + (u_n - u_{n-1}) + prediction,
+ * u_{n-1} the state at the previous guess; a column whose first Newton
+ * increment exceeds ten times its guessed one restarts from the plain
+ * start (CLM_COL_GUESS_FALLBACK). clm_load_mlp restarts the history (the
+ * first guess after it is the prediction alone); clm_set_state keeps it.
+ * Weights are a blob of clm_mlp_blob_bytes() bytes written by clm_mlp_get. */
 int clm_load_mlp(clm_handle* h, const void* weights, int64_t nbytes);
 
 /* Raw network inputs of every 20-layer column at time t (device array of

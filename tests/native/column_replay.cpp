@@ -24,7 +24,7 @@ namespace {
 
 template <typename JT, class CM, int kSrc, class Geom>
 void eh_one(const StepArgs& A, const Tables& Tb, int c, int n, double* v, double* ti, double* e,
-            const float* gv, const float* ge, const Geom& G, double t, double dt, int nsteps,
+            const float* gv, const float* ge, double* pv, double* pe, const Geom& G, double t, double dt, int nsteps,
             double& Fw, double& Fe, uint32_t& fl, int& it) {
   constexpr bool mixed = sizeof(JT) < sizeof(double);
   std::vector<double> xv(n), xe(n), fe(n), K(n), kap(n), irc(n), aw(n), iden(n);
@@ -57,6 +57,10 @@ void eh_one(const StepArgs& A, const Tables& Tb, int c, int n, double* v, double
     B.guess_v = Col<const float>{gv, 1};
     B.guess_e = Col<const float>{ge, 1};
   }
+  if (pv && pe) {
+    B.prev_v = Col<double>{pv, 1};
+    B.prev_e = Col<double>{pe, 1};
+  }
   eh_column<JT, CM, false, kSrc>(A, Tb, c, n, c, B, J, G, t, dt, nsteps, Fw, Fe, fl, it);
 }
 
@@ -77,29 +81,29 @@ void richards_one(const StepArgs& A, const Tables& Tb, int c, int n, double* v, 
 
 template <typename JT, class CM, class Geom>
 void column(const StepArgs& A, const Tables& Tb, int model, int src, int c, int n, double* v,
-            double* ti, double* e, const float* gv, const float* ge, const Geom& G, double t,
+            double* ti, double* e, const float* gv, const float* ge, double* pv, double* pe, const Geom& G, double t,
             double dt, int nsteps, double& Fw, double& Fe, uint32_t& fl, int& it) {
   if (model == CLM_MODEL_RICHARDS) {
     richards_one<JT, CM>(A, Tb, c, n, v, G, t, dt, nsteps, Fw, fl, it);
   } else if (src == kSrcRoots) {
-    eh_one<JT, CM, kSrcRoots>(A, Tb, c, n, v, ti, e, gv, ge, G, t, dt, nsteps, Fw, Fe, fl, it);
+    eh_one<JT, CM, kSrcRoots>(A, Tb, c, n, v, ti, e, gv, ge, pv, pe, G, t, dt, nsteps, Fw, Fe, fl, it);
   } else if (src == kSrcAtmos) {
-    eh_one<JT, CM, kSrcAtmos>(A, Tb, c, n, v, ti, e, gv, ge, G, t, dt, nsteps, Fw, Fe, fl, it);
+    eh_one<JT, CM, kSrcAtmos>(A, Tb, c, n, v, ti, e, gv, ge, pv, pe, G, t, dt, nsteps, Fw, Fe, fl, it);
   } else {
-    eh_one<JT, CM, kSrcNone>(A, Tb, c, n, v, ti, e, gv, ge, G, t, dt, nsteps, Fw, Fe, fl, it);
+    eh_one<JT, CM, kSrcNone>(A, Tb, c, n, v, ti, e, gv, ge, pv, pe, G, t, dt, nsteps, Fw, Fe, fl, it);
   }
 }
 
 template <typename JT, class CM>
 void column_geom(const StepArgs& A, const Tables& Tb, int model, int src, int c, int n, int64_t o,
-                 double* v, double* ti, double* e, const float* gv, const float* ge, double t,
+                 double* v, double* ti, double* e, const float* gv, const float* ge, double* pv, double* pe, double t,
                  double dt, int nsteps, double& Fw, double& Fe, uint32_t& fl, int& it) {
   if (A.geo.z) {
     const ColGeomS G(A.geo, o, 1, c, A.L.stride, A.z_lo[c], A.z_hi[c], n);
-    column<JT, CM>(A, Tb, model, src, c, n, v, ti, e, gv, ge, G, t, dt, nsteps, Fw, Fe, fl, it);
+    column<JT, CM>(A, Tb, model, src, c, n, v, ti, e, gv, ge, pv, pe, G, t, dt, nsteps, Fw, Fe, fl, it);
   } else {
     const ColGeom G(A.z_lo[c], A.z_hi[c], n);
-    column<JT, CM>(A, Tb, model, src, c, n, v, ti, e, gv, ge, G, t, dt, nsteps, Fw, Fe, fl, it);
+    column<JT, CM>(A, Tb, model, src, c, n, v, ti, e, gv, ge, pv, pe, G, t, dt, nsteps, Fw, Fe, fl, it);
   }
 }
 
@@ -109,14 +113,15 @@ void column_geom(const StepArgs& A, const Tables& Tb, int model, int src, int c,
 // forcing: 4 slot pointers or null; root, atmos: rows of ncol or null;
 // z_faces: n + 1 faces per column at offsets[c] + c, or null for uniform
 // layers; guess: a Newton starting increment of vartheta_l and rho_e_int
-// per cell (EnergyHydrology, tolerance mode), or null). Returns 0, or 1 on
-// an argument error.
+// per cell (EnergyHydrology, tolerance mode), or null; prev: the state at the
+// previous step's start for the extrapolated guess, per cell, updated in
+// place, or null). Returns 0, or 1 on an argument error.
 extern "C" int clmr_step(const clm_config* cfg, int ncol, const int32_t* offsets, const double* z_lo,
                          const double* z_hi, const double* z_faces, const double* params, int nparams,
                          const double* const* forcing, const double* root, const double* atmos,
                          const clm_atmos_params* ap, double* v, double* ti, double* e, double* Fw,
                          double* Fe, double t, double dt, int nsteps, uint32_t* flags, int32_t* iters,
-                         const float* guess_v, const float* guess_e) {
+                         const float* guess_v, const float* guess_e, double* prev_v, double* prev_e) {
   if (!cfg || ncol <= 0 || nparams < 1 || nparams > CLM_NPARAM_MAX) return 1;
   const bool eh = cfg->model == CLM_MODEL_ENERGY_HYDROLOGY;
   std::vector<double> prm((size_t)CLM_NPARAM_MAX * ncol, 0.0), lkap(2 * (size_t)ncol, 0.0);
@@ -195,12 +200,14 @@ extern "C" int clmr_step(const clm_config* cfg, int ncol, const int32_t* offsets
     double* ce = eh ? e + o : nullptr;
     const float* gv = guess_v ? guess_v + o : nullptr;
     const float* ge = guess_e ? guess_e + o : nullptr;
+    double* pv = prev_v ? prev_v + o : nullptr;
+    double* pe = prev_e ? prev_e + o : nullptr;
     if (mixed) {
-      if (bc) column_geom<float, BC>(A, Tb, cfg->model, src, c, n, o, cv, cti, ce, gv, ge, t, dt, nsteps, fw, fe, fl, it);
-      else column_geom<float, VG>(A, Tb, cfg->model, src, c, n, o, cv, cti, ce, gv, ge, t, dt, nsteps, fw, fe, fl, it);
+      if (bc) column_geom<float, BC>(A, Tb, cfg->model, src, c, n, o, cv, cti, ce, gv, ge, pv, pe, t, dt, nsteps, fw, fe, fl, it);
+      else column_geom<float, VG>(A, Tb, cfg->model, src, c, n, o, cv, cti, ce, gv, ge, pv, pe, t, dt, nsteps, fw, fe, fl, it);
     } else {
-      if (bc) column_geom<double, BC>(A, Tb, cfg->model, src, c, n, o, cv, cti, ce, gv, ge, t, dt, nsteps, fw, fe, fl, it);
-      else column_geom<double, VG>(A, Tb, cfg->model, src, c, n, o, cv, cti, ce, gv, ge, t, dt, nsteps, fw, fe, fl, it);
+      if (bc) column_geom<double, BC>(A, Tb, cfg->model, src, c, n, o, cv, cti, ce, gv, ge, pv, pe, t, dt, nsteps, fw, fe, fl, it);
+      else column_geom<double, VG>(A, Tb, cfg->model, src, c, n, o, cv, cti, ce, gv, ge, pv, pe, t, dt, nsteps, fw, fe, fl, it);
     }
     Fw[c] = fw;
     if (eh) Fe[c] = fe;

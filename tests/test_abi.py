@@ -76,6 +76,24 @@ def test_create_rejects_bad_config_before_touching_the_device(lib):
     assert lib.clm_last_error(None) == b"null handle"
 
 
+def test_guess_modes_match_the_header_and_are_checked(lib):
+    import re
+    text = (REPO / "include" / "climaland_cuda.h").read_text()
+    body = re.search(r"enum clm_guess \{([^}]*)\}", text).group(1)
+    vals = {k: int(v) for k, v in re.findall(r"(CLM_GUESS_\w+) = (\d+)", body)}
+    assert vals == {"CLM_GUESS_NONE": A.CLM_GUESS_NONE, "CLM_GUESS_NETWORK": A.CLM_GUESS_NETWORK,
+                    "CLM_GUESS_EXTRAPOLATE": A.CLM_GUESS_EXTRAPOLATE}
+    h = ctypes.c_void_p()
+    cfg = A.default_config()
+    cfg.ncol = 10
+    cfg.model = A.CLM_MODEL_ENERGY_HYDROLOGY
+    cfg.learned_guess = A.CLM_GUESS_EXTRAPOLATE  # with fixed Newton: nothing to start
+    assert lib.clm_create(ctypes.byref(cfg), ctypes.byref(h)) == A.CLM_ERR_ARG
+    cfg.newton_mode = A.CLM_NEWTON_TOL
+    cfg.learned_guess = 3
+    assert lib.clm_create(ctypes.byref(cfg), ctypes.byref(h)) == A.CLM_ERR_ARG
+
+
 def test_create_rejects_runoff_outside_richards(lib):
     # the precipitation/runoff top boundary is RichardsAtmosDrivenFluxBC: an
     # EnergyHydrology handle (whose atmosphere-driven boundary is

@@ -46,10 +46,12 @@ def _lib():
     return ctypes.CDLL(str(OUT))
 
 
-def replay(w, nsteps, t0=None, guess=None, **cfgkw):
+def replay(w, nsteps, t0=None, guess=None, prev=None, **cfgkw):
     """The column code on the host: (state, flags, iterations) after nsteps.
     guess: (vartheta_l, rho_e_int) per-cell float32 Newton starting
-    increments, or None."""
+    increments, or None; prev: (vartheta_l, rho_e_int) float64 arrays of the
+    state at the previous step's start for the extrapolated guess, updated
+    in place, or None."""
     L = _lib()
     cfg = A.ClmConfig.from_buffer_copy(w.cfg)
     for k, v in cfgkw.items():
@@ -86,7 +88,8 @@ def replay(w, nsteps, t0=None, guess=None, **cfgkw):
                      *[None if a is None else a.ctypes.data_as(_DP) for a in st],
                      ctypes.c_double(t), ctypes.c_double(w.dt), ctypes.c_int(nsteps),
                      fl.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
-                     it.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), *gp)
+                     it.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), *gp,
+                     *([None, None] if prev is None else [p.ctypes.data_as(_DP) for p in prev]))
     assert rc == 0
     return st, fl, it
 
@@ -234,3 +237,44 @@ def test_stretched_mixed_trajectory_within_1e8(name):
     one-step difference (the float Jacobian's slower convergence)."""
     w = STRETCHED[name]()
     _check(w, 48, 1e-8, "calibrated", nseeds=8, precision=A.CLM_PREC_MIXED)
+
+
+def test_extrapolated_guess_in_tolerance_mode():
+    """The extrapolated Newton start u_n + (u_n - u_{n-1}), its history kept
+    in the step's own arrays: one call of 48 steps gives the bits of 48
+    calls of one step and leaves the last step's starting state in the
+    history; at tolerance 1e-8 it takes fewer Newton iterations per column
+    than the plain start (2.25 against 2.55 measured) and stops within 1e-8
+    of the plain solve on 99 % of the columns (either start stops within
+    tolerance of the same root; a few chaotic columns amplify the
+    difference)."""
+    w = WL.full_scale_c4(ncol=2048, seed=3)
+    kw = dict(precision=A.CLM_PREC_MIXED, newton_mode=A.CLM_NEWTON_TOL, max_iters=20, newton_tol=1e-8,
+              energy_norm_scale=1e-9)
+    nsteps = 48
+
+    def per_step(prev):
+        st, its, start = list(w.copy_state()), [], None
+        for s in range(nsteps):
+            x = w.columns(0, w.ncol)
+            x.vartheta_l, x.theta_i, x.rho_e_int, x.intF_w, x.intF_e = [None if a is None else a.copy()
+                                                                        for a in st]
+            start = (st[0].copy(), st[2].copy())
+            r, fl, it = replay(x, 1, t0=w.t0 + s * w.dt, prev=prev, **kw)
+            st = list(r)
+            its.append(it)
+        return st, np.array(its), start
+
+    plain, ip, _ = per_step(None)
+    prev = [w.vartheta_l.copy(), w.rho_e_int.copy()]
+    ext, ie, start = per_step(prev)
+    prev_fused = [w.vartheta_l.copy(), w.rho_e_int.copy()]
+    fused, _, it_fused = replay(w, nsteps, prev=prev_fused, **kw)
+    for a, b in zip(fused, ext):
+        assert (a is None and b is None) or np.array_equal(a, b)
+    assert np.array_equal(it_fused, ie[-1])
+    for h, hf, s0 in zip(prev, prev_fused, start):
+        assert np.array_equal(h, s0) and np.array_equal(hf, s0)
+    assert ie[1:].mean() < ip[1:].mean() - 0.2, (ie[1:].mean(), ip[1:].mean())
+    d = np.maximum.reduceat(np.abs(plain[0] - ext[0]), w.offsets[:-1].astype(np.int64))
+    assert np.mean(d <= 1e-8) >= 0.99, float(np.mean(d <= 1e-8))

@@ -224,3 +224,25 @@ def test_tolerance_mode_regrouping_bitwise_equals_tile_order(torch, make):
         _same(ref, _run(w, calls, precision=prec, tol_regroup=1, **tol))
         _same(ref, _run(w, calls, precision=prec, tol_regroup=1, graph=1, **tol))
         _same(ref, _run(w, calls, precision=prec, tol_regroup=1, schedule=A.CLM_SCHED_DYNAMIC, **tol))
+
+
+@pytest.mark.parametrize("prec", [A.CLM_PREC_FP64, A.CLM_PREC_MIXED])
+def test_extrapolated_guess_bitwise_over_launch_shapes(torch, prec):
+    """CLM_GUESS_EXTRAPOLATE keeps its history in the handle: one call of 12
+    steps (one fused launch), twelve calls of one step, graph replay and
+    warp regrouping give the same bits; a state round trip through host
+    buffers between calls keeps the history."""
+    w = WL.full_scale_c4(ncol=3000, seed=5)
+    tol = dict(newton_mode=A.CLM_NEWTON_TOL, max_iters=20, newton_tol=1e-8, energy_norm_scale=1e-9,
+               learned_guess=A.CLM_GUESS_EXTRAPOLATE, precision=prec)
+    ones = [(w.t0 + i * w.dt, 1) for i in range(12)]
+    ref = _run(w, [(w.t0, 12)], tol_regroup=0, **tol)
+    for kw in (dict(tol_regroup=0), dict(tol_regroup=1), dict(tol_regroup=1, graph=1)):
+        got = _run(w, ones, **kw, **tol)
+        _same((ref[0], ref[1] | got[1], ref[2]), got)  # per-call flags: the last call's only
+    with SoilColumns(w, tol_regroup=1, **tol) as g:
+        for t, n in ones:
+            g.step(t, w.dt, n)
+            g.set_state(*g.get_state())
+        f, it = g.status()
+        _same((ref[0], ref[1] | f, ref[2]), (g.get_state(), f, it))

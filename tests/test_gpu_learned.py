@@ -130,7 +130,8 @@ def test_learned_guess_saves_newton_iterations(torch):
     predicted change (train's validation gate keeps the network only where
     its held-out error is below that of predicting no change); the previous
     increment alone (the network's output held at zero) is measured beside
-    it."""
+    it, and the step kernel's own extrapolation (CLM_GUESS_EXTRAPOLATE, the
+    same start without the network's launch)."""
     tol = dict(LG.TOL, newton_tol=1e-8)
     wtr = LG.training_workload(ncol=16384, seed=0)
     X, Y = LG.generate(wtr, 24, newton=tol)
@@ -139,8 +140,11 @@ def test_learned_guess_saves_newton_iterations(torch):
     wev = LG.eval_workload(ncol=65536, seed=1)
     nsteps = 24
     out = {}
-    for name, blob in (("plain", None), ("learned", res.blob), ("previous_increment", zero_blob)):
-        with SoilColumns(wev, learned_guess=1 if blob else None, **tol) as g:
+    runs = (("plain", None, None), ("learned", res.blob, A.CLM_GUESS_NETWORK),
+            ("previous_increment", zero_blob, A.CLM_GUESS_NETWORK),
+            ("extrapolated", None, A.CLM_GUESS_EXTRAPOLATE))
+    for name, blob, mode in runs:
+        with SoilColumns(wev, learned_guess=mode, **tol) as g:
             if blob:
                 g.load_mlp(blob)
             iters = []
@@ -155,7 +159,7 @@ def test_learned_guess_saves_newton_iterations(torch):
     stats = dict(train_rows=res.nrows, train_seconds=res.seconds, loss_first=float(res.loss[:50].mean()),
                  loss_last=float(res.loss[-50:].mean()), heldout_mse=res.val_mse,
                  heldout_mse_zero_change=res.val_mse_zero, gated=res.gated, iters_plain=ip)
-    for name in ("learned", "previous_increment"):
+    for name in ("learned", "previous_increment", "extrapolated"):
         sl, il, fl = out[name]
         colerr = np.max(np.abs(sp[0] - sl[0]).reshape(wev.ncol, 20), axis=1)
         stats[f"iters_{name}"] = il
@@ -163,5 +167,9 @@ def test_learned_guess_saves_newton_iterations(torch):
         stats[f"frac_cols_within_1e8_{name}"] = float(np.mean(colerr <= 1e-8))
         stats[f"max_err_{name}"] = float(colerr.max())
     print("LEARNED " + json.dumps(stats))
-    assert stats["iters_learned"] < ip
-    assert stats["frac_cols_within_1e8_learned"] >= 0.99
+    for name in ("learned", "extrapolated"):
+        assert stats[f"iters_{name}"] < ip, name
+        assert stats[f"frac_cols_within_1e8_{name}"] >= 0.99, name
+    # the in-kernel extrapolation is the zero-change network's guess in FP64
+    # instead of float: the same iteration counts to within a few columns
+    assert abs(stats["iters_extrapolated"] - stats["iters_previous_increment"]) < 0.02
