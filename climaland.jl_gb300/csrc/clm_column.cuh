@@ -621,6 +621,10 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       const double corr_v = mixed ? (sdv + sum_fv) / G.wsum() : 0.0;
       const double flux2 = fFw * fFw + fFe * fFe;  // integrated fluxes
       double state2 = 0.0;                           // state increments
+      // mixed path: the state increments' squares summed in float from the
+      // float increments (the tolerance test needs a few digits of the norm;
+      // the FP64 pipe is the mixed step's bound)
+      float state2f = 0.0f;
       // sweep 3 (bottom -> top): energy right-hand side, rho e forward
       // elimination (c'' into cp, d'' into dp behind the read of delta_v)
       {
@@ -692,7 +696,12 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
           d_prev = dk;
           const double dvd = dvd0;
           B.xv[k] -= dvd;
-          if (tol) state2 += dvd * dvd;
+          if (tol) {
+            if constexpr (mixed)
+              state2f = fmaf(dv0, dv0, state2f);
+            else
+              state2 += dvd * dvd;
+          }
           dvm = dv0; Dm = D0; dv0 = dvp; D0 = Dp;
           dvd0 = dvdp;
           ae_dn = ae_up;
@@ -717,11 +726,16 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
           // W_ee and W_ev + I have zero (width-weighted) column sums:
           // sum(w delta_e) = -sum(w f_e) - sum(w delta_v) = -sum(w f_e) + sum(w f_v)
           const double corr_e = (sde + sum_fe - sum_fv) / G.wsum();
+          const float cef = ff::narrow_trunc(corr_e), sef = ff::narrow_trunc(se);
           for (int k = 0; k < n; ++k) {
             const double d = from_jt<JT>(J.dp[k]) - corr_e;
             B.xe[k] -= d;
-            if (tol) state2 += (se * d) * (se * d);
+            if (tol) {
+              const float df = (J.dp[k] - cef) * sef;
+              state2f = fmaf(df, df, state2f);
+            }
           }
+          state2 = ff::widen_fast(state2f);
         } else {
           for (int k = n - 1; k >= 0; --k) {
             const JT d = J.dp[k] - J.cp[k] * nxt;
