@@ -410,6 +410,12 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
           ge = (double)B.guess_e[k];
         }
         double xv0 = Yv + gv, xe0 = Ye + ge;
+        // a zero guessed increment carries no information (the first step
+        // of a history): the layer starts from U
+        if (gv == 0.0 && ge == 0.0) {
+          xv0 = Uv;
+          xe0 = Ue;
+        }
         // a layer whose guess leaves the retention curve's domain
         // (vartheta_l <= theta_r) or is not finite starts from U
         if (!(xv0 > c.theta_r + kSqrtEps) || !isfinite(xv0)) xv0 = Uv;
@@ -510,6 +516,8 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
 
     // ---------------- stage 2: Newton ------------------------------------
     double prev_norm = 1e300;
+    // a guess that moved no layer off U is no guess: plain start, plain test
+    if (use_guess && !(pred2 > 0.0)) use_guess = false;
     for (int it = 1; it <= A.max_iters; ++it) {
       // sweep 1 (bottom -> top)
       JT cp_prev = 0, dp_prev = 0;

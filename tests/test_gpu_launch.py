@@ -237,12 +237,14 @@ def test_extrapolated_guess_bitwise_over_launch_shapes(torch, prec):
                learned_guess=A.CLM_GUESS_EXTRAPOLATE, precision=prec)
     ones = [(w.t0 + i * w.dt, 1) for i in range(12)]
     ref = _run(w, [(w.t0, 12)], tol_regroup=0, **tol)
+    # flags cover a call's steps: the last one-step call's are a subset of
+    # the twelve-step call's
     for kw in (dict(tol_regroup=0), dict(tol_regroup=1), dict(tol_regroup=1, graph=1)):
         got = _run(w, ones, **kw, **tol)
-        _same((ref[0], ref[1] | got[1], ref[2]), got)  # per-call flags: the last call's only
+        _same(ref, (got[0], got[1] | ref[1], got[2]))
     with SoilColumns(w, tol_regroup=1, **tol) as g:
         for t, n in ones:
             g.step(t, w.dt, n)
             g.set_state(*g.get_state())
         f, it = g.status()
-        _same((ref[0], ref[1] | f, ref[2]), (g.get_state(), f, it))
+        _same(ref, (g.get_state(), f | ref[1], it))
