@@ -164,7 +164,10 @@ CLM_HD void eh_point(const Tables& Tb, const Earth& E, const EHCol<CM>& c, const
 }
 
 struct EHBuffers {
-  Col<double> gv, gti, ge;          // state (holds U during a step)
+  Col<double> gv, gti, ge;          // U during a step (and the state, unless sv is set)
+  // the state arrays when U is kept apart from them (p == nullptr: U
+  // overwrites the state in gv, gti, ge)
+  Col<double> sv{nullptr, 0}, sti{nullptr, 0}, se{nullptr, 0};
   Col<double> xv, xe, fe;           // iterate, energy residual
   Col<double> K, kap, irc;          // frozen aux: K, face kappa / dz (after stage 1), 1 / rho c
   // mixed path: the Jacobian's face products dt K_face / dz^2, dt kappa_face /
@@ -250,6 +253,11 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
   constexpr bool kRoots = kSrc == kSrcRoots;
   constexpr bool kAtmos = kSrc == kSrcAtmos;
 
+  // Y_n is read from, and Y_{n+1} written to, the state arrays (Sv, Sti,
+  // Se); U lives in gv, gti, ge: the same arrays, or the warp's scratch
+  // when the caller keeps them apart (staged)
+  const bool staged = B.sv.p != nullptr;
+  const Col<double> Sv = staged ? B.sv : B.gv, Sti = staged ? B.sti : B.gti, Se = staged ? B.se : B.ge;
   bool finite = true;  // the last step's state, checked as it is stored
   for (int step = 0; step < nsteps; ++step) {
     const double t = t0 + step * dt;
@@ -281,13 +289,13 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
     EHRunoff ro{0.0, 0.0, 0.0, 0.0, 0.0};
     if constexpr (kAtmos) {
       auto theta_l_of = [&](int k) {
-        const double Yv = B.gv[k], nu_eff = c.nu - B.gti[k];
+        const double Yv = Sv[k], nu_eff = c.nu - Sti[k];
         const double v_safe = fmax(Yv, c.theta_r + kSqrtEps);
         const double nu_safe = fmax(nu_eff, c.theta_r + kSqrtEps);
         return (v_safe < nu_safe) ? v_safe : nu_safe;
       };
       const int k1 = n - 1;
-      const double Yv = B.gv[k1], Yti = B.gti[k1], Ye = B.ge[k1];
+      const double Yv = Sv[k1], Yti = Sti[k1], Ye = Se[k1];
       AtmosSfc sf;
       sf.th1 = theta_l_of(k1);
       sf.th2 = theta_l_of(k1 - 1);
@@ -308,9 +316,9 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       ro = eh_runoff(Tb, E, sc, A.runoff, G, c.nu, c.theta_r, c.K_sat, P[CLM_P_F_MAX * st + s],
                      P[CLM_P_F_OVER * st + s], P[CLM_P_R_SB * st + s], sf.th1, D(CLM_AT_P_LIQ),
                      [&](int k, double& v, double& ti, double& T) {
-                       v = B.gv[k];
-                       ti = B.gti[k];
-                       T = E.T_0 + (B.ge[k] + ti * E.rho_i_LH_f0) *
+                       v = Sv[k];
+                       ti = Sti[k];
+                       T = E.T_0 + (Se[k] + ti * E.rho_i_LH_f0) *
                                        fm::rcp(heat_capacity(E, theta_l_of(k), ti, c.rcds));
                      });
       sf.infil = ro.infil;
@@ -321,7 +329,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       sub_top = -ab.vice * E.rho_l / E.rho_i / (2.0 * dz_top);
     }
     for (int k = 0; k < n; ++k) {
-      const double Yv = B.gv[k], Yti = B.gti[k], Ye = B.ge[k];
+      const double Yv = Sv[k], Yti = Sti[k], Ye = Se[k];
       const double nu_eff = c.nu - Yti;
       // volumetric_liquid_fraction (soil_hydrology_parameterizations.jl:22-31)
       const double v_safe = fmax(Yv, c.theta_r + kSqrtEps);
@@ -387,6 +395,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       }
       B.gv[k] = Uv;
       B.gti[k] = Uti;
+      if (staged && !kRoots) B.ge[k] = Ue;
       if constexpr (kAtmos) {
         // TOPMODEL's implicit subsurface sink, constant through the Newton
         // solve: part of the residual's U + dt T_imp, not of the start x = U
@@ -518,6 +527,8 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
     double prev_norm = 1e300;
     // a guess that moved no layer off U is no guess: plain start, plain test
     if (use_guess && !(pred2 > 0.0)) use_guess = false;
+    double prev_state2 = 0.0;  // the state increments' norm of the last iteration (guess test)
+    int it_start = 0;          // iterations spent before a restart from U
     for (int it = 1; it <= A.max_iters; ++it) {
       // sweep 1 (bottom -> top)
       JT cp_prev = 0, dp_prev = 0;
@@ -756,10 +767,15 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       iters_done = it;
       if (tol) {
         const double nrm = sqrt(flux2 + state2);
-        // the guess test uses the state part only: the integrated-flux
-        // increments do not depend on the starting point
-        if (use_guess && it == 1 && state2 > 100.0 * pred2 && !(sqrt(state2) < A.tol)) {
-          // restart from the zero guess x = U
+        // the guess is abandoned (restart from x = U) when its first
+        // increment is more than ten times the guessed one, or when Newton
+        // from it stops contracting or leaves the finite numbers; the tests
+        // use the state part only (the integrated-flux increments do not
+        // depend on the starting point)
+        const bool drop_guess =
+            use_guess && (it == 1 ? state2 > 100.0 * pred2 && !(sqrt(state2) < A.tol)
+                                  : !(state2 < prev_state2));
+        if (drop_guess) {
           for (int k = 0; k < n; ++k) {
             B.xv[k] = B.gv[k];
             B.xe[k] = B.ge[k];
@@ -767,9 +783,11 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
           use_guess = false;
           flags |= CLM_COL_GUESS_FALLBACK;
           prev_norm = 1e300;
+          it_start = it;
           continue;
         }
-        if (nrm > prev_norm && it > 2) flags |= CLM_COL_DIVERGED;
+        prev_state2 = state2;
+        if (nrm > prev_norm && it - it_start > 2) flags |= CLM_COL_DIVERGED;
         prev_norm = nrm;
         // with a guess, the integrated fluxes start from their value at the
         // guessed state (U_F + dt T_F(x0)): their first increment is that
@@ -787,12 +805,14 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       const double v = Uv + dt * ((B.xv[k] - Uv) * inv_dt);
       const double e = Ue + dt * ((B.xe[k] - Ue) * inv_dt);
       if (last) {
-        B.gv.store_last(k, v);
-        B.ge.store_last(k, e);
+        Sv.store_last(k, v);
+        Se.store_last(k, e);
+        if (staged) Sti.store_last(k, B.gti[k]);
         finite = finite && isfinite(v) && isfinite(B.gti[k]) && isfinite(e);
       } else {
-        B.gv[k] = v;
-        B.ge[k] = e;
+        Sv[k] = v;
+        Se[k] = e;
+        if (staged) Sti[k] = B.gti[k];
       }
     }
     Fw = UFw + dt * ((xFw - UFw) * inv_dt);
