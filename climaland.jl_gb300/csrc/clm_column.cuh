@@ -164,10 +164,7 @@ CLM_HD void eh_point(const Tables& Tb, const Earth& E, const EHCol<CM>& c, const
 }
 
 struct EHBuffers {
-  Col<double> gv, gti, ge;          // U during a step (and the state, unless sv is set)
-  // the state arrays when U is kept apart from them (p == nullptr: U
-  // overwrites the state in gv, gti, ge)
-  Col<double> sv{nullptr, 0}, sti{nullptr, 0}, se{nullptr, 0};
+  Col<double> gv, gti, ge;          // state (holds U during a step)
   Col<double> xv, xe, fe;           // iterate, energy residual
   Col<double> K, kap, irc;          // frozen aux: K, face kappa / dz (after stage 1), 1 / rho c
   // mixed path: the Jacobian's face products dt K_face / dz^2, dt kappa_face /
@@ -253,11 +250,6 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
   constexpr bool kRoots = kSrc == kSrcRoots;
   constexpr bool kAtmos = kSrc == kSrcAtmos;
 
-  // Y_n is read from, and Y_{n+1} written to, the state arrays (Sv, Sti,
-  // Se); U lives in gv, gti, ge: the same arrays, or the warp's scratch
-  // when the caller keeps them apart (staged)
-  const bool staged = B.sv.p != nullptr;
-  const Col<double> Sv = staged ? B.sv : B.gv, Sti = staged ? B.sti : B.gti, Se = staged ? B.se : B.ge;
   bool finite = true;  // the last step's state, checked as it is stored
   for (int step = 0; step < nsteps; ++step) {
     const double t = t0 + step * dt;
@@ -289,13 +281,13 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
     EHRunoff ro{0.0, 0.0, 0.0, 0.0, 0.0};
     if constexpr (kAtmos) {
       auto theta_l_of = [&](int k) {
-        const double Yv = Sv[k], nu_eff = c.nu - Sti[k];
+        const double Yv = B.gv[k], nu_eff = c.nu - B.gti[k];
         const double v_safe = fmax(Yv, c.theta_r + kSqrtEps);
         const double nu_safe = fmax(nu_eff, c.theta_r + kSqrtEps);
         return (v_safe < nu_safe) ? v_safe : nu_safe;
       };
       const int k1 = n - 1;
-      const double Yv = Sv[k1], Yti = Sti[k1], Ye = Se[k1];
+      const double Yv = B.gv[k1], Yti = B.gti[k1], Ye = B.ge[k1];
       AtmosSfc sf;
       sf.th1 = theta_l_of(k1);
       sf.th2 = theta_l_of(k1 - 1);
@@ -316,9 +308,9 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       ro = eh_runoff(Tb, E, sc, A.runoff, G, c.nu, c.theta_r, c.K_sat, P[CLM_P_F_MAX * st + s],
                      P[CLM_P_F_OVER * st + s], P[CLM_P_R_SB * st + s], sf.th1, D(CLM_AT_P_LIQ),
                      [&](int k, double& v, double& ti, double& T) {
-                       v = Sv[k];
-                       ti = Sti[k];
-                       T = E.T_0 + (Se[k] + ti * E.rho_i_LH_f0) *
+                       v = B.gv[k];
+                       ti = B.gti[k];
+                       T = E.T_0 + (B.ge[k] + ti * E.rho_i_LH_f0) *
                                        fm::rcp(heat_capacity(E, theta_l_of(k), ti, c.rcds));
                      });
       sf.infil = ro.infil;
@@ -329,7 +321,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       sub_top = -ab.vice * E.rho_l / E.rho_i / (2.0 * dz_top);
     }
     for (int k = 0; k < n; ++k) {
-      const double Yv = Sv[k], Yti = Sti[k], Ye = Se[k];
+      const double Yv = B.gv[k], Yti = B.gti[k], Ye = B.ge[k];
       const double nu_eff = c.nu - Yti;
       // volumetric_liquid_fraction (soil_hydrology_parameterizations.jl:22-31)
       const double v_safe = fmax(Yv, c.theta_r + kSqrtEps);
@@ -395,7 +387,6 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       }
       B.gv[k] = Uv;
       B.gti[k] = Uti;
-      if (staged && !kRoots) B.ge[k] = Ue;
       if constexpr (kAtmos) {
         // TOPMODEL's implicit subsurface sink, constant through the Newton
         // solve: part of the residual's U + dt T_imp, not of the start x = U
@@ -773,7 +764,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         // use the state part only (the integrated-flux increments do not
         // depend on the starting point)
         const bool drop_guess =
-            use_guess && (it == 1 ? state2 > 100.0 * pred2 && !(sqrt(state2) < A.tol)
+            use_guess && (it == 1 ? !(state2 <= 100.0 * pred2) && !(sqrt(state2) < A.tol)
                                   : !(state2 < prev_state2));
         if (drop_guess) {
           for (int k = 0; k < n; ++k) {
@@ -805,14 +796,12 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       const double v = Uv + dt * ((B.xv[k] - Uv) * inv_dt);
       const double e = Ue + dt * ((B.xe[k] - Ue) * inv_dt);
       if (last) {
-        Sv.store_last(k, v);
-        Se.store_last(k, e);
-        if (staged) Sti.store_last(k, B.gti[k]);
+        B.gv.store_last(k, v);
+        B.ge.store_last(k, e);
         finite = finite && isfinite(v) && isfinite(B.gti[k]) && isfinite(e);
       } else {
-        Sv[k] = v;
-        Se[k] = e;
-        if (staged) Sti[k] = B.gti[k];
+        B.gv[k] = v;
+        B.ge[k] = e;
       }
     }
     Fw = UFw + dt * ((xFw - UFw) * inv_dt);

@@ -44,12 +44,8 @@ __host__ __device__ constexpr size_t richards_smem_per_layer() {
 // coefficient, the layer's saturation reciprocal. Mixed: K, face kappa / dz,
 // then the floats 1 / rho c, dt K_face / dz^2, dt kappa_face / dz^2 and the
 // energy-advection face coefficient packed into two slots, face K / dz, the
-// energy residual. Both: then U (vartheta_l, theta_i, rho_e_int) of a
-// regrouped launch, whose lanes' columns lie in 32 different tiles: the
-// Newton sweeps read U every iteration, coalesced from here instead of one
-// 8-byte word per 32-byte sector of the state arrays.
-__host__ __device__ constexpr int eh_scratch_slots(bool mixed) { return mixed ? 9 : 10; }
-__host__ __device__ constexpr int eh_scratch_u_slot(bool mixed) { return mixed ? 6 : 7; }
+// energy residual.
+__host__ __device__ constexpr int eh_scratch_slots(bool mixed) { return mixed ? 6 : 7; }
 
 // kSrc: the RootExtraction source (A.rx) or the atmosphere-driven top
 // boundary (A.atm) compiled in; separate kernels so that their registers do
@@ -109,15 +105,6 @@ __global__ void __launch_bounds__(128, 1)
       B.gv = Col<double>{A.v + base, kTile};
       B.gti = Col<double>{A.ti + base, kTile};
       B.ge = Col<double>{A.e + base, kTile};
-      if (A.order) {  // U in the warp's scratch, the state arrays read and written once
-        B.sv = B.gv;
-        B.sti = B.gti;
-        B.se = B.ge;
-        double* su = sw + eh_scratch_u_slot(kMixed) * lay + lane;
-        B.gv = Col<double>{su, kTile};
-        B.gti = Col<double>{su + lay, kTile};
-        B.ge = Col<double>{su + 2 * lay, kTile};
-      }
       if (A.guess) {
         B.guess_v = Col<const float>{A.guess + base, kTile};
         B.guess_e = Col<const float>{A.guess + A.L.ncells_int + base, kTile};
