@@ -421,6 +421,40 @@ def forms_block(args, torch, stream):
     wa = WL.with_atmos(w4)
     a64 = run(wa)
     amx = run(wa, precision=A.CLM_PREC_MIXED)
+    # the full-scale workload itself: device time per step of each Newton form
+    # (one step per call, as the headline line; 3 warm-up and 8 timed steps)
+    wf = WL.full_scale_c4(ncol=1048576, seed=0)
+
+    def timed(**kw):
+        with D.SoilColumns(wf, **kw) as g:
+            g.set_stream(stream.cuda_stream)
+            g.autotune(wf.t0, wf.dt, probe_steps=2)
+            t = wf.t0
+            for _ in range(3):
+                g.step_async(t, wf.dt, 1)
+                t += wf.dt
+            stream.synchronize()
+            e0.record(stream)
+            for _ in range(8):
+                g.step_async(t, wf.dt, 1)
+                t += wf.dt
+            e1.record(stream)
+            stream.synchronize()
+            ms = e0.elapsed_time(e1) / 8
+            f, it = g.status()
+            return {"ms_per_step": ms, "value": wf.ncol / ms * 1e3, "unit": "column-steps/s",
+                    "newton_iters_mean_last_step": float(it.mean()), "launch_config": g.launch_config()}
+
+    mxk = dict(precision=A.CLM_PREC_MIXED)
+    out["full_scale_1048576"] = {
+        "workload": wf.name, "steps": 8,
+        "mixed": timed(**mxk),
+        "plain_fp64_tol1e-8": timed(**tol),
+        "mixed_tol1e-8": timed(**mxk, **tol),
+        "extrapolated_mixed_tol1e-8": timed(learned_guess=A.CLM_GUESS_EXTRAPOLATE, **mxk, **tol),
+        "extrapolated_mixed_tol1e-8_tile_order": timed(learned_guess=A.CLM_GUESS_EXTRAPOLATE, tol_regroup=0,
+                                                         **mxk, **tol)}
+    del wf
     out["atmos_boundary"] = {"workload": wa.name, "plain_fp64": pub(a64, None, wa),
                              "mixed": pub(amx, a64, wa),
                              "cost_vs_flux_boundary_fp64": a64["ms_per_step"] / plain["ms_per_step"],
@@ -711,6 +745,10 @@ def main():
     forms = None
     if not args.no_forms and world == 1:
         forms = forms_block(args, torch, stream)
+        if w.ncol == 1048576 and w.cfg.model == 1:  # the same columns as this line's
+            for r in forms["full_scale_1048576"].values():
+                if isinstance(r, dict) and "value" in r:
+                    r["speedup_vs_this_line"] = r["value"] / value
     line = {
         "metric": "column-steps/s", "value": value, "unit": "column-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,

@@ -476,11 +476,13 @@ int ready(clm_handle* h) {
   return CLM_OK;
 }
 
-// The learned guess's history restarts at the current state (clm_load_mlp):
-// the first guess after it has no previous increment. clm_set_state keeps
-// the history, so a caller that round-trips its state every step keeps it;
-// a state unrelated to the previous one gives one poor first guess, which
-// the step's fallback replaces by the plain start.
+// The guesses' history (the state at the previous step's start) restarts
+// at the current state: at clm_load_mlp for the network guess, at the first
+// step call for the extrapolated one; the first guess after it has no
+// previous increment. clm_set_state keeps the history, so a caller that
+// round-trips its state every step keeps it; a state unrelated to the
+// previous one gives one poor first guess, which the step's restart rule
+// replaces by the plain start where it is grossly off.
 cudaError_t restart_guess_history(clm_handle* h) {
   if (!h->d_prev || !h->d_v || !h->d_e) return cudaSuccess;
   const size_t nb = sizeof(double) * (size_t)h->ncells_int;

@@ -71,8 +71,9 @@ enum clm_newton_mode {
  * EXTRAPOLATE: u_n plus the previous step increment, computed inside the
  *   step kernel (no network, no extra launch); the handle keeps the state
  *   at the previous step's start, initialised at the first step call.
- * Both fall back to U where the first Newton increment exceeds ten times
- * the guessed one (CLM_COL_GUESS_FALLBACK). */
+ * Both restart from U where the first Newton increment exceeds ten times
+ * the guessed one, or where Newton from the guess stops contracting
+ * (CLM_COL_GUESS_FALLBACK). */
 enum clm_guess { CLM_GUESS_NONE = 0, CLM_GUESS_NETWORK = 1, CLM_GUESS_EXTRAPOLATE = 2 };
 
 /* Tile order of the persistent step kernel (no reference counterpart: a
@@ -581,8 +582,9 @@ int clm_solve(clm_handle* h, const double* W_vv, const double* W_ev,
  * cfg->learned_guess = CLM_GUESS_NETWORK (EnergyHydrology, tolerance mode,
  * 20-layer columns) Newton starts from u_n + (u_n - u_{n-1}) + prediction,
  * u_{n-1} the state at the previous guess; a column whose first Newton
- * increment exceeds ten times its guessed one restarts from the plain
- * start (CLM_COL_GUESS_FALLBACK). clm_load_mlp restarts the history (the
+ * increment exceeds ten times its guessed one, or whose iteration from it
+ * stops contracting, restarts from the plain start
+ * (CLM_COL_GUESS_FALLBACK). clm_load_mlp restarts the history (the
  * first guess after it is the prediction alone); clm_set_state keeps it.
  * Weights are a blob of clm_mlp_blob_bytes() bytes written by clm_mlp_get. */
 int clm_load_mlp(clm_handle* h, const void* weights, int64_t nbytes);
