@@ -479,6 +479,9 @@ def full_run(args, torch):
     from climaland_gb300 import workloads as WL
 
     w = WL.full_scale_c4(ncol=args.ncol or 1048576, seed=0)
+    atmos = args.top == "atmos"
+    if atmos:  # the atmosphere-driven top boundary on the same columns: FP64 and mixed
+        w = WL.with_atmos(w)
     nst = w.nsteps
     chunk = 64
     stream = torch.cuda.Stream()
@@ -486,21 +489,26 @@ def full_run(args, torch):
     e1 = torch.cuda.Event(enable_timing=True)
     tol = dict(newton_mode=A.CLM_NEWTON_TOL, max_iters=20, newton_tol=1e-8, energy_norm_scale=1e-9)
     t0 = time.perf_counter()
-    wtr = WL.full_scale_c4(ncol=65536, seed=7)
-    X, Y = LG.generate(wtr, 32, newton=tol)
-    res = LG.train(X, Y, steps=20000, batch=4096, lr=2e-3, gate=False)  # the network as trained
-    del X, Y
+    res = None
+    if not atmos:
+        wtr = WL.full_scale_c4(ncol=65536, seed=7)
+        X, Y = LG.generate(wtr, 32, newton=tol)
+        res = LG.train(X, Y, steps=20000, batch=4096, lr=2e-3, gate=False)  # the network as trained
+        del X, Y
     train_s = time.perf_counter() - t0
     mx = dict(precision=A.CLM_PREC_MIXED)
     forms = [("plain_fp64", {}, None), ("plain_fp64_tol1e-8", dict(tol), None), ("mixed", mx, None),
              ("mixed_tol1e-8", dict(mx, **tol), None),
-             ("learned_mixed_tol1e-8_graph", dict(mx, learned_guess=1, graph=1, **tol), res.blob),
+             ("learned_mixed_tol1e-8_graph", dict(mx, learned_guess=1, graph=1, **tol), res and res.blob),
              ("extrapolated_mixed_tol1e-8_graph",
-              dict(mx, learned_guess=A.CLM_GUESS_EXTRAPOLATE, graph=1, **tol), None)]
+              dict(mx, learned_guess=A.CLM_GUESS_EXTRAPOLATE, graph=1, **tol), None)] if not atmos else \
+        [("plain_fp64", {}, None), ("mixed", mx, None)]
     out = {"workload": w.name, "columns": w.ncol, "steps": nst, "simulated_days": nst * w.dt / 86400.0,
-           "learned_training_s": train_s, "learned_heldout_mse": res.val_mse,
-           "learned_heldout_mse_zero_change": res.val_mse_zero,
-           "learned_validation_gate_would_replace_it": bool(not res.val_mse < res.val_mse_zero),
+           "top_boundary": "atmosphere-driven" if atmos else "flux",
+           "learned_training_s": train_s,
+           "learned_heldout_mse": res.val_mse if res else None,
+           "learned_heldout_mse_zero_change": res.val_mse_zero if res else None,
+           "learned_validation_gate_would_replace_it": bool(not res.val_mse < res.val_mse_zero) if res else None,
            "timing": f"device, calls of {chunk} steps"}
     for name, kw, blob in forms:
         with D.SoilColumns(w, **kw) as g:
