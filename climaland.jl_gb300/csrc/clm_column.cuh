@@ -138,7 +138,7 @@ CLM_HD void eh_iterate_point_mixed(const Tables& Tb, const EHCol<CM>& c, const E
   const F2 v = ff::from_double(xv);
   const F2 nu_eff = ff::sub(M.cf.nu, ti_f);
   q = temperature_rel_ff(M.Ef, ff::from_double(xe), ti_f, ff_min(nu_eff, v), M.rcds);
-  if (!psi_dpsi_ff(M.FT, M.cf, nu_eff, v, psi, D)) {
+  if (!psi_dpsi_ff(M.FT, M.cf, nu_eff, v, c.inv_S_s, psi, D)) {
     double d;
     psi_dpsi<true>(Tb, c.g, c.nu - ti, xv, c.theta_r, c.S_s, psi, d);
     D = (float)d;

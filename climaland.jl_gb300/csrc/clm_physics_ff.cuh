@@ -50,19 +50,28 @@ CLM_HD ColFF make_col_ff(double nu, double theta_r, const VG& g) {
   return c;
 }
 
-// pressure_head (S < 1) and dpsidvartheta (soil_hydrology_parameterizations.jl
-// :109-152) at vartheta = v with nu_eff = nu - theta_i:
+// pressure_head and dpsidvartheta (soil_hydrology_parameterizations.jl
+// :109-152) at vartheta = v with nu_eff = nu - theta_i: for S < 1
 //   psi = -(S^(-1/m) - 1)^(1/n) / alpha, dpsi = w^(1/n) u / (alpha m n w S (nu_safe - theta_r))
-// with u = S^(-1/m), w = u - 1 (dpsi from the logs of its factors, in float).
-CLM_HD bool psi_dpsi_ff(const ff::Tables& T, const ColFF& c, F2 nu_eff, F2 v, double& psi,
-                        float& dpsi) {
+// with u = S^(-1/m), w = u - 1 (dpsi from the logs of its factors, in float);
+// for S > 1 (saturated) psi = (v_safe - nu_safe) / S_s, dpsi = 1 / S_s.
+// S = 1 exactly, and S within a float rounding below 1, take the FP64 closure.
+CLM_HD bool psi_dpsi_ff(const ff::Tables& T, const ColFF& c, F2 nu_eff, F2 v, double inv_S_s,
+                        double& psi, float& dpsi) {
   using namespace ff;
   const F2 guard = add_f(c.theta_r, 1.4901161193847656e-08f);  // theta_r + sqrt(eps)
   const F2 vs = ff_max(v, guard);
   const F2 ns = ff_max(nu_eff, guard);
   const F2 den = sub(ns, c.theta_r);
   const F2 S = div(sub(vs, c.theta_r), den);
-  if (!(S.hi < 1.0f) || !(S.hi > 1e-30f)) return false;
+  if (!(S.hi < 1.0f)) {
+    const F2 d = sub(vs, ns);  // its sign is that of S - 1
+    if (!(d.hi > 0.0f)) return false;
+    psi = to_double(mul(d, from_double(inv_S_s)));
+    dpsi = narrow_trunc(inv_S_s);
+    return true;
+  }
+  if (!(S.hi > 1e-30f)) return false;
   const F2 L = log(T, S);
   const F2 a = mul(L, c.neg_inv_m);  // log u
   if (!(a.hi <= kExpMax)) return false;
@@ -102,17 +111,26 @@ struct ColFFOf<VG> { using type = ColFF; };
 template <>
 struct ColFFOf<BC> { using type = ColFFBC; };
 
-// Brooks-Corey pressure_head (S < 1) and dpsidvartheta (:219-230, :268-287):
-//   psi = psi_b u, dpsi = -psi_b u / (c S (nu_safe - theta_r)), u = S^(-1/c).
-CLM_HD bool psi_dpsi_ff(const ff::Tables& T, const ColFFBC& c, F2 nu_eff, F2 v, double& psi,
-                        float& dpsi) {
+// Brooks-Corey pressure_head and dpsidvartheta (:219-230, :268-287): for S < 1
+//   psi = psi_b u, dpsi = -psi_b u / (c S (nu_safe - theta_r)), u = S^(-1/c);
+// for S > 1 psi = (v_safe - nu_safe) / S_s + psi_b, dpsi = 1 / S_s (S = 1, and
+// S within a float rounding below 1, take the FP64 closure).
+CLM_HD bool psi_dpsi_ff(const ff::Tables& T, const ColFFBC& c, F2 nu_eff, F2 v, double inv_S_s,
+                        double& psi, float& dpsi) {
   using namespace ff;
   const F2 guard = add_f(c.theta_r, 1.4901161193847656e-08f);  // theta_r + sqrt(eps)
   const F2 vs = ff_max(v, guard);
   const F2 ns = ff_max(nu_eff, guard);
   const F2 den = sub(ns, c.theta_r);
   const F2 S = div(sub(vs, c.theta_r), den);
-  if (!(S.hi < 1.0f) || !(S.hi > 1e-30f)) return false;
+  if (!(S.hi < 1.0f)) {
+    const F2 d = sub(vs, ns);  // its sign is that of S - 1
+    if (!(d.hi > 0.0f)) return false;
+    psi = to_double(add(mul(d, from_double(inv_S_s)), c.psib));
+    dpsi = narrow_trunc(inv_S_s);
+    return true;
+  }
+  if (!(S.hi > 1e-30f)) return false;
   const F2 L = log(T, S);
   const F2 a = mul(L, c.neg_inv_c);  // log u
   if (!(a.hi <= kExpMax)) return false;
