@@ -31,3 +31,26 @@ def results(tmp_path_factory):
 ])
 def test_double_float_accuracy(results, name, bound):
     assert results[name] <= bound, (name, results[name], bound)
+
+
+@pytest.fixture(scope="module")
+def closure_results(tmp_path_factory):
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    exe = tmp_path_factory.mktemp("ffc") / "ff_closure_check"
+    subprocess.run([gxx, "-O2", "-std=c++17", "-ffp-contract=off", f"-I{CSRC}", f"-I{REPO / 'include'}",
+                    str(REPO / "tests" / "native" / "ff_closure_check.cpp"), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    return {ln.split()[0]: [float(x) for x in ln.split()[1:]] for ln in out.splitlines()}
+
+
+@pytest.mark.parametrize("name", ["vg_unsaturated", "vg_saturated", "bc_unsaturated", "bc_saturated"])
+def test_double_float_pressure_head_matches_fp64(closure_results, name):
+    """psi_dpsi_ff against the FP64 closure at the same (pair-held) inputs:
+    psi to 1e-11 of max(|psi|, 1 m), dpsi (float) to 1e-5 relative; the
+    saturated branch (S > 1) stays in double-float (no point handed back to
+    the FP64 closure)."""
+    e_psi, e_d, n_ff, n_back = closure_results[name]
+    assert e_psi <= 1e-11 and e_d <= 1e-5, (name, e_psi, e_d)
+    assert n_ff > 10000 and n_back == 0, (name, n_ff, n_back)
