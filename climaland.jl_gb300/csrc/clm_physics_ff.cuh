@@ -74,11 +74,17 @@ CLM_HD bool psi_dpsi_ff(const ff::Tables& T, const ColFF& c, F2 nu_eff, F2 v, do
   if (!(S.hi > 1e-30f)) return false;
   const F2 L = log(T, S);
   const F2 a = mul(L, c.neg_inv_m);  // log u
-  if (!(a.hi <= kExpMax)) return false;
-  const F2 u = exp(T, a);
-  const F2 w = add_f(u, -1.0f);
-  if (!(w.hi > 1e-30f)) return false;
-  const F2 lw = log(T, w);
+  F2 lw;                             // log w
+  if (a.hi <= kExpMax) {
+    const F2 u = exp(T, a);
+    const F2 w = add_f(u, -1.0f);
+    if (!(w.hi > 1e-30f)) return false;
+    lw = log(T, w);
+  } else {
+    // very dry (u = S^(-1/m) > e^80): log(u - 1) = log u + log(1 - 1/u), and
+    // 1/u < 2e-35 is far below the pair's precision
+    lw = a;
+  }
   const F2 b = mul(lw, c.inv_n);  // log w^(1/n)
   if (!(b.hi >= kExpMin && b.hi <= kExpMax)) return false;
   psi = -to_double(mul(exp(T, b), c.inv_alpha));

@@ -32,8 +32,10 @@ void check(const char* name, const Tables& Tb, std::mt19937_64& rng, CM (*make)(
     const double S_s = std::pow(10.0, -4.0 + 2.0 * U(rng));
     const double ti = U(rng) < 0.3 ? 0.1 * U(rng) : 0.0;
     const double nu_eff = nu - ti;
-    // vartheta from just above theta_r to 20 % above nu_eff
-    const double v = theta_r + 1e-6 + (1.2 * nu_eff - theta_r) * U(rng);
+    // vartheta from just above theta_r to 20 % above nu_eff; one point in
+    // five very dry (theta_r + 1e-12 .. 1e-4: S^(-1/m) beyond e^80 for small m)
+    const double v = U(rng) < 0.2 ? theta_r + std::pow(10.0, -12.0 + 8.0 * U(rng))
+                                  : theta_r + 1e-6 + (1.2 * nu_eff - theta_r) * U(rng);
     const int sat = v > nu_eff ? 1 : 0;
     // the FP64 closure at the inputs as the double-float pairs hold them
     // (about 48 significant bits): the comparison measures the closure's
@@ -52,7 +54,9 @@ void check(const char* name, const Tables& Tb, std::mt19937_64& rng, CM (*make)(
     // relative to max(|psi|, 1 m): near saturation psi is small and its
     // relative error is the cancellation in S^(-1/m) - 1, in FP64 as well
     e_psi[sat] = std::fmax(e_psi[sat], std::fabs(psi_f - psi) / std::fmax(std::fabs(psi), 1.0));
-    e_d[sat] = std::fmax(e_d[sat], std::fabs((double)d_f - d) / std::fabs(d));
+    // dpsi in float: compared where the FP64 value is inside the float range
+    // (beyond it, the FP64 closure's value rounds to infinity as well)
+    if (std::fabs(d) < 1e38) e_d[sat] = std::fmax(e_d[sat], std::fabs((double)d_f - d) / std::fabs(d));
   }
   for (int b = 0; b < 2; ++b)
     std::printf("%s_%s %.3e %.3e %d %d\n", name, b ? "saturated" : "unsaturated", e_psi[b], e_d[b], n_ff[b],
