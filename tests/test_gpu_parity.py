@@ -69,6 +69,20 @@ def test_full_scale_c4_tolerance_mode():
     report("full_scale_c4_tol", check_parity(w, 96, oracle_cfg=TOL_MODE, **TOL_MODE))
 
 
+@pytest.mark.parametrize("prec", [A.CLM_PREC_FP64, A.CLM_PREC_MIXED])
+def test_extrapolated_start_reaches_the_oracle_root(prec):
+    """Tolerance mode at 1e-12 from the extrapolated start u_n + (u_n -
+    u_{n-1}) against the oracle solving from U: a start changes the path to
+    the root, not the root, so the FP64 path meets the FP64 criterion and the
+    mixed path the mixed one."""
+    w = WL.full_scale_c4(ncol=1024, seed=4)
+    kw = dict(TOL_MODE, learned_guess=A.CLM_GUESS_EXTRAPOLATE)
+    if prec == A.CLM_PREC_MIXED:
+        kw.update(MIXED)
+    report(f"extrapolated_start_{'mixed' if prec == A.CLM_PREC_MIXED else 'fp64'}",
+           check_parity(w, 48, oracle_cfg=TOL_MODE, **kw))
+
+
 # Mixed path (FP32 Jacobian and Thomas; double-float closures; FP64 residual
 # assembly, increments, phase partition and budgets): 1e-8 wherever the
 # oracle reproduces itself under perturbations as large as the column's own
