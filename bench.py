@@ -451,9 +451,7 @@ def forms_block(args, torch, stream):
         "mixed": timed(**mxk),
         "plain_fp64_tol1e-8": timed(**tol),
         "mixed_tol1e-8": timed(**mxk, **tol),
-        "extrapolated_mixed_tol1e-8": timed(learned_guess=A.CLM_GUESS_EXTRAPOLATE, **mxk, **tol),
-        "extrapolated_mixed_tol1e-8_tile_order": timed(learned_guess=A.CLM_GUESS_EXTRAPOLATE, tol_regroup=0,
-                                                         **mxk, **tol)}
+        "extrapolated_mixed_tol1e-8": timed(learned_guess=A.CLM_GUESS_EXTRAPOLATE, **mxk, **tol)}
     del wf
     out["atmos_boundary"] = {"workload": wa.name, "plain_fp64": pub(a64, None, wa),
                              "mixed": pub(amx, a64, wa),
@@ -775,9 +773,10 @@ def main():
                    "l2": "inputs larger than L2 (state 48 B x cells)", "dt_s": w.dt},
         "e2e": {"value": e2e, "unit": "column-steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": h2d, "steps": e2e_steps},
-        # per step: the step kernel; in tolerance mode the regrouping's
-        # three kernels; with a guess, the guess kernel
-        "gpu_launches": args.steps * (1 + (3 if newton and not args.no_regroup else 0) + (1 if blob else 0)),
+        # per step: the step kernel; in tolerance mode without a guess the
+        # regrouping's three kernels; with the network guess, its kernel
+        "gpu_launches": args.steps * (1 + (3 if newton and not args.no_regroup and args.guess == "none" else 0)
+                                      + (1 if blob else 0)),
         "launch_config": dict(g.launch_config(), autotuned=tune is not None),
         "roofline": roofline,
         "compute_bound": compute,

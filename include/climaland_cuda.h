@@ -388,6 +388,10 @@ typedef struct clm_config {
                              warps by their last Newton iteration count each
                              step (a warp runs as many iterations as its
                              slowest column); 0 keeps the depth-sorted tiles.
+                             With a Newton guess (learned_guess != 0) the
+                             tiles are kept either way: the guess makes the
+                             last count a poor predictor and the regrouped
+                             warps' scattered loads cost more than they save.
                              Results do not depend on it                    */
   int32_t pad1;
 } clm_config;
