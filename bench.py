@@ -390,7 +390,8 @@ def forms_block(args, torch, stream):
         "pairs": res.nrows, "train_steps": 20000, "loss_first": float(res.loss[:50].mean()),
         "loss_last": float(res.loss[-200:].mean()), "train_s": res.seconds, "gen_train_s": gen_train_s,
         "heldout_mse": res.val_mse, "heldout_mse_zero_change": res.val_mse_zero,
-        "validation_gate_would_replace_it": bool(not res.val_mse < res.val_mse_zero)}
+        "validation_gate_would_replace_it": bool(not res.val_mse < res.val_mse_zero),
+        "heldout_metric": "tolerance-norm squared error (vartheta_l, 1e-9 rho_e_int)"}
     # (2) uneven columns, 4-30 layers, CSR: autotuned launch, CUDA graph replay
     w2 = WL.uneven_c2(ncol=args.forms_ncol, seed=0)
     u64 = run(w2, graph=1)
@@ -626,17 +627,21 @@ def main():
     if args.newton == "tol" or args.guess != "none":
         newton = dict(newton_mode=A.CLM_NEWTON_TOL, max_iters=20, newton_tol=1e-8, energy_norm_scale=1e-9)
     blob = None
+    learned_gated = None
     if args.guess in ("previous", "learned"):
         from climaland_gb300 import learned as LG
         if args.guess == "learned":
             X, Y = LG.generate(WL_full_scale(65536, 7), 32, newton=newton)
-            blob = LG.train(X, Y, steps=20000, batch=4096, lr=2e-3).blob
+            res = LG.train(X, Y, steps=20000, batch=4096, lr=2e-3)  # validation-gated
             del X, Y
+            blob = res.blob if res.guess_mode == A.CLM_GUESS_NETWORK else None
+            learned_gated = res.gated
         else:
             blob = LG.zero_change_blob()
     if newton and args.no_regroup:
         newton["tol_regroup"] = 0
-    mode = A.CLM_GUESS_NETWORK if blob else (A.CLM_GUESS_EXTRAPOLATE if args.guess == "extrapolate" else None)
+    mode = A.CLM_GUESS_NETWORK if blob else (A.CLM_GUESS_EXTRAPOLATE if args.guess in ("extrapolate", "learned")
+                                             else None)
     g = D.SoilColumns(w, precision=prec, learned_guess=mode, **newton)
     if blob:
         g.load_mlp(blob)
@@ -768,7 +773,9 @@ def main():
                               ("" if args.no_regroup else ", warps regrouped by iteration count")),
                    "newton_start": {"none": "U", "extrapolate": "previous increment (in the step kernel)",
                                     "previous": "previous increment (network launch, zero output)",
-                                    "learned": "previous increment + network"}[args.guess],
+                                    "learned": ("previous increment (in the step kernel: the validation gate "
+                                                "dropped the network)" if learned_gated else
+                                                "previous increment + network")}[args.guess],
                    "precision": args.precision,
                    "l2": "inputs larger than L2 (state 48 B x cells)", "dt_s": w.dt},
         "e2e": {"value": e2e, "unit": "column-steps/s", "h2d_bytes_per_step": h2d,

@@ -154,9 +154,16 @@ class TrainResult:
     loss: np.ndarray
     nrows: int
     seconds: float
-    val_mse: float = float("nan")       # held-out rows: the network's mean squared error
+    val_mse: float = float("nan")       # held-out rows: the network's error in the Newton norm
     val_mse_zero: float = float("nan")  # the same for a predicted change of zero
     gated: bool = False                 # blob is the zero-change network (see train)
+
+    @property
+    def guess_mode(self) -> int:
+        """The clm_config.learned_guess to run with: the network, or, when the
+        gate dropped it, the step kernel's own extrapolation (the same start
+        as the zero-change network without its launch)."""
+        return A.CLM_GUESS_EXTRAPOLATE if self.gated else A.CLM_GUESS_NETWORK
 
 
 def zero_change_blob() -> bytes:
@@ -169,12 +176,15 @@ def zero_change_blob() -> bytes:
     return blob
 
 
-def train(X, Y, steps=4000, batch=4096, lr=2e-3, seed=0, val_frac=0.05, gate=True):
+def train(X, Y, steps=4000, batch=4096, lr=2e-3, seed=0, val_frac=0.05, gate=True, energy_scale=1e-9):
     """Standardise, shuffle and train with the library's kernels; returns the
     weight blob for clm_load_mlp. A fraction val_frac of the shuffled rows is
-    held out; with gate, a network whose held-out error is not below that of
-    predicting no change is replaced by the zero-change weights (the guess
-    falls back to the previous increment)."""
+    held out and scored in the tolerance test's own norm (vartheta_l errors,
+    and rho_e_int errors times energy_scale, the clm_config's
+    energy_norm_scale): with gate, a network whose held-out error there is
+    not below that of predicting no change is replaced by the zero-change
+    weights (the guess is then the previous increment; TrainResult.guess_mode
+    says to run it as CLM_GUESS_EXTRAPOLATE)."""
     import time
     torch = _torch()
     gen = torch.Generator(device="cuda")
@@ -207,8 +217,10 @@ def train(X, Y, steps=4000, batch=4096, lr=2e-3, seed=0, val_frac=0.05, gate=Tru
     val = zero = float("nan")
     if nval > 0:
         P = tr.predict(Xv)
-        val = float(((P - Yv) ** 2).mean())
-        zero = float((Yv ** 2).mean())
+        w = torch.ones(N_OUT, device=Yv.device)
+        w[LAYERS:] = energy_scale ** 2
+        val = float((((P - Yv) ** 2) * w).sum(1).mean())
+        zero = float(((Yv ** 2) * w).sum(1).mean())
     tr.close()
     gated = bool(gate and nval > 0 and not val < zero)
     if gated:
