@@ -154,7 +154,7 @@ class TrainResult:
     loss: np.ndarray
     nrows: int
     seconds: float
-    val_mse: float = float("nan")       # held-out rows: the network's error in the Newton norm
+    val_mse: float = float("nan")       # held-out rows: mean log10 of the network's error norm
     val_mse_zero: float = float("nan")  # the same for a predicted change of zero
     gated: bool = False                 # blob is the zero-change network (see train)
 
@@ -179,12 +179,16 @@ def zero_change_blob() -> bytes:
 def train(X, Y, steps=4000, batch=4096, lr=2e-3, seed=0, val_frac=0.05, gate=True, energy_scale=1e-9):
     """Standardise, shuffle and train with the library's kernels; returns the
     weight blob for clm_load_mlp. A fraction val_frac of the shuffled rows is
-    held out and scored in the tolerance test's own norm (vartheta_l errors,
-    and rho_e_int errors times energy_scale, the clm_config's
-    energy_norm_scale): with gate, a network whose held-out error there is
-    not below that of predicting no change is replaced by the zero-change
-    weights (the guess is then the previous increment; TrainResult.guess_mode
-    says to run it as CLM_GUESS_EXTRAPOLATE)."""
+    held out; each row's error is its norm in the tolerance test's own terms
+    (vartheta_l errors, and rho_e_int errors times energy_scale, the
+    clm_config's energy_norm_scale), and the rows are scored by the mean of
+    its log10: Newton's iteration count follows the order of magnitude of a
+    column's start error, and a network that halves the large errors but
+    lifts the many small ones costs iterations (a mean squared error kept
+    such a network). With gate, a network whose score is not below that of
+    predicting no change is replaced by the zero-change weights (the guess
+    is then the previous increment; TrainResult.guess_mode says to run it as
+    CLM_GUESS_EXTRAPOLATE)."""
     import time
     torch = _torch()
     gen = torch.Generator(device="cuda")
@@ -219,8 +223,8 @@ def train(X, Y, steps=4000, batch=4096, lr=2e-3, seed=0, val_frac=0.05, gate=Tru
         P = tr.predict(Xv)
         w = torch.ones(N_OUT, device=Yv.device)
         w[LAYERS:] = energy_scale ** 2
-        val = float((((P - Yv) ** 2) * w).sum(1).mean())
-        zero = float(((Yv ** 2) * w).sum(1).mean())
+        val = float(torch.log10((((P - Yv) ** 2) * w).sum(1).sqrt() + 1e-30).mean())
+        zero = float(torch.log10(((Yv ** 2) * w).sum(1).sqrt() + 1e-30).mean())
     tr.close()
     gated = bool(gate and nval > 0 and not val < zero)
     if gated:

@@ -80,8 +80,9 @@ def test_training_fits_a_smooth_map(torch):
     res = LG.train(Xd, Yd, steps=3000, batch=2048, lr=2e-3)
     print(f"TRAIN loss {res.loss[:50].mean():.4f} -> {res.loss[-50:].mean():.4f} in {res.seconds:.2f}s")
     assert res.loss[-50:].mean() < 0.2 * res.loss[:50].mean()
-    # the held-out rows confirm the fit: the network is kept
-    assert res.val_mse < 0.2 * res.val_mse_zero and not res.gated
+    # the held-out rows confirm the fit (mean log10 error norm 0.2 decades
+    # or more below predicting zero): the network is kept
+    assert res.val_mse < res.val_mse_zero - 0.2 and not res.gated
 
 
 def test_validation_gate_drops_a_network_that_predicts_nothing(torch):
@@ -157,8 +158,8 @@ def test_learned_guess_saves_newton_iterations(torch):
             out[name] = (g.get_state(), np.mean(iters), f)
     sp, ip, _ = out["plain"]
     stats = dict(train_rows=res.nrows, train_seconds=res.seconds, loss_first=float(res.loss[:50].mean()),
-                 loss_last=float(res.loss[-50:].mean()), heldout_mse=res.val_mse,
-                 heldout_mse_zero_change=res.val_mse_zero, gated=res.gated, iters_plain=ip)
+                 loss_last=float(res.loss[-50:].mean()), heldout_log10_err=res.val_mse,
+                 heldout_log10_err_zero_change=res.val_mse_zero, gated=res.gated, iters_plain=ip)
     for name in ("learned", "previous_increment", "extrapolated"):
         sl, il, fl = out[name]
         colerr = np.max(np.abs(sp[0] - sl[0]).reshape(wev.ncol, 20), axis=1)
