@@ -23,7 +23,7 @@ namespace clm {
 cudaError_t launch_step(const StepArgs& A, int model, int precision, int wpc, int grid,
                         double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream);
 size_t step_smem_bytes(int model, int precision, int nmax, int wpc);
-cudaError_t step_grid(int model, int precision, int cm, bool str, int nmax, int wpc, int ntiles,
+cudaError_t step_grid(int model, int precision, int cm, bool str, bool tol, int nmax, int wpc, int ntiles,
                       int* grid);
 size_t step_scratch_doubles(int model, int precision, int nmax, int wpc, int grid);
 // clm_layout.cu
@@ -230,7 +230,7 @@ StepArgs step_args(const clm_handle* h) {
 // geometry) for the current warps per CTA, and its scratch.
 int configure_grid(clm_handle* h) {
   CLM_CUDA(h, step_grid(h->cfg.model, h->cfg.precision, h->cfg.hydrology_cm, h->d_geo != nullptr,
-                        h->nmax, h->wpc, h->ntiles, &h->grid));
+                        h->cfg.newton_mode == CLM_NEWTON_TOL, h->nmax, h->wpc, h->ntiles, &h->grid));
   const size_t nsc = step_scratch_doubles(h->cfg.model, h->cfg.precision, h->nmax, h->wpc, h->grid);
   if (nsc != h->scratch_doubles || (nsc && !h->d_scratch)) {
     dfree(h->d_scratch);
@@ -1214,8 +1214,8 @@ int clm_autotune(clm_handle* h, double t, double dt, int32_t probe_steps, clm_tu
   for (int w = 1; w <= 4; ++w) {
     if (step_smem_bytes(h->cfg.model, h->cfg.precision, h->nmax, w) > (size_t)dev_smem) break;
     int grid = 0;
-    CLM_CUDA(h, step_grid(h->cfg.model, h->cfg.precision, h->cfg.hydrology_cm, h->d_geo != nullptr, h->nmax,
-                          w, h->ntiles, &grid));
+    CLM_CUDA(h, step_grid(h->cfg.model, h->cfg.precision, h->cfg.hydrology_cm, h->d_geo != nullptr,
+                          h->cfg.newton_mode == CLM_NEWTON_TOL, h->nmax, w, h->ntiles, &grid));
     need = std::max(need, step_scratch_doubles(h->cfg.model, h->cfg.precision, h->nmax, w, grid));
     for (int sch : {CLM_SCHED_STATIC, CLM_SCHED_DYNAMIC}) {
       clm_tune_entry e{};

@@ -223,11 +223,19 @@ constexpr int kSrcNone = 0;
 constexpr int kSrcRoots = 1;  // RootExtraction (A.rx)
 constexpr int kSrcAtmos = 2;  // atmosphere-driven top boundary + SoilSublimation (A.atm)
 
+// Newton mode of a column-code instantiation: fixed iterations or
+// tolerance-stopped known when compiling (the step kernels instantiate both,
+// so that each carries only its own mode's code), or read from
+// StepArgs::newton_mode at run time.
+constexpr int kNewtonFixed = 0;
+constexpr int kNewtonTol = 1;
+constexpr int kNewtonRuntime = 2;
+
 // Geom: ColGeom (uniform layers) or ColGeomS (per-layer geometry); G holds
 // the column's. On a uniform column rdz(k) = dt / dz and the face means
 // 0.5 (a + b) / dz are exactly (a + b) hinv_gap(k).
 template <typename JT, class CM, bool kLogKappaHere = false, int kSrc = kSrcNone,
-          class Geom = ColGeom>
+          int kNewton = kNewtonRuntime, class Geom = ColGeom>
 CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int orig,
                       const EHBuffers& B, const EHJac<JT>& J, const Geom& G, double t0,
                       double dt, int nsteps, double& Fw, double& Fe, uint32_t& flags,
@@ -246,7 +254,8 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
   EHMixed<CM> MX;
   PCCol pcc = make_pc_col(c.nu, c.theta_r, G.width(0));
   if constexpr (mixed) MX = make_eh_mixed(Tb, E, sc, c);
-  const bool tol = A.newton_mode == CLM_NEWTON_TOL;  // the increment norms are needed only then
+  // the increment norms are needed only in tolerance mode
+  const bool tol = kNewton == kNewtonRuntime ? A.newton_mode == CLM_NEWTON_TOL : kNewton == kNewtonTol;
   constexpr bool kRoots = kSrc == kSrcRoots;
   constexpr bool kAtmos = kSrc == kSrcAtmos;
 

@@ -7,7 +7,9 @@
 
 namespace clm {
 
-void* step_fn_vg(int model, int precision, int src) { return step_fn_t<VG, false>(model, precision, src); }
+void* step_fn_vg(int model, int precision, int src, bool tol) {
+  return step_fn_t<VG, false>(model, precision, src, tol);
+}
 
 void launch_step_vg(const StepArgs& A, int model, int precision, int grid, dim3 block, size_t smem,
                     double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream) {
@@ -29,26 +31,29 @@ size_t step_smem_bytes(int model, int precision, int nmax, int wpc) {
   return tab * sizeof(double) + per_layer * (size_t)nmax * kTile * wpc;
 }
 
-static void* step_fn(int model, int precision, int cm, bool str, int src = kSrcNone) {
+static void* step_fn(int model, int precision, int cm, bool str, int src, bool tol) {
   if (cm == CLM_CM_BROOKS_COREY)
-    return str ? step_fn_bc_s(model, precision, src) : step_fn_bc(model, precision, src);
-  return str ? step_fn_vg_s(model, precision, src) : step_fn_vg(model, precision, src);
+    return str ? step_fn_bc_s(model, precision, src, tol) : step_fn_bc(model, precision, src, tol);
+  return str ? step_fn_vg_s(model, precision, src, tol) : step_fn_vg(model, precision, src, tol);
 }
 
 // CTAs of `wpc` warps that can be resident on the whole device (the
-// kernels of uniform columns, or with per-layer geometry when `str`).
-cudaError_t step_grid(int model, int precision, int cm, bool str, int nmax, int wpc, int ntiles,
+// kernels of uniform columns, or with per-layer geometry when `str`; of
+// tolerance-mode Newton when `tol`).
+cudaError_t step_grid(int model, int precision, int cm, bool str, bool tol, int nmax, int wpc, int ntiles,
                       int* grid) {
   const size_t smem = step_smem_bytes(model, precision, nmax, wpc);
-  void* fn = step_fn(model, precision, cm, str);
-  cudaError_t err = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (err != cudaSuccess) return err;
-  if (model == CLM_MODEL_ENERGY_HYDROLOGY) {  // the same launch shape with a source variant
-    for (int src : {kSrcRoots, kSrcAtmos})
-      if ((err = cudaFuncSetAttribute(step_fn(model, precision, cm, str, src),
+  cudaError_t err;
+  // every variant of the launch shape: source kinds and both Newton modes
+  for (int src : {kSrcNone, kSrcRoots, kSrcAtmos}) {
+    for (bool t : {false, true}) {
+      if (model != CLM_MODEL_ENERGY_HYDROLOGY && (src != kSrcNone || t)) continue;
+      if ((err = cudaFuncSetAttribute(step_fn(model, precision, cm, str, src, t),
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
         return err;
+    }
   }
+  void* fn = step_fn(model, precision, cm, str, kSrcNone, tol && model == CLM_MODEL_ENERGY_HYDROLOGY);
   int dev = 0, nsm = 0, per_sm = 0;
   if ((err = cudaGetDevice(&dev)) != cudaSuccess) return err;
   if ((err = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return err;

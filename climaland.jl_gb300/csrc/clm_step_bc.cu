@@ -6,7 +6,9 @@
 
 namespace clm {
 
-void* step_fn_bc(int model, int precision, int src) { return step_fn_t<BC, false>(model, precision, src); }
+void* step_fn_bc(int model, int precision, int src, bool tol) {
+  return step_fn_t<BC, false>(model, precision, src, tol);
+}
 
 void launch_step_bc(const StepArgs& A, int model, int precision, int grid, dim3 block, size_t smem,
                     double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream) {

@@ -5,7 +5,9 @@
 
 namespace clm {
 
-void* step_fn_bc_s(int model, int precision, int src) { return step_fn_t<BC, true>(model, precision, src); }
+void* step_fn_bc_s(int model, int precision, int src, bool tol) {
+  return step_fn_t<BC, true>(model, precision, src, tol);
+}
 
 void launch_step_bc_s(const StepArgs& A, int model, int precision, int grid, dim3 block, size_t smem,
                       double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream) {

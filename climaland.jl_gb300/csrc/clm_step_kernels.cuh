@@ -49,8 +49,13 @@ __host__ __device__ constexpr int eh_scratch_slots(bool mixed) { return mixed ? 
 
 // kSrc: the RootExtraction source (A.rx) or the atmosphere-driven top
 // boundary (A.atm) compiled in; separate kernels so that their registers do
-// not weigh on the step without them. kStr: per-layer geometry.
-template <typename JT, class CM, int kSrc, bool kStr>
+// not weigh on the step without them. kStr: per-layer geometry. kTol: the
+// tolerance-mode Newton (norms, stopping, guesses) compiled in; the
+// fixed-iteration kernel carries none of its code, and each has a smaller
+// instruction footprint (with both modes in one kernel, instruction-fetch
+// stalls measured 0.81 cycles per issued instruction in tolerance mode with a
+// guess, 0.23 in fixed mode).
+template <typename JT, class CM, int kSrc, bool kStr, bool kTol = false>
 __global__ void __launch_bounds__(128, 1)
     eh_step_kernel(StepArgs A, double* __restrict__ scratch, StepClock clk, int nsteps) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -117,8 +122,8 @@ __global__ void __launch_bounds__(128, 1)
       uint32_t flags = 0;
       int iters = 0;
       const auto G = GeomOf<kStr>::make(A, base, s, n);
-      eh_column<JT, CM, false, kSrc>(A, Tb, s, n, A.L.perm[s], B, J, G, t0, dt, nsteps, Fw, Fe, flags,
-                                     iters);
+      eh_column<JT, CM, false, kSrc, kTol ? kNewtonTol : kNewtonFixed>(A, Tb, s, n, A.L.perm[s], B, J, G,
+                                                                       t0, dt, nsteps, Fw, Fe, flags, iters);
       A.Fw[s] = Fw;
       A.Fe[s] = Fe;
       A.flags[s] |= flags;  // cleared at the start of each step call
@@ -184,36 +189,50 @@ inline int step_src(const StepArgs& A) {
 
 // The kernel of (model, precision, source variant) for closure CM and
 // geometry kStr, and its launch.
+template <class CM, bool kStr, bool kTol>
+void* eh_fn_t(bool mx, int src) {
+  if (src == kSrcRoots)
+    return mx ? (void*)eh_step_kernel<float, CM, kSrcRoots, kStr, kTol>
+              : (void*)eh_step_kernel<double, CM, kSrcRoots, kStr, kTol>;
+  if (src == kSrcAtmos)
+    return mx ? (void*)eh_step_kernel<float, CM, kSrcAtmos, kStr, kTol>
+              : (void*)eh_step_kernel<double, CM, kSrcAtmos, kStr, kTol>;
+  return mx ? (void*)eh_step_kernel<float, CM, kSrcNone, kStr, kTol>
+            : (void*)eh_step_kernel<double, CM, kSrcNone, kStr, kTol>;
+}
+
 template <class CM, bool kStr>
-void* step_fn_t(int model, int precision, int src = kSrcNone) {
+void* step_fn_t(int model, int precision, int src = kSrcNone, bool tol = false) {
   if (model == CLM_MODEL_ENERGY_HYDROLOGY) {
     const bool mx = precision == CLM_PREC_MIXED;
-    if (src == kSrcRoots)
-      return mx ? (void*)eh_step_kernel<float, CM, kSrcRoots, kStr>
-                : (void*)eh_step_kernel<double, CM, kSrcRoots, kStr>;
-    if (src == kSrcAtmos)
-      return mx ? (void*)eh_step_kernel<float, CM, kSrcAtmos, kStr>
-                : (void*)eh_step_kernel<double, CM, kSrcAtmos, kStr>;
-    return mx ? (void*)eh_step_kernel<float, CM, kSrcNone, kStr>
-              : (void*)eh_step_kernel<double, CM, kSrcNone, kStr>;
+    return tol ? eh_fn_t<CM, kStr, true>(mx, src) : eh_fn_t<CM, kStr, false>(mx, src);
   }
   return precision == CLM_PREC_MIXED ? (void*)richards_step_kernel<float, CM, kStr>
                                      : (void*)richards_step_kernel<double, CM, kStr>;
 }
 
+template <typename JT, class CM, bool kStr, bool kTol>
+void launch_eh_mode(const StepArgs& A, int grid, dim3 block, size_t smem, double* scratch,
+                    const StepClock& clk, int nsteps, cudaStream_t stream) {
+  switch (step_src(A)) {
+    case kSrcRoots:
+      eh_step_kernel<JT, CM, kSrcRoots, kStr, kTol><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
+      break;
+    case kSrcAtmos:
+      eh_step_kernel<JT, CM, kSrcAtmos, kStr, kTol><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
+      break;
+    default:
+      eh_step_kernel<JT, CM, kSrcNone, kStr, kTol><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
+  }
+}
+
 template <typename JT, class CM, bool kStr>
 void launch_eh_t(const StepArgs& A, int grid, dim3 block, size_t smem, double* scratch,
                  const StepClock& clk, int nsteps, cudaStream_t stream) {
-  switch (step_src(A)) {
-    case kSrcRoots:
-      eh_step_kernel<JT, CM, kSrcRoots, kStr><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
-      break;
-    case kSrcAtmos:
-      eh_step_kernel<JT, CM, kSrcAtmos, kStr><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
-      break;
-    default:
-      eh_step_kernel<JT, CM, kSrcNone, kStr><<<grid, block, smem, stream>>>(A, scratch, clk, nsteps);
-  }
+  if (A.newton_mode == CLM_NEWTON_TOL)
+    launch_eh_mode<JT, CM, kStr, true>(A, grid, block, smem, scratch, clk, nsteps, stream);
+  else
+    launch_eh_mode<JT, CM, kStr, false>(A, grid, block, smem, scratch, clk, nsteps, stream);
 }
 
 template <class CM, bool kStr>
@@ -235,10 +254,10 @@ void launch_step_t(const StepArgs& A, int model, int precision, int grid, dim3 b
 // One translation unit per (closure, geometry) instantiates these: the entry
 // points each defines (clm_step.cu, clm_step_bc.cu, clm_step_s.cu,
 // clm_step_bc_s.cu).
-void* step_fn_vg(int model, int precision, int src);
-void* step_fn_bc(int model, int precision, int src);
-void* step_fn_vg_s(int model, int precision, int src);
-void* step_fn_bc_s(int model, int precision, int src);
+void* step_fn_vg(int model, int precision, int src, bool tol);
+void* step_fn_bc(int model, int precision, int src, bool tol);
+void* step_fn_vg_s(int model, int precision, int src, bool tol);
+void* step_fn_bc_s(int model, int precision, int src, bool tol);
 void launch_step_vg(const StepArgs& A, int model, int precision, int grid, dim3 block, size_t smem,
                     double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream);
 void launch_step_bc(const StepArgs& A, int model, int precision, int grid, dim3 block, size_t smem,
