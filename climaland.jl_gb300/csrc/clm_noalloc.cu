@@ -3,8 +3,9 @@
 //
 // Some hosts run this library inside a memory budget they do not control:
 // a CUDA.jl or PyTorch caching allocator that owns the device heap, a
-// captured CUDA graph (where a cudaMalloc would break the capture), or an
-// embedding that forbids allocations after start-up. The handle API
+// time-stepping loop that cannot afford the device-wide synchronisation a
+// cudaMalloc/cudaFree may bring, or an embedding that forbids allocations
+// after start-up. The handle API
 // (clm_create) allocates its layout, staging and scratch buffers, so such
 // callers cannot use it. This entry point takes every input and output as
 // caller-owned device memory, in the reference's column layout, and keeps

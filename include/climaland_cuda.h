@@ -626,8 +626,9 @@ int clm_mlp_set(clm_mlp* m, const void* blob, int64_t nbytes);
 /* ---- allocation-free step (no reference counterpart) -----------------
  * The EnergyHydrology step for callers that cannot allocate device memory:
  * hosts whose device heap belongs to another allocator (CUDA.jl or PyTorch
- * caching allocators under a fixed budget), code running inside a CUDA
- * graph capture, or embeddings that forbid allocation after start-up.
+ * caching allocators under a fixed budget), time-stepping loops that cannot
+ * take the synchronisation a cudaMalloc/cudaFree may bring, or embeddings
+ * that forbid allocation after start-up.
  * Everything is caller-owned device memory in the reference layout: z_lo,
  * z_hi (ncol), params (CLM_NPARAM_EH rows of ncol), the state (cell = c * nlayers + k) and intF_w / intF_e (ncol),
  * updated in place; flags (ncol, CLM_COL_*) may be NULL. forcing is a

@@ -1,7 +1,8 @@
 """The allocation-free step (clm_step_eh_noalloc) against the handle path.
 
-Callers whose device memory belongs to another allocator, or who run inside
-a CUDA graph capture, cannot let the library call cudaMalloc; this entry
+Callers whose device memory belongs to another allocator (a caching
+allocator under a fixed budget), or who forbid allocation after start-up,
+cannot let the library call cudaMalloc; this entry
 point takes every buffer from the caller and keeps its working scratch in a
 fixed array inside the library. The test drives it through the C ABI on
 caller-owned device buffers for two calls in a row and compares each result
