@@ -374,18 +374,32 @@ def forms_block(args, torch, stream):
     res = LG.train(X, Y, steps=20000, batch=4096, lr=2e-3, gate=False)
     gen_train_s = time.perf_counter() - t0
     del X, Y
+    # the library's default schedule (CLM_TOL_AUTO): FP64 from U regrouped by
+    # iteration count, everything else split Newton (two iterations for every
+    # column, then the unconverged columns packed 32 to a warp); beside them
+    # the other schedules (the same bits)
+    mxt = dict(tol, precision=A.CLM_PREC_MIXED)
     plain_tol = run(w4, **tol)
-    mixed_tol = run(w4, precision=A.CLM_PREC_MIXED, **tol)
-    learned = run(w4, blob=res.blob, learned_guess=1, precision=A.CLM_PREC_MIXED, **tol)
+    plain_split = run(w4, tol_regroup=A.CLM_TOL_SPLIT, **tol)
+    mixed_tol = run(w4, **mxt)
+    mixed_regroup = run(w4, tol_regroup=A.CLM_TOL_REGROUP, **mxt)
+    learned = run(w4, blob=res.blob, learned_guess=1, **mxt)
     # the previous increment alone (the network's output held at zero)
-    persist = run(w4, blob=LG.zero_change_blob(), learned_guess=1, precision=A.CLM_PREC_MIXED, **tol)
+    persist = run(w4, blob=LG.zero_change_blob(), learned_guess=1, **mxt)
     # the same start computed inside the step kernel (no network launch)
-    extrap = run(w4, learned_guess=A.CLM_GUESS_EXTRAPOLATE, precision=A.CLM_PREC_MIXED, **tol)
-    out["full_scale_subset"]["plain_fp64_tol1e-8"] = pub(plain_tol, plain, w4, tol)
-    out["full_scale_subset"]["mixed_tol1e-8"] = pub(mixed_tol, plain, w4, tol)
-    out["full_scale_subset"]["learned_mixed_tol1e-8"] = pub(learned, plain, w4, tol)
-    out["full_scale_subset"]["previous_increment_mixed_tol1e-8"] = pub(persist, plain, w4, tol)
-    out["full_scale_subset"]["extrapolated_mixed_tol1e-8"] = pub(extrap, plain, w4, tol)
+    extrap = run(w4, learned_guess=A.CLM_GUESS_EXTRAPOLATE, **mxt)
+    extrap_tiles = run(w4, learned_guess=A.CLM_GUESS_EXTRAPOLATE, tol_regroup=A.CLM_TOL_TILES, **mxt)
+    fs = out["full_scale_subset"]
+    fs["plain_fp64_tol1e-8"] = pub(plain_tol, plain, w4, tol)
+    fs["plain_fp64_tol1e-8_split"] = pub(plain_split, plain, w4, tol)
+    fs["mixed_tol1e-8"] = pub(mixed_tol, plain, w4, tol)
+    fs["mixed_tol1e-8_regroup"] = pub(mixed_regroup, plain, w4, tol)
+    fs["learned_mixed_tol1e-8"] = pub(learned, plain, w4, tol)
+    fs["previous_increment_mixed_tol1e-8"] = pub(persist, plain, w4, tol)
+    fs["extrapolated_mixed_tol1e-8"] = pub(extrap, plain, w4, tol)
+    fs["extrapolated_mixed_tol1e-8_tiles"] = pub(extrap_tiles, plain, w4, tol)
+    fs["tolerance_schedules"] = ("default CLM_TOL_AUTO: FP64 from U regrouped by iteration count, the "
+                                 "others split Newton; _split, _regroup, _tiles: that schedule forced")
     out["full_scale_subset"]["learned_training"] = {
         "pairs": res.nrows, "train_steps": 20000, "loss_first": float(res.loss[:50].mean()),
         "loss_last": float(res.loss[-200:].mean()), "train_s": res.seconds, "gen_train_s": gen_train_s,
@@ -452,7 +466,10 @@ def forms_block(args, torch, stream):
         "mixed": timed(**mxk),
         "plain_fp64_tol1e-8": timed(**tol),
         "mixed_tol1e-8": timed(**mxk, **tol),
-        "extrapolated_mixed_tol1e-8": timed(learned_guess=A.CLM_GUESS_EXTRAPOLATE, **mxk, **tol)}
+        "extrapolated_mixed_tol1e-8": timed(learned_guess=A.CLM_GUESS_EXTRAPOLATE, **mxk, **tol),
+        "plain_fp64_tol1e-8_split": timed(tol_regroup=A.CLM_TOL_SPLIT, **tol),
+        "extrapolated_fp64_tol1e-8": timed(learned_guess=A.CLM_GUESS_EXTRAPOLATE, **tol),
+        "tolerance_schedules": "as full_scale_subset"}
     del wf
     out["atmos_boundary"] = {"workload": wa.name, "plain_fp64": pub(a64, None, wa),
                              "mixed": pub(amx, a64, wa),
@@ -568,6 +585,9 @@ def main():
                     help="fixed: the configuration's 3 iterations; tol: stop at 1e-8 (at most 20)")
     ap.add_argument("--no-regroup", action="store_true",
                     help="tolerance mode without regrouping the columns into warps by iteration count")
+    ap.add_argument("--split", action="store_true",
+                    help="tolerance mode with split Newton: two iterations for every column, then the "
+                         "unconverged columns packed 32 to a warp in a second launch")
     ap.add_argument("--guess", default="none", choices=["none", "extrapolate", "previous", "learned"],
                     help="Newton start (tolerance mode): U; the previous increment, inside the step "
                          "kernel (extrapolate) or through the network's launch with the network's "
@@ -639,7 +659,13 @@ def main():
         else:
             blob = LG.zero_change_blob()
     if newton and args.no_regroup:
-        newton["tol_regroup"] = 0
+        newton["tol_regroup"] = A.CLM_TOL_TILES
+    if newton and args.split:
+        newton["tol_regroup"] = A.CLM_TOL_SPLIT
+    sched = newton.get("tol_regroup", A.CLM_TOL_AUTO) if newton else None
+    if sched == A.CLM_TOL_AUTO:  # the library's rule
+        sched = (A.CLM_TOL_REGROUP if w.cfg.model != 1 or (prec == A.CLM_PREC_FP64 and args.guess == "none")
+                 else A.CLM_TOL_SPLIT)
     mode = A.CLM_GUESS_NETWORK if blob else (A.CLM_GUESS_EXTRAPOLATE if args.guess in ("extrapolate", "learned")
                                              else None)
     g = D.SoilColumns(w, precision=prec, learned_guess=mode, **newton)
@@ -770,7 +796,11 @@ def main():
                    "model": "EnergyHydrology" if w.cfg.model == 1 else "RichardsModel",
                    "newton": (f"fixed {w.cfg.max_iters} iterations" if not newton else
                               "tolerance 1e-8 (at most 20 iterations)" +
-                              ("" if args.no_regroup else ", warps regrouped by iteration count")),
+                              {A.CLM_TOL_TILES: ", depth-sorted tiles",
+                               A.CLM_TOL_REGROUP: (", warps regrouped by iteration count" if args.guess == "none"
+                                                   else ", depth-sorted tiles"),
+                               A.CLM_TOL_SPLIT: ", split Newton (two iterations, then the unconverged columns "
+                                                "packed 32 to a warp)"}[sched]),
                    "newton_start": {"none": "U", "extrapolate": "previous increment (in the step kernel)",
                                     "previous": "previous increment (network launch, zero output)",
                                     "learned": ("previous increment (in the step kernel: the validation gate "
@@ -781,9 +811,10 @@ def main():
         "e2e": {"value": e2e, "unit": "column-steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": h2d, "steps": e2e_steps},
         # per step: the step kernel; in tolerance mode without a guess the
-        # regrouping's three kernels; with the network guess, its kernel
-        "gpu_launches": args.steps * (1 + (3 if newton and not args.no_regroup and args.guess == "none" else 0)
-                                      + (1 if blob else 0)),
+        # regrouping's three kernels, with split Newton the resuming kernel;
+        # with the network guess, its kernel
+        "gpu_launches": args.steps * (1 + (3 if sched == A.CLM_TOL_REGROUP and args.guess == "none" else 0)
+                                      + (1 if sched == A.CLM_TOL_SPLIT else 0) + (1 if blob else 0)),
         "launch_config": dict(g.launch_config(), autotuned=tune is not None),
         "roofline": roofline,
         "compute_bound": compute,

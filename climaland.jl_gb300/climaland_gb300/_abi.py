@@ -47,6 +47,10 @@ CLM_GUESS_NETWORK = 1
 CLM_GUESS_EXTRAPOLATE = 2
 CLM_SCHED_STATIC = 0
 CLM_SCHED_DYNAMIC = 1
+CLM_TOL_TILES = 0
+CLM_TOL_REGROUP = 1
+CLM_TOL_SPLIT = 2
+CLM_TOL_AUTO = 3
 CLM_BC_FLUX = 0
 CLM_BC_FREE_DRAINAGE = 1
 CLM_BC_STATE = 2
@@ -248,7 +252,7 @@ def default_config() -> ClmConfig:
     c.cols_per_cta = 0
     c.schedule = CLM_SCHED_STATIC
     c.graph = 0
-    c.tol_regroup = 1
+    c.tol_regroup = CLM_TOL_AUTO
     return c
 
 

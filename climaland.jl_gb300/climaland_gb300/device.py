@@ -68,7 +68,7 @@ class SoilColumns:
         if learned_guess is not None:
             cfg.learned_guess = int(learned_guess)
         if tol_regroup is not None:
-            cfg.tol_regroup = int(bool(tol_regroup))
+            cfg.tol_regroup = int(tol_regroup)  # enum clm_tol_schedule (a bool: tiles or regroup)
         if schedule is not None:
             cfg.schedule = int(schedule)
         if graph is not None:

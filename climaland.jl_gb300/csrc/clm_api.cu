@@ -26,6 +26,10 @@ size_t step_smem_bytes(int model, int precision, int nmax, int wpc);
 cudaError_t step_grid(int model, int precision, int cm, bool str, bool tol, int nmax, int wpc, int ntiles,
                       int* grid);
 size_t step_scratch_doubles(int model, int precision, int nmax, int wpc, int grid);
+cudaError_t resume_setup(int precision, int cm, bool str, int nmax, int wpc);
+size_t split_queue_doubles(int cap, int nmax);
+cudaError_t launch_resume(const StepArgs& A, int precision, int wpc, int grid, const StepClock& clk,
+                          cudaStream_t stream);
 // clm_layout.cu
 cudaError_t ref_to_internal(const Layout& L, const XFields& F, cudaStream_t st, int tile0 = 0,
                             int ntl = -1);
@@ -94,6 +98,11 @@ struct clm_handle {
   int* d_ctr = nullptr;          // dynamic tile order: [next tile, warps done]
   int* d_order = nullptr;        // iteration-class slot order (tolerance mode)
   int* d_order_bins = nullptr;   // its counting-sort bins
+  // split Newton: entries of the columns left unconverged by the step kernel
+  // and their count (tolerance mode, CLM_TOL_SPLIT)
+  double* d_queue = nullptr;
+  int* d_qcount = nullptr;
+  size_t queue_doubles = 0;
   double* d_scratch = nullptr;  // per-warp-slot frozen aux arrays
   size_t scratch_doubles = 0;
   int guess_grid = 0;           // persistent grid of the guess kernel
@@ -152,9 +161,33 @@ bool is_eh(const clm_handle* h) { return h->cfg.model == CLM_MODEL_ENERGY_HYDROL
 // Warps regrouped by iteration count: tolerance mode without a Newton guess
 // (with one, tile order measured faster: 19.5 against 21.0 ms per
 // 1,048,576-column mixed step with the extrapolated start).
+// The tolerance schedule in use: CLM_TOL_AUTO resolved by the measured rule
+// (1,048,576 x 20 EnergyHydrology columns at tolerance 1e-8: FP64 from U
+// 32.2 ms per step regrouped against 33.9 split; mixed from U 18.7 against
+// 17.2; mixed from the extrapolated start 19.7 in tiles against 16.9 split).
+int tol_schedule(const clm_handle* h) {
+  const int t = h->cfg.tol_regroup;
+  if (t != CLM_TOL_AUTO) return t;
+  if (!is_eh(h) || (h->cfg.precision == CLM_PREC_FP64 && h->cfg.learned_guess == CLM_GUESS_NONE))
+    return CLM_TOL_REGROUP;
+  return CLM_TOL_SPLIT;
+}
+
 bool regroups(const clm_handle* h) {
-  return h->cfg.newton_mode == CLM_NEWTON_TOL && h->cfg.tol_regroup && h->d_order &&
+  return h->cfg.newton_mode == CLM_NEWTON_TOL && tol_schedule(h) == CLM_TOL_REGROUP && h->d_order &&
          h->cfg.learned_guess == CLM_GUESS_NONE;
+}
+
+// Split Newton (EnergyHydrology, tolerance mode): each step is two launches,
+// the step kernel running every column through its first kSplitIters
+// iterations and the resuming kernel finishing the columns that have not
+// converged, packed 32 to a warp. Warps in lockstep then run as many
+// iterations as the columns need, not as the slowest of 32 neighbours.
+constexpr int kSplitIters = 2;
+
+bool splits(const clm_handle* h) {
+  return h->cfg.newton_mode == CLM_NEWTON_TOL && tol_schedule(h) == CLM_TOL_SPLIT && is_eh(h) &&
+         h->d_queue && h->cfg.max_iters > kSplitIters;
 }
 
 // Captured graphs hold kernel arguments by value (buffer pointers, launch
@@ -238,6 +271,21 @@ int configure_grid(clm_handle* h) {
     h->scratch_doubles = nsc;
   }
   h->guess_grid = 0;
+  // split Newton's queue: room for every column (each defers at most once a
+  // step), allocated here so that no step call allocates
+  if (h->cfg.newton_mode == CLM_NEWTON_TOL && tol_schedule(h) == CLM_TOL_SPLIT && is_eh(h)) {
+    const size_t nq = split_queue_doubles(h->stride, h->nmax);
+    if (nq != h->queue_doubles || !h->d_queue) {
+      drop_graphs(h);  // captured launches hold the queue's address
+      dfree(h->d_queue);
+      h->queue_doubles = 0;
+      CLM_CUDA(h, cudaMalloc(&h->d_queue, sizeof(double) * nq));
+      h->queue_doubles = nq;
+    }
+    if (!h->d_qcount) CLM_CUDA(h, cudaMalloc(&h->d_qcount, sizeof(int)));
+    // the resuming kernel's shared memory for the largest CTA clm_autotune tries
+    CLM_CUDA(h, resume_setup(h->cfg.precision, h->cfg.hydrology_cm, h->d_geo != nullptr, h->nmax, 4));
+  }
   return CLM_OK;
 }
 
@@ -364,7 +412,7 @@ struct Launch {
 // regrouping, one step launch per step, each followed by the regrouping.
 std::vector<Launch> launch_sequence(const clm_handle* h, int nsteps) {
   std::vector<Launch> seq;
-  if (h->cfg.learned_guess == CLM_GUESS_NETWORK || regroups(h)) {  // per step: guess, or regroup, in between
+  if (h->cfg.learned_guess == CLM_GUESS_NETWORK || regroups(h) || splits(h)) {  // one launch sequence per step
     const bool guess = h->cfg.learned_guess == CLM_GUESS_NETWORK;
     for (int i = 0; i < nsteps; ++i) seq.push_back({i, 1, guess});
   } else {
@@ -379,6 +427,15 @@ int issue(clm_handle* h, const Launch& l, const StepClock& clk, cudaStream_t st)
   if (l.guess) {
     const float* P = h->d_mlp;
     CLM_CUDA(h, mlp_guess(A, P, P + kMlpParams, clk, h->d_guess, h->d_prev, h->guess_grid, st));
+  }
+  if (splits(h) && l.nsteps == 1) {
+    StepArgs S = A;
+    S.split = SplitQueue{h->d_queue, h->d_qcount, h->stride, h->nmax};
+    S.split_at = kSplitIters;
+    CLM_CUDA(h, cudaMemsetAsync(h->d_qcount, 0, sizeof(int), st));
+    CLM_CUDA(h, launch_step(S, h->cfg.model, h->cfg.precision, h->wpc, h->grid, h->d_scratch, clk, 1, st));
+    CLM_CUDA(h, launch_resume(S, h->cfg.precision, h->wpc, h->grid, clk, st));
+    return CLM_OK;
   }
   CLM_CUDA(h, launch_step(A, h->cfg.model, h->cfg.precision, h->wpc, h->grid, h->d_scratch, clk,
                           l.nsteps, st));
@@ -396,7 +453,7 @@ int step_graph(clm_handle* h, double t, double dt, int nsteps) {
     CLM_CUDA(h, cudaMallocHost(&h->h_clock, sizeof(double) * (kClockSlots + 1) * clm_handle::kRing));
     for (auto& ev : h->clock_ev) CLM_CUDA(h, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   }
-  const int per_launch = (h->cfg.learned_guess == CLM_GUESS_NETWORK || regroups(h)) ? 1 : 64;
+  const int per_launch = (h->cfg.learned_guess == CLM_GUESS_NETWORK || regroups(h) || splits(h)) ? 1 : 64;
   const int piece_max = per_launch * kClockSlots;
   for (int s_begin = 0; s_begin < nsteps; s_begin += piece_max) {
     const int P = std::min(piece_max, nsteps - s_begin);
@@ -580,7 +637,7 @@ int check_config(const clm_config* cfg) {
   if (cfg->newton_mode != CLM_NEWTON_FIXED && cfg->newton_mode != CLM_NEWTON_TOL) return CLM_ERR_ARG;
   if (cfg->schedule != CLM_SCHED_STATIC && cfg->schedule != CLM_SCHED_DYNAMIC) return CLM_ERR_ARG;
   if (cfg->graph != 0 && cfg->graph != 1) return CLM_ERR_ARG;
-  if (cfg->tol_regroup != 0 && cfg->tol_regroup != 1) return CLM_ERR_ARG;
+  if (cfg->tol_regroup < CLM_TOL_TILES || cfg->tol_regroup > CLM_TOL_AUTO) return CLM_ERR_ARG;
   if (cfg->cols_per_cta < 0) return CLM_ERR_ARG;
   if (cfg->hydrology_cm != CLM_CM_VAN_GENUCHTEN && cfg->hydrology_cm != CLM_CM_BROOKS_COREY)
     return CLM_ERR_ARG;
@@ -644,7 +701,7 @@ void clm_config_default(clm_config* c) {
   c->earth.LH_f0 = 2834400.0 - 2500800.0;
   c->earth.grav = 9.81;
   c->phase_change = 1;
-  c->tol_regroup = 1;
+  c->tol_regroup = CLM_TOL_AUTO;
 }
 
 int clm_create(const clm_config* cfg, clm_handle** out) {
@@ -726,6 +783,8 @@ void clm_destroy(clm_handle* h) {
   dfree(h->d_ctr);
   dfree(h->d_order);
   dfree(h->d_order_bins);
+  dfree(h->d_queue);
+  dfree(h->d_qcount);
   drop_graphs(h);
   dfree(h->d_clock);
   if (h->h_clock) cudaFreeHost(h->h_clock);

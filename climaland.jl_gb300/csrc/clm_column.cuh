@@ -183,6 +183,9 @@ struct EHBuffers {
   // start, read for the guess u_n + (u_n - u_{n-1}) and replaced by u_n
   // (p == nullptr: no extrapolation)
   Col<double> prev_v{nullptr, 0}, prev_e{nullptr, 0};
+  // resumed solve (kResume): gv, gti, ge hold the saved stage value U and the
+  // final state goes to the column's own state arrays ov, oe
+  Col<double> ov{nullptr, 0}, oe{nullptr, 0};
 };
 
 // FP64 <-> Jacobian-type conversions: identities on the FP64 path; on the
@@ -218,6 +221,33 @@ struct EHJac {
   Col<JT> cp, dp, d, ae;            // Thomas c', d' (then delta_v, d''), dpsi, face coef
 };
 
+// What a column's Newton solve carries from one iteration to the next
+// besides its arrays (the iterate x, the stage value U and the aux frozen
+// through the solve): the split Newton schedule saves it after the first
+// iterations of the columns that have not converged and resumes them in a
+// second launch (eh_column's Defer and kResume).
+struct EHNewtonCtx {
+  double Ftw, Fth, Fbw, Fbh;  // boundary fluxes at Y_n, frozen through the solve
+  double UFw, UFe, xFw, xFe;  // integrated fluxes: stage value and iterate
+  double R_ss, R_ess;         // TOPMODEL's subsurface water and energy sinks
+  double prev_norm, prev_state2, pred2;
+  int it_start;               // iterations spent before a restart from U
+  int it_done;                // the last iteration run
+  bool use_guess;
+};
+
+// Deferral hook of eh_column: none (every column finishes its solve where
+// it started). A deferring hook has kEnabled, `at` (the first iteration
+// after which an unconverged column may leave; 0: never) and
+// bool operator()(const EHBuffers&, int n, const EHNewtonCtx&), which saves
+// the column and returns true, or returns false (the column carries on).
+struct NoDefer {
+  static constexpr bool kEnabled = false;
+  int at = 0;
+  template <class B, class X>
+  CLM_HD bool operator()(const B&, int, const X&) const { return false; }
+};
+
 // Explicit sources and top boundaries compiled into a step kernel.
 constexpr int kSrcNone = 0;
 constexpr int kSrcRoots = 1;  // RootExtraction (A.rx)
@@ -234,12 +264,20 @@ constexpr int kNewtonRuntime = 2;
 // Geom: ColGeom (uniform layers) or ColGeomS (per-layer geometry); G holds
 // the column's. On a uniform column rdz(k) = dt / dz and the face means
 // 0.5 (a + b) / dz are exactly (a + b) hinv_gap(k).
+// Defer / kResume (tolerance mode, one step per call): with a deferring
+// hook, a column that has not converged after iteration defer.at is saved
+// (arrays through the hook, the rest as an EHNewtonCtx) and left without its
+// final combination; kResume runs such a column from its saved context
+// (*resume) to the end of the step. The two launches run the same
+// arithmetic in the same order as one uninterrupted solve.
 template <typename JT, class CM, bool kLogKappaHere = false, int kSrc = kSrcNone,
-          int kNewton = kNewtonRuntime, class Geom = ColGeom>
+          int kNewton = kNewtonRuntime, class Geom = ColGeom, class Defer = NoDefer,
+          bool kResume = false>
 CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int orig,
                       const EHBuffers& B, const EHJac<JT>& J, const Geom& G, double t0,
                       double dt, int nsteps, double& Fw, double& Fe, uint32_t& flags,
-                      int& iters_done) {
+                      int& iters_done, const Defer& defer = Defer{},
+                      const EHNewtonCtx* resume = nullptr) {
   const Earth& E = A.E;
   const EHScalars& sc = A.sc;
   const EHCol<CM> c = load_eh_col<CM, kLogKappaHere>(A, Tb, s, n);
@@ -261,6 +299,18 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
 
   bool finite = true;  // the last step's state, checked as it is stored
   for (int step = 0; step < nsteps; ++step) {
+    EHNewtonCtx X;
+    bool& use_guess = X.use_guess;
+    double& pred2 = X.pred2;
+    double &Ftw = X.Ftw, &Fth = X.Fth, &Fbw = X.Fbw, &Fbh = X.Fbh;
+    double &UFw = X.UFw, &UFe = X.UFe, &xFw = X.xFw, &xFe = X.xFe;
+    double &prev_norm = X.prev_norm, &prev_state2 = X.prev_state2;
+    int& it_start = X.it_start;
+    int it_first = 1;
+    if constexpr (kResume) {
+      X = *resume;
+      it_first = X.it_done + 1;
+    } else {
     const double t = t0 + step * dt;
     // Newton guess (tolerance mode only): Newton starts from u_n + a guessed
     // increment instead of U -- the learned guess's (guess_v, guess_e) or the
@@ -269,9 +319,9 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
     // wrong guess; one a little worse than U still converges about as fast,
     // while a restart costs the whole warp an iteration)
     const bool extrap = B.prev_v.p != nullptr && tol;
-    bool use_guess = extrap || (B.guess_v.p != nullptr && tol && isfinite(B.guess_v[0]) &&
-                                isfinite(B.guess_e[0]));
-    double pred2 = 0.0;
+    use_guess = extrap || (B.guess_v.p != nullptr && tol && isfinite(B.guess_v[0]) &&
+                           isfinite(B.guess_e[0]));
+    pred2 = 0.0;
     // ---------------- stage 1: aux at Y_n, explicit tendency, U ----------
     double K0 = 0, T0 = 0, kap0 = 0, psi0 = 0;
     double Kt = 0, Tt = 0, kapt = 0, psit = 0;
@@ -476,7 +526,6 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       }
     }
     // boundary fluxes at t, frozen through the Newton solve
-    double Ftw, Fth, Fbw, Fbh;
     {
       const double ftw = forcing_value(A.forc[CLM_BC_TOP_WATER], st, s, A.col0 + orig, t, A.seed);
       const double fth = forcing_value(A.forc[CLM_BC_TOP_HEAT], st, s, A.col0 + orig, t, A.seed);
@@ -519,17 +568,22 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         Fbh = fbh;
       }
     }
-    const double UFw = kRoots ? Fw + dt * root_w : kAtmos ? Fw + dt * (0.0 + -ab.vice) : Fw;
-    const double UFe = kRoots ? Fe + dt * root_e : Fe;
-    double xFw = UFw, xFe = UFe;
+    UFw = kRoots ? Fw + dt * root_w : kAtmos ? Fw + dt * (0.0 + -ab.vice) : Fw;
+    UFe = kRoots ? Fe + dt * root_e : Fe;
+    xFw = UFw;
+    xFe = UFe;
+    X.R_ss = ro.R_ss;
+    X.R_ess = ro.R_ess;
 
     // ---------------- stage 2: Newton ------------------------------------
-    double prev_norm = 1e300;
+    prev_norm = 1e300;
     // a guess that moved no layer off U is no guess: plain start, plain test
     if (use_guess && !(pred2 > 0.0)) use_guess = false;
-    double prev_state2 = 0.0;  // the state increments' norm of the last iteration (guess test)
-    int it_start = 0;          // iterations spent before a restart from U
-    for (int it = 1; it <= A.max_iters; ++it) {
+    prev_state2 = 0.0;  // the state increments' norm of the last iteration (guess test)
+    it_start = 0;       // iterations spent before a restart from U
+    }  // !kResume
+    bool deferred = false;
+    for (int it = it_first; it <= A.max_iters; ++it) {
       // sweep 1 (bottom -> top)
       JT cp_prev = 0, dp_prev = 0;
       JT U_prev = 0, sp_prev = -1, piv_prev = -1;  // mixed: reduced column sums
@@ -621,8 +675,8 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         Tc = Tn; psic = psin; Dc = Dn; Kc = Kn; relKc = relKn;
       }
       // integrated fluxes (their Jacobian block is -I): x += f
-      const double fFw = UFw + dt * ((-(Ftw - Fbw)) - ro.R_ss) - xFw;
-      const double fFe = UFe + dt * ((-(Fth - Fbh)) - ro.R_ess) - xFe;
+      const double fFw = UFw + dt * ((-(Ftw - Fbw)) - X.R_ss) - xFw;
+      const double fFe = UFe + dt * ((-(Fth - Fbh)) - X.R_ess) - xFe;
       xFw += fFw;
       xFe += fFe;
       // sweep 2 (top -> bottom): delta vartheta into dp
@@ -784,6 +838,16 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
           flags |= CLM_COL_GUESS_FALLBACK;
           prev_norm = 1e300;
           it_start = it;
+          // split Newton: the restart from U runs in the resuming launch
+          if constexpr (Defer::kEnabled) {
+            if (defer.at > 0 && it >= defer.at && it < A.max_iters) {
+              X.it_done = it;
+              if (defer(B, n, X)) {
+                deferred = true;
+                break;
+              }
+            }
+          }
           continue;
         }
         prev_state2 = state2;
@@ -795,22 +859,36 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         const double conv = (use_guess && it == 1) ? sqrt(state2) : nrm;
         if (conv < A.tol) break;
         if (it == A.max_iters) flags |= CLM_COL_NOT_CONVERGED;
+        // split Newton: an unconverged column leaves after iteration
+        // defer.at (or the first one after it that ends in this test) with
+        // its context saved; it finishes in the resuming launch
+        if constexpr (Defer::kEnabled) {
+          if (defer.at > 0 && it >= defer.at && it < A.max_iters) {
+            X.it_done = it;
+            if (defer(B, n, X)) {
+              deferred = true;
+              break;
+            }
+          }
+        }
       }
     }
+    if (deferred) break;  // one step per call with a deferring hook
     // ---------------- final combination ---------------------------------
     const double inv_dt = 1.0 / dt;
     const bool last = step == nsteps - 1;
+    const Col<double> OV = kResume ? B.ov : B.gv, OE = kResume ? B.oe : B.ge;
     for (int k = 0; k < n; ++k) {
       const double Uv = B.gv[k], Ue = B.ge[k];
       const double v = Uv + dt * ((B.xv[k] - Uv) * inv_dt);
       const double e = Ue + dt * ((B.xe[k] - Ue) * inv_dt);
       if (last) {
-        B.gv.store_last(k, v);
-        B.ge.store_last(k, e);
+        OV.store_last(k, v);
+        OE.store_last(k, e);
         finite = finite && isfinite(v) && isfinite(B.gti[k]) && isfinite(e);
       } else {
-        B.gv[k] = v;
-        B.ge[k] = e;
+        OV[k] = v;
+        OE[k] = e;
       }
     }
     Fw = UFw + dt * ((xFw - UFw) * inv_dt);

@@ -41,6 +41,16 @@ struct XFields {
   int nf;
 };
 
+// Split Newton (tolerance mode, EnergyHydrology): the columns that have not
+// converged after the first iterations of a step, saved by the step kernel
+// for the resuming kernel (clm_step_kernels.cuh has the entry layout).
+struct SplitQueue {
+  double* q = nullptr;   // entries (arrays and scalars), null: no split
+  int* count = nullptr;  // entries written this step (zeroed before the step kernel)
+  int cap = 0;           // capacity in entries, a multiple of 32
+  int nmax = 0;          // layers per entry array
+};
+
 struct StepArgs {
   Layout L;
   const double* z_lo;   // [stride]
@@ -83,6 +93,10 @@ struct StepArgs {
   int64_t col0 = 0;     // global index of column 0 (rain-pulse hash)
   int tile_begin = 0;   // the launch's tiles: [tile_begin, tile_end)
   int tile_end = -1;    // -1: through the last tile
+  // split Newton: columns unconverged after iteration split_at go to
+  // split.q (one-step launches of the tolerance-mode step kernel only)
+  SplitQueue split;
+  int split_at = 0;
 };
 
 // The column's geometry: uniform layers from z_lo, z_hi, or the per-layer

@@ -16,6 +16,13 @@ void launch_step_vg(const StepArgs& A, int model, int precision, int grid, dim3 
   launch_step_t<VG, false>(A, model, precision, grid, block, smem, scratch, clk, nsteps, stream);
 }
 
+void* resume_fn_vg(int precision) { return resume_fn_t<VG, false>(precision); }
+
+void launch_resume_vg(const StepArgs& A, int precision, int grid, dim3 block, size_t smem,
+                      const StepClock& clk, cudaStream_t stream) {
+  launch_resume_t<VG, false>(A, precision, grid, block, smem, clk, stream);
+}
+
 // ---------------------------------------------------------------------------
 // launch configuration
 // ---------------------------------------------------------------------------
@@ -63,6 +70,55 @@ cudaError_t step_grid(int model, int precision, int cm, bool str, bool tol, int 
   const int need = (ntiles + wpc - 1) / wpc;
   *grid = per_sm * nsm < need ? per_sm * nsm : need;
   return cudaSuccess;
+}
+
+// Split Newton's resuming kernel: its shared memory (tables and Thomas
+// arrays) and the attribute that allows it; the queue's size in doubles.
+size_t resume_smem_bytes(int precision, int nmax, int wpc) {
+  const bool mx = precision == CLM_PREC_MIXED;
+  const size_t per_layer = mx ? eh_resume_smem_per_layer<float>() : eh_resume_smem_per_layer<double>();
+  const int tab = mx ? fm::stage_doubles<true>() : fm::stage_doubles<false>();
+  return tab * sizeof(double) + per_layer * (size_t)nmax * kTile * wpc;
+}
+
+static void* resume_fn(int precision, int cm, bool str) {
+  if (cm == CLM_CM_BROOKS_COREY) return str ? resume_fn_bc_s(precision) : resume_fn_bc(precision);
+  return str ? resume_fn_vg_s(precision) : resume_fn_vg(precision);
+}
+
+// The attribute covers the largest CTA (up to wpc warps) whose shared memory
+// the device offers, as the step kernel's launch shapes do.
+cudaError_t resume_setup(int precision, int cm, bool str, int nmax, int wpc) {
+  int dev = 0, cap = 0;
+  cudaError_t err;
+  if ((err = cudaGetDevice(&dev)) != cudaSuccess) return err;
+  if ((err = cudaDeviceGetAttribute(&cap, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) != cudaSuccess)
+    return err;
+  size_t bytes = resume_smem_bytes(precision, nmax, 1);
+  for (int w = wpc; w >= 1; --w)
+    if (resume_smem_bytes(precision, nmax, w) <= (size_t)cap) {
+      bytes = resume_smem_bytes(precision, nmax, w);
+      break;
+    }
+  return cudaFuncSetAttribute(resume_fn(precision, cm, str), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)bytes);
+}
+
+size_t split_queue_doubles(int cap, int nmax) { return (size_t)queue_doubles(cap, nmax); }
+
+cudaError_t launch_resume(const StepArgs& A, int precision, int wpc, int grid, const StepClock& clk,
+                          cudaStream_t stream) {
+  const size_t smem = resume_smem_bytes(precision, A.L.nmax, wpc);
+  const dim3 block(32 * wpc);
+  const bool str = A.geo.z != nullptr;
+  if (A.cm == CLM_CM_BROOKS_COREY) {
+    if (str) launch_resume_bc_s(A, precision, grid, block, smem, clk, stream);
+    else launch_resume_bc(A, precision, grid, block, smem, clk, stream);
+  } else {
+    if (str) launch_resume_vg_s(A, precision, grid, block, smem, clk, stream);
+    else launch_resume_vg(A, precision, grid, block, smem, clk, stream);
+  }
+  return cudaGetLastError();
 }
 
 size_t step_scratch_doubles(int model, int precision, int nmax, int wpc, int grid) {

@@ -15,4 +15,11 @@ void launch_step_bc(const StepArgs& A, int model, int precision, int grid, dim3 
   launch_step_t<BC, false>(A, model, precision, grid, block, smem, scratch, clk, nsteps, stream);
 }
 
+void* resume_fn_bc(int precision) { return resume_fn_t<BC, false>(precision); }
+
+void launch_resume_bc(const StepArgs& A, int precision, int grid, dim3 block, size_t smem,
+                      const StepClock& clk, cudaStream_t stream) {
+  launch_resume_t<BC, false>(A, precision, grid, block, smem, clk, stream);
+}
+
 }  // namespace clm

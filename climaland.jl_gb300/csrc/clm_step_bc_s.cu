@@ -14,4 +14,11 @@ void launch_step_bc_s(const StepArgs& A, int model, int precision, int grid, dim
   launch_step_t<BC, true>(A, model, precision, grid, block, smem, scratch, clk, nsteps, stream);
 }
 
+void* resume_fn_bc_s(int precision) { return resume_fn_t<BC, true>(precision); }
+
+void launch_resume_bc_s(const StepArgs& A, int precision, int grid, dim3 block, size_t smem,
+                        const StepClock& clk, cudaStream_t stream) {
+  launch_resume_t<BC, true>(A, precision, grid, block, smem, clk, stream);
+}
+
 }  // namespace clm

@@ -47,6 +47,123 @@ __host__ __device__ constexpr size_t richards_smem_per_layer() {
 // energy residual.
 __host__ __device__ constexpr int eh_scratch_slots(bool mixed) { return mixed ? 6 : 7; }
 
+// Split Newton queue. Entry e belongs to group e / 32 (one resuming warp,
+// lane e % 32); a group is one contiguous block of kQArrays arrays of
+// nmax x 32 doubles ([array][layer][lane], so that a warp's access to one
+// layer is one 256-byte segment) followed by the scalars [kQScalars][32], so
+// that one bulk prefetch brings a group into L2.
+// Arrays: the stage value U (vartheta_l, theta_i, rho_e_int), the iterate,
+// K, the face conductances kappa / dz and K / dz, two slots of aux (FP64:
+// 1 / rho c and the saturation reciprocal; mixed: the floats 1 / rho c,
+// dt K_face / dz^2, dt kappa_face / dz^2 and the energy-advection face
+// coefficient), and the per-iteration energy residual and (FP64) advection
+// face coefficient of the resumed solve.
+constexpr int kQArrays = 12;
+enum QueueArray { kQUv, kQUti, kQUe, kQXv, kQXe, kQK, kQKap, kQAw, kQAux0, kQAux1, kQFe, kQAe };
+enum QueueScalar {
+  kQsSlot, kQsFtw, kQsFth, kQsFbw, kQsFbh, kQsUFw, kQsUFe, kQsXFw, kQsXFe, kQsRss, kQsRess,
+  kQsPrevNorm, kQsPrevState2, kQsPred2, kQsItStart, kQsItDone, kQsUseGuess, kQScalars
+};
+
+__host__ __device__ inline int64_t queue_doubles(int cap, int nmax) {
+  return (int64_t)cap * ((int64_t)kQArrays * nmax + kQScalars);
+}
+
+struct QueueView {
+  SplitQueue Q;
+  __device__ int64_t lay() const { return (int64_t)Q.nmax * kTile; }
+  // doubles per group block (a multiple of 32: 256-byte aligned blocks)
+  __device__ int64_t block() const { return (int64_t)kQArrays * lay() + kQScalars * kTile; }
+  __device__ double* group(int g) const { return Q.q + (int64_t)g * block(); }
+  __device__ double* arr0(int e, int a) const { return group(e / kTile) + a * lay() + e % kTile; }
+  __device__ Col<double> arr(int e, int a) const { return Col<double>{arr0(e, a), kTile}; }
+  // the four float arrays of the mixed path's aux slots
+  __device__ Col<float> farr(int e, int j) const {
+    return Col<float>{reinterpret_cast<float*>(group(e / kTile) + kQAux0 * lay()) + j * lay() + e % kTile,
+                      kTile};
+  }
+  __device__ double& scal(int e, int f) const {
+    return group(e / kTile)[kQArrays * lay() + f * kTile + e % kTile];
+  }
+  // Bulk L2 prefetch of group g's block (TMA engine, no registers or shared
+  // memory involved): lanes 0.. each issue one 16 KB piece. Every byte lies
+  // inside the queue (g < cap / 32); sizes are multiples of 256 bytes.
+  __device__ void prefetch_group(int g, int lane) const {
+    const int64_t bytes = block() * (int64_t)sizeof(double);
+    constexpr int64_t kPiece = 16384;
+    const int64_t off = (int64_t)lane * kPiece;
+    if (off < bytes) {
+      const int64_t sz = bytes - off < kPiece ? bytes - off : kPiece;
+      const char* p = reinterpret_cast<const char*>(group(g)) + off;
+      asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"((unsigned)sz) : "memory");
+    }
+  }
+};
+
+// The step kernel's deferring hook: claims an entry (one atomic per group of
+// lanes that defer together) and copies the column's arrays and context.
+template <typename JT>
+struct QueueDefer {
+  static constexpr bool kEnabled = true;
+  int at;
+  QueueView V;
+  int s;
+  __device__ bool operator()(const EHBuffers& B, int n, const EHNewtonCtx& X) const {
+    constexpr bool kMixed = sizeof(JT) < sizeof(double);
+    const unsigned m = __activemask();
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(V.Q.count, __popc(m));
+    base = __shfl_sync(m, base, leader);
+    const int e = base + __popc(m & ((1u << lane) - 1u));
+    if (e >= V.Q.cap) return false;  // no room: the column finishes here
+    const Col<double> uv = V.arr(e, kQUv), uti = V.arr(e, kQUti), ue = V.arr(e, kQUe);
+    const Col<double> xv = V.arr(e, kQXv), xe = V.arr(e, kQXe), K = V.arr(e, kQK);
+    const Col<double> kap = V.arr(e, kQKap), aw = V.arr(e, kQAw);
+    for (int k = 0; k < n; ++k) {
+      uv[k] = B.gv[k];
+      uti[k] = B.gti[k];
+      ue[k] = B.ge[k];
+      xv[k] = B.xv[k];
+      xe[k] = B.xe[k];
+      K[k] = B.K[k];
+      if constexpr (kMixed) {
+        V.farr(e, 0)[k] = B.ircf[k];
+      } else {
+        V.arr(e, kQAux0)[k] = B.irc[k];
+        V.arr(e, kQAux1)[k] = B.iden[k];
+      }
+    }
+    for (int k = 0; k < n - 1; ++k) {  // faces k|k+1
+      kap[k] = B.kap[k];
+      aw[k] = B.aw[k];
+      if constexpr (kMixed) {
+        V.farr(e, 1)[k] = B.awr[k];
+        V.farr(e, 2)[k] = B.akr[k];
+      }
+    }
+    V.scal(e, kQsSlot) = s;
+    V.scal(e, kQsFtw) = X.Ftw;
+    V.scal(e, kQsFth) = X.Fth;
+    V.scal(e, kQsFbw) = X.Fbw;
+    V.scal(e, kQsFbh) = X.Fbh;
+    V.scal(e, kQsUFw) = X.UFw;
+    V.scal(e, kQsUFe) = X.UFe;
+    V.scal(e, kQsXFw) = X.xFw;
+    V.scal(e, kQsXFe) = X.xFe;
+    V.scal(e, kQsRss) = X.R_ss;
+    V.scal(e, kQsRess) = X.R_ess;
+    V.scal(e, kQsPrevNorm) = X.prev_norm;
+    V.scal(e, kQsPrevState2) = X.prev_state2;
+    V.scal(e, kQsPred2) = X.pred2;
+    V.scal(e, kQsItStart) = X.it_start;
+    V.scal(e, kQsItDone) = X.it_done;
+    V.scal(e, kQsUseGuess) = X.use_guess ? 1.0 : 0.0;
+    return true;
+  }
+};
+
 // kSrc: the RootExtraction source (A.rx) or the atmosphere-driven top
 // boundary (A.atm) compiled in; separate kernels so that their registers do
 // not weigh on the step without them. kStr: per-layer geometry. kTol: the
@@ -122,8 +239,16 @@ __global__ void __launch_bounds__(128, 1)
       uint32_t flags = 0;
       int iters = 0;
       const auto G = GeomOf<kStr>::make(A, base, s, n);
-      eh_column<JT, CM, false, kSrc, kTol ? kNewtonTol : kNewtonFixed>(A, Tb, s, n, A.L.perm[s], B, J, G,
-                                                                       t0, dt, nsteps, Fw, Fe, flags, iters);
+      if constexpr (kTol) {
+        // split Newton: one-step launches with a queue defer their
+        // unconverged columns after iteration split_at
+        const QueueDefer<JT> D{(A.split.q && nsteps == 1) ? A.split_at : 0, QueueView{A.split}, s};
+        eh_column<JT, CM, false, kSrc, kNewtonTol, typename GeomOf<kStr>::type, QueueDefer<JT>>(
+            A, Tb, s, n, A.L.perm[s], B, J, G, t0, dt, nsteps, Fw, Fe, flags, iters, D);
+      } else {
+        eh_column<JT, CM, false, kSrc, kNewtonFixed>(A, Tb, s, n, A.L.perm[s], B, J, G, t0, dt, nsteps, Fw,
+                                                     Fe, flags, iters);
+      }
       A.Fw[s] = Fw;
       A.Fe[s] = Fe;
       A.flags[s] |= flags;  // cleared at the start of each step call
@@ -132,6 +257,109 @@ __global__ void __launch_bounds__(128, 1)
     tile = dyn ? A.tile_begin + claim_tile(A.tile_ctr) : tile + nwarps;
   }
   if (dyn) release_tiles(A.tile_ctr, nwarps);
+}
+
+// Split Newton, second launch: the queued columns, 32 to a warp in the order
+// they were saved, from their saved context to the end of the step (the
+// explicit source and top-boundary variants differ only before the Newton
+// solve, so one kernel serves them all). Shared memory: the tables and the
+// Thomas arrays of each warp; the iterate, U and the aux stay in the entry.
+template <typename JT>
+__host__ __device__ constexpr size_t eh_resume_smem_per_layer() {
+  return eh_smem_per_layer<JT>();  // as the step kernel: xv, xe | cp, dp, d
+}
+
+template <typename JT, class CM, bool kStr>
+__global__ void __launch_bounds__(128, 1) eh_resume_kernel(StepArgs A, StepClock clk) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* tab = reinterpret_cast<double*>(smem_raw);
+  constexpr bool kMixed = sizeof(JT) < sizeof(double);
+  constexpr int kTab = fm::stage_doubles<kMixed>();
+  const Tables Tb = fm::stage_tables<kMixed>(tab);
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int wpc = blockDim.x >> 5;
+  const int64_t lay = (int64_t)A.L.nmax * kTile;
+  double* dw = tab + kTab + (int64_t)warp * 2 * lay;
+  JT* jw = reinterpret_cast<JT*>(tab + kTab + (int64_t)wpc * 2 * lay) + (int64_t)warp * 3 * lay;
+  EHJac<JT> J;
+  J.cp = Col<JT>{jw + lane, kTile};
+  J.dp = Col<JT>{jw + lay + lane, kTile};
+  J.d = Col<JT>{jw + 2 * lay + lane, kTile};
+  const QueueView V{A.split};
+  const int count = min(*A.split.count, A.split.cap);
+  const int ngroups = (count + kTile - 1) / kTile;
+  const double t0 = clk.start(), dt = clk.step();
+  const int nw = gridDim.x * wpc;
+  int grp = blockIdx.x * wpc + warp;
+  if (grp < ngroups) V.prefetch_group(grp, lane);
+  for (; grp < ngroups; grp += nw) {
+    // the warp's next group comes into L2 while this one runs
+    if (grp + nw < ngroups) V.prefetch_group(grp + nw, lane);
+    const int e = grp * kTile + lane;
+    if (e >= count) continue;  // the column code has no warp collectives
+    const int s = (int)V.scal(e, kQsSlot);
+    const int n = A.L.col_n[s];
+    const int64_t base = A.L.tile_off[s / kTile] + s % kTile;
+    EHBuffers B;
+    B.gv = V.arr(e, kQUv);
+    B.gti = V.arr(e, kQUti);
+    B.ge = V.arr(e, kQUe);
+    // the iterate in shared memory, as in the step kernel
+    B.xv = Col<double>{dw + lane, kTile};
+    B.xe = Col<double>{dw + lay + lane, kTile};
+    {
+      const Col<double> qv = V.arr(e, kQXv), qe = V.arr(e, kQXe);
+      for (int k = 0; k < n; ++k) {
+        B.xv[k] = qv[k];
+        B.xe[k] = qe[k];
+      }
+    }
+    B.K = V.arr(e, kQK);
+    B.kap = V.arr(e, kQKap);
+    B.aw = V.arr(e, kQAw);
+    B.fe = V.arr(e, kQFe);
+    if constexpr (kMixed) {
+      B.ircf = V.farr(e, 0);
+      B.awr = V.farr(e, 1);
+      B.akr = V.farr(e, 2);
+      J.ae = Col<JT>{reinterpret_cast<JT*>(V.farr(e, 3).p), kTile};
+    } else {
+      B.irc = V.arr(e, kQAux0);
+      B.iden = V.arr(e, kQAux1);
+      J.ae = Col<JT>{reinterpret_cast<JT*>(V.arr0(e, kQAe)), kTile};
+    }
+    B.ov = Col<double>{A.v + base, kTile};
+    B.oe = Col<double>{A.e + base, kTile};
+    EHNewtonCtx X;
+    X.Ftw = V.scal(e, kQsFtw);
+    X.Fth = V.scal(e, kQsFth);
+    X.Fbw = V.scal(e, kQsFbw);
+    X.Fbh = V.scal(e, kQsFbh);
+    X.UFw = V.scal(e, kQsUFw);
+    X.UFe = V.scal(e, kQsUFe);
+    X.xFw = V.scal(e, kQsXFw);
+    X.xFe = V.scal(e, kQsXFe);
+    X.R_ss = V.scal(e, kQsRss);
+    X.R_ess = V.scal(e, kQsRess);
+    X.prev_norm = V.scal(e, kQsPrevNorm);
+    X.prev_state2 = V.scal(e, kQsPrevState2);
+    X.pred2 = V.scal(e, kQsPred2);
+    X.it_start = (int)V.scal(e, kQsItStart);
+    X.it_done = (int)V.scal(e, kQsItDone);
+    X.use_guess = V.scal(e, kQsUseGuess) != 0.0;
+    double Fw = A.Fw[s], Fe = A.Fe[s];
+    uint32_t flags = 0;
+    int iters = 0;
+    const auto G = GeomOf<kStr>::make(A, base, s, n);
+    eh_column<JT, CM, false, kSrcNone, kNewtonTol, typename GeomOf<kStr>::type, NoDefer, true>(
+        A, Tb, s, n, A.L.perm[s], B, J, G, t0, dt, 1, Fw, Fe, flags, iters, NoDefer{}, &X);
+    A.Fw[s] = Fw;
+    A.Fe[s] = Fe;
+    A.flags[s] |= flags;
+    A.iters[s] = iters;
+  }
 }
 
 template <typename JT, class CM, bool kStr>
@@ -251,6 +479,21 @@ void launch_step_t(const StepArgs& A, int model, int precision, int grid, dim3 b
   }
 }
 
+template <class CM, bool kStr>
+void* resume_fn_t(int precision) {
+  return precision == CLM_PREC_MIXED ? (void*)eh_resume_kernel<float, CM, kStr>
+                                     : (void*)eh_resume_kernel<double, CM, kStr>;
+}
+
+template <class CM, bool kStr>
+void launch_resume_t(const StepArgs& A, int precision, int grid, dim3 block, size_t smem,
+                     const StepClock& clk, cudaStream_t stream) {
+  if (precision == CLM_PREC_MIXED)
+    eh_resume_kernel<float, CM, kStr><<<grid, block, smem, stream>>>(A, clk);
+  else
+    eh_resume_kernel<double, CM, kStr><<<grid, block, smem, stream>>>(A, clk);
+}
+
 // One translation unit per (closure, geometry) instantiates these: the entry
 // points each defines (clm_step.cu, clm_step_bc.cu, clm_step_s.cu,
 // clm_step_bc_s.cu).
@@ -266,5 +509,17 @@ void launch_step_vg_s(const StepArgs& A, int model, int precision, int grid, dim
                       double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream);
 void launch_step_bc_s(const StepArgs& A, int model, int precision, int grid, dim3 block, size_t smem,
                       double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream);
+void* resume_fn_vg(int precision);
+void* resume_fn_bc(int precision);
+void* resume_fn_vg_s(int precision);
+void* resume_fn_bc_s(int precision);
+void launch_resume_vg(const StepArgs& A, int precision, int grid, dim3 block, size_t smem,
+                      const StepClock& clk, cudaStream_t stream);
+void launch_resume_bc(const StepArgs& A, int precision, int grid, dim3 block, size_t smem,
+                      const StepClock& clk, cudaStream_t stream);
+void launch_resume_vg_s(const StepArgs& A, int precision, int grid, dim3 block, size_t smem,
+                        const StepClock& clk, cudaStream_t stream);
+void launch_resume_bc_s(const StepArgs& A, int precision, int grid, dim3 block, size_t smem,
+                        const StepClock& clk, cudaStream_t stream);
 
 }  // namespace clm

@@ -15,4 +15,11 @@ void launch_step_vg_s(const StepArgs& A, int model, int precision, int grid, dim
   launch_step_t<VG, true>(A, model, precision, grid, block, smem, scratch, clk, nsteps, stream);
 }
 
+void* resume_fn_vg_s(int precision) { return resume_fn_t<VG, true>(precision); }
+
+void launch_resume_vg_s(const StepArgs& A, int precision, int grid, dim3 block, size_t smem,
+                        const StepClock& clk, cudaStream_t stream) {
+  launch_resume_t<VG, true>(A, precision, grid, block, smem, clk, stream);
+}
+
 }  // namespace clm

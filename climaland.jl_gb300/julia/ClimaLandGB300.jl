@@ -25,6 +25,10 @@ const CLM_NEWTON_TOL = Int32(1)
 const CLM_GUESS_NONE = Int32(0)
 const CLM_GUESS_NETWORK = Int32(1)
 const CLM_GUESS_EXTRAPOLATE = Int32(2)
+const CLM_TOL_TILES = Int32(0)
+const CLM_TOL_REGROUP = Int32(1)
+const CLM_TOL_SPLIT = Int32(2)
+const CLM_TOL_AUTO = Int32(3)
 const CLM_BC_FLUX = Int32(0)
 const CLM_BC_FREE_DRAINAGE = Int32(1)
 const CLM_BC_STATE = Int32(2)

@@ -84,6 +84,26 @@ enum clm_schedule {
   CLM_SCHED_DYNAMIC = 1  /* warps claim the next tile from an atomic counter */
 };
 
+/* How tolerance-mode Newton maps columns to warps (clm_config.tol_regroup;
+ * no reference counterpart: a scheduling choice). A warp runs its 32
+ * columns in lockstep, as many iterations as its slowest column needs.
+ * Results do not depend on the choice (the same arithmetic per column). */
+enum clm_tol_schedule {
+  CLM_TOL_TILES = 0,    /* the depth-sorted tiles                           */
+  CLM_TOL_REGROUP = 1,  /* slots re-sorted after every step by the column's
+                           last iteration count (without a Newton guess;
+                           with one, the tiles)                             */
+  CLM_TOL_SPLIT = 2,    /* EnergyHydrology: every step is two launches; the
+                           first runs every column through two iterations,
+                           the second finishes the columns that have not
+                           converged, packed 32 to a warp in a queue the
+                           handle keeps (about 96 n + 136 bytes per column
+                           of n layers); RichardsModel: the tiles           */
+  CLM_TOL_AUTO = 3      /* (default) CLM_TOL_REGROUP for FP64 without a
+                           Newton guess and for RichardsModel, otherwise
+                           CLM_TOL_SPLIT (each measured the faster there)   */
+};
+
 /* Boundary-condition kinds (src/standalone/Soil/boundary_conditions.jl). */
 enum clm_bc_kind {
   CLM_BC_FLUX = 0,            /* WaterFluxBC / HeatFluxBC: F = f(t)        */
@@ -384,14 +404,13 @@ typedef struct clm_config {
                              rain-pulse hash uses the global column index  */
   int32_t host_chunks;    /* clm_step_host pipeline depth (0: by size)      */
   int32_t runoff;         /* enum clm_runoff (CLM_BC_PRECIP_RUNOFF)         */
-  int32_t tol_regroup;    /* tolerance mode: 1 (default) groups columns into
-                             warps by their last Newton iteration count each
-                             step (a warp runs as many iterations as its
-                             slowest column); 0 keeps the depth-sorted tiles.
-                             With a Newton guess (learned_guess != 0) the
-                             tiles are kept either way: the guess makes the
-                             last count a poor predictor and the regrouped
-                             warps' scattered loads cost more than they save.
+  int32_t tol_regroup;    /* enum clm_tol_schedule: how tolerance-mode
+                             Newton maps columns to warps (default
+                             CLM_TOL_AUTO). CLM_TOL_REGROUP keeps the
+                             depth-sorted tiles when a Newton guess is set
+                             (learned_guess != 0): the guess makes the last
+                             count a poor predictor and the regrouped warps'
+                             scattered loads cost more than they save.
                              Results do not depend on it                    */
   int32_t pad1;
 } clm_config;

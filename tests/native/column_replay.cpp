@@ -22,6 +22,55 @@ using namespace clm;
 
 namespace {
 
+// Split Newton emulation (clmr_set_split): iteration after which an
+// unconverged column is saved and resumed from its saved context with fresh
+// per-iteration arrays (0: one uninterrupted solve).
+int g_split_at = 0;
+
+// What the step kernel's deferring hook saves to the queue.
+struct Saved {
+  std::vector<double> uv, uti, ue, xv, xe, K, kap, aw, irc, iden;
+  std::vector<float> ircf, awr, akr;
+  EHNewtonCtx X{};
+  bool done = false;
+};
+
+struct HostDefer {
+  static constexpr bool kEnabled = true;
+  int at;
+  Saved* sv;
+  bool mixed;
+  bool operator()(const EHBuffers& B, int n, const EHNewtonCtx& X) const {
+    auto take = [n](const Col<double>& c, std::vector<double>& out, int m) {
+      out.assign(n, 0.0);
+      for (int k = 0; k < m; ++k) out[k] = c[k];
+    };
+    auto takef = [n](const Col<float>& c, std::vector<float>& out, int m) {
+      out.assign(n, 0.0f);
+      for (int k = 0; k < m; ++k) out[k] = c[k];
+    };
+    take(B.gv, sv->uv, n);
+    take(B.gti, sv->uti, n);
+    take(B.ge, sv->ue, n);
+    take(B.xv, sv->xv, n);
+    take(B.xe, sv->xe, n);
+    take(B.K, sv->K, n);
+    take(B.kap, sv->kap, n - 1);
+    take(B.aw, sv->aw, n - 1);
+    if (mixed) {
+      takef(B.ircf, sv->ircf, n);
+      takef(B.awr, sv->awr, n - 1);
+      takef(B.akr, sv->akr, n - 1);
+    } else {
+      take(B.irc, sv->irc, n);
+      take(B.iden, sv->iden, n);
+    }
+    sv->X = X;
+    sv->done = true;
+    return true;
+  }
+};
+
 template <typename JT, class CM, int kSrc, class Geom>
 void eh_one(const StepArgs& A, const Tables& Tb, int c, int n, double* v, double* ti, double* e,
             const float* gv, const float* ge, double* pv, double* pe, const Geom& G, double t, double dt, int nsteps,
@@ -61,7 +110,48 @@ void eh_one(const StepArgs& A, const Tables& Tb, int c, int n, double* v, double
     B.prev_v = Col<double>{pv, 1};
     B.prev_e = Col<double>{pe, 1};
   }
-  eh_column<JT, CM, false, kSrc>(A, Tb, c, n, c, B, J, G, t, dt, nsteps, Fw, Fe, fl, it);
+  if (!(g_split_at > 0 && nsteps == 1 && A.newton_mode == CLM_NEWTON_TOL)) {
+    eh_column<JT, CM, false, kSrc>(A, Tb, c, n, c, B, J, G, t, dt, nsteps, Fw, Fe, fl, it);
+    return;
+  }
+  Saved sv;
+  eh_column<JT, CM, false, kSrc, kNewtonRuntime, Geom, HostDefer>(A, Tb, c, n, c, B, J, G, t, dt, 1, Fw, Fe,
+                                                                   fl, it, HostDefer{g_split_at, &sv, mixed});
+  if (!sv.done) return;
+  // resume from the saved arrays and context only: the per-iteration arrays
+  // start as NaN, so that anything the save left out shows in the result
+  const double qnan = std::nan("");
+  std::vector<double> fe2(n, qnan);
+  std::vector<JT> cp2(n, (JT)qnan), dp2(n, (JT)qnan), d2(n, (JT)qnan), ae2(n, (JT)qnan);
+  EHBuffers R;
+  R.gv = Col<double>{sv.uv.data(), 1};
+  R.gti = Col<double>{sv.uti.data(), 1};
+  R.ge = Col<double>{sv.ue.data(), 1};
+  R.xv = Col<double>{sv.xv.data(), 1};
+  R.xe = Col<double>{sv.xe.data(), 1};
+  R.fe = Col<double>{fe2.data(), 1};
+  R.K = Col<double>{sv.K.data(), 1};
+  R.kap = Col<double>{sv.kap.data(), 1};
+  R.aw = Col<double>{sv.aw.data(), 1};
+  if (mixed) {
+    R.ircf = Col<float>{sv.ircf.data(), 1};
+    R.awr = Col<float>{sv.awr.data(), 1};
+    R.akr = Col<float>{sv.akr.data(), 1};
+  } else {
+    R.irc = Col<double>{sv.irc.data(), 1};
+    R.iden = Col<double>{sv.iden.data(), 1};
+  }
+  R.ov = Col<double>{v, 1};
+  R.oe = Col<double>{e, 1};
+  EHJac<JT> J2;
+  J2.cp = Col<JT>{cp2.data(), 1};
+  J2.dp = Col<JT>{dp2.data(), 1};
+  J2.d = Col<JT>{d2.data(), 1};
+  J2.ae = Col<JT>{ae2.data(), 1};
+  uint32_t fl2 = 0;
+  eh_column<JT, CM, false, kSrcNone, kNewtonRuntime, Geom, NoDefer, true>(A, Tb, c, n, c, R, J2, G, t, dt, 1,
+                                                                          Fw, Fe, fl2, it, NoDefer{}, &sv.X);
+  fl |= fl2;
 }
 
 template <typename JT, class CM, class Geom>
@@ -108,6 +198,9 @@ void column_geom(const StepArgs& A, const Tables& Tb, int model, int src, int c,
 }
 
 }  // namespace
+
+// Split Newton emulation for later clmr_step calls (see g_split_at).
+extern "C" void clmr_set_split(int at) { g_split_at = at; }
 
 // One call advances every column nsteps steps in place (reference layout;
 // forcing: 4 slot pointers or null; root, atmos: rows of ncol or null;

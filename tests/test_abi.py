@@ -94,6 +94,32 @@ def test_guess_modes_match_the_header_and_are_checked(lib):
     assert lib.clm_create(ctypes.byref(cfg), ctypes.byref(h)) == A.CLM_ERR_ARG
 
 
+def test_tolerance_schedules_match_the_header_and_are_checked(lib):
+    """enum clm_tol_schedule in the header, the ctypes mirror and the Julia
+    binding agree; the default is CLM_TOL_AUTO (clm_config_default and the
+    mirror's default_config); values outside the enum are refused before
+    the device is touched."""
+    import re
+    text = (REPO / "include" / "climaland_cuda.h").read_text()
+    body = re.search(r"enum clm_tol_schedule \{([^}]*)\}", text).group(1)
+    vals = {k: int(v) for k, v in re.findall(r"(CLM_TOL_\w+) = (\d+)", body)}
+    assert vals == {"CLM_TOL_TILES": A.CLM_TOL_TILES, "CLM_TOL_REGROUP": A.CLM_TOL_REGROUP,
+                    "CLM_TOL_SPLIT": A.CLM_TOL_SPLIT, "CLM_TOL_AUTO": A.CLM_TOL_AUTO}
+    jl = (REPO / "climaland.jl_gb300" / "julia" / "ClimaLandGB300.jl").read_text()
+    for k, v in vals.items():
+        assert re.search(rf"const {k} = Int32\({v}\)", jl), k
+    c = A.ClmConfig()
+    lib.clm_config_default(ctypes.byref(c))
+    assert c.tol_regroup == A.CLM_TOL_AUTO == A.default_config().tol_regroup
+    h = ctypes.c_void_p()
+    for bad in (-1, 4):
+        cfg = A.default_config()
+        cfg.ncol = 10
+        cfg.newton_mode = A.CLM_NEWTON_TOL
+        cfg.tol_regroup = bad
+        assert lib.clm_create(ctypes.byref(cfg), ctypes.byref(h)) == A.CLM_ERR_ARG
+
+
 def test_create_rejects_runoff_outside_richards(lib):
     # the precipitation/runoff top boundary is RichardsAtmosDrivenFluxBC: an
     # EnergyHydrology handle (whose atmosphere-driven boundary is

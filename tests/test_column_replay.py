@@ -278,3 +278,65 @@ def test_extrapolated_guess_in_tolerance_mode():
     assert ie[1:].mean() < ip[1:].mean() - 0.2, (ie[1:].mean(), ip[1:].mean())
     d = np.maximum.reduceat(np.abs(plain[0] - ext[0]), w.offsets[:-1].astype(np.int64))
     assert np.mean(d <= 1e-8) >= 0.99, float(np.mean(d <= 1e-8))
+
+
+SPLIT_CASES = {
+    "fp64": (lambda: WL.full_scale_c4(ncol=1024, seed=3), A.CLM_PREC_FP64, None),
+    "mixed": (lambda: WL.full_scale_c4(ncol=1024, seed=3), A.CLM_PREC_MIXED, None),
+    "mixed_extrapolated": (lambda: WL.full_scale_c4(ncol=1024, seed=3), A.CLM_PREC_MIXED, "prev"),
+    "fp64_guess": (lambda: WL.full_scale_c4(ncol=1024, seed=3), A.CLM_PREC_FP64, "guess"),
+    "atmos_topmodel": (lambda: WL.with_atmos(WL.full_scale_c4(ncol=512, seed=4), runoff=A.CLM_RUNOFF_TOPMODEL),
+                       A.CLM_PREC_MIXED, None),
+    "stretched_brooks_corey": (lambda: WL.brooks_corey(WL.stretched(WL.full_scale_c4(ncol=512, seed=5))),
+                               A.CLM_PREC_FP64, "prev"),
+}
+
+
+@pytest.mark.parametrize("name", list(SPLIT_CASES))
+def test_split_newton_resume_is_bitwise(name):
+    """Split Newton (CLM_TOL_SPLIT): a column that has not converged after
+    its second iteration is saved (the arrays the step kernel's hook copies
+    to the queue and an EHNewtonCtx) and resumed from them alone, with its
+    per-iteration arrays starting as NaN. Over eight one-step calls in
+    tolerance mode the states, flags and iteration counts are those of one
+    uninterrupted solve bit for bit: the save leaves nothing out. Covers
+    FP64 and mixed, the plain, extrapolated and guessed starts, the
+    atmosphere-driven boundary with TOPMODEL's sinks, stretched columns and
+    Brooks-Corey."""
+    make, prec, start = SPLIT_CASES[name]
+    w = make()
+    kw = dict(precision=prec, newton_mode=A.CLM_NEWTON_TOL, max_iters=20, newton_tol=1e-8,
+              energy_norm_scale=1e-9)
+    L = _lib()
+
+    def run(split_at):
+        L.clmr_set_split(ctypes.c_int(split_at))
+        try:
+            st = list(w.copy_state())
+            prev = [w.vartheta_l.copy(), w.rho_e_int.copy()] if start == "prev" else None
+            last = None
+            out = []
+            for s in range(8):
+                x = w.columns(0, w.ncol)
+                x.vartheta_l, x.theta_i, x.rho_e_int, x.intF_w, x.intF_e = [None if a is None else a.copy()
+                                                                            for a in st]
+                guess = None
+                if start == "guess" and last is not None:
+                    guess = ((st[0] - last[0]).astype(np.float32), (st[2] - last[1]).astype(np.float32))
+                last = (st[0].copy(), st[2].copy())
+                r, fl, it = replay(x, 1, t0=w.t0 + s * w.dt, guess=guess, prev=prev, **kw)
+                st = list(r)
+                out.append((fl.copy(), it.copy()))
+            return st, out
+        finally:
+            L.clmr_set_split(ctypes.c_int(0))
+
+    ref, ref_steps = run(0)
+    got, got_steps = run(2)
+    for a, b in zip(ref, got):
+        assert (a is None and b is None) or np.array_equal(a, b), name
+    deferred = 0
+    for (fa, ia), (fb, ib) in zip(ref_steps, got_steps):
+        assert np.array_equal(fa, fb) and np.array_equal(ia, ib), name
+        deferred += int(np.count_nonzero(ia > 2))
+    assert deferred > 0, name  # the resumed path ran

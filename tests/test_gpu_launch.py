@@ -224,6 +224,9 @@ def test_tolerance_mode_regrouping_bitwise_equals_tile_order(torch, make):
         _same(ref, _run(w, calls, precision=prec, tol_regroup=1, **tol))
         _same(ref, _run(w, calls, precision=prec, tol_regroup=1, graph=1, **tol))
         _same(ref, _run(w, calls, precision=prec, tol_regroup=1, schedule=A.CLM_SCHED_DYNAMIC, **tol))
+        # split Newton: the unconverged columns finish in a second launch
+        for kw in (dict(), dict(graph=1), dict(schedule=A.CLM_SCHED_DYNAMIC, cols_per_cta=128)):
+            _same(ref, _run(w, calls, precision=prec, tol_regroup=A.CLM_TOL_SPLIT, **kw, **tol))
 
 
 @pytest.mark.parametrize("prec", [A.CLM_PREC_FP64, A.CLM_PREC_MIXED])
@@ -239,9 +242,12 @@ def test_extrapolated_guess_bitwise_over_launch_shapes(torch, prec):
     ref = _run(w, [(w.t0, 12)], tol_regroup=0, **tol)
     # flags cover a call's steps: the last one-step call's are a subset of
     # the twelve-step call's
-    for kw in (dict(tol_regroup=0), dict(tol_regroup=1), dict(tol_regroup=1, graph=1)):
+    for kw in (dict(tol_regroup=0), dict(tol_regroup=1), dict(tol_regroup=1, graph=1),
+               dict(tol_regroup=A.CLM_TOL_SPLIT), dict(tol_regroup=A.CLM_TOL_SPLIT, graph=1)):
         got = _run(w, ones, **kw, **tol)
         _same(ref, (got[0], got[1] | ref[1], got[2]))
+    # a twelve-step call under split Newton: twelve step pairs, the same bits
+    _same(ref, _run(w, [(w.t0, 12)], tol_regroup=A.CLM_TOL_SPLIT, **tol))
     with SoilColumns(w, tol_regroup=1, **tol) as g:
         for t, n in ones:
             g.step(t, w.dt, n)

@@ -174,3 +174,33 @@ def test_learned_guess_saves_newton_iterations(torch):
     # the in-kernel extrapolation is the zero-change network's guess in FP64
     # instead of float: the same iteration counts to within a few columns
     assert abs(stats["iters_extrapolated"] - stats["iters_previous_increment"]) < 0.02
+
+
+@pytest.mark.parametrize("prec", [A.CLM_PREC_FP64, A.CLM_PREC_MIXED])
+def test_network_guess_under_split_newton_is_bitwise(torch, prec):
+    """The network's guess launch followed by split Newton (the step kernel,
+    then the resuming kernel for the columns that have not converged after
+    two iterations) gives the bits of the depth-sorted tiles, direct and
+    graph-replayed: states, flags and iteration counts."""
+    w = WL.full_scale_c4(ncol=3000, seed=8)
+    tol = dict(LG.TOL, newton_tol=1e-8, precision=prec, learned_guess=A.CLM_GUESS_NETWORK)
+    blob = LG.zero_change_blob()
+
+    def run(**kw):
+        with SoilColumns(w, **tol, **kw) as g:
+            g.load_mlp(blob)
+            t = w.t0
+            for _ in range(6):
+                g.step(t, w.dt, 1)
+                t += w.dt
+            g.step(t, w.dt, 4)
+            f, it = g.status()
+            return g.get_state(), f, it
+
+    ref = run(tol_regroup=A.CLM_TOL_TILES)
+    for kw in (dict(tol_regroup=A.CLM_TOL_SPLIT), dict(tol_regroup=A.CLM_TOL_SPLIT, graph=1)):
+        got = run(**kw)
+        for a, b in zip(ref[0], got[0]):
+            assert (a is None and b is None) or np.array_equal(a, b)
+        assert np.array_equal(ref[1], got[1]) and np.array_equal(ref[2], got[2])
+    assert int(np.count_nonzero(ref[2] > 2)) > 0  # some columns resumed
