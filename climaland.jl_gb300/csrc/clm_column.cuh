@@ -462,8 +462,15 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         if (extrap) {
           gv = Yv - B.prev_v[k];
           ge = Ye - B.prev_e[k];
-          B.prev_v[k] = Yv;
-          B.prev_e[k] = Ye;
+          // read again by the next step: evict-first when that is another
+          // launch, kept in cache when it is this column's next step here
+          if (nsteps == 1) {
+            B.prev_v.store_last(k, Yv);
+            B.prev_e.store_last(k, Ye);
+          } else {
+            B.prev_v[k] = Yv;
+            B.prev_e[k] = Ye;
+          }
         } else {
           gv = (double)B.guess_v[k];
           ge = (double)B.guess_e[k];
@@ -873,8 +880,11 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
         }
       }
     }
-    if (deferred) break;  // one step per call with a deferring hook
     // ---------------- final combination ---------------------------------
+    // (not for a deferred column: its solve ends in the resuming launch; a
+    // deferring hook is used with one step per call, so the step loop needs
+    // no second exit)
+    if (!deferred) {
     const double inv_dt = 1.0 / dt;
     const bool last = step == nsteps - 1;
     const Col<double> OV = kResume ? B.ov : B.gv, OE = kResume ? B.oe : B.ge;
@@ -893,6 +903,7 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
     }
     Fw = UFw + dt * ((xFw - UFw) * inv_dt);
     Fe = UFe + dt * ((xFe - UFe) * inv_dt);
+    }  // !deferred
   }
   finite = finite && isfinite(Fw) && isfinite(Fe);
   if (!finite) flags |= CLM_COL_NONFINITE;

@@ -7,7 +7,7 @@
 
 namespace clm {
 
-void* step_fn_vg(int model, int precision, int src, bool tol) {
+void* step_fn_vg(int model, int precision, int src, int tol) {
   return step_fn_t<VG, false>(model, precision, src, tol);
 }
 
@@ -38,7 +38,7 @@ size_t step_smem_bytes(int model, int precision, int nmax, int wpc) {
   return tab * sizeof(double) + per_layer * (size_t)nmax * kTile * wpc;
 }
 
-static void* step_fn(int model, int precision, int cm, bool str, int src, bool tol) {
+static void* step_fn(int model, int precision, int cm, bool str, int src, int tol) {
   if (cm == CLM_CM_BROOKS_COREY)
     return str ? step_fn_bc_s(model, precision, src, tol) : step_fn_bc(model, precision, src, tol);
   return str ? step_fn_vg_s(model, precision, src, tol) : step_fn_vg(model, precision, src, tol);
@@ -51,16 +51,17 @@ cudaError_t step_grid(int model, int precision, int cm, bool str, bool tol, int 
                       int* grid) {
   const size_t smem = step_smem_bytes(model, precision, nmax, wpc);
   cudaError_t err;
-  // every variant of the launch shape: source kinds and both Newton modes
+  // every variant of the launch shape: source kinds and Newton modes (fixed,
+  // tolerance, tolerance with split Newton's deferring hook)
   for (int src : {kSrcNone, kSrcRoots, kSrcAtmos}) {
-    for (bool t : {false, true}) {
+    for (int t : {0, 1, 2}) {
       if (model != CLM_MODEL_ENERGY_HYDROLOGY && (src != kSrcNone || t)) continue;
       if ((err = cudaFuncSetAttribute(step_fn(model, precision, cm, str, src, t),
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
         return err;
     }
   }
-  void* fn = step_fn(model, precision, cm, str, kSrcNone, tol && model == CLM_MODEL_ENERGY_HYDROLOGY);
+  void* fn = step_fn(model, precision, cm, str, kSrcNone, (tol && model == CLM_MODEL_ENERGY_HYDROLOGY) ? 1 : 0);
   int dev = 0, nsm = 0, per_sm = 0;
   if ((err = cudaGetDevice(&dev)) != cudaSuccess) return err;
   if ((err = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return err;

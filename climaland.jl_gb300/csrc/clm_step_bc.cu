@@ -6,7 +6,7 @@
 
 namespace clm {
 
-void* step_fn_bc(int model, int precision, int src, bool tol) {
+void* step_fn_bc(int model, int precision, int src, int tol) {
   return step_fn_t<BC, false>(model, precision, src, tol);
 }
 

@@ -5,7 +5,7 @@
 
 namespace clm {
 
-void* step_fn_bc_s(int model, int precision, int src, bool tol) {
+void* step_fn_bc_s(int model, int precision, int src, int tol) {
   return step_fn_t<BC, true>(model, precision, src, tol);
 }
 

@@ -100,8 +100,13 @@ struct QueueView {
   }
 };
 
-// The step kernel's deferring hook: claims an entry (one atomic per group of
-// lanes that defer together) and copies the column's arrays and context.
+// The step kernel's deferring hook: claims an entry (one atomic per lane: a
+// warp-aggregated claim would put a warp collective inside the Newton loop,
+// whose reconvergence point keeps the lanes of a multi-step launch from
+// running ahead into their next step; measured 60 % slower fused launches)
+// and copies the column's arrays and context with evict-first stores (the
+// resuming launch prefetches them back; meanwhile they should not push the
+// step kernel's L2-resident scratch out).
 template <typename JT>
 struct QueueDefer {
   static constexpr bool kEnabled = true;
@@ -110,69 +115,67 @@ struct QueueDefer {
   int s;
   __device__ bool operator()(const EHBuffers& B, int n, const EHNewtonCtx& X) const {
     constexpr bool kMixed = sizeof(JT) < sizeof(double);
-    const unsigned m = __activemask();
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(m) - 1;
-    int base = 0;
-    if (lane == leader) base = atomicAdd(V.Q.count, __popc(m));
-    base = __shfl_sync(m, base, leader);
-    const int e = base + __popc(m & ((1u << lane) - 1u));
+    const int e = atomicAdd(V.Q.count, 1);
     if (e >= V.Q.cap) return false;  // no room: the column finishes here
     const Col<double> uv = V.arr(e, kQUv), uti = V.arr(e, kQUti), ue = V.arr(e, kQUe);
     const Col<double> xv = V.arr(e, kQXv), xe = V.arr(e, kQXe), K = V.arr(e, kQK);
     const Col<double> kap = V.arr(e, kQKap), aw = V.arr(e, kQAw);
     for (int k = 0; k < n; ++k) {
-      uv[k] = B.gv[k];
-      uti[k] = B.gti[k];
-      ue[k] = B.ge[k];
-      xv[k] = B.xv[k];
-      xe[k] = B.xe[k];
-      K[k] = B.K[k];
+      uv.store_last(k, B.gv[k]);
+      uti.store_last(k, B.gti[k]);
+      ue.store_last(k, B.ge[k]);
+      xv.store_last(k, B.xv[k]);
+      xe.store_last(k, B.xe[k]);
+      K.store_last(k, B.K[k]);
       if constexpr (kMixed) {
-        V.farr(e, 0)[k] = B.ircf[k];
+        V.farr(e, 0).store_last(k, B.ircf[k]);
       } else {
-        V.arr(e, kQAux0)[k] = B.irc[k];
-        V.arr(e, kQAux1)[k] = B.iden[k];
+        V.arr(e, kQAux0).store_last(k, B.irc[k]);
+        V.arr(e, kQAux1).store_last(k, B.iden[k]);
       }
     }
     for (int k = 0; k < n - 1; ++k) {  // faces k|k+1
-      kap[k] = B.kap[k];
-      aw[k] = B.aw[k];
+      kap.store_last(k, B.kap[k]);
+      aw.store_last(k, B.aw[k]);
       if constexpr (kMixed) {
-        V.farr(e, 1)[k] = B.awr[k];
-        V.farr(e, 2)[k] = B.akr[k];
+        V.farr(e, 1).store_last(k, B.awr[k]);
+        V.farr(e, 2).store_last(k, B.akr[k]);
       }
     }
-    V.scal(e, kQsSlot) = s;
-    V.scal(e, kQsFtw) = X.Ftw;
-    V.scal(e, kQsFth) = X.Fth;
-    V.scal(e, kQsFbw) = X.Fbw;
-    V.scal(e, kQsFbh) = X.Fbh;
-    V.scal(e, kQsUFw) = X.UFw;
-    V.scal(e, kQsUFe) = X.UFe;
-    V.scal(e, kQsXFw) = X.xFw;
-    V.scal(e, kQsXFe) = X.xFe;
-    V.scal(e, kQsRss) = X.R_ss;
-    V.scal(e, kQsRess) = X.R_ess;
-    V.scal(e, kQsPrevNorm) = X.prev_norm;
-    V.scal(e, kQsPrevState2) = X.prev_state2;
-    V.scal(e, kQsPred2) = X.pred2;
-    V.scal(e, kQsItStart) = X.it_start;
-    V.scal(e, kQsItDone) = X.it_done;
-    V.scal(e, kQsUseGuess) = X.use_guess ? 1.0 : 0.0;
+    auto put = [&](int f, double v) { __stcs(&V.scal(e, f), v); };
+    put(kQsSlot, s);
+    put(kQsFtw, X.Ftw);
+    put(kQsFth, X.Fth);
+    put(kQsFbw, X.Fbw);
+    put(kQsFbh, X.Fbh);
+    put(kQsUFw, X.UFw);
+    put(kQsUFe, X.UFe);
+    put(kQsXFw, X.xFw);
+    put(kQsXFe, X.xFe);
+    put(kQsRss, X.R_ss);
+    put(kQsRess, X.R_ess);
+    put(kQsPrevNorm, X.prev_norm);
+    put(kQsPrevState2, X.prev_state2);
+    put(kQsPred2, X.pred2);
+    put(kQsItStart, X.it_start);
+    put(kQsItDone, X.it_done);
+    put(kQsUseGuess, X.use_guess ? 1.0 : 0.0);
     return true;
   }
 };
 
 // kSrc: the RootExtraction source (A.rx) or the atmosphere-driven top
 // boundary (A.atm) compiled in; separate kernels so that their registers do
-// not weigh on the step without them. kStr: per-layer geometry. kTol: the
-// tolerance-mode Newton (norms, stopping, guesses) compiled in; the
-// fixed-iteration kernel carries none of its code, and each has a smaller
-// instruction footprint (with both modes in one kernel, instruction-fetch
-// stalls measured 0.81 cycles per issued instruction in tolerance mode with a
-// guess, 0.23 in fixed mode).
-template <typename JT, class CM, int kSrc, bool kStr, bool kTol = false>
+// not weigh on the step without them. kStr: per-layer geometry. kTol: 0
+// fixed Newton iterations, 1 the tolerance-mode Newton (norms, stopping,
+// guesses) compiled in, 2 that with split Newton's deferring hook (the
+// first launch of a split step). Each carries only its own mode's code and
+// has a smaller instruction footprint (with both Newton modes in one kernel,
+// instruction-fetch stalls measured 0.81 cycles per issued instruction in
+// tolerance mode with a guess, 0.23 in fixed mode; with the hook compiled
+// into every tolerance kernel, multi-step launches ran 1.5x slower: its
+// exit from the Newton loop changes how lanes that have converged run ahead).
+template <typename JT, class CM, int kSrc, bool kStr, int kTol = 0>
 __global__ void __launch_bounds__(128, 1)
     eh_step_kernel(StepArgs A, double* __restrict__ scratch, StepClock clk, int nsteps) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -239,12 +242,15 @@ __global__ void __launch_bounds__(128, 1)
       uint32_t flags = 0;
       int iters = 0;
       const auto G = GeomOf<kStr>::make(A, base, s, n);
-      if constexpr (kTol) {
+      if constexpr (kTol == 2) {
         // split Newton: one-step launches with a queue defer their
         // unconverged columns after iteration split_at
         const QueueDefer<JT> D{(A.split.q && nsteps == 1) ? A.split_at : 0, QueueView{A.split}, s};
         eh_column<JT, CM, false, kSrc, kNewtonTol, typename GeomOf<kStr>::type, QueueDefer<JT>>(
             A, Tb, s, n, A.L.perm[s], B, J, G, t0, dt, nsteps, Fw, Fe, flags, iters, D);
+      } else if constexpr (kTol == 1) {
+        eh_column<JT, CM, false, kSrc, kNewtonTol>(A, Tb, s, n, A.L.perm[s], B, J, G, t0, dt, nsteps, Fw, Fe,
+                                                   flags, iters);
       } else {
         eh_column<JT, CM, false, kSrc, kNewtonFixed>(A, Tb, s, n, A.L.perm[s], B, J, G, t0, dt, nsteps, Fw,
                                                      Fe, flags, iters);
@@ -417,7 +423,7 @@ inline int step_src(const StepArgs& A) {
 
 // The kernel of (model, precision, source variant) for closure CM and
 // geometry kStr, and its launch.
-template <class CM, bool kStr, bool kTol>
+template <class CM, bool kStr, int kTol>
 void* eh_fn_t(bool mx, int src) {
   if (src == kSrcRoots)
     return mx ? (void*)eh_step_kernel<float, CM, kSrcRoots, kStr, kTol>
@@ -429,17 +435,20 @@ void* eh_fn_t(bool mx, int src) {
             : (void*)eh_step_kernel<double, CM, kSrcNone, kStr, kTol>;
 }
 
+// tol: 0 fixed iterations, 1 tolerance mode, 2 tolerance mode with split
+// Newton's deferring hook
 template <class CM, bool kStr>
-void* step_fn_t(int model, int precision, int src = kSrcNone, bool tol = false) {
+void* step_fn_t(int model, int precision, int src = kSrcNone, int tol = 0) {
   if (model == CLM_MODEL_ENERGY_HYDROLOGY) {
     const bool mx = precision == CLM_PREC_MIXED;
-    return tol ? eh_fn_t<CM, kStr, true>(mx, src) : eh_fn_t<CM, kStr, false>(mx, src);
+    if (tol == 2) return eh_fn_t<CM, kStr, 2>(mx, src);
+    return tol ? eh_fn_t<CM, kStr, 1>(mx, src) : eh_fn_t<CM, kStr, 0>(mx, src);
   }
   return precision == CLM_PREC_MIXED ? (void*)richards_step_kernel<float, CM, kStr>
                                      : (void*)richards_step_kernel<double, CM, kStr>;
 }
 
-template <typename JT, class CM, bool kStr, bool kTol>
+template <typename JT, class CM, bool kStr, int kTol>
 void launch_eh_mode(const StepArgs& A, int grid, dim3 block, size_t smem, double* scratch,
                     const StepClock& clk, int nsteps, cudaStream_t stream) {
   switch (step_src(A)) {
@@ -457,10 +466,12 @@ void launch_eh_mode(const StepArgs& A, int grid, dim3 block, size_t smem, double
 template <typename JT, class CM, bool kStr>
 void launch_eh_t(const StepArgs& A, int grid, dim3 block, size_t smem, double* scratch,
                  const StepClock& clk, int nsteps, cudaStream_t stream) {
-  if (A.newton_mode == CLM_NEWTON_TOL)
-    launch_eh_mode<JT, CM, kStr, true>(A, grid, block, smem, scratch, clk, nsteps, stream);
+  if (A.newton_mode == CLM_NEWTON_TOL && A.split.q && nsteps == 1)
+    launch_eh_mode<JT, CM, kStr, 2>(A, grid, block, smem, scratch, clk, nsteps, stream);
+  else if (A.newton_mode == CLM_NEWTON_TOL)
+    launch_eh_mode<JT, CM, kStr, 1>(A, grid, block, smem, scratch, clk, nsteps, stream);
   else
-    launch_eh_mode<JT, CM, kStr, false>(A, grid, block, smem, scratch, clk, nsteps, stream);
+    launch_eh_mode<JT, CM, kStr, 0>(A, grid, block, smem, scratch, clk, nsteps, stream);
 }
 
 template <class CM, bool kStr>
@@ -497,10 +508,10 @@ void launch_resume_t(const StepArgs& A, int precision, int grid, dim3 block, siz
 // One translation unit per (closure, geometry) instantiates these: the entry
 // points each defines (clm_step.cu, clm_step_bc.cu, clm_step_s.cu,
 // clm_step_bc_s.cu).
-void* step_fn_vg(int model, int precision, int src, bool tol);
-void* step_fn_bc(int model, int precision, int src, bool tol);
-void* step_fn_vg_s(int model, int precision, int src, bool tol);
-void* step_fn_bc_s(int model, int precision, int src, bool tol);
+void* step_fn_vg(int model, int precision, int src, int tol);
+void* step_fn_bc(int model, int precision, int src, int tol);
+void* step_fn_vg_s(int model, int precision, int src, int tol);
+void* step_fn_bc_s(int model, int precision, int src, int tol);
 void launch_step_vg(const StepArgs& A, int model, int precision, int grid, dim3 block, size_t smem,
                     double* scratch, const StepClock& clk, int nsteps, cudaStream_t stream);
 void launch_step_bc(const StepArgs& A, int model, int precision, int grid, dim3 block, size_t smem,

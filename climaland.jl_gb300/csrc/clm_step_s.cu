@@ -6,7 +6,7 @@
 
 namespace clm {
 
-void* step_fn_vg_s(int model, int precision, int src, bool tol) {
+void* step_fn_vg_s(int model, int precision, int src, int tol) {
   return step_fn_t<VG, true>(model, precision, src, tol);
 }
 
