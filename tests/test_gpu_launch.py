@@ -254,3 +254,29 @@ def test_extrapolated_guess_bitwise_over_launch_shapes(torch, prec):
             g.set_state(*g.get_state())
         f, it = g.status()
         _same(ref, (g.get_state(), f | ref[1], it))
+
+
+@pytest.mark.parametrize("make", [
+    lambda: WL.stretched(WL.full_scale_c4(ncol=2000, seed=12)),
+    lambda: WL.brooks_corey(WL.full_scale_c4(ncol=2000, seed=13)),
+    lambda: WL.brooks_corey(WL.stretched(WL.uneven_c2(ncol=2000, seed=14))),
+    lambda: WL.with_atmos(WL.full_scale_c4(ncol=2000, seed=15), runoff=A.CLM_RUNOFF_TOPMODEL),
+    lambda: WL.with_root_extraction(WL.full_scale_c4(ncol=2000, seed=16)),
+])
+def test_split_newton_bitwise_across_kernel_variants(torch, make):
+    """Split Newton on every step-kernel variant that defers (per-layer
+    geometry, Brooks-Corey, the atmosphere-driven boundary with TOPMODEL's
+    sinks, root extraction) and the resuming kernel of each closure and
+    geometry: the states, flags and iteration counts of the depth-sorted
+    tiles bit for bit, FP64 and mixed, from U and from the extrapolated
+    start."""
+    w = make()
+    tol = dict(newton_mode=A.CLM_NEWTON_TOL, max_iters=20, newton_tol=1e-8, energy_norm_scale=1e-9)
+    ones = [(w.t0 + i * w.dt, 1) for i in range(6)]
+    for prec in (A.CLM_PREC_FP64, A.CLM_PREC_MIXED):
+        for guess in (A.CLM_GUESS_NONE, A.CLM_GUESS_EXTRAPOLATE):
+            kw = dict(tol, precision=prec, learned_guess=guess)
+            ref = _run(w, ones, tol_regroup=A.CLM_TOL_TILES, **kw)
+            got = _run(w, ones, tol_regroup=A.CLM_TOL_SPLIT, **kw)
+            _same(ref, got)
+            assert int(np.count_nonzero(ref[2] > 2)) > 0  # the resuming kernel ran
