@@ -1234,12 +1234,29 @@ int clm_step_host(clm_handle* h, double* v, double* ti, double* e, double* Fw, d
     A.tile_begin = T0;
     A.tile_end = T1;
     A.order = nullptr;  // a chunk's launch covers its own tiles' columns
-    for (int s0 = 0; s0 < nsteps; s0 += 64) {
-      StepClock clk;
-      clk.t0 = step_time(t, s0, dt);
-      clk.dt = dt;
-      CLM_CUDA(h, launch_step(A, h->cfg.model, h->cfg.precision, h->wpc, h->grid, h->d_scratch, clk,
-                              std::min(64, nsteps - s0), h->stream));
+    if (splits(h)) {
+      // split Newton per step: the chunk's tiles, then its deferred columns
+      // (the queue serves one chunk at a time: the launches share the stream)
+      StepArgs S = A;
+      S.split = SplitQueue{h->d_queue, h->d_qcount, h->stride, h->nmax};
+      S.split_at = kSplitIters;
+      for (int s0 = 0; s0 < nsteps; ++s0) {
+        StepClock clk;
+        clk.t0 = step_time(t, s0, dt);
+        clk.dt = dt;
+        CLM_CUDA(h, cudaMemsetAsync(h->d_qcount, 0, sizeof(int), h->stream));
+        CLM_CUDA(h, launch_step(S, h->cfg.model, h->cfg.precision, h->wpc, h->grid, h->d_scratch, clk, 1,
+                                h->stream));
+        CLM_CUDA(h, launch_resume(S, h->cfg.precision, h->wpc, h->grid, clk, h->stream));
+      }
+    } else {
+      for (int s0 = 0; s0 < nsteps; s0 += 64) {
+        StepClock clk;
+        clk.t0 = step_time(t, s0, dt);
+        clk.dt = dt;
+        CLM_CUDA(h, launch_step(A, h->cfg.model, h->cfg.precision, h->wpc, h->grid, h->d_scratch, clk,
+                                std::min(64, nsteps - s0), h->stream));
+      }
     }
     CLM_CUDA(h, internal_to_ref(L, Fo, h->stream, T0, T1 - T0));
     CLM_CUDA(h, cudaEventRecord(ev_done, h->stream));

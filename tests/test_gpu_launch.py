@@ -150,6 +150,23 @@ def test_host_step_equals_set_step_get(torch, name, make, chunks, nsteps):
     _same(ref, (dev, f, it))
 
 
+@pytest.mark.parametrize("prec", [A.CLM_PREC_FP64, A.CLM_PREC_MIXED])
+def test_host_step_split_newton_equals_device_step(torch, prec):
+    """Tolerance mode with split Newton through the host-buffer path
+    (clm_step_host: per chunk and step, the chunk's tiles then its deferred
+    columns) gives the bits of the device-resident step."""
+    w = WL.full_scale_c4(ncol=3000, seed=17)
+    kw = dict(newton_mode=A.CLM_NEWTON_TOL, max_iters=20, newton_tol=1e-8, energy_norm_scale=1e-9,
+              precision=prec, tol_regroup=A.CLM_TOL_SPLIT)
+    ref = _run(w, [(w.t0, 4)], **kw)
+    st = w.copy_state()
+    with SoilColumns(w, host_chunks=3, **kw) as g:
+        g.step_host(st, w.t0, w.dt, 4)
+        f, it = g.status()
+    _same(ref, (st, f, it))
+    assert int(np.count_nonzero(it > 2)) > 0
+
+
 def test_atmos_boundary_graph_host_and_dynamic_paths_agree(torch):
     """The atmosphere-driven step (with TOPMODEL runoff) gives the same bits
     through direct launches, CUDA graph replay, the dynamic tile order and the
