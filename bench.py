@@ -519,6 +519,9 @@ def full_run(args, torch):
              ("extrapolated_mixed_tol1e-8_graph",
               dict(mx, learned_guess=A.CLM_GUESS_EXTRAPOLATE, graph=1, **tol), None)] if not atmos else \
         [("plain_fp64", {}, None), ("mixed", mx, None)]
+    if args.full_forms:  # a subset, the FP64 path always (the speed-ups' base)
+        keep = set(args.full_forms.split(",")) | {"plain_fp64"}
+        forms = [f for f in forms if f[0] in keep]
     out = {"workload": w.name, "columns": w.ncol, "steps": nst, "simulated_days": nst * w.dt / 86400.0,
            "top_boundary": "atmosphere-driven" if atmos else "flux",
            "learned_training_s": train_s,
@@ -611,6 +614,8 @@ def main():
                     help="the full-scale configuration's whole 8-day run per form (minutes), "
                          "instead of the bench line")
     ap.add_argument("--full-oracle-cols", type=int, default=8192)
+    ap.add_argument("--full-forms", default=None,
+                    help="--full-run: comma-separated form names to run (default: all)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
