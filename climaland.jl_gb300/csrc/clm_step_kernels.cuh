@@ -268,8 +268,9 @@ __global__ void __launch_bounds__(128, 1)
 // Split Newton, second launch: the queued columns, 32 to a warp in the order
 // they were saved, from their saved context to the end of the step (the
 // explicit source and top-boundary variants differ only before the Newton
-// solve, so one kernel serves them all). Shared memory: the tables and the
-// Thomas arrays of each warp; the iterate, U and the aux stay in the entry.
+// solve, so one kernel serves them all). Shared memory as the step kernel's:
+// the tables, then per warp the iterate (copied in from the entry) and the
+// Thomas arrays; U, the aux and the per-iteration residuals stay in the entry.
 template <typename JT>
 __host__ __device__ constexpr size_t eh_resume_smem_per_layer() {
   return eh_smem_per_layer<JT>();  // as the step kernel: xv, xe | cp, dp, d
