@@ -311,283 +311,283 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
       X = *resume;
       it_first = X.it_done + 1;
     } else {
-    const double t = t0 + step * dt;
-    // Newton guess (tolerance mode only): Newton starts from u_n + a guessed
-    // increment instead of U -- the learned guess's (guess_v, guess_e) or the
-    // previous step's increment (prev_v, prev_e) -- and falls back to U when
-    // its first increment is more than ten times the guessed one (a grossly
-    // wrong guess; one a little worse than U still converges about as fast,
-    // while a restart costs the whole warp an iteration)
-    const bool extrap = B.prev_v.p != nullptr && tol;
-    use_guess = extrap || (B.guess_v.p != nullptr && tol && isfinite(B.guess_v[0]) &&
-                           isfinite(B.guess_e[0]));
-    pred2 = 0.0;
-    // ---------------- stage 1: aux at Y_n, explicit tendency, U ----------
-    double K0 = 0, T0 = 0, kap0 = 0, psi0 = 0;
-    double Kt = 0, Tt = 0, kapt = 0, psit = 0;
-    double kap_prev = 0.0, K_prev = 0.0;
-    // RootExtraction (soil_canopy_root_interactions.jl:8-39, 139-159): the
-    // explicit source at Y_n and its column integrals for intF_w / intF_e
-    RootCol rcol;
-    if constexpr (kRoots) rcol = load_root_col(Tb, A.rx, st, s);
-    double root_w = 0.0, root_e = 0.0;
-    // atmosphere-driven top boundary at Y_n (update_aux values of the top
-    // layers), frozen through the Newton solve
-    AtmosOut ab{};
-    double dz_top = 0.0;
-    double sub_top = 0.0;  // SoilSublimation's theta_i tendency in the layers k >= k_sub
-    int k_sub = n;
-    EHRunoff ro{0.0, 0.0, 0.0, 0.0, 0.0};
-    if constexpr (kAtmos) {
-      auto theta_l_of = [&](int k) {
-        const double Yv = B.gv[k], nu_eff = c.nu - B.gti[k];
+      const double t = t0 + step * dt;
+      // Newton guess (tolerance mode only): Newton starts from u_n + a guessed
+      // increment instead of U -- the learned guess's (guess_v, guess_e) or the
+      // previous step's increment (prev_v, prev_e) -- and falls back to U when
+      // its first increment is more than ten times the guessed one (a grossly
+      // wrong guess; one a little worse than U still converges about as fast,
+      // while a restart costs the whole warp an iteration)
+      const bool extrap = B.prev_v.p != nullptr && tol;
+      use_guess = extrap || (B.guess_v.p != nullptr && tol && isfinite(B.guess_v[0]) &&
+                             isfinite(B.guess_e[0]));
+      pred2 = 0.0;
+      // ---------------- stage 1: aux at Y_n, explicit tendency, U ----------
+      double K0 = 0, T0 = 0, kap0 = 0, psi0 = 0;
+      double Kt = 0, Tt = 0, kapt = 0, psit = 0;
+      double kap_prev = 0.0, K_prev = 0.0;
+      // RootExtraction (soil_canopy_root_interactions.jl:8-39, 139-159): the
+      // explicit source at Y_n and its column integrals for intF_w / intF_e
+      RootCol rcol;
+      if constexpr (kRoots) rcol = load_root_col(Tb, A.rx, st, s);
+      double root_w = 0.0, root_e = 0.0;
+      // atmosphere-driven top boundary at Y_n (update_aux values of the top
+      // layers), frozen through the Newton solve
+      AtmosOut ab{};
+      double dz_top = 0.0;
+      double sub_top = 0.0;  // SoilSublimation's theta_i tendency in the layers k >= k_sub
+      int k_sub = n;
+      EHRunoff ro{0.0, 0.0, 0.0, 0.0, 0.0};
+      if constexpr (kAtmos) {
+        auto theta_l_of = [&](int k) {
+          const double Yv = B.gv[k], nu_eff = c.nu - B.gti[k];
+          const double v_safe = fmax(Yv, c.theta_r + kSqrtEps);
+          const double nu_safe = fmax(nu_eff, c.theta_r + kSqrtEps);
+          return (v_safe < nu_safe) ? v_safe : nu_safe;
+        };
+        const int k1 = n - 1;
+        const double Yv = B.gv[k1], Yti = B.gti[k1], Ye = B.ge[k1];
+        AtmosSfc sf;
+        sf.th1 = theta_l_of(k1);
+        sf.th2 = theta_l_of(k1 - 1);
+        sf.T = E.T_0 + (Ye + Yti * E.rho_i_LH_f0) * fm::rcp(heat_capacity(E, sf.th1, Yti, c.rcds));
+        double d;
+        psi_dpsi<false>(Tb, c.g, c.nu - Yti, Yv, c.theta_r, c.S_s, sf.psi, d);
+        sf.Tf = tf_depressed_aux(Tb, E, c.g, c.nu, c.theta_r, sf.th1, Yti);
+        sf.z1 = G.centre(k1);
+        sf.z2 = G.centre(k1 - 1);
+        dz_top = G.top_gap();
+        sf.dz_top = dz_top;
+        sf.ti = Yti;
+        const AtmosRow D{A.atm, st, s};
+        sf.th_alb = albedo_theta(G, D(CLM_AT_ALBEDO_TOP_THICKNESS), theta_l_of);
+        // the runoff model's infiltration (and TOPMODEL's subsurface sink) from
+        // the update_aux values at Y_n
+        const double* P = A.prm;
+        ro = eh_runoff(Tb, E, sc, A.runoff, G, c.nu, c.theta_r, c.K_sat, P[CLM_P_F_MAX * st + s],
+                       P[CLM_P_F_OVER * st + s], P[CLM_P_R_SB * st + s], sf.th1, D(CLM_AT_P_LIQ),
+                       [&](int k, double& v, double& ti, double& T) {
+                         v = B.gv[k];
+                         ti = B.gti[k];
+                         T = E.T_0 + (B.ge[k] + ti * E.rho_i_LH_f0) *
+                                         fm::rcp(heat_capacity(E, theta_l_of(k), ti, c.rcds));
+                       });
+        sf.infil = ro.infil;
+        ab = atmos_bc(Tb, A.ak, E, D, c.g, c.nu, c.theta_r, sf);
+        // H(z_k + 2 dz_top) rises with k: the source reaches the layers from
+        // k_sub up (the top layer alone for a surface at z = 0)
+        while (k_sub > 0 && sublimation_weight(G, k_sub - 1, dz_top) != 0.0) --k_sub;
+        sub_top = -ab.vice * E.rho_l / E.rho_i / (2.0 * dz_top);
+      }
+      for (int k = 0; k < n; ++k) {
+        const double Yv = B.gv[k], Yti = B.gti[k], Ye = B.ge[k];
+        const double nu_eff = c.nu - Yti;
+        // volumetric_liquid_fraction (soil_hydrology_parameterizations.jl:22-31)
         const double v_safe = fmax(Yv, c.theta_r + kSqrtEps);
         const double nu_safe = fmax(nu_eff, c.theta_r + kSqrtEps);
-        return (v_safe < nu_safe) ? v_safe : nu_safe;
-      };
-      const int k1 = n - 1;
-      const double Yv = B.gv[k1], Yti = B.gti[k1], Ye = B.ge[k1];
-      AtmosSfc sf;
-      sf.th1 = theta_l_of(k1);
-      sf.th2 = theta_l_of(k1 - 1);
-      sf.T = E.T_0 + (Ye + Yti * E.rho_i_LH_f0) * fm::rcp(heat_capacity(E, sf.th1, Yti, c.rcds));
-      double d;
-      psi_dpsi<false>(Tb, c.g, c.nu - Yti, Yv, c.theta_r, c.S_s, sf.psi, d);
-      sf.Tf = tf_depressed_aux(Tb, E, c.g, c.nu, c.theta_r, sf.th1, Yti);
-      sf.z1 = G.centre(k1);
-      sf.z2 = G.centre(k1 - 1);
-      dz_top = G.top_gap();
-      sf.dz_top = dz_top;
-      sf.ti = Yti;
-      const AtmosRow D{A.atm, st, s};
-      sf.th_alb = albedo_theta(G, D(CLM_AT_ALBEDO_TOP_THICKNESS), theta_l_of);
-      // the runoff model's infiltration (and TOPMODEL's subsurface sink) from
-      // the update_aux values at Y_n
-      const double* P = A.prm;
-      ro = eh_runoff(Tb, E, sc, A.runoff, G, c.nu, c.theta_r, c.K_sat, P[CLM_P_F_MAX * st + s],
-                     P[CLM_P_F_OVER * st + s], P[CLM_P_R_SB * st + s], sf.th1, D(CLM_AT_P_LIQ),
-                     [&](int k, double& v, double& ti, double& T) {
-                       v = B.gv[k];
-                       ti = B.gti[k];
-                       T = E.T_0 + (B.ge[k] + ti * E.rho_i_LH_f0) *
-                                       fm::rcp(heat_capacity(E, theta_l_of(k), ti, c.rcds));
-                     });
-      sf.infil = ro.infil;
-      ab = atmos_bc(Tb, A.ak, E, D, c.g, c.nu, c.theta_r, sf);
-      // H(z_k + 2 dz_top) rises with k: the source reaches the layers from
-      // k_sub up (the top layer alone for a surface at z = 0)
-      while (k_sub > 0 && sublimation_weight(G, k_sub - 1, dz_top) != 0.0) --k_sub;
-      sub_top = -ab.vice * E.rho_l / E.rho_i / (2.0 * dz_top);
-    }
-    for (int k = 0; k < n; ++k) {
-      const double Yv = B.gv[k], Yti = B.gti[k], Ye = B.ge[k];
-      const double nu_eff = c.nu - Yti;
-      // volumetric_liquid_fraction (soil_hydrology_parameterizations.jl:22-31)
-      const double v_safe = fmax(Yv, c.theta_r + kSqrtEps);
-      const double nu_safe = fmax(nu_eff, c.theta_r + kSqrtEps);
-      const double tl = (v_safe < nu_safe) ? v_safe : nu_safe;
-      const double rc = heat_capacity(E, tl, Yti, c.rcds);
-      // thermal_time's 1 / (3 dz^2) of this layer
-      if constexpr (kStr) pcc.inv_3dz2 = fm::rcp(3.0 * (G.width(k) * G.width(k)));
-      // one reciprocal of rho c for T and the phase change
-      const double inv_rc = fm::rcp(rc);
-      const double T = E.T_0 + (Ye + Yti * E.rho_i_LH_f0) * inv_rc;
-      double kap = 0.0, K = 0.0;
-      bool aux_ff = false;
-      if constexpr (mixed) {
-        // kappa and K in double-float
-        const F2 tl_f = ff::from_double(tl), ti_f = ff::from_double(Yti);
-        const F2 guard = ff::add_f(MX.cf.theta_r, 1.4901161193847656e-08f);
-        const F2 S = ff::div(ff::sub(ff_max(ff::from_double(Yv), guard), MX.cf.theta_r),
-                             ff::sub(ff_max(MX.cf.nu, guard), MX.cf.theta_r));
-        // f_i = 0 without the division only where theta_i is exactly 0 (a
-        // negative theta_i gives the reference's f_i < 0)
-        const F2 fi = Yti != 0.0 ? ff::div(ti_f, ff::sub(ff::add(tl_f, ti_f), MX.cf.theta_r))
-                                : ff::make(0.0f);
-        const F2 lnf = ff::add(ff::neg(ff::mul(MX.omega_ln10, fi)),
-                               ff::mul(MX.visc_gamma, ff::sub(ff::from_double(T), MX.visc_T_ref)));
-        aux_ff = kappa_ff(MX.FT, MX.kf, tl, Yti, tl_f, ti_f, kap) &&
-                 conductivity_ff(MX.FT, MX.cf, MX.K_sat, S, lnf, K);
-      }
-      if (!aux_ff) {
-        kap = conductivity_heat(Tb, sc, tl, Yti, c.nu, c.kdry, c.ksu, c.ksf, c.lku, c.lkf, c.nuom,
-                                c.nuq, c.nug);
-        const double SK = saturation_r(pcc.inv_den, Yv, c.theta_r);
-        const double fi = Yti != 0.0 ? Yti / (tl + Yti - c.theta_r) : 0.0;
-        // impedance_factor * viscosity_factor * hydraulic_conductivity, with
-        // the sqrt(S) of the van Genuchten K inside the same exponential
-        const double lnf = -sc.omega_ln10 * fi + sc.visc_gamma * (T - sc.visc_gamma_T_ref);
-        K = conductivity_scaled(Tb, c.g, c.K_sat, SK, lnf);
-      }
-      double Uv = Yv, Uti = Yti, Ue = Ye;
-      double pc = 0.0;
-      if (A.phase_change) {
-        pc = mixed ? phase_change_reduced(Tb, E, c.g, c.nu, c.theta_r, pcc, tl, Yti, T, inv_rc, kap)
-                   : phase_change_r(Tb, E, c.g, c.nu, c.theta_r, pcc, tl, Yti, T, inv_rc, kap, flags);
-        Uv = Yv + dt * (-pc);
-        Uti = Yti + dt * (E.rho_l_over_rho_i * pc);
-      }
-      if constexpr (kAtmos) {
-        // SoilSublimation after PhaseChange in the sources tuple
-        const double sub = k >= k_sub ? sub_top : 0.0;
-        Uti = Yti + dt * ((A.phase_change ? E.rho_l_over_rho_i * pc : 0.0) + sub);
-      }
-      if constexpr (kRoots) {
-        // psi at Y_n (update_aux!), the layer centre z, K and T of this stage
-        double psi_n, d;
-        psi_dpsi<false>(Tb, c.g, nu_eff, Yv, c.theta_r, c.S_s, psi_n, d);
-        const double re = root_rate(Tb, rcol, G.face_centre(k), psi_n, K);
-        const double ree = re * rho_e_liq(E, T);
-        Uv = Yv + dt * ((-pc) + (-1.0 * re));  // sources in the reference's order
-        Ue = Ye + dt * (-1.0 * ree);
-        root_e += G.width(k) * ree;
-        root_w += G.width(k) * re;
-        B.ge[k] = Ue;
-      }
-      B.gv[k] = Uv;
-      B.gti[k] = Uti;
-      if constexpr (kAtmos) {
-        // TOPMODEL's implicit subsurface sink, constant through the Newton
-        // solve: part of the residual's U + dt T_imp, not of the start x = U
-        if (ro.cw != 0.0 || ro.ce != 0.0) {
-          const double w = sat_weight(Yv - c.theta_r, c.nu - c.theta_r);
-          B.gv[k] = Uv - dt * (ro.cw * w);
-          B.ge[k] = Ue - dt * (ro.ce * w);
-        }
-      }
-      if constexpr (!mixed)
-        if (B.iden.p) B.iden[k] = sat_inv(c.nu - Uti, c.theta_r);
-      if (use_guess) {
-        double gv, ge;
-        if (extrap) {
-          gv = Yv - B.prev_v[k];
-          ge = Ye - B.prev_e[k];
-          // read again by the next step: evict-first when that is another
-          // launch, kept in cache when it is this column's next step here
-          if (nsteps == 1) {
-            B.prev_v.store_last(k, Yv);
-            B.prev_e.store_last(k, Ye);
-          } else {
-            B.prev_v[k] = Yv;
-            B.prev_e[k] = Ye;
-          }
-        } else {
-          gv = (double)B.guess_v[k];
-          ge = (double)B.guess_e[k];
-        }
-        double xv0 = Yv + gv, xe0 = Ye + ge;
-        // a zero guessed increment carries no information (the first step
-        // of a history): the layer starts from U
-        if (gv == 0.0 && ge == 0.0) {
-          xv0 = Uv;
-          xe0 = Ue;
-        }
-        // a layer whose guess leaves the retention curve's domain
-        // (vartheta_l <= theta_r) or is not finite starts from U
-        if (!(xv0 > c.theta_r + kSqrtEps) || !isfinite(xv0)) xv0 = Uv;
-        if (!isfinite(xe0)) xe0 = Ue;
-        B.xv[k] = xv0;
-        B.xe[k] = xe0;
-        const double dv = xv0 - Uv, de = A.energy_scale * (xe0 - Ue);
-        pred2 += dv * dv + de * de;
-      } else {
-        B.xv[k] = Uv;
-        B.xe[k] = Ue;
-      }
-      B.K[k] = K;
-      // face conductances k-1|k, frozen through the Newton solve: kappa on
-      // the face into kappa's slot (the cell value is not used after stage 1)
-      if (k > 0) {
-        const double ak = (kap_prev + kap) * G.hinv_gap(k - 1);
-        const double aw = (K_prev + K) * G.hinv_gap(k - 1);
-        B.kap[k - 1] = ak;
-        if (B.aw.p) B.aw[k - 1] = aw;
+        const double tl = (v_safe < nu_safe) ? v_safe : nu_safe;
+        const double rc = heat_capacity(E, tl, Yti, c.rcds);
+        // thermal_time's 1 / (3 dz^2) of this layer
+        if constexpr (kStr) pcc.inv_3dz2 = fm::rcp(3.0 * (G.width(k) * G.width(k)));
+        // one reciprocal of rho c for T and the phase change
+        const double inv_rc = fm::rcp(rc);
+        const double T = E.T_0 + (Ye + Yti * E.rho_i_LH_f0) * inv_rc;
+        double kap = 0.0, K = 0.0;
+        bool aux_ff = false;
         if constexpr (mixed) {
-          // the float rows' face products: dt K_face / (dz gap) (uniform:
-          // W's own rows), or dt K_face / gap (stretched: W's rows times the
-          // layer width)
-          const double fac = kStr ? dt : rdz(k - 1);
-          B.awr[k - 1] = ff::narrow_trunc(fac * aw);
-          B.akr[k - 1] = ff::narrow_trunc(fac * ak);
+          // kappa and K in double-float
+          const F2 tl_f = ff::from_double(tl), ti_f = ff::from_double(Yti);
+          const F2 guard = ff::add_f(MX.cf.theta_r, 1.4901161193847656e-08f);
+          const F2 S = ff::div(ff::sub(ff_max(ff::from_double(Yv), guard), MX.cf.theta_r),
+                               ff::sub(ff_max(MX.cf.nu, guard), MX.cf.theta_r));
+          // f_i = 0 without the division only where theta_i is exactly 0 (a
+          // negative theta_i gives the reference's f_i < 0)
+          const F2 fi = Yti != 0.0 ? ff::div(ti_f, ff::sub(ff::add(tl_f, ti_f), MX.cf.theta_r))
+                                  : ff::make(0.0f);
+          const F2 lnf = ff::add(ff::neg(ff::mul(MX.omega_ln10, fi)),
+                                 ff::mul(MX.visc_gamma, ff::sub(ff::from_double(T), MX.visc_T_ref)));
+          aux_ff = kappa_ff(MX.FT, MX.kf, tl, Yti, tl_f, ti_f, kap) &&
+                   conductivity_ff(MX.FT, MX.cf, MX.K_sat, S, lnf, K);
+        }
+        if (!aux_ff) {
+          kap = conductivity_heat(Tb, sc, tl, Yti, c.nu, c.kdry, c.ksu, c.ksf, c.lku, c.lkf, c.nuom,
+                                  c.nuq, c.nug);
+          const double SK = saturation_r(pcc.inv_den, Yv, c.theta_r);
+          const double fi = Yti != 0.0 ? Yti / (tl + Yti - c.theta_r) : 0.0;
+          // impedance_factor * viscosity_factor * hydraulic_conductivity, with
+          // the sqrt(S) of the van Genuchten K inside the same exponential
+          const double lnf = -sc.omega_ln10 * fi + sc.visc_gamma * (T - sc.visc_gamma_T_ref);
+          K = conductivity_scaled(Tb, c.g, c.K_sat, SK, lnf);
+        }
+        double Uv = Yv, Uti = Yti, Ue = Ye;
+        double pc = 0.0;
+        if (A.phase_change) {
+          pc = mixed ? phase_change_reduced(Tb, E, c.g, c.nu, c.theta_r, pcc, tl, Yti, T, inv_rc, kap)
+                     : phase_change_r(Tb, E, c.g, c.nu, c.theta_r, pcc, tl, Yti, T, inv_rc, kap, flags);
+          Uv = Yv + dt * (-pc);
+          Uti = Yti + dt * (E.rho_l_over_rho_i * pc);
+        }
+        if constexpr (kAtmos) {
+          // SoilSublimation after PhaseChange in the sources tuple
+          const double sub = k >= k_sub ? sub_top : 0.0;
+          Uti = Yti + dt * ((A.phase_change ? E.rho_l_over_rho_i * pc : 0.0) + sub);
+        }
+        if constexpr (kRoots) {
+          // psi at Y_n (update_aux!), the layer centre z, K and T of this stage
+          double psi_n, d;
+          psi_dpsi<false>(Tb, c.g, nu_eff, Yv, c.theta_r, c.S_s, psi_n, d);
+          const double re = root_rate(Tb, rcol, G.face_centre(k), psi_n, K);
+          const double ree = re * rho_e_liq(E, T);
+          Uv = Yv + dt * ((-pc) + (-1.0 * re));  // sources in the reference's order
+          Ue = Ye + dt * (-1.0 * ree);
+          root_e += G.width(k) * ree;
+          root_w += G.width(k) * re;
+          B.ge[k] = Ue;
+        }
+        B.gv[k] = Uv;
+        B.gti[k] = Uti;
+        if constexpr (kAtmos) {
+          // TOPMODEL's implicit subsurface sink, constant through the Newton
+          // solve: part of the residual's U + dt T_imp, not of the start x = U
+          if (ro.cw != 0.0 || ro.ce != 0.0) {
+            const double w = sat_weight(Yv - c.theta_r, c.nu - c.theta_r);
+            B.gv[k] = Uv - dt * (ro.cw * w);
+            B.ge[k] = Ue - dt * (ro.ce * w);
+          }
+        }
+        if constexpr (!mixed)
+          if (B.iden.p) B.iden[k] = sat_inv(c.nu - Uti, c.theta_r);
+        if (use_guess) {
+          double gv, ge;
+          if (extrap) {
+            gv = Yv - B.prev_v[k];
+            ge = Ye - B.prev_e[k];
+            // read again by the next step: evict-first when that is another
+            // launch, kept in cache when it is this column's next step here
+            if (nsteps == 1) {
+              B.prev_v.store_last(k, Yv);
+              B.prev_e.store_last(k, Ye);
+            } else {
+              B.prev_v[k] = Yv;
+              B.prev_e[k] = Ye;
+            }
+          } else {
+            gv = (double)B.guess_v[k];
+            ge = (double)B.guess_e[k];
+          }
+          double xv0 = Yv + gv, xe0 = Ye + ge;
+          // a zero guessed increment carries no information (the first step
+          // of a history): the layer starts from U
+          if (gv == 0.0 && ge == 0.0) {
+            xv0 = Uv;
+            xe0 = Ue;
+          }
+          // a layer whose guess leaves the retention curve's domain
+          // (vartheta_l <= theta_r) or is not finite starts from U
+          if (!(xv0 > c.theta_r + kSqrtEps) || !isfinite(xv0)) xv0 = Uv;
+          if (!isfinite(xe0)) xe0 = Ue;
+          B.xv[k] = xv0;
+          B.xe[k] = xe0;
+          const double dv = xv0 - Uv, de = A.energy_scale * (xe0 - Ue);
+          pred2 += dv * dv + de * de;
+        } else {
+          B.xv[k] = Uv;
+          B.xe[k] = Ue;
+        }
+        B.K[k] = K;
+        // face conductances k-1|k, frozen through the Newton solve: kappa on
+        // the face into kappa's slot (the cell value is not used after stage 1)
+        if (k > 0) {
+          const double ak = (kap_prev + kap) * G.hinv_gap(k - 1);
+          const double aw = (K_prev + K) * G.hinv_gap(k - 1);
+          B.kap[k - 1] = ak;
+          if (B.aw.p) B.aw[k - 1] = aw;
+          if constexpr (mixed) {
+            // the float rows' face products: dt K_face / (dz gap) (uniform:
+            // W's own rows), or dt K_face / gap (stretched: W's rows times the
+            // layer width)
+            const double fac = kStr ? dt : rdz(k - 1);
+            B.awr[k - 1] = ff::narrow_trunc(fac * aw);
+            B.akr[k - 1] = ff::narrow_trunc(fac * ak);
+          }
+        }
+        kap_prev = kap;
+        K_prev = K;
+        if constexpr (mixed)
+          B.ircf[k] = 1.0f / ff::narrow_trunc(heat_capacity(E, tl, Uti, c.rcds));
+        else
+          B.irc[k] = fm::rcp(heat_capacity(E, tl, Uti, c.rcds));
+        if (k == 0) {
+          K0 = K; T0 = T; kap0 = kap;
+          if (A.bc_bw == CLM_BC_STATE) {
+            double d;
+            psi_dpsi<false>(Tb, c.g, nu_eff, Yv, c.theta_r, c.S_s, psi0, d);
+          }
+        }
+        if (k == n - 1) {
+          Kt = K; Tt = T; kapt = kap;
+          if (A.bc_tw == CLM_BC_STATE) {
+            double d;
+            psi_dpsi<false>(Tb, c.g, nu_eff, Yv, c.theta_r, c.S_s, psit, d);
+          }
         }
       }
-      kap_prev = kap;
-      K_prev = K;
-      if constexpr (mixed)
-        B.ircf[k] = 1.0f / ff::narrow_trunc(heat_capacity(E, tl, Uti, c.rcds));
-      else
-        B.irc[k] = fm::rcp(heat_capacity(E, tl, Uti, c.rcds));
-      if (k == 0) {
-        K0 = K; T0 = T; kap0 = kap;
-        if (A.bc_bw == CLM_BC_STATE) {
-          double d;
-          psi_dpsi<false>(Tb, c.g, nu_eff, Yv, c.theta_r, c.S_s, psi0, d);
+      // boundary fluxes at t, frozen through the Newton solve
+      {
+        const double ftw = forcing_value(A.forc[CLM_BC_TOP_WATER], st, s, A.col0 + orig, t, A.seed);
+        const double fth = forcing_value(A.forc[CLM_BC_TOP_HEAT], st, s, A.col0 + orig, t, A.seed);
+        const double fbw = forcing_value(A.forc[CLM_BC_BOTTOM_WATER], st, s, A.col0 + orig, t, A.seed);
+        const double fbh = forcing_value(A.forc[CLM_BC_BOTTOM_HEAT], st, s, A.col0 + orig, t, A.seed);
+        if (kAtmos) {
+          Ftw = ab.top_w;
+        } else if (A.bc_tw == CLM_BC_STATE) {
+          double pb, d;
+          psi_dpsi<false>(Tb, c.g, c.nu, ftw, c.theta_r, c.S_s, pb, d);
+          Ftw = -Kt * ((pb + G.half_top()) - psit) / G.half_top();  // diffusive_flux
+        } else {
+          Ftw = ftw;
+        }
+        if (A.bc_bw == CLM_BC_FREE_DRAINAGE) {
+          Fbw = -1.0 * K0;
+        } else if (A.bc_bw == CLM_BC_STATE) {
+          double pb, d;
+          psi_dpsi<false>(Tb, c.g, c.nu, fbw, c.theta_r, c.S_s, pb, d);
+          Fbw = -K0 * ((psi0 + G.half_bot()) - pb) / G.half_bot();
+        } else {
+          Fbw = fbw;
+        }
+        if (kAtmos) {
+          Fth = ab.top_h;
+        } else if (A.bc_th == CLM_BC_STATE) {
+          Fth = -kapt * (fth - Tt) / G.half_top();
+        } else if (A.bc_th == CLM_BC_FLUX_ADVECTIVE) {
+          const double* F = A.forc[CLM_BC_TOP_HEAT];
+          const double Tadv = F ? F[CLM_F_T_ADV * st + s] : E.T_0;
+          Fth = fth + Ftw * rho_e_liq(E, Tadv);
+        } else {
+          Fth = fth;
+        }
+        if (A.bc_bh == CLM_BC_FREE_DRAINAGE) {
+          Fbh = -1.0 * K0 * rho_e_liq(E, T0);
+        } else if (A.bc_bh == CLM_BC_STATE) {
+          Fbh = -kap0 * (T0 - fbh) / G.half_bot();
+        } else {
+          Fbh = fbh;
         }
       }
-      if (k == n - 1) {
-        Kt = K; Tt = T; kapt = kap;
-        if (A.bc_tw == CLM_BC_STATE) {
-          double d;
-          psi_dpsi<false>(Tb, c.g, nu_eff, Yv, c.theta_r, c.S_s, psit, d);
-        }
-      }
-    }
-    // boundary fluxes at t, frozen through the Newton solve
-    {
-      const double ftw = forcing_value(A.forc[CLM_BC_TOP_WATER], st, s, A.col0 + orig, t, A.seed);
-      const double fth = forcing_value(A.forc[CLM_BC_TOP_HEAT], st, s, A.col0 + orig, t, A.seed);
-      const double fbw = forcing_value(A.forc[CLM_BC_BOTTOM_WATER], st, s, A.col0 + orig, t, A.seed);
-      const double fbh = forcing_value(A.forc[CLM_BC_BOTTOM_HEAT], st, s, A.col0 + orig, t, A.seed);
-      if (kAtmos) {
-        Ftw = ab.top_w;
-      } else if (A.bc_tw == CLM_BC_STATE) {
-        double pb, d;
-        psi_dpsi<false>(Tb, c.g, c.nu, ftw, c.theta_r, c.S_s, pb, d);
-        Ftw = -Kt * ((pb + G.half_top()) - psit) / G.half_top();  // diffusive_flux
-      } else {
-        Ftw = ftw;
-      }
-      if (A.bc_bw == CLM_BC_FREE_DRAINAGE) {
-        Fbw = -1.0 * K0;
-      } else if (A.bc_bw == CLM_BC_STATE) {
-        double pb, d;
-        psi_dpsi<false>(Tb, c.g, c.nu, fbw, c.theta_r, c.S_s, pb, d);
-        Fbw = -K0 * ((psi0 + G.half_bot()) - pb) / G.half_bot();
-      } else {
-        Fbw = fbw;
-      }
-      if (kAtmos) {
-        Fth = ab.top_h;
-      } else if (A.bc_th == CLM_BC_STATE) {
-        Fth = -kapt * (fth - Tt) / G.half_top();
-      } else if (A.bc_th == CLM_BC_FLUX_ADVECTIVE) {
-        const double* F = A.forc[CLM_BC_TOP_HEAT];
-        const double Tadv = F ? F[CLM_F_T_ADV * st + s] : E.T_0;
-        Fth = fth + Ftw * rho_e_liq(E, Tadv);
-      } else {
-        Fth = fth;
-      }
-      if (A.bc_bh == CLM_BC_FREE_DRAINAGE) {
-        Fbh = -1.0 * K0 * rho_e_liq(E, T0);
-      } else if (A.bc_bh == CLM_BC_STATE) {
-        Fbh = -kap0 * (T0 - fbh) / G.half_bot();
-      } else {
-        Fbh = fbh;
-      }
-    }
-    UFw = kRoots ? Fw + dt * root_w : kAtmos ? Fw + dt * (0.0 + -ab.vice) : Fw;
-    UFe = kRoots ? Fe + dt * root_e : Fe;
-    xFw = UFw;
-    xFe = UFe;
-    X.R_ss = ro.R_ss;
-    X.R_ess = ro.R_ess;
+      UFw = kRoots ? Fw + dt * root_w : kAtmos ? Fw + dt * (0.0 + -ab.vice) : Fw;
+      UFe = kRoots ? Fe + dt * root_e : Fe;
+      xFw = UFw;
+      xFe = UFe;
+      X.R_ss = ro.R_ss;
+      X.R_ess = ro.R_ess;
 
-    // ---------------- stage 2: Newton ------------------------------------
-    prev_norm = 1e300;
-    // a guess that moved no layer off U is no guess: plain start, plain test
-    if (use_guess && !(pred2 > 0.0)) use_guess = false;
-    prev_state2 = 0.0;  // the state increments' norm of the last iteration (guess test)
-    it_start = 0;       // iterations spent before a restart from U
+      // ---------------- stage 2: Newton ------------------------------------
+      prev_norm = 1e300;
+      // a guess that moved no layer off U is no guess: plain start, plain test
+      if (use_guess && !(pred2 > 0.0)) use_guess = false;
+      prev_state2 = 0.0;  // the state increments' norm of the last iteration (guess test)
+      it_start = 0;       // iterations spent before a restart from U
     }  // !kResume
     bool deferred = false;
     for (int it = it_first; it <= A.max_iters; ++it) {
@@ -885,24 +885,24 @@ CLM_HD void eh_column(const StepArgs& A, const Tables& Tb, int s, int n, int ori
     // deferring hook is used with one step per call, so the step loop needs
     // no second exit)
     if (!deferred) {
-    const double inv_dt = 1.0 / dt;
-    const bool last = step == nsteps - 1;
-    const Col<double> OV = kResume ? B.ov : B.gv, OE = kResume ? B.oe : B.ge;
-    for (int k = 0; k < n; ++k) {
-      const double Uv = B.gv[k], Ue = B.ge[k];
-      const double v = Uv + dt * ((B.xv[k] - Uv) * inv_dt);
-      const double e = Ue + dt * ((B.xe[k] - Ue) * inv_dt);
-      if (last) {
-        OV.store_last(k, v);
-        OE.store_last(k, e);
-        finite = finite && isfinite(v) && isfinite(B.gti[k]) && isfinite(e);
-      } else {
-        OV[k] = v;
-        OE[k] = e;
+      const double inv_dt = 1.0 / dt;
+      const bool last = step == nsteps - 1;
+      const Col<double> OV = kResume ? B.ov : B.gv, OE = kResume ? B.oe : B.ge;
+      for (int k = 0; k < n; ++k) {
+        const double Uv = B.gv[k], Ue = B.ge[k];
+        const double v = Uv + dt * ((B.xv[k] - Uv) * inv_dt);
+        const double e = Ue + dt * ((B.xe[k] - Ue) * inv_dt);
+        if (last) {
+          OV.store_last(k, v);
+          OE.store_last(k, e);
+          finite = finite && isfinite(v) && isfinite(B.gti[k]) && isfinite(e);
+        } else {
+          OV[k] = v;
+          OE[k] = e;
+        }
       }
-    }
-    Fw = UFw + dt * ((xFw - UFw) * inv_dt);
-    Fe = UFe + dt * ((xFe - UFe) * inv_dt);
+      Fw = UFw + dt * ((xFw - UFw) * inv_dt);
+      Fe = UFe + dt * ((xFe - UFe) * inv_dt);
     }  // !deferred
   }
   finite = finite && isfinite(Fw) && isfinite(Fe);
