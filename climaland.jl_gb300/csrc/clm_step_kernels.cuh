@@ -100,13 +100,10 @@ struct QueueView {
   }
 };
 
-// The step kernel's deferring hook: claims an entry (one atomic per lane: a
-// warp-aggregated claim would put a warp collective inside the Newton loop,
-// whose reconvergence point keeps the lanes of a multi-step launch from
-// running ahead into their next step; measured 60 % slower fused launches)
-// and copies the column's arrays and context with evict-first stores (the
-// resuming launch prefetches them back; meanwhile they should not push the
-// step kernel's L2-resident scratch out).
+// The step kernel's deferring hook: claims an entry (one atomic per lane, no
+// warp collective inside the Newton loop) and copies the column's arrays and
+// context with evict-first stores (the resuming launch prefetches them back;
+// meanwhile they should not push the step kernel's L2-resident scratch out).
 template <typename JT>
 struct QueueDefer {
   static constexpr bool kEnabled = true;
@@ -173,8 +170,8 @@ struct QueueDefer {
 // has a smaller instruction footprint (with both Newton modes in one kernel,
 // instruction-fetch stalls measured 0.81 cycles per issued instruction in
 // tolerance mode with a guess, 0.23 in fixed mode; with the hook compiled
-// into every tolerance kernel, multi-step launches ran 1.5x slower: its
-// exit from the Newton loop changes how lanes that have converged run ahead).
+// into every tolerance kernel, never taken there, multi-step launches of the
+// tiles measured 1.5-1.65x slower).
 template <typename JT, class CM, int kSrc, bool kStr, int kTol = 0>
 __global__ void __launch_bounds__(128, 1)
     eh_step_kernel(StepArgs A, double* __restrict__ scratch, StepClock clk, int nsteps) {
