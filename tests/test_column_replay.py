@@ -335,6 +335,10 @@ def test_split_newton_resume_is_bitwise(name):
     got, got_steps = run(2)
     for a, b in zip(ref, got):
         assert (a is None and b is None) or np.array_equal(a, b), name
+    # a later split point saves a solve further along (norm history, restarts)
+    got3, _ = run(3)
+    for a, b in zip(ref, got3):
+        assert (a is None and b is None) or np.array_equal(a, b), name
     deferred = restarted = 0
     for (fa, ia), (fb, ib) in zip(ref_steps, got_steps):
         assert np.array_equal(fa, fb) and np.array_equal(ia, ib), name
