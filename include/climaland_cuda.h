@@ -514,8 +514,10 @@ int clm_sync(clm_handle* h);
  * nsteps and copied back, pipelined over chunks of columns so that each
  * chunk's copies overlap the kernels of its neighbours. Replaces
  * step!(landsim) (Simulations.jl:312-314) for a host-resident Y.soil; the
- * same bits as clm_set_state + clm_step + clm_get_state (which it becomes
- * when columns are not already in depth order or the learned guess is on). */
+ * same bits as clm_set_state + clm_step + clm_get_state (which it becomes,
+ * without the overlap, when columns are not already in depth order or a
+ * Newton guess is set: learned_guess != 0). With split Newton each chunk
+ * runs the two launches of every step. */
 int clm_step_host(clm_handle* h, double* vartheta_l, double* theta_i, double* rho_e_int,
                   double* intF_w, double* intF_e, double t, double dt, int32_t nsteps);
 
